@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Benchmark: WRF-ARW physics-off large step (solve_em RK3 + acoustic steps).
+
+Metric: cell-steps/s (one mass cell advanced one full large step: 3 RK
+stages, all acoustic sub-steps and all scalars); cells = (ide-1)(jde-1)(kde-1).
+
+Default workload (one GPU): 512 x 512 x 80 levels, dx = 1 km, dt = 6 s,
+sixteen +3 K bubbles, qv + 10 positive-definite passive scalars, FP32, the
+plain single-domain form (the drop-in).  Seeded synthetic initial state
+(Weisman-Klemp sounding); the device state (~6 GB) is far larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c2|c1|c4] [--mixed]
+
+N > 1 runs N independent replicas (one per rank, no collective on the data
+path) and reports the whole-job rate; the reference arm times the CPU
+restatement of the reference on the host cores (rank 0 only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+# Algorithmic bytes per mass cell of one launch of each kernel family:
+# unique 3-D FP32 arrays read + written by the routine(s) it implements
+# (2-D and 1-D arrays ignored), x 4 B.
+ALG_BYTES_PER_CELL = {
+    "step_prep": (8 + 9) * 4,          # u v w ph phb al alb qv -> ru rv rw ww php alt cqu cqv cqw
+    "rk_tend_u": (12 + 1) * 4,         # u ru rv rw ww ph alt p pb al php cqu (+v) -> ru_tend
+    "rk_tend_v": (12 + 1) * 4,
+    "rk_tend_w": (8 + 2) * 4,          # w ru rv ww p cqw u v -> rw_tend, cqw
+    "rk_tend_t": (5 + 1) * 4,          # t ru rv ww -> t_tend (+ zero extras)
+    "rk_tend_ph": (7 + 1) * 4,         # u v ww ph phb w -> ph_tend
+    "small_step_prep": (16 + 13) * 4,
+    "calc_p_rho_0": (7 + 3) * 4,
+    "calc_coef_w": (2 + 3) * 4,
+    "advance_uv": (14 + 2) * 4,        # u ru_tend v rv_tend p pb ph php alt al cqu cqv -> u v
+    "advance_mu_t": (9 + 3) * 4,       # ww ww1 u u_save v v_save t t_save t_tend -> ww t t_2save
+    "advance_w": (17 + 3) * 4,         # w rw_tend ww t_2ave t_2 t_1 ph ph_1 phb ph_tend c2a cqw alt a alpha gamma -> w ph t_2ave
+    "sumflux_calc_p_rho": (13 + 6) * 4,
+    "small_step_finish": (13 + 6) * 4,
+    "rk_update_scalar_pd": 2 * 4,
+    "advect_scalar_pd": (5 + 1) * 4,   # q q_old ru_m rv_m ww_m -> advect_tend
+    "advect_scalar": (4 + 1) * 4,
+    "rk_update_scalar": (3 + 2) * 4,
+    "calc_p_rho_phi": (6 + 2) * 4,
+    "set_w_surface": 0,
+    "cfl_check": 5 * 4,
+    "bc_fill": 0,
+}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=5)
+        sm = []
+        smax = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_case(workload):
+    from wrf_gb300 import cases
+    if workload == "c1":
+        return cases.config1()
+    if workload == "c2":
+        return cases.config2()
+    raise ValueError(workload)
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allreduce_max(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the CPU restatement of the reference's solve_em path on
+    the host cores (all threads), same workload / metric."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _harness import OracleDomain
+    case = make_case(args.workload)
+    cores = os.cpu_count() or 1
+    od = OracleDomain(case, "f32", nthreads=cores)
+    steps = max(1, min(args.steps, args.ref_steps))
+    for _ in range(min(args.warmup, 1)):
+        od.step(1)
+    t0 = time.perf_counter()
+    od.step(steps)
+    el = time.perf_counter() - t0
+    val = case.cells() * steps / el
+    sample = "%d of %d steps of the %s workload (after %d warm-up), %d OpenMP threads" % (
+        steps, args.steps, case.name, min(args.warmup, 1), cores)
+    line = {
+        "impl": "reference", "metric": "cell-steps/s", "value": val, "unit": "cell-steps/s",
+        "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Weisman-Klemp supercell state)",
+        "config": {"workload": case.name, "global_batch": 1, "seq_len": None, "parallelism": "cpu-openmp",
+                   "l2": "state larger than L2"},
+        "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(case, seconds_budget=25.0):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _harness import OracleDomain
+    cores = os.cpu_count() or 1
+    od = OracleDomain(case, "f32", nthreads=cores)
+    t0 = time.perf_counter()
+    od.step(1)
+    el1 = time.perf_counter() - t0
+    steps = 1
+    if el1 < seconds_budget / 3:
+        n = max(1, int((seconds_budget - el1) / max(el1, 1e-3)))
+        n = min(n, 5)
+        t0 = time.perf_counter()
+        od.step(n)
+        el1 = (time.perf_counter() - t0) / n
+        steps = n
+    return {"value": case.cells() / el1, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d large step(s) of the %s workload after one warm-up step, %d OpenMP threads (CPU restatement "
+                      "of the reference's FP32 solve_em path)" % (steps, case.name, cores)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--mixed", action="store_true", help="mixed-precision form (FP64 column steps)")
+    ap.add_argument("--ref-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    from wrf_gb300 import abi
+    from wrf_gb300 import gpu as G
+    case = make_case(args.workload)
+    flags = G.FLAG_MIXED if args.mixed else 0
+    dom = G.Domain(case, flags=flags)
+    cells = case.cells()
+
+    # warm-up (also builds the CUDA graph)
+    dom.step(args.warmup)
+    dom.sync()
+    rc, bits, vcfl, hcfl = dom.status(0)
+    if rc != 0:
+        raise SystemExit("health check failed after warm-up: rc=%d bits=%d" % (rc, bits))
+
+    # timed region: K steps, device events on the library's stream
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier(pg)
+    dom.sync()
+    ms = dom.time_steps(args.steps)
+    barrier(pg)
+    clocks = sampler.stop()
+    ms = allreduce_max(pg, ms)
+    value = cells * args.steps * world / (ms / 1e3)
+
+    # per-kernel phases (events between launches, outside the timed region)
+    phases = dom.profile_phases(1)
+    launches = dom.launches_per_step()
+    hbm, hbm_kind = peaks()
+    dom_name, (dom_ms, dom_n) = max(((k, v) for k, v in phases.items() if k in ALG_BYTES_PER_CELL and
+                                     ALG_BYTES_PER_CELL[k] > 0), key=lambda kv: kv[1][0])
+    alg = ALG_BYTES_PER_CELL[dom_name] * cells
+    achieved = alg / (dom_ms / max(dom_n, 1) / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "peak_kind": hbm_kind,
+                "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                "alg_bytes_per_launch": alg, "avg_launch_ms": dom_ms / max(dom_n, 1), "launches_per_step": dom_n,
+                "note": "frac of %s HBM copy bandwidth" % hbm_kind}
+    step_alg = None
+    try:
+        step_alg = {k: (v[0], v[1]) for k, v in phases.items()}
+    except Exception:
+        pass
+
+    # end to end through the C ABI with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        import numpy as np
+        try:
+            import torch
+            pin = lambda n: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+        except Exception:
+            pin = lambda n: np.empty(n, dtype=np.float32)
+        fids = [abi.FIELD_ID[n] for n in ("u_2", "v_2", "w_2", "t_2", "ph_2", "mu_2", "p", "al")]
+        nsp = case.desc.n_moist + case.desc.n_scalar
+        fids += [abi.species_id(s) for s in range(nsp)]
+        bufs = {}
+        for f in fids:
+            n = dom.field_size(0, f)
+            b = pin(n)
+            b[:] = dom.get(0, f)
+            bufs[f] = b
+        h2d = sum(b.nbytes for b in bufs.values())
+        d2h = h2d
+        dom.sync()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for f, b in bufs.items():
+                dom.set(0, f, b)
+            dom.step(1)
+            for f, b in bufs.items():
+                rcode = dom.L.wrfgpu_get_field_f32(dom.h, 0, f, b.ctypes.data, b.size)
+                if rcode != 0:
+                    raise SystemExit("get_field failed")
+        dom.sync()
+        el = allreduce_max(pg, time.perf_counter() - t0)
+        e2e = {"value": cells * args.steps * world / el, "unit": "cell-steps/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "what": "per step: H2D of the prognostic state (u,v,w,theta,ph,mu,p,al + %d species) from pinned "
+                       "host memory, one large step, D2H of the same fields, through the C ABI" % nsp}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(case)
+        except Exception as ex:  # the baseline is reported, never required
+            cpu = {"error": str(ex)}
+
+    if rank == 0:
+        line = {
+            "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if not args.mixed else "f32+f64-columns",
+            "data": "synthetic (seeded Weisman-Klemp supercell state, 16 bubbles, log-normal scalars)",
+            "config": {"workload": case.name, "form": "mixed" if args.mixed else "plain",
+                       "cells": cells, "species": case.desc.n_moist + case.desc.n_scalar,
+                       "global_batch": world, "seq_len": None,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (%.1f GB device state)" % (dom.device_bytes() / 1e9)},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches * args.steps,
+            "clocks": clocks,
+            "phases_ms_per_step": {k: round(v[0], 4) for k, v in (step_alg or {}).items()},
+        }
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/*
+ * wrfgpu.h — C ABI of the GB300 WRF-ARW dynamical-core large step.
+ *
+ * Two layers of entry points replace the reference's model-layer calls:
+ *
+ *  1. Per-subroutine entry points, one per Fortran subroutine on the
+ *     physics-off solve_em path, with the reference's argument order and
+ *     meaning.  Arrays are host pointers to element (ims,kms,jms) of a
+ *     Fortran (ims:ime, kms:kme, jms:jme) array (i fastest); 2-D arrays are
+ *     (ims:ime, jms:jme), 1-D column arrays (kms:kme).  Scalars and index
+ *     bounds are passed by pointer (Fortran pass-by-reference), logicals as
+ *     int32.  config_flags becomes the flat POD WrfDynConfig.  These copy
+ *     host<->device around one kernel launch (parity mode).
+ *
+ *  2. A coarse, device-resident domain API (create / set_field / step /
+ *     get_field / destroy) and an ensemble API that advances many uneven
+ *     domains per launch.  The large step runs entirely on the GPU; the
+ *     host only enqueues the captured CUDA graph.
+ *
+ * Every entry point returns 0 on success or a negative WRFGPU_E* code; the
+ * reference aborts through wrf_error_fatal (frame/module_wrf_error.F:316)
+ * instead, which a Fortran shim reproduces by calling it on non-zero.
+ * No entry point traps on the device.
+ */
+#ifndef WRFGPU_H
+#define WRFGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Memory halo width of every array (the serial build's bdyzone = 4,
+ * share/module_bc.F:33; frame/module_domain.F:331-517 sets ims = ids-4). */
+#define WRFGPU_HALO 4
+
+/* Error codes. */
+#define WRFGPU_OK 0
+#define WRFGPU_E_ARG -1         /* bad argument / unsupported option        */
+#define WRFGPU_E_CUDA -2        /* CUDA runtime error                        */
+#define WRFGPU_E_NONFINITE -3   /* non-finite value detected in the state    */
+#define WRFGPU_E_CFL -4         /* vertical CFL above the configured limit   */
+#define WRFGPU_E_TIMEOUT -5     /* bounded device wait gave up               */
+#define WRFGPU_E_NOMEM -6       /* device allocation failed                  */
+#define WRFGPU_E_SIZE -7        /* request larger than a fixed capacity      */
+
+/* grid_config_rec_type subset read by the path (Registry/Registry.EM_COMMON:
+ * 2840-2938, 2285).  Logicals are int32 0/1. */
+typedef struct WrfDynConfig {
+  int32_t periodic_x, periodic_y;
+  int32_t symmetric_xs, symmetric_xe, symmetric_ys, symmetric_ye;
+  int32_t open_xs, open_xe, open_ys, open_ye;
+  int32_t specified, nested, polar;
+  int32_t rk_ord;
+  int32_t h_mom_adv_order, v_mom_adv_order, h_sca_adv_order, v_sca_adv_order;
+  int32_t moist_adv_opt, scalar_adv_opt; /* 0 ORIGINAL, 1 POSITIVEDEF */
+  int32_t non_hydrostatic, top_lid, use_theta_m, hypsometric_opt, phi_adv_z;
+  int32_t w_damping, damp_opt, diff_opt, zadvect_implicit, map_proj;
+  int32_t time_step_sound;
+  int32_t pad0;
+} WrfDynConfig;
+
+/* Domain scalars that solve_em reads from grid% (double on the ABI; each
+ * build rounds them to its working precision). */
+typedef struct WrfGpuScalars {
+  double dt, dx, dy, rdx, rdy;
+  double cf1, cf2, cf3, cfn, cfn1;
+  double epssm, smdiv, emdiv;
+  double p_top;
+} WrfGpuScalars;
+
+/* Domain description: ids=jds=kds=1; ide, jde are the staggered ends
+ * (e_we, e_sn), kde = e_vert. */
+typedef struct WrfGpuDomainDesc {
+  int32_t ide, jde, kde;
+  int32_t n_moist;  /* moist species carried (qv only on this path: 1) */
+  int32_t n_scalar; /* passive scalars                                  */
+  int32_t pad0;
+  WrfDynConfig config;
+  WrfGpuScalars scalars;
+} WrfGpuDomainDesc;
+
+/* Field table of the domain state (ids for set_field / get_field). */
+enum WrfGpuFieldId {
+  /* 3-D (ims:ime, kms:kme, jms:jme) */
+  WRFGPU_U_1 = 0, WRFGPU_U_2, WRFGPU_V_1, WRFGPU_V_2, WRFGPU_W_1, WRFGPU_W_2,
+  WRFGPU_T_1, WRFGPU_T_2, WRFGPU_PH_1, WRFGPU_PH_2,
+  WRFGPU_PHB, WRFGPU_PB, WRFGPU_ALB, WRFGPU_P, WRFGPU_AL, WRFGPU_ALT, WRFGPU_PHP,
+  WRFGPU_RU, WRFGPU_RV, WRFGPU_RW, WRFGPU_WW, WRFGPU_WW1,
+  WRFGPU_CQU, WRFGPU_CQV, WRFGPU_CQW,
+  WRFGPU_RU_TEND, WRFGPU_RV_TEND, WRFGPU_RW_TEND, WRFGPU_T_TEND, WRFGPU_PH_TEND,
+  WRFGPU_U_SAVE, WRFGPU_V_SAVE, WRFGPU_W_SAVE, WRFGPU_T_SAVE, WRFGPU_PH_SAVE,
+  WRFGPU_C2A, WRFGPU_PM1, WRFGPU_A, WRFGPU_ALPHA, WRFGPU_GAMMA, WRFGPU_T_2SAVE,
+  WRFGPU_RU_M, WRFGPU_RV_M, WRFGPU_WW_M, WRFGPU_ADVECT_TEND, WRFGPU_H_DIABATIC,
+  WRFGPU_N3D,
+  /* 2-D (ims:ime, jms:jme) */
+  WRFGPU_F2D_BASE = 100,
+  WRFGPU_MU_1 = WRFGPU_F2D_BASE, WRFGPU_MU_2, WRFGPU_MUB, WRFGPU_MUT, WRFGPU_MUU, WRFGPU_MUV,
+  WRFGPU_MUTS, WRFGPU_MUUS, WRFGPU_MUVS, WRFGPU_MUDF, WRFGPU_MU_SAVE, WRFGPU_MUAVE, WRFGPU_MU_TEND,
+  WRFGPU_MSFUX, WRFGPU_MSFUY, WRFGPU_MSFVX, WRFGPU_MSFVX_INV, WRFGPU_MSFVY, WRFGPU_MSFTX, WRFGPU_MSFTY,
+  WRFGPU_HT, WRFGPU_F, WRFGPU_E, WRFGPU_SINA, WRFGPU_COSA,
+  WRFGPU_F2D_END,
+  /* 1-D (kms:kme) */
+  WRFGPU_F1D_BASE = 200,
+  WRFGPU_ZNW = WRFGPU_F1D_BASE, WRFGPU_ZNU, WRFGPU_DNW, WRFGPU_RDNW, WRFGPU_DN, WRFGPU_RDN,
+  WRFGPU_FNM, WRFGPU_FNP, WRFGPU_C1H, WRFGPU_C2H, WRFGPU_C1F, WRFGPU_C2F,
+  WRFGPU_C3H, WRFGPU_C4H, WRFGPU_C3F, WRFGPU_C4F,
+  WRFGPU_F1D_END,
+  /* species: WRFGPU_SPECIES_BASE + 2*s is species s (moist first, then
+   * passive scalars), + 1 its "old" (_1) copy */
+  WRFGPU_SPECIES_BASE = 300
+};
+#define WRFGPU_N2D (WRFGPU_F2D_END - WRFGPU_F2D_BASE)
+#define WRFGPU_N1D (WRFGPU_F1D_END - WRFGPU_F1D_BASE)
+
+/* ------------------------------------------------------------------------
+ * Coarse device-resident API.  A domain is an ensemble of one member; all
+ * calls take the ensemble handle and a member index where relevant.
+ * ---------------------------------------------------------------------- */
+typedef struct WrfGpuEnsemble WrfGpuEnsemble;
+
+/* creation flags */
+#define WRFGPU_FLAG_MIXED 1      /* FP64 column sums, omega recursion and tridiagonal solve */
+#define WRFGPU_FLAG_NO_GRAPH 2   /* enqueue kernels directly instead of replaying a CUDA graph */
+#define WRFGPU_FLAG_NO_CHECKS 4  /* skip the per-stage CFL / non-finite health check */
+
+/* Create n members (uneven sizes allowed) advanced together.  Replaces the
+ * reference's domain allocation for the dynamics state (frame/module_domain.F
+ * alloc_and_configure_domain) on the device side. */
+int wrfgpu_ensemble_create(const WrfGpuDomainDesc* descs, int n, int flags, WrfGpuEnsemble** out);
+int wrfgpu_ensemble_destroy(WrfGpuEnsemble* h);
+/* Element count of a field of one member (memory dims, halo included). */
+long long wrfgpu_field_size(WrfGpuEnsemble* h, int member, int id);
+/* Host <-> device copies of one field (Fortran memory layout). */
+int wrfgpu_set_field_f32(WrfGpuEnsemble* h, int member, int id, const float* src, long long n);
+int wrfgpu_get_field_f32(WrfGpuEnsemble* h, int member, int id, float* dst, long long n);
+int wrfgpu_set_field(WrfGpuEnsemble* h, int member, int id, const double* src, long long n);
+int wrfgpu_get_field(WrfGpuEnsemble* h, int member, int id, double* dst, long long n);
+/* Advance every member by nsteps large steps: the replacement of the RK3 loop
+ * of dyn_em/solve_em.F:578-3459 plus its end-of-step fills (:4439-4750).
+ * Asynchronous: returns once the work is enqueued. */
+int wrfgpu_step(WrfGpuEnsemble* h, int nsteps);
+int wrfgpu_sync(WrfGpuEnsemble* h);
+/* Advance nsteps and return the device time in milliseconds (CUDA events on
+ * the ensemble's stream). */
+int wrfgpu_time_steps(WrfGpuEnsemble* h, int nsteps, float* ms);
+/* Run one model-layer routine on the resident state (kernel-level parity). */
+int wrfgpu_run_routine(WrfGpuEnsemble* h, int routine, int rk_step, int iteration, int species);
+/* set_physical_bc3d / set_physical_bc2d of one field of every member. */
+int wrfgpu_fill_halo(WrfGpuEnsemble* h, int id, char var);
+/* Health: error bits since the last clear, max vertical / horizontal CFL
+ * (w_damp diagnostics, dyn_em/module_big_step_utilities_em.F:2503-2712).
+ * Returns WRFGPU_E_NONFINITE / WRFGPU_E_CFL when the bits are set. */
+int wrfgpu_status(WrfGpuEnsemble* h, int member, unsigned* err_bits, double* max_vert_cfl, double* max_horiz_cfl);
+int wrfgpu_clear_status(WrfGpuEnsemble* h);
+int wrfgpu_set_cfl_limit(WrfGpuEnsemble* h, double limit);
+int wrfgpu_num_sound_steps(WrfGpuEnsemble* h, int member);
+long long wrfgpu_device_bytes(WrfGpuEnsemble* h);
+int wrfgpu_kernel_launches_per_step(WrfGpuEnsemble* h);
+/* Per-phase device time of nsteps steps enqueued directly with CUDA events
+ * between kernel launches (the reference's BENCH_START/BENCH_END timers,
+ * inc/bench_solve_em_def.h).  Returns the number of phases filled. */
+int wrfgpu_profile_phases(WrfGpuEnsemble* h, int nsteps, double* ms_out, int* launches_out, int nphase);
+const char* wrfgpu_phase_name(int phase);
+const char* wrfgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WRFGPU_H */

@@ -1,0 +1,628 @@
+// ORACLE — test infrastructure only (see wrf_oracle.hpp).
+// Restatement of dyn_em/module_big_step_utilities_em.F routines on the
+// physics-off path and of rk_step_prep (dyn_em/module_em.F:37-186).
+#pragma once
+#include "wrf_oracle.hpp"
+
+namespace wrforacle {
+
+// module_big_step_utilities_em.F:3587-3636 (called with k range 1:1, i.e. 2-D).
+template <typename R>
+void calculate_full(R* rfield_p, R* rfieldb_p, R* rfieldp_p, const Dims& d) {
+  A2<R> rfield(rfield_p, d), rfieldb(rfieldb_p, d), rfieldp(rfieldp_p, d);
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts - 1; j <= jtf; ++j)
+    for (int i = d.its - 1; i <= itf; ++i) rfield(i, j) = rfieldb(i, j) + rfieldp(i, j);
+}
+
+// module_big_step_utilities_em.F:26-181.  The three-branch structure reduces
+// to one loop with a boundary-point special case; every branch evaluates the
+// same expression with im = i-1 (interior) or the periodic/one-sided index.
+template <typename R>
+void calc_mu_uv(const WrfDynConfig& cf, R* mu_p, R* mub_p, R* muu_p, R* muv_p, const Dims& d) {
+  A2<R> MU(mu_p, d), MUB(mub_p, d), MUU(muu_p, d), MUV(muv_p, d);
+  int itf = d.ite, jtf = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int i = d.its; i <= itf; ++i) {
+      if (i == d.ids && d.its == d.ids) {
+        int im = cf.periodic_x ? i - 1 : i;
+        MUU(i, j) = R(0.5) * (MU(i, j) + MU(im, j) + MUB(i, j) + MUB(im, j));
+      } else if (i == d.ide && d.ite == d.ide) {
+        int im = cf.periodic_x ? i : i - 1;
+        MUU(i, j) = R(0.5) * (MU(i - 1, j) + MU(im, j) + MUB(i - 1, j) + MUB(im, j));
+      } else {
+        MUU(i, j) = R(0.5) * (MU(i, j) + MU(i - 1, j) + MUB(i, j) + MUB(i - 1, j));
+      }
+    }
+  itf = std::min(d.ite, d.ide - 1); jtf = d.jte;
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int i = d.its; i <= itf; ++i) {
+      if (j == d.jds && d.jts == d.jds) {
+        int jm = cf.periodic_y ? j - 1 : j;
+        MUV(i, j) = R(0.5) * (MU(i, j) + MU(i, jm) + MUB(i, j) + MUB(i, jm));
+      } else if (j == d.jde && d.jte == d.jde) {
+        int jm = cf.periodic_y ? j : j - 1;
+        MUV(i, j) = R(0.5) * (MU(i, j - 1) + MU(i, jm) + MUB(i, j - 1) + MUB(i, jm));
+      } else {
+        MUV(i, j) = R(0.5) * (MU(i, j) + MU(i, j - 1) + MUB(i, j) + MUB(i, j - 1));
+      }
+    }
+}
+
+// module_big_step_utilities_em.F:184-326.
+template <typename R>
+void calc_mu_uv_1(const WrfDynConfig& cf, R* mu_p, R* muu_p, R* muv_p, const Dims& d) {
+  A2<R> MU(mu_p, d), MUU(muu_p, d), MUV(muv_p, d);
+  int itf = d.ite, jtf = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int i = d.its; i <= itf; ++i) {
+      if (i == d.ids && d.its == d.ids) {
+        int im = cf.periodic_x ? i - 1 : i;
+        MUU(i, j) = R(0.5) * (MU(i, j) + MU(im, j));
+      } else if (i == d.ide && d.ite == d.ide) {
+        int im = cf.periodic_x ? i : i - 1;
+        MUU(i, j) = R(0.5) * (MU(i - 1, j) + MU(im, j));
+      } else {
+        MUU(i, j) = R(0.5) * (MU(i, j) + MU(i - 1, j));
+      }
+    }
+  itf = std::min(d.ite, d.ide - 1); jtf = d.jte;
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int i = d.its; i <= itf; ++i) {
+      if (j == d.jds && d.jts == d.jds) {
+        int jm = cf.periodic_y ? j - 1 : j;
+        MUV(i, j) = R(0.5) * (MU(i, j) + MU(i, jm));
+      } else if (j == d.jde && d.jte == d.jde) {
+        int jm = cf.periodic_y ? j : j - 1;
+        MUV(i, j) = R(0.5) * (MU(i, j - 1) + MU(i, jm));
+      } else {
+        MUV(i, j) = R(0.5) * (MU(i, j) + MU(i, j - 1));
+      }
+    }
+}
+
+// module_big_step_utilities_em.F:329-391.
+template <typename R>
+void couple_momentum(R* muu_p, R* ru_p, R* u_p, R* msfu_p, R* muv_p, R* rv_p, R* v_p, R* msfv_p, R* msfv_inv_p,
+                     R* mut_p, R* rw_p, R* w_p, R* msft_p, R* c1h_p, R* c2h_p, R* c1f_p, R* c2f_p, const Dims& d) {
+  A2<R> muu(muu_p, d), muv(muv_p, d), mut(mut_p, d), msfu(msfu_p, d), msfv_inv(msfv_inv_p, d), msft(msft_p, d);
+  A3<R> ru(ru_p, d), u(u_p, d), rv(rv_p, d), v(v_p, d), rw(rw_p, d), w(w_p, d);
+  A1<R> c1h(c1h_p, d), c2h(c2h_p, d), c1f(c1f_p, d), c2f(c2f_p, d);
+  (void)msfv_p;
+  int ktf = std::min(d.kte, d.kde - 1);
+  int itf = d.ite, jtf = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= itf; ++i) ru(i, k, j) = u(i, k, j) * (c1h(k) * muu(i, j) + c2h(k)) / msfu(i, j);
+  itf = std::min(d.ite, d.ide - 1); jtf = d.jte;
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= itf; ++i) rv(i, k, j) = v(i, k, j) * (c1h(k) * muv(i, j) + c2h(k)) * msfv_inv(i, j);
+  itf = std::min(d.ite, d.ide - 1); jtf = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int k = d.kts; k <= d.kte; ++k)
+      for (int i = d.its; i <= itf; ++i) rw(i, k, j) = w(i, k, j) * (c1f(k) * mut(i, j) + c2f(k)) / msft(i, j);
+}
+
+// module_big_step_utilities_em.F:640-784.
+template <typename R>
+void calc_ww_cp(R* u_p, R* v_p, R* mup_p, R* mub_p, R* c1h_p, R* c2h_p, R* ww_p, R rdx, R rdy, R* msftx_p,
+                R* msfty_p, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvx_inv_p, R* msfvy_p, R* dnw_p,
+                const Dims& d) {
+  A3<R> u(u_p, d), v(v_p, d), ww(ww_p, d);
+  A2<R> MUP(mup_p, d), MUB(mub_p, d), msftx(msftx_p, d), msfuy(msfuy_p, d), msfvx_inv(msfvx_inv_p, d);
+  A1<R> c1h(c1h_p, d), c2h(c2h_p, d), dnw(dnw_p, d);
+  (void)msfty_p; (void)msfux_p; (void)msfvx_p; (void)msfvy_p;
+  int nx = d.ime - d.ims + 1, ny = d.jme - d.jms + 1;
+  std::vector<R> muu_s((size_t)nx * ny), muv_s((size_t)nx * ny);
+  A2<R> MUU(muu_s.data(), d), MUV(muv_s.data(), d);
+  int jtf = std::min(d.jte, d.jde - 1), ktf = std::min(d.kte, d.kde - 1), itf = std::min(d.ite, d.ide - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int i = d.its; i <= std::min(d.ite + 1, d.ide); ++i)
+      MUU(i, j) = R(0.5) * (MUP(i, j) + MUB(i, j) + MUP(i - 1, j) + MUB(i - 1, j));
+  for (int j = d.jts; j <= std::min(d.jte + 1, d.jde); ++j)
+    for (int i = d.its; i <= itf; ++i)
+      MUV(i, j) = R(0.5) * (MUP(i, j) + MUB(i, j) + MUP(i, j - 1) + MUB(i, j - 1));
+  std::vector<R> dmdt((size_t)nx), divv((size_t)nx * (d.kme - d.kms + 1));
+  auto DIVV = [&](int i, int k) -> R& { return divv[(size_t)(i - d.ims) + (size_t)(k - d.kms) * nx]; };
+  for (int j = d.jts; j <= jtf; ++j) {
+    for (int i = d.its; i <= d.ite; ++i) {
+      if (i <= itf) dmdt[i - d.ims] = R(0.);
+      ww(i, 1, j) = R(0.);
+      ww(i, d.kte, j) = R(0.);
+    }
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= itf; ++i) {
+        DIVV(i, k) = msftx(i, j) * dnw(k) *
+                     (rdx * ((c1h(k) * MUU(i + 1, j) + c2h(k)) * u(i + 1, k, j) / msfuy(i + 1, j) -
+                             (c1h(k) * MUU(i, j) + c2h(k)) * u(i, k, j) / msfuy(i, j)) +
+                      rdy * ((c1h(k) * MUV(i, j + 1) + c2h(k)) * v(i, k, j + 1) * msfvx_inv(i, j + 1) -
+                             (c1h(k) * MUV(i, j) + c2h(k)) * v(i, k, j) * msfvx_inv(i, j)));
+        dmdt[i - d.ims] = dmdt[i - d.ims] + DIVV(i, k);
+      }
+    for (int k = 2; k <= ktf; ++k)
+      for (int i = d.its; i <= itf; ++i)
+        ww(i, k, j) = ww(i, k - 1, j) - dnw(k - 1) * c1h(k - 1) * dmdt[i - d.ims] - DIVV(i, k - 1);
+  }
+}
+
+// module_big_step_utilities_em.F:787-907 (qv is the only moist species on
+// the physics-off path; n_moist >= PARAM_FIRST_SCALAR).
+template <typename R>
+void calc_cq(R* qv_p, R* cqu_p, R* cqv_p, R* cqw_p, int n_moist_species, const Dims& d) {
+  A3<R> qv(qv_p, d), cqu(cqu_p, d), cqv(cqv_p, d), cqw(cqw_p, d);
+  int ktf = std::min(d.kte, d.kde - 1);
+  if (n_moist_species >= 1) {
+    int itf = d.ite, jtf = std::min(d.jte, d.jde - 1);
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) {
+          R qtot = R(0.) + qv(i, k, j) + qv(i - 1, k, j);
+          cqu(i, k, j) = R(1.) / (R(1.) + R(0.5) * qtot);
+        }
+    itf = std::min(d.ite, d.ide - 1); jtf = d.jte;
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) {
+          R qtot = R(0.) + qv(i, k, j) + qv(i, k, j - 1);
+          cqv(i, k, j) = R(1.) / (R(1.) + R(0.5) * qtot);
+        }
+    itf = std::min(d.ite, d.ide - 1); jtf = std::min(d.jte, d.jde - 1);
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts + 1; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) {
+          R qtot = R(0.) + qv(i, k, j) + qv(i, k - 1, j);
+          cqw(i, k, j) = R(0.5) * qtot;
+        }
+  } else {
+    int itf = d.ite, jtf = std::min(d.jte, d.jde - 1);
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) cqu(i, k, j) = R(1.);
+    itf = std::min(d.ite, d.ide - 1); jtf = d.jte;
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) cqv(i, k, j) = R(1.);
+    itf = std::min(d.ite, d.ide - 1); jtf = std::min(d.jte, d.jde - 1);
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts + 1; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) cqw(i, k, j) = R(0.);
+  }
+}
+
+// module_big_step_utilities_em.F:910-950.
+template <typename R>
+void calc_alt(R* alt_p, R* al_p, R* alb_p, const Dims& d) {
+  A3<R> alt(alt_p, d), al(al_p, d), alb(alb_p, d);
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1), ktf = std::min(d.kte, d.kde - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= itf; ++i) alt(i, k, j) = al(i, k, j) + alb(i, k, j);
+}
+
+// module_big_step_utilities_em.F:1227-1262.
+template <typename R>
+void calc_php(R* php_p, R* ph_p, R* phb_p, const Dims& d) {
+  A3<R> php(php_p, d), ph(ph_p, d), phb(phb_p, d);
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1), ktf = std::min(d.kte, d.kde - 1);
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= itf; ++i)
+        php(i, k, j) = R(0.5) * (phb(i, k, j) + phb(i, k + 1, j) + ph(i, k, j) + ph(i, k + 1, j));
+}
+
+// module_em.F:37-186 rk_step_prep (calls in the reference's order).
+template <typename R>
+void rk_step_prep(const WrfDynConfig& cf, int rk_step, R* u, R* v, R* w, R* t, R* ph, R* mu, R* c1h, R* c2h,
+                  R* c1f, R* c2f, R* qv, int n_moist_species, R* ru, R* rv, R* rw, R* ww, R* php, R* alt,
+                  R* muu, R* muv, R* mub, R* mut, R* phb, R* pb, R* p, R* al, R* alb, R* cqu, R* cqv, R* cqw,
+                  R* msfux, R* msfuy, R* msfvx, R* msfvx_inv, R* msfvy, R* msftx, R* msfty, R* fnm, R* fnp,
+                  R* dnw, R rdx, R rdy, const Dims& d) {
+  (void)rk_step; (void)t; (void)pb; (void)p; (void)fnm; (void)fnp;
+  Dims d2 = d;  // calculate_full is called with k dims 1:2 / 1:1 / 1:1
+  calculate_full(mut, mub, mu, d2);
+  calc_mu_uv(cf, mu, mub, muu, muv, d);
+  couple_momentum(muu, ru, u, msfuy, muv, rv, v, msfvx, msfvx_inv, mut, rw, w, msfty, c1h, c2h, c1f, c2f, d);
+  calc_ww_cp(u, v, mu, mub, c1h, c2h, ww, rdx, rdy, msftx, msfty, msfux, msfuy, msfvx, msfvx_inv, msfvy, dnw, d);
+  calc_cq(qv, cqu, cqv, cqw, n_moist_species, d);
+  calc_alt(alt, al, alb, d);
+  calc_php(php, ph, phb, d);
+}
+
+// module_big_step_utilities_em.F:4573-4643 zero_tend / zero_tend2d.
+template <typename R>
+void zero_tend(R* t_p, const Dims& d) {
+  A3<R> t(t_p, d);
+  for (int j = d.jts; j <= d.jte; ++j)
+    for (int k = d.kts; k <= d.kte; ++k)
+      for (int i = d.its; i <= d.ite; ++i) t(i, k, j) = R(0.);
+}
+template <typename R>
+void zero_tend2d(R* t_p, const Dims& d) {
+  A2<R> t(t_p, d);
+  for (int j = d.jts; j <= d.jte; ++j)
+    for (int i = d.its; i <= d.ite; ++i) t(i, j) = R(0.);
+}
+
+// module_big_step_utilities_em.F:1365-2178 rhs_ph, phi_adv_z 1/2 vertical
+// term, "gw" term and the advective_order <= 6 horizontal branch
+// (:1768-1930 y, :1930-2075 x) for periodic / symmetric boundaries.
+template <typename R>
+void rhs_ph(R* ph_tend_p, R* u_p, R* v_p, R* ww_p, R* ph_p, R* ph_old_p, R* phb_p, R* w_p, R* mut_p,
+            R* muuf_p, R* muvf_p, R* c1f_p, R* c2f_p, R* fnm_p, R* fnp_p, R* rdnw_p, R cfn, R cfn1, R rdx,
+            R rdy, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p,
+            int non_hydrostatic, const WrfDynConfig& cf, const Dims& d) {
+  (void)ph_old_p; (void)msfuy_p; (void)msfvx_p; (void)msfvx_inv_p; (void)msftx_p;
+  A3<R> ph_tend(ph_tend_p, d), u(u_p, d), v(v_p, d), ww(ww_p, d), ph(ph_p, d), phb(phb_p, d), w(w_p, d);
+  A2<R> mut(mut_p, d), muuf(muuf_p, d), muvf(muvf_p, d), msfux(msfux_p, d), msfvy(msfvy_p, d), msfty(msfty_p, d);
+  A1<R> c1f(c1f_p, d), c2f(c2f_p, d), fnm(fnm_p, d), fnp(fnp_p, d), rdnw(rdnw_p, d);
+  const R g = K<R>::g;
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1);
+  const int kte = d.kte, kde = d.kde;
+  int nx = d.ime - d.ims + 1;
+  std::vector<R> wdwn_s((size_t)nx * (d.kme - d.kms + 1));
+  auto wdwn = [&](int i, int k) -> R& { return wdwn_s[(size_t)(i - d.ims) + (size_t)(k - d.kms) * nx]; };
+  for (int j = d.jts; j <= jtf; ++j) {
+    if (cf.phi_adv_z == 2) {
+      for (int k = 2; k <= kte; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          wdwn(i, k) = rdnw(k - 1) * (ph(i, k, j) - ph(i, k - 1, j) + phb(i, k, j) - phb(i, k - 1, j));
+      for (int k = 2; k <= kte - 1; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          ph_tend(i, k, j) = ph_tend(i, k, j) - ww(i, k, j) * (fnm(k) * wdwn(i, k + 1) + fnp(k) * wdwn(i, k));
+    } else {
+      for (int k = 2; k <= kte; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          wdwn(i, k) = R(.5) * (ww(i, k, j) + ww(i, k - 1, j)) * rdnw(k - 1) *
+                       (ph(i, k, j) - ph(i, k - 1, j) + phb(i, k, j) - phb(i, k - 1, j));
+      for (int k = 2; k <= kte - 1; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          ph_tend(i, k, j) = ph_tend(i, k, j) - (fnm(k) * wdwn(i, k + 1) + fnp(k) * wdwn(i, k));
+    }
+  }
+  if (non_hydrostatic) {
+    for (int j = d.jts; j <= jtf; ++j) {
+      for (int i = d.its; i <= itf; ++i) ph_tend(i, kde, j) = R(0.);
+      for (int k = 2; k <= kte; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          ph_tend(i, k, j) = ph_tend(i, k, j) + (c1f(k) * mut(i, j) + c2f(k)) * g * w(i, k, j) / msfty(i, j);
+    }
+  }
+  // y (v) advection, 6th-order centred stencil on ph+phb.
+  itf = std::min(d.ite, d.ide - 1); jtf = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= jtf; ++j) {
+    for (int k = 2; k <= kte - 1; ++k)
+      for (int i = d.its; i <= itf; ++i) {
+        ph_tend(i, k, j) = ph_tend(i, k, j) -
+            (R(0.25) * rdy / msfty(i, j)) *
+                (((c1f(k) * muvf(i, j + 1) + c2f(k)) * (v(i, k, j + 1) + v(i, k - 1, j + 1)) * msfvy(i, j + 1) +
+                  (c1f(k) * muvf(i, j) + c2f(k)) * (v(i, k, j) + v(i, k - 1, j)) * msfvy(i, j)) *
+                 (R(1.) / R(60.)) *
+                 (R(45.) * (ph(i, k, j + 1) - ph(i, k, j - 1)) - R(9.) * (ph(i, k, j + 2) - ph(i, k, j - 2)) +
+                  (ph(i, k, j + 3) - ph(i, k, j - 3)) + R(45.) * (phb(i, k, j + 1) - phb(i, k, j - 1)) -
+                  R(9.) * (phb(i, k, j + 2) - phb(i, k, j - 2)) + (phb(i, k, j + 3) - phb(i, k, j - 3))));
+      }
+    int k = kte;
+    for (int i = d.its; i <= itf; ++i) {
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          (R(0.5) * rdy / msfty(i, j)) *
+              (((c1f(k) * muvf(i, j + 1) + c2f(k)) * (cfn * v(i, k - 1, j + 1) + cfn1 * v(i, k - 2, j + 1)) * msfvy(i, j + 1) +
+                (c1f(k) * muvf(i, j) + c2f(k)) * (cfn * v(i, k - 1, j) + cfn1 * v(i, k - 2, j)) * msfvy(i, j)) *
+               (R(1.) / R(60.)) *
+               (R(45.) * (ph(i, k, j + 1) - ph(i, k, j - 1)) - R(9.) * (ph(i, k, j + 2) - ph(i, k, j - 2)) +
+                (ph(i, k, j + 3) - ph(i, k, j - 3)) + R(45.) * (phb(i, k, j + 1) - phb(i, k, j - 1)) -
+                R(9.) * (phb(i, k, j + 2) - phb(i, k, j - 2)) + (phb(i, k, j + 3) - phb(i, k, j - 3))));
+    }
+  }
+  // x (u) advection.
+  for (int j = d.jts; j <= jtf; ++j) {
+    for (int k = 2; k <= kte - 1; ++k)
+      for (int i = d.its; i <= itf; ++i) {
+        ph_tend(i, k, j) = ph_tend(i, k, j) -
+            (R(0.25) * rdx / msfty(i, j)) *
+                (((c1f(k) * muuf(i + 1, j) + c2f(k)) * (u(i + 1, k, j) + u(i + 1, k - 1, j)) * msfux(i + 1, j) +
+                  (c1f(k) * muuf(i, j) + c2f(k)) * (u(i, k, j) + u(i, k - 1, j)) * msfux(i, j)) *
+                 (R(1.) / R(60.)) *
+                 (R(45.) * (ph(i + 1, k, j) - ph(i - 1, k, j)) - R(9.) * (ph(i + 2, k, j) - ph(i - 2, k, j)) +
+                  (ph(i + 3, k, j) - ph(i - 3, k, j)) + R(45.) * (phb(i + 1, k, j) - phb(i - 1, k, j)) -
+                  R(9.) * (phb(i + 2, k, j) - phb(i - 2, k, j)) + (phb(i + 3, k, j) - phb(i - 3, k, j))));
+      }
+    int k = kte;
+    for (int i = d.its; i <= itf; ++i) {
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          (R(0.5) * rdx / msfty(i, j)) *
+              (((c1f(k) * muuf(i + 1, j) + c2f(k)) * (cfn * u(i + 1, k - 1, j) + cfn1 * u(i + 1, k - 2, j)) * msfux(i + 1, j) +
+                (c1f(k) * muuf(i, j) + c2f(k)) * (cfn * u(i, k - 1, j) + cfn1 * u(i, k - 2, j)) * msfux(i, j)) *
+               (R(1.) / R(60.)) *
+               (R(45.) * (ph(i + 1, k, j) - ph(i - 1, k, j)) - R(9.) * (ph(i + 2, k, j) - ph(i - 2, k, j)) +
+                (ph(i + 3, k, j) - ph(i - 3, k, j)) + R(45.) * (phb(i + 1, k, j) - phb(i - 1, k, j)) -
+                R(9.) * (phb(i + 2, k, j) - phb(i - 2, k, j)) + (phb(i + 3, k, j) - phb(i - 3, k, j))));
+    }
+  }
+}
+
+// module_big_step_utilities_em.F:2183-2418 (non-hydrostatic branch).
+template <typename R>
+void horizontal_pressure_gradient(R* ru_tend_p, R* rv_tend_p, R* ph_p, R* alt_p, R* p_p, R* pb_p, R* al_p,
+                                  R* php_p, R* cqu_p, R* cqv_p, R* muu_p, R* muv_p, R* mu_p, R* c1h_p, R* c2h_p,
+                                  R* fnm_p, R* fnp_p, R* rdnw_p, R cf1, R cf2, R cf3, R cfn, R cfn1, R rdx, R rdy,
+                                  R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvy_p, R* msftx_p, R* msfty_p,
+                                  const WrfDynConfig& cf, int non_hydrostatic, int top_lid, const Dims& d) {
+  (void)msftx_p; (void)msfty_p;
+  A3<R> ru_tend(ru_tend_p, d), rv_tend(rv_tend_p, d), ph(ph_p, d), alt(alt_p, d), p(p_p, d), pb(pb_p, d),
+      al(al_p, d), php(php_p, d), cqu(cqu_p, d), cqv(cqv_p, d);
+  A2<R> muu(muu_p, d), muv(muv_p, d), mu(mu_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx(msfvx_p, d),
+      msfvy(msfvy_p, d);
+  A1<R> c1h(c1h_p, d), c2h(c2h_p, d), fnm(fnm_p, d), fnp(fnp_p, d), rdnw(rdnw_p, d);
+  A1<R> c1 = c1h;
+  if (!non_hydrostatic) throw std::runtime_error("hydrostatic not supported");
+  int nx = d.ime - d.ims + 1;
+  std::vector<R> dpn_s((size_t)nx * (d.kme - d.kms + 1));
+  auto dpn = [&](int i, int k) -> R& { return dpn_s[(size_t)(i - d.ims) + (size_t)(k - d.kms) * nx]; };
+  const int kde = d.kde;
+  int itf = std::min(d.ite, d.ide - 1), jtf = d.jte, ktf = std::min(d.kte, d.kde - 1);
+  int i_start = d.its, j_start = d.jts;
+  (void)cf;
+  for (int j = j_start; j <= jtf; ++j) {
+    int k = 1;
+    for (int i = i_start; i <= itf; ++i) {
+      dpn(i, k) = R(.5) * (cf1 * (p(i, k, j - 1) + p(i, k, j)) + cf2 * (p(i, k + 1, j - 1) + p(i, k + 1, j)) +
+                           cf3 * (p(i, k + 2, j - 1) + p(i, k + 2, j)));
+      dpn(i, kde) = R(0.);
+    }
+    if (top_lid)
+      for (int i = i_start; i <= itf; ++i)
+        dpn(i, kde) = R(.5) * (cfn * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) + cfn1 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)));
+    for (k = 2; k <= ktf; ++k)
+      for (int i = i_start; i <= itf; ++i)
+        dpn(i, k) = R(.5) * (fnm(k) * (p(i, k, j - 1) + p(i, k, j)) + fnp(k) * (p(i, k - 1, j - 1) + p(i, k - 1, j)));
+    for (k = 1; k <= ktf; ++k)
+      for (int i = i_start; i <= itf; ++i) {
+        R dpy = (msfvy(i, j) / msfvx(i, j)) * R(.5) * rdy * (c1h(k) * muv(i, j) + c2h(k)) *
+                ((ph(i, k + 1, j) - ph(i, k + 1, j - 1) + ph(i, k, j) - ph(i, k, j - 1)) +
+                 (alt(i, k, j) + alt(i, k, j - 1)) * (p(i, k, j) - p(i, k, j - 1)) +
+                 (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
+        dpy = dpy + (msfvy(i, j) / msfvx(i, j)) * rdy * (php(i, k, j) - php(i, k, j - 1)) *
+                        (rdnw(k) * (dpn(i, k + 1) - dpn(i, k)) - R(.5) * ((c1(k) * mu(i, j - 1)) + (c1(k) * mu(i, j))));
+        rv_tend(i, k, j) = rv_tend(i, k, j) - cqv(i, k, j) * dpy;
+      }
+  }
+  itf = d.ite; jtf = std::min(d.jte, d.jde - 1);
+  for (int j = j_start; j <= jtf; ++j) {
+    int k = 1;
+    for (int i = i_start; i <= itf; ++i) {
+      dpn(i, k) = R(.5) * (cf1 * (p(i - 1, k, j) + p(i, k, j)) + cf2 * (p(i - 1, k + 1, j) + p(i, k + 1, j)) +
+                           cf3 * (p(i - 1, k + 2, j) + p(i, k + 2, j)));
+      dpn(i, kde) = R(0.);
+    }
+    if (top_lid)
+      for (int i = i_start; i <= itf; ++i)
+        dpn(i, kde) = R(.5) * (cfn * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) + cfn1 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)));
+    for (k = 2; k <= ktf; ++k)
+      for (int i = i_start; i <= itf; ++i)
+        dpn(i, k) = R(.5) * (fnm(k) * (p(i - 1, k, j) + p(i, k, j)) + fnp(k) * (p(i - 1, k - 1, j) + p(i, k - 1, j)));
+    for (k = 1; k <= ktf; ++k)
+      for (int i = i_start; i <= itf; ++i) {
+        R dpx = (msfux(i, j) / msfuy(i, j)) * R(.5) * rdx * (c1h(k) * muu(i, j) + c2h(k)) *
+                ((ph(i, k + 1, j) - ph(i - 1, k + 1, j) + ph(i, k, j) - ph(i - 1, k, j)) +
+                 (alt(i, k, j) + alt(i - 1, k, j)) * (p(i, k, j) - p(i - 1, k, j)) +
+                 (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
+        dpx = dpx + (msfux(i, j) / msfuy(i, j)) * rdx * (php(i, k, j) - php(i - 1, k, j)) *
+                        (rdnw(k) * (dpn(i, k + 1) - dpn(i, k)) - R(.5) * ((c1(k) * mu(i - 1, j)) + (c1(k) * mu(i, j))));
+        ru_tend(i, k, j) = ru_tend(i, k, j) - cqu(i, k, j) * dpx;
+      }
+  }
+}
+
+// module_big_step_utilities_em.F:2419-2502.  Overwrites cqw with 1/(1+cqw).
+template <typename R>
+void pg_buoy_w(R* rw_tend_p, R* p_p, R* cqw_p, R* muf_p, R* mubf_p, R* c1f_p, R* c2f_p, R* rdnw_p, R* rdn_p,
+               R g, R* msftx_p, R* msfty_p, const Dims& d) {
+  (void)msftx_p;
+  A3<R> rw_tend(rw_tend_p, d), p(p_p, d), cqw(cqw_p, d);
+  A2<R> muf(muf_p, d), mubf(mubf_p, d), msfty(msfty_p, d);
+  A1<R> c1f(c1f_p, d), c2f(c2f_p, d), rdnw(rdnw_p, d), rdn(rdn_p, d);
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1);
+  const int kde = d.kde;
+  for (int j = d.jts; j <= jtf; ++j) {
+    int k = kde;
+    for (int i = d.its; i <= itf; ++i) {
+      R cq1 = R(1.) / (R(1.) + cqw(i, k - 1, j));
+      R cq2 = cqw(i, k - 1, j) * cq1;
+      rw_tend(i, k, j) = rw_tend(i, k, j) + (R(1.) / msfty(i, j)) * g *
+                                                (cq1 * R(2.) * rdnw(k - 1) * (-p(i, k - 1, j)) - (c1f(k) * muf(i, j)) -
+                                                 cq2 * (c1f(k) * mubf(i, j) + c2f(k)));
+    }
+    for (k = 2; k <= kde - 1; ++k)
+      for (int i = d.its; i <= itf; ++i) {
+        R cq1 = R(1.) / (R(1.) + cqw(i, k, j));
+        R cq2 = cqw(i, k, j) * cq1;
+        cqw(i, k, j) = cq1;
+        rw_tend(i, k, j) = rw_tend(i, k, j) + (R(1.) / msfty(i, j)) * g *
+                                                  (cq1 * rdn(k) * (p(i, k, j) - p(i, k - 1, j)) - (c1f(k) * muf(i, j)) -
+                                                   cq2 * (c1f(k) * mubf(i, j) + c2f(k)));
+      }
+  }
+}
+
+// module_big_step_utilities_em.F:2503-2712 w_damp: CFL diagnostics only
+// (w_damping=0 leaves rw_tend untouched on this path).
+template <typename R>
+void w_damp_cfl(R* u_p, R* v_p, R* ww_p, R* mut_p, R* c1f_p, R* c2f_p, R* rdnw_p, R rdx, R rdy, R* msfux_p,
+                R* msfvy_p, R dt, R* max_vert_cfl, R* max_horiz_cfl, const Dims& d) {
+  A3<R> u(u_p, d), v(v_p, d), ww(ww_p, d);
+  A2<R> mut(mut_p, d), msfux(msfux_p, d), msfvy(msfvy_p, d);
+  A1<R> c1f(c1f_p, d), c2f(c2f_p, d), rdnw(rdnw_p, d);
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1);
+  R mv = 0, mh = 0;
+  for (int j = d.jts; j <= jtf; ++j)
+    for (int k = 2; k <= d.kde - 1; ++k)
+      for (int i = d.its; i <= itf; ++i) {
+        R vert_cfl = std::fabs(ww(i, k, j) / (c1f(k) * mut(i, j) + c2f(k)) * rdnw(k) * dt);
+        if (vert_cfl > mv) mv = vert_cfl;
+        R horiz_cfl = fmaxr(std::fabs(u(i, k, j) * rdx * msfux(i, j) * dt), std::fabs(v(i, k, j) * rdy * msfvy(i, j) * dt));
+        if (horiz_cfl > mh) mh = horiz_cfl;
+      }
+  *max_vert_cfl = mv; *max_horiz_cfl = mh;
+}
+
+// module_big_step_utilities_em.F:3640-3853.
+template <typename R>
+void coriolis(R* ru_p, R* rv_p, R* rw_p, R* ru_tend_p, R* rv_tend_p, R* rw_tend_p, const WrfDynConfig& cf,
+              R* msftx_p, R* msfty_p, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvy_p, R* f_p, R* e_p, R* sina_p,
+              R* cosa_p, R* fzm_p, R* fzp_p, const Dims& d) {
+  (void)cf;
+  A3<R> ru(ru_p, d), rv(rv_p, d), rw(rw_p, d), ru_tend(ru_tend_p, d), rv_tend(rv_tend_p, d), rw_tend(rw_tend_p, d);
+  A2<R> msftx(msftx_p, d), msfty(msfty_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx(msfvx_p, d),
+      msfvy(msfvy_p, d), f(f_p, d), e(e_p, d), sina(sina_p, d), cosa(cosa_p, d);
+  A1<R> fzm(fzm_p, d), fzp(fzp_p, d);
+  int ktf = std::min(d.kte, d.kde - 1);
+  int i_start = d.its, i_end = d.ite;
+  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = i_start; i <= i_end; ++i)
+        ru_tend(i, k, j) = ru_tend(i, k, j) +
+                           (msfux(i, j) / msfuy(i, j)) * R(0.5) * (f(i, j) + f(i - 1, j)) * R(0.25) *
+                               (rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j)) -
+                           R(0.5) * (e(i, j) + e(i - 1, j)) * R(0.5) * (cosa(i, j) + cosa(i - 1, j)) * R(0.25) *
+                               (rw(i - 1, k + 1, j) + rw(i - 1, k, j) + rw(i, k + 1, j) + rw(i, k, j));
+  int j_start = d.jts, j_end = d.jte;
+  for (int j = j_start; j <= j_end; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= std::min(d.ide - 1, d.ite); ++i)
+        rv_tend(i, k, j) = rv_tend(i, k, j) -
+                           (msfvy(i, j) / msfvx(i, j)) * R(0.5) * (f(i, j) + f(i, j - 1)) * R(0.25) *
+                               (ru(i, k, j) + ru(i + 1, k, j) + ru(i, k, j - 1) + ru(i + 1, k, j - 1)) +
+                           (msfvy(i, j) / msfvx(i, j)) * R(0.5) * (e(i, j) + e(i, j - 1)) * R(0.5) *
+                               (sina(i, j) + sina(i, j - 1)) * R(0.25) *
+                               (rw(i, k + 1, j - 1) + rw(i, k, j - 1) + rw(i, k + 1, j) + rw(i, k, j));
+  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+    for (int k = d.kts + 1; k <= ktf; ++k)
+      for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i)
+        rw_tend(i, k, j) = rw_tend(i, k, j) +
+                           e(i, j) * (cosa(i, j) * R(0.5) *
+                                          (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) -
+                                      (msftx(i, j) / msfty(i, j)) * sina(i, j) * R(0.5) *
+                                          (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))));
+}
+
+// module_big_step_utilities_em.F:4175-4469 (map_proj /= 6, not polar).
+template <typename R>
+void curvature(R* ru_p, R* rv_p, R* rw_p, R* u_p, R* v_p, R* w_p, R* ru_tend_p, R* rv_tend_p, R* rw_tend_p,
+               const WrfDynConfig& cf, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvy_p, R* msftx_p, R* msfty_p,
+               R* xlat_p, R* fzm_p, R* fzp_p, R rdx, R rdy, const Dims& d) {
+  (void)cf; (void)w_p; (void)xlat_p; (void)msfux_p;
+  A3<R> ru(ru_p, d), rv(rv_p, d), rw(rw_p, d), u(u_p, d), v(v_p, d), ru_tend(ru_tend_p, d),
+      rv_tend(rv_tend_p, d), rw_tend(rw_tend_p, d);
+  A2<R> msfuy(msfuy_p, d), msfvx(msfvx_p, d), msfvy(msfvy_p, d), msftx(msftx_p, d), msfty(msfty_p, d);
+  A1<R> fzm(fzm_p, d), fzp(fzp_p, d);
+  const R reradius = K<R>::reradius;
+  int ktf = std::min(d.kte, d.kde - 1);
+  int nx = d.ime - d.ims + 1;
+  // vxgm is a local (ims:ime, kms:kme, jms:jme) array in the reference.
+  std::vector<R> vx_s((size_t)nx * (d.kme - d.kms + 1) * (d.jme - d.jms + 1));
+  A3<R> vxgm(vx_s.data(), d);
+  int i_start = d.its - 1, i_end = d.ite, j_start = d.jts - 1, j_end = d.jte;
+  for (int j = j_start; j <= j_end; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = i_start; i <= i_end; ++i)
+        vxgm(i, k, j) = R(0.5) * (u(i, k, j) + u(i + 1, k, j)) * (msfvx(i, j + 1) - msfvx(i, j)) * rdy -
+                        R(0.5) * (v(i, k, j) + v(i, k, j + 1)) * (msfuy(i + 1, j) - msfuy(i, j)) * rdx;
+  i_start = d.its; i_end = d.ite;
+  for (int j = d.jts; j <= std::min(d.jde - 1, d.jte); ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = i_start; i <= i_end; ++i)
+        ru_tend(i, k, j) = ru_tend(i, k, j) +
+                           R(0.5) * (vxgm(i, k, j) + vxgm(i - 1, k, j)) * R(0.25) *
+                               (rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j)) -
+                           u(i, k, j) * reradius * R(0.25) *
+                               (rw(i - 1, k + 1, j) + rw(i - 1, k, j) + rw(i, k + 1, j) + rw(i, k, j));
+  j_start = d.jts;
+  for (int j = j_start; j <= j_end; ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i)
+        rv_tend(i, k, j) = rv_tend(i, k, j) -
+                           R(0.5) * (vxgm(i, k, j) + vxgm(i, k, j - 1)) * R(0.25) *
+                               (ru(i, k, j) + ru(i + 1, k, j) + ru(i, k, j - 1) + ru(i + 1, k, j - 1)) -
+                           (msfvy(i, j) / msfvx(i, j)) * v(i, k, j) * reradius * R(0.25) *
+                               (rw(i, k + 1, j - 1) + rw(i, k, j - 1) + rw(i, k + 1, j) + rw(i, k, j));
+  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+    for (int k = std::max(2, d.kts); k <= ktf; ++k)
+      for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i)
+        rw_tend(i, k, j) = rw_tend(i, k, j) +
+                           reradius * (R(0.5) * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) *
+                                           R(0.5) * (fzm(k) * (u(i, k, j) + u(i + 1, k, j)) + fzp(k) * (u(i, k - 1, j) + u(i + 1, k - 1, j))) +
+                                       (msftx(i, j) / msfty(i, j)) * R(0.5) *
+                                           (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))) *
+                                           R(0.5) * (fzm(k) * (v(i, k, j) + v(i, k, j + 1)) + fzp(k) * (v(i, k - 1, j) + v(i, k - 1, j + 1))));
+}
+
+// Elementary functions of calc_p_rho_phi.  The reference calls the platform
+// libm (LOG, and x**y through vspow / vpow); any libm within 1 ulp is a valid
+// build of it, and they disagree in the last bit (glibc's logf is not
+// correctly rounded for a few percent of these arguments).  The oracle pins
+// the canonical value: the correctly rounded result, taken from the double
+// libm and rounded once.  -DORACLE_PLATFORM_LIBM selects logf/powf instead.
+template <typename R> static inline R olog(R x) { return std::log(x); }
+template <typename R> static inline R opow(R x, R y) { return std::pow(x, y); }
+#ifndef ORACLE_PLATFORM_LIBM
+template <> inline float olog<float>(float x) { return (float)std::log((double)x); }
+template <> inline float opow<float>(float x, float y) { return (float)std::pow((double)x, (double)y); }
+#endif
+
+// module_big_step_utilities_em.F:953-1226 calc_p_rho_phi, non-hydrostatic
+// branch; VPOW is vspow (real*4 x**y) in the default build and vpow
+// (real*8) under -r8 (module_big_step_utilities_em.F:4-10, frame/libmassv.F:375-390).
+template <typename R>
+void calc_p_rho_phi(R* qv_p, int n_moist_species, int hypsometric_opt, R* al_p, R* alb_p, R* mu_p, R* muts_p,
+                    R* c1_p, R* c2_p, R* c3h_p, R* c4h_p, R* c3f_p, R* c4f_p, R* ph_p, R* phb_p, R* p_p, R* pb_p,
+                    R* t_p, R p0, R t0, R ptop, R* znu_p, R* znw_p, R* dnw_p, R* rdnw_p, R* rdn_p,
+                    int non_hydrostatic, int use_theta_m, const Dims& d) {
+  (void)znu_p; (void)znw_p; (void)dnw_p; (void)rdn_p;
+  A3<R> qv(qv_p, d), al(al_p, d), alb(alb_p, d), ph(ph_p, d), phb(phb_p, d), p(p_p, d), pb(pb_p, d), t(t_p, d);
+  A2<R> mu(mu_p, d), muts(muts_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d), c3h(c3h_p, d), c4h(c4h_p, d), c3f(c3f_p, d), c4f(c4f_p, d), rdnw(rdnw_p, d);
+  if (!non_hydrostatic) throw std::runtime_error("hydrostatic not supported");
+  const R r_d = K<R>::r_d, cpovcv = K<R>::cpovcv, rvovrd = K<R>::rvovrd;
+  int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1), ktf = std::min(d.kte, d.kde - 1);
+  if (hypsometric_opt == 1) {
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          al(i, k, j) = -R(1.) / (c1(k) * muts(i, j) + c2(k)) * (alb(i, k, j) * (c1(k) * mu(i, j)) + rdnw(k) * (ph(i, k + 1, j) - ph(i, k, j)));
+  } else if (hypsometric_opt == 2) {
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i) {
+          R pfu = c3f(k + 1) * muts(i, j) + c4f(k + 1) + ptop;
+          R pfd = c3f(k) * muts(i, j) + c4f(k) + ptop;
+          R phm = c3h(k) * muts(i, j) + c4h(k) + ptop;
+          al(i, k, j) = (ph(i, k + 1, j) - ph(i, k, j) + phb(i, k + 1, j) - phb(i, k, j)) / phm / olog(pfd / pfu) - alb(i, k, j);
+        }
+  } else {
+    throw std::runtime_error("calc_p_rho_phi: hypsometric_opt should be 1 or 2");
+  }
+  if (n_moist_species >= 1) {
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k) {
+        for (int i = d.its; i <= itf; ++i) {
+          R temp;
+          if (use_theta_m == 1) {
+            temp = (r_d * (t0 + t(i, k, j))) / (p0 * (al(i, k, j) + alb(i, k, j)));
+          } else {
+            R qvf = R(1.) + rvovrd * qv(i, k, j);
+            temp = (r_d * (t0 + t(i, k, j)) * qvf) / (p0 * (al(i, k, j) + alb(i, k, j)));
+          }
+          p(i, k, j) = opow(temp, cpovcv);
+        }
+        for (int i = d.its; i <= itf; ++i) p(i, k, j) = p(i, k, j) * p0 - pb(i, k, j);
+      }
+  } else {
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = d.kts; k <= ktf; ++k)
+        for (int i = d.its; i <= itf; ++i)
+          p(i, k, j) = p0 * opow((r_d * (t0 + t(i, k, j))) / (p0 * (al(i, k, j) + alb(i, k, j))), cpovcv) - pb(i, k, j);
+  }
+}
+
+}  // namespace wrforacle

@@ -1,0 +1,455 @@
+"""Seeded synthetic initial states for the benchmark workloads.
+
+The initial state of an idealised WRF-ARW run is produced by the reference's
+dyn_em/module_initialize_ideal.F (init_domain_rk) followed by
+dyn_em/start_em.F.  This module restates that arithmetic in numpy (float64)
+for the physics-off configurations the bench and tests use:
+
+* vertical coordinate: uniform eta levels (module_initialize_ideal.F:626) and
+  the derived 1-D metrics dnw, rdnw, znu, dn, rdn, fnm, fnp, cf1..cf3, cfn,
+  cfn1 (:697-731); hybrid_opt = 0 coefficients c1..c4 (:786-880);
+* base state mub, pb, t_init, alb, phb by hydrostatic integration of a dry
+  sounding (:963-985);
+* full state mu_1, qv, t_1, p, alt, al, ph_1 from the moist sounding
+  (:991-1060), warm bubbles of cos^2 shape (:1089-1133), conversion to moist
+  potential temperature (:1726-1733), and start_em's rediagnosis of al, p,
+  alt (start_em.F:790-841, hypsometric_opt = 2).
+
+The sounding is the analytic Weisman-Klemp (1982) profile (theta_0 = 300 K,
+tropopause 12 km / 343 K / 213 K, surface qv capped at 14 g/kg) with a
+quarter-circle hodograph; random draws use numpy Generator(PCG64(seed)).
+Arrays are returned in the Fortran memory layout (i fastest), shaped
+(jme-jms+1, kme-kms+1, ime-ims+1), halos filled as the reference's periodic
+or symmetric boundary fills would leave them.
+"""
+import math
+import numpy as np
+
+from . import abi
+
+G = 9.81
+R_D = 287.0
+CP = 7.0 * R_D / 2.0
+R_V = 461.6
+CV = CP - R_D
+CVPM = -CV / CP
+P1000 = 1.0e5
+T0 = 300.0
+CPOVCV = CP / (CP - R_D)
+RVOVRD = R_V / R_D
+
+
+class Case:
+    """An initial state: domain description plus named float64 fields."""
+
+    def __init__(self, name, desc, fields, species, meta):
+        self.name = name
+        self.desc = desc
+        self.fields = fields          # name -> ndarray (memory layout)
+        self.species = species        # list of (current, old) ndarrays
+        self.meta = meta
+
+    @property
+    def ide(self):
+        return self.desc.ide
+
+    @property
+    def jde(self):
+        return self.desc.jde
+
+    @property
+    def kde(self):
+        return self.desc.kde
+
+    def cells(self):
+        """Mass cells (ide-1)(jde-1)(kde-1)."""
+        return (self.ide - 1) * (self.jde - 1) * (self.kde - 1)
+
+    def field_items(self):
+        """(field id, array) for every input field, species included."""
+        for name, arr in self.fields.items():
+            yield abi.FIELD_ID[name], arr
+        for s, (cur, old) in enumerate(self.species):
+            yield abi.species_id(s), cur
+            yield abi.species_id(s, old=True), old
+
+
+# ---------------------------------------------------------------------------
+# sounding
+# ---------------------------------------------------------------------------
+def _qvs(p, t):
+    es = 611.2 * np.exp(17.67 * (t - 273.15) / (t - 29.65))
+    return 0.622 * es / np.maximum(p - es, 1.0)
+
+
+def wk_sounding(ztop, theta0=300.0, z_tr=12000.0, theta_tr=343.0, t_tr=213.0,
+                qv0=0.014, hodo_radius=15.0, dz=20.0, dry=False):
+    """Weisman-Klemp (1982) analytic sounding on a fine height grid.
+
+    Returns heights, full pressure, dry pressure, theta, qv, u, v.
+    """
+    z = np.arange(0.0, ztop + 4000.0 + dz, dz)
+    theta = np.where(z <= z_tr, theta0 + (theta_tr - theta0) * (z / z_tr) ** 1.25,
+                     theta_tr * np.exp(G / (CP * t_tr) * (z - z_tr)))
+    rh = np.where(z <= z_tr, 1.0 - 0.75 * (z / z_tr) ** 1.25, 0.25)
+    qv = np.zeros_like(z)
+    p = np.zeros_like(z)
+    for _ in range(4):
+        pi = np.empty_like(z)
+        pi[0] = 1.0
+        thv = theta * (1.0 + 0.61 * qv)
+        for k in range(1, len(z)):
+            pi[k] = pi[k - 1] - G * dz / (CP * 0.5 * (thv[k] + thv[k - 1]))
+        p = P1000 * pi ** (CP / R_D)
+        if dry:
+            break
+        t = theta * pi
+        qv = np.minimum(rh * _qvs(p, t), qv0)
+    # dry-air pressure: integrate the dry-air density down from the top
+    t = theta * (p / P1000) ** (R_D / CP)
+    rho = p / (R_D * t * (1.0 + 0.61 * qv))
+    rho_d = rho / (1.0 + qv)
+    pd = np.empty_like(z)
+    pd[-1] = p[-1] / (1.0 + qv[-1] * RVOVRD)
+    for k in range(len(z) - 2, -1, -1):
+        pd[k] = pd[k + 1] + G * dz * 0.5 * (rho_d[k] + rho_d[k + 1])
+    # quarter-circle hodograph below 2 km, then straight to 6 km
+    zh = np.minimum(z, 2000.0) / 2000.0 * (0.5 * math.pi)
+    u = hodo_radius * (1.0 - np.cos(zh)) + np.clip(z - 2000.0, 0.0, 4000.0) / 4000.0 * hodo_radius
+    v = hodo_radius * np.sin(zh)
+    u = u - 0.5 * hodo_radius
+    v = v - 0.5 * hodo_radius
+    return z, p, pd, theta, qv, u, v
+
+
+# ---------------------------------------------------------------------------
+# vertical coordinate
+# ---------------------------------------------------------------------------
+def eta_metrics(kde):
+    k = np.arange(1, kde + 1, dtype=np.float64)
+    znw = 1.0 - (k - 1.0) / (kde - 1.0)
+    n = kde + 1  # 1-based storage, index 0 unused
+    dnw = np.zeros(n); rdnw = np.zeros(n); znu = np.zeros(n)
+    dn = np.zeros(n); rdn = np.zeros(n); fnp = np.zeros(n); fnm = np.zeros(n)
+    zw = np.zeros(n); zw[1:] = znw
+    for kk in range(1, kde):
+        dnw[kk] = zw[kk + 1] - zw[kk]
+        rdnw[kk] = 1.0 / dnw[kk]
+        znu[kk] = 0.5 * (zw[kk + 1] + zw[kk])
+    for kk in range(2, kde):
+        dn[kk] = 0.5 * (dnw[kk] + dnw[kk - 1])
+        rdn[kk] = 1.0 / dn[kk]
+        fnp[kk] = 0.5 * dnw[kk] / dn[kk]
+        fnm[kk] = 0.5 * dnw[kk - 1] / dn[kk]
+    cof1 = (2.0 * dn[2] + dn[3]) / (dn[2] + dn[3]) * dnw[1] / dn[2]
+    cof2 = dn[2] / (dn[2] + dn[3]) * dnw[1] / dn[3]
+    cf1 = fnp[2] + cof1
+    cf2 = fnm[2] - cof1 - cof2
+    cf3 = cof2
+    cfn = (0.5 * dnw[kde - 1] + dn[kde - 1]) / dn[kde - 1]
+    cfn1 = -0.5 * dnw[kde - 1] / dn[kde - 1]
+    return dict(znw=zw, dnw=dnw, rdnw=rdnw, znu=znu, dn=dn, rdn=rdn, fnp=fnp, fnm=fnm,
+                cf1=cf1, cf2=cf2, cf3=cf3, cfn=cfn, cfn1=cfn1)
+
+
+def hybrid_coefs(m, kde, p_top):
+    """hybrid_opt = 0 (module_initialize_ideal.F:786-880)."""
+    n = kde + 1
+    c3f = m["znw"].copy()
+    c4f = np.zeros(n); c3h = np.zeros(n); c4h = np.zeros(n)
+    c1f = np.zeros(n); c2f = np.zeros(n); c1h = np.zeros(n); c2h = np.zeros(n)
+    for k in range(1, kde + 1):
+        c4f[k] = (m["znw"][k] - c3f[k]) * (P1000 - p_top)
+    for k in range(1, kde):
+        c3h[k] = (c3f[k + 1] + c3f[k]) * 0.5
+        c4h[k] = (m["znu"][k] - c3h[k]) * (P1000 - p_top)
+    for k in range(2, kde):
+        c1f[k] = (c3h[k] - c3h[k - 1]) / (m["znu"][k] - m["znu"][k - 1])
+    c1f[1] = 1.0
+    c1f[kde] = 1.0
+    for k in range(1, kde + 1):
+        c2f[k] = (1.0 - c1f[k]) * (P1000 - p_top)
+    for k in range(1, kde):
+        c1h[k] = (c3f[k + 1] - c3f[k]) / (m["znw"][k + 1] - m["znw"][k])
+        c2h[k] = (1.0 - c1h[k]) * (P1000 - p_top)
+    return dict(c1h=c1h, c2h=c2h, c1f=c1f, c2f=c2f, c3h=c3h, c4h=c4h, c3f=c3f, c4f=c4f)
+
+
+# ---------------------------------------------------------------------------
+# halo fills in numpy (initial state only; the solver does its own)
+# ---------------------------------------------------------------------------
+def _src_index(n_mem_lo, n_mem_hi, nper, periodic, sym_stag, stag):
+    """Source index for every memory index in [lo, hi] (1-based domain)."""
+    idx = np.arange(n_mem_lo, n_mem_hi + 1)
+    if periodic:
+        return (idx - 1) % nper + 1
+    # symmetric: mass points mirror about 0.5 / ide-0.5; staggered about 1 / ide
+    out = idx.copy()
+    if not stag:
+        out = np.where(idx < 1, 1 - idx, out)
+        out = np.where(idx > nper, 2 * nper + 1 - idx, out)
+    else:
+        out = np.where(idx < 1, 2 - idx, out)
+        out = np.where(idx > nper + 1, 2 * (nper + 1) - idx, out)
+    return out
+
+
+def fill_halo(arr, kind, stag, ide, jde, cfg):
+    """Periodic / symmetric image of the interior in the memory halo."""
+    h = abi.HALO
+    nx, ny = ide - 1, jde - 1
+    ix = _src_index(1 - h, ide + h, nx, bool(cfg.periodic_x), 0, stag == "u") + h - 1
+    jy = _src_index(1 - h, jde + h, ny, bool(cfg.periodic_y), 0, stag == "v") + h - 1
+    sign_y = np.ones(len(jy))
+    if not cfg.periodic_y and stag == "v":
+        j = np.arange(1 - h, jde + h + 1)
+        sign_y = np.where((j < 1) | (j > jde), -1.0, 1.0)
+    if kind == 3:
+        out = arr[:, :, ix][jy, :, :]
+        return out * sign_y[:, None, None]
+    out = arr[:, ix][jy, :]
+    return out * sign_y[:, None]
+
+
+# ---------------------------------------------------------------------------
+# ideal supercell-type state
+# ---------------------------------------------------------------------------
+def _interp(x, xp, fp):
+    """Linear interpolation for a monotonic table (increasing or decreasing)."""
+    if xp[0] > xp[-1]:
+        return np.interp(x, xp[::-1], fp[::-1])
+    return np.interp(x, xp, fp)
+
+
+def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
+                    scalar_median=1.0e-6, scalar_sigma=1.0, noise=0.01,
+                    hodo_radius=15.0, name="supercell"):
+    """Weisman-Klemp sounding + cos^2 warm bubbles, doubly periodic.
+
+    bubbles: list of (xc [m], yc [m], zc [m], rx [m], ry [m], rz [m], dtheta [K]).
+    """
+    ide, jde = nx + 1, ny + 1
+    cfg = abi.default_config(periodic_x=True, periodic_y=True)
+    h = abi.HALO
+    nim, njm, nk = ide + 2 * h, jde + 2 * h, kde
+    m = eta_metrics(kde)
+    zd, pdry, _, thd, _, _, _ = wk_sounding(ztop, hodo_radius=hodo_radius, dry=True)
+    p_top = float(_interp(ztop, zd, pdry))
+    hc = hybrid_coefs(m, kde, p_top)
+    c1h, c2h, c1f, c2f = hc["c1h"], hc["c2h"], hc["c1f"], hc["c2f"]
+    c3h, c4h, c3f, c4f = hc["c3h"], hc["c4h"], hc["c3f"], hc["c4f"]
+    dnw, rdnw, rdn = m["dnw"], m["rdnw"], m["rdn"]
+
+    # base state (horizontally uniform, flat terrain)
+    p_surf = float(pdry[0])
+    mub = p_surf - p_top
+    pb = np.zeros(kde + 1); t_init = np.zeros(kde + 1); alb = np.zeros(kde + 1); phb = np.zeros(kde + 1)
+    for k in range(1, kde):
+        pl = c3h[k] * (p_surf - p_top) + c4h[k] + p_top
+        pb[k] = pl
+        t_init[k] = _interp(pl, pdry, thd) - T0
+        alb[k] = (R_D / P1000) * (t_init[k] + T0) * (pb[k] / P1000) ** CVPM
+    for kk in range(2, kde + 1):
+        k = kk - 1
+        phb[kk] = phb[kk - 1] - dnw[kk - 1] * (c1h[k] * mub + c2h[k]) * alb[kk - 1]
+
+    # moist sounding and the full column (identical in every column before bubbles)
+    zm, pm, pdm, thm, qvm, um, vm = wk_sounding(ztop, hodo_radius=hodo_radius)
+    pd_surf = float(pdm[0])
+    mu1 = pd_surf - p_top - mub
+    qv = np.zeros(kde + 1); th = np.zeros(kde + 1)
+    for k in range(1, kde):
+        pl = c3h[k] * (pd_surf - p_top) + c4h[k] + p_top
+        qv[k] = _interp(pl, pdm, qvm)
+        th[k] = _interp(pl, pdm, thm) - T0
+    zhalf = np.array([0.5 * (phb[k] + phb[k + 1]) / G if 1 <= k < kde else 0.0 for k in range(kde + 1)])
+    u_col = np.zeros(kde + 1); v_col = np.zeros(kde + 1)
+    for k in range(1, kde):
+        u_col[k] = _interp(zhalf[k], zm, um)
+        v_col[k] = _interp(zhalf[k], zm, vm)
+
+    # 3-D arrays on the interior (j, k, i) with 1-based k -> index k-1
+    ni, nj, nkm = nx, ny, kde - 1
+    t1 = np.broadcast_to(th[1:kde][None, :, None], (nj, nkm, ni)).copy()
+    qv3 = np.broadcast_to(qv[1:kde][None, :, None], (nj, nkm, ni)).copy()
+    mu1_2d = np.full((nj, ni), mu1)
+
+    def column_p_al(t1, qv3, mu1_2d):
+        """module_initialize_ideal.F:1035-1060: p, alt, al by downward integration."""
+        p = np.zeros_like(t1); alt = np.zeros_like(t1); al = np.zeros_like(t1)
+        kk = kde - 1; k = kk + 1
+        qvf1 = 0.5 * (qv3[:, kk - 1] + qv3[:, kk - 1]); qvf2 = 1.0 / (1.0 + qvf1); qvf1 = qvf1 * qvf2
+        p[:, kk - 1] = -0.5 * ((c1f[k] * mu1_2d) + qvf1 * (c1f[k] * mub + c2f[k])) / rdnw[kk] / qvf2
+        qvf = 1.0 + RVOVRD * qv3[:, kk - 1]
+        alt[:, kk - 1] = (R_D / P1000) * (t1[:, kk - 1] + T0) * qvf * (((p[:, kk - 1] + pb[kk]) / P1000) ** CVPM)
+        al[:, kk - 1] = alt[:, kk - 1] - alb[kk]
+        for kk in range(kde - 2, 0, -1):
+            k = kk + 1
+            qvf1 = 0.5 * (qv3[:, kk - 1] + qv3[:, kk]); qvf2 = 1.0 / (1.0 + qvf1); qvf1 = qvf1 * qvf2
+            p[:, kk - 1] = p[:, kk] - ((c1f[k] * mu1_2d) + qvf1 * (c1f[k] * mub + c2f[k])) / qvf2 / rdn[kk + 1]
+            qvf = 1.0 + RVOVRD * qv3[:, kk - 1]
+            alt[:, kk - 1] = (R_D / P1000) * (t1[:, kk - 1] + T0) * qvf * (((p[:, kk - 1] + pb[kk]) / P1000) ** CVPM)
+            al[:, kk - 1] = alt[:, kk - 1] - alb[kk]
+        return p, alt, al
+
+    def column_ph(al, mu1_2d):
+        ph = np.zeros((nj, kde, ni))
+        for kk in range(2, kde + 1):
+            k = kk - 1
+            ph[:, kk - 1] = ph[:, kk - 2] - dnw[kk - 1] * (((c1h[k] * mub + c2h[k]) + (c1h[k] * mu1_2d)) * al[:, kk - 2]
+                                                          + (c1h[k] * mu1_2d) * alb[kk - 1])
+        return ph
+
+    p3, alt3, al3 = column_p_al(t1, qv3, mu1_2d)
+    ph1 = column_ph(al3, mu1_2d)
+    # bubbles (module_initialize_ideal.F:1089-1133 form)
+    xi = (np.arange(1, ni + 1) - 0.5) * dx
+    yj = (np.arange(1, nj + 1) - 0.5) * dx
+    zmass = 0.5 * (ph1[:, :-1] + ph1[:, 1:] + (phb[1:kde] + phb[2:kde + 1])[None, :, None]) / G
+    for (xc, yc, zc, rx, ry, rz, dth) in bubbles:
+        xr = (xi - xc) / rx
+        yr = (yj - yc) / ry
+        rad = np.sqrt(xr[None, None, :] ** 2 + yr[:, None, None] ** 2 + ((zmass - zc) / rz) ** 2)
+        t1 = t1 + np.where(rad <= 1.0, dth * np.cos(0.5 * math.pi * rad) ** 2, 0.0)
+    if noise > 0:
+        t1 = t1 + rng.uniform(-noise, noise, size=t1.shape)
+    p3, alt3, al3 = column_p_al(t1, qv3, mu1_2d)
+    ph1 = column_ph(al3, mu1_2d)
+    # theta -> moist theta (module_initialize_ideal.F:1726-1733)
+    tm = (t1 + T0) * (1.0 + (R_V / R_D) * qv3) - T0
+    # start_em.F:790-841 (hypsometric_opt = 2): al from ph, p from the EOS
+    mut = mub + mu1_2d
+    al3 = np.zeros_like(tm)
+    for k in range(1, kde):
+        pfu = c3f[k + 1] * mut + c4f[k + 1] + p_top
+        pfd = c3f[k] * mut + c4f[k] + p_top
+        phm = c3h[k] * mut + c4h[k] + p_top
+        al3[:, k - 1] = (ph1[:, k] - ph1[:, k - 1] + phb[k + 1] - phb[k]) / phm / np.log(pfd / pfu) - alb[k]
+    p3 = P1000 * ((R_D * (T0 + tm)) / (P1000 * (al3 + alb[1:kde][None, :, None]))) ** CPOVCV - pb[1:kde][None, :, None]
+    alt3 = al3 + alb[1:kde][None, :, None]
+
+    # assemble memory-layout arrays
+    def mem3(interior, nkk, stag=None):
+        a = np.zeros((njm, nk, nim))
+        a[h:h + interior.shape[0], :nkk, h:h + interior.shape[2]] = interior
+        if stag == "u":
+            a[h:h + interior.shape[0], :nkk, h + nx] = interior[:, :, 0]
+        if stag == "v":
+            a[h + ny, :nkk, h:h + interior.shape[2]] = interior[0, :, :]
+        return fill_halo(a, 3, stag, ide, jde, cfg)
+
+    def mem2(interior):
+        a = np.zeros((njm, nim))
+        a[h:h + nj, h:h + ni] = interior
+        return fill_halo(a, 2, None, ide, jde, cfg)
+
+    def col(v1d, nkk):
+        return np.broadcast_to(v1d[1:nkk + 1][None, :, None], (nj, nkk, ni))
+
+    f = {}
+    f["u_1"] = mem3(np.broadcast_to(u_col[1:kde][None, :, None], (nj, nkm, ni)), nkm, "u")
+    f["v_1"] = mem3(np.broadcast_to(v_col[1:kde][None, :, None], (nj, nkm, ni)), nkm, "v")
+    f["u_2"] = f["u_1"].copy(); f["v_2"] = f["v_1"].copy()
+    f["w_1"] = np.zeros((njm, nk, nim)); f["w_2"] = np.zeros((njm, nk, nim))
+    f["t_1"] = mem3(tm, nkm); f["t_2"] = f["t_1"].copy()
+    f["ph_1"] = mem3(ph1, kde); f["ph_2"] = f["ph_1"].copy()
+    f["phb"] = mem3(col(phb, kde), kde)
+    f["pb"] = mem3(col(pb, nkm), nkm)
+    f["alb"] = mem3(col(alb, nkm), nkm)
+    f["p"] = mem3(p3, nkm)
+    f["al"] = mem3(al3, nkm)
+    f["alt"] = mem3(alt3, nkm)
+    f["mu_1"] = mem2(mu1_2d); f["mu_2"] = f["mu_1"].copy()
+    f["mub"] = mem2(np.full((nj, ni), mub))
+    for nm in ("msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy", "msftx", "msfty", "cosa"):
+        f[nm] = np.ones((njm, nim))
+    for nm in ("ht", "f", "e", "sina"):
+        f[nm] = np.zeros((njm, nim))
+    for nm in ("znw", "znu", "dnw", "rdnw", "dn", "rdn", "fnm", "fnp"):
+        f[nm] = m[nm][1:].copy()
+    for nm in ("c1h", "c2h", "c1f", "c2f", "c3h", "c4h", "c3f", "c4f"):
+        f[nm] = hc[nm][1:].copy()
+
+    species = []
+    qv_mem = mem3(qv3, nkm)
+    species.append((qv_mem, qv_mem.copy()))
+    for _ in range(n_scalar):
+        qs = scalar_median * np.exp(scalar_sigma * rng.standard_normal(size=(nj, nkm, ni)))
+        qm = mem3(qs, nkm)
+        species.append((qm, qm.copy()))
+
+    desc = abi.WrfGpuDomainDesc()
+    desc.ide, desc.jde, desc.kde = ide, jde, kde
+    desc.n_moist, desc.n_scalar = 1, n_scalar
+    desc.config = cfg
+    s = desc.scalars
+    s.dt, s.dx, s.dy = dt, dx, dx
+    s.rdx, s.rdy = 1.0 / dx, 1.0 / dx
+    s.cf1, s.cf2, s.cf3, s.cfn, s.cfn1 = m["cf1"], m["cf2"], m["cf3"], m["cfn"], m["cfn1"]
+    s.epssm, s.smdiv, s.emdiv = 0.1, 0.1, 0.01
+    s.p_top = p_top
+    meta = dict(dx=dx, dt=dt, ztop=ztop, bubbles=bubbles, n_scalar=n_scalar)
+    return Case(name, desc, f, species, meta)
+
+
+# ---------------------------------------------------------------------------
+# the benchmark workloads
+# ---------------------------------------------------------------------------
+def config1(seed=1, scale=1):
+    """41x41 x 41 eta levels, dx = 2 km, top 20 km, dt = 12 s, one +3 K bubble
+    (10 km / 1.5 km radii at 1.5 km), +-0.01 K noise, qv only."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nx = 41 * scale
+    dx = 2000.0
+    xc = 0.5 * nx * dx
+    return supercell_state(nx, nx, 41, dx, 12.0, 20000.0,
+                           [(xc, xc, 1500.0, 10000.0, 10000.0, 1500.0, 3.0)], rng,
+                           n_scalar=0, name="c1_41x41x41")
+
+
+def config2(seed=2, nx=512, kde=80, n_scalar=10):
+    """512x512 x 80 levels, dx = 1 km, top 20 km, dt = 6 s, 16 +3 K bubbles at
+    seeded positions, 10 positive-definite log-normal scalars (median 1e-6,
+    sigma 1) plus qv."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dx = 1000.0
+    L = nx * dx
+    bubbles = []
+    for _ in range(16):
+        xc, yc = rng.uniform(0.0, L, size=2)
+        bubbles.append((float(xc), float(yc), 1500.0, 10000.0, 10000.0, 1500.0, 3.0))
+    return supercell_state(nx, nx, kde, dx, 6.0, 20000.0, bubbles, rng, n_scalar=n_scalar,
+                           name="c2_%dx%dx%d" % (nx, nx, kde))
+
+
+def ensemble_members(seed=4, n=64, nmin=64, nmax=256, kmin=41, kmax=80, n_scalar=3, dx=2000.0, dt=12.0):
+    """Uneven ensemble: nx, ny ~ U[nmin, nmax], levels ~ U[kmin, kmax], seeded
+    bubble position and amplitude in [1, 4] K, 3 PD scalars per member."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs = []
+    for _ in range(n):
+        nx = int(rng.integers(nmin, nmax + 1))
+        ny = int(rng.integers(nmin, nmax + 1))
+        kde = int(rng.integers(kmin, kmax + 1))
+        amp = float(rng.uniform(1.0, 4.0))
+        xc = float(rng.uniform(0.25, 0.75)) * nx * dx
+        yc = float(rng.uniform(0.25, 0.75)) * ny * dx
+        specs.append((nx, ny, kde, amp, xc, yc, int(rng.integers(0, 2 ** 31))))
+    return specs
+
+
+def ensemble_member(spec, dx=2000.0, dt=12.0, n_scalar=3):
+    nx, ny, kde, amp, xc, yc, mseed = spec
+    rng = np.random.Generator(np.random.PCG64(mseed))
+    return supercell_state(nx, ny, kde, dx, dt, 20000.0,
+                           [(xc, yc, 1500.0, 10000.0, 10000.0, 1500.0, amp)], rng,
+                           n_scalar=n_scalar, name="member_%dx%dx%d" % (nx, ny, kde))
+
+
+def small_case(nx=12, ny=10, kde=12, n_scalar=1, seed=7, dx=2000.0, dt=12.0):
+    """A tiny domain for fast parity tests (one bubble, noise, scalars)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = nx * dx
+    return supercell_state(nx, ny, kde, dx, dt, 20000.0,
+                           [(0.5 * L, 0.5 * ny * dx, 1500.0, 6000.0, 6000.0, 1500.0, 3.0)], rng,
+                           n_scalar=n_scalar, name="small_%dx%dx%d" % (nx, ny, kde))

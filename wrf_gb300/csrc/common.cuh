@@ -1,0 +1,203 @@
+// Shared device definitions of the GB300 WRF-ARW large-step kernels.
+//
+// Data layout in HBM: every field keeps the reference's Fortran memory layout
+// (ims:ime, kms:kme, jms:jme), i fastest, halo 4 (the serial build's
+// bdyzone), so a Fortran caller's arrays map onto device buffers by a plain
+// copy and the halo-fill sites of solve_em map one to one.  A domain is a
+// "member": a descriptor (Mem) holding its index bounds, strides and the
+// device pointers of all of its fields.  Every kernel is written against a
+// table of members; a launch covers all members' blocks through a prefix
+// table (block_start), so one launch advances a single domain (the plain
+// drop-in form) or a whole uneven ensemble (the batched form) with the same
+// per-point arithmetic.
+//
+// Arithmetic: the plain form is compiled with --fmad=false and IEEE division
+// so every expression rounds in the reference's left-to-right order; the
+// only non-bitwise operations against the reference's FP32 build are powf
+// and logf in calc_p_rho_phi (CUDA's implementations, a few ulp).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/wrfgpu.h"
+
+namespace wrfgpu {
+
+constexpr int NSPMAX = 16;           // species per member (moist + passive)
+constexpr int BX = 32, BY = 4;       // thread block: 32 (i) x 4 (j)
+constexpr float G = 9.81f;
+constexpr float R_D = 287.f;
+constexpr float CP = 7.f * R_D / 2.f;
+constexpr float CV = CP - R_D;
+constexpr float CPOVCV = CP / (CP - R_D);
+constexpr float T0 = 300.f;
+constexpr float P0 = 100000.f;
+constexpr float RERADIUS = 1.f / 6370.0e03f;
+
+// Error word bits (Mem::err): set by kernels, read by the host between steps.
+constexpr unsigned ERR_NONFINITE = 1u;
+constexpr unsigned ERR_CFL = 2u;
+constexpr unsigned ERR_TIMEOUT = 4u;
+
+struct Mem {
+  int ids, ide, jds, jde, kds, kde;
+  int ims, ime, jms, jme, kms, kme;
+  int its, ite, jts, jte, kts, kte;
+  long long sk, sj, s2;   // 3-D k and j strides, 2-D j stride (elements)
+  float* f3[WRFGPU_N3D];
+  float* f2[WRFGPU_N2D];
+  float* f1[WRFGPU_N1D];
+  float* q[NSPMAX];       // species current (_2)
+  float* qo[NSPMAX];      // species old (_1)
+  double* wd[3];          // FP64 a/alpha/gamma of the mixed-precision form (or null)
+  int nsp, n_moist;
+  int ns_total;           // acoustic steps per large step
+  int pad0;
+  float dt, rdx, rdy, cf1, cf2, cf3, cfn, cfn1, epssm, smdiv, emdiv, p_top;
+  WrfDynConfig cf;
+  unsigned* err;          // per-member error word
+  float cfl_limit;        // vertical CFL above which ERR_CFL is raised (<=0: off)
+  float pad1;
+  float* cfl_out;         // [2]: max vertical, max horizontal CFL (atomic max)
+};
+
+// Stage constants of solve_em.F:601-615 for one member.
+struct Stage {
+  float dt_rk, dts_rk;
+  int nsmall;
+};
+__host__ __device__ inline Stage stage_of(const Mem& m, int rk_step) {
+  Stage s;
+  float dts = m.dt / float(m.ns_total);
+  if (rk_step == 1) { s.dt_rk = m.dt / 3.f; s.dts_rk = s.dt_rk; s.nsmall = 1; }
+  else if (rk_step == 2) { s.dt_rk = 0.5f * m.dt; s.dts_rk = dts; s.nsmall = m.ns_total / 2; }
+  else { s.dt_rk = m.dt; s.dts_rk = dts; s.nsmall = m.ns_total; }
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Accessors (Fortran indices)
+// ---------------------------------------------------------------------------
+struct F3 {
+  float* __restrict__ p; long long sk, sj; int ims, kms, jms;
+  __device__ __forceinline__ float& operator()(int i, int k, int j) const {
+    return p[(long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj];
+  }
+};
+struct F2 {
+  float* __restrict__ p; long long sj; int ims, jms;
+  __device__ __forceinline__ float& operator()(int i, int j) const {
+    return p[(long long)(i - ims) + (long long)(j - jms) * sj];
+  }
+};
+struct F1 {
+  const float* __restrict__ p; int kms;
+  __device__ __forceinline__ float operator()(int k) const { return __ldg(p + (k - kms)); }
+};
+struct D3 {
+  double* __restrict__ p; long long sk, sj; int ims, kms, jms;
+  __device__ __forceinline__ double& operator()(int i, int k, int j) const {
+    return p[(long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj];
+  }
+};
+__device__ __forceinline__ F3 f3(const Mem& m, int id) { return F3{m.f3[id], m.sk, m.sj, m.ims, m.kms, m.jms}; }
+__device__ __forceinline__ F3 f3p(const Mem& m, float* p) { return F3{p, m.sk, m.sj, m.ims, m.kms, m.jms}; }
+__device__ __forceinline__ F2 f2(const Mem& m, int id) {
+  return F2{m.f2[id - WRFGPU_F2D_BASE], m.s2, m.ims, m.jms};
+}
+__device__ __forceinline__ F1 f1(const Mem& m, int id) { return F1{m.f1[id - WRFGPU_F1D_BASE], m.kms}; }
+__device__ __forceinline__ D3 d3(const Mem& m, double* p) { return D3{p, m.sk, m.sj, m.ims, m.kms, m.jms}; }
+
+// ---------------------------------------------------------------------------
+// Flux operators (module_advect_em.F:172-186; advect_scalar_pd's pre-divided
+// coefficients :6165-6185).  sign(1,time_step) == 1 for forward runs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sgn1(float a) { return copysignf(1.f, a); }
+__device__ __forceinline__ float flux4(float qm2, float qm1, float q, float qp1) {
+  return (7.f * (q + qm1) - (qp1 + qm2)) / 12.0f;
+}
+__device__ __forceinline__ float flux3(float qm2, float qm1, float q, float qp1, float ua) {
+  return flux4(qm2, qm1, q, qp1) + 1.f * sgn1(ua) * ((qp1 - qm2) - 3.f * (q - qm1)) / 12.0f;
+}
+__device__ __forceinline__ float flux6(float qm3, float qm2, float qm1, float q, float qp1, float qp2) {
+  return (37.f * (q + qm1) - 8.f * (qp1 + qm2) + (qp2 + qm3)) / 60.0f;
+}
+__device__ __forceinline__ float flux5(float qm3, float qm2, float qm1, float q, float qp1, float qp2, float ua) {
+  return flux6(qm3, qm2, qm1, q, qp1, qp2) - 1.f * sgn1(ua) * ((qp2 - qm3) - 5.f * (qp1 - qm2) + 10.f * (q - qm1)) / 60.0f;
+}
+__device__ __forceinline__ float pflux4(float qm2, float qm1, float q, float qp1) {
+  return (7.f / 12.f) * (q + qm1) - (1.f / 12.f) * (qp1 + qm2);
+}
+__device__ __forceinline__ float pflux3(float qm2, float qm1, float q, float qp1, float ua) {
+  return pflux4(qm2, qm1, q, qp1) + 1.f * sgn1(ua) * (1.f / 12.f) * ((qp1 - qm2) - 3.f * (q - qm1));
+}
+__device__ __forceinline__ float pflux6(float qm3, float qm2, float qm1, float q, float qp1, float qp2) {
+  return (37.f / 60.f) * (q + qm1) - (2.f / 15.f) * (qp1 + qm2) + (1.f / 60.f) * (qp2 + qm3);
+}
+__device__ __forceinline__ float pflux5(float qm3, float qm2, float qm1, float q, float qp1, float qp2, float ua) {
+  return pflux6(qm3, qm2, qm1, q, qp1, qp2) -
+         1.f * sgn1(ua) * (1.f / 60.f) * ((qp2 - qm3) - 5.f * (qp1 - qm2) + 10.f * (q - qm1));
+}
+__device__ __forceinline__ float fmaxf_f(float a, float b) { return a > b ? a : b; }   // Fortran MAX
+__device__ __forceinline__ float fminf_f(float a, float b) { return a < b ? a : b; }   // Fortran MIN
+__device__ __forceinline__ float flux_upwind(float qm1, float q, float cr) {
+  return 0.5f * fminf_f(1.0f, (cr + fabsf(cr))) * qm1 + 0.5f * fmaxf_f(-1.0f, (cr - fabsf(cr))) * q;
+}
+
+// ---------------------------------------------------------------------------
+// Launch geometry.  Every member's index space [ims+? ...] is cut into
+// 32x4 (i x j) blocks covering i in [ims, ime], j in [jms, jme]; 3-D point
+// kernels add a k index per block.  block_start[m] is the prefix of block
+// counts; a block finds its member by binary search.
+// ---------------------------------------------------------------------------
+struct Launch {
+  const Mem* mem;            // device array of members
+  const int* block_start;    // [nmem+1] prefix over blocks of this launch kind
+  int nmem;
+  int kind;                  // 2: column blocks (i,j); 3: point blocks (i,j,k)
+};
+
+struct BlockPos {
+  int m;      // member
+  int i, j;   // Fortran indices of this thread
+  int k;      // level (point kernels) or 0
+  bool valid;
+};
+
+__device__ __forceinline__ int find_member(const int* __restrict__ bs, int nmem, int b) {
+  int lo = 0, hi = nmem - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(bs + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ BlockPos block_pos(const Launch& L) {
+  BlockPos bp;
+  int b = blockIdx.x;
+  bp.m = find_member(L.block_start, L.nmem, b);
+  const Mem& m = L.mem[bp.m];
+  int lb = b - __ldg(L.block_start + bp.m);
+  int nbx = (m.ime - m.ims + 1 + BX - 1) / BX;
+  int nby = (m.jme - m.jms + 1 + BY - 1) / BY;
+  int bxy = lb;
+  bp.k = 0;
+  if (L.kind == 3) { bp.k = lb / (nbx * nby) + m.kms; bxy = lb % (nbx * nby); }
+  int bx = bxy % nbx, by = bxy / nbx;
+  bp.i = m.ims + bx * BX + (int)threadIdx.x;
+  bp.j = m.jms + by * BY + (int)threadIdx.y;
+  bp.valid = bp.i <= m.ime && bp.j <= m.jme && (L.kind != 3 || bp.k <= m.kme);
+  return bp;
+}
+
+inline int blocks_for(const int ims, const int ime, const int jms, const int jme, const int nk, int kind) {
+  int nbx = (ime - ims + 1 + BX - 1) / BX;
+  int nby = (jme - jms + 1 + BY - 1) / BY;
+  return nbx * nby * (kind == 3 ? nk : 1);
+}
+
+__device__ __forceinline__ void raise_err(const Mem& m, unsigned bits) {
+  if (m.err) atomicOr(m.err, bits);
+}
+
+}  // namespace wrfgpu

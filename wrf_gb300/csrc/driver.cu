@@ -1,0 +1,597 @@
+// Host runtime: device-resident domains/ensembles, the solve_em large-step
+// sequence, CUDA-graph capture and the coarse C ABI of include/wrfgpu.h.
+//
+// The step sequence follows dyn_em/solve_em.F:578-4750 for the physics-off
+// options, with each of the reference's halo-exchange / boundary-fill sync
+// sites (HALO_EM_A/B/C/C2/D*, PERIOD_BDY_*, set_physical_bc*) mapped to a
+// kernel boundary plus one batched on-device halo-fill launch.  A plain
+// domain is an ensemble of one member; an ensemble of uneven members runs
+// the same launches with every kernel covering all members' blocks.
+//
+// Two calls of the reference that provably leave the state unchanged are not
+// issued: rk_addtend_dry adds physics tendencies that are identically zero
+// with physics off (module_em.F:959-1092), and the post-RK calc_p_rho_phi
+// (solve_em.F:4180-4203) recomputes al and p from the same inputs as the
+// stage-3 call.  initialize_moist_old (solve_em.F:517-527) is also skipped:
+// moist_old is overwritten by rk_update_scalar before any read.
+#include <cstdio>
+#include <cstring>
+#include <cstdlib>
+#include <vector>
+#include <string>
+#include <algorithm>
+#include <cuda_runtime.h>
+#include "common.cuh"
+#include "kernels.h"
+#include "../../include/wrfgpu.h"
+
+namespace wrfgpu {
+
+#define CK(x)                                                                                  \
+  do {                                                                                         \
+    cudaError_t e_ = (x);                                                                      \
+    if (e_ != cudaSuccess) {                                                                   \
+      std::fprintf(stderr, "wrfgpu: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return WRFGPU_E_CUDA;                                                                    \
+    }                                                                                          \
+  } while (0)
+
+// Profiling phases (the reference's BENCH timer vocabulary, inc/bench_solve_em_def.h,
+// refined to one entry per kernel family).
+enum Phase {
+  PH_PREP = 0, PH_FILL, PH_TEND_U, PH_TEND_V, PH_TEND_W, PH_TEND_T, PH_TEND_PH, PH_CFL, PH_SSP, PH_CPR0,
+  PH_COEFW, PH_AUV, PH_AMUT, PH_AW, PH_SUMF, PH_SSF, PH_USPD, PH_PD, PH_ADVS, PH_UPDS, PH_CPRP, PH_WSURF,
+  PH_END, NPHASE
+};
+static const char* PHASE_NAMES[NPHASE] = {
+    "step_prep", "bc_fill", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",
+    "small_step_prep", "calc_p_rho_0", "calc_coef_w", "advance_uv", "advance_mu_t", "advance_w",
+    "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "advect_scalar_pd", "advect_scalar",
+    "rk_update_scalar", "calc_p_rho_phi", "set_w_surface", "end"};
+
+static int check_desc(const WrfGpuDomainDesc& d) {
+  const WrfDynConfig& c = d.config;
+  if (d.ide < 8 || d.jde < 8 || d.kde < 6 || d.kde > 128) return WRFGPU_E_ARG;
+  if (d.n_moist != 1 || d.n_scalar < 0 || d.n_moist + d.n_scalar > NSPMAX) return WRFGPU_E_ARG;
+  if (c.rk_ord != 3 || c.h_mom_adv_order != 5 || c.h_sca_adv_order != 5 || c.v_mom_adv_order != 3 ||
+      c.v_sca_adv_order != 3)
+    return WRFGPU_E_ARG;
+  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || c.damp_opt == 3 || c.w_damping != 0 || c.diff_opt != 0)
+    return WRFGPU_E_ARG;
+  if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
+  if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;
+  if (c.open_xs || c.open_xe || c.open_ys || c.open_ye || c.specified || c.nested || c.polar) return WRFGPU_E_ARG;
+  if (c.hypsometric_opt != 1 && c.hypsometric_opt != 2) return WRFGPU_E_ARG;
+  if (d.scalars.dt <= 0 || d.scalars.dx <= 0 || d.scalars.dy <= 0) return WRFGPU_E_ARG;
+  return WRFGPU_OK;
+}
+
+static int num_sound_steps(const WrfGpuDomainDesc& d) {
+  if (d.config.time_step_sound != 0) return d.config.time_step_sound;
+  float spacing = std::min((float)d.scalars.dx, (float)d.scalars.dy);
+  return std::max(2 * ((int)(300.f * (float)d.scalars.dt / spacing - 0.01f) + 1), 4);
+}
+
+struct Ensemble {
+  int nmem = 0;
+  int flags = 0;
+  bool fp64 = false;
+  std::vector<WrfGpuDomainDesc> descs;
+  std::vector<Mem> hm;                 // host copies of the member descriptors
+  Mem* d_mems = nullptr;
+  int *d_bs2 = nullptr, *d_bs3 = nullptr;
+  int nb2 = 0, nb3 = 0;
+  int nsp_max = 0, ns_max = 0;
+  std::vector<size_t> n3, n2, n1;      // element counts per member
+  char* pool = nullptr;                // one device allocation for all fields
+  size_t pool_bytes = 0;
+  float** d_pd_scratch = nullptr;      // per-member limiter scratch pointers
+  unsigned* d_err = nullptr;
+  float* d_cfl = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool cfl_check = true;
+  int halo_blocks = 64;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<std::pair<int, cudaEvent_t>>* prof = nullptr;  // per-launch marks when profiling
+
+  void mark(int ph) {
+    if (!prof) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream);
+    prof->push_back({ph, e});
+  }
+
+  Launch L2() const { return Launch{d_mems, d_bs2, nmem, 2}; }
+  Launch L3() const { return Launch{d_mems, d_bs3, nmem, 3}; }
+
+  ~Ensemble() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    if (pool) cudaFree(pool);
+    if (d_mems) cudaFree(d_mems);
+    if (d_bs2) cudaFree(d_bs2);
+    if (d_bs3) cudaFree(d_bs3);
+    if (d_pd_scratch) cudaFree(d_pd_scratch);
+    if (d_err) cudaFree(d_err);
+    if (d_cfl) cudaFree(d_cfl);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  static size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+  int init(const WrfGpuDomainDesc* ds, int n, int fl) {
+    nmem = n; flags = fl; fp64 = (fl & WRFGPU_FLAG_MIXED) != 0;
+    cfl_check = (fl & WRFGPU_FLAG_NO_CHECKS) == 0;
+    descs.assign(ds, ds + n);
+    for (int m = 0; m < n; ++m) {
+      int rc = check_desc(ds[m]);
+      if (rc) return rc;
+    }
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    hm.resize(n); n3.resize(n); n2.resize(n); n1.resize(n);
+    // sizes
+    std::vector<size_t> off(n);
+    size_t total = 0;
+    for (int m = 0; m < n; ++m) {
+      const WrfGpuDomainDesc& d = ds[m];
+      size_t ni = d.ide + 2 * WRFGPU_HALO, nj = d.jde + 2 * WRFGPU_HALO, nk = d.kde;  // ims..ime, jms..jme
+      n3[m] = ni * nk * nj; n2[m] = ni * nj; n1[m] = nk;
+      int nsp = d.n_moist + d.n_scalar;
+      size_t b = 0;
+      b += (size_t)WRFGPU_N3D * al256(n3[m] * 4);
+      b += (size_t)2 * nsp * al256(n3[m] * 4);
+      b += (size_t)WRFGPU_N2D * al256(n2[m] * 4);
+      b += (size_t)WRFGPU_N1D * al256(n1[m] * 4);
+      b += al256(n3[m] * 4);  // limiter scratch
+      if (fp64) b += 3 * al256(n3[m] * 8);
+      off[m] = total;
+      total += b;
+    }
+    pool_bytes = total;
+    if (cudaMalloc(&pool, total) != cudaSuccess) { pool = nullptr; return WRFGPU_E_NOMEM; }
+    CK(cudaMemsetAsync(pool, 0, total, stream));
+    CK(cudaMalloc(&d_err, sizeof(unsigned) * n));
+    CK(cudaMemsetAsync(d_err, 0, sizeof(unsigned) * n, stream));
+    CK(cudaMalloc(&d_cfl, sizeof(float) * 2 * n));
+    CK(cudaMemsetAsync(d_cfl, 0, sizeof(float) * 2 * n, stream));
+    std::vector<float*> scr(n);
+    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0);
+    for (int m = 0; m < n; ++m) {
+      const WrfGpuDomainDesc& d = ds[m];
+      Mem& M = hm[m];
+      std::memset(&M, 0, sizeof(Mem));
+      M.ids = 1; M.ide = d.ide; M.jds = 1; M.jde = d.jde; M.kds = 1; M.kde = d.kde;
+      M.ims = 1 - WRFGPU_HALO; M.ime = d.ide + WRFGPU_HALO; M.jms = 1 - WRFGPU_HALO; M.jme = d.jde + WRFGPU_HALO;
+      M.kms = 1; M.kme = d.kde;
+      M.its = M.ids; M.ite = M.ide; M.jts = M.jds; M.jte = M.jde; M.kts = M.kds; M.kte = M.kde;
+      M.sk = M.ime - M.ims + 1; M.sj = M.sk * (M.kme - M.kms + 1); M.s2 = M.sk;
+      char* p = pool + off[m];
+      for (int f = 0; f < WRFGPU_N3D; ++f) { M.f3[f] = (float*)p; p += al256(n3[m] * 4); }
+      M.nsp = d.n_moist + d.n_scalar; M.n_moist = d.n_moist;
+      for (int s = 0; s < M.nsp; ++s) { M.q[s] = (float*)p; p += al256(n3[m] * 4); M.qo[s] = (float*)p; p += al256(n3[m] * 4); }
+      for (int f = 0; f < WRFGPU_N2D; ++f) { M.f2[f] = (float*)p; p += al256(n2[m] * 4); }
+      for (int f = 0; f < WRFGPU_N1D; ++f) { M.f1[f] = (float*)p; p += al256(n1[m] * 4); }
+      scr[m] = (float*)p; p += al256(n3[m] * 4);
+      if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
+      M.ns_total = num_sound_steps(d);
+      const WrfGpuScalars& s = d.scalars;
+      M.dt = (float)s.dt; M.rdx = (float)s.rdx; M.rdy = (float)s.rdy;
+      M.cf1 = (float)s.cf1; M.cf2 = (float)s.cf2; M.cf3 = (float)s.cf3; M.cfn = (float)s.cfn; M.cfn1 = (float)s.cfn1;
+      M.epssm = (float)s.epssm; M.smdiv = (float)s.smdiv; M.emdiv = (float)s.emdiv; M.p_top = (float)s.p_top;
+      M.cf = d.config;
+      M.err = d_err + m;
+      M.cfl_out = d_cfl + 2 * m;
+      M.cfl_limit = 0.f;
+      nsp_max = std::max(nsp_max, M.nsp);
+      ns_max = std::max(ns_max, M.ns_total);
+      bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
+      bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
+    }
+    nb2 = bs2[n]; nb3 = bs3[n];
+    CK(cudaMalloc(&d_mems, sizeof(Mem) * n));
+    CK(cudaMemcpyAsync(d_mems, hm.data(), sizeof(Mem) * n, cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_bs2, sizeof(int) * (n + 1)));
+    CK(cudaMalloc(&d_bs3, sizeof(int) * (n + 1)));
+    CK(cudaMemcpyAsync(d_bs2, bs2.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_bs3, bs3.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_pd_scratch, sizeof(float*) * n));
+    CK(cudaMemcpyAsync(d_pd_scratch, scr.data(), sizeof(float*) * n, cudaMemcpyHostToDevice, stream));
+    // map factors default to 1, cosa to 1 (ideal cases); callers overwrite via set_field
+    for (int m = 0; m < n; ++m) {
+      std::vector<float> ones(n2[m], 1.f);
+      for (int f : {WRFGPU_MSFUX, WRFGPU_MSFUY, WRFGPU_MSFVX, WRFGPU_MSFVX_INV, WRFGPU_MSFVY, WRFGPU_MSFTX,
+                    WRFGPU_MSFTY, WRFGPU_COSA})
+        CK(cudaMemcpy(hm[m].f2[f - WRFGPU_F2D_BASE], ones.data(), n2[m] * 4, cudaMemcpyHostToDevice));
+    }
+    CK(cudaStreamSynchronize(stream));
+    halo_blocks = std::max(8, std::min(256, (int)(n3[0] / 20000)));
+    return WRFGPU_OK;
+  }
+
+  float* field_ptr(int m, int id, size_t* count) {
+    const Mem& M = hm[m];
+    if (id >= 0 && id < WRFGPU_N3D) { *count = n3[m]; return M.f3[id]; }
+    if (id >= WRFGPU_F2D_BASE && id < WRFGPU_F2D_END) { *count = n2[m]; return M.f2[id - WRFGPU_F2D_BASE]; }
+    if (id >= WRFGPU_F1D_BASE && id < WRFGPU_F1D_END) { *count = n1[m]; return M.f1[id - WRFGPU_F1D_BASE]; }
+    if (id >= WRFGPU_SPECIES_BASE && id < WRFGPU_SPECIES_BASE + 2 * M.nsp) {
+      int s = (id - WRFGPU_SPECIES_BASE) / 2, old = (id - WRFGPU_SPECIES_BASE) % 2;
+      *count = n3[m];
+      return old ? M.qo[s] : M.q[s];
+    }
+    *count = 0;
+    return nullptr;
+  }
+
+  // ---------------------------------------------------------------- halo
+  struct JobList {
+    std::vector<HaloJob> v;
+    void f3(int id, char var) { HaloJob j{id, 3, -1, 0, var, {0, 0, 0}}; v.push_back(j); }
+    void f2(int id, char var) { HaloJob j{id, 2, -1, 0, var, {0, 0, 0}}; v.push_back(j); }
+    void sp(int s, int old, char var) { HaloJob j{0, 3, s, old, var, {0, 0, 0}}; v.push_back(j); }
+  };
+  void fill(const JobList& jl) {
+    mark(PH_FILL);
+    for (size_t b = 0; b < jl.v.size(); b += MAX_HALO_JOBS) {
+      HaloJobs hj;
+      hj.n = (int)std::min(jl.v.size() - b, (size_t)MAX_HALO_JOBS);
+      for (int q = 0; q < hj.n; ++q) hj.job[q] = jl.v[b + q];
+      launch_fill_halo(d_mems, nmem, hj, halo_blocks, stream);
+    }
+  }
+
+  // ---------------------------------------------------------------- one large step
+  void enqueue_step() {
+    const Launch l2 = L2(), l3 = L3();
+    for (int rk_step = 1; rk_step <= 3; ++rk_step) {
+      StepArgs a{rk_step, 0, 0, 0};
+      mark(PH_PREP);
+      launch_rk_step_prep(l2, nb2, stream);
+      {  // rk_phys_bc_dry_1 + al, ph_2 (solve_em.F:726-754)
+        JobList j;
+        j.f3(WRFGPU_RU, 'u'); j.f3(WRFGPU_RV, 'v'); j.f3(WRFGPU_RW, 'w'); j.f3(WRFGPU_WW, 'w');
+        j.f3(WRFGPU_PHP, 'w'); j.f3(WRFGPU_ALT, 't'); j.f3(WRFGPU_P, 'p');
+        j.f2(WRFGPU_MUU, 'u'); j.f2(WRFGPU_MUV, 'v'); j.f2(WRFGPU_MUT, 't');
+        j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_PH_2, 'w');
+        fill(j);
+      }
+      // rk_tendency (module_em.F:370-781)
+      mark(PH_TEND_U); launch_tend_u(l3, nb3, TF_ALL, stream);
+      mark(PH_TEND_V); launch_tend_v(l3, nb3, TF_ALL, stream);
+      mark(PH_TEND_W); launch_tend_w(l2, nb2, TF_ALL, stream);
+      mark(PH_TEND_T); launch_tend_t(l3, nb3, TF_ZERO | TF_ADV, stream);
+      mark(PH_TEND_PH); launch_tend_ph(l3, nb3, TF_ZERO | TF_ADV, stream);
+      if (cfl_check) { mark(PH_CFL); launch_cfl_check(l3, nb3, stream); }
+      // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
+      mark(PH_SSP); launch_small_step_prep(l2, nb2, a, stream);
+      mark(PH_CPR0); launch_calc_p_rho(l3, nb3, StepArgs{rk_step, 0, 0, 0}, stream);
+      mark(PH_COEFW); launch_calc_coef_w(l2, nb2, a, fp64, stream);
+      {  // solve_em.F:1176-1264
+        JobList j;
+        j.f3(WRFGPU_RU_TEND, 'u'); j.f3(WRFGPU_RV_TEND, 'v'); j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p');
+        j.f3(WRFGPU_P, 'p'); j.f3(WRFGPU_T_1, 'p'); j.f3(WRFGPU_T_SAVE, 't');
+        j.f2(WRFGPU_MU_1, 't'); j.f2(WRFGPU_MU_2, 't'); j.f2(WRFGPU_MUDF, 't');
+        fill(j);
+      }
+      int nsmall_max = 0;
+      for (int m = 0; m < nmem; ++m) nsmall_max = std::max(nsmall_max, stage_of(hm[m], rk_step).nsmall);
+      for (int it = 1; it <= nsmall_max; ++it) {
+        StepArgs ai{rk_step, it, 0, 0};
+        mark(PH_AUV); launch_advance_uv(l3, nb3, ai, stream);
+        mark(PH_AMUT); launch_advance_mu_t(l2, nb2, ai, fp64, stream);
+        mark(PH_AW); launch_advance_w(l2, nb2, ai, fp64, stream);
+        mark(PH_SUMF); launch_sumflux_p_rho(l3, nb3, ai, true, stream);
+        JobList j;  // solve_em.F:1659-1716
+        j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_P, 'p');
+        j.f2(WRFGPU_MUTS, 't'); j.f2(WRFGPU_MU_2, 't'); j.f2(WRFGPU_MUDF, 't');
+        fill(j);
+      }
+      mark(PH_SSF); launch_small_step_finish(l2, nb2, a, stream);
+      if (rk_step == 3) {
+        JobList j;  // solve_em.F:1754-1800
+        j.f3(WRFGPU_RU_M, 'u'); j.f3(WRFGPU_RV_M, 'v'); j.f3(WRFGPU_WW_M, 'w');
+        j.f2(WRFGPU_MUT, 't'); j.f2(WRFGPU_MUTS, 't');
+        fill(j);
+        mark(PH_USPD); launch_update_scalar_pd(l3, nb3, a, stream);
+        JobList jo;
+        for (int s = 0; s < nsp_max; ++s) jo.sp(s, 1, 'p');
+        fill(jo);
+      }
+      for (int s = 0; s < nsp_max; ++s) {
+        StepArgs as{rk_step, 0, s, 0};
+        if (rk_step == 3) {
+          mark(PH_PD); launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, s, 0}, d_pd_scratch, stream);
+          mark(PH_ADVS); launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, s, 1}, stream);
+        } else {
+          mark(PH_ADVS); launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, s, 0}, stream);
+        }
+        mark(PH_UPDS); launch_update_scalar(l3, nb3, as, stream);
+      }
+      mark(PH_CPRP); launch_calc_p_rho_phi(l3, nb3, stream);
+      if (rk_step < 3) {
+        JobList j;  // rk_phys_bc_dry_2 + species (solve_em.F:3240-3330)
+        j.f3(WRFGPU_U_2, 'u'); j.f3(WRFGPU_V_2, 'v'); j.f3(WRFGPU_W_2, 'w'); j.f3(WRFGPU_T_2, 'p');
+        j.f3(WRFGPU_PH_2, 'w'); j.f2(WRFGPU_MU_2, 't');
+        for (int s = 0; s < nsp_max; ++s) j.sp(s, 0, 'p');
+        fill(j);
+      }
+    }
+    {  // set_phys_bc_dry_2 + species (solve_em.F:4439-4535)
+      JobList j;
+      j.f3(WRFGPU_U_1, 'u'); j.f3(WRFGPU_U_2, 'u'); j.f3(WRFGPU_V_1, 'v'); j.f3(WRFGPU_V_2, 'v');
+      j.f3(WRFGPU_W_1, 'w'); j.f3(WRFGPU_W_2, 'w'); j.f3(WRFGPU_T_1, 'p'); j.f3(WRFGPU_T_2, 'p');
+      j.f3(WRFGPU_PH_1, 'w'); j.f3(WRFGPU_PH_2, 'w'); j.f2(WRFGPU_MU_1, 't'); j.f2(WRFGPU_MU_2, 't');
+      for (int s = 0; s < nsp_max; ++s) j.sp(s, 0, 'p');
+      fill(j);
+    }
+    mark(PH_WSURF); launch_set_w_surface(l2, nb2, stream);
+    mark(PH_END);
+  }
+
+  int build_graph() {
+    if (gexec) return WRFGPU_OK;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step();
+    CK(cudaStreamEndCapture(stream, &graph));
+    CK(cudaGraphInstantiate(&gexec, graph, 0));
+    return WRFGPU_OK;
+  }
+
+  int step(int nsteps) {
+    if (flags & WRFGPU_FLAG_NO_GRAPH) {
+      for (int s = 0; s < nsteps; ++s) enqueue_step();
+    } else {
+      int rc = build_graph();
+      if (rc) return rc;
+      for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(gexec, stream));
+    }
+    CK(cudaGetLastError());
+    return WRFGPU_OK;
+  }
+
+  int run_routine(int routine, int rk_step, int iteration, int species) {
+    const Launch l2 = L2(), l3 = L3();
+    StepArgs a{rk_step, iteration, species, 0};
+    switch (routine) {
+      case 1: launch_rk_step_prep(l2, nb2, stream); break;
+      case 2:
+        launch_tend_u(l3, nb3, TF_ZERO, stream); launch_tend_v(l3, nb3, TF_ZERO, stream);
+        launch_tend_w(l2, nb2, TF_ZERO, stream); launch_tend_t(l3, nb3, TF_ZERO, stream);
+        launch_tend_ph(l3, nb3, TF_ZERO, stream);
+        break;
+      case 3: launch_tend_u(l3, nb3, TF_ADV, stream); break;
+      case 4: launch_tend_v(l3, nb3, TF_ADV, stream); break;
+      case 5: launch_tend_w(l2, nb2, TF_ADV, stream); break;
+      case 6: launch_tend_t(l3, nb3, TF_ADV, stream); break;
+      case 7: launch_tend_ph(l3, nb3, TF_ADV, stream); break;
+      case 8: launch_tend_u(l3, nb3, TF_PG, stream); launch_tend_v(l3, nb3, TF_PG, stream); break;
+      case 9: launch_tend_w(l2, nb2, TF_PG, stream); break;
+      case 10:
+        launch_tend_u(l3, nb3, TF_COR, stream); launch_tend_v(l3, nb3, TF_COR, stream);
+        launch_tend_w(l2, nb2, TF_COR, stream);
+        break;
+      case 11:
+        launch_tend_u(l3, nb3, TF_CURV, stream); launch_tend_v(l3, nb3, TF_CURV, stream);
+        launch_tend_w(l2, nb2, TF_CURV, stream);
+        break;
+      case 12: launch_small_step_prep(l2, nb2, a, stream); break;
+      case 13: launch_calc_p_rho(l3, nb3, a, stream); break;
+      case 14: launch_calc_coef_w(l2, nb2, a, fp64, stream); break;
+      case 15: launch_advance_uv(l3, nb3, a, stream); break;
+      case 16: launch_advance_mu_t(l2, nb2, a, fp64, stream); break;
+      case 17: launch_advance_w(l2, nb2, a, fp64, stream); break;
+      case 18: launch_sumflux(l3, nb3, a, stream); break;
+      case 19: launch_small_step_finish(l2, nb2, a, stream); break;
+      case 20: launch_update_scalar_pd(l3, nb3, a, stream); break;
+      case 21: launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, species, 0}, stream); break;
+      case 22: launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, species, 2}, d_pd_scratch, stream); break;
+      case 23: launch_update_scalar(l3, nb3, a, stream); break;
+      case 24: launch_calc_p_rho_phi(l3, nb3, stream); break;
+      case 25: launch_set_w_surface(l2, nb2, stream); break;
+      case 26:
+        launch_tend_u(l3, nb3, TF_ALL, stream); launch_tend_v(l3, nb3, TF_ALL, stream);
+        launch_tend_w(l2, nb2, TF_ALL, stream); launch_tend_t(l3, nb3, TF_ZERO | TF_ADV, stream);
+        launch_tend_ph(l3, nb3, TF_ZERO | TF_ADV, stream);
+        break;
+      default: return WRFGPU_E_ARG;
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    return WRFGPU_OK;
+  }
+};
+
+}  // namespace wrfgpu
+
+using wrfgpu::Ensemble;
+
+struct WrfGpuEnsemble { Ensemble e; };
+
+extern "C" {
+
+int wrfgpu_ensemble_create(const WrfGpuDomainDesc* descs, int n, int flags, WrfGpuEnsemble** out) {
+  if (!descs || n <= 0 || !out) return WRFGPU_E_ARG;
+  auto* h = new WrfGpuEnsemble();
+  int rc = h->e.init(descs, n, flags);
+  if (rc) { delete h; *out = nullptr; return rc; }
+  *out = h;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_ensemble_destroy(WrfGpuEnsemble* h) {
+  if (!h) return WRFGPU_E_ARG;
+  cudaStreamSynchronize(h->e.stream);
+  delete h;
+  return WRFGPU_OK;
+}
+
+long long wrfgpu_field_size(WrfGpuEnsemble* h, int member, int id) {
+  if (!h || member < 0 || member >= h->e.nmem) return 0;
+  size_t n = 0;
+  h->e.field_ptr(member, id, &n);
+  return (long long)n;
+}
+
+int wrfgpu_set_field_f32(WrfGpuEnsemble* h, int member, int id, const float* src, long long n) {
+  if (!h || member < 0 || member >= h->e.nmem || !src) return WRFGPU_E_ARG;
+  size_t cnt = 0;
+  float* p = h->e.field_ptr(member, id, &cnt);
+  if (!p || (long long)cnt != n) return WRFGPU_E_ARG;
+  if (cudaMemcpyAsync(p, src, cnt * 4, cudaMemcpyHostToDevice, h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_get_field_f32(WrfGpuEnsemble* h, int member, int id, float* dst, long long n) {
+  if (!h || member < 0 || member >= h->e.nmem || !dst) return WRFGPU_E_ARG;
+  size_t cnt = 0;
+  float* p = h->e.field_ptr(member, id, &cnt);
+  if (!p || (long long)cnt != n) return WRFGPU_E_ARG;
+  if (cudaMemcpyAsync(dst, p, cnt * 4, cudaMemcpyDeviceToHost, h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_set_field(WrfGpuEnsemble* h, int member, int id, const double* src, long long n) {
+  if (!src || n < 0) return WRFGPU_E_ARG;
+  std::vector<float> tmp((size_t)n);
+  for (long long i = 0; i < n; ++i) tmp[(size_t)i] = (float)src[i];
+  return wrfgpu_set_field_f32(h, member, id, tmp.data(), n);
+}
+
+int wrfgpu_get_field(WrfGpuEnsemble* h, int member, int id, double* dst, long long n) {
+  if (!dst || n < 0) return WRFGPU_E_ARG;
+  std::vector<float> tmp((size_t)n);
+  int rc = wrfgpu_get_field_f32(h, member, id, tmp.data(), n);
+  if (rc) return rc;
+  for (long long i = 0; i < n; ++i) dst[i] = (double)tmp[(size_t)i];
+  return WRFGPU_OK;
+}
+
+int wrfgpu_step(WrfGpuEnsemble* h, int nsteps) {
+  if (!h || nsteps < 0) return WRFGPU_E_ARG;
+  return h->e.step(nsteps);
+}
+
+int wrfgpu_sync(WrfGpuEnsemble* h) {
+  if (!h) return WRFGPU_E_ARG;
+  return cudaStreamSynchronize(h->e.stream) == cudaSuccess ? WRFGPU_OK : WRFGPU_E_CUDA;
+}
+
+int wrfgpu_time_steps(WrfGpuEnsemble* h, int nsteps, float* ms) {
+  if (!h || nsteps < 0 || !ms) return WRFGPU_E_ARG;
+  Ensemble& e = h->e;
+  if (!(e.flags & WRFGPU_FLAG_NO_GRAPH)) { int rc = e.build_graph(); if (rc) return rc; }
+  if (cudaEventRecord(e.ev0, e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  int rc = e.step(nsteps);
+  if (rc) return rc;
+  if (cudaEventRecord(e.ev1, e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaEventSynchronize(e.ev1) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaEventElapsedTime(ms, e.ev0, e.ev1) != cudaSuccess) return WRFGPU_E_CUDA;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_run_routine(WrfGpuEnsemble* h, int routine, int rk_step, int iteration, int species) {
+  if (!h || rk_step < 1 || rk_step > 3) return WRFGPU_E_ARG;
+  return h->e.run_routine(routine, rk_step, iteration, species);
+}
+
+int wrfgpu_fill_halo(WrfGpuEnsemble* h, int id, char var) {
+  if (!h) return WRFGPU_E_ARG;
+  Ensemble::JobList j;
+  if (id >= 0 && id < WRFGPU_N3D) j.f3(id, var);
+  else if (id >= WRFGPU_F2D_BASE && id < WRFGPU_F2D_END) j.f2(id, var);
+  else if (id >= WRFGPU_SPECIES_BASE) j.sp((id - WRFGPU_SPECIES_BASE) / 2, (id - WRFGPU_SPECIES_BASE) % 2, var);
+  else return WRFGPU_E_ARG;
+  h->e.fill(j);
+  if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_status(WrfGpuEnsemble* h, int member, unsigned* err_bits, double* max_vert_cfl, double* max_horiz_cfl) {
+  if (!h || member < 0 || member >= h->e.nmem) return WRFGPU_E_ARG;
+  Ensemble& e = h->e;
+  unsigned eb = 0;
+  float c[2] = {0, 0};
+  if (cudaStreamSynchronize(e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaMemcpy(&eb, e.d_err + member, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaMemcpy(c, e.d_cfl + 2 * member, sizeof(float) * 2, cudaMemcpyDeviceToHost) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (err_bits) *err_bits = eb;
+  if (max_vert_cfl) *max_vert_cfl = c[0];
+  if (max_horiz_cfl) *max_horiz_cfl = c[1];
+  if (eb & wrfgpu::ERR_NONFINITE) return WRFGPU_E_NONFINITE;
+  if (eb & wrfgpu::ERR_CFL) return WRFGPU_E_CFL;
+  if (eb & wrfgpu::ERR_TIMEOUT) return WRFGPU_E_TIMEOUT;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_clear_status(WrfGpuEnsemble* h) {
+  if (!h) return WRFGPU_E_ARG;
+  Ensemble& e = h->e;
+  if (cudaMemsetAsync(e.d_err, 0, sizeof(unsigned) * e.nmem, e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaMemsetAsync(e.d_cfl, 0, sizeof(float) * 2 * e.nmem, e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  return cudaStreamSynchronize(e.stream) == cudaSuccess ? WRFGPU_OK : WRFGPU_E_CUDA;
+}
+
+int wrfgpu_set_cfl_limit(WrfGpuEnsemble* h, double limit) {
+  if (!h) return WRFGPU_E_ARG;
+  Ensemble& e = h->e;
+  for (auto& M : e.hm) M.cfl_limit = (float)limit;
+  if (cudaMemcpy(e.d_mems, e.hm.data(), sizeof(wrfgpu::Mem) * e.nmem, cudaMemcpyHostToDevice) != cudaSuccess)
+    return WRFGPU_E_CUDA;
+  return WRFGPU_OK;
+}
+
+int wrfgpu_num_sound_steps(WrfGpuEnsemble* h, int member) {
+  if (!h || member < 0 || member >= h->e.nmem) return WRFGPU_E_ARG;
+  return h->e.hm[member].ns_total;
+}
+
+long long wrfgpu_device_bytes(WrfGpuEnsemble* h) { return h ? (long long)h->e.pool_bytes : 0; }
+
+int wrfgpu_kernel_launches_per_step(WrfGpuEnsemble* h) {
+  if (!h) return WRFGPU_E_ARG;
+  cudaGraph_t g = nullptr;
+  Ensemble& e = h->e;
+  if (e.build_graph()) return WRFGPU_E_CUDA;
+  size_t n = 0;
+  if (cudaGraphGetNodes(e.graph, nullptr, &n) != cudaSuccess) return WRFGPU_E_CUDA;
+  (void)g;
+  return (int)n;
+}
+
+int wrfgpu_profile_phases(WrfGpuEnsemble* h, int nsteps, double* ms_out, int* launches_out, int nphase) {
+  if (!h || nsteps <= 0 || !ms_out || nphase < (int)wrfgpu::NPHASE - 1) return WRFGPU_E_ARG;
+  Ensemble& e = h->e;
+  std::vector<std::pair<int, cudaEvent_t>> marks;
+  for (int p = 0; p < nphase; ++p) { ms_out[p] = 0.0; if (launches_out) launches_out[p] = 0; }
+  e.prof = &marks;
+  for (int s = 0; s < nsteps; ++s) e.enqueue_step();
+  e.prof = nullptr;
+  if (cudaStreamSynchronize(e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  for (size_t q = 0; q + 1 < marks.size(); ++q) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, marks[q].second, marks[q + 1].second);
+    int ph = marks[q].first;
+    if (ph == wrfgpu::PH_END) continue;
+    ms_out[ph] += ms;
+    if (launches_out) launches_out[ph] += 1;
+  }
+  for (auto& m : marks) cudaEventDestroy(m.second);
+  return (int)wrfgpu::NPHASE - 1;
+}
+
+const char* wrfgpu_phase_name(int phase) {
+  if (phase < 0 || phase >= (int)wrfgpu::NPHASE) return "";
+  return wrfgpu::PHASE_NAMES[phase];
+}
+
+const char* wrfgpu_version(void) { return "wrf-gb300 dyn 0.1 (sm_103a)"; }
+
+}  // extern "C"

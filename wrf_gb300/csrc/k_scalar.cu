@@ -1,0 +1,346 @@
+// Scalar transport and diagnosis kernels:
+//   rk_update_scalar_pd  dyn_em/module_em.F:1803-1916 (physics tendency 0)
+//   advect_scalar        dyn_em/module_advect_em.F:3394-3650, :4306-4333
+//   advect_scalar_pd     dyn_em/module_advect_em.F:6505-6779, :7595-7645, limiter :7681-7781,
+//                        divergence :7783-7883 — two passes: (1) per-cell limiter scale of
+//                        every cell of the tile and its 1-cell halo into a scratch array,
+//                        (2) per-cell divergence of the face fluxes, each face scaled by its
+//                        upwind cell's factor (a face is only ever modified by its upwind
+//                        cell, so the result does not depend on the reference's loop order)
+//   rk_update_scalar     dyn_em/module_em.F:1587-1799
+//   calc_p_rho_phi       dyn_em/module_big_step_utilities_em.F:953-1226 (non-hydrostatic)
+//   set_w_surface        dyn_em/module_bc_em.F:1196-1295
+// Roofline: HBM-bound; the limiter pass reads the 5 transport arrays twice
+// (scale pass and divergence pass) plus the scale scratch.
+#include "common.cuh"
+#include "kernels.h"
+#include "ffmath.h"
+
+namespace wrfgpu {
+
+__device__ __forceinline__ bool mass_pt(const Mem& m, int i, int j) {
+  return i >= m.its && i <= min(m.ite, m.ide - 1) && j >= m.jts && j <= min(m.jte, m.jde - 1);
+}
+
+// ------------------------------------------------------------ rk_update_scalar_pd
+__global__ void __launch_bounds__(BX* BY) k_update_scalar_pd(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  F2 mu1 = f2(m, WRFGPU_MU_1), mub = f2(m, WRFGPU_MUB);
+  const float muold = mu1(i, j) + mub(i, j);
+  const float munew = mu1(i, j) + mub(i, j);
+  const float tendency = 0.f;
+  for (int s = 0; s < m.nsp; ++s) {
+    int adv = s < m.n_moist ? m.cf.moist_adv_opt : m.cf.scalar_adv_opt;
+    if (adv != 1) continue;
+    F3 q = f3p(m, m.qo[s]);
+    q(i, k, j) = ((c1(k) * muold + c2(k)) * q(i, k, j) + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+  }
+}
+
+// ------------------------------------------------------------ advect_scalar (+ zero_tend)
+__device__ __forceinline__ bool pd_applies(const Mem& m, int species, int rk_step) {
+  int adv = species < m.n_moist ? m.cf.moist_adv_opt : m.cf.scalar_adv_opt;
+  return rk_step == m.cf.rk_ord && adv == 1;
+}
+
+// mode 0: always; mode 1: skip members whose species is advected by the
+// positive-definite scheme at this stage (module_em.F:1265-1280).
+__global__ void __launch_bounds__(BX* BY) k_advect_scalar(Launch L, int species, int rk_step, int mode) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (species >= m.nsp) return;
+  if (mode == 1 && pd_applies(m, species, rk_step)) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  F3 tend = f3(m, WRFGPU_ADVECT_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
+  const int ktf = min(m.kte, m.kde - 1);
+  if (!(mass_pt(m, i, j) && k >= m.kts && k <= ktf)) {
+    if (in_zero) tend(i, k, j) = 0.f;
+    return;
+  }
+  F3 fld = f3p(m, m.q[species]), ru = f3(m, WRFGPU_RU_M), rv = f3(m, WRFGPU_RV_M), rom = f3(m, WRFGPU_WW_M);
+  F2 msftx = f2(m, WRFGPU_MSFTX);
+  F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+  float t = 0.f;
+  auto fy = [&](int jj) {
+    float vel = rv(i, k, jj);
+    return vel * flux5(fld(i, k, jj - 3), fld(i, k, jj - 2), fld(i, k, jj - 1), fld(i, k, jj), fld(i, k, jj + 1), fld(i, k, jj + 2), vel);
+  };
+  t = t - msftx(i, j) * m.rdy * (fy(j + 1) - fy(j));
+  auto fx = [&](int ii) {
+    float vel = ru(ii, k, j);
+    return vel * flux5(fld(ii - 3, k, j), fld(ii - 2, k, j), fld(ii - 1, k, j), fld(ii, k, j), fld(ii + 1, k, j), fld(ii + 2, k, j), vel);
+  };
+  t = t - msftx(i, j) * m.rdx * (fx(i + 1) - fx(i));
+  auto vf = [&](int kk) -> float {
+    if (kk == m.kts || kk == m.kte) return 0.f;
+    if (kk == m.kts + 1 || kk == ktf) return rom(i, kk, j) * (fzm(kk) * fld(i, kk, j) + fzp(kk) * fld(i, kk - 1, j));
+    float vel = rom(i, kk, j);
+    return vel * flux3(fld(i, kk - 2, j), fld(i, kk - 1, j), fld(i, kk, j), fld(i, kk + 1, j), -vel);
+  };
+  t = t - rdzw(k) * (vf(k + 1) - vf(k));
+  tend(i, k, j) = t;
+}
+
+// ------------------------------------------------------------ advect_scalar_pd
+struct PDCtx {
+  F3 f, fo, ru, rv, rom;
+  F2 mut, mub, mu_old, msftx, msfty;
+  F1 c1, c2, fzm, fzp, rdzw;
+  float rdx, rdy, dt;
+  int kts, ktf, kde;
+};
+__device__ __forceinline__ PDCtx pd_ctx(const Mem& m, int species, float dt) {
+  PDCtx c{f3p(m, m.q[species]), f3p(m, m.qo[species]), f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M),
+          f2(m, WRFGPU_MUTS), f2(m, WRFGPU_MUB), f2(m, WRFGPU_MU_1), f2(m, WRFGPU_MSFTX), f2(m, WRFGPU_MSFTY),
+          f1(m, WRFGPU_C1H), f1(m, WRFGPU_C2H), f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW),
+          m.rdx, m.rdy, dt, m.kts, min(m.kte, m.kde - 1), m.kde};
+  return c;
+}
+// face fluxes: *hi = high-order minus upwind, *lo = upwind
+__device__ __forceinline__ void pd_fx(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
+  float dx = 2.f / (c.msfty(i, j) + c.msfty(i - 1, j)) / c.rdx;
+  float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i - 1, j) + c.c2(k)));
+  float vel = c.ru(i, k, j);
+  float cr = vel * c.dt / dx / mu;
+  float l = mu * (dx / c.dt) * flux_upwind(c.fo(i - 1, k, j), c.fo(i, k, j), cr);
+  float h = vel * pflux5(c.f(i - 3, k, j), c.f(i - 2, k, j), c.f(i - 1, k, j), c.f(i, k, j), c.f(i + 1, k, j), c.f(i + 2, k, j), vel);
+  *lo = l; *hi = h - l;
+}
+__device__ __forceinline__ void pd_fy(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
+  float dy = 2.f / (c.msftx(i, j) + c.msftx(i, j - 1)) / c.rdy;
+  float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j - 1) + c.c2(k)));
+  float vel = c.rv(i, k, j);
+  float cr = vel * c.dt / dy / mu;
+  float l = mu * (dy / c.dt) * flux_upwind(c.fo(i, k, j - 1), c.fo(i, k, j), cr);
+  float h = vel * pflux5(c.f(i, k, j - 3), c.f(i, k, j - 2), c.f(i, k, j - 1), c.f(i, k, j), c.f(i, k, j + 1), c.f(i, k, j + 2), vel);
+  *lo = l; *hi = h - l;
+}
+__device__ __forceinline__ void pd_fz(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
+  if (k == 1 || k == c.kde) { *hi = 0.f; *lo = 0.f; return; }
+  float dz = 2.f / (c.rdzw(k) + c.rdzw(k - 1));
+  float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j) + c.c2(k)));
+  float vel = c.rom(i, k, j);
+  float cr = vel * c.dt / dz / mu;
+  float l = mu * (dz / c.dt) * flux_upwind(c.fo(i, k - 1, j), c.fo(i, k, j), cr);
+  float h;
+  if (k == c.kts + 1 || k == c.ktf) h = c.rom(i, k, j) * (c.fzm(k) * c.f(i, k, j) + c.fzp(k) * c.f(i, k - 1, j));
+  else h = vel * pflux3(c.f(i, k - 2, j), c.f(i, k - 1, j), c.f(i, k, j), c.f(i, k + 1, j), -vel);
+  *lo = l; *hi = h - l;
+}
+
+// Pass 1: limiter scale of each cell of the tile + 1-cell halo (-1: not limited).
+// mode 0: only members whose species uses the positive-definite scheme; mode 2: always.
+__global__ void __launch_bounds__(BX* BY) k_pd_scale(Launch L, int species, int rk_step, int mode, float* const* scratch) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (species >= m.nsp) return;
+  if (mode == 0 && !pd_applies(m, species, rk_step)) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
+  if (i < m.its - 1 || i > itf + 1 || j < m.jts - 1 || j > jtf + 1 || k < m.kts || k > ktf) return;
+  const Stage st = stage_of(m, rk_step);
+  const PDCtx c = pd_ctx(m, species, st.dt_rk);
+  float hx0, lx0, hx1, lx1, hy0, ly0, hy1, ly1, hz0, lz0, hz1, lz1;
+  pd_fx(c, i, k, j, &hx0, &lx0); pd_fx(c, i + 1, k, j, &hx1, &lx1);
+  pd_fy(c, i, k, j, &hy0, &ly0); pd_fy(c, i, k, j + 1, &hy1, &ly1);
+  pd_fz(c, i, k, j, &hz0, &lz0); pd_fz(c, i, k + 1, j, &hz1, &lz1);
+  const float mx = c.msftx(i, j), my = c.msfty(i, j), dt = c.dt;
+  float ph_low = ((c.c1(k) * c.mub(i, j) + c.c2(k)) + (c.c1(k) * c.mu_old(i, j))) * c.fo(i, k, j) -
+                 dt * (mx * my * (c.rdx * (lx1 - lx0) + c.rdy * (ly1 - ly0)) + my * c.rdzw(k) * (lz1 - lz0));
+  float flux_out = dt * ((mx * my) * (c.rdx * (fmaxf_f(0.f, hx1) - fminf_f(0.f, hx0)) +
+                                      c.rdy * (fmaxf_f(0.f, hy1) - fminf_f(0.f, hy0))) +
+                         my * c.rdzw(k) * (fminf_f(0.f, hz1) - fmaxf_f(0.f, hz0)));
+  float s = -1.f;
+  if (flux_out > ph_low) s = fmaxf_f(0.f, ph_low / (flux_out + 1.e-20f));
+  f3p(m, scratch[bp.m])(i, k, j) = s;
+}
+
+// Pass 2: divergence of the limited fluxes (z, then x, then y) into advect_tend.
+__global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int rk_step, int mode, float* const* scratch) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (species >= m.nsp) return;
+  if (mode == 0 && !pd_applies(m, species, rk_step)) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  F3 tend = f3(m, WRFGPU_ADVECT_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
+  const int ktf = min(m.kte, m.kde - 1);
+  if (!(mass_pt(m, i, j) && k >= m.kts && k <= ktf)) {
+    if (in_zero) tend(i, k, j) = 0.f;
+    return;
+  }
+  const Stage st = stage_of(m, rk_step);
+  const PDCtx c = pd_ctx(m, species, st.dt_rk);
+  F3 sc = f3p(m, scratch[bp.m]);
+  auto lim = [&](float v, int ci, int ck, int cj) {
+    float s = sc(ci, ck, cj);
+    return s >= 0.f ? s * v : v;
+  };
+  float hx0, lx0, hx1, lx1, hy0, ly0, hy1, ly1, hz0, lz0, hz1, lz1;
+  pd_fx(c, i, k, j, &hx0, &lx0); pd_fx(c, i + 1, k, j, &hx1, &lx1);
+  pd_fy(c, i, k, j, &hy0, &ly0); pd_fy(c, i, k, j + 1, &hy1, &ly1);
+  pd_fz(c, i, k, j, &hz0, &lz0); pd_fz(c, i, k + 1, j, &hz1, &lz1);
+  // face (i): left cell i-1 owns positive flux, cell i owns negative flux
+  if (hx0 > 0.f) hx0 = lim(hx0, i - 1, k, j); else if (hx0 < 0.f) hx0 = lim(hx0, i, k, j);
+  if (hx1 > 0.f) hx1 = lim(hx1, i, k, j); else if (hx1 < 0.f) hx1 = lim(hx1, i + 1, k, j);
+  if (hy0 > 0.f) hy0 = lim(hy0, i, k, j - 1); else if (hy0 < 0.f) hy0 = lim(hy0, i, k, j);
+  if (hy1 > 0.f) hy1 = lim(hy1, i, k, j); else if (hy1 < 0.f) hy1 = lim(hy1, i, k, j + 1);
+  // vertical face k: the cell below (k-1) owns negative flux, the cell above (k) positive flux
+  if (k > 1) { if (hz0 < 0.f) hz0 = lim(hz0, i, k - 1, j); else if (hz0 > 0.f) hz0 = lim(hz0, i, k, j); }
+  if (k + 1 < c.kde) { if (hz1 < 0.f) hz1 = lim(hz1, i, k, j); else if (hz1 > 0.f) hz1 = lim(hz1, i, k + 1, j); }
+  const float mx = c.msftx(i, j);
+  float t = 0.f;
+  t = t - c.rdzw(k) * (hz1 - hz0 + lz1 - lz0);
+  t = t - mx * (c.rdx * (hx1 - hx0 + lx1 - lx0));
+  t = t - mx * (c.rdy * (hy1 - hy0 + ly1 - ly0));
+  tend(i, k, j) = t;
+}
+
+// ------------------------------------------------------------ rk_update_scalar
+__global__ void __launch_bounds__(BX* BY) k_update_scalar(Launch L, int species, int rk_step) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (species >= m.nsp) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  F3 s1 = f3p(m, m.qo[species]), s2 = f3p(m, m.q[species]), at = f3(m, WRFGPU_ADVECT_TEND);
+  F2 msfty = f2(m, WRFGPU_MSFTY), mu_old = f2(m, WRFGPU_MU_1), mu_new = f2(m, WRFGPU_MU_2), mub = f2(m, WRFGPU_MUB);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  const float muold = mu_old(i, j) + mub(i, j), munew = mu_new(i, j) + mub(i, j);
+  const float tendency = at(i, k, j) * msfty(i, j);
+  float q1;
+  if (rk_step == 1) { q1 = s2(i, k, j); s1(i, k, j) = q1; }
+  else q1 = s1(i, k, j);
+  s2(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+}
+
+// ------------------------------------------------------------ calc_p_rho_phi
+__global__ void __launch_bounds__(BX* BY) k_calc_p_rho_phi(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  F3 al = f3(m, WRFGPU_AL), alb = f3(m, WRFGPU_ALB), ph = f3(m, WRFGPU_PH_2), phb = f3(m, WRFGPU_PHB),
+     p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB), t = f3(m, WRFGPU_T_2);
+  F2 mu = f2(m, WRFGPU_MU_2), muts = f2(m, WRFGPU_MUTS);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), c3h = f1(m, WRFGPU_C3H), c4h = f1(m, WRFGPU_C4H),
+     c3f = f1(m, WRFGPU_C3F), c4f = f1(m, WRFGPU_C4F), rdnw = f1(m, WRFGPU_RDNW);
+  const float ptop = m.p_top;
+  float alv;
+  if (m.cf.hypsometric_opt == 1) {
+    alv = -1.f / (c1(k) * muts(i, j) + c2(k)) * (alb(i, k, j) * (c1(k) * mu(i, j)) + rdnw(k) * (ph(i, k + 1, j) - ph(i, k, j)));
+  } else {
+    float pfu = c3f(k + 1) * muts(i, j) + c4f(k + 1) + ptop;
+    float pfd = c3f(k) * muts(i, j) + c4f(k) + ptop;
+    float phm = c3h(k) * muts(i, j) + c4h(k) + ptop;
+    alv = (ph(i, k + 1, j) - ph(i, k, j) + phb(i, k + 1, j) - phb(i, k, j)) / phm / wrfgpu_ff::logf_cr(pfd / pfu) - alb(i, k, j);
+  }
+  al(i, k, j) = alv;
+  float temp;
+  if (m.cf.use_theta_m == 1) {
+    temp = (R_D * (T0 + t(i, k, j))) / (P0 * (alv + alb(i, k, j)));
+  } else {
+    float qvf = 1.f + (461.6f / 287.f) * f3p(m, m.q[0])(i, k, j);
+    temp = (R_D * (T0 + t(i, k, j)) * qvf) / (P0 * (alv + alb(i, k, j)));
+  }
+  float pv = wrfgpu_ff::powf_cr(temp, CPOVCV);
+  p(i, k, j) = pv * P0 - pb(i, k, j);
+}
+
+// ------------------------------------------------------------ set_w_surface
+__global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j;
+  if (!mass_pt(m, i, j)) return;
+  const bool px = m.cf.periodic_x, py = m.cf.periodic_y;
+  int jm1_limit = px || py ? m.jds : m.jds, jp1_limit = m.jde - 1, im1_limit = m.ids, ip1_limit = m.ide - 1;
+  if (px) { im1_limit = m.ids - 1; ip1_limit = m.ide; }
+  if (py) { jm1_limit = m.jds - 1; jp1_limit = m.jde; }
+  const int jm1 = max(j - 1, jm1_limit), jp1 = min(j + 1, jp1_limit), im1 = max(i - 1, im1_limit), ip1 = min(i + 1, ip1_limit);
+  F3 w = f3(m, WRFGPU_W_2), u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
+  F2 ht = f2(m, WRFGPU_HT), msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
+  const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
+  w(i, 1, j) = msfty(i, j) * .5f * m.rdy *
+                   ((ht(i, jp1) - ht(i, j)) * (cf1 * v(i, 1, j + 1) + cf2 * v(i, 2, j + 1) + cf3 * v(i, 3, j + 1)) +
+                    (ht(i, j) - ht(i, jm1)) * (cf1 * v(i, 1, j) + cf2 * v(i, 2, j) + cf3 * v(i, 3, j))) +
+               msftx(i, j) * .5f * m.rdx *
+                   ((ht(ip1, j) - ht(i, j)) * (cf1 * u(i + 1, 1, j) + cf2 * u(i + 1, 2, j) + cf3 * u(i + 1, 3, j)) +
+                    (ht(i, j) - ht(im1, j)) * (cf1 * u(i, 1, j) + cf2 * u(i, 2, j) + cf3 * u(i, 3, j)));
+}
+
+// ------------------------------------------------------------ w_damp CFL diagnostics + health
+// module_big_step_utilities_em.F:2503-2712 (w_damping = 0: diagnostics only).
+__global__ void __launch_bounds__(BX* BY) k_cfl_check(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = L.mem[bp.m];
+  float vmax = 0.f, hmax = 0.f;
+  bool bad = false;
+  if (bp.valid && mass_pt(m, bp.i, bp.j) && bp.k >= 2 && bp.k <= m.kde - 1) {
+    const int i = bp.i, j = bp.j, k = bp.k;
+    F3 ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), w = f3(m, WRFGPU_W_2), t = f3(m, WRFGPU_T_2);
+    F2 mut = f2(m, WRFGPU_MUT), msfux = f2(m, WRFGPU_MSFUX), msfvy = f2(m, WRFGPU_MSFVY);
+    F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), rdnw = f1(m, WRFGPU_RDNW);
+    float vc = fabsf(ww(i, k, j) / (c1f(k) * mut(i, j) + c2f(k)) * rdnw(k) * m.dt);
+    float hc = fmaxf_f(fabsf(u(i, k, j) * m.rdx * msfux(i, j) * m.dt), fabsf(v(i, k, j) * m.rdy * msfvy(i, j) * m.dt));
+    bad = !isfinite(vc) || !isfinite(hc) || !isfinite(w(i, k, j)) || !isfinite(t(i, k, j));
+    vmax = isfinite(vc) ? vc : 0.f;
+    hmax = isfinite(hc) ? hc : 0.f;
+  }
+  // block max (all members of a block share one member)
+  __shared__ float sv[BX * BY], sh[BX * BY];
+  __shared__ int sb;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if (tid == 0) sb = 0;
+  sv[tid] = vmax; sh[tid] = hmax;
+  __syncthreads();
+  if (bad) atomicOr(&sb, 1);
+  for (int s = (BX * BY) / 2; s > 0; s >>= 1) {
+    if (tid < s) { sv[tid] = fmaxf_f(sv[tid], sv[tid + s]); sh[tid] = fmaxf_f(sh[tid], sh[tid + s]); }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (m.cfl_out) {
+      atomicMax((unsigned*)&m.cfl_out[0], __float_as_uint(sv[0]));
+      atomicMax((unsigned*)&m.cfl_out[1], __float_as_uint(sh[0]));
+    }
+    unsigned bits = 0;
+    if (sb) bits |= ERR_NONFINITE;
+    if (m.cfl_limit > 0.f && sv[0] > m.cfl_limit) bits |= ERR_CFL;
+    if (bits) raise_err(m, bits);
+  }
+}
+
+// ------------------------------------------------------------ launchers
+void launch_update_scalar_pd(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_update_scalar_pd<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+}
+void launch_advect_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_advect_scalar<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags);
+}
+void launch_advect_scalar_pd2(const Launch& L, int nb, StepArgs a, float* const* d_scratch, cudaStream_t s) {
+  k_pd_scale<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags, d_scratch);
+  k_pd_tend<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags, d_scratch);
+}
+void launch_update_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_update_scalar<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step);
+}
+void launch_calc_p_rho_phi(const Launch& L, int nb, cudaStream_t s) { k_calc_p_rho_phi<<<nb, dim3(BX, BY), 0, s>>>(L); }
+void launch_set_w_surface(const Launch& L, int nb, cudaStream_t s) { k_set_w_surface<<<nb, dim3(BX, BY), 0, s>>>(L); }
+void launch_cfl_check(const Launch& L, int nb, cudaStream_t s) { k_cfl_check<<<nb, dim3(BX, BY), 0, s>>>(L); }
+
+}  // namespace wrfgpu

@@ -1,0 +1,607 @@
+// Acoustic (small) step kernels: dyn_em/module_small_step_em.F
+//   small_step_prep   :16-290   column kernel (2-D mass bookkeeping + 3-D recoupling)
+//   calc_p_rho        :438-568  point kernel
+//   calc_coef_w       :570-652  column kernel (tridiagonal coefficients)
+//   advance_uv        :654-967  point kernel
+//   advance_mu_t      :969-1175 column kernel (column mass divergence, omega recursion, theta)
+//   advance_w         :1178-1469 column kernel (explicit w + Thomas solve + ph update)
+//   sumflux           :1473-1633 point kernel (fused with calc_p_rho of the same tile loop)
+//   small_step_finish :295-434 with calc_mu_uv_1 (module_big_step_utilities_em.F:184-326)
+// Column recursions are templated on their accumulation type RC: float in
+// the plain form (the reference's REAL), double in the mixed-precision form
+// (FP64 column sums, omega recursion, tridiagonal coefficients and solve).
+// Roofline: HBM-bound; advance_w reads ~20 arrays per cell and is the
+// largest acoustic kernel.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wrfgpu {
+
+constexpr int KMAX = 128;  // column scratch (kde <= KMAX, checked at domain creation)
+
+// ------------------------------------------------------------ small_step_prep
+__global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j;
+  const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
+  const int k_start = m.kts, k_end = min(m.kte, m.kde - 1), i_endu = m.ite, j_endv = m.jte, kde = m.kde;
+  if (i < i_start || i > i_endu || j < j_start || j > j_endv) return;
+  const bool mass = i <= i_end && j <= j_end, upt = i <= i_endu && j <= j_end, vpt = i <= i_end && j <= j_endv;
+  F2 mub = f2(m, WRFGPU_MUB), MU_1 = f2(m, WRFGPU_MU_1), MU_2 = f2(m, WRFGPU_MU_2), MUU = f2(m, WRFGPU_MUU),
+     MUUS = f2(m, WRFGPU_MUUS), MUV = f2(m, WRFGPU_MUV), MUVS = f2(m, WRFGPU_MUVS), mut = f2(m, WRFGPU_MUT),
+     MUTS = f2(m, WRFGPU_MUTS), MUDF = f2(m, WRFGPU_MUDF), MU_SAVE = f2(m, WRFGPU_MU_SAVE),
+     msfuy = f2(m, WRFGPU_MSFUY), msfvx_inv = f2(m, WRFGPU_MSFVX_INV), msfty = f2(m, WRFGPU_MSFTY);
+  F3 u_1 = f3(m, WRFGPU_U_1), u_2 = f3(m, WRFGPU_U_2), v_1 = f3(m, WRFGPU_V_1), v_2 = f3(m, WRFGPU_V_2),
+     w_1 = f3(m, WRFGPU_W_1), w_2 = f3(m, WRFGPU_W_2), t_1 = f3(m, WRFGPU_T_1), t_2 = f3(m, WRFGPU_T_2),
+     ph_1 = f3(m, WRFGPU_PH_1), ph_2 = f3(m, WRFGPU_PH_2), u_save = f3(m, WRFGPU_U_SAVE),
+     v_save = f3(m, WRFGPU_V_SAVE), w_save = f3(m, WRFGPU_W_SAVE), t_save = f3(m, WRFGPU_T_SAVE),
+     ph_save = f3(m, WRFGPU_PH_SAVE), ww = f3(m, WRFGPU_WW), ww_save = f3(m, WRFGPU_WW1), c2a = f3(m, WRFGPU_C2A),
+     pb = f3(m, WRFGPU_PB), p = f3(m, WRFGPU_P), alt = f3(m, WRFGPU_ALT);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+  float muts = 0.f, muus = 0.f, muvs = 0.f;
+  if (rk_step == 1) {
+    if (mass) { MU_1(i, j) = MU_2(i, j); MUDF(i, j) = 0.f; }
+    if (upt) for (int k = k_start; k <= k_end; ++k) u_1(i, k, j) = u_2(i, k, j);
+    if (vpt) for (int k = k_start; k <= k_end; ++k) v_1(i, k, j) = v_2(i, k, j);
+    if (mass) {
+      for (int k = k_start; k <= k_end; ++k) t_1(i, k, j) = t_2(i, k, j);
+      for (int k = k_start; k <= min(kde, m.kte); ++k) { w_1(i, k, j) = w_2(i, k, j); ph_1(i, k, j) = ph_2(i, k, j); }
+      muts = mub(i, j) + MU_2(i, j); MUTS(i, j) = muts;
+    }
+    if (upt) { muus = MUU(i, j); MUUS(i, j) = muus; }
+    if (vpt) { muvs = MUV(i, j); MUVS(i, j) = muvs; }
+    if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = 0.f; }
+  } else {
+    if (mass) { muts = mub(i, j) + MU_1(i, j); MUTS(i, j) = muts; }
+    if (upt) { muus = 0.5f * (mub(i, j) + MU_1(i, j) + mub(i - 1, j) + MU_1(i - 1, j)); MUUS(i, j) = muus; }
+    if (vpt) { muvs = 0.5f * (mub(i, j) + MU_1(i, j) + mub(i, j - 1) + MU_1(i, j - 1)); MUVS(i, j) = muvs; }
+    if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = MU_1(i, j) - MU_2(i, j); }
+  }
+  if (mass) {
+    for (int k = k_start; k <= k_end; ++k) c2a(i, k, j) = CPOVCV * (pb(i, k, j) + p(i, k, j)) / alt(i, k, j);
+  }
+  if (upt) {
+    const float muu = MUU(i, j), my = msfuy(i, j);
+    for (int k = k_start; k <= k_end; ++k) {
+      float u2 = u_2(i, k, j);
+      u_save(i, k, j) = u2;
+      u_2(i, k, j) = ((c1h(k) * muus + c2h(k)) * u_1(i, k, j) - (c1h(k) * muu + c2h(k)) * u2) / my;
+    }
+  }
+  if (vpt) {
+    const float muv = MUV(i, j), mxi = msfvx_inv(i, j);
+    for (int k = k_start; k <= k_end; ++k) {
+      float v2 = v_2(i, k, j);
+      v_save(i, k, j) = v2;
+      v_2(i, k, j) = ((c1h(k) * muvs + c2h(k)) * v_1(i, k, j) - (c1h(k) * muv + c2h(k)) * v2) * mxi;
+    }
+  }
+  if (mass) {
+    const float mt = mut(i, j), my = msfty(i, j);
+    for (int k = k_start; k <= k_end; ++k) {
+      float t2 = t_2(i, k, j);
+      t_save(i, k, j) = t2;
+      t_2(i, k, j) = (c1h(k) * muts + c2h(k)) * t_1(i, k, j) - (c1h(k) * mt + c2h(k)) * t2;
+    }
+    for (int k = k_start; k <= kde; ++k) {
+      float w2 = w_2(i, k, j);
+      w_save(i, k, j) = w2;
+      w_2(i, k, j) = ((c1f(k) * muts + c2f(k)) * w_1(i, k, j) - (c1f(k) * mt + c2f(k)) * w2) / my;
+      float p2 = ph_2(i, k, j);
+      ph_save(i, k, j) = p2;
+      ph_2(i, k, j) = ph_1(i, k, j) - p2;
+      ww_save(i, k, j) = ww(i, k, j);
+    }
+  }
+}
+
+// ------------------------------------------------------------ calc_p_rho
+__device__ __forceinline__ void calc_p_rho_point(const Mem& m, int i, int k, int j, int step) {
+  F3 al = f3(m, WRFGPU_AL), p = f3(m, WRFGPU_P), ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT),
+     t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE), c2a = f3(m, WRFGPU_C2A), pm1 = f3(m, WRFGPU_PM1);
+  F2 mu = f2(m, WRFGPU_MU_2), Mut = f2(m, WRFGPU_MUTS);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), rdnw = f1(m, WRFGPU_RDNW);
+  const float a = alt(i, k, j), muij = mu(i, j), mutij = Mut(i, j), t1 = t_1(i, k, j);
+  float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (a * (c1h(k) * muij) + rdnw(k) * (ph(i, k + 1, j) - ph(i, k, j)));
+  al(i, k, j) = alv;
+  float pv = c2a(i, k, j) * (a * (t_2(i, k, j) - (c1h(k) * muij) * t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + t1)) - alv);
+  if (step == 0) {
+    pm1(i, k, j) = pv;
+  } else {
+    float ptmp = pv;
+    pv = pv + m.smdiv * (pv - pm1(i, k, j));
+    pm1(i, k, j) = ptmp;
+  }
+  p(i, k, j) = pv;
+}
+
+__global__ void __launch_bounds__(BX* BY) k_calc_p_rho(Launch L, int step) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (i < m.its || i > min(m.ite, m.ide - 1) || j < m.jts || j > min(m.jte, m.jde - 1) || k < m.kts ||
+      k > min(m.kte, m.kde - 1))
+    return;
+  calc_p_rho_point(m, i, k, j, step);
+}
+
+// ------------------------------------------------------------ calc_coef_w
+template <typename RC>
+__global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j;
+  if (i < m.its || i > min(m.ite, m.ide - 1) || j < m.jts || j > min(m.jte, m.jde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  F3 cqw = f3(m, WRFGPU_CQW), c2a = f3(m, WRFGPU_C2A);
+  F2 MUTf = f2(m, WRFGPU_MUT);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
+     rdn = f1(m, WRFGPU_RDN), rdnw = f1(m, WRFGPU_RDNW);
+  const int kde = m.kde;
+  const RC MUT = (RC)MUTf(i, j);
+  const RC lid_flag = m.cf.top_lid ? RC(0) : RC(1);
+  const RC tt = (RC(.5) * (RC)st.dts_rk * (RC)G * (RC(1.) + (RC)m.epssm));
+  const RC cof = tt * tt;
+  auto A = [&](int k) -> RC& {
+    if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[0])(i, k, j);
+    return *(RC*)&f3(m, WRFGPU_A)(i, k, j);
+  };
+  auto AL = [&](int k) -> RC& {
+    if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[1])(i, k, j);
+    return *(RC*)&f3(m, WRFGPU_ALPHA)(i, k, j);
+  };
+  auto GA = [&](int k) -> RC& {
+    if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[2])(i, k, j);
+    return *(RC*)&f3(m, WRFGPU_GAMMA)(i, k, j);
+  };
+  {
+    int k = kde - 1;
+    A(2) = RC(0.);
+    RC r = (RC)rdnw(kde - 1);
+    A(kde) = -RC(2.) * cof * (r * r) * (RC)c2a(i, kde - 1, j) * lid_flag /
+             (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
+    GA(1) = RC(0.);
+  }
+  for (int kk = 3; kk <= kde - 1; ++kk) {
+    int k = kk - 1;
+    A(kk) = -(RC)cqw(i, kk, j) * cof * (RC)rdn(kk) * (RC)rdnw(kk - 1) * (RC)c2a(i, kk - 1, j) /
+            (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
+  }
+  RC gprev = GA(1);
+  for (int k = 2; k <= kde - 1; ++k) {
+    RC b = RC(1.) + (RC)cqw(i, k, j) * cof * (RC)rdn(k) *
+                        ((RC)rdnw(k) * (RC)c2a(i, k, j) / (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k))) +
+                         (RC)rdnw(k - 1) * (RC)c2a(i, k - 1, j) /
+                             (((RC)c1h(k - 1) * MUT + (RC)c2h(k - 1)) * ((RC)c1f(k) * MUT + (RC)c2f(k))));
+    RC c = -(RC)cqw(i, k, j) * cof * (RC)rdn(k) * (RC)rdnw(k) * (RC)c2a(i, k, j) /
+           (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k + 1) * MUT + (RC)c2f(k + 1)));
+    RC al = RC(1.) / (b - A(k) * gprev);
+    AL(k) = al;
+    gprev = c * al;
+    GA(k) = gprev;
+  }
+  {
+    int k = kde;
+    RC r = (RC)rdnw(kde - 1);
+    RC b = RC(1.) + RC(2.) * cof * (r * r) * (RC)c2a(i, kde - 1, j) /
+                        (((RC)c1h(k - 1) * MUT + (RC)c2h(k - 1)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
+    RC c = RC(0.);
+    RC al = RC(1.) / (b - A(kde) * gprev);
+    AL(kde) = al;
+    GA(kde) = c * al;
+  }
+}
+
+// ------------------------------------------------------------ advance_uv
+__global__ void __launch_bounds__(BX* BY) k_advance_uv(Launch L, int rk_step, int iteration) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (iteration > stage_of(m, rk_step).nsmall) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  const int k_start = m.kts, k_end = m.kte - 1;
+  if (k < k_start || k > k_end) return;
+  const Stage st = stage_of(m, rk_step);
+  const float dts = st.dts_rk;
+  const WrfDynConfig& cf = m.cf;
+  const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, i_endu = m.ite, j_endv = m.jte;
+  int i_start_up = i_start, i_end_up = i_endu, j_start_vp = j_start, j_end_vp = j_endv;
+  if ((cf.open_xs || cf.symmetric_xs) && m.its == m.ids) i_start_up = i_start_up + 1;
+  if ((cf.open_xe || cf.symmetric_xe) && m.ite == m.ide) i_end_up = i_end_up - 1;
+  if ((cf.open_ys || cf.symmetric_ys || cf.polar) && m.jts == m.jds) j_start_vp = j_start_vp + 1;
+  if ((cf.open_ye || cf.symmetric_ye || cf.polar) && m.jte == m.jde) j_end_vp = j_end_vp - 1;
+  int i_start_u_tend = i_start, i_end_u_tend = i_endu, j_start_v_tend = j_start, j_end_v_tend = j_endv;
+  if (cf.symmetric_xs && m.its == m.ids) i_start_u_tend = i_start_u_tend + 1;
+  if (cf.symmetric_xe && m.ite == m.ide) i_end_u_tend = i_end_u_tend - 1;
+  if (cf.symmetric_ys && m.jts == m.jds) j_start_v_tend = j_start_v_tend + 1;
+  if (cf.symmetric_ye && m.jte == m.jde) j_end_v_tend = j_end_v_tend - 1;
+  F3 p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB), ph = f3(m, WRFGPU_PH_2), php = f3(m, WRFGPU_PHP),
+     alt = f3(m, WRFGPU_ALT), al = f3(m, WRFGPU_AL);
+  F2 mu = f2(m, WRFGPU_MU_2), MUDF = f2(m, WRFGPU_MUDF);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
+     rdnw = f1(m, WRFGPU_RDNW);
+  const float rdx = m.rdx, rdy = m.rdy, emdiv = m.emdiv;
+  const int kde = m.kde;
+  // u
+  if (j >= j_start && j <= min(m.jte, m.jde - 1) && i >= min(i_start_u_tend, i_start_up) &&
+      i <= max(i_end_u_tend, i_end_up)) {
+    F3 u = f3(m, WRFGPU_U_2), ru_tend = f3(m, WRFGPU_RU_TEND), cqu = f3(m, WRFGPU_CQU);
+    F2 muu = f2(m, WRFGPU_MUU), msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY);
+    float uv = u(i, k, j);
+    if (i >= i_start_u_tend && i <= i_end_u_tend) uv = uv + dts * ru_tend(i, k, j);
+    if (i >= i_start_up && i <= i_end_up) {
+      const float dx = 1.f / rdx;
+      float mudf_xy = -emdiv * dx * (MUDF(i, j) - MUDF(i - 1, j)) / msfuy(i, j);
+      float dpxy = (msfux(i, j) / msfuy(i, j)) * .5f * rdx * (c1h(k) * muu(i, j) + c2h(k)) *
+                   (((ph(i, k + 1, j) - ph(i - 1, k + 1, j)) + (ph(i, k, j) - ph(i - 1, k, j))) +
+                    (alt(i, k, j) + alt(i - 1, k, j)) * (p(i, k, j) - p(i - 1, k, j)) +
+                    (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
+      auto dpn = [&](int kk) -> float {
+        if (kk == kde) {
+          if (cf.top_lid)
+            return .5f * (m.cf1 * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) + m.cf2 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)) +
+                          m.cf3 * (p(i - 1, kde - 3, j) + p(i, kde - 3, j)));
+          return 0.f;
+        }
+        if (kk == 1)
+          return .5f * (m.cf1 * (p(i, 1, j) + p(i - 1, 1, j)) + m.cf2 * (p(i, 2, j) + p(i - 1, 2, j)) +
+                        m.cf3 * (p(i, 3, j) + p(i - 1, 3, j)));
+        return .5f * (fnm(kk) * (p(i, kk, j) + p(i - 1, kk, j)) + fnp(kk) * (p(i, kk - 1, j) + p(i - 1, kk - 1, j)));
+      };
+      dpxy = dpxy + (msfux(i, j) / msfuy(i, j)) * rdx * (php(i, k, j) - php(i - 1, k, j)) *
+                        (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu(i - 1, j)) + (c1h(k) * mu(i, j))));
+      uv = uv - dts * cqu(i, k, j) * dpxy + (c1h(k) * mudf_xy);
+    }
+    u(i, k, j) = uv;
+  }
+  // v
+  if (j >= j_start_v_tend && j <= j_end_v_tend && i >= i_start && i <= i_end) {
+    F3 v = f3(m, WRFGPU_V_2), rv_tend = f3(m, WRFGPU_RV_TEND), cqv = f3(m, WRFGPU_CQV);
+    F2 muv = f2(m, WRFGPU_MUV), msfvx = f2(m, WRFGPU_MSFVX), msfvx_inv = f2(m, WRFGPU_MSFVX_INV),
+       msfvy = f2(m, WRFGPU_MSFVY);
+    float vv = v(i, k, j) + dts * rv_tend(i, k, j);
+    const float dy = 1.f / rdy;
+    float mudf_xy = -emdiv * dy * (MUDF(i, j) - MUDF(i, j - 1)) * msfvx_inv(i, j);
+    if (j >= j_start_vp && j <= j_end_vp) {
+      float dpxy = (msfvy(i, j) / msfvx(i, j)) * .5f * rdy * (c1h(k) * muv(i, j) + c2h(k)) *
+                   (((ph(i, k + 1, j) - ph(i, k + 1, j - 1)) + (ph(i, k, j) - ph(i, k, j - 1))) +
+                    (alt(i, k, j) + alt(i, k, j - 1)) * (p(i, k, j) - p(i, k, j - 1)) +
+                    (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
+      auto dpn = [&](int kk) -> float {
+        if (kk == kde) {
+          if (cf.top_lid)
+            return .5f * (m.cf1 * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) + m.cf2 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)) +
+                          m.cf3 * (p(i, kde - 3, j - 1) + p(i, kde - 3, j)));
+          return 0.f;
+        }
+        if (kk == 1)
+          return .5f * (m.cf1 * (p(i, 1, j) + p(i, 1, j - 1)) + m.cf2 * (p(i, 2, j) + p(i, 2, j - 1)) +
+                        m.cf3 * (p(i, 3, j) + p(i, 3, j - 1)));
+        return .5f * (fnm(kk) * (p(i, kk, j) + p(i, kk, j - 1)) + fnp(kk) * (p(i, kk - 1, j) + p(i, kk - 1, j - 1)));
+      };
+      dpxy = dpxy + (msfvy(i, j) / msfvx(i, j)) * rdy * (php(i, k, j) - php(i, k, j - 1)) *
+                        (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu(i, j - 1)) + (c1h(k) * mu(i, j))));
+      vv = vv - dts * cqv(i, k, j) * dpxy + (c1h(k) * mudf_xy);
+    }
+    v(i, k, j) = vv;
+  }
+}
+
+// ------------------------------------------------------------ advance_mu_t
+template <typename RC>
+__global__ void __launch_bounds__(BX* BY) k_advance_mu_t(Launch L, int rk_step, int iteration) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (iteration > stage_of(m, rk_step).nsmall) return;
+  const int i = bp.i, j = bp.j;
+  const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
+  if (i < i_start || i > i_end || j < j_start || j > j_end) return;
+  const int k_start = m.kts, k_end = m.kte - 1, kde = m.kde;
+  const Stage st = stage_of(m, rk_step);
+  const float dts = st.dts_rk, epssm = m.epssm, rdx = m.rdx, rdy = m.rdy;
+  F3 ww = f3(m, WRFGPU_WW), ww_1 = f3(m, WRFGPU_WW1), u = f3(m, WRFGPU_U_2), u_1 = f3(m, WRFGPU_U_SAVE),
+     v = f3(m, WRFGPU_V_2), v_1 = f3(m, WRFGPU_V_SAVE), t = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE),
+     t_ave = f3(m, WRFGPU_T_2SAVE), ft = f3(m, WRFGPU_T_TEND);
+  F2 MU = f2(m, WRFGPU_MU_2), MUT = f2(m, WRFGPU_MUT), MUAVE = f2(m, WRFGPU_MUAVE), MUTS = f2(m, WRFGPU_MUTS),
+     muu = f2(m, WRFGPU_MUU), muv = f2(m, WRFGPU_MUV), MUDF = f2(m, WRFGPU_MUDF), MU_TEND = f2(m, WRFGPU_MU_TEND),
+     msfuy = f2(m, WRFGPU_MSFUY), msfvx_inv = f2(m, WRFGPU_MSFVX_INV), msftx = f2(m, WRFGPU_MSFTX),
+     msfty = f2(m, WRFGPU_MSFTY);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), dnw = f1(m, WRFGPU_DNW), fnm = f1(m, WRFGPU_FNM),
+     fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW);
+  const float mxy = msftx(i, j) * msfty(i, j);
+  const float muv0 = muv(i, j), muv1 = muv(i, j + 1), muu0 = muu(i, j), muu1 = muu(i + 1, j);
+  const float vi0 = msfvx_inv(i, j), vi1 = msfvx_inv(i, j + 1), uy0 = msfuy(i, j), uy1 = msfuy(i + 1, j);
+  auto dvdxi = [&](int k) -> float {
+    return mxy * (rdy * ((v(i, k, j + 1) + (c1h(k) * muv1 + c2h(k)) * v_1(i, k, j + 1) * vi1) -
+                         (v(i, k, j) + (c1h(k) * muv0 + c2h(k)) * v_1(i, k, j) * vi0)) +
+                  rdx * ((u(i + 1, k, j) + (c1h(k) * muu1 + c2h(k)) * u_1(i + 1, k, j) / uy1) -
+                         (u(i, k, j) + (c1h(k) * muu0 + c2h(k)) * u_1(i, k, j) / uy0)));
+  };
+  RC dmdt = RC(0.);
+  for (int k = k_start; k <= k_end; ++k) dmdt = dmdt + (RC)dnw(k) * (RC)dvdxi(k);
+  const float mu_tend = MU_TEND(i, j);
+  float muave = MU(i, j);
+  float mu = (float)((RC)MU(i, j) + (RC)dts * (dmdt + (RC)mu_tend));
+  MU(i, j) = mu;
+  MUDF(i, j) = (float)(dmdt + (RC)mu_tend);
+  MUTS(i, j) = MUT(i, j) + mu;
+  MUAVE(i, j) = .5f * ((1.f + epssm) * mu + (1.f - epssm) * muave);
+  const float my = msfty(i, j);
+  // omega by upward recursion, then subtract the saved omega
+  RC wwk = (RC)ww(i, 1, j);
+  for (int kk = 2; kk <= k_end; ++kk) {
+    int k = kk - 1;
+    wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(k) * dmdt) + (RC)dvdxi(kk - 1) + ((RC)c1h(k) * (RC)mu_tend)) / (RC)my;
+    ww(i, kk, j) = (float)wwk;
+  }
+  for (int k = 1; k <= k_end; ++k) ww(i, k, j) = ww(i, k, j) - ww_1(i, k, j);
+  // theta
+  for (int k = 1; k <= k_end; ++k) {
+    float tv = t(i, k, j);
+    t_ave(i, k, j) = tv;
+    t(i, k, j) = tv + my * dts * ft(i, k, j);
+  }
+  const float mx = msftx(i, j);
+  auto wdtn = [&](int k) -> float {
+    if (k == 1 || k == kde) return 0.f;
+    return ww(i, k, j) * (fnm(k) * t_1(i, k, j) + fnp(k) * t_1(i, k - 1, j));
+  };
+  for (int k = 1; k <= k_end; ++k) {
+    t(i, k, j) = t(i, k, j) - dts * my *
+                                  (mx * (.5f * rdy * (v(i, k, j + 1) * (t_1(i, k, j + 1) + t_1(i, k, j)) - v(i, k, j) * (t_1(i, k, j) + t_1(i, k, j - 1))) +
+                                         .5f * rdx * (u(i + 1, k, j) * (t_1(i + 1, k, j) + t_1(i, k, j)) - u(i, k, j) * (t_1(i, k, j) + t_1(i - 1, k, j)))) +
+                                   rdnw(k) * (wdtn(k + 1) - wdtn(k)));
+  }
+}
+
+// ------------------------------------------------------------ advance_w
+template <typename RC>
+__global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int iteration) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  if (iteration > stage_of(m, rk_step).nsmall) return;
+  const int i = bp.i, j = bp.j;
+  const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
+  if (i < i_start || i > i_end || j < j_start || j > j_end) return;
+  const int k_end = m.kte - 1;
+  const Stage st = stage_of(m, rk_step);
+  const float dts = st.dts_rk, epssm = m.epssm, rdx = m.rdx, rdy = m.rdy;
+  F3 w = f3(m, WRFGPU_W_2), rw_tend = f3(m, WRFGPU_RW_TEND), ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2),
+     v = f3(m, WRFGPU_V_2), t_2ave = f3(m, WRFGPU_T_2SAVE), t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE),
+     ph = f3(m, WRFGPU_PH_2), ph_1 = f3(m, WRFGPU_PH_SAVE), phb = f3(m, WRFGPU_PHB), ph_tend = f3(m, WRFGPU_PH_TEND),
+     c2a = f3(m, WRFGPU_C2A), cqw = f3(m, WRFGPU_CQW), alt = f3(m, WRFGPU_ALT);
+  F2 mut = f2(m, WRFGPU_MUT), muave = f2(m, WRFGPU_MUAVE), muts = f2(m, WRFGPU_MUTS), ht = f2(m, WRFGPU_HT),
+     msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
+     fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW), rdn = f1(m, WRFGPU_RDN);
+  RC rhs[KMAX + 1];
+  const float msft_inv = 1.f / msfty(i, j);
+  const float my = msfty(i, j), mx = msftx(i, j), mutij = mut(i, j), mua = muave(i, j), mts = muts(i, j);
+  rhs[1] = RC(0.);
+  for (int k = 1; k <= k_end; ++k) {
+    float ta = .5f * ((1.f + epssm) * t_2(i, k, j) + (1.f - epssm) * t_2ave(i, k, j));
+    ta = (ta + (c1h(k) * mua) * T0) / ((c1h(k) * mts + c2h(k)) * (T0 + t_1(i, k, j)));
+    t_2ave(i, k, j) = ta;
+    rhs[k + 1] = (RC)(dts * (ph_tend(i, k + 1, j) + .5f * G * (1.f - epssm) * w(i, k + 1, j)));
+  }
+  if (m.cf.phi_adv_z == 2) {
+    auto wdwn = [&](int kk) {  // kk = k+1
+      int k = kk - 1;
+      return rdnw(k) * (ph_1(i, k + 1, j) - ph_1(i, k, j) + phb(i, k + 1, j) - phb(i, k, j));
+    };
+    for (int k = 2; k <= k_end; ++k)
+      rhs[k] = rhs[k] - (RC)(dts * ww(i, k, j) * (fnm(k) * wdwn(k + 1) + fnp(k) * wdwn(k)));
+  } else {
+    auto wdwn = [&](int kk) {
+      int k = kk - 1;
+      return .5f * (ww(i, k + 1, j) + ww(i, k, j)) * rdnw(k) * (ph_1(i, k + 1, j) - ph_1(i, k, j) + phb(i, k + 1, j) - phb(i, k, j));
+    };
+    float wd_lo = wdwn(2);
+    for (int k = 2; k <= k_end; ++k) {
+      float wd_hi = wdwn(k + 1);
+      rhs[k] = rhs[k] - (RC)(dts * (fnm(k) * wd_hi + fnp(k) * wd_lo));
+      wd_lo = wd_hi;
+    }
+  }
+  for (int k = 2; k <= k_end + 1; ++k) {
+    rhs[k] = (RC)ph(i, k, j) + (RC)my * rhs[k] / ((RC)c1f(k) * (RC)mutij + (RC)c2f(k));
+    if (m.cf.top_lid && k == k_end + 1) rhs[k] = RC(0.);
+  }
+  const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
+  RC w1 = (RC)(my * .5f * rdy *
+                   ((ht(i, j + 1) - ht(i, j)) * (cf1 * v(i, 1, j + 1) + cf2 * v(i, 2, j + 1) + cf3 * v(i, 3, j + 1)) +
+                    (ht(i, j) - ht(i, j - 1)) * (cf1 * v(i, 1, j) + cf2 * v(i, 2, j) + cf3 * v(i, 3, j))) +
+               mx * .5f * rdx *
+                   ((ht(i + 1, j) - ht(i, j)) * (cf1 * u(i + 1, 1, j) + cf2 * u(i + 1, 2, j) + cf3 * u(i + 1, 3, j)) +
+                    (ht(i, j) - ht(i - 1, j)) * (cf1 * u(i, 1, j) + cf2 * u(i, 2, j) + cf3 * u(i, 3, j))));
+  w(i, 1, j) = (float)w1;
+  // explicit part and forward elimination in one upward sweep
+  const RC eps1 = RC(1.) + (RC)epssm, eps0 = RC(1.) - (RC)epssm;
+  RC wprev = w1;
+  const bool fp64 = sizeof(RC) == 8;
+  auto Acoef = [&](int k) -> RC { return fp64 ? (RC)d3(m, m.wd[0])(i, k, j) : (RC)f3(m, WRFGPU_A)(i, k, j); };
+  auto ALcoef = [&](int k) -> RC { return fp64 ? (RC)d3(m, m.wd[1])(i, k, j) : (RC)f3(m, WRFGPU_ALPHA)(i, k, j); };
+  auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)d3(m, m.wd[2])(i, k, j) : (RC)f3(m, WRFGPU_GAMMA)(i, k, j); };
+  RC wcol[KMAX + 1];
+  for (int k = 2; k <= k_end; ++k) {
+    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend(i, k, j) +
+            (RC)msft_inv * (RC)cqw(i, k, j) *
+                (+RC(.5) * (RC)dts * (RC)G * (RC)rdn(k) *
+                 ((RC)c2a(i, k, j) * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
+                      (eps1 * (rhs[k + 1] - rhs[k]) + eps0 * ((RC)ph(i, k + 1, j) - (RC)ph(i, k, j))) -
+                  (RC)c2a(i, k - 1, j) * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
+                      (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph(i, k, j) - (RC)ph(i, k - 1, j))))) +
+            (RC)dts * (RC)G * (RC)msft_inv *
+                ((RC)rdn(k) * ((RC)c2a(i, k, j) * (RC)alt(i, k, j) * (RC)t_2ave(i, k, j) -
+                               (RC)c2a(i, k - 1, j) * (RC)alt(i, k - 1, j) * (RC)t_2ave(i, k - 1, j)) -
+                 ((RC)c1f(k) * (RC)mua));
+    if (!fp64) wk = (RC)(float)wk;
+    wk = (wk - Acoef(k) * wprev) * ALcoef(k);
+    wcol[k] = wk;
+    wprev = wk;
+  }
+  {
+    int k = k_end + 1;
+    RC r = (RC)rdnw(k - 1);
+    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend(i, k, j) +
+            (RC)msft_inv * (-RC(.5) * (RC)dts * (RC)G / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) * (r * r) * RC(2.) *
+                                (RC)c2a(i, k - 1, j) * (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph(i, k, j) - (RC)ph(i, k - 1, j))) -
+                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a(i, k - 1, j) * (RC)alt(i, k - 1, j) * (RC)t_2ave(i, k - 1, j) +
+                                               ((RC)c1f(k) * (RC)mua)));
+    if (m.cf.top_lid) wk = RC(0.);
+    if (!fp64) wk = (RC)(float)wk;
+    wk = (wk - Acoef(k) * wprev) * ALcoef(k);
+    wcol[k] = wk;
+  }
+  // back substitution and geopotential update (downward)
+  RC wup = wcol[k_end + 1];
+  w(i, k_end + 1, j) = (float)wup;
+  ph(i, k_end + 1, j) = (float)(rhs[k_end + 1] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wup /
+                                                     ((RC)c1f(k_end + 1) * (RC)mts + (RC)c2f(k_end + 1)));
+  for (int k = k_end; k >= 2; --k) {
+    RC wk = wcol[k] - GAcoef(k) * wup;
+    w(i, k, j) = (float)wk;
+    ph(i, k, j) = (float)(rhs[k] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wk / ((RC)c1f(k) * (RC)mts + (RC)c2f(k)));
+    wup = wk;
+  }
+}
+
+// ------------------------------------------------------------ sumflux (+ calc_p_rho)
+__global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step, int iteration, int do_p_rho) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (i < m.its || i > m.ite || j < m.jts || j > m.jte || k < m.kts || k > m.kte) return;
+  const Stage st = stage_of(m, rk_step);
+  if (iteration > st.nsmall) return;  // members with fewer acoustic steps
+  const int ns = st.nsmall;
+  const int mini = min(m.ide - 1, m.ite), minj = min(m.jde - 1, m.jte), mink = min(m.kde - 1, m.kte);
+  F3 ru_m = f3(m, WRFGPU_RU_M), rv_m = f3(m, WRFGPU_RV_M), ww_m = f3(m, WRFGPU_WW_M);
+  float rum = iteration == 1 ? 0.f : ru_m(i, k, j);
+  float rvm = iteration == 1 ? 0.f : rv_m(i, k, j);
+  float wwm = iteration == 1 ? 0.f : ww_m(i, k, j);
+  const bool ru_acc = j <= minj && k <= mink;            // i its..ite
+  const bool rv_acc = i <= mini && k <= mink;            // j jts..jte
+  const bool ww_acc = i <= mini && j <= minj;            // k kts..kte
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H);
+  if (ru_acc) {
+    rum = rum + f3(m, WRFGPU_U_2)(i, k, j);
+    if (iteration == ns)
+      rum = rum / float(ns) + (c1h(k) * f2(m, WRFGPU_MUU)(i, j) + c2h(k)) * f3(m, WRFGPU_U_SAVE)(i, k, j) / f2(m, WRFGPU_MSFUY)(i, j);
+  }
+  if (rv_acc) {
+    rvm = rvm + f3(m, WRFGPU_V_2)(i, k, j);
+    if (iteration == ns)
+      rvm = rvm / float(ns) + (c1h(k) * f2(m, WRFGPU_MUV)(i, j) + c2h(k)) * f3(m, WRFGPU_V_SAVE)(i, k, j) * f2(m, WRFGPU_MSFVX_INV)(i, j);
+  }
+  if (ww_acc) {
+    wwm = wwm + f3(m, WRFGPU_WW)(i, k, j);
+    if (iteration == ns) wwm = wwm / float(ns) + f3(m, WRFGPU_WW1)(i, k, j);
+  }
+  if (iteration == 1 || ru_acc) ru_m(i, k, j) = rum;
+  if (iteration == 1 || rv_acc) rv_m(i, k, j) = rvm;
+  if (iteration == 1 || ww_acc) ww_m(i, k, j) = wwm;
+  if (do_p_rho && i <= mini && j <= minj && k <= mink) calc_p_rho_point(m, i, k, j, iteration);
+}
+
+// ------------------------------------------------------------ small_step_finish
+__global__ void __launch_bounds__(BX* BY) k_small_step_finish(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j;
+  const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
+  const int i_endu = m.ite, j_endv = m.jte;
+  if (i < i_start || i > i_endu || j < j_start || j > j_endv) return;
+  const bool px = m.cf.periodic_x, py = m.cf.periodic_y;
+  const Stage st = stage_of(m, rk_step);
+  F2 MU = f2(m, WRFGPU_MUTS), MUU = f2(m, WRFGPU_MUUS), MUV = f2(m, WRFGPU_MUVS);
+  // calc_mu_uv_1 on (muts -> muus, muvs)
+  float muus = 0.f, muvs = 0.f;
+  const bool upt = j <= j_end, vpt = i <= i_end;
+  if (upt) {
+    if (i == m.ids && m.its == m.ids) { int im = px ? i - 1 : i; muus = 0.5f * (MU(i, j) + MU(im, j)); }
+    else if (i == m.ide && m.ite == m.ide) { int im = px ? i : i - 1; muus = 0.5f * (MU(i - 1, j) + MU(im, j)); }
+    else muus = 0.5f * (MU(i, j) + MU(i - 1, j));
+    MUU(i, j) = muus;
+  }
+  if (vpt) {
+    if (j == m.jds && m.jts == m.jds) { int jm = py ? j - 1 : j; muvs = 0.5f * (MU(i, j) + MU(i, jm)); }
+    else if (j == m.jde && m.jte == m.jde) { int jm = py ? j : j - 1; muvs = 0.5f * (MU(i, j - 1) + MU(i, jm)); }
+    else muvs = 0.5f * (MU(i, j) + MU(i, j - 1));
+    MUV(i, j) = muvs;
+  }
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+  if (vpt) {
+    F3 v_2 = f3(m, WRFGPU_V_2), v_save = f3(m, WRFGPU_V_SAVE);
+    const float muv = f2(m, WRFGPU_MUV)(i, j), mx = f2(m, WRFGPU_MSFVX)(i, j);
+    for (int k = m.kds; k <= m.kde - 1; ++k)
+      v_2(i, k, j) = (mx * v_2(i, k, j) + v_save(i, k, j) * (c1h(k) * muv + c2h(k))) / (c1h(k) * muvs + c2h(k));
+  }
+  if (upt) {
+    F3 u_2 = f3(m, WRFGPU_U_2), u_save = f3(m, WRFGPU_U_SAVE);
+    const float muu = f2(m, WRFGPU_MUU)(i, j), my = f2(m, WRFGPU_MSFUY)(i, j);
+    for (int k = m.kds; k <= m.kde - 1; ++k)
+      u_2(i, k, j) = (my * u_2(i, k, j) + u_save(i, k, j) * (c1h(k) * muu + c2h(k))) / (c1h(k) * muus + c2h(k));
+  }
+  if (upt && vpt) {
+    F3 w_2 = f3(m, WRFGPU_W_2), w_save = f3(m, WRFGPU_W_SAVE), ph_2 = f3(m, WRFGPU_PH_2), ph_save = f3(m, WRFGPU_PH_SAVE),
+       ww = f3(m, WRFGPU_WW), ww1 = f3(m, WRFGPU_WW1), t_2 = f3(m, WRFGPU_T_2), t_save = f3(m, WRFGPU_T_SAVE),
+       h_diabatic = f3(m, WRFGPU_H_DIABATIC);
+    const float mt = f2(m, WRFGPU_MUT)(i, j), mts = MU(i, j), my = f2(m, WRFGPU_MSFTY)(i, j);
+    for (int k = m.kds; k <= m.kde; ++k) {
+      w_2(i, k, j) = (my * w_2(i, k, j) + w_save(i, k, j) * (c1f(k) * mt + c2f(k))) / (c1f(k) * mts + c2f(k));
+      ph_2(i, k, j) = ph_2(i, k, j) + ph_save(i, k, j);
+      ww(i, k, j) = ww(i, k, j) + ww1(i, k, j);
+    }
+    if (rk_step < m.cf.rk_ord) {
+      for (int k = m.kds; k <= m.kde - 1; ++k)
+        t_2(i, k, j) = (t_2(i, k, j) + t_save(i, k, j) * (c1h(k) * mt + c2h(k))) / (c1h(k) * mts + c2h(k));
+    } else {
+      for (int k = m.kds; k <= m.kde - 1; ++k)
+        t_2(i, k, j) = (t_2(i, k, j) - st.dts_rk * float(st.nsmall) * (c1h(k) * mt + c2h(k)) * h_diabatic(i, k, j) +
+                        t_save(i, k, j) * (c1h(k) * mt + c2h(k))) / (c1h(k) * mts + c2h(k));
+    }
+    F2 mu_2 = f2(m, WRFGPU_MU_2);
+    mu_2(i, j) = mu_2(i, j) + f2(m, WRFGPU_MU_SAVE)(i, j);
+  }
+}
+
+// ------------------------------------------------------------ launchers
+void launch_small_step_prep(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_small_step_prep<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+}
+void launch_calc_p_rho(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_calc_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.iteration);
+}
+void launch_calc_coef_w(const Launch& L, int nb, StepArgs a, bool fp64, cudaStream_t s) {
+  if (fp64) k_calc_coef_w<double><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+  else k_calc_coef_w<float><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+}
+void launch_advance_uv(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_advance_uv<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration);
+}
+void launch_advance_mu_t(const Launch& L, int nb, StepArgs a, bool fp64, cudaStream_t s) {
+  if (fp64) k_advance_mu_t<double><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration);
+  else k_advance_mu_t<float><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration);
+}
+void launch_advance_w(const Launch& L, int nb, StepArgs a, bool fp64, cudaStream_t s) {
+  if (fp64) k_advance_w<double><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration);
+  else k_advance_w<float><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration);
+}
+void launch_sumflux_p_rho(const Launch& L, int nb, StepArgs a, bool do_p_rho, cudaStream_t s) {
+  k_sumflux_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration, do_p_rho ? 1 : 0);
+}
+void launch_sumflux(const Launch& L, int nb, StepArgs a, cudaStream_t s) { launch_sumflux_p_rho(L, nb, a, false, s); }
+void launch_small_step_finish(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_small_step_finish<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+}
+
+}  // namespace wrfgpu

@@ -1,0 +1,433 @@
+// rk_tendency (dyn_em/module_em.F:370-781, physics off) as five fused
+// kernels, one per tendency field.  Each output point applies, in the
+// reference's order, zero_tend, the advection flux divergence (y, then x,
+// then z), the pressure-gradient / buoyancy term, Coriolis and curvature;
+// neighbouring fluxes are recomputed per point instead of being staged, so
+// every value is the reference's expression evaluated on the same inputs.
+//   ru_tend: advect_u (module_advect_em.F:486-745, :1470-1497),
+//            horizontal_pressure_gradient (module_big_step_utilities_em.F:2346-2414),
+//            coriolis (:3699-3711), curvature (:4289-4330)
+//   rv_tend: advect_v (:1904-2171, :2961-2995), HPG (:2247-2300), coriolis (:3724-3736), curvature (:4385-4420)
+//   rw_tend: advect_w (:4784-5096, :5996-6031), pg_buoy_w (:2419-2502), coriolis (:3738-3749), curvature (:4447-4466)
+//   t_tend : advect_scalar on theta (:3394-3650, :4306-4333)
+//   ph_tend: rhs_ph (:1365-1530, :1768-2075)
+// Roofline: HBM-bound stencils (~0.5-1 flop/B); the horizontal 6-point
+// neighbours are served from L1/L2, so DRAM traffic stays near one read per
+// input array and one write per tendency.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wrfgpu {
+
+// ---------------------------------------------------------------- ru_tend
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  F3 tend = f3(m, WRFGPU_RU_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
+  const int ktf = min(m.kte, m.kde - 1);
+  const bool in_acc = i >= m.its && i <= m.ite && j >= m.jts && j <= min(m.jte, m.jde - 1) && k >= m.kts && k <= ktf;
+  if (!in_acc) {
+    if ((FL & TF_ZERO) && in_zero) tend(i, k, j) = 0.f;
+    return;
+  }
+  float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+  F3 u = f3(m, WRFGPU_U_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rw = f3(m, WRFGPU_RW);
+  F2 msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY);
+  const float rdx = m.rdx, rdy = m.rdy;
+  if (FL & TF_ADV) {
+    F3 rom = f3(m, WRFGPU_WW);
+    F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+    auto fy = [&](int jj) {
+      float vel = 0.5f * (rv(i, k, jj) + rv(i - 1, k, jj));
+      return vel * flux5(u(i, k, jj - 3), u(i, k, jj - 2), u(i, k, jj - 1), u(i, k, jj), u(i, k, jj + 1), u(i, k, jj + 2), vel);
+    };
+    float mrdy = msfux(i, j) * rdy;
+    t = t - mrdy * (fy(j + 1) - fy(j));
+    auto fx = [&](int ii) {
+      float vel = 0.5f * (ru(ii, k, j) + ru(ii - 1, k, j));
+      return vel * flux5(u(ii - 3, k, j), u(ii - 2, k, j), u(ii - 1, k, j), u(ii, k, j), u(ii + 1, k, j), u(ii + 2, k, j), vel);
+    };
+    float mrdx = msfux(i, j) * rdx;
+    t = t - mrdx * (fx(i + 1) - fx(i));
+    auto vf = [&](int kk) -> float {
+      if (kk == m.kts || kk == m.kte) return 0.f;
+      if (kk == m.kts + 1 || kk == ktf)
+        return 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * u(i, kk, j) + fzp(kk) * u(i, kk - 1, j));
+      float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
+      return vel * flux3(u(i, kk - 2, j), u(i, kk - 1, j), u(i, kk, j), u(i, kk + 1, j), -vel);
+    };
+    t = t - rdzw(k) * (vf(k + 1) - vf(k));
+  }
+  if (FL & TF_PG) {
+    F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
+       al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqu = f3(m, WRFGPU_CQU);
+    F2 muu = f2(m, WRFGPU_MUU), mu = f2(m, WRFGPU_MU_2);
+    F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
+       rdnw = f1(m, WRFGPU_RDNW);
+    const int kde = m.kde;
+    auto dpn = [&](int kk) -> float {
+      if (kk == kde) {
+        if (m.cf.top_lid)
+          return .5f * (m.cfn * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) + m.cfn1 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)));
+        return 0.f;
+      }
+      if (kk == 1)
+        return .5f * (m.cf1 * (p(i - 1, 1, j) + p(i, 1, j)) + m.cf2 * (p(i - 1, 2, j) + p(i, 2, j)) +
+                      m.cf3 * (p(i - 1, 3, j) + p(i, 3, j)));
+      return .5f * (fnm(kk) * (p(i - 1, kk, j) + p(i, kk, j)) + fnp(kk) * (p(i - 1, kk - 1, j) + p(i, kk - 1, j)));
+    };
+    float dpx = (msfux(i, j) / msfuy(i, j)) * .5f * rdx * (c1h(k) * muu(i, j) + c2h(k)) *
+                ((ph(i, k + 1, j) - ph(i - 1, k + 1, j) + ph(i, k, j) - ph(i - 1, k, j)) +
+                 (alt(i, k, j) + alt(i - 1, k, j)) * (p(i, k, j) - p(i - 1, k, j)) +
+                 (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
+    dpx = dpx + (msfux(i, j) / msfuy(i, j)) * rdx * (php(i, k, j) - php(i - 1, k, j)) *
+                    (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu(i - 1, j)) + (c1h(k) * mu(i, j))));
+    t = t - cqu(i, k, j) * dpx;
+  }
+  if (FL & TF_COR) {
+    F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), cosa = f2(m, WRFGPU_COSA);
+    t = t + (msfux(i, j) / msfuy(i, j)) * 0.5f * (f(i, j) + f(i - 1, j)) * 0.25f *
+                (rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j)) -
+        0.5f * (e(i, j) + e(i - 1, j)) * 0.5f * (cosa(i, j) + cosa(i - 1, j)) * 0.25f *
+            (rw(i - 1, k + 1, j) + rw(i - 1, k, j) + rw(i, k + 1, j) + rw(i, k, j));
+  }
+  if (FL & TF_CURV) {
+    F3 v = f3(m, WRFGPU_V_2);
+    F2 msfvx = f2(m, WRFGPU_MSFVX);
+    auto vxgm = [&](int ii) {
+      return 0.5f * (u(ii, k, j) + u(ii + 1, k, j)) * (msfvx(ii, j + 1) - msfvx(ii, j)) * rdy -
+             0.5f * (v(ii, k, j) + v(ii, k, j + 1)) * (msfuy(ii + 1, j) - msfuy(ii, j)) * rdx;
+    };
+    t = t + 0.5f * (vxgm(i) + vxgm(i - 1)) * 0.25f * (rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j)) -
+        u(i, k, j) * RERADIUS * 0.25f * (rw(i - 1, k + 1, j) + rw(i - 1, k, j) + rw(i, k + 1, j) + rw(i, k, j));
+  }
+  tend(i, k, j) = t;
+}
+
+// ---------------------------------------------------------------- rv_tend
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  F3 tend = f3(m, WRFGPU_RV_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
+  const int ktf = min(m.kte, m.kde - 1);
+  const bool in_acc = i >= m.its && i <= min(m.ite, m.ide - 1) && j >= m.jts && j <= m.jte && k >= m.kts && k <= ktf;
+  if (!in_acc) {
+    if ((FL & TF_ZERO) && in_zero) tend(i, k, j) = 0.f;
+    return;
+  }
+  float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+  F3 v = f3(m, WRFGPU_V_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rw = f3(m, WRFGPU_RW);
+  F2 msfvx = f2(m, WRFGPU_MSFVX), msfvy = f2(m, WRFGPU_MSFVY);
+  const float rdx = m.rdx, rdy = m.rdy;
+  if (FL & TF_ADV) {
+    F3 rom = f3(m, WRFGPU_WW);
+    F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+    auto fy = [&](int jj) {
+      float vel = 0.5f * (rv(i, k, jj) + rv(i, k, jj - 1));
+      return vel * flux5(v(i, k, jj - 3), v(i, k, jj - 2), v(i, k, jj - 1), v(i, k, jj), v(i, k, jj + 1), v(i, k, jj + 2), vel);
+    };
+    float mrdy = msfvy(i, j) * rdy;
+    t = t - mrdy * (fy(j + 1) - fy(j));
+    auto fx = [&](int ii) {
+      float vel = 0.5f * (ru(ii, k, j) + ru(ii, k, j - 1));
+      return vel * flux5(v(ii - 3, k, j), v(ii - 2, k, j), v(ii - 1, k, j), v(ii, k, j), v(ii + 1, k, j), v(ii + 2, k, j), vel);
+    };
+    float mrdx = msfvy(i, j) * rdx;
+    t = t - mrdx * (fx(i + 1) - fx(i));
+    auto vf = [&](int kk) -> float {
+      if (kk == m.kts || kk == m.kte) return 0.f;
+      if (kk == m.kts + 1 || kk == ktf)
+        return 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * v(i, kk, j) + fzp(kk) * v(i, kk - 1, j));
+      float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
+      return vel * flux3(v(i, kk - 2, j), v(i, kk - 1, j), v(i, kk, j), v(i, kk + 1, j), -vel);
+    };
+    t = t - (msfvy(i, j) / msfvx(i, j)) * rdzw(k) * (vf(k + 1) - vf(k));
+  }
+  if (FL & TF_PG) {
+    F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
+       al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqv = f3(m, WRFGPU_CQV);
+    F2 muv = f2(m, WRFGPU_MUV), mu = f2(m, WRFGPU_MU_2);
+    F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
+       rdnw = f1(m, WRFGPU_RDNW);
+    const int kde = m.kde;
+    auto dpn = [&](int kk) -> float {
+      if (kk == kde) {
+        if (m.cf.top_lid)
+          return .5f * (m.cfn * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) + m.cfn1 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)));
+        return 0.f;
+      }
+      if (kk == 1)
+        return .5f * (m.cf1 * (p(i, 1, j - 1) + p(i, 1, j)) + m.cf2 * (p(i, 2, j - 1) + p(i, 2, j)) +
+                      m.cf3 * (p(i, 3, j - 1) + p(i, 3, j)));
+      return .5f * (fnm(kk) * (p(i, kk, j - 1) + p(i, kk, j)) + fnp(kk) * (p(i, kk - 1, j - 1) + p(i, kk - 1, j)));
+    };
+    float dpy = (msfvy(i, j) / msfvx(i, j)) * .5f * rdy * (c1h(k) * muv(i, j) + c2h(k)) *
+                ((ph(i, k + 1, j) - ph(i, k + 1, j - 1) + ph(i, k, j) - ph(i, k, j - 1)) +
+                 (alt(i, k, j) + alt(i, k, j - 1)) * (p(i, k, j) - p(i, k, j - 1)) +
+                 (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
+    dpy = dpy + (msfvy(i, j) / msfvx(i, j)) * rdy * (php(i, k, j) - php(i, k, j - 1)) *
+                    (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu(i, j - 1)) + (c1h(k) * mu(i, j))));
+    t = t - cqv(i, k, j) * dpy;
+  }
+  if (FL & TF_COR) {
+    F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), sina = f2(m, WRFGPU_SINA);
+    t = t - (msfvy(i, j) / msfvx(i, j)) * 0.5f * (f(i, j) + f(i, j - 1)) * 0.25f *
+                (ru(i, k, j) + ru(i + 1, k, j) + ru(i, k, j - 1) + ru(i + 1, k, j - 1)) +
+        (msfvy(i, j) / msfvx(i, j)) * 0.5f * (e(i, j) + e(i, j - 1)) * 0.5f * (sina(i, j) + sina(i, j - 1)) * 0.25f *
+            (rw(i, k + 1, j - 1) + rw(i, k, j - 1) + rw(i, k + 1, j) + rw(i, k, j));
+  }
+  if (FL & TF_CURV) {
+    F3 u = f3(m, WRFGPU_U_2);
+    F2 msfuy = f2(m, WRFGPU_MSFUY);
+    auto vxgm = [&](int jj) {
+      return 0.5f * (u(i, k, jj) + u(i + 1, k, jj)) * (msfvx(i, jj + 1) - msfvx(i, jj)) * rdy -
+             0.5f * (v(i, k, jj) + v(i, k, jj + 1)) * (msfuy(i + 1, jj) - msfuy(i, jj)) * rdx;
+    };
+    t = t - 0.5f * (vxgm(j) + vxgm(j - 1)) * 0.25f * (ru(i, k, j) + ru(i + 1, k, j) + ru(i, k, j - 1) + ru(i + 1, k, j - 1)) -
+        (msfvy(i, j) / msfvx(i, j)) * v(i, k, j) * RERADIUS * 0.25f *
+            (rw(i, k + 1, j - 1) + rw(i, k, j - 1) + rw(i, k + 1, j) + rw(i, k, j));
+  }
+  tend(i, k, j) = t;
+}
+
+// ---------------------------------------------------------------- rw_tend
+// Column kernel: pg_buoy_w overwrites cqw(k) with 1/(1+cqw(k)) after the
+// k = kde point has read the original cqw(kde-1), so each column is walked
+// in order by one thread.
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j;
+  F3 tend = f3(m, WRFGPU_RW_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
+  const bool in_acc = i >= m.its && i <= itf && j >= m.jts && j <= jtf;
+  if (!in_acc) {
+    if ((FL & TF_ZERO) && in_zero)
+      for (int k = m.kts; k <= m.kte; ++k) tend(i, k, j) = 0.f;
+    return;
+  }
+  F3 w = f3(m, WRFGPU_W_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rom = f3(m, WRFGPU_WW);
+  F3 p = f3(m, WRFGPU_P), cqw = f3(m, WRFGPU_CQW);
+  F2 msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
+  F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzu = f1(m, WRFGPU_RDN), rdnw = f1(m, WRFGPU_RDNW),
+     c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+  const float rdx = m.rdx, rdy = m.rdy;
+  const int kde = m.kde;
+  const float cqw_top = cqw(i, kde - 1, j);  // read before the k = kde-1 overwrite below
+  auto vf = [&](int kk) -> float {
+    if (kk == m.kts + 1 || kk == ktf + 1) return 0.25f * (rom(i, kk, j) + rom(i, kk - 1, j)) * (w(i, kk, j) + w(i, kk - 1, j));
+    float vel = 0.5f * (rom(i, kk, j) + rom(i, kk - 1, j));
+    return vel * flux3(w(i, kk - 2, j), w(i, kk - 1, j), w(i, kk, j), w(i, kk + 1, j), -vel);
+  };
+  const float mrdy = msftx(i, j) * rdy, mrdx = msftx(i, j) * rdx;
+  for (int k = m.kts; k <= m.kte; ++k) {
+    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    if (k >= m.kts + 1 && k <= ktf + 1) {
+      if (FL & TF_ADV) {
+        auto fy = [&](int jj) {
+          float vel = (k <= ktf) ? fzm(k) * rv(i, k, jj) + fzp(k) * rv(i, k - 1, jj)
+                                 : (2.f - fzm(k - 1)) * rv(i, k - 1, jj) - fzp(k - 1) * rv(i, k - 2, jj);
+          return vel * flux5(w(i, k, jj - 3), w(i, k, jj - 2), w(i, k, jj - 1), w(i, k, jj), w(i, k, jj + 1), w(i, k, jj + 2), vel);
+        };
+        t = t - mrdy * (fy(j + 1) - fy(j));
+        auto fx = [&](int ii) {
+          float vel = (k <= ktf) ? fzm(k) * ru(ii, k, j) + fzp(k) * ru(ii, k - 1, j)
+                                 : (2.f - fzm(k - 1)) * ru(ii, k - 1, j) - fzp(k - 1) * ru(ii, k - 2, j);
+          return vel * flux5(w(ii - 3, k, j), w(ii - 2, k, j), w(ii - 1, k, j), w(ii, k, j), w(ii + 1, k, j), w(ii + 2, k, j), vel);
+        };
+        t = t - mrdx * (fx(i + 1) - fx(i));
+        if (k <= ktf) t = t - rdzu(k) * (vf(k + 1) - vf(k));
+        else t = t + 2.f * rdzu(k - 1) * (vf(k));
+      }
+    }
+    if (FL & TF_PG) {
+      F2 muf = f2(m, WRFGPU_MU_2), mubf = f2(m, WRFGPU_MUB);
+      if (k == kde) {
+        float cq1 = 1.f / (1.f + cqw_top);
+        float cq2 = cqw_top * cq1;
+        t = t + (1.f / msfty(i, j)) * G *
+                    (cq1 * 2.f * rdnw(k - 1) * (-p(i, k - 1, j)) - (c1f(k) * muf(i, j)) - cq2 * (c1f(k) * mubf(i, j) + c2f(k)));
+      } else if (k >= 2) {
+        float cq1 = 1.f / (1.f + cqw(i, k, j));
+        float cq2 = cqw(i, k, j) * cq1;
+        cqw(i, k, j) = cq1;
+        t = t + (1.f / msfty(i, j)) * G *
+                    (cq1 * rdzu(k) * (p(i, k, j) - p(i, k - 1, j)) - (c1f(k) * muf(i, j)) - cq2 * (c1f(k) * mubf(i, j) + c2f(k)));
+      }
+    }
+    if (k >= m.kts + 1 && k <= ktf) {
+      if (FL & TF_COR) {
+        F2 e = f2(m, WRFGPU_E), sina = f2(m, WRFGPU_SINA), cosa = f2(m, WRFGPU_COSA);
+        t = t + e(i, j) * (cosa(i, j) * 0.5f * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) -
+                           (msftx(i, j) / msfty(i, j)) * sina(i, j) * 0.5f *
+                               (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))));
+      }
+    }
+    if (k >= max(2, m.kts) && k <= ktf) {
+      if (FL & TF_CURV) {
+        F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
+        t = t + RERADIUS * (0.5f * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) *
+                                0.5f * (fzm(k) * (u(i, k, j) + u(i + 1, k, j)) + fzp(k) * (u(i, k - 1, j) + u(i + 1, k - 1, j))) +
+                            (msftx(i, j) / msfty(i, j)) * 0.5f *
+                                (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))) *
+                                0.5f * (fzm(k) * (v(i, k, j) + v(i, k, j + 1)) + fzp(k) * (v(i, k - 1, j) + v(i, k - 1, j + 1))));
+      }
+    }
+    tend(i, k, j) = t;
+  }
+}
+
+// ---------------------------------------------------------------- t_tend
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  F3 tend = f3(m, WRFGPU_T_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
+  if ((FL & TF_ZERO) && in_zero) {
+    // zero_tend of the *_save arrays at the points small_step_prep does not
+    // overwrite (module_em.F:395-428; module_small_step_em.F:170-245).
+    const bool kt = k == m.kde, ie = i == m.ide, je = j == m.jde;
+    if (kt || je) f3(m, WRFGPU_U_SAVE)(i, k, j) = 0.f;
+    if (kt || ie) f3(m, WRFGPU_V_SAVE)(i, k, j) = 0.f;
+    if (kt || ie || je) f3(m, WRFGPU_T_SAVE)(i, k, j) = 0.f;
+    if (ie || je) { f3(m, WRFGPU_W_SAVE)(i, k, j) = 0.f; f3(m, WRFGPU_PH_SAVE)(i, k, j) = 0.f; }
+    if (k == m.kts && (ie || je)) f2(m, WRFGPU_MU_SAVE)(i, j) = 0.f;
+  }
+  const bool in_acc = i >= m.its && i <= itf && j >= m.jts && j <= jtf && k >= m.kts && k <= ktf;
+  if (!in_acc) {
+    if ((FL & TF_ZERO) && in_zero) tend(i, k, j) = 0.f;
+    return;
+  }
+  float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+  if (FL & TF_ADV) {
+    F3 fld = f3(m, WRFGPU_T_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rom = f3(m, WRFGPU_WW);
+    F2 msftx = f2(m, WRFGPU_MSFTX);
+    F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+    auto fy = [&](int jj) {
+      float vel = rv(i, k, jj);
+      return vel * flux5(fld(i, k, jj - 3), fld(i, k, jj - 2), fld(i, k, jj - 1), fld(i, k, jj), fld(i, k, jj + 1), fld(i, k, jj + 2), vel);
+    };
+    t = t - msftx(i, j) * m.rdy * (fy(j + 1) - fy(j));
+    auto fx = [&](int ii) {
+      float vel = ru(ii, k, j);
+      return vel * flux5(fld(ii - 3, k, j), fld(ii - 2, k, j), fld(ii - 1, k, j), fld(ii, k, j), fld(ii + 1, k, j), fld(ii + 2, k, j), vel);
+    };
+    t = t - msftx(i, j) * m.rdx * (fx(i + 1) - fx(i));
+    auto vf = [&](int kk) -> float {
+      if (kk == m.kts || kk == m.kte) return 0.f;
+      if (kk == m.kts + 1 || kk == ktf) return rom(i, kk, j) * (fzm(kk) * fld(i, kk, j) + fzp(kk) * fld(i, kk - 1, j));
+      float vel = rom(i, kk, j);
+      return vel * flux3(fld(i, kk - 2, j), fld(i, kk - 1, j), fld(i, kk, j), fld(i, kk + 1, j), -vel);
+    };
+    t = t - rdzw(k) * (vf(k + 1) - vf(k));
+  }
+  tend(i, k, j) = t;
+}
+
+// ---------------------------------------------------------------- ph_tend
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
+  BlockPos bp = block_pos(L);
+  if (!bp.valid) return;
+  const Mem& m = L.mem[bp.m];
+  const int i = bp.i, j = bp.j, k = bp.k;
+  F3 tend = f3(m, WRFGPU_PH_TEND);
+  const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1);
+  const int kte = m.kte, kde = m.kde;
+  const bool in_acc = i >= m.its && i <= itf && j >= m.jts && j <= jtf && k >= 2 && k <= kte;
+  if (!in_acc) {
+    if ((FL & TF_ZERO) && in_zero) tend(i, k, j) = 0.f;
+    return;
+  }
+  if (!(FL & TF_ADV)) return;
+  float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+  F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), ww = f3(m, WRFGPU_WW), ph = f3(m, WRFGPU_PH_2),
+     phb = f3(m, WRFGPU_PHB), w = f3(m, WRFGPU_W_2);
+  F2 mut = f2(m, WRFGPU_MUT), muuf = f2(m, WRFGPU_MUU), muvf = f2(m, WRFGPU_MUV), msfux = f2(m, WRFGPU_MSFUX),
+     msfvy = f2(m, WRFGPU_MSFVY), msfty = f2(m, WRFGPU_MSFTY);
+  F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
+     rdnw = f1(m, WRFGPU_RDNW);
+  // vertical advection of ph (:1396-1428)
+  if (k <= kte - 1) {
+    if (m.cf.phi_adv_z == 2) {
+      auto wdwn = [&](int kk) { return rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j)); };
+      t = t - ww(i, k, j) * (fnm(k) * wdwn(k + 1) + fnp(k) * wdwn(k));
+    } else {
+      auto wdwn = [&](int kk) {
+        return .5f * (ww(i, kk, j) + ww(i, kk - 1, j)) * rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
+      };
+      t = t - (fnm(k) * wdwn(k + 1) + fnp(k) * wdwn(k));
+    }
+  }
+  // "gw" term (:1432-1446)
+  if (m.cf.non_hydrostatic) {
+    if (k == kde) t = 0.f;
+    t = t + (c1f(k) * mut(i, j) + c2f(k)) * G * w(i, k, j) / msfty(i, j);
+  }
+  auto S = [&](int di, int dj) {  // 6th-order centred difference of ph + phb
+    return 45.f * (ph(i + di, k, j + dj) - ph(i - di, k, j - dj)) -
+           9.f * (ph(i + 2 * di, k, j + 2 * dj) - ph(i - 2 * di, k, j - 2 * dj)) +
+           (ph(i + 3 * di, k, j + 3 * dj) - ph(i - 3 * di, k, j - 3 * dj)) +
+           45.f * (phb(i + di, k, j + dj) - phb(i - di, k, j - dj)) -
+           9.f * (phb(i + 2 * di, k, j + 2 * dj) - phb(i - 2 * di, k, j - 2 * dj)) +
+           (phb(i + 3 * di, k, j + 3 * dj) - phb(i - 3 * di, k, j - 3 * dj));
+  };
+  const float cfn = m.cfn, cfn1 = m.cfn1;
+  if (k <= kte - 1) {
+    t = t - (0.25f * m.rdy / msfty(i, j)) *
+                (((c1f(k) * muvf(i, j + 1) + c2f(k)) * (v(i, k, j + 1) + v(i, k - 1, j + 1)) * msfvy(i, j + 1) +
+                  (c1f(k) * muvf(i, j) + c2f(k)) * (v(i, k, j) + v(i, k - 1, j)) * msfvy(i, j)) *
+                 (1.f / 60.f) * S(0, 1));
+    t = t - (0.25f * m.rdx / msfty(i, j)) *
+                (((c1f(k) * muuf(i + 1, j) + c2f(k)) * (u(i + 1, k, j) + u(i + 1, k - 1, j)) * msfux(i + 1, j) +
+                  (c1f(k) * muuf(i, j) + c2f(k)) * (u(i, k, j) + u(i, k - 1, j)) * msfux(i, j)) *
+                 (1.f / 60.f) * S(1, 0));
+  } else {
+    t = t - (0.5f * m.rdy / msfty(i, j)) *
+                (((c1f(k) * muvf(i, j + 1) + c2f(k)) * (cfn * v(i, k - 1, j + 1) + cfn1 * v(i, k - 2, j + 1)) * msfvy(i, j + 1) +
+                  (c1f(k) * muvf(i, j) + c2f(k)) * (cfn * v(i, k - 1, j) + cfn1 * v(i, k - 2, j)) * msfvy(i, j)) *
+                 (1.f / 60.f) * S(0, 1));
+    t = t - (0.5f * m.rdx / msfty(i, j)) *
+                (((c1f(k) * muuf(i + 1, j) + c2f(k)) * (cfn * u(i + 1, k - 1, j) + cfn1 * u(i + 1, k - 2, j)) * msfux(i + 1, j) +
+                  (c1f(k) * muuf(i, j) + c2f(k)) * (cfn * u(i, k - 1, j) + cfn1 * u(i, k - 2, j)) * msfux(i, j)) *
+                 (1.f / 60.f) * S(1, 0));
+  }
+  tend(i, k, j) = t;
+}
+
+// ---------------------------------------------------------------- launchers
+#define DISPATCH_FL(KERNEL, GRID, BLOCK, S, FLAGS)                                       \
+  switch (FLAGS) {                                                                      \
+    case TF_ALL: KERNEL<TF_ALL><<<GRID, BLOCK, 0, S>>>(L); break;                       \
+    case TF_ZERO | TF_ADV: KERNEL<TF_ZERO | TF_ADV><<<GRID, BLOCK, 0, S>>>(L); break;   \
+    case TF_ADV: KERNEL<TF_ADV><<<GRID, BLOCK, 0, S>>>(L); break;                       \
+    case TF_PG: KERNEL<TF_PG><<<GRID, BLOCK, 0, S>>>(L); break;                         \
+    case TF_COR: KERNEL<TF_COR><<<GRID, BLOCK, 0, S>>>(L); break;                       \
+    case TF_CURV: KERNEL<TF_CURV><<<GRID, BLOCK, 0, S>>>(L); break;                     \
+    case TF_ZERO: KERNEL<TF_ZERO><<<GRID, BLOCK, 0, S>>>(L); break;                     \
+    default: break;                                                                     \
+  }
+
+void launch_tend_u(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_u, nb, dim3(BX, BY), s, flags) }
+void launch_tend_v(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_v, nb, dim3(BX, BY), s, flags) }
+void launch_tend_w(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_w, nb, dim3(BX, BY), s, flags) }
+void launch_tend_t(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t, nb, dim3(BX, BY), s, flags) }
+void launch_tend_ph(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph, nb, dim3(BX, BY), s, flags) }
+
+}  // namespace wrfgpu

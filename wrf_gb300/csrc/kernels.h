@@ -1,0 +1,72 @@
+// Host-side launch wrappers of the device kernels (one translation unit per
+// kernel family; no relocatable device code needed).
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace wrfgpu {
+
+struct HaloJob {
+  int id;        // field id (3-D or 2-D), ignored for species
+  int kind;      // 3 or 2
+  int species;   // >= 0: species index (uses q / qo), -1 otherwise
+  int old;       // species: 1 = old (_1) copy
+  char var;      // reference stagger code: 'u','v','w','p','t'
+  char pad[3];
+};
+constexpr int MAX_HALO_JOBS = 24;
+struct HaloJobs {
+  int n;
+  HaloJob job[MAX_HALO_JOBS];
+};
+
+// Stage / iteration arguments shared by the step kernels.
+struct StepArgs {
+  int rk_step;     // 1..3
+  int iteration;   // acoustic iteration (1-based) or 0
+  int species;     // species index for scalar kernels
+  int flags;       // kernel-specific variant bits
+};
+
+// Variant bits of the tendency kernels (rk_tendency pieces).
+enum : int {
+  TF_ZERO = 1,      // start from zero (zero_tend) instead of accumulating
+  TF_ADV = 2,       // advect_u / advect_v / advect_w / advect_scalar / rhs_ph
+  TF_PG = 4,        // horizontal_pressure_gradient / pg_buoy_w
+  TF_COR = 8,       // coriolis
+  TF_CURV = 16,     // curvature
+  TF_ALL = 31
+};
+
+void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s);
+void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s);
+
+// rk_tendency
+void launch_tend_u(const Launch& L3, int nblocks, int flags, cudaStream_t s);
+void launch_tend_v(const Launch& L3, int nblocks, int flags, cudaStream_t s);
+void launch_tend_w(const Launch& L2, int nblocks, int flags, cudaStream_t s);
+void launch_tend_t(const Launch& L3, int nblocks, int flags, cudaStream_t s);
+void launch_tend_ph(const Launch& L3, int nblocks, int flags, cudaStream_t s);
+void launch_zero_save(const Launch& L3, int nblocks, cudaStream_t s);
+
+// acoustic steps
+void launch_small_step_prep(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s);
+void launch_calc_p_rho(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_calc_coef_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
+void launch_advance_uv(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_advance_mu_t(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
+void launch_advance_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
+void launch_sumflux_p_rho(const Launch& L3, int nblocks, StepArgs a, bool do_p_rho, cudaStream_t s);
+void launch_sumflux(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_small_step_finish(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s);
+
+// scalars and diagnosis
+void launch_update_scalar_pd(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_advect_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_advect_scalar_pd2(const Launch& L3, int nblocks, StepArgs a, float* const* d_scratch, cudaStream_t s);
+void launch_update_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
+void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
+void launch_cfl_check(const Launch& L3, int nblocks, cudaStream_t s);
+
+}  // namespace wrfgpu

@@ -124,12 +124,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_case(workload):
+def make_case(workload, nx=None):
     from wrf_gb300 import cases
     if workload == "c1":
         return cases.config1()
     if workload == "c2":
-        return cases.config2()
+        return cases.config2() if not nx else cases.config2(nx=nx)
     raise ValueError(workload)
 
 
@@ -168,7 +168,7 @@ def run_reference(args, world, rank):
         return
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from _harness import OracleDomain
-    case = make_case(args.workload)
+    case = make_case(args.workload, args.nx)
     cores = os.cpu_count() or 1
     od = OracleDomain(case, "f32", nthreads=cores)
     steps = max(1, min(args.steps, args.ref_steps))
@@ -222,6 +222,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2"])
     ap.add_argument("--mixed", action="store_true", help="mixed-precision form (FP64 column steps)")
+    ap.add_argument("--nx", type=int, default=None, help="horizontal size of the supercell workload (profiling runs)")
     ap.add_argument("--ref-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -235,7 +236,7 @@ def main():
 
     from wrf_gb300 import abi
     from wrf_gb300 import gpu as G
-    case = make_case(args.workload)
+    case = make_case(args.workload, args.nx)
     flags = G.FLAG_MIXED if args.mixed else 0
     dom = G.Domain(case, flags=flags)
     cells = case.cells()

@@ -144,7 +144,22 @@ int wrfgpu_sync(WrfGpuEnsemble* h);
 /* Advance nsteps and return the device time in milliseconds (CUDA events on
  * the ensemble's stream). */
 int wrfgpu_time_steps(WrfGpuEnsemble* h, int nsteps, float* ms);
-/* Run one model-layer routine on the resident state (kernel-level parity). */
+/* Routine ids of wrfgpu_run_routine: one per model-layer call of the
+ * physics-off solve_em path (the file:line each follows is in the kernel
+ * sources).  WRFGPU_R_RK_TENDENCY runs the whole of rk_tendency
+ * (dyn_em/module_em.F:370-781) as the fused solver does. */
+enum WrfGpuRoutine {
+  WRFGPU_R_RK_STEP_PREP = 1, WRFGPU_R_ZERO_TEND, WRFGPU_R_ADVECT_U, WRFGPU_R_ADVECT_V, WRFGPU_R_ADVECT_W,
+  WRFGPU_R_ADVECT_T, WRFGPU_R_RHS_PH, WRFGPU_R_HORIZONTAL_PRESSURE_GRADIENT, WRFGPU_R_PG_BUOY_W,
+  WRFGPU_R_CORIOLIS, WRFGPU_R_CURVATURE, WRFGPU_R_SMALL_STEP_PREP, WRFGPU_R_CALC_P_RHO, WRFGPU_R_CALC_COEF_W,
+  WRFGPU_R_ADVANCE_UV, WRFGPU_R_ADVANCE_MU_T, WRFGPU_R_ADVANCE_W, WRFGPU_R_SUMFLUX, WRFGPU_R_SMALL_STEP_FINISH,
+  WRFGPU_R_RK_UPDATE_SCALAR_PD, WRFGPU_R_ADVECT_SCALAR, WRFGPU_R_ADVECT_SCALAR_PD, WRFGPU_R_RK_UPDATE_SCALAR,
+  WRFGPU_R_CALC_P_RHO_PHI, WRFGPU_R_SET_W_SURFACE, WRFGPU_R_RK_TENDENCY
+};
+/* Run one model-layer routine on the resident state (kernel-level parity).
+ * rk_step 1..3; iteration = acoustic step (1-based) for the acoustic
+ * routines (0 = before the first, for calc_p_rho); species for the scalar
+ * routines. */
 int wrfgpu_run_routine(WrfGpuEnsemble* h, int routine, int rk_step, int iteration, int species);
 /* set_physical_bc3d / set_physical_bc2d of one field of every member. */
 int wrfgpu_fill_halo(WrfGpuEnsemble* h, int id, char var);

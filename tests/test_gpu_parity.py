@@ -3,8 +3,10 @@
 * Routine level: the oracle's state is copied into the GPU before every
   routine of one solve_em large step, both run the routine, and every field
   is compared.  The plain form is built with --fmad=false and IEEE division,
-  so all routines must agree bit for bit except calc_p_rho_phi, whose powf /
-  logf come from CUDA rather than glibc (a few ulp).
+  so all routines must agree bit for bit except calc_p_rho_phi: its log and
+  pow are correctly rounded on both sides (float-float on the GPU, double
+  libm rounded once in the oracle), and the float-float pow misses the
+  correctly rounded result by one ulp in ~5e-5 of inputs.
 * Step level: 1 large step of the 41x41x41 supercell configuration, relative
   L2 (diffwrf serr) per field <= 1e-5; growth tracked over steps.
 * Batched == plain and graph == no-graph, bit for bit.
@@ -150,7 +152,7 @@ def test_routine_sequence_bitwise(gpulib, small):
             adv = "advect_scalar_pd" if rk == 3 else "advect_scalar"
             rc(adv, rk, 0, s)
             rc("rk_update_scalar", rk, 0, s)
-        rc("calc_p_rho_phi", rk, tol=2e-6, label="calc_p_rho_phi rk=%d" % rk)
+        rc("calc_p_rho_phi", rk, tol=1e-7, label="calc_p_rho_phi rk=%d" % rk)
         if rk < 3:
             fill_cmp(BC5, "BC5", species_cur=True)
     rc("set_w_surface", 3)
@@ -257,7 +259,10 @@ def test_cfl_limit_reported(gpulib, small):
 
 def test_mixed_precision_close_to_fp64(gpulib):
     """The mixed form (FP64 column sums / Thomas) tracks the FP64 oracle at
-    least as well as the plain FP32 form does, within 1e-4 after 10 steps."""
+    least as well as the plain FP32 form does, within 1e-4 after 10 steps
+    for u, v, theta, ph and mu (the FP32 oracle itself is 1e-5..6e-5 off
+    there; w, p and al, whose FP32 error is 2e-4..2e-3, are reported by
+    the bench instead)."""
     case = cases.config1()
     o64 = OracleDomain(case, "f64")
     o64.step(10)
@@ -272,5 +277,5 @@ def test_mixed_precision_close_to_fp64(gpulib):
         ref = interior(case, fid, o64.get(fid))
         ep = serr(interior(case, fid, plain.get(0, fid)), ref)
         em = serr(interior(case, fid, mixed.get(0, fid)), ref)
-        assert em <= 1e-4, (nm, em)
+        assert em <= 1e-4, (nm, em, ep)
         assert em <= 3 * ep + 1e-7, (nm, em, ep)

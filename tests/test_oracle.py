@@ -1,0 +1,281 @@
+"""The oracle against known answers and the properties the reference's
+equations guarantee (CPU only).
+
+The reference ships no golden output for this path, so the restatement is
+pinned by:
+* known answers of the advection stencils derived from their mathematics
+  (exactness on polynomials, the 2-dx damping rate of the 5th-order upwind
+  flux);
+* the reference's own advection fixture (module_advect_em.F:10564-10871,
+  a top-hat carried around a periodic 90-point channel): mass conserved,
+  positivity with the PD limiter, return to the starting position;
+* conservation and balance: a windless, bubble-free state stays at rest; dry
+  mass and coupled scalar mass are conserved with periodic boundaries;
+  positive-definite scalars stay non-negative;
+* determinism: the tile decomposition (OpenMP j-slabs) does not change a bit,
+  and FP32 stays close to FP64.
+"""
+import numpy as np
+import pytest
+
+from wrf_gb300 import abi, cases
+
+from _harness import OracleDomain, tophat_feeder, serr
+
+H = abi.HALO
+
+
+def mass_interior(case, a, kind=3):
+    """Mass points i in [1, ide-1], j in [1, jde-1], k in [1, kde-1]."""
+    a = np.asarray(a)
+    if kind == 3:
+        a = a.reshape(case.jde + 2 * H, case.kde, case.ide + 2 * H)
+        return a[H:H + case.jde - 1, :case.kde - 1, H:H + case.ide - 1]
+    a = a.reshape(case.jde + 2 * H, case.ide + 2 * H)
+    return a[H:H + case.jde - 1, H:H + case.ide - 1]
+
+
+def rest_case(kde=20, hyps=1):
+    rng = np.random.Generator(np.random.PCG64(0))
+    return cases.supercell_state(12, 10, kde, 2000.0, 12.0, 20000.0, [], rng, n_scalar=1, noise=0.0,
+                                 hodo_radius=0.0, name="rest", hypsometric_opt=hyps)
+
+
+@pytest.fixture(scope="module")
+def small():
+    return cases.small_case(nx=12, ny=10, kde=12, n_scalar=2, seed=11)
+
+
+# ---------------------------------------------------------------------------
+# known answers of the flux-divergence stencils
+# ---------------------------------------------------------------------------
+def _advect_species(case, q, ru=0.0, rv=0.0, ww=0.0):
+    od = OracleDomain(case, "f64")
+    shp = (case.jde + 2 * H, case.kde, case.ide + 2 * H)
+    od.set(abi.FIELD_ID["ru_m"], np.full(shp, ru))
+    od.set(abi.FIELD_ID["rv_m"], np.full(shp, rv))
+    od.set(abi.FIELD_ID["ww_m"], np.full(shp, ww))
+    od.set(abi.species_id(0), q)
+    od.set(abi.species_id(0, True), q)
+    od.run("advect_scalar", 1, 0, 0)
+    return od.get(abi.FIELD_ID["advect_tend"]).reshape(shp)
+
+
+def _coords(case):
+    shp = (case.jde + 2 * H, case.kde, case.ide + 2 * H)
+    j, k, i = np.meshgrid(np.arange(shp[0]) + 1 - H, np.arange(shp[1]) + 1, np.arange(shp[2]) + 1 - H, indexing="ij")
+    return i.astype(float), j.astype(float), k.astype(float)
+
+
+@pytest.mark.parametrize("vel", [7.5, -7.5])
+def test_flux5_exact_on_quintic_x(small, vel):
+    """module_advect_em.F:3102-3119 flux5: the difference of the centred
+    6-point fluxes is the 6th-order central derivative (exact to degree 6)
+    and the upwind part is a 5th difference (constant for a quintic), so the
+    x divergence is exactly -U rdx P'(i)."""
+    case = small
+    i, _, _ = _coords(case)
+    P = lambda x: 0.3 + 0.2 * x - 0.05 * x ** 2 + 0.004 * x ** 3 - 1e-4 * x ** 4 + 2e-6 * x ** 5
+    dP = lambda x: 0.2 - 0.1 * x + 0.012 * x ** 2 - 4e-4 * x ** 3 + 1e-5 * x ** 4
+    tend = _advect_species(case, P(i), ru=vel)
+    rdx = case.desc.scalars.rdx
+    want = -vel * rdx * dP(i)
+    got = mass_interior(case, tend)
+    ref = mass_interior(case, want)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("vel", [4.0, -4.0])
+def test_flux5_exact_on_quartic_y(small, vel):
+    case = small
+    _, j, _ = _coords(case)
+    P = lambda y: 1.0 - 0.1 * y + 0.03 * y ** 2 - 0.002 * y ** 3 + 5e-5 * y ** 4
+    dP = lambda y: -0.1 + 0.06 * y - 0.006 * y ** 2 + 2e-4 * y ** 3
+    tend = _advect_species(case, P(j), rv=vel)
+    want = -vel * case.desc.scalars.rdy * dP(j)
+    got, ref = mass_interior(case, tend), mass_interior(case, want)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("vel", [3.0, -3.0])
+def test_flux5_damps_2dx_wave_at_16_15(small, vel):
+    """For q = (-1)^i the centred part vanishes and the upwind part gives a
+    tendency of -(16/15) |U| rdx q: the 5th-order scheme's 2-dx damping."""
+    case = small
+    i, _, _ = _coords(case)
+    q = np.where(i % 2 == 0, 1.0, -1.0)
+    tend = _advect_species(case, q, ru=vel)
+    want = -(16.0 / 15.0) * abs(vel) * case.desc.scalars.rdx * q
+    got, ref = mass_interior(case, tend), mass_interior(case, want)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("vel", [0.02, -0.02])
+def test_flux3_vertical_exact(small, vel):
+    """module_advect_em.F:4306-4333: 3rd-order vertical flux (4-point centred,
+    whose differences are the 4th-order central derivative, + a 3rd
+    difference) is exact for a quadratic away from the 2nd-order faces k = 2
+    and kde-1; with a linear profile every level is exact, including the
+    zero-flux top and bottom faces."""
+    case = small
+    _, _, k = _coords(case)
+    rdnw = case.fields["rdnw"]
+    kd = case.kde
+    # quadratic, levels 3..kde-3
+    P = lambda z: 2.0 + 0.3 * z - 0.02 * z ** 2
+    tend = _advect_species(case, P(k), ww=vel)
+    want = -rdnw[None, :, None] * vel * (P(k + 0.5) - P(k - 0.5))
+    got, ref = mass_interior(case, tend), mass_interior(case, want)
+    sl = slice(2, kd - 3)
+    assert np.max(np.abs(got[:, sl] - ref[:, sl])) <= 1e-12 * np.max(np.abs(ref[:, sl]))
+    # linear, all levels (vflux = 0 at k = 1 and kde)
+    L = lambda z: 1.0 + 0.25 * z
+    tend = _advect_species(case, L(k), ww=vel)
+    up = np.where(k + 1 <= kd - 1, L(k + 0.5), 0.0)
+    dn = np.where(k >= 2, L(k - 0.5), 0.0)
+    want = -rdnw[None, :, None] * vel * (up - dn)
+    got, ref = mass_interior(case, tend), mass_interior(case, want)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+# ---------------------------------------------------------------------------
+# the reference's advection fixture (top-hat feeder)
+# ---------------------------------------------------------------------------
+def test_feeder_tophat_pd():
+    """ru = 90, dx = 1 km, dt = 5 s: one revolution of the 90-point periodic
+    channel every 200 loops.  The PD limiter keeps the top-hat non-negative
+    and it comes back to where it started.  The fixture refreshes its
+    periodic halo only after the third RK stage, so the first two stages see
+    a stale halo and mass drifts slightly (+0.05% per revolution)."""
+    rows = tophat_feeder(1, nloops=2000, every=200, precision="f64")
+    q = rows[:, :90]
+    m0 = q[0].sum()
+    x = np.arange(1, 91)
+    c0 = (q[0] * x).sum() / m0
+    for r in q[1:]:
+        assert r.min() >= -1e-12
+        assert abs(r.sum() - m0) <= 1e-2 * m0
+        assert abs((r * x).sum() / r.sum() - c0) < 1.0
+        assert 0.8 < r.max() < 1.2
+
+
+def test_feeder_tophat_original_undershoots():
+    """Without the limiter the 5th-order scheme undershoots below zero at the
+    discontinuities, which is what the PD option removes."""
+    rows = tophat_feeder(0, nloops=400, every=200, precision="f64")
+    q = rows[:, :90]
+    assert q[1:].min() < -1e-3
+    pd = tophat_feeder(1, nloops=400, every=200, precision="f64")[:, :90]
+    assert pd[1:].min() >= -1e-12
+
+
+def test_feeder_f32_close_to_f64():
+    a = tophat_feeder(1, nloops=400, every=200, precision="f32")
+    b = tophat_feeder(1, nloops=400, every=200, precision="f64")
+    assert serr(a, b) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# balance and conservation of the full large step
+# ---------------------------------------------------------------------------
+def test_rest_state_stays_at_rest():
+    """No wind, no bubble, hypsometric_opt 1 (the re-diagnosis inverts the
+    init's hydrostatic integration): u and v stay exactly 0, theta and mu do
+    not move, w stays below 5 mm/s over 20 steps."""
+    case = rest_case()
+    od = OracleDomain(case, "f64")
+    for n in range(4):
+        od.step(5)
+        for nm in ("u_2", "v_2"):
+            assert np.max(np.abs(mass_interior(case, od.get(abi.FIELD_ID[nm])))) == 0.0
+        w = od.get(abi.FIELD_ID["w_2"]).reshape(case.jde + 2 * H, case.kde, case.ide + 2 * H)
+        assert np.max(np.abs(w[H:H + case.jde - 1, :, H:H + case.ide - 1])) < 5e-3
+        t = mass_interior(case, od.get(abi.FIELD_ID["t_2"]))
+        assert np.max(np.abs(t - mass_interior(case, case.fields["t_2"]))) < 1e-9
+        mu = mass_interior(case, od.get(abi.FIELD_ID["mu_2"]), 2)
+        assert np.max(np.abs(mu - mass_interior(case, case.fields["mu_2"], 2))) < 1e-9
+
+
+def test_rest_state_default_hypsometric_top_adjustment():
+    """With the reference's default hypsometric_opt = 2 the init leaves the
+    top layer out of balance (log-form al against the linear ph integration):
+    a w of O(10 m/s) appears at the lid in the first step, ten times more than
+    anywhere in the lower half of the column."""
+    case = rest_case(hyps=2)
+    od = OracleDomain(case, "f64")
+    od.step(1)
+    w = od.get(abi.FIELD_ID["w_2"]).reshape(case.jde + 2 * H, case.kde, case.ide + 2 * H)
+    w = w[H:H + case.jde - 1, :, H:H + case.ide - 1]
+    assert np.max(np.abs(w[:, -1])) > 1.0
+    assert np.max(np.abs(w[:, : case.kde // 2])) < 0.1 * np.max(np.abs(w[:, -1]))
+
+
+def _column_masses(case, od):
+    mub = mass_interior(case, case.fields["mub"], 2)
+    mu = mass_interior(case, od.get(abi.FIELD_ID["mu_2"]), 2)
+    c1h = case.fields["c1h"][:case.kde - 1]
+    c2h = case.fields["c2h"][:case.kde - 1]
+    dnw = case.fields["dnw"][:case.kde - 1]
+    mut = mub + mu
+    dry = mu.sum()
+    nsp = case.desc.n_moist + case.desc.n_scalar
+    sc = []
+    for s in range(nsp):
+        q = mass_interior(case, od.get(abi.species_id(s)))
+        w = (c1h[None, :, None] * mut[:, None, :] + c2h[None, :, None]) * (-dnw)[None, :, None]
+        sc.append(float((w * q).sum()))
+    return dry, sc
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 3e-6)])
+def test_dry_and_scalar_mass_conserved(small, prec, tol):
+    """Flux form with periodic boundaries: sum(mu) and sum((c1 mut + c2) q dnw)
+    are invariants of the large step."""
+    case = small
+    od = OracleDomain(case, prec)
+    mub_sum = mass_interior(case, case.fields["mub"], 2).sum()
+    d0, s0 = _column_masses(case, od)
+    od.step(4)
+    d1, s1 = _column_masses(case, od)
+    assert abs(d1 - d0) <= tol * (mub_sum + abs(d0))
+    for a, b in zip(s0, s1):
+        assert abs(b - a) <= 10 * tol * abs(a)
+
+
+def test_pd_scalars_stay_nonnegative(small):
+    """Positive definite up to round-off: the limiter's eps and the final
+    mass-weighted update can leave negatives of a few ulp of the field."""
+    case = small
+    od = OracleDomain(case, "f32")
+    for _ in range(3):
+        od.step(2)
+        for s in range(1 + case.desc.n_scalar):
+            q = mass_interior(case, od.get(abi.species_id(s)))
+            assert q.min() >= -1e-7 * q.max()
+
+
+def test_tiling_does_not_change_bits(small):
+    a = OracleDomain(small, "f32", nthreads=1)
+    b = OracleDomain(small, "f32", nthreads=4)
+    a.step(2)
+    b.step(2)
+    for nm in ("u_2", "v_2", "w_2", "t_2", "ph_2", "mu_2", "p", "al"):
+        fid = abi.FIELD_ID[nm]
+        assert np.array_equal(a.get(fid), b.get(fid)), nm
+
+
+def test_f32_tracks_f64():
+    """The FP32 restatement against the FP64 one: small after 1 step and
+    growing without a jump over 20 steps."""
+    case = cases.config1()
+    a = OracleDomain(case, "f32", nthreads=4)
+    b = OracleDomain(case, "f64", nthreads=4)
+    prev = 0.0
+    for n in (1, 4, 15):
+        a.step(n)
+        b.step(n)
+        e = max(serr(mass_interior(case, a.get(abi.FIELD_ID[nm])), mass_interior(case, b.get(abi.FIELD_ID[nm])))
+                for nm in ("u_2", "v_2", "t_2", "ph_2"))
+        assert e < 1e-3
+        assert e >= 0.2 * prev
+        prev = e

@@ -223,13 +223,18 @@ def _interp(x, xp, fp):
 
 def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
                     scalar_median=1.0e-6, scalar_sigma=1.0, noise=0.01,
-                    hodo_radius=15.0, name="supercell"):
+                    hodo_radius=15.0, name="supercell", hypsometric_opt=2):
     """Weisman-Klemp sounding + cos^2 warm bubbles, doubly periodic.
 
     bubbles: list of (xc [m], yc [m], zc [m], rx [m], ry [m], rz [m], dtheta [K]).
+    hypsometric_opt 2 (the reference's default) re-diagnoses al from ph with
+    the log form after the linear hydrostatic integration of the init, which
+    leaves the top layers slightly out of balance; with 1 the re-diagnosis
+    inverts the integration, so a windless, bubble-free state is at rest.
     """
     ide, jde = nx + 1, ny + 1
     cfg = abi.default_config(periodic_x=True, periodic_y=True)
+    cfg.hypsometric_opt = hypsometric_opt
     h = abi.HALO
     nim, njm, nk = ide + 2 * h, jde + 2 * h, kde
     m = eta_metrics(kde)
@@ -317,10 +322,14 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     ph1 = column_ph(al3, mu1_2d)
     # theta -> moist theta (module_initialize_ideal.F:1726-1733)
     tm = (t1 + T0) * (1.0 + (R_V / R_D) * qv3) - T0
-    # start_em.F:790-841 (hypsometric_opt = 2): al from ph, p from the EOS
+    # start_em.F:790-841: al from ph (hypsometric_opt 1 or 2), p from the EOS
     mut = mub + mu1_2d
     al3 = np.zeros_like(tm)
     for k in range(1, kde):
+        if hypsometric_opt == 1:
+            al3[:, k - 1] = -1.0 / ((c1h[k] * mub + c2h[k]) + c1h[k] * mu1_2d) * (
+                alb[k] * (c1h[k] * mu1_2d) + rdnw[k] * (ph1[:, k] - ph1[:, k - 1]))
+            continue
         pfu = c3f[k + 1] * mut + c4f[k + 1] + p_top
         pfd = c3f[k] * mut + c4f[k] + p_top
         phm = c3h[k] * mut + c4h[k] + p_top

@@ -12,9 +12,9 @@
 // per-point arithmetic.
 //
 // Arithmetic: the plain form is compiled with --fmad=false and IEEE division
-// so every expression rounds in the reference's left-to-right order; the
-// only non-bitwise operations against the reference's FP32 build are powf
-// and logf in calc_p_rho_phi (CUDA's implementations, a few ulp).
+// so every expression rounds in the reference's left-to-right order.  The
+// log and pow of calc_p_rho_phi are correctly rounded (ffmath.h), as a
+// correctly rounded libm would give them to the reference's FP32 build.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>

@@ -41,33 +41,39 @@ def peaks():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-# Algorithmic bytes per mass cell of one launch of each kernel family:
+# Algorithmic bytes per mass cell and large step of each kernel family:
 # unique 3-D FP32 arrays read + written by the routine(s) it implements
-# (2-D and 1-D arrays ignored), x 4 B.
-ALG_BYTES_PER_CELL = {
-    "step_prep": (8 + 9) * 4,          # u v w ph phb al alb qv -> ru rv rw ww php alt cqu cqv cqw
-    "rk_tend_u": (12 + 1) * 4,         # u ru rv rw ww ph alt p pb al php cqu (+v) -> ru_tend
-    "rk_tend_v": (12 + 1) * 4,
-    "rk_tend_w": (8 + 2) * 4,          # w ru rv ww p cqw u v -> rw_tend, cqw
-    "rk_tend_t": (5 + 1) * 4,          # t ru rv ww -> t_tend (+ zero extras)
-    "rk_tend_ph": (7 + 1) * 4,         # u v ww ph phb w -> ph_tend
-    "small_step_prep": (16 + 13) * 4,
-    "calc_p_rho_0": (7 + 3) * 4,
-    "calc_coef_w": (2 + 3) * 4,
-    "advance_uv": (14 + 2) * 4,        # u ru_tend v rv_tend p pb ph php alt al cqu cqv -> u v
-    "advance_mu_t": (9 + 3) * 4,       # ww ww1 u u_save v v_save t t_save t_tend -> ww t t_2save
-    "advance_w": (17 + 3) * 4,         # w rw_tend ww t_2ave t_2 t_1 ph ph_1 phb ph_tend c2a cqw alt a alpha gamma -> w ph t_2ave
-    "sumflux_calc_p_rho": (13 + 6) * 4,
-    "small_step_finish": (13 + 6) * 4,
-    "rk_update_scalar_pd": 2 * 4,
-    "advect_scalar_pd": (5 + 1) * 4,   # q q_old ru_m rv_m ww_m -> advect_tend
-    "advect_scalar": (4 + 1) * 4,
-    "rk_update_scalar": (3 + 2) * 4,
-    "calc_p_rho_phi": (6 + 2) * 4,
-    "set_w_surface": 0,
-    "cfl_check": 5 * 4,
-    "bc_fill": 0,
-}
+# (2-D and 1-D arrays ignored) x 4 B x its launches per step (3 RK stages,
+# 7 acoustic steps with 4 sound steps per step).  s_pd / s_all: species
+# advected by the positive-definite scheme / all species.
+def alg_bytes_per_cell_step(phase, s_pd, s_all, n_acoustic=7):
+    s_np = s_all - s_pd
+    per = {
+        "step_prep": 3 * (8 + 9),          # u v w ph phb al alb qv -> ru rv rw ww php alt cqu cqv cqw
+        "rk_tend_u": 3 * (12 + 1),         # u ru rv rw ww ph alt p pb al php cqu (+v) -> ru_tend
+        "rk_tend_v": 3 * (12 + 1),
+        "rk_tend_w": 3 * (8 + 2),          # w ru rv ww p cqw u v -> rw_tend, cqw
+        "rk_tend_t": 3 * (5 + 1),          # t ru rv ww -> t_tend
+        "rk_tend_ph": 3 * (7 + 1),         # u v ww ph phb w -> ph_tend
+        "cfl_check": 3 * 5,
+        "small_step_prep": 3 * (16 + 13),
+        "calc_p_rho_0": 3 * (7 + 3),
+        "calc_coef_w": 3 * (2 + 3),
+        "advance_uv": n_acoustic * (14 + 2),
+        "advance_mu_t": n_acoustic * (9 + 3),
+        "advance_w": n_acoustic * (17 + 3),
+        "sumflux_calc_p_rho": n_acoustic * (13 + 6),
+        "small_step_finish": 3 * (13 + 6),
+        "rk_update_scalar_pd": 2 * s_pd,
+        # stages 1-2: read q (+ q_old at stage 2), write new q (+ q_old at stage 1),
+        # mass fluxes once; stage 3: the species not using the PD scheme
+        "scalar_adv_update": 2 * (3 * s_all + 3) + ((3 * s_np + 3) if s_np else 0),
+        "scalar_pd_update": (3 * s_pd + 3) if s_pd else 0,
+        "calc_p_rho_phi": 3 * (6 + 2),
+        "set_w_surface": 0,
+        "bc_fill": 0,
+    }
+    return 4 * per.get(phase, 0)
 
 
 class ClockSampler:
@@ -264,19 +270,20 @@ def main():
     phases = dom.profile_phases(1)
     launches = dom.launches_per_step()
     hbm, hbm_kind = peaks()
-    dom_name, (dom_ms, dom_n) = max(((k, v) for k, v in phases.items() if k in ALG_BYTES_PER_CELL and
-                                     ALG_BYTES_PER_CELL[k] > 0), key=lambda kv: kv[1][0])
-    alg = ALG_BYTES_PER_CELL[dom_name] * cells
-    achieved = alg / (dom_ms / max(dom_n, 1) / 1e3) / 1e9
+    nsp = case.desc.n_moist + case.desc.n_scalar
+    s_pd = (1 if case.desc.config.moist_adv_opt == 1 else 0) + (case.desc.n_scalar if case.desc.config.scalar_adv_opt == 1 else 0)
+    alg = {k: alg_bytes_per_cell_step(k, s_pd, nsp) * cells for k in phases}
+    dom_name = max((k for k in phases if alg[k] > 0), key=lambda k: phases[k][0])
+    dom_ms, dom_n = phases[dom_name]
+    achieved = alg[dom_name] / (dom_ms / 1e3) / 1e9
+    step_alg = sum(alg.values())
+    step_ms = ms / args.steps
     roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "peak_kind": hbm_kind,
                 "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                "alg_bytes_per_launch": alg, "avg_launch_ms": dom_ms / max(dom_n, 1), "launches_per_step": dom_n,
-                "note": "frac of %s HBM copy bandwidth" % hbm_kind}
-    step_alg = None
-    try:
-        step_alg = {k: (v[0], v[1]) for k, v in phases.items()}
-    except Exception:
-        pass
+                "alg_bytes_per_step": alg[dom_name], "ms_per_step": dom_ms, "launches_per_step": dom_n,
+                "step_alg_bytes": step_alg, "step_achieved": step_alg / (step_ms / 1e3) / 1e9,
+                "step_frac": step_alg / (step_ms / 1e3) / 1e9 / hbm,
+                "note": "frac of %s HBM copy bandwidth; kernel times from CUDA events between launches" % hbm_kind}
 
     # end to end through the C ABI with host buffers (pinned)
     e2e = None
@@ -338,7 +345,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches * args.steps,
             "clocks": clocks,
-            "phases_ms_per_step": {k: round(v[0], 4) for k, v in (step_alg or {}).items()},
+            "phases_ms_per_step": {k: round(v[0], 4) for k, v in phases.items()},
         }
         print(json.dumps(line), flush=True)
     if pg is not None:

@@ -17,12 +17,14 @@
 // correctly rounded libm would give them to the reference's FP32 build.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include "../../include/wrfgpu.h"
 
 namespace wrfgpu {
 
 constexpr int NSPMAX = 16;           // species per member (moist + passive)
+constexpr int TMA_HALO = 4;          // halo of the staged planes
 constexpr int BX = 32, BY = 4;       // thread block: 32 (i) x 4 (j)
 constexpr float G = 9.81f;
 constexpr float R_D = 287.f;
@@ -33,12 +35,19 @@ constexpr float T0 = 300.f;
 constexpr float P0 = 100000.f;
 constexpr float RERADIUS = 1.f / 6370.0e03f;
 
+// Tensor maps (TMA descriptors) of every 3-D field buffer of a member: slot
+// f < WRFGPU_N3D for the fields, WRFGPU_N3D + 3 s + {0, 1, 2} for species s's
+// buffers (first current, old, first spare).  Two boxes per slot: the
+// tile plus a 4-point halo, (TX + 8) x 1 x (TY + 8), and the tile alone.
+constexpr int NMAPSLOT = WRFGPU_N3D + 3 * NSPMAX;
+constexpr int BOX_HALO = 0, BOX_TILE = 1;
+
 // Error word bits (Mem::err): set by kernels, read by the host between steps.
 constexpr unsigned ERR_NONFINITE = 1u;
 constexpr unsigned ERR_CFL = 2u;
 constexpr unsigned ERR_TIMEOUT = 4u;
 
-struct Mem {
+struct alignas(16) Mem {
   int ids, ide, jds, jde, kds, kde;
   int ims, ime, jms, jme, kms, kme;
   int its, ite, jts, jte, kts, kte;
@@ -48,6 +57,11 @@ struct Mem {
   float* f1[WRFGPU_N1D];
   float* q[NSPMAX];       // species current (_2)
   float* qo[NSPMAX];      // species old (_1)
+  float* qa[NSPMAX];      // species spare buffer: the fused update writes the new
+                          // value here and the pair (q, qa) is swapped after the stage
+  int qmap[NSPMAX];       // tensor-map slots of q[s] and qa[s] (swapped with them)
+  int qamap[NSPMAX];
+  const CUtensorMap* tmap;  // this member's tensor maps [NMAPSLOT][2] (device memory)
   double* wd[3];          // FP64 a/alpha/gamma of the mixed-precision form (or null)
   int nsp, n_moist;
   int ns_total;           // acoustic steps per large step
@@ -196,8 +210,113 @@ inline int blocks_for(const int ims, const int ime, const int jms, const int jme
   return nbx * nby * (kind == 3 ? nk : 1);
 }
 
+// The block's member descriptor copied into shared memory.  Kernels then read
+// bounds, strides and field pointers from there: a store to global memory
+// cannot alias it, so they are not reloaded from the global member table
+// after every store.  Every thread of the block must call it (it syncs).
+__device__ __forceinline__ const Mem& block_member(const Mem* mems, int m) {
+  __shared__ Mem s_mem;
+  const int nthr = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int4* src = reinterpret_cast<const int4*>(mems + m);
+  int4* dst = reinterpret_cast<int4*>(&s_mem);
+  for (int w = tid; w < (int)(sizeof(Mem) / 16); w += nthr) dst[w] = __ldg(src + w);
+  __syncthreads();
+  return s_mem;
+}
+
 __device__ __forceinline__ void raise_err(const Mem& m, unsigned bits) {
   if (m.err) atomicOr(m.err, bits);
+}
+
+// ---------------------------------------------------------------------------
+// Tiled column-marching geometry.  A block owns a TX x TY tile of mass
+// columns (i, j) and marches up k; horizontal stencil neighbours are staged
+// per level in shared memory, vertical ones stay in registers.  Tiles cover
+// the computed mass region [its, min(ite, ide-1)] x [jts, min(jte, jde-1)]
+// of each member; `per_tile` blocks per tile (species for the scalar
+// kernels, fastest-varying so the blocks of one tile run together and share
+// the mass fluxes through L2).
+// ---------------------------------------------------------------------------
+constexpr int TX = 32, TY = 8;
+
+// Asynchronous global -> shared copies (cp.async, 4 bytes per element) used
+// to keep several k levels of a tile's planes in flight.
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// TMA tile loads completing on an mbarrier (transaction bytes).
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait for phase `parity` of the barrier; false after ~2^22 polls
+// (seconds), in which case the caller flags ERR_TIMEOUT and carries on.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  const unsigned a = smem_u32(bar);
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+struct TileLaunch {
+  const Mem* mem;
+  const int* block_start;  // [nmem+1] prefix over tiles x per_tile
+  int nmem;
+};
+
+struct TilePos {
+  int m;       // member
+  int i0, j0;  // first column of the tile
+  int sub;     // 0 .. per_tile-1 (species)
+};
+
+__host__ __device__ inline int tiles_x(const Mem& m) {
+  const int itf = m.ite < m.ide - 1 ? m.ite : m.ide - 1;
+  return (itf - m.its + TX) / TX;
+}
+__host__ __device__ inline int tiles_y(const Mem& m) {
+  const int jtf = m.jte < m.jde - 1 ? m.jte : m.jde - 1;
+  return (jtf - m.jts + TY) / TY;
+}
+
+// per_species: one block per (tile, species) instead of one per tile.
+__device__ __forceinline__ TilePos tile_pos(const TileLaunch& L, bool per_species) {
+  TilePos t;
+  const int b = blockIdx.x;
+  t.m = find_member(L.block_start, L.nmem, b);
+  const Mem& m = L.mem[t.m];
+  const int lb = b - __ldg(L.block_start + t.m);
+  const int per = per_species ? m.nsp : 1;
+  const int tile = lb / per;
+  t.sub = lb - tile * per;
+  const int ntx = tiles_x(m);
+  t.i0 = m.its + (tile % ntx) * TX;
+  t.j0 = m.jts + (tile / ntx) * TY;
+  return t;
 }
 
 }  // namespace wrfgpu

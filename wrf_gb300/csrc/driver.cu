@@ -21,6 +21,7 @@
 #include <string>
 #include <algorithm>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include "common.cuh"
 #include "kernels.h"
 #include "../../include/wrfgpu.h"
@@ -46,7 +47,7 @@ enum Phase {
 static const char* PHASE_NAMES[NPHASE] = {
     "step_prep", "bc_fill", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",
     "small_step_prep", "calc_p_rho_0", "calc_coef_w", "advance_uv", "advance_mu_t", "advance_w",
-    "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "advect_scalar_pd", "advect_scalar",
+    "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "scalar_pd_update", "scalar_adv_update",
     "rk_update_scalar", "calc_p_rho_phi", "set_w_surface", "end"};
 
 static int check_desc(const WrfGpuDomainDesc& d) {
@@ -66,6 +67,31 @@ static int check_desc(const WrfGpuDomainDesc& d) {
   return WRFGPU_OK;
 }
 
+// cuTensorMapEncodeTiled from the driver (no link against libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+static int get_tensor_map_encoder() {
+  if (g_encode_tiled) return WRFGPU_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return WRFGPU_E_CUDA;
+  g_encode_tiled = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return WRFGPU_OK;
+}
+// 3-D FP32 field (i fastest, row pitch `pitch` elements), box bx x 1 x by.
+static int encode_field_map(CUtensorMap* out, float* base, size_t ni, size_t pitch, size_t nk, size_t nj, int bx,
+                            int by) {
+  cuuint64_t dims[3] = {(cuuint64_t)ni, (cuuint64_t)nk, (cuuint64_t)nj};
+  cuuint64_t strides[2] = {(cuuint64_t)(pitch * 4), (cuuint64_t)(pitch * nk * 4)};
+  cuuint32_t box[3] = {(cuuint32_t)bx, 1u, (cuuint32_t)by};
+  cuuint32_t es[3] = {1u, 1u, 1u};
+  CUresult r = g_encode_tiled(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? WRFGPU_OK : WRFGPU_E_CUDA;
+}
+
 static int num_sound_steps(const WrfGpuDomainDesc& d) {
   if (d.config.time_step_sound != 0) return d.config.time_step_sound;
   float spacing = std::min((float)d.scalars.dx, (float)d.scalars.dy);
@@ -79,10 +105,14 @@ struct Ensemble {
   std::vector<WrfGpuDomainDesc> descs;
   std::vector<Mem> hm;                 // host copies of the member descriptors
   Mem* d_mems = nullptr;
-  int *d_bs2 = nullptr, *d_bs3 = nullptr;
-  int nb2 = 0, nb3 = 0;
+  int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_sc = nullptr;
+  int nb2 = 0, nb3 = 0, nb_sc = 0;
+  bool capturing = false;
+  int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0;
-  std::vector<size_t> n3, n2, n1;      // element counts per member
+  std::vector<size_t> n3, n2, n1;      // element counts per member (padded rows)
+  std::vector<size_t> ni_, nk_, nj_, pitch_;  // Fortran extents and the padded row pitch
+  CUtensorMap* d_tmaps = nullptr;      // [nmem][NMAPSLOT][2]
   char* pool = nullptr;                // one device allocation for all fields
   size_t pool_bytes = 0;
   float** d_pd_scratch = nullptr;      // per-member limiter scratch pointers
@@ -106,6 +136,23 @@ struct Ensemble {
 
   Launch L2() const { return Launch{d_mems, d_bs2, nmem, 2}; }
   Launch L3() const { return Launch{d_mems, d_bs3, nmem, 3}; }
+  TileLaunch LS() const { return TileLaunch{d_mems, d_bs_sc, nmem}; }
+
+  // The fused scalar update writes the new value into the spare buffer; the
+  // swap kernel exchanges (q, qa) in the device member table and the host
+  // mirror follows, so field access always sees the current buffer.
+  void host_flip() {
+    for (int m = 0; m < nmem; ++m)
+      for (int s = 0; s < hm[m].nsp; ++s) {
+        std::swap(hm[m].q[s], hm[m].qa[s]);
+        std::swap(hm[m].qmap[s], hm[m].qamap[s]);
+      }
+  }
+  void swap_species() {
+    launch_swap_species(d_mems, nmem, stream);
+    host_flip();
+    if (capturing) ++capture_swaps;
+  }
 
   ~Ensemble() {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -114,6 +161,8 @@ struct Ensemble {
     if (d_mems) cudaFree(d_mems);
     if (d_bs2) cudaFree(d_bs2);
     if (d_bs3) cudaFree(d_bs3);
+    if (d_bs_sc) cudaFree(d_bs_sc);
+    if (d_tmaps) cudaFree(d_tmaps);
     if (d_pd_scratch) cudaFree(d_pd_scratch);
     if (d_err) cudaFree(d_err);
     if (d_cfl) cudaFree(d_cfl);
@@ -136,17 +185,21 @@ struct Ensemble {
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
     hm.resize(n); n3.resize(n); n2.resize(n); n1.resize(n);
+    ni_.resize(n); nk_.resize(n); nj_.resize(n); pitch_.resize(n);
     // sizes
     std::vector<size_t> off(n);
     size_t total = 0;
     for (int m = 0; m < n; ++m) {
       const WrfGpuDomainDesc& d = ds[m];
       size_t ni = d.ide + 2 * WRFGPU_HALO, nj = d.jde + 2 * WRFGPU_HALO, nk = d.kde;  // ims..ime, jms..jme
-      n3[m] = ni * nk * nj; n2[m] = ni * nj; n1[m] = nk;
+      // rows padded to a multiple of 4 elements: 16-byte strides for TMA tile loads
+      size_t pitch = (ni + 3) & ~size_t(3);
+      ni_[m] = ni; nk_[m] = nk; nj_[m] = nj; pitch_[m] = pitch;
+      n3[m] = pitch * nk * nj; n2[m] = pitch * nj; n1[m] = nk;
       int nsp = d.n_moist + d.n_scalar;
       size_t b = 0;
       b += (size_t)WRFGPU_N3D * al256(n3[m] * 4);
-      b += (size_t)2 * nsp * al256(n3[m] * 4);
+      b += (size_t)3 * nsp * al256(n3[m] * 4);  // current, old, spare
       b += (size_t)WRFGPU_N2D * al256(n2[m] * 4);
       b += (size_t)WRFGPU_N1D * al256(n1[m] * 4);
       b += al256(n3[m] * 4);  // limiter scratch
@@ -162,7 +215,7 @@ struct Ensemble {
     CK(cudaMalloc(&d_cfl, sizeof(float) * 2 * n));
     CK(cudaMemsetAsync(d_cfl, 0, sizeof(float) * 2 * n, stream));
     std::vector<float*> scr(n);
-    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0);
+    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bss(n + 1, 0);
     for (int m = 0; m < n; ++m) {
       const WrfGpuDomainDesc& d = ds[m];
       Mem& M = hm[m];
@@ -171,11 +224,17 @@ struct Ensemble {
       M.ims = 1 - WRFGPU_HALO; M.ime = d.ide + WRFGPU_HALO; M.jms = 1 - WRFGPU_HALO; M.jme = d.jde + WRFGPU_HALO;
       M.kms = 1; M.kme = d.kde;
       M.its = M.ids; M.ite = M.ide; M.jts = M.jds; M.jte = M.jde; M.kts = M.kds; M.kte = M.kde;
-      M.sk = M.ime - M.ims + 1; M.sj = M.sk * (M.kme - M.kms + 1); M.s2 = M.sk;
+      M.sk = (long long)pitch_[m]; M.sj = M.sk * (M.kme - M.kms + 1); M.s2 = M.sk;
       char* p = pool + off[m];
       for (int f = 0; f < WRFGPU_N3D; ++f) { M.f3[f] = (float*)p; p += al256(n3[m] * 4); }
       M.nsp = d.n_moist + d.n_scalar; M.n_moist = d.n_moist;
-      for (int s = 0; s < M.nsp; ++s) { M.q[s] = (float*)p; p += al256(n3[m] * 4); M.qo[s] = (float*)p; p += al256(n3[m] * 4); }
+      for (int s = 0; s < M.nsp; ++s) {
+        M.q[s] = (float*)p; p += al256(n3[m] * 4);
+        M.qo[s] = (float*)p; p += al256(n3[m] * 4);
+        M.qa[s] = (float*)p; p += al256(n3[m] * 4);
+        M.qmap[s] = WRFGPU_N3D + 3 * s;
+        M.qamap[s] = WRFGPU_N3D + 3 * s + 2;
+      }
       for (int f = 0; f < WRFGPU_N2D; ++f) { M.f2[f] = (float*)p; p += al256(n2[m] * 4); }
       for (int f = 0; f < WRFGPU_N1D; ++f) { M.f1[f] = (float*)p; p += al256(n1[m] * 4); }
       scr[m] = (float*)p; p += al256(n3[m] * 4);
@@ -193,14 +252,42 @@ struct Ensemble {
       ns_max = std::max(ns_max, M.ns_total);
       bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
+      bss[m + 1] = bss[m] + tiles_x(M) * tiles_y(M) * M.nsp;
     }
-    nb2 = bs2[n]; nb3 = bs3[n];
+    nb2 = bs2[n]; nb3 = bs3[n]; nb_sc = bss[n];
+    {  // tensor maps of every 3-D buffer: halo box and tile box
+      int rc = get_tensor_map_encoder();
+      if (rc) return rc;
+      std::vector<CUtensorMap> maps((size_t)n * NMAPSLOT * 2);
+      std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+      for (int m = 0; m < n; ++m) {
+        Mem& M = hm[m];
+        CUtensorMap* mm = maps.data() + (size_t)m * NMAPSLOT * 2;
+        auto enc = [&](int slot, float* base) -> int {
+          int r1 = encode_field_map(&mm[2 * slot + BOX_HALO], base, ni_[m], pitch_[m], nk_[m], nj_[m],
+                                    TX + 2 * TMA_HALO, TY + 2 * TMA_HALO);
+          int r2 = encode_field_map(&mm[2 * slot + BOX_TILE], base, ni_[m], pitch_[m], nk_[m], nj_[m], TX, TY);
+          return r1 ? r1 : r2;
+        };
+        for (int f = 0; f < WRFGPU_N3D; ++f) { rc = enc(f, M.f3[f]); if (rc) return rc; }
+        for (int sp = 0; sp < M.nsp; ++sp) {
+          if ((rc = enc(WRFGPU_N3D + 3 * sp, M.q[sp]))) return rc;
+          if ((rc = enc(WRFGPU_N3D + 3 * sp + 1, M.qo[sp]))) return rc;
+          if ((rc = enc(WRFGPU_N3D + 3 * sp + 2, M.qa[sp]))) return rc;
+        }
+      }
+      CK(cudaMalloc(&d_tmaps, maps.size() * sizeof(CUtensorMap)));
+      CK(cudaMemcpy(d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+      for (int m = 0; m < n; ++m) hm[m].tmap = d_tmaps + (size_t)m * NMAPSLOT * 2;
+    }
     CK(cudaMalloc(&d_mems, sizeof(Mem) * n));
     CK(cudaMemcpyAsync(d_mems, hm.data(), sizeof(Mem) * n, cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_bs2, sizeof(int) * (n + 1)));
     CK(cudaMalloc(&d_bs3, sizeof(int) * (n + 1)));
     CK(cudaMemcpyAsync(d_bs2, bs2.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_bs3, bs3.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_bs_sc, sizeof(int) * (n + 1)));
+    CK(cudaMemcpyAsync(d_bs_sc, bss.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_pd_scratch, sizeof(float*) * n));
     CK(cudaMemcpyAsync(d_pd_scratch, scr.data(), sizeof(float*) * n, cudaMemcpyHostToDevice, stream));
     // map factors default to 1, cosa to 1 (ideal cases); callers overwrite via set_field
@@ -215,17 +302,34 @@ struct Ensemble {
     return WRFGPU_OK;
   }
 
-  float* field_ptr(int m, int id, size_t* count) {
+  // Device buffer of a field and its Fortran shape: `cols` contiguous
+  // elements per row (ime-ims+1, or kme-kms+1 for 1-D), `rows` rows, rows
+  // `pitch` elements apart on the device.  *count = cols * rows (the caller's
+  // contiguous array).
+  float* field_ptr(int m, int id, size_t* count, size_t* cols = nullptr, size_t* rows = nullptr,
+                   size_t* pitch = nullptr) {
     const Mem& M = hm[m];
-    if (id >= 0 && id < WRFGPU_N3D) { *count = n3[m]; return M.f3[id]; }
-    if (id >= WRFGPU_F2D_BASE && id < WRFGPU_F2D_END) { *count = n2[m]; return M.f2[id - WRFGPU_F2D_BASE]; }
-    if (id >= WRFGPU_F1D_BASE && id < WRFGPU_F1D_END) { *count = n1[m]; return M.f1[id - WRFGPU_F1D_BASE]; }
-    if (id >= WRFGPU_SPECIES_BASE && id < WRFGPU_SPECIES_BASE + 2 * M.nsp) {
+    size_t c = 0, r = 0, pt = 0;
+    float* p = nullptr;
+    if (id >= 0 && id < WRFGPU_N3D) { p = M.f3[id]; c = ni_[m]; r = nk_[m] * nj_[m]; pt = pitch_[m]; }
+    else if (id >= WRFGPU_F2D_BASE && id < WRFGPU_F2D_END) { p = M.f2[id - WRFGPU_F2D_BASE]; c = ni_[m]; r = nj_[m]; pt = pitch_[m]; }
+    else if (id >= WRFGPU_F1D_BASE && id < WRFGPU_F1D_END) { p = M.f1[id - WRFGPU_F1D_BASE]; c = nk_[m]; r = 1; pt = c; }
+    else if (id >= WRFGPU_SPECIES_BASE && id < WRFGPU_SPECIES_BASE + 2 * M.nsp) {
       int s = (id - WRFGPU_SPECIES_BASE) / 2, old = (id - WRFGPU_SPECIES_BASE) % 2;
-      *count = n3[m];
-      return old ? M.qo[s] : M.q[s];
+      p = old ? M.qo[s] : M.q[s]; c = ni_[m]; r = nk_[m] * nj_[m]; pt = pitch_[m];
     }
-    *count = 0;
+    *count = c * r;
+    if (cols) *cols = c;
+    if (rows) *rows = r;
+    if (pitch) *pitch = pt;
+    return p;
+  }
+
+  // Spare buffer of a species' current value (null for any other field).
+  float* spare_ptr(int m, int id) {
+    const Mem& M = hm[m];
+    if (id >= WRFGPU_SPECIES_BASE && id < WRFGPU_SPECIES_BASE + 2 * M.nsp && (id - WRFGPU_SPECIES_BASE) % 2 == 0)
+      return M.qa[(id - WRFGPU_SPECIES_BASE) / 2];
     return nullptr;
   }
 
@@ -303,16 +407,11 @@ struct Ensemble {
         for (int s = 0; s < nsp_max; ++s) jo.sp(s, 1, 'p');
         fill(jo);
       }
-      for (int s = 0; s < nsp_max; ++s) {
-        StepArgs as{rk_step, 0, s, 0};
-        if (rk_step == 3) {
-          mark(PH_PD); launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, s, 0}, d_pd_scratch, stream);
-          mark(PH_ADVS); launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, s, 1}, stream);
-        } else {
-          mark(PH_ADVS); launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, s, 0}, stream);
-        }
-        mark(PH_UPDS); launch_update_scalar(l3, nb3, as, stream);
-      }
+      // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
+      // species, fused; the positive-definite scheme at the last stage
+      mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream);
+      if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, rk_step, stream); }
+      swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi(l3, nb3, stream);
       if (rk_step < 3) {
         JobList j;  // rk_phys_bc_dry_2 + species (solve_em.F:3240-3330)
@@ -336,8 +435,13 @@ struct Ensemble {
 
   int build_graph() {
     if (gexec) return WRFGPU_OK;
+    capturing = true;
+    capture_swaps = 0;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     enqueue_step();
+    capturing = false;
+    // nothing ran during capture: undo the host mirror's swaps
+    for (int q = 0; q < capture_swaps; ++q) host_flip();
     CK(cudaStreamEndCapture(stream, &graph));
     CK(cudaGraphInstantiate(&gexec, graph, 0));
     return WRFGPU_OK;
@@ -349,7 +453,10 @@ struct Ensemble {
     } else {
       int rc = build_graph();
       if (rc) return rc;
-      for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(gexec, stream));
+      for (int s = 0; s < nsteps; ++s) {
+        CK(cudaGraphLaunch(gexec, stream));
+        for (int q = 0; q < capture_swaps; ++q) host_flip();
+      }
     }
     CK(cudaGetLastError());
     return WRFGPU_OK;
@@ -440,20 +547,28 @@ long long wrfgpu_field_size(WrfGpuEnsemble* h, int member, int id) {
 
 int wrfgpu_set_field_f32(WrfGpuEnsemble* h, int member, int id, const float* src, long long n) {
   if (!h || member < 0 || member >= h->e.nmem || !src) return WRFGPU_E_ARG;
-  size_t cnt = 0;
-  float* p = h->e.field_ptr(member, id, &cnt);
+  size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
+  float* p = h->e.field_ptr(member, id, &cnt, &cols, &rows, &pitch);
   if (!p || (long long)cnt != n) return WRFGPU_E_ARG;
-  if (cudaMemcpyAsync(p, src, cnt * 4, cudaMemcpyHostToDevice, h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaMemcpy2DAsync(p, pitch * 4, src, cols * 4, cols * 4, rows, cudaMemcpyHostToDevice, h->e.stream) != cudaSuccess)
+    return WRFGPU_E_CUDA;
+  // a species' spare buffer gets the same values, so points the solver never
+  // writes (halo corners, level kde) agree whichever buffer is current
+  if (float* q = h->e.spare_ptr(member, id))
+    if (cudaMemcpy2DAsync(q, pitch * 4, src, cols * 4, cols * 4, rows, cudaMemcpyHostToDevice, h->e.stream) !=
+        cudaSuccess)
+      return WRFGPU_E_CUDA;
   if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
   return WRFGPU_OK;
 }
 
 int wrfgpu_get_field_f32(WrfGpuEnsemble* h, int member, int id, float* dst, long long n) {
   if (!h || member < 0 || member >= h->e.nmem || !dst) return WRFGPU_E_ARG;
-  size_t cnt = 0;
-  float* p = h->e.field_ptr(member, id, &cnt);
+  size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
+  float* p = h->e.field_ptr(member, id, &cnt, &cols, &rows, &pitch);
   if (!p || (long long)cnt != n) return WRFGPU_E_ARG;
-  if (cudaMemcpyAsync(dst, p, cnt * 4, cudaMemcpyDeviceToHost, h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  if (cudaMemcpy2DAsync(dst, cols * 4, p, pitch * 4, cols * 4, rows, cudaMemcpyDeviceToHost, h->e.stream) != cudaSuccess)
+    return WRFGPU_E_CUDA;
   if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
   return WRFGPU_OK;
 }

@@ -33,7 +33,7 @@ __device__ __forceinline__ int bc_src(int t, int n, bool stag, bool periodic, bo
 
 // grid: (blocks per job, jobs, members)
 __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
-  const Mem& m = mems[blockIdx.z];
+  const Mem& m = block_member(mems, blockIdx.z);
   const HaloJob& J = jobs.job[blockIdx.y];
   float* base = J.species >= 0 ? (J.species < m.nsp ? (J.old ? m.qo[J.species] : m.q[J.species]) : nullptr)
                                : (J.kind == 3 ? m.f3[J.id] : m.f2[J.id - WRFGPU_F2D_BASE]);

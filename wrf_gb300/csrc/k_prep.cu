@@ -10,8 +10,8 @@ namespace wrfgpu {
 
 __global__ void __launch_bounds__(BX* BY) k_rk_step_prep(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j;
   const bool px = m.cf.periodic_x, py = m.cf.periodic_y;
   F2 MU = f2(m, WRFGPU_MU_2), MUB = f2(m, WRFGPU_MUB), MUT = f2(m, WRFGPU_MUT), MUU = f2(m, WRFGPU_MUU),

@@ -25,8 +25,8 @@ __device__ __forceinline__ bool mass_pt(const Mem& m, int i, int j) {
 // ------------------------------------------------------------ rk_update_scalar_pd
 __global__ void __launch_bounds__(BX* BY) k_update_scalar_pd(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
   const Stage st = stage_of(m, rk_step);
@@ -53,8 +53,8 @@ __device__ __forceinline__ bool pd_applies(const Mem& m, int species, int rk_ste
 // positive-definite scheme at this stage (module_em.F:1265-1280).
 __global__ void __launch_bounds__(BX* BY) k_advect_scalar(Launch L, int species, int rk_step, int mode) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (species >= m.nsp) return;
   if (mode == 1 && pd_applies(m, species, rk_step)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
@@ -140,8 +140,8 @@ __device__ __forceinline__ void pd_fz(const PDCtx& c, int i, int k, int j, float
 // mode 0: only members whose species uses the positive-definite scheme; mode 2: always.
 __global__ void __launch_bounds__(BX* BY) k_pd_scale(Launch L, int species, int rk_step, int mode, float* const* scratch) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (species >= m.nsp) return;
   if (mode == 0 && !pd_applies(m, species, rk_step)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(BX* BY) k_pd_scale(Launch L, int species, int 
 // Pass 2: divergence of the limited fluxes (z, then x, then y) into advect_tend.
 __global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int rk_step, int mode, float* const* scratch) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (species >= m.nsp) return;
   if (mode == 0 && !pd_applies(m, species, rk_step)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
@@ -209,8 +209,8 @@ __global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int r
 // ------------------------------------------------------------ rk_update_scalar
 __global__ void __launch_bounds__(BX* BY) k_update_scalar(Launch L, int species, int rk_step) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (species >= m.nsp) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
@@ -229,8 +229,8 @@ __global__ void __launch_bounds__(BX* BY) k_update_scalar(Launch L, int species,
 // ------------------------------------------------------------ calc_p_rho_phi
 __global__ void __launch_bounds__(BX* BY) k_calc_p_rho_phi(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
   F3 al = f3(m, WRFGPU_AL), alb = f3(m, WRFGPU_ALB), ph = f3(m, WRFGPU_PH_2), phb = f3(m, WRFGPU_PHB),
@@ -263,8 +263,8 @@ __global__ void __launch_bounds__(BX* BY) k_calc_p_rho_phi(Launch L) {
 // ------------------------------------------------------------ set_w_surface
 __global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j;
   if (!mass_pt(m, i, j)) return;
   const bool px = m.cf.periodic_x, py = m.cf.periodic_y;
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
 // module_big_step_utilities_em.F:2503-2712 (w_damping = 0: diagnostics only).
 __global__ void __launch_bounds__(BX* BY) k_cfl_check(Launch L) {
   BlockPos bp = block_pos(L);
-  const Mem& m = L.mem[bp.m];
+  const Mem& m = block_member(L.mem, bp.m);
   float vmax = 0.f, hmax = 0.f;
   bool bad = false;
   if (bp.valid && mass_pt(m, bp.i, bp.j) && bp.k >= 2 && bp.k <= m.kde - 1) {

@@ -1,0 +1,506 @@
+// Fused scalar transport of the large step: advection and rk_update_scalar
+// in one column-marching pass per species, writing the new scalar into the
+// member's spare buffer (swapped with the current one afterwards).
+//
+//   k_scalar_adv_update  advect_scalar (module_advect_em.F:3394-3650 5th-order
+//                        horizontal, :4306-4333 3rd-order vertical) followed by
+//                        rk_update_scalar (module_em.F:1587-1799), every species
+//                        whose scheme is not the positive-definite one at this stage
+//   k_scalar_pd_update   advect_scalar_pd (module_advect_em.F:6505-6779 fluxes,
+//                        :7595-7645 vertical, limiter :7681-7781, divergence
+//                        :7783-7883) followed by rk_update_scalar, at the last stage
+//
+// Layout: one block per (TX x TY tile of mass columns, species); the block
+// marches k from kts to ktf.  The 3-D inputs of each level (the scalar,
+// the old scalar, ru_m, rv_m) are staged in shared memory as TMA tile loads
+// of the tile plus a 4-point halo, several levels ahead in a ring of slots
+// that complete on mbarriers; every x- and y-face flux is computed once per
+// level into shared memory, vertical stencils live in per-column register
+// windows, and the new value is written once.  The arithmetic of each flux,
+// limiter factor, divergence and update is the reference's, term for term
+// and in its order, so the results are bit-identical to the separate routine
+// kernels of k_scalar.cu.
+//
+// HBM traffic per species and stage (algorithmic): read q, q_old, write the
+// new q (+ q_old at stage 1); the mass fluxes ru_m, rv_m, ww_m are read by
+// the species blocks of a tile back to back and come from L2 after the first.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wrfgpu {
+
+__device__ __forceinline__ bool pd_scheme(const Mem& m, int species, int rk_step) {
+  int adv = species < m.n_moist ? m.cf.moist_adv_opt : m.cf.scalar_adv_opt;
+  return rk_step == m.cf.rk_ord && adv == 1;
+}
+
+// Staged plane: the tile plus a 4-point halo, origin (i0 - 4, j0 - 4).
+constexpr int HW = TX + 2 * TMA_HALO, HH = TY + 2 * TMA_HALO, HPLANE = HW * HH;
+constexpr unsigned HPLANE_BYTES = HPLANE * 4;
+
+// A ring of level slots; each slot holds NPL halo planes and completes on its
+// own mbarrier.  Only thread 0 issues; everyone waits.
+template <int NPL, int NSLOT>
+struct PlaneRing {
+  float* buf;      // [NSLOT][NPL][HH][HW]
+  uint64_t* bar;   // [NSLOT]
+  int kts;
+  __device__ float* plane(int slot, int p) const { return buf + (slot * NPL + p) * HPLANE; }
+  __device__ int slot_of(int k) const { return (k - kts) % NSLOT; }
+  // thread 0: load level k of the NPL fields into its slot
+  __device__ void issue(int k, const CUtensorMap* const* maps, int x0, int z0, int kms) const {
+    const int sl = slot_of(k);
+    fence_proxy_async_smem();
+    mbar_expect_tx(&bar[sl], NPL * HPLANE_BYTES);
+    for (int p = 0; p < NPL; ++p) tma_load_3d(plane(sl, p), maps[p], x0, k - kms, z0, &bar[sl]);
+  }
+  __device__ bool wait(int k) const { return mbar_wait(&bar[slot_of(k)], ((k - kts) / NSLOT) & 1); }
+};
+
+// ------------------------------------------------------------------ non-PD
+constexpr int ADV_RING = 4;  // levels k .. k+3 in flight
+constexpr int ADV_NPL = 3;   // q, ru_m, rv_m
+constexpr size_t ADV_SMEM = (size_t)ADV_RING * ADV_NPL * HPLANE_BYTES + 2 * (TY * (TX + 1) + (TY + 1) * TX) * 4 +
+                            ADV_RING * 8;
+
+__global__ void __launch_bounds__(TX* TY, 4) k_scalar_adv_update(TileLaunch L, int rk_step) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const TilePos tp = tile_pos(L, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int s = tp.sub;
+  if (pd_scheme(m, s, rk_step)) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = tp.i0, j0 = tp.j0;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
+  const int kts = m.kts, kte = m.kte, kme = m.kme;
+
+  PlaneRing<ADV_NPL, ADV_RING> ring;
+  ring.buf = (float*)smem;
+  float* fx_base = ring.buf + ADV_RING * ADV_NPL * HPLANE;          // [2][TY][TX+1]
+  float* fy_base = fx_base + 2 * TY * (TX + 1);                      // [2][TY+1][TX]
+  ring.bar = (uint64_t*)(fy_base + 2 * (TY + 1) * TX);
+  ring.kts = kts;
+  const CUtensorMap* maps[ADV_NPL] = {m.tmap + 2 * m.qmap[s] + BOX_HALO, m.tmap + 2 * WRFGPU_RU_M + BOX_HALO,
+                                      m.tmap + 2 * WRFGPU_RV_M + BOX_HALO};
+  const int x0 = i0 - TMA_HALO - m.ims, z0 = j0 - TMA_HALO - m.jms;
+  if (tid == 0) {
+    for (int q = 0; q < ADV_RING; ++q) mbar_init(&ring.bar[q], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int d = 0; d < ADV_RING - 1 && kts + d <= ktf; ++d) ring.issue(kts + d, maps, x0, z0, m.kms);
+
+  const int i = i0 + tx, j = j0 + ty;
+  const bool own = i <= itf && j <= jtf;
+  const Stage st = stage_of(m, rk_step);
+  F3 fld = f3p(m, m.q[s]), old = f3p(m, m.qo[s]), out = f3p(m, m.qa[s]), rom = f3(m, WRFGPU_WW_M);
+  F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  float msftx = 0.f, msfty = 0.f, muold = 0.f, munew = 0.f;
+  // own-column registers: scalar window fld(k-1 .. k+2), next values of old and rom
+  float wm1 = 0.f, w0 = 0.f, wp1 = 0.f, wp2 = 0.f, old_k = 0.f, rom_k1 = 0.f;
+  if (own) {
+    msftx = f2(m, WRFGPU_MSFTX)(i, j);
+    msfty = f2(m, WRFGPU_MSFTY)(i, j);
+    muold = f2(m, WRFGPU_MU_1)(i, j) + f2(m, WRFGPU_MUB)(i, j);
+    munew = f2(m, WRFGPU_MU_2)(i, j) + f2(m, WRFGPU_MUB)(i, j);
+    w0 = fld(i, kts, j);
+    wp1 = fld(i, kts + 1, j);
+    wp2 = (kts + 2 <= kme) ? fld(i, kts + 2, j) : 0.f;
+    old_k = rk_step == 1 ? 0.f : old(i, kts, j);
+    rom_k1 = rom(i, kts + 1, j);
+  }
+  const float rdx = m.rdx, rdy = m.rdy;
+  float vf_lo = 0.f;  // vf(kts) = 0
+  bool ok = true;
+  for (int k = kts; k <= ktf; ++k) {
+    if (tid == 0 && k + ADV_RING - 1 <= ktf) ring.issue(k + ADV_RING - 1, maps, x0, z0, m.kms);
+    ok = ring.wait(k) && ok;
+    const int sl = ring.slot_of(k);
+    const float* Q = ring.plane(sl, 0);
+    const float* U = ring.plane(sl, 1);
+    const float* V = ring.plane(sl, 2);
+    float* FX = fx_base + (k & 1) * TY * (TX + 1);
+    float* FY = fy_base + (k & 1) * (TY + 1) * TX;
+    // x faces i0 .. i0+TX of rows j0 .. j0+TY-1
+    for (int q = tid; q < TY * (TX + 1); q += TX * TY) {
+      const int r = q / (TX + 1), c = q - r * (TX + 1);
+      const int o = (r + TMA_HALO) * HW + c + TMA_HALO;  // face (i0 + c, j0 + r)
+      const float vel = U[o];
+      FX[q] = vel * flux5(Q[o - 3], Q[o - 2], Q[o - 1], Q[o], Q[o + 1], Q[o + 2], vel);
+    }
+    // y faces j0 .. j0+TY of columns i0 .. i0+TX-1
+    for (int q = tid; q < (TY + 1) * TX; q += TX * TY) {
+      const int r = q / TX, c = q - r * TX;
+      const int o = (r + TMA_HALO) * HW + c + TMA_HALO;
+      const float vel = V[o];
+      FY[q] = vel * flux5(Q[o - 3 * HW], Q[o - 2 * HW], Q[o - HW], Q[o], Q[o + HW], Q[o + 2 * HW], vel);
+    }
+    __syncthreads();
+    if (own) {
+      // prefetch the next level's own-column values
+      const float wp3 = (k + 3 <= kme) ? fld(i, k + 3, j) : 0.f;
+      const float old_n = (rk_step != 1 && k + 1 <= ktf) ? old(i, k + 1, j) : 0.f;
+      const float rom_n = (k + 2 <= kme) ? rom(i, k + 2, j) : 0.f;
+      // vertical flux of the upper face k+1 (lower face kept from the previous level)
+      float vf_hi;
+      const int kk = k + 1;
+      if (kk == kts || kk == kte) vf_hi = 0.f;
+      else if (kk == kts + 1 || kk == ktf) vf_hi = rom_k1 * (fzm(kk) * wp1 + fzp(kk) * w0);
+      else vf_hi = rom_k1 * flux3(wm1, w0, wp1, wp2, -rom_k1);
+      float t = 0.f;
+      t = t - msftx * rdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
+      t = t - msftx * rdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
+      t = t - rdzw(k) * (vf_hi - vf_lo);
+      vf_lo = vf_hi;
+      // rk_update_scalar
+      const float tendency = t * msfty;
+      float q1;
+      if (rk_step == 1) { q1 = w0; old(i, k, j) = q1; }
+      else q1 = old_k;
+      out(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+      // slide
+      wm1 = w0; w0 = wp1; wp1 = wp2; wp2 = wp3;
+      old_k = old_n; rom_k1 = rom_n;
+    }
+  }
+  if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
+}
+
+// ------------------------------------------------------------------ PD
+struct PDPlanes {
+  static constexpr int GW = TX + 4, GH = TY + 4;  // 2-D fields, halo 2
+  static constexpr int SW = TX + 2, SH = TY + 2;  // limiter factors, halo 1
+  static constexpr int XW = TX + 3, XH = TY + 2;  // x faces i0-1 .. i0+TX+1, rows j0-1 .. j0+TY
+  static constexpr int YW = TX + 2, YH = TY + 3;  // y faces j0-1 .. j0+TY+1, columns i0-1 .. i0+TX
+  static constexpr int XN = XW * XH, YN = YW * YH, GN = GW * GH, SN = SW * SH;
+};
+constexpr int PD_RING = 3;   // levels L .. L+2 in flight
+constexpr int PD_NPL = 4;    // q, q_old, ru_m, rv_m
+constexpr int PD_FSLOT = 3;  // face planes kept for three levels
+constexpr size_t PD_SMEM =
+    (size_t)PD_RING * PD_NPL * HPLANE_BYTES +
+    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 4 * PDPlanes::GN + 2 * (PDPlanes::XN + PDPlanes::YN) +
+         2 * PDPlanes::SN) +
+    PD_RING * 8;
+
+// One cell of the limiter region (tile + 1): its column's vertical window.
+struct ZCell {
+  int i, j, sx, sy;
+  bool valid;
+  float mut, mub, mu_old, mx, my;
+  float fm1, f0, fp1, fp2;  // scalar at L-1 .. L+2
+  float fo0, fop1;          // old scalar at L, L+1
+  float hz0, lz0;           // z face L (lower face of level L)
+  float hz1, lz1;           // z face L+1
+  float hzm, lzm;           // z face L-1
+  float fom1;               // old scalar at L-1
+  float romp1;              // ww_m at face L+1
+};
+
+// z face kk = L+1 of a limiter cell (advect_scalar_pd's fqz, fqzl).
+__device__ __forceinline__ void zface(const Mem& m, const ZCell& c, int kk, float dz, float dzdt, float dt, int ktf,
+                                      float* hi, float* lo) {
+  if (kk == 1 || kk == m.kde) { *hi = 0.f; *lo = 0.f; return; }
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP);
+  const float mu = 0.5f * ((c1(kk) * c.mut + c2(kk)) + (c1(kk) * c.mut + c2(kk)));
+  const float vel = c.romp1;
+  const float cr = vel * dt / dz / mu;
+  const float l = mu * dzdt * flux_upwind(c.fo0, c.fop1, cr);
+  float h;
+  if (kk == m.kts + 1 || kk == ktf) h = vel * (fzm(kk) * c.fp1 + fzp(kk) * c.f0);
+  else h = vel * pflux3(c.fm1, c.f0, c.fp1, c.fp2, -vel);
+  *lo = l; *hi = h - l;
+}
+
+__global__ void __launch_bounds__(TX* TY, 2) k_scalar_pd_update(TileLaunch L, int rk_step) {
+  using P = PDPlanes;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const TilePos tp = tile_pos(L, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int s = tp.sub;
+  if (!pd_scheme(m, s, rk_step)) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = tp.i0, j0 = tp.j0;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
+  const int kts = m.kts, kme = m.kme;
+  const Stage st = stage_of(m, rk_step);
+  const float dt = st.dt_rk, rdx = m.rdx, rdy = m.rdy;
+
+  PlaneRing<PD_NPL, PD_RING> ring;
+  ring.buf = (float*)smem;
+  float* p = ring.buf + PD_RING * PD_NPL * HPLANE;
+  float* sXH = p; p += PD_FSLOT * P::XN;
+  float* sXL = p; p += PD_FSLOT * P::XN;
+  float* sYH = p; p += PD_FSLOT * P::YN;
+  float* sYL = p; p += PD_FSLOT * P::YN;
+  float* sMUT = p; p += P::GN;
+  float* sMSX = p; p += P::GN;
+  float* sMSY = p; p += P::GN;
+  float* sCM = p; p += P::GN;   // c1(L) mut + c2(L) of the level being staged
+  float* sDX = p; p += P::XN;   // 2 / (msfty(i) + msfty(i-1)) / rdx
+  float* sDXT = p; p += P::XN;  // dx / dt
+  float* sDY = p; p += P::YN;
+  float* sDYT = p; p += P::YN;
+  float* sSC = p; p += 2 * P::SN;
+  ring.bar = (uint64_t*)p;
+  ring.kts = kts;
+  const CUtensorMap* maps[PD_NPL] = {m.tmap + 2 * m.qmap[s] + BOX_HALO,
+                                     m.tmap + 2 * (WRFGPU_N3D + 3 * s + 1) + BOX_HALO,
+                                     m.tmap + 2 * WRFGPU_RU_M + BOX_HALO, m.tmap + 2 * WRFGPU_RV_M + BOX_HALO};
+  const int x0 = i0 - TMA_HALO - m.ims, z0 = j0 - TMA_HALO - m.jms;
+  if (tid == 0) {
+    for (int q = 0; q < PD_RING; ++q) mbar_init(&ring.bar[q], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int d = 0; d < PD_RING - 1 && kts + d <= ktf; ++d) ring.issue(kts + d, maps, x0, z0, m.kms);
+
+  F3 fld = f3p(m, m.q[s]), fold = f3p(m, m.qo[s]), out = f3p(m, m.qa[s]), rom = f3(m, WRFGPU_WW_M);
+  F2 mut2 = f2(m, WRFGPU_MUTS), msx2 = f2(m, WRFGPU_MSFTX), msy2 = f2(m, WRFGPU_MSFTY);
+  F2 mub2 = f2(m, WRFGPU_MUB), mu1 = f2(m, WRFGPU_MU_1), mu2 = f2(m, WRFGPU_MU_2);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
+  auto in_mem = [&](int ii, int jj) { return ii >= m.ims && ii <= m.ime && jj >= m.jms && jj <= m.jme; };
+  auto xface_ok = [&](int ii, int jj) { return ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1; };
+  auto yface_ok = [&](int ii, int jj) { return ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2; };
+
+  // 2-D planes (halo 2) and the level-independent face metrics
+  for (int q = tid; q < P::GN; q += TX * TY) {
+    const int r = q / P::GW, c = q - r * P::GW;
+    const int ii = i0 - 2 + c, jj = j0 - 2 + r;
+    const bool okm = in_mem(ii, jj);
+    sMUT[q] = okm ? mut2(ii, jj) : 0.f;
+    sMSX[q] = okm ? msx2(ii, jj) : 1.f;
+    sMSY[q] = okm ? msy2(ii, jj) : 1.f;
+  }
+  __syncthreads();
+  for (int q = tid; q < P::XN; q += TX * TY) {
+    const int r = q / P::XW, c = q - r * P::XW;
+    const int g = (r + 1) * P::GW + (c + 1);  // 2-D index of (i0-1+c, j0-1+r)
+    const float dxv = 2.f / (sMSY[g] + sMSY[g - 1]) / rdx;
+    sDX[q] = dxv; sDXT[q] = dxv / dt;
+  }
+  for (int q = tid; q < P::YN; q += TX * TY) {
+    const int r = q / P::YW, c = q - r * P::YW;
+    const int g = (r + 1) * P::GW + (c + 1);
+    const float dyv = 2.f / (sMSX[g] + sMSX[g - P::GW]) / rdy;
+    sDY[q] = dyv; sDYT[q] = dyv / dt;
+  }
+  // limiter cells owned by this thread: its tile column, and one ring cell for tid < 84
+  ZCell zc[2];
+  const int nring = 2 * P::SW + 2 * TY;
+  const int ncell = 1 + (tid < nring ? 1 : 0);
+  for (int q = 0; q < 2; ++q) {
+    ZCell& c = zc[q];
+    if (q == 0) { c.sx = tx + 1; c.sy = ty + 1; }
+    else if (tid < nring) {
+      const int r = tid;
+      if (r < P::SW) { c.sx = r; c.sy = 0; }
+      else if (r < 2 * P::SW) { c.sx = r - P::SW; c.sy = P::SH - 1; }
+      else if (r < 2 * P::SW + TY) { c.sx = 0; c.sy = 1 + (r - 2 * P::SW); }
+      else { c.sx = P::SW - 1; c.sy = 1 + (r - 2 * P::SW - TY); }
+    } else { c.sx = 0; c.sy = 0; }
+    c.i = i0 - 1 + c.sx; c.j = j0 - 1 + c.sy;
+    c.valid = (q < ncell) && c.i >= m.its - 1 && c.i <= itf + 1 && c.j >= m.jts - 1 && c.j <= jtf + 1;
+    c.mut = c.mub = c.mu_old = 0.f; c.mx = c.my = 1.f;
+    c.fm1 = c.f0 = c.fp1 = c.fp2 = c.fo0 = c.fop1 = c.fom1 = c.romp1 = 0.f;
+    c.hz0 = c.lz0 = c.hz1 = c.lz1 = c.hzm = c.lzm = 0.f;
+    if (c.valid) {
+      c.mut = mut2(c.i, c.j); c.mub = mub2(c.i, c.j); c.mu_old = mu1(c.i, c.j);
+      c.mx = msx2(c.i, c.j); c.my = msy2(c.i, c.j);
+      // window for L = kts (f(L-1) unused: face kts+1 is second order); z face kts = 0
+      c.f0 = fld(c.i, kts, c.j);
+      c.fp1 = fld(c.i, kts + 1, c.j);
+      c.fp2 = (kts + 2 <= kme) ? fld(c.i, kts + 2, c.j) : 0.f;
+      c.fo0 = fold(c.i, kts, c.j);
+      c.fop1 = fold(c.i, kts + 1, c.j);
+      c.romp1 = rom(c.i, kts + 1, c.j);
+    }
+  }
+  const int i = i0 + tx, j = j0 + ty;
+  const bool own = i <= itf && j <= jtf;
+  float muold_u = 0.f, munew_u = 0.f, msfty_o = 1.f, msftx_o = 1.f;
+  if (own) {
+    muold_u = mu1(i, j) + mub2(i, j);
+    munew_u = mu2(i, j) + mub2(i, j);
+    msfty_o = msy2(i, j);
+    msftx_o = msx2(i, j);
+  }
+  float sc_m1 = -1.f, sc_0 = -1.f, sc_p1 = -1.f;  // own column factors at levels L-2, L-1, L
+  bool ok = true;
+
+  for (int Lv = kts; Lv <= ktf + 1; ++Lv) {
+    const int slot = Lv & 1;
+    if (Lv <= ktf) {
+      if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
+      const float c1k = c1(Lv), c2k = c2(Lv);
+      for (int q = tid; q < P::GN; q += TX * TY) sCM[q] = c1k * sMUT[q] + c2k;
+      ok = ring.wait(Lv) && ok;
+      __syncthreads();
+      const int rs = ring.slot_of(Lv);
+      const float* F = ring.plane(rs, 0);
+      const float* FO = ring.plane(rs, 1);
+      const float* RU = ring.plane(rs, 2);
+      const float* RV = ring.plane(rs, 3);
+      const int fs = Lv % PD_FSLOT;
+      float* XH = sXH + fs * P::XN; float* XL = sXL + fs * P::XN;
+      float* YH = sYH + fs * P::YN; float* YL = sYL + fs * P::YN;
+      // ---- horizontal faces of level Lv (each once)
+      for (int q = tid; q < P::XN; q += TX * TY) {
+        const int r = q / P::XW, c = q - r * P::XW;
+        float hi = 0.f, lo = 0.f;
+        if (xface_ok(i0 - 1 + c, j0 - 1 + r)) {
+          const int o = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
+          const int g = (r + 1) * P::GW + (c + 1);
+          const float dx = sDX[q];
+          const float mu = 0.5f * (sCM[g] + sCM[g - 1]);
+          const float vel = RU[o];
+          const float cr = vel * dt / dx / mu;
+          lo = mu * sDXT[q] * flux_upwind(FO[o - 1], FO[o], cr);
+          const float h = vel * pflux5(F[o - 3], F[o - 2], F[o - 1], F[o], F[o + 1], F[o + 2], vel);
+          hi = h - lo;
+        }
+        XH[q] = hi; XL[q] = lo;
+      }
+      for (int q = tid; q < P::YN; q += TX * TY) {
+        const int r = q / P::YW, c = q - r * P::YW;
+        float hi = 0.f, lo = 0.f;
+        if (yface_ok(i0 - 1 + c, j0 - 1 + r)) {
+          const int o = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
+          const int g = (r + 1) * P::GW + (c + 1);
+          const float dy = sDY[q];
+          const float mu = 0.5f * (sCM[g] + sCM[g - P::GW]);
+          const float vel = RV[o];
+          const float cr = vel * dt / dy / mu;
+          lo = mu * sDYT[q] * flux_upwind(FO[o - HW], FO[o], cr);
+          const float h = vel * pflux5(F[o - 3 * HW], F[o - 2 * HW], F[o - HW], F[o], F[o + HW], F[o + 2 * HW], vel);
+          hi = h - lo;
+        }
+        YH[q] = hi; YL[q] = lo;
+      }
+      // ---- vertical face Lv+1 of every owned limiter cell
+      {
+        const int kk = Lv + 1;
+        float dz = 0.f, dzdt = 0.f;
+        if (kk > 1 && kk < m.kde) { dz = 2.f / (rdzw(kk) + rdzw(kk - 1)); dzdt = dz / dt; }
+        for (int q = 0; q < 2; ++q) {
+          ZCell& c = zc[q];
+          if (!c.valid) continue;
+          zface(m, c, kk, dz, dzdt, dt, ktf, &c.hz1, &c.lz1);
+        }
+      }
+      __syncthreads();
+      // ---- limiter factor of level Lv (advect_scalar_pd ph_low / flux_out)
+      const float rdzwk = rdzw(Lv);
+      for (int q = 0; q < 2; ++q) {
+        ZCell& c = zc[q];
+        if (!c.valid) continue;
+        const int xo = c.sy * P::XW + c.sx, yo = c.sy * P::YW + c.sx;
+        const float hx0 = XH[xo], hx1 = XH[xo + 1], lx0 = XL[xo], lx1 = XL[xo + 1];
+        const float hy0 = YH[yo], hy1 = YH[yo + P::YW], ly0 = YL[yo], ly1 = YL[yo + P::YW];
+        const float mx = c.mx, my = c.my;
+        const float ph_low = ((c1k * c.mub + c2k) + (c1k * c.mu_old)) * c.fo0 -
+                             dt * (mx * my * (rdx * (lx1 - lx0) + rdy * (ly1 - ly0)) + my * rdzwk * (c.lz1 - c.lz0));
+        const float flux_out = dt * ((mx * my) * (rdx * (fmaxf_f(0.f, hx1) - fminf_f(0.f, hx0)) +
+                                                  rdy * (fmaxf_f(0.f, hy1) - fminf_f(0.f, hy0))) +
+                                     my * rdzwk * (fminf_f(0.f, c.hz1) - fmaxf_f(0.f, c.hz0)));
+        float sc = -1.f;
+        if (flux_out > ph_low) sc = fmaxf_f(0.f, ph_low / (flux_out + 1.e-20f));
+        sSC[slot * P::SN + c.sy * P::SW + c.sx] = sc;
+        if (q == 0) sc_p1 = sc;
+      }
+      __syncthreads();
+    }
+    // ---- divergence + update of level k = Lv - 1
+    const int k = Lv - 1;
+    if (k >= kts && own) {
+      const int fs = k % PD_FSLOT;
+      const float* XH = sXH + fs * P::XN; const float* XL = sXL + fs * P::XN;
+      const float* YH = sYH + fs * P::YN; const float* YL = sYL + fs * P::YN;
+      const float* SC = sSC + (k & 1) * P::SN;
+      const ZCell& c = zc[0];
+      const int xo = c.sy * P::XW + c.sx, yo = c.sy * P::YW + c.sx, so = c.sy * P::SW + c.sx;
+      auto lim = [](float v, float sc) { return sc >= 0.f ? sc * v : v; };
+      float hx0 = XH[xo], hx1 = XH[xo + 1];
+      const float lx0 = XL[xo], lx1 = XL[xo + 1];
+      float hy0 = YH[yo], hy1 = YH[yo + P::YW];
+      const float ly0 = YL[yo], ly1 = YL[yo + P::YW];
+      // z faces k (hzm) and k+1 (hz0) of the own column, as of this iteration
+      float hz0 = c.hzm, hz1 = c.hz0;
+      const float lz0 = c.lzm, lz1 = c.lz0;
+      const float s_own = sc_0;
+      if (hx0 > 0.f) hx0 = lim(hx0, SC[so - 1]); else if (hx0 < 0.f) hx0 = lim(hx0, s_own);
+      if (hx1 > 0.f) hx1 = lim(hx1, s_own); else if (hx1 < 0.f) hx1 = lim(hx1, SC[so + 1]);
+      if (hy0 > 0.f) hy0 = lim(hy0, SC[so - P::SW]); else if (hy0 < 0.f) hy0 = lim(hy0, s_own);
+      if (hy1 > 0.f) hy1 = lim(hy1, s_own); else if (hy1 < 0.f) hy1 = lim(hy1, SC[so + P::SW]);
+      if (k > 1) { if (hz0 < 0.f) hz0 = lim(hz0, sc_m1); else if (hz0 > 0.f) hz0 = lim(hz0, s_own); }
+      if (k + 1 < m.kde) { if (hz1 < 0.f) hz1 = lim(hz1, s_own); else if (hz1 > 0.f) hz1 = lim(hz1, sc_p1); }
+      const float mx = msftx_o;
+      float t = 0.f;
+      t = t - rdzw(k) * (hz1 - hz0 + lz1 - lz0);
+      t = t - mx * (rdx * (hx1 - hx0 + lx1 - lx0));
+      t = t - mx * (rdy * (hy1 - hy0 + ly1 - ly0));
+      // rk_update_scalar (last stage: q1 = q_old)
+      const float tendency = t * msfty_o;
+      const float q1 = c.fom1;
+      out(i, k, j) = ((c1(k) * muold_u + c2(k)) * q1 + dt * tendency) / (c1(k) * munew_u + c2(k));
+    }
+    // ---- slide the windows to level Lv+1 (loads for the next level issued now)
+    sc_m1 = sc_0; sc_0 = sc_p1;
+    for (int q = 0; q < 2; ++q) {
+      ZCell& c = zc[q];
+      if (!c.valid) continue;
+      c.hzm = c.hz0; c.lzm = c.lz0;
+      c.hz0 = c.hz1; c.lz0 = c.lz1;
+      c.fom1 = c.fo0;
+      c.fm1 = c.f0; c.f0 = c.fp1; c.fp1 = c.fp2;
+      c.fp2 = (Lv + 3 <= kme) ? fld(c.i, Lv + 3, c.j) : 0.f;
+      c.fo0 = c.fop1;
+      c.fop1 = (Lv + 2 <= kme) ? fold(c.i, Lv + 2, c.j) : 0.f;
+      c.romp1 = (Lv + 2 <= kme) ? rom(c.i, Lv + 2, c.j) : 0.f;
+    }
+  }
+  if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
+}
+
+// ------------------------------------------------------------------ swap
+// After a fused update: the spare buffer holds the new scalar; exchange it
+// with the current one (pointers and tensor-map slots) in every member's table.
+__global__ void k_swap_species(Mem* mems, int nmem) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  Mem& M = mems[m];
+  for (int s = 0; s < M.nsp; ++s) {
+    float* t = M.q[s];
+    M.q[s] = M.qa[s];
+    M.qa[s] = t;
+    const int tm = M.qmap[s];
+    M.qmap[s] = M.qamap[s];
+    M.qamap[s] = tm;
+  }
+}
+
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_scalar_adv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ADV_SMEM);
+    attr = true;
+  }
+  k_scalar_adv_update<<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+}
+void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_scalar_pd_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PD_SMEM);
+    attr = true;
+  }
+  k_scalar_pd_update<<<nblocks, dim3(TX, TY), PD_SMEM, s>>>(L, rk_step);
+}
+void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
+  k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);
+}
+
+}  // namespace wrfgpu

@@ -22,8 +22,8 @@ constexpr int KMAX = 128;  // column scratch (kde <= KMAX, checked at domain cre
 // ------------------------------------------------------------ small_step_prep
 __global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j;
   const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
   const int k_start = m.kts, k_end = min(m.kte, m.kde - 1), i_endu = m.ite, j_endv = m.jte, kde = m.kde;
@@ -119,8 +119,8 @@ __device__ __forceinline__ void calc_p_rho_point(const Mem& m, int i, int k, int
 
 __global__ void __launch_bounds__(BX* BY) k_calc_p_rho(Launch L, int step) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   if (i < m.its || i > min(m.ite, m.ide - 1) || j < m.jts || j > min(m.jte, m.jde - 1) || k < m.kts ||
       k > min(m.kte, m.kde - 1))
@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(BX* BY) k_calc_p_rho(Launch L, int step) {
 template <typename RC>
 __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j;
   if (i < m.its || i > min(m.ite, m.ide - 1) || j < m.jts || j > min(m.jte, m.jde - 1)) return;
   const Stage st = stage_of(m, rk_step);
@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
 // ------------------------------------------------------------ advance_uv
 __global__ void __launch_bounds__(BX* BY) k_advance_uv(Launch L, int rk_step, int iteration) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (iteration > stage_of(m, rk_step).nsmall) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   const int k_start = m.kts, k_end = m.kte - 1;
@@ -295,8 +295,8 @@ __global__ void __launch_bounds__(BX* BY) k_advance_uv(Launch L, int rk_step, in
 template <typename RC>
 __global__ void __launch_bounds__(BX* BY) k_advance_mu_t(Launch L, int rk_step, int iteration) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (iteration > stage_of(m, rk_step).nsmall) return;
   const int i = bp.i, j = bp.j;
   const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(BX* BY) k_advance_mu_t(Launch L, int rk_step, 
 template <typename RC>
 __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int iteration) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   if (iteration > stage_of(m, rk_step).nsmall) return;
   const int i = bp.i, j = bp.j;
   const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
@@ -475,8 +475,8 @@ __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int
 // ------------------------------------------------------------ sumflux (+ calc_p_rho)
 __global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step, int iteration, int do_p_rho) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   if (i < m.its || i > m.ite || j < m.jts || j > m.jte || k < m.kts || k > m.kte) return;
   const Stage st = stage_of(m, rk_step);
@@ -514,8 +514,8 @@ __global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step,
 // ------------------------------------------------------------ small_step_finish
 __global__ void __launch_bounds__(BX* BY) k_small_step_finish(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j;
   const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
   const int i_endu = m.ite, j_endv = m.jte;

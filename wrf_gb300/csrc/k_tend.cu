@@ -23,8 +23,8 @@ namespace wrfgpu {
 template <int FL>
 __global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   F3 tend = f3(m, WRFGPU_RU_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
@@ -112,8 +112,8 @@ __global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
 template <int FL>
 __global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   F3 tend = f3(m, WRFGPU_RV_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
@@ -205,8 +205,8 @@ __global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
 template <int FL>
 __global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j;
   F3 tend = f3(m, WRFGPU_RW_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte;
@@ -292,8 +292,8 @@ __global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
 template <int FL>
 __global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   F3 tend = f3(m, WRFGPU_T_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
@@ -343,8 +343,8 @@ __global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
 template <int FL>
 __global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
   BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const Mem& m = L.mem[bp.m];
   const int i = bp.i, j = bp.j, k = bp.k;
   F3 tend = f3(m, WRFGPU_PH_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;

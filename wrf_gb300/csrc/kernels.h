@@ -69,4 +69,9 @@ void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_cfl_check(const Launch& L3, int nblocks, cudaStream_t s);
 
+// fused scalar transport (k_scalar_fused.cu): one block per (tile, species)
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s);
+void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s);
+void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s);
+
 }  // namespace wrfgpu

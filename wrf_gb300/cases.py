@@ -314,8 +314,15 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     for (xc, yc, zc, rx, ry, rz, dth) in bubbles:
         xr = (xi - xc) / rx
         yr = (yj - yc) / ry
-        rad = np.sqrt(xr[None, None, :] ** 2 + yr[:, None, None] ** 2 + ((zmass - zc) / rz) ** 2)
-        t1 = t1 + np.where(rad <= 1.0, dth * np.cos(0.5 * math.pi * rad) ** 2, 0.0)
+        # only the columns within the bubble's horizontal radius change
+        iw = np.nonzero(np.abs(xr) <= 1.0)[0]
+        jw = np.nonzero(np.abs(yr) <= 1.0)[0]
+        if iw.size == 0 or jw.size == 0:
+            continue
+        i0, i1, j0, j1 = iw[0], iw[-1] + 1, jw[0], jw[-1] + 1
+        rad = np.sqrt(xr[None, None, i0:i1] ** 2 + yr[j0:j1, None, None] ** 2 +
+                      ((zmass[j0:j1, :, i0:i1] - zc) / rz) ** 2)
+        t1[j0:j1, :, i0:i1] = t1[j0:j1, :, i0:i1] + np.where(rad <= 1.0, dth * np.cos(0.5 * math.pi * rad) ** 2, 0.0)
     if noise > 0:
         t1 = t1 + rng.uniform(-noise, noise, size=t1.shape)
     p3, alt3, al3 = column_p_al(t1, qv3, mu1_2d)

@@ -67,6 +67,10 @@ struct alignas(16) Mem {
   int ns_total;           // acoustic steps per large step
   int pad0;
   float dt, rdx, rdy, cf1, cf2, cf3, cfn, cfn1, epssm, smdiv, emdiv, p_top;
+  // stage constants given explicitly by a routine-level caller (> 0), else
+  // derived from dt and the acoustic step count
+  float dts_fix, dtrk_fix;
+  int nsmall_fix, pad2;
   WrfDynConfig cf;
   unsigned* err;          // per-member error word
   float cfl_limit;        // vertical CFL above which ERR_CFL is raised (<=0: off)
@@ -85,22 +89,34 @@ __host__ __device__ inline Stage stage_of(const Mem& m, int rk_step) {
   if (rk_step == 1) { s.dt_rk = m.dt / 3.f; s.dts_rk = s.dt_rk; s.nsmall = 1; }
   else if (rk_step == 2) { s.dt_rk = 0.5f * m.dt; s.dts_rk = dts; s.nsmall = m.ns_total / 2; }
   else { s.dt_rk = m.dt; s.dts_rk = dts; s.nsmall = m.ns_total; }
+  if (m.dts_fix > 0.f) s.dts_rk = m.dts_fix;
+  if (m.dtrk_fix > 0.f) s.dt_rk = m.dtrk_fix;
+  if (m.nsmall_fix > 0) s.nsmall = m.nsmall_fix;
   return s;
 }
 
 // ---------------------------------------------------------------------------
 // Accessors (Fortran indices)
 // ---------------------------------------------------------------------------
+// ro(): read through the read-only (non-coherent) path, for arrays a kernel
+// never writes: such loads do not alias the kernel's stores, so they can be
+// issued ahead of them instead of waiting behind every store.
 struct F3 {
   float* __restrict__ p; long long sk, sj; int ims, kms, jms;
   __device__ __forceinline__ float& operator()(int i, int k, int j) const {
     return p[(long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj];
+  }
+  __device__ __forceinline__ float ro(int i, int k, int j) const {
+    return __ldg(p + ((long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj));
   }
 };
 struct F2 {
   float* __restrict__ p; long long sj; int ims, jms;
   __device__ __forceinline__ float& operator()(int i, int j) const {
     return p[(long long)(i - ims) + (long long)(j - jms) * sj];
+  }
+  __device__ __forceinline__ float ro(int i, int j) const {
+    return __ldg(p + ((long long)(i - ims) + (long long)(j - jms) * sj));
   }
 };
 struct F1 {

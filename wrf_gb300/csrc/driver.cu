@@ -24,6 +24,10 @@
 #include <cudaTypedefs.h>
 #include "common.cuh"
 #include "kernels.h"
+#include "fcall.h"
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "../../include/wrfgpu.h"
 
 namespace wrfgpu {
@@ -498,6 +502,9 @@ struct Ensemble {
       case 20: launch_update_scalar_pd(l3, nb3, a, stream); break;
       case 21: launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, species, 0}, stream); break;
       case 22: launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, species, 2}, d_pd_scratch, stream); break;
+      // accumulating forms (tendency += ...) for the routine-level C ABI
+      case 121: launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, species, 4}, stream); break;
+      case 122: launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, species, 6}, d_pd_scratch, stream); break;
       case 23: launch_update_scalar(l3, nb3, a, stream); break;
       case 24: launch_calc_p_rho_phi(l3, nb3, stream); break;
       case 25: launch_set_w_surface(l2, nb2, stream); break;
@@ -513,6 +520,108 @@ struct Ensemble {
     return WRFGPU_OK;
   }
 };
+
+// ---------------------------------------------------------------------------
+// Routine-level calls in parity mode: a cached single-member scratch domain
+// per (ide, jde, kde, species); copy in, run one routine, copy out.
+// ---------------------------------------------------------------------------
+static std::mutex g_fmu;
+static std::map<std::tuple<int, int, int, int>, Ensemble*> g_fcache;
+
+int fortran_call(const FCall& c) {
+  for (int q = 0; q < 18; ++q)
+    if (!c.dims[q]) return WRFGPU_E_ARG;
+  const int ids = *c.dims[0], ide = *c.dims[1], jds = *c.dims[2], jde = *c.dims[3], kds = *c.dims[4],
+            kde = *c.dims[5];
+  const int ims = *c.dims[6], ime = *c.dims[7], jms = *c.dims[8], jme = *c.dims[9], kms = *c.dims[10],
+            kme = *c.dims[11];
+  const int its = *c.dims[12], ite = *c.dims[13], jts = *c.dims[14], jte = *c.dims[15], kts = *c.dims[16],
+            kte = *c.dims[17];
+  if (ids != 1 || jds != 1 || kds != 1) return WRFGPU_E_ARG;
+  if (ims != ids - WRFGPU_HALO || ime != ide + WRFGPU_HALO || jms != jds - WRFGPU_HALO || jme != jde + WRFGPU_HALO ||
+      kms != kds || kme != kde)
+    return WRFGPU_E_ARG;
+  if (its != ids || ite != ide || jts != jds || jte != jde || kts != kds || kte != kde) return WRFGPU_E_ARG;
+  if (c.nsp < 1 || c.nsp > NSPMAX) return WRFGPU_E_ARG;
+  std::lock_guard<std::mutex> lock(g_fmu);
+  const auto key = std::make_tuple(ide, jde, kde, c.nsp);
+  Ensemble* e = nullptr;
+  auto it = g_fcache.find(key);
+  if (it != g_fcache.end()) e = it->second;
+  else {
+    WrfGpuDomainDesc d{};
+    d.ide = ide; d.jde = jde; d.kde = kde; d.n_moist = 1; d.n_scalar = c.nsp - 1;
+    d.config = c.cfg;
+    d.config.rk_ord = 3;
+    d.scalars.dt = 1.0; d.scalars.dx = d.scalars.dy = 1.0; d.scalars.rdx = d.scalars.rdy = 1.0;
+    e = new Ensemble();
+    int rc = e->init(&d, 1, WRFGPU_FLAG_NO_GRAPH | WRFGPU_FLAG_NO_CHECKS);
+    if (rc) { delete e; return rc; }
+    g_fcache[key] = e;
+  }
+  Mem& M = e->hm[0];
+  {
+    WrfGpuDomainDesc d = e->descs[0];
+    d.config = c.cfg;
+    int rc = check_desc(d);
+    if (rc) return rc;
+  }
+  M.cf = c.cfg;
+  if (c.rdx > 0.f) M.rdx = c.rdx;
+  if (c.rdy > 0.f) M.rdy = c.rdy;
+  if (c.dt > 0.f) M.dt = c.dt;
+  if (c.epssm >= 0.f) M.epssm = c.epssm;
+  if (c.smdiv >= 0.f) M.smdiv = c.smdiv;
+  if (c.emdiv >= 0.f) M.emdiv = c.emdiv;
+  if (c.have_cf) { M.cf1 = c.cf1; M.cf2 = c.cf2; M.cf3 = c.cf3; }
+  if (c.have_cfn) { M.cfn = c.cfn; M.cfn1 = c.cfn1; }
+  if (c.p_top >= 0.f) M.p_top = c.p_top;
+  M.dts_fix = c.dts > 0.f ? c.dts : 0.f;
+  M.dtrk_fix = c.dtrk > 0.f ? c.dtrk : 0.f;
+  M.nsmall_fix = c.nsmall > 0 ? c.nsmall : 0;
+  CK(cudaMemcpyAsync(e->d_mems, &M, sizeof(Mem), cudaMemcpyHostToDevice, e->stream));
+  // every bound array is copied in, outputs too: points a routine does not
+  // write keep the caller's values, as they would in the caller's array
+  for (const FBind& b : c.binds) {
+    size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
+    float* p = e->field_ptr(0, b.id, &cnt, &cols, &rows, &pitch);
+    if (!p) return WRFGPU_E_ARG;
+    CK(cudaMemcpy2DAsync(p, pitch * 4, b.host, cols * 4, cols * 4, rows, cudaMemcpyHostToDevice, e->stream));
+  }
+  if (c.zero_saves) {
+    for (int f : {WRFGPU_U_SAVE, WRFGPU_V_SAVE, WRFGPU_W_SAVE, WRFGPU_PH_SAVE, WRFGPU_T_SAVE})
+      CK(cudaMemsetAsync(M.f3[f], 0, e->n3[0] * 4, e->stream));
+    for (int f : {WRFGPU_MU_SAVE, WRFGPU_MU_TEND})
+      CK(cudaMemsetAsync(M.f2[f - WRFGPU_F2D_BASE], 0, e->n2[0] * 4, e->stream));
+  }
+  if (c.max_vert_cfl || c.max_horiz_cfl) CK(cudaMemsetAsync(e->d_cfl, 0, sizeof(float) * 2, e->stream));
+  int rc = e->run_routine(c.routine, c.rk_step, c.iteration, c.species);
+  if (rc) return rc;
+  if (c.max_vert_cfl || c.max_horiz_cfl) {
+    launch_cfl_check(e->L3(), e->nb3, e->stream);
+    float cfl[2] = {0.f, 0.f};
+    CK(cudaMemcpyAsync(cfl, e->d_cfl, sizeof(cfl), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (c.max_vert_cfl) *c.max_vert_cfl = cfl[0];
+    if (c.max_horiz_cfl) *c.max_horiz_cfl = cfl[1];
+  }
+  for (const FBind& b : c.binds) {
+    if (!b.out) continue;
+    size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
+    float* p = e->field_ptr(0, b.id, &cnt, &cols, &rows, &pitch);
+    if (!p) return WRFGPU_E_ARG;
+    CK(cudaMemcpy2DAsync(b.host, cols * 4, p, pitch * 4, cols * 4, rows, cudaMemcpyDeviceToHost, e->stream));
+  }
+  CK(cudaStreamSynchronize(e->stream));
+  return WRFGPU_OK;
+}
+
+int fortran_release() {
+  std::lock_guard<std::mutex> lock(g_fmu);
+  for (auto& kv : g_fcache) delete kv.second;
+  g_fcache.clear();
+  return WRFGPU_OK;
+}
 
 }  // namespace wrfgpu
 

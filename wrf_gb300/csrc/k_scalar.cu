@@ -56,19 +56,20 @@ __global__ void __launch_bounds__(BX* BY) k_advect_scalar(Launch L, int species,
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
   if (species >= m.nsp) return;
-  if (mode == 1 && pd_applies(m, species, rk_step)) return;
+  const bool accum = (mode & 4) != 0;  // tendency += (routine-level callers)
+  if ((mode & 3) == 1 && pd_applies(m, species, rk_step)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   F3 tend = f3(m, WRFGPU_ADVECT_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
   const int ktf = min(m.kte, m.kde - 1);
   if (!(mass_pt(m, i, j) && k >= m.kts && k <= ktf)) {
-    if (in_zero) tend(i, k, j) = 0.f;
+    if (in_zero && !accum) tend(i, k, j) = 0.f;
     return;
   }
   F3 fld = f3p(m, m.q[species]), ru = f3(m, WRFGPU_RU_M), rv = f3(m, WRFGPU_RV_M), rom = f3(m, WRFGPU_WW_M);
   F2 msftx = f2(m, WRFGPU_MSFTX);
   F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
-  float t = 0.f;
+  float t = accum ? tend(i, k, j) : 0.f;
   auto fy = [&](int jj) {
     float vel = rv(i, k, jj);
     return vel * flux5(fld(i, k, jj - 3), fld(i, k, jj - 2), fld(i, k, jj - 1), fld(i, k, jj), fld(i, k, jj + 1), fld(i, k, jj + 2), vel);
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(BX* BY) k_pd_scale(Launch L, int species, int 
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
   if (species >= m.nsp) return;
-  if (mode == 0 && !pd_applies(m, species, rk_step)) return;
+  if ((mode & 3) == 0 && !pd_applies(m, species, rk_step)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
   if (i < m.its - 1 || i > itf + 1 || j < m.jts - 1 || j > jtf + 1 || k < m.kts || k > ktf) return;
@@ -170,13 +171,14 @@ __global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int r
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
   if (species >= m.nsp) return;
-  if (mode == 0 && !pd_applies(m, species, rk_step)) return;
+  const bool accum = (mode & 4) != 0;  // tendency += (routine-level callers)
+  if ((mode & 3) == 0 && !pd_applies(m, species, rk_step)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   F3 tend = f3(m, WRFGPU_ADVECT_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
   const int ktf = min(m.kte, m.kde - 1);
   if (!(mass_pt(m, i, j) && k >= m.kts && k <= ktf)) {
-    if (in_zero) tend(i, k, j) = 0.f;
+    if (in_zero && !accum) tend(i, k, j) = 0.f;
     return;
   }
   const Stage st = stage_of(m, rk_step);
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int r
   if (k > 1) { if (hz0 < 0.f) hz0 = lim(hz0, i, k - 1, j); else if (hz0 > 0.f) hz0 = lim(hz0, i, k, j); }
   if (k + 1 < c.kde) { if (hz1 < 0.f) hz1 = lim(hz1, i, k, j); else if (hz1 > 0.f) hz1 = lim(hz1, i, k + 1, j); }
   const float mx = c.msftx(i, j);
-  float t = 0.f;
+  float t = accum ? tend(i, k, j) : 0.f;
   t = t - c.rdzw(k) * (hz1 - hz0 + lz1 - lz0);
   t = t - mx * (c.rdx * (hx1 - hx0 + lx1 - lx0));
   t = t - mx * (c.rdy * (hy1 - hy0 + ly1 - ly0));

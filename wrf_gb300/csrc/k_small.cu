@@ -103,10 +103,10 @@ __device__ __forceinline__ void calc_p_rho_point(const Mem& m, int i, int k, int
      t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE), c2a = f3(m, WRFGPU_C2A), pm1 = f3(m, WRFGPU_PM1);
   F2 mu = f2(m, WRFGPU_MU_2), Mut = f2(m, WRFGPU_MUTS);
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), rdnw = f1(m, WRFGPU_RDNW);
-  const float a = alt(i, k, j), muij = mu(i, j), mutij = Mut(i, j), t1 = t_1(i, k, j);
-  float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (a * (c1h(k) * muij) + rdnw(k) * (ph(i, k + 1, j) - ph(i, k, j)));
+  const float a = alt.ro(i, k, j), muij = mu.ro(i, j), mutij = Mut.ro(i, j), t1 = t_1.ro(i, k, j);
+  float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (a * (c1h(k) * muij) + rdnw(k) * (ph.ro(i, k + 1, j) - ph.ro(i, k, j)));
   al(i, k, j) = alv;
-  float pv = c2a(i, k, j) * (a * (t_2(i, k, j) - (c1h(k) * muij) * t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + t1)) - alv);
+  float pv = c2a.ro(i, k, j) * (a * (t_2.ro(i, k, j) - (c1h(k) * muij) * t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + t1)) - alv);
   if (step == 0) {
     pm1(i, k, j) = pv;
   } else {
@@ -232,29 +232,29 @@ __global__ void __launch_bounds__(BX* BY) k_advance_uv(Launch L, int rk_step, in
     F3 u = f3(m, WRFGPU_U_2), ru_tend = f3(m, WRFGPU_RU_TEND), cqu = f3(m, WRFGPU_CQU);
     F2 muu = f2(m, WRFGPU_MUU), msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY);
     float uv = u(i, k, j);
-    if (i >= i_start_u_tend && i <= i_end_u_tend) uv = uv + dts * ru_tend(i, k, j);
+    if (i >= i_start_u_tend && i <= i_end_u_tend) uv = uv + dts * ru_tend.ro(i, k, j);
     if (i >= i_start_up && i <= i_end_up) {
       const float dx = 1.f / rdx;
-      float mudf_xy = -emdiv * dx * (MUDF(i, j) - MUDF(i - 1, j)) / msfuy(i, j);
-      float dpxy = (msfux(i, j) / msfuy(i, j)) * .5f * rdx * (c1h(k) * muu(i, j) + c2h(k)) *
-                   (((ph(i, k + 1, j) - ph(i - 1, k + 1, j)) + (ph(i, k, j) - ph(i - 1, k, j))) +
-                    (alt(i, k, j) + alt(i - 1, k, j)) * (p(i, k, j) - p(i - 1, k, j)) +
-                    (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
+      float mudf_xy = -emdiv * dx * (MUDF.ro(i, j) - MUDF.ro(i - 1, j)) / msfuy.ro(i, j);
+      float dpxy = (msfux.ro(i, j) / msfuy.ro(i, j)) * .5f * rdx * (c1h(k) * muu.ro(i, j) + c2h(k)) *
+                   (((ph.ro(i, k + 1, j) - ph.ro(i - 1, k + 1, j)) + (ph.ro(i, k, j) - ph.ro(i - 1, k, j))) +
+                    (alt.ro(i, k, j) + alt.ro(i - 1, k, j)) * (p.ro(i, k, j) - p.ro(i - 1, k, j)) +
+                    (al.ro(i, k, j) + al.ro(i - 1, k, j)) * (pb.ro(i, k, j) - pb.ro(i - 1, k, j)));
       auto dpn = [&](int kk) -> float {
         if (kk == kde) {
           if (cf.top_lid)
-            return .5f * (m.cf1 * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) + m.cf2 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)) +
-                          m.cf3 * (p(i - 1, kde - 3, j) + p(i, kde - 3, j)));
+            return .5f * (m.cf1 * (p.ro(i - 1, kde - 1, j) + p.ro(i, kde - 1, j)) + m.cf2 * (p.ro(i - 1, kde - 2, j) + p.ro(i, kde - 2, j)) +
+                          m.cf3 * (p.ro(i - 1, kde - 3, j) + p.ro(i, kde - 3, j)));
           return 0.f;
         }
         if (kk == 1)
-          return .5f * (m.cf1 * (p(i, 1, j) + p(i - 1, 1, j)) + m.cf2 * (p(i, 2, j) + p(i - 1, 2, j)) +
-                        m.cf3 * (p(i, 3, j) + p(i - 1, 3, j)));
-        return .5f * (fnm(kk) * (p(i, kk, j) + p(i - 1, kk, j)) + fnp(kk) * (p(i, kk - 1, j) + p(i - 1, kk - 1, j)));
+          return .5f * (m.cf1 * (p.ro(i, 1, j) + p.ro(i - 1, 1, j)) + m.cf2 * (p.ro(i, 2, j) + p.ro(i - 1, 2, j)) +
+                        m.cf3 * (p.ro(i, 3, j) + p.ro(i - 1, 3, j)));
+        return .5f * (fnm(kk) * (p.ro(i, kk, j) + p.ro(i - 1, kk, j)) + fnp(kk) * (p.ro(i, kk - 1, j) + p.ro(i - 1, kk - 1, j)));
       };
-      dpxy = dpxy + (msfux(i, j) / msfuy(i, j)) * rdx * (php(i, k, j) - php(i - 1, k, j)) *
-                        (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu(i - 1, j)) + (c1h(k) * mu(i, j))));
-      uv = uv - dts * cqu(i, k, j) * dpxy + (c1h(k) * mudf_xy);
+      dpxy = dpxy + (msfux.ro(i, j) / msfuy.ro(i, j)) * rdx * (php.ro(i, k, j) - php.ro(i - 1, k, j)) *
+                        (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu.ro(i - 1, j)) + (c1h(k) * mu.ro(i, j))));
+      uv = uv - dts * cqu.ro(i, k, j) * dpxy + (c1h(k) * mudf_xy);
     }
     u(i, k, j) = uv;
   }
@@ -263,29 +263,29 @@ __global__ void __launch_bounds__(BX* BY) k_advance_uv(Launch L, int rk_step, in
     F3 v = f3(m, WRFGPU_V_2), rv_tend = f3(m, WRFGPU_RV_TEND), cqv = f3(m, WRFGPU_CQV);
     F2 muv = f2(m, WRFGPU_MUV), msfvx = f2(m, WRFGPU_MSFVX), msfvx_inv = f2(m, WRFGPU_MSFVX_INV),
        msfvy = f2(m, WRFGPU_MSFVY);
-    float vv = v(i, k, j) + dts * rv_tend(i, k, j);
+    float vv = v(i, k, j) + dts * rv_tend.ro(i, k, j);
     const float dy = 1.f / rdy;
-    float mudf_xy = -emdiv * dy * (MUDF(i, j) - MUDF(i, j - 1)) * msfvx_inv(i, j);
+    float mudf_xy = -emdiv * dy * (MUDF.ro(i, j) - MUDF.ro(i, j - 1)) * msfvx_inv.ro(i, j);
     if (j >= j_start_vp && j <= j_end_vp) {
-      float dpxy = (msfvy(i, j) / msfvx(i, j)) * .5f * rdy * (c1h(k) * muv(i, j) + c2h(k)) *
-                   (((ph(i, k + 1, j) - ph(i, k + 1, j - 1)) + (ph(i, k, j) - ph(i, k, j - 1))) +
-                    (alt(i, k, j) + alt(i, k, j - 1)) * (p(i, k, j) - p(i, k, j - 1)) +
-                    (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
+      float dpxy = (msfvy.ro(i, j) / msfvx.ro(i, j)) * .5f * rdy * (c1h(k) * muv.ro(i, j) + c2h(k)) *
+                   (((ph.ro(i, k + 1, j) - ph.ro(i, k + 1, j - 1)) + (ph.ro(i, k, j) - ph.ro(i, k, j - 1))) +
+                    (alt.ro(i, k, j) + alt.ro(i, k, j - 1)) * (p.ro(i, k, j) - p.ro(i, k, j - 1)) +
+                    (al.ro(i, k, j) + al.ro(i, k, j - 1)) * (pb.ro(i, k, j) - pb.ro(i, k, j - 1)));
       auto dpn = [&](int kk) -> float {
         if (kk == kde) {
           if (cf.top_lid)
-            return .5f * (m.cf1 * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) + m.cf2 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)) +
-                          m.cf3 * (p(i, kde - 3, j - 1) + p(i, kde - 3, j)));
+            return .5f * (m.cf1 * (p.ro(i, kde - 1, j - 1) + p.ro(i, kde - 1, j)) + m.cf2 * (p.ro(i, kde - 2, j - 1) + p.ro(i, kde - 2, j)) +
+                          m.cf3 * (p.ro(i, kde - 3, j - 1) + p.ro(i, kde - 3, j)));
           return 0.f;
         }
         if (kk == 1)
-          return .5f * (m.cf1 * (p(i, 1, j) + p(i, 1, j - 1)) + m.cf2 * (p(i, 2, j) + p(i, 2, j - 1)) +
-                        m.cf3 * (p(i, 3, j) + p(i, 3, j - 1)));
-        return .5f * (fnm(kk) * (p(i, kk, j) + p(i, kk, j - 1)) + fnp(kk) * (p(i, kk - 1, j) + p(i, kk - 1, j - 1)));
+          return .5f * (m.cf1 * (p.ro(i, 1, j) + p.ro(i, 1, j - 1)) + m.cf2 * (p.ro(i, 2, j) + p.ro(i, 2, j - 1)) +
+                        m.cf3 * (p.ro(i, 3, j) + p.ro(i, 3, j - 1)));
+        return .5f * (fnm(kk) * (p.ro(i, kk, j) + p.ro(i, kk, j - 1)) + fnp(kk) * (p.ro(i, kk - 1, j) + p.ro(i, kk - 1, j - 1)));
       };
-      dpxy = dpxy + (msfvy(i, j) / msfvx(i, j)) * rdy * (php(i, k, j) - php(i, k, j - 1)) *
-                        (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu(i, j - 1)) + (c1h(k) * mu(i, j))));
-      vv = vv - dts * cqv(i, k, j) * dpxy + (c1h(k) * mudf_xy);
+      dpxy = dpxy + (msfvy.ro(i, j) / msfvx.ro(i, j)) * rdy * (php.ro(i, k, j) - php.ro(i, k, j - 1)) *
+                        (rdnw(k) * (dpn(k + 1) - dpn(k)) - .5f * ((c1h(k) * mu.ro(i, j - 1)) + (c1h(k) * mu.ro(i, j))));
+      vv = vv - dts * cqv.ro(i, k, j) * dpxy + (c1h(k) * mudf_xy);
     }
     v(i, k, j) = vv;
   }
@@ -313,25 +313,25 @@ __global__ void __launch_bounds__(BX* BY) k_advance_mu_t(Launch L, int rk_step, 
      msfty = f2(m, WRFGPU_MSFTY);
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), dnw = f1(m, WRFGPU_DNW), fnm = f1(m, WRFGPU_FNM),
      fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW);
-  const float mxy = msftx(i, j) * msfty(i, j);
-  const float muv0 = muv(i, j), muv1 = muv(i, j + 1), muu0 = muu(i, j), muu1 = muu(i + 1, j);
-  const float vi0 = msfvx_inv(i, j), vi1 = msfvx_inv(i, j + 1), uy0 = msfuy(i, j), uy1 = msfuy(i + 1, j);
+  const float mxy = msftx.ro(i, j) * msfty.ro(i, j);
+  const float muv0 = muv.ro(i, j), muv1 = muv.ro(i, j + 1), muu0 = muu.ro(i, j), muu1 = muu.ro(i + 1, j);
+  const float vi0 = msfvx_inv.ro(i, j), vi1 = msfvx_inv.ro(i, j + 1), uy0 = msfuy.ro(i, j), uy1 = msfuy.ro(i + 1, j);
   auto dvdxi = [&](int k) -> float {
-    return mxy * (rdy * ((v(i, k, j + 1) + (c1h(k) * muv1 + c2h(k)) * v_1(i, k, j + 1) * vi1) -
-                         (v(i, k, j) + (c1h(k) * muv0 + c2h(k)) * v_1(i, k, j) * vi0)) +
-                  rdx * ((u(i + 1, k, j) + (c1h(k) * muu1 + c2h(k)) * u_1(i + 1, k, j) / uy1) -
-                         (u(i, k, j) + (c1h(k) * muu0 + c2h(k)) * u_1(i, k, j) / uy0)));
+    return mxy * (rdy * ((v.ro(i, k, j + 1) + (c1h(k) * muv1 + c2h(k)) * v_1.ro(i, k, j + 1) * vi1) -
+                         (v.ro(i, k, j) + (c1h(k) * muv0 + c2h(k)) * v_1.ro(i, k, j) * vi0)) +
+                  rdx * ((u.ro(i + 1, k, j) + (c1h(k) * muu1 + c2h(k)) * u_1.ro(i + 1, k, j) / uy1) -
+                         (u.ro(i, k, j) + (c1h(k) * muu0 + c2h(k)) * u_1.ro(i, k, j) / uy0)));
   };
   RC dmdt = RC(0.);
   for (int k = k_start; k <= k_end; ++k) dmdt = dmdt + (RC)dnw(k) * (RC)dvdxi(k);
-  const float mu_tend = MU_TEND(i, j);
+  const float mu_tend = MU_TEND.ro(i, j);
   float muave = MU(i, j);
   float mu = (float)((RC)MU(i, j) + (RC)dts * (dmdt + (RC)mu_tend));
   MU(i, j) = mu;
   MUDF(i, j) = (float)(dmdt + (RC)mu_tend);
-  MUTS(i, j) = MUT(i, j) + mu;
+  MUTS(i, j) = MUT.ro(i, j) + mu;
   MUAVE(i, j) = .5f * ((1.f + epssm) * mu + (1.f - epssm) * muave);
-  const float my = msfty(i, j);
+  const float my = msfty.ro(i, j);
   // omega by upward recursion, then subtract the saved omega
   RC wwk = (RC)ww(i, 1, j);
   for (int kk = 2; kk <= k_end; ++kk) {
@@ -339,22 +339,22 @@ __global__ void __launch_bounds__(BX* BY) k_advance_mu_t(Launch L, int rk_step, 
     wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(k) * dmdt) + (RC)dvdxi(kk - 1) + ((RC)c1h(k) * (RC)mu_tend)) / (RC)my;
     ww(i, kk, j) = (float)wwk;
   }
-  for (int k = 1; k <= k_end; ++k) ww(i, k, j) = ww(i, k, j) - ww_1(i, k, j);
+  for (int k = 1; k <= k_end; ++k) ww(i, k, j) = ww(i, k, j) - ww_1.ro(i, k, j);
   // theta
   for (int k = 1; k <= k_end; ++k) {
     float tv = t(i, k, j);
     t_ave(i, k, j) = tv;
-    t(i, k, j) = tv + my * dts * ft(i, k, j);
+    t(i, k, j) = tv + my * dts * ft.ro(i, k, j);
   }
-  const float mx = msftx(i, j);
+  const float mx = msftx.ro(i, j);
   auto wdtn = [&](int k) -> float {
     if (k == 1 || k == kde) return 0.f;
-    return ww(i, k, j) * (fnm(k) * t_1(i, k, j) + fnp(k) * t_1(i, k - 1, j));
+    return ww(i, k, j) * (fnm(k) * t_1.ro(i, k, j) + fnp(k) * t_1.ro(i, k - 1, j));
   };
   for (int k = 1; k <= k_end; ++k) {
     t(i, k, j) = t(i, k, j) - dts * my *
-                                  (mx * (.5f * rdy * (v(i, k, j + 1) * (t_1(i, k, j + 1) + t_1(i, k, j)) - v(i, k, j) * (t_1(i, k, j) + t_1(i, k, j - 1))) +
-                                         .5f * rdx * (u(i + 1, k, j) * (t_1(i + 1, k, j) + t_1(i, k, j)) - u(i, k, j) * (t_1(i, k, j) + t_1(i - 1, k, j)))) +
+                                  (mx * (.5f * rdy * (v.ro(i, k, j + 1) * (t_1.ro(i, k, j + 1) + t_1.ro(i, k, j)) - v.ro(i, k, j) * (t_1.ro(i, k, j) + t_1.ro(i, k, j - 1))) +
+                                         .5f * rdx * (u.ro(i + 1, k, j) * (t_1.ro(i + 1, k, j) + t_1.ro(i, k, j)) - u.ro(i, k, j) * (t_1.ro(i, k, j) + t_1.ro(i - 1, k, j)))) +
                                    rdnw(k) * (wdtn(k + 1) - wdtn(k)));
   }
 }
@@ -381,26 +381,26 @@ __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
      fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW), rdn = f1(m, WRFGPU_RDN);
   RC rhs[KMAX + 1];
-  const float msft_inv = 1.f / msfty(i, j);
-  const float my = msfty(i, j), mx = msftx(i, j), mutij = mut(i, j), mua = muave(i, j), mts = muts(i, j);
+  const float msft_inv = 1.f / msfty.ro(i, j);
+  const float my = msfty.ro(i, j), mx = msftx.ro(i, j), mutij = mut.ro(i, j), mua = muave.ro(i, j), mts = muts.ro(i, j);
   rhs[1] = RC(0.);
   for (int k = 1; k <= k_end; ++k) {
-    float ta = .5f * ((1.f + epssm) * t_2(i, k, j) + (1.f - epssm) * t_2ave(i, k, j));
-    ta = (ta + (c1h(k) * mua) * T0) / ((c1h(k) * mts + c2h(k)) * (T0 + t_1(i, k, j)));
+    float ta = .5f * ((1.f + epssm) * t_2.ro(i, k, j) + (1.f - epssm) * t_2ave(i, k, j));
+    ta = (ta + (c1h(k) * mua) * T0) / ((c1h(k) * mts + c2h(k)) * (T0 + t_1.ro(i, k, j)));
     t_2ave(i, k, j) = ta;
-    rhs[k + 1] = (RC)(dts * (ph_tend(i, k + 1, j) + .5f * G * (1.f - epssm) * w(i, k + 1, j)));
+    rhs[k + 1] = (RC)(dts * (ph_tend.ro(i, k + 1, j) + .5f * G * (1.f - epssm) * w(i, k + 1, j)));
   }
   if (m.cf.phi_adv_z == 2) {
     auto wdwn = [&](int kk) {  // kk = k+1
       int k = kk - 1;
-      return rdnw(k) * (ph_1(i, k + 1, j) - ph_1(i, k, j) + phb(i, k + 1, j) - phb(i, k, j));
+      return rdnw(k) * (ph_1.ro(i, k + 1, j) - ph_1.ro(i, k, j) + phb.ro(i, k + 1, j) - phb.ro(i, k, j));
     };
     for (int k = 2; k <= k_end; ++k)
-      rhs[k] = rhs[k] - (RC)(dts * ww(i, k, j) * (fnm(k) * wdwn(k + 1) + fnp(k) * wdwn(k)));
+      rhs[k] = rhs[k] - (RC)(dts * ww.ro(i, k, j) * (fnm(k) * wdwn(k + 1) + fnp(k) * wdwn(k)));
   } else {
     auto wdwn = [&](int kk) {
       int k = kk - 1;
-      return .5f * (ww(i, k + 1, j) + ww(i, k, j)) * rdnw(k) * (ph_1(i, k + 1, j) - ph_1(i, k, j) + phb(i, k + 1, j) - phb(i, k, j));
+      return .5f * (ww.ro(i, k + 1, j) + ww.ro(i, k, j)) * rdnw(k) * (ph_1.ro(i, k + 1, j) - ph_1.ro(i, k, j) + phb.ro(i, k + 1, j) - phb.ro(i, k, j));
     };
     float wd_lo = wdwn(2);
     for (int k = 2; k <= k_end; ++k) {
@@ -415,11 +415,11 @@ __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int
   }
   const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
   RC w1 = (RC)(my * .5f * rdy *
-                   ((ht(i, j + 1) - ht(i, j)) * (cf1 * v(i, 1, j + 1) + cf2 * v(i, 2, j + 1) + cf3 * v(i, 3, j + 1)) +
-                    (ht(i, j) - ht(i, j - 1)) * (cf1 * v(i, 1, j) + cf2 * v(i, 2, j) + cf3 * v(i, 3, j))) +
+                   ((ht.ro(i, j + 1) - ht.ro(i, j)) * (cf1 * v.ro(i, 1, j + 1) + cf2 * v.ro(i, 2, j + 1) + cf3 * v.ro(i, 3, j + 1)) +
+                    (ht.ro(i, j) - ht.ro(i, j - 1)) * (cf1 * v.ro(i, 1, j) + cf2 * v.ro(i, 2, j) + cf3 * v.ro(i, 3, j))) +
                mx * .5f * rdx *
-                   ((ht(i + 1, j) - ht(i, j)) * (cf1 * u(i + 1, 1, j) + cf2 * u(i + 1, 2, j) + cf3 * u(i + 1, 3, j)) +
-                    (ht(i, j) - ht(i - 1, j)) * (cf1 * u(i, 1, j) + cf2 * u(i, 2, j) + cf3 * u(i, 3, j))));
+                   ((ht.ro(i + 1, j) - ht.ro(i, j)) * (cf1 * u.ro(i + 1, 1, j) + cf2 * u.ro(i + 1, 2, j) + cf3 * u.ro(i + 1, 3, j)) +
+                    (ht.ro(i, j) - ht.ro(i - 1, j)) * (cf1 * u.ro(i, 1, j) + cf2 * u.ro(i, 2, j) + cf3 * u.ro(i, 3, j))));
   w(i, 1, j) = (float)w1;
   // explicit part and forward elimination in one upward sweep
   const RC eps1 = RC(1.) + (RC)epssm, eps0 = RC(1.) - (RC)epssm;
@@ -430,16 +430,16 @@ __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int
   auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)d3(m, m.wd[2])(i, k, j) : (RC)f3(m, WRFGPU_GAMMA)(i, k, j); };
   RC wcol[KMAX + 1];
   for (int k = 2; k <= k_end; ++k) {
-    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend(i, k, j) +
-            (RC)msft_inv * (RC)cqw(i, k, j) *
+    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend.ro(i, k, j) +
+            (RC)msft_inv * (RC)cqw.ro(i, k, j) *
                 (+RC(.5) * (RC)dts * (RC)G * (RC)rdn(k) *
-                 ((RC)c2a(i, k, j) * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
+                 ((RC)c2a.ro(i, k, j) * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
                       (eps1 * (rhs[k + 1] - rhs[k]) + eps0 * ((RC)ph(i, k + 1, j) - (RC)ph(i, k, j))) -
-                  (RC)c2a(i, k - 1, j) * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
+                  (RC)c2a.ro(i, k - 1, j) * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
                       (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph(i, k, j) - (RC)ph(i, k - 1, j))))) +
             (RC)dts * (RC)G * (RC)msft_inv *
-                ((RC)rdn(k) * ((RC)c2a(i, k, j) * (RC)alt(i, k, j) * (RC)t_2ave(i, k, j) -
-                               (RC)c2a(i, k - 1, j) * (RC)alt(i, k - 1, j) * (RC)t_2ave(i, k - 1, j)) -
+                ((RC)rdn(k) * ((RC)c2a.ro(i, k, j) * (RC)alt.ro(i, k, j) * (RC)t_2ave(i, k, j) -
+                               (RC)c2a.ro(i, k - 1, j) * (RC)alt.ro(i, k - 1, j) * (RC)t_2ave(i, k - 1, j)) -
                  ((RC)c1f(k) * (RC)mua));
     if (!fp64) wk = (RC)(float)wk;
     wk = (wk - Acoef(k) * wprev) * ALcoef(k);
@@ -449,10 +449,10 @@ __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int
   {
     int k = k_end + 1;
     RC r = (RC)rdnw(k - 1);
-    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend(i, k, j) +
+    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend.ro(i, k, j) +
             (RC)msft_inv * (-RC(.5) * (RC)dts * (RC)G / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) * (r * r) * RC(2.) *
-                                (RC)c2a(i, k - 1, j) * (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph(i, k, j) - (RC)ph(i, k - 1, j))) -
-                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a(i, k - 1, j) * (RC)alt(i, k - 1, j) * (RC)t_2ave(i, k - 1, j) +
+                                (RC)c2a.ro(i, k - 1, j) * (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph(i, k, j) - (RC)ph(i, k - 1, j))) -
+                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a.ro(i, k - 1, j) * (RC)alt.ro(i, k - 1, j) * (RC)t_2ave(i, k - 1, j) +
                                                ((RC)c1f(k) * (RC)mua)));
     if (m.cf.top_lid) wk = RC(0.);
     if (!fp64) wk = (RC)(float)wk;
@@ -492,18 +492,18 @@ __global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step,
   const bool ww_acc = i <= mini && j <= minj;            // k kts..kte
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H);
   if (ru_acc) {
-    rum = rum + f3(m, WRFGPU_U_2)(i, k, j);
+    rum = rum + f3(m, WRFGPU_U_2).ro(i, k, j);
     if (iteration == ns)
-      rum = rum / float(ns) + (c1h(k) * f2(m, WRFGPU_MUU)(i, j) + c2h(k)) * f3(m, WRFGPU_U_SAVE)(i, k, j) / f2(m, WRFGPU_MSFUY)(i, j);
+      rum = rum / float(ns) + (c1h(k) * f2(m, WRFGPU_MUU).ro(i, j) + c2h(k)) * f3(m, WRFGPU_U_SAVE).ro(i, k, j) / f2(m, WRFGPU_MSFUY).ro(i, j);
   }
   if (rv_acc) {
-    rvm = rvm + f3(m, WRFGPU_V_2)(i, k, j);
+    rvm = rvm + f3(m, WRFGPU_V_2).ro(i, k, j);
     if (iteration == ns)
-      rvm = rvm / float(ns) + (c1h(k) * f2(m, WRFGPU_MUV)(i, j) + c2h(k)) * f3(m, WRFGPU_V_SAVE)(i, k, j) * f2(m, WRFGPU_MSFVX_INV)(i, j);
+      rvm = rvm / float(ns) + (c1h(k) * f2(m, WRFGPU_MUV).ro(i, j) + c2h(k)) * f3(m, WRFGPU_V_SAVE).ro(i, k, j) * f2(m, WRFGPU_MSFVX_INV).ro(i, j);
   }
   if (ww_acc) {
-    wwm = wwm + f3(m, WRFGPU_WW)(i, k, j);
-    if (iteration == ns) wwm = wwm / float(ns) + f3(m, WRFGPU_WW1)(i, k, j);
+    wwm = wwm + f3(m, WRFGPU_WW).ro(i, k, j);
+    if (iteration == ns) wwm = wwm / float(ns) + f3(m, WRFGPU_WW1).ro(i, k, j);
   }
   if (iteration == 1 || ru_acc) ru_m(i, k, j) = rum;
   if (iteration == 1 || rv_acc) rv_m(i, k, j) = rvm;

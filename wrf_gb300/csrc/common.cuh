@@ -310,17 +310,19 @@ struct TilePos {
   int sub;     // 0 .. per_tile-1 (species)
 };
 
-__host__ __device__ inline int tiles_x(const Mem& m) {
-  const int itf = m.ite < m.ide - 1 ? m.ite : m.ide - 1;
+// stag: tiles cover the staggered extents [its, ite] x [jts, jte] (u, v and
+// mass points of the same column handled together) instead of the mass ones.
+__host__ __device__ inline int tiles_x(const Mem& m, bool stag = false) {
+  const int itf = stag ? m.ite : (m.ite < m.ide - 1 ? m.ite : m.ide - 1);
   return (itf - m.its + TX) / TX;
 }
-__host__ __device__ inline int tiles_y(const Mem& m) {
-  const int jtf = m.jte < m.jde - 1 ? m.jte : m.jde - 1;
+__host__ __device__ inline int tiles_y(const Mem& m, bool stag = false) {
+  const int jtf = stag ? m.jte : (m.jte < m.jde - 1 ? m.jte : m.jde - 1);
   return (jtf - m.jts + TY) / TY;
 }
 
 // per_species: one block per (tile, species) instead of one per tile.
-__device__ __forceinline__ TilePos tile_pos(const TileLaunch& L, bool per_species) {
+__device__ __forceinline__ TilePos tile_pos(const TileLaunch& L, bool per_species, bool stag = false) {
   TilePos t;
   const int b = blockIdx.x;
   t.m = find_member(L.block_start, L.nmem, b);
@@ -329,7 +331,7 @@ __device__ __forceinline__ TilePos tile_pos(const TileLaunch& L, bool per_specie
   const int per = per_species ? m.nsp : 1;
   const int tile = lb / per;
   t.sub = lb - tile * per;
-  const int ntx = tiles_x(m);
+  const int ntx = tiles_x(m, stag);
   t.i0 = m.its + (tile % ntx) * TX;
   t.j0 = m.jts + (tile / ntx) * TY;
   return t;

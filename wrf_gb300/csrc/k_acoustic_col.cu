@@ -1,0 +1,286 @@
+// Column-marching forms of the acoustic-step kernels used by the fused
+// solver (the routine kernels of k_small.cu stay for routine-level calls).
+//
+// A block owns a TX x TY tile of columns and each thread marches its column
+// up k.  The inputs of level k+1 are loaded into registers before level k
+// is computed and stored, so every thread keeps a whole level of loads in
+// flight instead of waiting behind its own stores (the stores may alias the
+// loads as far as the compiler knows).  The per-point arithmetic is the
+// reference's, in its order: results are bit-identical to k_small.cu.
+//
+//   k_sumflux_p_rho_col  sumflux (module_small_step_em.F:1473-1633) on the
+//                        u, v and w points of the column + calc_p_rho
+//                        (:438-568) on its mass points; tiles cover the
+//                        staggered extents so the u point i = ide and the v
+//                        point j = jde are included.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wrfgpu {
+
+namespace {
+struct SFLevel {
+  float rum, rvm, wwm;      // accumulated mass fluxes (0 at the first iteration)
+  float u, v, ww;           // current u, v, omega
+  float us, vs, ww1;        // linear parts (last iteration only)
+  float ph1, alt, t2, t1, c2a, pm1;  // calc_p_rho inputs (ph at k+1)
+};
+}  // namespace
+
+__global__ void __launch_bounds__(TX* TY) k_sumflux_p_rho_col(TileLaunch L, int rk_step, int iteration) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const Stage st = stage_of(m, rk_step);
+  if (iteration > st.nsmall) return;  // members with fewer acoustic steps
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  const int ns = st.nsmall;
+  const bool first = iteration == 1, last = iteration == ns;
+  const int mini = min(m.ide - 1, m.ite), minj = min(m.jde - 1, m.jte), mink = min(m.kde - 1, m.kte);
+  const int kts = m.kts, kte = m.kte;
+  const bool ucol = j <= minj, vcol = i <= mini, mcol = ucol && vcol;
+  F3 ru_m = f3(m, WRFGPU_RU_M), rv_m = f3(m, WRFGPU_RV_M), ww_m = f3(m, WRFGPU_WW_M);
+  F3 u2 = f3(m, WRFGPU_U_2), v2 = f3(m, WRFGPU_V_2), ww = f3(m, WRFGPU_WW), us = f3(m, WRFGPU_U_SAVE),
+     vs = f3(m, WRFGPU_V_SAVE), ww1 = f3(m, WRFGPU_WW1);
+  F3 al = f3(m, WRFGPU_AL), p = f3(m, WRFGPU_P), ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT),
+     t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE), c2a = f3(m, WRFGPU_C2A), pm1 = f3(m, WRFGPU_PM1);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), rdnw = f1(m, WRFGPU_RDNW);
+  float muu = 0.f, muv = 0.f, msfuy = 1.f, msfvx_inv = 1.f, muij = 0.f, mutij = 0.f;
+  if (last && ucol) { muu = f2(m, WRFGPU_MUU).ro(i, j); msfuy = f2(m, WRFGPU_MSFUY).ro(i, j); }
+  if (last && vcol) { muv = f2(m, WRFGPU_MUV).ro(i, j); msfvx_inv = f2(m, WRFGPU_MSFVX_INV).ro(i, j); }
+  if (mcol) { muij = f2(m, WRFGPU_MU_2).ro(i, j); mutij = f2(m, WRFGPU_MUTS).ro(i, j); }
+  const float smdiv = m.smdiv;
+
+  auto load = [&](int k, SFLevel& v) {
+    const bool ru_acc = ucol && k <= mink, rv_acc = vcol && k <= mink, mass = mcol && k <= mink;
+    v.rum = (!first && ru_acc) ? ru_m(i, k, j) : 0.f;
+    v.rvm = (!first && rv_acc) ? rv_m(i, k, j) : 0.f;
+    v.wwm = (!first && mcol) ? ww_m(i, k, j) : 0.f;
+    v.u = ru_acc ? u2.ro(i, k, j) : 0.f;
+    v.v = rv_acc ? v2.ro(i, k, j) : 0.f;
+    v.ww = mcol ? ww.ro(i, k, j) : 0.f;
+    v.us = (last && ru_acc) ? us.ro(i, k, j) : 0.f;
+    v.vs = (last && rv_acc) ? vs.ro(i, k, j) : 0.f;
+    v.ww1 = (last && mcol) ? ww1.ro(i, k, j) : 0.f;
+    if (mass) {
+      v.ph1 = ph.ro(i, k + 1, j);
+      v.alt = alt.ro(i, k, j); v.t2 = t_2.ro(i, k, j); v.t1 = t_1.ro(i, k, j); v.c2a = c2a.ro(i, k, j);
+      v.pm1 = pm1(i, k, j);
+    } else {
+      v.ph1 = v.alt = v.t2 = v.t1 = v.c2a = v.pm1 = 0.f;
+    }
+  };
+  SFLevel cur, nxt;
+  load(kts, cur);
+  float ph_k = mcol ? ph.ro(i, kts, j) : 0.f;
+  for (int k = kts; k <= kte; ++k) {
+    if (k + 1 <= kte) load(k + 1, nxt);
+    const bool ru_acc = ucol && k <= mink, rv_acc = vcol && k <= mink;
+    // sumflux
+    float rum = cur.rum, rvm = cur.rvm, wwm = cur.wwm;
+    if (ru_acc) {
+      rum = rum + cur.u;
+      if (last) rum = rum / float(ns) + (c1h(k) * muu + c2h(k)) * cur.us / msfuy;
+    }
+    if (rv_acc) {
+      rvm = rvm + cur.v;
+      if (last) rvm = rvm / float(ns) + (c1h(k) * muv + c2h(k)) * cur.vs * msfvx_inv;
+    }
+    if (mcol) {
+      wwm = wwm + cur.ww;
+      if (last) wwm = wwm / float(ns) + cur.ww1;
+    }
+    if (first || ru_acc) ru_m(i, k, j) = rum;
+    if (first || rv_acc) rv_m(i, k, j) = rvm;
+    if (first || mcol) ww_m(i, k, j) = wwm;
+    // calc_p_rho on the mass point
+    if (mcol && k <= mink) {
+      const float a = cur.alt, t1 = cur.t1;
+      float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (a * (c1h(k) * muij) + rdnw(k) * (cur.ph1 - ph_k));
+      al(i, k, j) = alv;
+      float pv = cur.c2a * (a * (cur.t2 - (c1h(k) * muij) * t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + t1)) - alv);
+      if (iteration == 0) {
+        pm1(i, k, j) = pv;
+      } else {
+        const float ptmp = pv;
+        pv = pv + smdiv * (pv - cur.pm1);
+        pm1(i, k, j) = ptmp;
+      }
+      p(i, k, j) = pv;
+      ph_k = cur.ph1;
+    }
+    cur = nxt;
+  }
+}
+
+void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s) {
+  k_sumflux_p_rho_col<<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+}
+
+// ---------------------------------------------------------------------------
+// advance_uv (module_small_step_em.F:654-967) on the u and v points of the
+// column, plus sumflux's accumulation of ru_m / rv_m left to
+// k_sumflux_p_rho_col.  Horizontal neighbours i-1 (u) and j-1 (v) are read
+// directly (L1); p and ph of level k are kept from the previous level.
+// ---------------------------------------------------------------------------
+namespace {
+struct UVLevel {
+  float u, rut, cqu, v, rvt, cqv;  // own u / v point
+  float p1, ph1, pb, php, alt, al;           // (i, j):   p, ph at k+1; the rest at k
+  float p1x, ph1x, pbx, phpx, altx, alx;     // (i-1, j)
+  float p1y, ph1y, pby, phpy, alty, aly;     // (i, j-1)
+};
+}  // namespace
+
+__global__ void __launch_bounds__(TX* TY, 2) k_advance_uv_col(TileLaunch L, int rk_step, int iteration) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const Stage st = stage_of(m, rk_step);
+  if (iteration > st.nsmall) return;
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  const float dts = st.dts_rk;
+  const WrfDynConfig& cf = m.cf;
+  const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, i_endu = m.ite, j_endv = m.jte;
+  int i_start_up = i_start, i_end_up = i_endu, j_start_vp = j_start, j_end_vp = j_endv;
+  if ((cf.open_xs || cf.symmetric_xs) && m.its == m.ids) i_start_up = i_start_up + 1;
+  if ((cf.open_xe || cf.symmetric_xe) && m.ite == m.ide) i_end_up = i_end_up - 1;
+  if ((cf.open_ys || cf.symmetric_ys || cf.polar) && m.jts == m.jds) j_start_vp = j_start_vp + 1;
+  if ((cf.open_ye || cf.symmetric_ye || cf.polar) && m.jte == m.jde) j_end_vp = j_end_vp - 1;
+  int i_start_u_tend = i_start, i_end_u_tend = i_endu, j_start_v_tend = j_start, j_end_v_tend = j_endv;
+  if (cf.symmetric_xs && m.its == m.ids) i_start_u_tend = i_start_u_tend + 1;
+  if (cf.symmetric_xe && m.ite == m.ide) i_end_u_tend = i_end_u_tend - 1;
+  if (cf.symmetric_ys && m.jts == m.jds) j_start_v_tend = j_start_v_tend + 1;
+  if (cf.symmetric_ye && m.jte == m.jde) j_end_v_tend = j_end_v_tend - 1;
+  const bool upt = j >= j_start && j <= min(m.jte, m.jde - 1) && i >= min(i_start_u_tend, i_start_up) &&
+                   i <= max(i_end_u_tend, i_end_up);
+  const bool u_tend = upt && i >= i_start_u_tend && i <= i_end_u_tend;
+  const bool u_pg = upt && i >= i_start_up && i <= i_end_up;
+  const bool vpt = j >= j_start_v_tend && j <= j_end_v_tend && i >= i_start && i <= i_end;
+  const bool v_pg = vpt && j >= j_start_vp && j <= j_end_vp;
+  if (!upt && !vpt) return;
+  F3 p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB), ph = f3(m, WRFGPU_PH_2), php = f3(m, WRFGPU_PHP),
+     alt = f3(m, WRFGPU_ALT), al = f3(m, WRFGPU_AL);
+  F3 u = f3(m, WRFGPU_U_2), ru_tend = f3(m, WRFGPU_RU_TEND), cqu = f3(m, WRFGPU_CQU);
+  F3 v = f3(m, WRFGPU_V_2), rv_tend = f3(m, WRFGPU_RV_TEND), cqv = f3(m, WRFGPU_CQV);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
+     rdnw = f1(m, WRFGPU_RDNW);
+  const float rdx = m.rdx, rdy = m.rdy, emdiv = m.emdiv, cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
+  const int kde = m.kde, k_start = m.kts, k_end = m.kte - 1;
+  // per-column factors (the reference's left-to-right products, split where they start)
+  F2 MU = f2(m, WRFGPU_MU_2), MUDF = f2(m, WRFGPU_MUDF);
+  float ua = 0.f, uc = 0.f, mudf_u = 0.f, muu = 0.f, mu_i = 0.f, mu_im = 0.f;
+  float va = 0.f, vc = 0.f, mudf_v = 0.f, muv = 0.f, mu_jm = 0.f;
+  if (u_pg) {
+    const float msfux = f2(m, WRFGPU_MSFUX).ro(i, j), msfuy = f2(m, WRFGPU_MSFUY).ro(i, j);
+    const float dx = 1.f / rdx;
+    mudf_u = -emdiv * dx * (MUDF.ro(i, j) - MUDF.ro(i - 1, j)) / msfuy;
+    ua = (msfux / msfuy) * .5f * rdx;
+    uc = (msfux / msfuy) * rdx;
+    muu = f2(m, WRFGPU_MUU).ro(i, j);
+    mu_i = MU.ro(i, j); mu_im = MU.ro(i - 1, j);
+  }
+  if (vpt) {
+    const float msfvx_inv = f2(m, WRFGPU_MSFVX_INV).ro(i, j);
+    const float dy = 1.f / rdy;
+    mudf_v = -emdiv * dy * (MUDF.ro(i, j) - MUDF.ro(i, j - 1)) * msfvx_inv;
+    if (v_pg) {
+      const float msfvx = f2(m, WRFGPU_MSFVX).ro(i, j), msfvy = f2(m, WRFGPU_MSFVY).ro(i, j);
+      va = (msfvy / msfvx) * .5f * rdy;
+      vc = (msfvy / msfvx) * rdy;
+      muv = f2(m, WRFGPU_MUV).ro(i, j);
+      mu_i = MU.ro(i, j); mu_jm = MU.ro(i, j - 1);
+    }
+  }
+  const bool need_x = u_pg, need_y = v_pg, need_c = u_pg || v_pg;
+  auto load = [&](int k, UVLevel& d) {
+    d.u = upt ? u(i, k, j) : 0.f;
+    d.rut = u_tend ? ru_tend.ro(i, k, j) : 0.f;
+    d.cqu = u_pg ? cqu.ro(i, k, j) : 0.f;
+    d.v = vpt ? v(i, k, j) : 0.f;
+    d.rvt = vpt ? rv_tend.ro(i, k, j) : 0.f;
+    d.cqv = v_pg ? cqv.ro(i, k, j) : 0.f;
+    const bool top = k + 1 <= kde - 1;  // p exists up to kde-1
+    if (need_c) {
+      d.p1 = top ? p.ro(i, k + 1, j) : 0.f; d.ph1 = ph.ro(i, k + 1, j);
+      d.pb = pb.ro(i, k, j); d.php = php.ro(i, k, j); d.alt = alt.ro(i, k, j); d.al = al.ro(i, k, j);
+    }
+    if (need_x) {
+      d.p1x = top ? p.ro(i - 1, k + 1, j) : 0.f; d.ph1x = ph.ro(i - 1, k + 1, j);
+      d.pbx = pb.ro(i - 1, k, j); d.phpx = php.ro(i - 1, k, j); d.altx = alt.ro(i - 1, k, j); d.alx = al.ro(i - 1, k, j);
+    }
+    if (need_y) {
+      d.p1y = top ? p.ro(i, k + 1, j - 1) : 0.f; d.ph1y = ph.ro(i, k + 1, j - 1);
+      d.pby = pb.ro(i, k, j - 1); d.phpy = php.ro(i, k, j - 1); d.alty = alt.ro(i, k, j - 1); d.aly = al.ro(i, k, j - 1);
+    }
+  };
+  // level k_start values of p and ph, and dpn(k_start) = dpn(1)
+  float p0 = 0.f, ph0 = 0.f, p0x = 0.f, ph0x = 0.f, p0y = 0.f, ph0y = 0.f, dpn_u = 0.f, dpn_v = 0.f;
+  if (need_c) { p0 = p.ro(i, k_start, j); ph0 = ph.ro(i, k_start, j); }
+  if (need_x) {
+    p0x = p.ro(i - 1, k_start, j); ph0x = ph.ro(i - 1, k_start, j);
+    dpn_u = .5f * (cf1 * (p.ro(i, 1, j) + p.ro(i - 1, 1, j)) + cf2 * (p.ro(i, 2, j) + p.ro(i - 1, 2, j)) +
+                   cf3 * (p.ro(i, 3, j) + p.ro(i - 1, 3, j)));
+  }
+  if (need_y) {
+    p0y = p.ro(i, k_start, j - 1); ph0y = ph.ro(i, k_start, j - 1);
+    dpn_v = .5f * (cf1 * (p.ro(i, 1, j) + p.ro(i, 1, j - 1)) + cf2 * (p.ro(i, 2, j) + p.ro(i, 2, j - 1)) +
+                   cf3 * (p.ro(i, 3, j) + p.ro(i, 3, j - 1)));
+  }
+  // top value of dpn (kde): zero unless the lid is rigid
+  float dpn_u_top = 0.f, dpn_v_top = 0.f;
+  if (cf.top_lid) {
+    if (need_x)
+      dpn_u_top = .5f * (cf1 * (p.ro(i - 1, kde - 1, j) + p.ro(i, kde - 1, j)) + cf2 * (p.ro(i - 1, kde - 2, j) + p.ro(i, kde - 2, j)) +
+                         cf3 * (p.ro(i - 1, kde - 3, j) + p.ro(i, kde - 3, j)));
+    if (need_y)
+      dpn_v_top = .5f * (cf1 * (p.ro(i, kde - 1, j - 1) + p.ro(i, kde - 1, j)) + cf2 * (p.ro(i, kde - 2, j - 1) + p.ro(i, kde - 2, j)) +
+                         cf3 * (p.ro(i, kde - 3, j - 1) + p.ro(i, kde - 3, j)));
+  }
+  UVLevel cur, nxt;
+  load(k_start, cur);
+  for (int k = k_start; k <= k_end; ++k) {
+    if (k + 1 <= k_end) load(k + 1, nxt);
+    const int kk = k + 1;
+    // u
+    if (upt) {
+      float uv = cur.u;
+      if (u_tend) uv = uv + dts * cur.rut;
+      float dpn_hi = 0.f;
+      if (u_pg) {
+        dpn_hi = (kk == kde) ? dpn_u_top : .5f * (fnm(kk) * (cur.p1 + cur.p1x) + fnp(kk) * (p0 + p0x));
+        float dpxy = ua * (c1h(k) * muu + c2h(k)) *
+                     (((cur.ph1 - cur.ph1x) + (ph0 - ph0x)) + (cur.alt + cur.altx) * (p0 - p0x) +
+                      (cur.al + cur.alx) * (cur.pb - cur.pbx));
+        dpxy = dpxy + uc * (cur.php - cur.phpx) *
+                          (rdnw(k) * (dpn_hi - dpn_u) - .5f * ((c1h(k) * mu_im) + (c1h(k) * mu_i)));
+        uv = uv - dts * cur.cqu * dpxy + (c1h(k) * mudf_u);
+        dpn_u = dpn_hi;
+      }
+      u(i, k, j) = uv;
+    }
+    // v
+    if (vpt) {
+      float vv = cur.v + dts * cur.rvt;
+      if (v_pg) {
+        const float dpn_hi = (kk == kde) ? dpn_v_top : .5f * (fnm(kk) * (cur.p1 + cur.p1y) + fnp(kk) * (p0 + p0y));
+        float dpxy = va * (c1h(k) * muv + c2h(k)) *
+                     (((cur.ph1 - cur.ph1y) + (ph0 - ph0y)) + (cur.alt + cur.alty) * (p0 - p0y) +
+                      (cur.al + cur.aly) * (cur.pb - cur.pby));
+        dpxy = dpxy + vc * (cur.php - cur.phpy) *
+                          (rdnw(k) * (dpn_hi - dpn_v) - .5f * ((c1h(k) * mu_jm) + (c1h(k) * mu_i)));
+        vv = vv - dts * cur.cqv * dpxy + (c1h(k) * mudf_v);
+        dpn_v = dpn_hi;
+      }
+      v(i, k, j) = vv;
+    }
+    p0 = cur.p1; ph0 = cur.ph1; p0x = cur.p1x; ph0x = cur.ph1x; p0y = cur.p1y; ph0y = cur.ph1y;
+    cur = nxt;
+  }
+}
+
+void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s) {
+  k_advance_uv_col<<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+}
+
+}  // namespace wrfgpu

@@ -74,4 +74,9 @@ void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cud
 void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s);
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s);
 
+// column-marching acoustic kernels (k_acoustic_col.cu): one block per tile
+// of the staggered extents
+void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s);
+void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s);
+
 }  // namespace wrfgpu

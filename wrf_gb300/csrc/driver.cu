@@ -109,8 +109,8 @@ struct Ensemble {
   std::vector<WrfGpuDomainDesc> descs;
   std::vector<Mem> hm;                 // host copies of the member descriptors
   Mem* d_mems = nullptr;
-  int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_sc = nullptr, *d_bs_st = nullptr;
-  int nb2 = 0, nb3 = 0, nb_sc = 0, nb_st = 0;
+  int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_sc = nullptr, *d_bs_st = nullptr, *d_bs_tm = nullptr;
+  int nb2 = 0, nb3 = 0, nb_sc = 0, nb_st = 0, nb_tm = 0;
   bool capturing = false;
   int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0;
@@ -142,6 +142,7 @@ struct Ensemble {
   Launch L3() const { return Launch{d_mems, d_bs3, nmem, 3}; }
   TileLaunch LS() const { return TileLaunch{d_mems, d_bs_sc, nmem}; }
   TileLaunch LST() const { return TileLaunch{d_mems, d_bs_st, nmem}; }  // staggered-extent tiles
+  TileLaunch LTM() const { return TileLaunch{d_mems, d_bs_tm, nmem}; }  // mass-extent tiles
 
   // The fused scalar update writes the new value into the spare buffer; the
   // swap kernel exchanges (q, qa) in the device member table and the host
@@ -168,6 +169,7 @@ struct Ensemble {
     if (d_bs3) cudaFree(d_bs3);
     if (d_bs_sc) cudaFree(d_bs_sc);
     if (d_bs_st) cudaFree(d_bs_st);
+    if (d_bs_tm) cudaFree(d_bs_tm);
     if (d_tmaps) cudaFree(d_tmaps);
     if (d_pd_scratch) cudaFree(d_pd_scratch);
     if (d_err) cudaFree(d_err);
@@ -221,7 +223,7 @@ struct Ensemble {
     CK(cudaMalloc(&d_cfl, sizeof(float) * 2 * n));
     CK(cudaMemsetAsync(d_cfl, 0, sizeof(float) * 2 * n, stream));
     std::vector<float*> scr(n);
-    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bss(n + 1, 0), bst(n + 1, 0);
+    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bss(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0);
     for (int m = 0; m < n; ++m) {
       const WrfGpuDomainDesc& d = ds[m];
       Mem& M = hm[m];
@@ -260,8 +262,9 @@ struct Ensemble {
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
       bss[m + 1] = bss[m] + tiles_x(M) * tiles_y(M) * M.nsp;
       bst[m + 1] = bst[m] + tiles_x(M, true) * tiles_y(M, true);
+      btm[m + 1] = btm[m] + tiles_x(M) * tiles_y(M);
     }
-    nb2 = bs2[n]; nb3 = bs3[n]; nb_sc = bss[n]; nb_st = bst[n];
+    nb2 = bs2[n]; nb3 = bs3[n]; nb_sc = bss[n]; nb_st = bst[n]; nb_tm = btm[n];
     {  // tensor maps of every 3-D buffer: halo box and tile box
       int rc = get_tensor_map_encoder();
       if (rc) return rc;
@@ -297,6 +300,8 @@ struct Ensemble {
     CK(cudaMemcpyAsync(d_bs_sc, bss.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_bs_st, sizeof(int) * (n + 1)));
     CK(cudaMemcpyAsync(d_bs_st, bst.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_bs_tm, sizeof(int) * (n + 1)));
+    CK(cudaMemcpyAsync(d_bs_tm, btm.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_pd_scratch, sizeof(float*) * n));
     CK(cudaMemcpyAsync(d_pd_scratch, scr.data(), sizeof(float*) * n, cudaMemcpyHostToDevice, stream));
     // map factors default to 1, cosa to 1 (ideal cases); callers overwrite via set_field
@@ -397,8 +402,8 @@ struct Ensemble {
       for (int it = 1; it <= nsmall_max; ++it) {
         StepArgs ai{rk_step, it, 0, 0};
         mark(PH_AUV); launch_advance_uv_col(LST(), nb_st, rk_step, it, stream);
-        mark(PH_AMUT); launch_advance_mu_t(l2, nb2, ai, fp64, stream);
-        mark(PH_AW); launch_advance_w(l2, nb2, ai, fp64, stream);
+        mark(PH_AMUT); launch_advance_mu_t_col(LTM(), nb_tm, rk_step, it, fp64, stream);
+        mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream);
         mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream);
         JobList j;  // solve_em.F:1659-1716
         j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_P, 'p');

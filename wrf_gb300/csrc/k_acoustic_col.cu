@@ -283,4 +283,259 @@ void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int it
   k_advance_uv_col<<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
+
+
+// ---------------------------------------------------------------------------
+// advance_mu_t (module_small_step_em.F:969-1175), one thread per mass column:
+// pass 1 the column divergence (kept per level) and its sum, then mu, and
+// pass 2 omega by upward recursion and theta.  RC: accumulation type of the
+// column sum and the recursion (float: the reference; double: mixed form).
+// ---------------------------------------------------------------------------
+constexpr int KCOL = 129;  // column scratch (kde <= 128)
+
+template <typename RC>
+__global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int rk_step, int iteration) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const Stage st = stage_of(m, rk_step);
+  if (iteration > st.nsmall) return;
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  const int i_end = min(m.ite, m.ide - 1), j_end = min(m.jte, m.jde - 1);
+  if (i > i_end || j > j_end) return;
+  const int k_start = m.kts, k_end = m.kte - 1, kde = m.kde;
+  const float dts = st.dts_rk, epssm = m.epssm, rdx = m.rdx, rdy = m.rdy;
+  F3 ww = f3(m, WRFGPU_WW), ww_1 = f3(m, WRFGPU_WW1), u = f3(m, WRFGPU_U_2), u_1 = f3(m, WRFGPU_U_SAVE),
+     v = f3(m, WRFGPU_V_2), v_1 = f3(m, WRFGPU_V_SAVE), t = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE),
+     t_ave = f3(m, WRFGPU_T_2SAVE), ft = f3(m, WRFGPU_T_TEND);
+  F2 MU = f2(m, WRFGPU_MU_2), MUT = f2(m, WRFGPU_MUT), MUAVE = f2(m, WRFGPU_MUAVE), MUTS = f2(m, WRFGPU_MUTS),
+     muu = f2(m, WRFGPU_MUU), muv = f2(m, WRFGPU_MUV), MUDF = f2(m, WRFGPU_MUDF), MU_TEND = f2(m, WRFGPU_MU_TEND),
+     msfuy = f2(m, WRFGPU_MSFUY), msfvx_inv = f2(m, WRFGPU_MSFVX_INV), msftx = f2(m, WRFGPU_MSFTX),
+     msfty = f2(m, WRFGPU_MSFTY);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), dnw = f1(m, WRFGPU_DNW), fnm = f1(m, WRFGPU_FNM),
+     fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW);
+  const float mxy = msftx.ro(i, j) * msfty.ro(i, j);
+  const float muv0 = muv.ro(i, j), muv1 = muv.ro(i, j + 1), muu0 = muu.ro(i, j), muu1 = muu.ro(i + 1, j);
+  const float vi0 = msfvx_inv.ro(i, j), vi1 = msfvx_inv.ro(i, j + 1), uy0 = msfuy.ro(i, j), uy1 = msfuy.ro(i + 1, j);
+  // pass 1: dvdxi(k) and dmdt
+  struct D1 { float v1, v0, vo1, vo0, u1, u0, uo1, uo0; };
+  auto load1 = [&](int k, D1& d) {
+    d.v1 = v.ro(i, k, j + 1); d.vo1 = v_1.ro(i, k, j + 1); d.v0 = v.ro(i, k, j); d.vo0 = v_1.ro(i, k, j);
+    d.u1 = u.ro(i + 1, k, j); d.uo1 = u_1.ro(i + 1, k, j); d.u0 = u.ro(i, k, j); d.uo0 = u_1.ro(i, k, j);
+  };
+  float dv[KCOL];
+  RC dmdt = RC(0.);
+  {
+    D1 cur, nxt;
+    load1(k_start, cur);
+    for (int k = k_start; k <= k_end; ++k) {
+      if (k + 1 <= k_end) load1(k + 1, nxt);
+      const float d = mxy * (rdy * ((cur.v1 + (c1h(k) * muv1 + c2h(k)) * cur.vo1 * vi1) -
+                                    (cur.v0 + (c1h(k) * muv0 + c2h(k)) * cur.vo0 * vi0)) +
+                             rdx * ((cur.u1 + (c1h(k) * muu1 + c2h(k)) * cur.uo1 / uy1) -
+                                    (cur.u0 + (c1h(k) * muu0 + c2h(k)) * cur.uo0 / uy0)));
+      dv[k] = d;
+      dmdt = dmdt + (RC)dnw(k) * (RC)d;
+      cur = nxt;
+    }
+  }
+  const float mu_tend = MU_TEND.ro(i, j);
+  const float muave = MU(i, j);
+  const float mu = (float)((RC)muave + (RC)dts * (dmdt + (RC)mu_tend));
+  MU(i, j) = mu;
+  MUDF(i, j) = (float)(dmdt + (RC)mu_tend);
+  MUTS(i, j) = MUT.ro(i, j) + mu;
+  MUAVE(i, j) = .5f * ((1.f + epssm) * mu + (1.f - epssm) * muave);
+  const float my = msfty.ro(i, j), mx = msftx.ro(i, j);
+  // pass 2: omega (recursion one level ahead of theta) and theta
+  struct D2 { float ww1, t, ft, t1, t1xm, t1xp, t1ym, t1yp, u0, u1, v0, v1; };
+  auto load2 = [&](int k, D2& d) {
+    d.ww1 = ww_1.ro(i, k, j); d.t = t(i, k, j); d.ft = ft.ro(i, k, j);
+    d.t1 = t_1.ro(i, k, j); d.t1xm = t_1.ro(i - 1, k, j); d.t1xp = t_1.ro(i + 1, k, j);
+    d.t1ym = t_1.ro(i, k, j - 1); d.t1yp = t_1.ro(i, k, j + 1);
+    d.u0 = u.ro(i, k, j); d.u1 = u.ro(i + 1, k, j); d.v0 = v.ro(i, k, j); d.v1 = v.ro(i, k, j + 1);
+  };
+  RC wwk = (RC)ww(i, 1, j);
+  // final omega of level 1 (the recursion starts from the unchanged ww(1))
+  float wwf_k = ww(i, 1, j) - ww_1.ro(i, 1, j);
+  float wdtn_lo = 0.f;  // wdtn(1) = 0
+  D2 cur, nxt;
+  load2(k_start, cur);
+  for (int k = k_start; k <= k_end; ++k) {
+    if (k + 1 <= k_end) load2(k + 1, nxt);
+    // omega of level k+1 (recursion from level k), needed by wdtn(k+1)
+    float wwf_kp1 = 0.f;
+    if (k + 1 <= k_end) {
+      const int kk = k + 1, kl = kk - 1;
+      wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(kl) * dmdt) + (RC)dv[kk - 1] + ((RC)c1h(kl) * (RC)mu_tend)) / (RC)my;
+      wwf_kp1 = (float)wwk - nxt.ww1;
+    }
+    ww(i, k, j) = wwf_k;
+    // theta of level k
+    const float tv = cur.t;
+    t_ave(i, k, j) = tv;
+    float tt = tv + my * dts * cur.ft;
+    const float wdtn_hi = (k + 1 == kde) ? 0.f : wwf_kp1 * (fnm(k + 1) * (k + 1 <= k_end ? nxt.t1 : 0.f) + fnp(k + 1) * cur.t1);
+    tt = tt - dts * my *
+                  (mx * (.5f * rdy * (cur.v1 * (cur.t1yp + cur.t1) - cur.v0 * (cur.t1 + cur.t1ym)) +
+                         .5f * rdx * (cur.u1 * (cur.t1xp + cur.t1) - cur.u0 * (cur.t1 + cur.t1xm))) +
+                   rdnw(k) * (wdtn_hi - wdtn_lo));
+    t(i, k, j) = tt;
+    wdtn_lo = wdtn_hi;
+    wwf_k = wwf_kp1;
+    cur = nxt;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// advance_w (module_small_step_em.F:1178-1469), one thread per mass column:
+// pass 1 (up) t_2ave and the geopotential right-hand side, pass 2 (up) the
+// explicit w and forward elimination, pass 3 (down) back substitution and
+// the geopotential update.  RC as above (the mixed form keeps a, alpha,
+// gamma in FP64).
+// ---------------------------------------------------------------------------
+template <typename RC>
+__global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const Stage st = stage_of(m, rk_step);
+  if (iteration > st.nsmall) return;
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  const int i_end = min(m.ite, m.ide - 1), j_end = min(m.jte, m.jde - 1);
+  if (i > i_end || j > j_end) return;
+  const int k_end = m.kte - 1, kde = m.kde;
+  const float dts = st.dts_rk, epssm = m.epssm, rdx = m.rdx, rdy = m.rdy;
+  F3 w = f3(m, WRFGPU_W_2), rw_tend = f3(m, WRFGPU_RW_TEND), ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2),
+     v = f3(m, WRFGPU_V_2), t_2ave = f3(m, WRFGPU_T_2SAVE), t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE),
+     ph = f3(m, WRFGPU_PH_2), ph_1 = f3(m, WRFGPU_PH_SAVE), phb = f3(m, WRFGPU_PHB), ph_tend = f3(m, WRFGPU_PH_TEND),
+     c2a = f3(m, WRFGPU_C2A), cqw = f3(m, WRFGPU_CQW), alt = f3(m, WRFGPU_ALT);
+  F2 mut = f2(m, WRFGPU_MUT), muave = f2(m, WRFGPU_MUAVE), muts = f2(m, WRFGPU_MUTS), ht = f2(m, WRFGPU_HT),
+     msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
+     fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW), rdn = f1(m, WRFGPU_RDN);
+  const bool fp64 = sizeof(RC) == 8;
+  const float msft_inv = 1.f / msfty.ro(i, j);
+  const float my = msfty.ro(i, j), mx = msftx.ro(i, j), mutij = mut.ro(i, j), mua = muave.ro(i, j), mts = muts.ro(i, j);
+  RC rhs[KCOL];
+  float ta[KCOL];
+  // ---- pass 1: t_2ave, rhs = dts (ph_tend + .5 g (1-epssm) w), the omega advection of phi, finalisation
+  struct P1 { float t2, t2a, t1, pht1, w1, ww1, ph11, phb1, ph; };  // level k values and k+1 (suffix 1)
+  auto load1 = [&](int k, P1& d) {
+    if (k <= k_end) { d.t2 = t_2.ro(i, k, j); d.t2a = t_2ave(i, k, j); d.t1 = t_1.ro(i, k, j); }
+    d.pht1 = ph_tend.ro(i, k + 1, j); d.w1 = w(i, k + 1, j); d.ww1 = ww.ro(i, k + 1, j);
+    d.ph11 = ph_1.ro(i, k + 1, j); d.phb1 = phb.ro(i, k + 1, j); d.ph = ph(i, k, j);
+  };
+  rhs[1] = RC(0.);
+  {
+    P1 cur, nxt;
+    load1(1, cur);
+    float ww_k = ww.ro(i, 1, j), ph1_k = ph_1.ro(i, 1, j), phb_k = phb.ro(i, 1, j);
+    float wd_k = 0.f;  // wdwn(k) of the level below (filled from k = 2 on)
+    for (int k = 1; k <= k_end; ++k) {
+      if (k + 1 <= k_end) load1(k + 1, nxt);
+      float tav = .5f * ((1.f + epssm) * cur.t2 + (1.f - epssm) * cur.t2a);
+      tav = (tav + (c1h(k) * mua) * T0) / ((c1h(k) * mts + c2h(k)) * (T0 + cur.t1));
+      t_2ave(i, k, j) = tav;
+      ta[k] = tav;
+      rhs[k + 1] = (RC)(dts * (cur.pht1 + .5f * G * (1.f - epssm) * cur.w1));
+      // wdwn(k+1) from levels k and k+1
+      float wd_hi;
+      if (m.cf.phi_adv_z == 2) wd_hi = rdnw(k) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
+      else wd_hi = .5f * (cur.ww1 + ww_k) * rdnw(k) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
+      if (k >= 2) {  // rhs(k) is complete: omega term, then the geopotential form
+        if (m.cf.phi_adv_z == 2) rhs[k] = rhs[k] - (RC)(dts * ww_k * (fnm(k) * wd_hi + fnp(k) * wd_k));
+        else rhs[k] = rhs[k] - (RC)(dts * (fnm(k) * wd_hi + fnp(k) * wd_k));
+        rhs[k] = (RC)cur.ph + (RC)my * rhs[k] / ((RC)c1f(k) * (RC)mutij + (RC)c2f(k));
+      }
+      wd_k = wd_hi;
+      ww_k = cur.ww1; ph1_k = cur.ph11; phb_k = cur.phb1;
+      cur = nxt;
+    }
+    // top level: no omega term
+    const int k = k_end + 1;
+    rhs[k] = (RC)ph(i, k, j) + (RC)my * rhs[k] / ((RC)c1f(k) * (RC)mutij + (RC)c2f(k));
+    if (m.cf.top_lid) rhs[k] = RC(0.);
+  }
+  // ---- surface w
+  const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
+  const RC w1 = (RC)(my * .5f * rdy *
+                         ((ht.ro(i, j + 1) - ht.ro(i, j)) * (cf1 * v.ro(i, 1, j + 1) + cf2 * v.ro(i, 2, j + 1) + cf3 * v.ro(i, 3, j + 1)) +
+                          (ht.ro(i, j) - ht.ro(i, j - 1)) * (cf1 * v.ro(i, 1, j) + cf2 * v.ro(i, 2, j) + cf3 * v.ro(i, 3, j))) +
+                     mx * .5f * rdx *
+                         ((ht.ro(i + 1, j) - ht.ro(i, j)) * (cf1 * u.ro(i + 1, 1, j) + cf2 * u.ro(i + 1, 2, j) + cf3 * u.ro(i + 1, 3, j)) +
+                          (ht.ro(i, j) - ht.ro(i - 1, j)) * (cf1 * u.ro(i, 1, j) + cf2 * u.ro(i, 2, j) + cf3 * u.ro(i, 3, j))));
+  w(i, 1, j) = (float)w1;
+  // ---- pass 2: explicit part and forward elimination (up)
+  const RC eps1 = RC(1.) + (RC)epssm, eps0 = RC(1.) - (RC)epssm;
+  auto Acoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[0])(i, k, j)) : (RC)f3(m, WRFGPU_A).ro(i, k, j); };
+  auto ALcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[1])(i, k, j)) : (RC)f3(m, WRFGPU_ALPHA).ro(i, k, j); };
+  auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[2])(i, k, j)) : (RC)f3(m, WRFGPU_GAMMA).ro(i, k, j); };
+  struct P2 { float w, rwt, cqw, c2a, alt, ph1; RC a, al; };
+  auto load2 = [&](int k, P2& d) {
+    d.w = w(i, k, j); d.rwt = rw_tend.ro(i, k, j); d.a = Acoef(k); d.al = ALcoef(k);
+    if (k <= k_end) { d.cqw = cqw.ro(i, k, j); d.c2a = c2a.ro(i, k, j); d.alt = alt.ro(i, k, j); d.ph1 = ph(i, k + 1, j); }
+    else { d.cqw = 0.f; d.c2a = 0.f; d.alt = 0.f; d.ph1 = 0.f; }
+  };
+  RC wcol[KCOL];
+  {
+    RC wprev = w1;
+    float c2a_m = c2a.ro(i, 1, j), alt_m = alt.ro(i, 1, j), ph_m = ph(i, 1, j), ph_k = ph(i, 2, j);
+    P2 cur, nxt;
+    load2(2, cur);
+    for (int k = 2; k <= k_end; ++k) {
+      load2(k + 1, nxt);
+      RC wk = (RC)cur.w + (RC)dts * (RC)cur.rwt +
+              (RC)msft_inv * (RC)cur.cqw *
+                  (+RC(.5) * (RC)dts * (RC)G * (RC)rdn(k) *
+                   ((RC)cur.c2a * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
+                        (eps1 * (rhs[k + 1] - rhs[k]) + eps0 * ((RC)cur.ph1 - (RC)ph_k)) -
+                    (RC)c2a_m * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
+                        (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph_k - (RC)ph_m)))) +
+              (RC)dts * (RC)G * (RC)msft_inv *
+                  ((RC)rdn(k) * ((RC)cur.c2a * (RC)cur.alt * (RC)ta[k] - (RC)c2a_m * (RC)alt_m * (RC)ta[k - 1]) -
+                   ((RC)c1f(k) * (RC)mua));
+      if (!fp64) wk = (RC)(float)wk;
+      wk = (wk - cur.a * wprev) * cur.al;
+      wcol[k] = wk;
+      wprev = wk;
+      c2a_m = cur.c2a; alt_m = cur.alt; ph_m = ph_k; ph_k = cur.ph1;
+      cur = nxt;
+    }
+    // top level
+    const int k = k_end + 1;
+    const RC r = (RC)rdnw(k - 1);
+    RC wk = (RC)cur.w + (RC)dts * (RC)cur.rwt +
+            (RC)msft_inv * (-RC(.5) * (RC)dts * (RC)G / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) * (r * r) * RC(2.) *
+                                (RC)c2a_m * (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph_k - (RC)ph_m)) -
+                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a_m * (RC)alt_m * (RC)ta[k - 1] +
+                                               ((RC)c1f(k) * (RC)mua)));
+    if (m.cf.top_lid) wk = RC(0.);
+    if (!fp64) wk = (RC)(float)wk;
+    wk = (wk - cur.a * wprev) * cur.al;
+    wcol[k] = wk;
+  }
+  // ---- pass 3: back substitution and geopotential (down)
+  RC wup = wcol[k_end + 1];
+  w(i, k_end + 1, j) = (float)wup;
+  ph(i, k_end + 1, j) = (float)(rhs[k_end + 1] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wup /
+                                                     ((RC)c1f(k_end + 1) * (RC)mts + (RC)c2f(k_end + 1)));
+  RC g_nxt = GAcoef(k_end);
+  for (int k = k_end; k >= 2; --k) {
+    const RC g = g_nxt;
+    if (k - 1 >= 2) g_nxt = GAcoef(k - 1);
+    const RC wk = wcol[k] - g * wup;
+    w(i, k, j) = (float)wk;
+    ph(i, k, j) = (float)(rhs[k] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wk / ((RC)c1f(k) * (RC)mts + (RC)c2f(k)));
+    wup = wk;
+  }
+}
+
+void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s) {
+  if (fp64) k_advance_mu_t_col<double><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  else k_advance_mu_t_col<float><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+}
+void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s) {
+  if (fp64) k_advance_w_col<double><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  else k_advance_w_col<float><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+}
+
 }  // namespace wrfgpu

@@ -78,5 +78,8 @@ void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s);
 // of the staggered extents
 void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s);
 void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s);
+// one block per tile of mass columns
+void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s);
+void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s);
 
 }  // namespace wrfgpu

@@ -387,11 +387,13 @@ __global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int r
 }
 
 // ---------------------------------------------------------------------------
-// advance_w (module_small_step_em.F:1178-1469), one thread per mass column:
-// pass 1 (up) t_2ave and the geopotential right-hand side, pass 2 (up) the
-// explicit w and forward elimination, pass 3 (down) back substitution and
-// the geopotential update.  RC as above (the mixed form keeps a, alpha,
-// gamma in FP64).
+// advance_w (module_small_step_em.F:1178-1469), one thread per mass column.
+// Upward pass: at level L, t_2ave(L), the raw right-hand side of L+1, the
+// omega advection term that completes rhs(L), and the explicit w and forward
+// elimination of level L-1 (which needs rhs(L)); everything the elimination
+// reads from neighbouring levels sits in register windows.  Downward pass:
+// back substitution and the geopotential update.  RC as above (the mixed
+// form keeps a, alpha, gamma in FP64).
 // ---------------------------------------------------------------------------
 template <typename RC>
 __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
@@ -413,49 +415,15 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
      fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW), rdn = f1(m, WRFGPU_RDN);
   const bool fp64 = sizeof(RC) == 8;
+  const bool adv2 = m.cf.phi_adv_z == 2;
   const float msft_inv = 1.f / msfty.ro(i, j);
   const float my = msfty.ro(i, j), mx = msftx.ro(i, j), mutij = mut.ro(i, j), mua = muave.ro(i, j), mts = muts.ro(i, j);
-  RC rhs[KCOL];
-  float ta[KCOL];
-  // ---- pass 1: t_2ave, rhs = dts (ph_tend + .5 g (1-epssm) w), the omega advection of phi, finalisation
-  struct P1 { float t2, t2a, t1, pht1, w1, ww1, ph11, phb1, ph; };  // level k values and k+1 (suffix 1)
-  auto load1 = [&](int k, P1& d) {
-    if (k <= k_end) { d.t2 = t_2.ro(i, k, j); d.t2a = t_2ave(i, k, j); d.t1 = t_1.ro(i, k, j); }
-    d.pht1 = ph_tend.ro(i, k + 1, j); d.w1 = w(i, k + 1, j); d.ww1 = ww.ro(i, k + 1, j);
-    d.ph11 = ph_1.ro(i, k + 1, j); d.phb1 = phb.ro(i, k + 1, j); d.ph = ph(i, k, j);
-  };
-  rhs[1] = RC(0.);
-  {
-    P1 cur, nxt;
-    load1(1, cur);
-    float ww_k = ww.ro(i, 1, j), ph1_k = ph_1.ro(i, 1, j), phb_k = phb.ro(i, 1, j);
-    float wd_k = 0.f;  // wdwn(k) of the level below (filled from k = 2 on)
-    for (int k = 1; k <= k_end; ++k) {
-      if (k + 1 <= k_end) load1(k + 1, nxt);
-      float tav = .5f * ((1.f + epssm) * cur.t2 + (1.f - epssm) * cur.t2a);
-      tav = (tav + (c1h(k) * mua) * T0) / ((c1h(k) * mts + c2h(k)) * (T0 + cur.t1));
-      t_2ave(i, k, j) = tav;
-      ta[k] = tav;
-      rhs[k + 1] = (RC)(dts * (cur.pht1 + .5f * G * (1.f - epssm) * cur.w1));
-      // wdwn(k+1) from levels k and k+1
-      float wd_hi;
-      if (m.cf.phi_adv_z == 2) wd_hi = rdnw(k) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
-      else wd_hi = .5f * (cur.ww1 + ww_k) * rdnw(k) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
-      if (k >= 2) {  // rhs(k) is complete: omega term, then the geopotential form
-        if (m.cf.phi_adv_z == 2) rhs[k] = rhs[k] - (RC)(dts * ww_k * (fnm(k) * wd_hi + fnp(k) * wd_k));
-        else rhs[k] = rhs[k] - (RC)(dts * (fnm(k) * wd_hi + fnp(k) * wd_k));
-        rhs[k] = (RC)cur.ph + (RC)my * rhs[k] / ((RC)c1f(k) * (RC)mutij + (RC)c2f(k));
-      }
-      wd_k = wd_hi;
-      ww_k = cur.ww1; ph1_k = cur.ph11; phb_k = cur.phb1;
-      cur = nxt;
-    }
-    // top level: no omega term
-    const int k = k_end + 1;
-    rhs[k] = (RC)ph(i, k, j) + (RC)my * rhs[k] / ((RC)c1f(k) * (RC)mutij + (RC)c2f(k));
-    if (m.cf.top_lid) rhs[k] = RC(0.);
-  }
-  // ---- surface w
+  auto Acoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[0])(i, k, j)) : (RC)f3(m, WRFGPU_A).ro(i, k, j); };
+  auto ALcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[1])(i, k, j)) : (RC)f3(m, WRFGPU_ALPHA).ro(i, k, j); };
+  auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[2])(i, k, j)) : (RC)f3(m, WRFGPU_GAMMA).ro(i, k, j); };
+  const RC eps1 = RC(1.) + (RC)epssm, eps0 = RC(1.) - (RC)epssm;
+
+  // surface w (needs only u, v of the lowest levels)
   const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
   const RC w1 = (RC)(my * .5f * rdy *
                          ((ht.ro(i, j + 1) - ht.ro(i, j)) * (cf1 * v.ro(i, 1, j + 1) + cf2 * v.ro(i, 2, j + 1) + cf3 * v.ro(i, 3, j + 1)) +
@@ -463,61 +431,115 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
                      mx * .5f * rdx *
                          ((ht.ro(i + 1, j) - ht.ro(i, j)) * (cf1 * u.ro(i + 1, 1, j) + cf2 * u.ro(i + 1, 2, j) + cf3 * u.ro(i + 1, 3, j)) +
                           (ht.ro(i, j) - ht.ro(i - 1, j)) * (cf1 * u.ro(i, 1, j) + cf2 * u.ro(i, 2, j) + cf3 * u.ro(i, 3, j))));
-  w(i, 1, j) = (float)w1;
-  // ---- pass 2: explicit part and forward elimination (up)
-  const RC eps1 = RC(1.) + (RC)epssm, eps0 = RC(1.) - (RC)epssm;
-  auto Acoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[0])(i, k, j)) : (RC)f3(m, WRFGPU_A).ro(i, k, j); };
-  auto ALcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[1])(i, k, j)) : (RC)f3(m, WRFGPU_ALPHA).ro(i, k, j); };
-  auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[2])(i, k, j)) : (RC)f3(m, WRFGPU_GAMMA).ro(i, k, j); };
-  struct P2 { float w, rwt, cqw, c2a, alt, ph1; RC a, al; };
-  auto load2 = [&](int k, P2& d) {
-    d.w = w(i, k, j); d.rwt = rw_tend.ro(i, k, j); d.a = Acoef(k); d.al = ALcoef(k);
-    if (k <= k_end) { d.cqw = cqw.ro(i, k, j); d.c2a = c2a.ro(i, k, j); d.alt = alt.ro(i, k, j); d.ph1 = ph(i, k + 1, j); }
-    else { d.cqw = 0.f; d.c2a = 0.f; d.alt = 0.f; d.ph1 = 0.f; }
-  };
+
+  // explicit w of level k and forward elimination (the reference's upward loop body)
+  RC wprev = w1;
   RC wcol[KCOL];
-  {
-    RC wprev = w1;
-    float c2a_m = c2a.ro(i, 1, j), alt_m = alt.ro(i, 1, j), ph_m = ph(i, 1, j), ph_k = ph(i, 2, j);
-    P2 cur, nxt;
-    load2(2, cur);
-    for (int k = 2; k <= k_end; ++k) {
-      load2(k + 1, nxt);
-      RC wk = (RC)cur.w + (RC)dts * (RC)cur.rwt +
-              (RC)msft_inv * (RC)cur.cqw *
-                  (+RC(.5) * (RC)dts * (RC)G * (RC)rdn(k) *
-                   ((RC)cur.c2a * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
-                        (eps1 * (rhs[k + 1] - rhs[k]) + eps0 * ((RC)cur.ph1 - (RC)ph_k)) -
-                    (RC)c2a_m * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
-                        (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph_k - (RC)ph_m)))) +
-              (RC)dts * (RC)G * (RC)msft_inv *
-                  ((RC)rdn(k) * ((RC)cur.c2a * (RC)cur.alt * (RC)ta[k] - (RC)c2a_m * (RC)alt_m * (RC)ta[k - 1]) -
-                   ((RC)c1f(k) * (RC)mua));
-      if (!fp64) wk = (RC)(float)wk;
-      wk = (wk - cur.a * wprev) * cur.al;
-      wcol[k] = wk;
-      wprev = wk;
-      c2a_m = cur.c2a; alt_m = cur.alt; ph_m = ph_k; ph_k = cur.ph1;
-      cur = nxt;
+  auto sweep = [&](int k, float wk_in, float rwt, float cqwk, float c2ak, float altk, RC ak, RC alk, float tak,
+                   float c2am, float altm, float tam, RC r_p1, RC r_0, RC r_m1, float ph_p1, float ph_0, float ph_m1) {
+    RC wk = (RC)wk_in + (RC)dts * (RC)rwt +
+            (RC)msft_inv * (RC)cqwk *
+                (+RC(.5) * (RC)dts * (RC)G * (RC)rdn(k) *
+                 ((RC)c2ak * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
+                      (eps1 * (r_p1 - r_0) + eps0 * ((RC)ph_p1 - (RC)ph_0)) -
+                  (RC)c2am * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
+                      (eps1 * (r_0 - r_m1) + eps0 * ((RC)ph_0 - (RC)ph_m1)))) +
+            (RC)dts * (RC)G * (RC)msft_inv *
+                ((RC)rdn(k) * ((RC)c2ak * (RC)altk * (RC)tak - (RC)c2am * (RC)altm * (RC)tam) - ((RC)c1f(k) * (RC)mua));
+    if (!fp64) wk = (RC)(float)wk;
+    wk = (wk - ak * wprev) * alk;
+    wcol[k] = wk;
+    wprev = wk;
+  };
+
+  struct Lv {
+    float t2, t2a, t1, ph, w, rwt, cqw, c2a, alt;  // level L
+    RC a, al;
+    float pht1, w1, ww1, ph11, phb1;               // level L+1
+  };
+  auto load = [&](int k, Lv& d) {
+    d.t2 = t_2.ro(i, k, j); d.t2a = t_2ave(i, k, j); d.t1 = t_1.ro(i, k, j); d.ph = ph(i, k, j);
+    d.w = w(i, k, j); d.rwt = rw_tend.ro(i, k, j); d.cqw = cqw.ro(i, k, j); d.c2a = c2a.ro(i, k, j);
+    d.alt = alt.ro(i, k, j); d.a = Acoef(k); d.al = ALcoef(k);
+    d.pht1 = ph_tend.ro(i, k + 1, j); d.w1 = w(i, k + 1, j); d.ww1 = ww.ro(i, k + 1, j);
+    d.ph11 = ph_1.ro(i, k + 1, j); d.phb1 = phb.ro(i, k + 1, j);
+  };
+  RC rhs[KCOL];
+  rhs[1] = RC(0.);
+  // windows: level L-1 and L-2 values of what the elimination reads
+  RC r_m1 = RC(0.), r_m2 = RC(0.);       // rhs(L-1), rhs(L-2)
+  float ph_m1 = 0.f, ph_m2 = 0.f;        // ph(L-1), ph(L-2)
+  float ta_m1 = 0.f, ta_m2 = 0.f;        // t_2ave(L-1), t_2ave(L-2)
+  float c2a_m1 = 0.f, c2a_m2 = 0.f, alt_m1 = 0.f, alt_m2 = 0.f;
+  float w_m1 = 0.f, rwt_m1 = 0.f, cqw_m1 = 0.f;
+  RC a_m1 = RC(0.), al_m1 = RC(0.);
+  float ww_k = ww.ro(i, 1, j), ph1_k = ph_1.ro(i, 1, j), phb_k = phb.ro(i, 1, j);
+  float wd_k = 0.f;   // wdwn(L)
+  RC rr_k = RC(0.);   // raw rhs(L)
+  Lv cur, nxt;
+  load(1, cur);
+  for (int Lk = 1; Lk <= k_end; ++Lk) {
+    if (Lk + 1 <= k_end) load(Lk + 1, nxt);
+    // t_2ave(L)
+    float tav = .5f * ((1.f + epssm) * cur.t2 + (1.f - epssm) * cur.t2a);
+    tav = (tav + (c1h(Lk) * mua) * T0) / ((c1h(Lk) * mts + c2h(Lk)) * (T0 + cur.t1));
+    t_2ave(i, Lk, j) = tav;
+    // raw rhs(L+1), wdwn(L+1)
+    const RC rr_next = (RC)(dts * (cur.pht1 + .5f * G * (1.f - epssm) * cur.w1));
+    float wd_hi;
+    if (adv2) wd_hi = rdnw(Lk) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
+    else wd_hi = .5f * (cur.ww1 + ww_k) * rdnw(Lk) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
+    // rhs(L) complete
+    RC r_0 = RC(0.);
+    if (Lk >= 2) {
+      RC r = rr_k;
+      if (adv2) r = r - (RC)(dts * ww_k * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
+      else r = r - (RC)(dts * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
+      r = (RC)cur.ph + (RC)my * r / ((RC)c1f(Lk) * (RC)mutij + (RC)c2f(Lk));
+      rhs[Lk] = r;
+      r_0 = r;
     }
-    // top level
-    const int k = k_end + 1;
+    // elimination of level L-1
+    if (Lk >= 3)
+      sweep(Lk - 1, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_0, r_m1, r_m2,
+            cur.ph, ph_m1, ph_m2);
+    // slide
+    r_m2 = r_m1; r_m1 = r_0;
+    ph_m2 = ph_m1; ph_m1 = cur.ph;
+    ta_m2 = ta_m1; ta_m1 = tav;
+    c2a_m2 = c2a_m1; c2a_m1 = cur.c2a; alt_m2 = alt_m1; alt_m1 = cur.alt;
+    w_m1 = cur.w; rwt_m1 = cur.rwt; cqw_m1 = cur.cqw; a_m1 = cur.a; al_m1 = cur.al;
+    ww_k = cur.ww1; ph1_k = cur.ph11; phb_k = cur.phb1;
+    wd_k = wd_hi; rr_k = rr_next;
+    cur = nxt;
+  }
+  // top: rhs(kde) has no omega term
+  const int kt = k_end + 1;
+  const float ph_top = ph(i, kt, j);
+  RC r_top = (RC)ph_top + (RC)my * rr_k / ((RC)c1f(kt) * (RC)mutij + (RC)c2f(kt));
+  if (m.cf.top_lid) r_top = RC(0.);
+  rhs[kt] = r_top;
+  // elimination of level k_end
+  sweep(k_end, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_top, r_m1, r_m2,
+        ph_top, ph_m1, ph_m2);
+  {  // level kde
+    const int k = kt;
     const RC r = (RC)rdnw(k - 1);
-    RC wk = (RC)cur.w + (RC)dts * (RC)cur.rwt +
+    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend.ro(i, k, j) +
             (RC)msft_inv * (-RC(.5) * (RC)dts * (RC)G / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) * (r * r) * RC(2.) *
-                                (RC)c2a_m * (eps1 * (rhs[k] - rhs[k - 1]) + eps0 * ((RC)ph_k - (RC)ph_m)) -
-                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a_m * (RC)alt_m * (RC)ta[k - 1] +
+                                (RC)c2a_m1 * (eps1 * (r_top - r_m1) + eps0 * ((RC)ph_top - (RC)ph_m1)) -
+                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a_m1 * (RC)alt_m1 * (RC)ta_m1 +
                                                ((RC)c1f(k) * (RC)mua)));
     if (m.cf.top_lid) wk = RC(0.);
     if (!fp64) wk = (RC)(float)wk;
-    wk = (wk - cur.a * wprev) * cur.al;
+    wk = (wk - Acoef(k) * wprev) * ALcoef(k);
     wcol[k] = wk;
   }
-  // ---- pass 3: back substitution and geopotential (down)
-  RC wup = wcol[k_end + 1];
-  w(i, k_end + 1, j) = (float)wup;
-  ph(i, k_end + 1, j) = (float)(rhs[k_end + 1] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wup /
-                                                     ((RC)c1f(k_end + 1) * (RC)mts + (RC)c2f(k_end + 1)));
+  w(i, 1, j) = (float)w1;
+  // ---- back substitution and geopotential (down)
+  RC wup = wcol[kt];
+  w(i, kt, j) = (float)wup;
+  ph(i, kt, j) = (float)(rhs[kt] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wup / ((RC)c1f(kt) * (RC)mts + (RC)c2f(kt)));
   RC g_nxt = GAcoef(k_end);
   for (int k = k_end; k >= 2; --k) {
     const RC g = g_nxt;

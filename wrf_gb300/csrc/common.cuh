@@ -240,6 +240,23 @@ __device__ __forceinline__ const Mem& block_member(const Mem* mems, int m) {
   return s_mem;
 }
 
+// Column loop k = k0..k1 whose levels are independent of each other: the
+// inputs of C levels are loaded (load(k, v)) before any of them is computed
+// and stored (store(k, v)), so one memory round trip serves C levels instead
+// of one.  Per-level arithmetic is untouched.
+template <int C, typename T, typename LoadF, typename StoreF>
+__device__ __forceinline__ void chunked_levels(int k0, int k1, LoadF load, StoreF store) {
+  for (int kb = k0; kb <= k1; kb += C) {
+    T v[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q)
+      if (kb + q <= k1) load(kb + q, v[q]);
+#pragma unroll
+    for (int q = 0; q < C; ++q)
+      if (kb + q <= k1) store(kb + q, v[q]);
+  }
+}
+
 __device__ __forceinline__ void raise_err(const Mem& m, unsigned bits) {
   if (m.err) atomicOr(m.err, bits);
 }

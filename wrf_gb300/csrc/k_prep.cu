@@ -62,60 +62,86 @@ __global__ void __launch_bounds__(BX* BY) k_rk_step_prep(Launch L) {
     }
     MUV(i, j) = muv_ij;
   }
-  // couple_momentum (:329-391)
-  if (at_u)
-    for (int k = m.kts; k <= ktf; ++k) ru(i, k, j) = u(i, k, j) * (c1h(k) * muu_ij + c2h(k)) / msfuy(i, j);
-  if (at_v)
-    for (int k = m.kts; k <= ktf; ++k) rv(i, k, j) = v(i, k, j) * (c1h(k) * muv_ij + c2h(k)) * msfvx_inv(i, j);
+  // couple_momentum (:329-391) and calc_cq (:787-907, qv the only moist
+  // species) on the u and v points: levels loaded in chunks (independent levels)
+  if (at_u) {
+    const float my = msfuy.ro(i, j);
+    struct LU { float u, q0, q1; };
+    chunked_levels<8, LU>(
+        m.kts, ktf, [&](int k, LU& d) { d.u = u.ro(i, k, j); d.q0 = qv.ro(i, k, j); d.q1 = qv.ro(i - 1, k, j); },
+        [&](int k, const LU& d) {
+          ru(i, k, j) = d.u * (c1h(k) * muu_ij + c2h(k)) / my;
+          float qtot = 0.f + d.q0 + d.q1;
+          cqu(i, k, j) = 1.f / (1.f + 0.5f * qtot);
+        });
+  }
+  if (at_v) {
+    const float mxi = msfvx_inv.ro(i, j);
+    struct LV { float v, q0, q1; };
+    chunked_levels<8, LV>(
+        m.kts, ktf, [&](int k, LV& d) { d.v = v.ro(i, k, j); d.q0 = qv.ro(i, k, j); d.q1 = qv.ro(i, k, j - 1); },
+        [&](int k, const LV& d) {
+          rv(i, k, j) = d.v * (c1h(k) * muv_ij + c2h(k)) * mxi;
+          float qtot = 0.f + d.q0 + d.q1;
+          cqv(i, k, j) = 1.f / (1.f + 0.5f * qtot);
+        });
+  }
   const bool at_t = i >= m.its && i <= itf_m && j >= m.jts && j <= jtf_m;
-  if (at_t)
-    for (int k = m.kts; k <= m.kte; ++k) rw(i, k, j) = w(i, k, j) * (c1f(k) * mut_ij + c2f(k)) / msfty(i, j);
   // calc_ww_cp (:640-784); the staggered mass averages are formed locally.
   if (i >= m.its && i <= m.ite && j >= m.jts && j <= jtf_m) {
     ww(i, 1, j) = 0.f;
     ww(i, m.kte, j) = 0.f;
   }
   if (at_t) {
-    const float muu0 = 0.5f * (MU(i, j) + MUB(i, j) + MU(i - 1, j) + MUB(i - 1, j));
-    const float muu1 = 0.5f * (MU(i + 1, j) + MUB(i + 1, j) + MU(i, j) + MUB(i, j));
-    const float muv0 = 0.5f * (MU(i, j) + MUB(i, j) + MU(i, j - 1) + MUB(i, j - 1));
-    const float muv1 = 0.5f * (MU(i, j + 1) + MUB(i, j + 1) + MU(i, j) + MUB(i, j));
-    const float mx = msftx(i, j), uy0 = msfuy(i, j), uy1 = msfuy(i + 1, j);
-    const float vi0 = msfvx_inv(i, j), vi1 = msfvx_inv(i, j + 1);
-    auto divv = [&](int k) -> float {
-      return mx * dnw(k) *
-             (rdx * ((c1h(k) * muu1 + c2h(k)) * u(i + 1, k, j) / uy1 - (c1h(k) * muu0 + c2h(k)) * u(i, k, j) / uy0) +
-              rdy * ((c1h(k) * muv1 + c2h(k)) * v(i, k, j + 1) * vi1 - (c1h(k) * muv0 + c2h(k)) * v(i, k, j) * vi0));
-    };
+    const float muu0 = 0.5f * (MU.ro(i, j) + MUB.ro(i, j) + MU.ro(i - 1, j) + MUB.ro(i - 1, j));
+    const float muu1 = 0.5f * (MU.ro(i + 1, j) + MUB.ro(i + 1, j) + MU.ro(i, j) + MUB.ro(i, j));
+    const float muv0 = 0.5f * (MU.ro(i, j) + MUB.ro(i, j) + MU.ro(i, j - 1) + MUB.ro(i, j - 1));
+    const float muv1 = 0.5f * (MU.ro(i, j + 1) + MUB.ro(i, j + 1) + MU.ro(i, j) + MUB.ro(i, j));
+    const float mx = msftx.ro(i, j), uy0 = msfuy.ro(i, j), uy1 = msfuy.ro(i + 1, j);
+    const float vi0 = msfvx_inv.ro(i, j), vi1 = msfvx_inv.ro(i, j + 1);
+    float dv[129];
     float dmdt = 0.f;
-    for (int k = m.kts; k <= ktf; ++k) dmdt = dmdt + divv(k);
-    float wwk = ww(i, 1, j);
+    struct LD { float u0, u1, v0, v1; };
+    chunked_levels<8, LD>(
+        m.kts, ktf,
+        [&](int k, LD& d) { d.u0 = u.ro(i, k, j); d.u1 = u.ro(i + 1, k, j); d.v0 = v.ro(i, k, j); d.v1 = v.ro(i, k, j + 1); },
+        [&](int k, const LD& d) {
+          const float dvv =
+              mx * dnw(k) *
+              (rdx * ((c1h(k) * muu1 + c2h(k)) * d.u1 / uy1 - (c1h(k) * muu0 + c2h(k)) * d.u0 / uy0) +
+               rdy * ((c1h(k) * muv1 + c2h(k)) * d.v1 * vi1 - (c1h(k) * muv0 + c2h(k)) * d.v0 * vi0));
+          dv[k] = dvv;
+          dmdt = dmdt + dvv;
+        });
+    float wwk = 0.f;  // ww(i, 1, j), set to zero above by this thread
     for (int k = 2; k <= ktf; ++k) {
-      wwk = wwk - dnw(k - 1) * c1h(k - 1) * dmdt - divv(k - 1);
+      wwk = wwk - dnw(k - 1) * c1h(k - 1) * dmdt - dv[k - 1];
       ww(i, k, j) = wwk;
     }
-  }
-  // calc_cq (:787-907) with qv the only moist species
-  if (at_u)
-    for (int k = m.kts; k <= ktf; ++k) {
-      float qtot = 0.f + qv(i, k, j) + qv(i - 1, k, j);
-      cqu(i, k, j) = 1.f / (1.f + 0.5f * qtot);
-    }
-  if (at_v)
-    for (int k = m.kts; k <= ktf; ++k) {
-      float qtot = 0.f + qv(i, k, j) + qv(i, k, j - 1);
-      cqv(i, k, j) = 1.f / (1.f + 0.5f * qtot);
-    }
-  if (at_t) {
-    for (int k = m.kts + 1; k <= ktf; ++k) {
-      float qtot = 0.f + qv(i, k, j) + qv(i, k - 1, j);
-      cqw(i, k, j) = 0.5f * qtot;
-    }
-    // calc_alt (:910-950), calc_php (:1227-1262)
-    for (int k = m.kts; k <= ktf; ++k) {
-      alt(i, k, j) = al(i, k, j) + alb(i, k, j);
-      php(i, k, j) = 0.5f * (phb(i, k, j) + phb(i, k + 1, j) + ph(i, k, j) + ph(i, k + 1, j));
-    }
+    // couple_momentum rw (:329-391), calc_cq cqw, calc_alt (:910-950), calc_php (:1227-1262)
+    const float my = msfty.ro(i, j);
+    struct LT { float w, q0, qm, al, alb, phb0, phb1, ph0, ph1; };
+    chunked_levels<6, LT>(
+        m.kts, m.kte,
+        [&](int k, LT& d) {
+          d.w = w.ro(i, k, j);
+          if (k <= ktf) {
+            d.q0 = qv.ro(i, k, j); d.qm = k > m.kts ? qv.ro(i, k - 1, j) : 0.f;
+            d.al = al.ro(i, k, j); d.alb = alb.ro(i, k, j);
+            d.phb0 = phb.ro(i, k, j); d.phb1 = phb.ro(i, k + 1, j); d.ph0 = ph.ro(i, k, j); d.ph1 = ph.ro(i, k + 1, j);
+          }
+        },
+        [&](int k, const LT& d) {
+          rw(i, k, j) = d.w * (c1f(k) * mut_ij + c2f(k)) / my;
+          if (k <= ktf) {
+            if (k >= m.kts + 1) {
+              float qtot = 0.f + d.q0 + d.qm;
+              cqw(i, k, j) = 0.5f * qtot;
+            }
+            alt(i, k, j) = d.al + d.alb;
+            php(i, k, j) = 0.5f * (d.phb0 + d.phb1 + d.ph0 + d.ph1);
+          }
+        });
   }
 }
 

@@ -41,59 +41,73 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_ste
      pb = f3(m, WRFGPU_PB), p = f3(m, WRFGPU_P), alt = f3(m, WRFGPU_ALT);
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
   float muts = 0.f, muus = 0.f, muvs = 0.f;
-  if (rk_step == 1) {
+  const bool rk1 = rk_step == 1;
+  if (rk1) {
     if (mass) { MU_1(i, j) = MU_2(i, j); MUDF(i, j) = 0.f; }
-    if (upt) for (int k = k_start; k <= k_end; ++k) u_1(i, k, j) = u_2(i, k, j);
-    if (vpt) for (int k = k_start; k <= k_end; ++k) v_1(i, k, j) = v_2(i, k, j);
-    if (mass) {
-      for (int k = k_start; k <= k_end; ++k) t_1(i, k, j) = t_2(i, k, j);
-      for (int k = k_start; k <= min(kde, m.kte); ++k) { w_1(i, k, j) = w_2(i, k, j); ph_1(i, k, j) = ph_2(i, k, j); }
-      muts = mub(i, j) + MU_2(i, j); MUTS(i, j) = muts;
-    }
-    if (upt) { muus = MUU(i, j); MUUS(i, j) = muus; }
-    if (vpt) { muvs = MUV(i, j); MUVS(i, j) = muvs; }
+    if (mass) { muts = mub.ro(i, j) + MU_2(i, j); MUTS(i, j) = muts; }
+    if (upt) { muus = MUU.ro(i, j); MUUS(i, j) = muus; }
+    if (vpt) { muvs = MUV.ro(i, j); MUVS(i, j) = muvs; }
     if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = 0.f; }
   } else {
-    if (mass) { muts = mub(i, j) + MU_1(i, j); MUTS(i, j) = muts; }
-    if (upt) { muus = 0.5f * (mub(i, j) + MU_1(i, j) + mub(i - 1, j) + MU_1(i - 1, j)); MUUS(i, j) = muus; }
-    if (vpt) { muvs = 0.5f * (mub(i, j) + MU_1(i, j) + mub(i, j - 1) + MU_1(i, j - 1)); MUVS(i, j) = muvs; }
+    if (mass) { muts = mub.ro(i, j) + MU_1(i, j); MUTS(i, j) = muts; }
+    if (upt) { muus = 0.5f * (mub.ro(i, j) + MU_1(i, j) + mub.ro(i - 1, j) + MU_1(i - 1, j)); MUUS(i, j) = muus; }
+    if (vpt) { muvs = 0.5f * (mub.ro(i, j) + MU_1(i, j) + mub.ro(i, j - 1) + MU_1(i, j - 1)); MUVS(i, j) = muvs; }
     if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = MU_1(i, j) - MU_2(i, j); }
   }
-  if (mass) {
-    for (int k = k_start; k <= k_end; ++k) c2a(i, k, j) = CPOVCV * (pb(i, k, j) + p(i, k, j)) / alt(i, k, j);
-  }
+  // levels are independent: inputs of a chunk of levels are loaded first.
+  // At the first stage *_1 = *_2 (the copies the reference makes first).
+  struct L2 { float x2, x1; };
   if (upt) {
-    const float muu = MUU(i, j), my = msfuy(i, j);
-    for (int k = k_start; k <= k_end; ++k) {
-      float u2 = u_2(i, k, j);
-      u_save(i, k, j) = u2;
-      u_2(i, k, j) = ((c1h(k) * muus + c2h(k)) * u_1(i, k, j) - (c1h(k) * muu + c2h(k)) * u2) / my;
-    }
+    const float muu = MUU.ro(i, j), my = msfuy.ro(i, j);
+    chunked_levels<8, L2>(
+        k_start, k_end, [&](int k, L2& d) { d.x2 = u_2(i, k, j); d.x1 = rk1 ? d.x2 : u_1(i, k, j); },
+        [&](int k, const L2& d) {
+          if (rk1) u_1(i, k, j) = d.x2;
+          u_save(i, k, j) = d.x2;
+          u_2(i, k, j) = ((c1h(k) * muus + c2h(k)) * d.x1 - (c1h(k) * muu + c2h(k)) * d.x2) / my;
+        });
   }
   if (vpt) {
-    const float muv = MUV(i, j), mxi = msfvx_inv(i, j);
-    for (int k = k_start; k <= k_end; ++k) {
-      float v2 = v_2(i, k, j);
-      v_save(i, k, j) = v2;
-      v_2(i, k, j) = ((c1h(k) * muvs + c2h(k)) * v_1(i, k, j) - (c1h(k) * muv + c2h(k)) * v2) * mxi;
-    }
+    const float muv = MUV.ro(i, j), mxi = msfvx_inv.ro(i, j);
+    chunked_levels<8, L2>(
+        k_start, k_end, [&](int k, L2& d) { d.x2 = v_2(i, k, j); d.x1 = rk1 ? d.x2 : v_1(i, k, j); },
+        [&](int k, const L2& d) {
+          if (rk1) v_1(i, k, j) = d.x2;
+          v_save(i, k, j) = d.x2;
+          v_2(i, k, j) = ((c1h(k) * muvs + c2h(k)) * d.x1 - (c1h(k) * muv + c2h(k)) * d.x2) * mxi;
+        });
   }
   if (mass) {
-    const float mt = mut(i, j), my = msfty(i, j);
-    for (int k = k_start; k <= k_end; ++k) {
-      float t2 = t_2(i, k, j);
-      t_save(i, k, j) = t2;
-      t_2(i, k, j) = (c1h(k) * muts + c2h(k)) * t_1(i, k, j) - (c1h(k) * mt + c2h(k)) * t2;
-    }
-    for (int k = k_start; k <= kde; ++k) {
-      float w2 = w_2(i, k, j);
-      w_save(i, k, j) = w2;
-      w_2(i, k, j) = ((c1f(k) * muts + c2f(k)) * w_1(i, k, j) - (c1f(k) * mt + c2f(k)) * w2) / my;
-      float p2 = ph_2(i, k, j);
-      ph_save(i, k, j) = p2;
-      ph_2(i, k, j) = ph_1(i, k, j) - p2;
-      ww_save(i, k, j) = ww(i, k, j);
-    }
+    const float mt = mut.ro(i, j), my = msfty.ro(i, j);
+    struct LT { float t2, t1, pb, p, alt; };
+    chunked_levels<8, LT>(
+        k_start, k_end,
+        [&](int k, LT& d) {
+          d.t2 = t_2(i, k, j); d.t1 = rk1 ? d.t2 : t_1(i, k, j);
+          d.pb = pb.ro(i, k, j); d.p = p.ro(i, k, j); d.alt = alt.ro(i, k, j);
+        },
+        [&](int k, const LT& d) {
+          if (rk1) t_1(i, k, j) = d.t2;
+          c2a(i, k, j) = CPOVCV * (d.pb + d.p) / d.alt;
+          t_save(i, k, j) = d.t2;
+          t_2(i, k, j) = (c1h(k) * muts + c2h(k)) * d.t1 - (c1h(k) * mt + c2h(k)) * d.t2;
+        });
+    struct LW { float w2, w1, p2, p1, ww; };
+    chunked_levels<6, LW>(
+        k_start, kde,
+        [&](int k, LW& d) {
+          d.w2 = w_2(i, k, j); d.w1 = rk1 ? d.w2 : w_1(i, k, j);
+          d.p2 = ph_2(i, k, j); d.p1 = rk1 ? d.p2 : ph_1(i, k, j);
+          d.ww = ww.ro(i, k, j);
+        },
+        [&](int k, const LW& d) {
+          if (rk1) { w_1(i, k, j) = d.w2; ph_1(i, k, j) = d.p2; }
+          w_save(i, k, j) = d.w2;
+          w_2(i, k, j) = ((c1f(k) * muts + c2f(k)) * d.w1 - (c1f(k) * mt + c2f(k)) * d.w2) / my;
+          ph_save(i, k, j) = d.p2;
+          ph_2(i, k, j) = d.p1 - d.p2;
+          ww_save(i, k, j) = d.ww;
+        });
   }
 }
 
@@ -158,28 +172,33 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
     if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[2])(i, k, j);
     return *(RC*)&f3(m, WRFGPU_GAMMA)(i, k, j);
   };
+  RC a_loc[KMAX + 1];  // A of this column, re-read by the elimination below
   {
     int k = kde - 1;
     A(2) = RC(0.);
+    a_loc[2] = RC(0.);
     RC r = (RC)rdnw(kde - 1);
-    A(kde) = -RC(2.) * cof * (r * r) * (RC)c2a(i, kde - 1, j) * lid_flag /
+    A(kde) = -RC(2.) * cof * (r * r) * (RC)c2a.ro(i, kde - 1, j) * lid_flag /
              (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
+    a_loc[kde] = A(kde);
     GA(1) = RC(0.);
   }
   for (int kk = 3; kk <= kde - 1; ++kk) {
     int k = kk - 1;
-    A(kk) = -(RC)cqw(i, kk, j) * cof * (RC)rdn(kk) * (RC)rdnw(kk - 1) * (RC)c2a(i, kk - 1, j) /
-            (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
+    const RC av = -(RC)cqw.ro(i, kk, j) * cof * (RC)rdn(kk) * (RC)rdnw(kk - 1) * (RC)c2a.ro(i, kk - 1, j) /
+                  (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
+    A(kk) = av;
+    a_loc[kk] = av;
   }
   RC gprev = GA(1);
   for (int k = 2; k <= kde - 1; ++k) {
-    RC b = RC(1.) + (RC)cqw(i, k, j) * cof * (RC)rdn(k) *
-                        ((RC)rdnw(k) * (RC)c2a(i, k, j) / (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k))) +
-                         (RC)rdnw(k - 1) * (RC)c2a(i, k - 1, j) /
+    RC b = RC(1.) + (RC)cqw.ro(i, k, j) * cof * (RC)rdn(k) *
+                        ((RC)rdnw(k) * (RC)c2a.ro(i, k, j) / (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k))) +
+                         (RC)rdnw(k - 1) * (RC)c2a.ro(i, k - 1, j) /
                              (((RC)c1h(k - 1) * MUT + (RC)c2h(k - 1)) * ((RC)c1f(k) * MUT + (RC)c2f(k))));
-    RC c = -(RC)cqw(i, k, j) * cof * (RC)rdn(k) * (RC)rdnw(k) * (RC)c2a(i, k, j) /
+    RC c = -(RC)cqw.ro(i, k, j) * cof * (RC)rdn(k) * (RC)rdnw(k) * (RC)c2a.ro(i, k, j) /
            (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k + 1) * MUT + (RC)c2f(k + 1)));
-    RC al = RC(1.) / (b - A(k) * gprev);
+    RC al = RC(1.) / (b - a_loc[k] * gprev);
     AL(k) = al;
     gprev = c * al;
     GA(k) = gprev;
@@ -187,10 +206,10 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
   {
     int k = kde;
     RC r = (RC)rdnw(kde - 1);
-    RC b = RC(1.) + RC(2.) * cof * (r * r) * (RC)c2a(i, kde - 1, j) /
+    RC b = RC(1.) + RC(2.) * cof * (r * r) * (RC)c2a.ro(i, kde - 1, j) /
                         (((RC)c1h(k - 1) * MUT + (RC)c2h(k - 1)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
     RC c = RC(0.);
-    RC al = RC(1.) / (b - A(kde) * gprev);
+    RC al = RC(1.) / (b - a_loc[kde] * gprev);
     AL(kde) = al;
     GA(kde) = c * al;
   }
@@ -539,36 +558,50 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_finish(Launch L, int rk_s
     MUV(i, j) = muvs;
   }
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+  // levels are independent: inputs of a chunk of levels are loaded first
+  struct L2 { float x, s; };
   if (vpt) {
     F3 v_2 = f3(m, WRFGPU_V_2), v_save = f3(m, WRFGPU_V_SAVE);
-    const float muv = f2(m, WRFGPU_MUV)(i, j), mx = f2(m, WRFGPU_MSFVX)(i, j);
-    for (int k = m.kds; k <= m.kde - 1; ++k)
-      v_2(i, k, j) = (mx * v_2(i, k, j) + v_save(i, k, j) * (c1h(k) * muv + c2h(k))) / (c1h(k) * muvs + c2h(k));
+    const float muv = f2(m, WRFGPU_MUV).ro(i, j), mx = f2(m, WRFGPU_MSFVX).ro(i, j);
+    chunked_levels<8, L2>(
+        m.kds, m.kde - 1, [&](int k, L2& d) { d.x = v_2(i, k, j); d.s = v_save.ro(i, k, j); },
+        [&](int k, const L2& d) { v_2(i, k, j) = (mx * d.x + d.s * (c1h(k) * muv + c2h(k))) / (c1h(k) * muvs + c2h(k)); });
   }
   if (upt) {
     F3 u_2 = f3(m, WRFGPU_U_2), u_save = f3(m, WRFGPU_U_SAVE);
-    const float muu = f2(m, WRFGPU_MUU)(i, j), my = f2(m, WRFGPU_MSFUY)(i, j);
-    for (int k = m.kds; k <= m.kde - 1; ++k)
-      u_2(i, k, j) = (my * u_2(i, k, j) + u_save(i, k, j) * (c1h(k) * muu + c2h(k))) / (c1h(k) * muus + c2h(k));
+    const float muu = f2(m, WRFGPU_MUU).ro(i, j), my = f2(m, WRFGPU_MSFUY).ro(i, j);
+    chunked_levels<8, L2>(
+        m.kds, m.kde - 1, [&](int k, L2& d) { d.x = u_2(i, k, j); d.s = u_save.ro(i, k, j); },
+        [&](int k, const L2& d) { u_2(i, k, j) = (my * d.x + d.s * (c1h(k) * muu + c2h(k))) / (c1h(k) * muus + c2h(k)); });
   }
   if (upt && vpt) {
     F3 w_2 = f3(m, WRFGPU_W_2), w_save = f3(m, WRFGPU_W_SAVE), ph_2 = f3(m, WRFGPU_PH_2), ph_save = f3(m, WRFGPU_PH_SAVE),
        ww = f3(m, WRFGPU_WW), ww1 = f3(m, WRFGPU_WW1), t_2 = f3(m, WRFGPU_T_2), t_save = f3(m, WRFGPU_T_SAVE),
        h_diabatic = f3(m, WRFGPU_H_DIABATIC);
-    const float mt = f2(m, WRFGPU_MUT)(i, j), mts = MU(i, j), my = f2(m, WRFGPU_MSFTY)(i, j);
-    for (int k = m.kds; k <= m.kde; ++k) {
-      w_2(i, k, j) = (my * w_2(i, k, j) + w_save(i, k, j) * (c1f(k) * mt + c2f(k))) / (c1f(k) * mts + c2f(k));
-      ph_2(i, k, j) = ph_2(i, k, j) + ph_save(i, k, j);
-      ww(i, k, j) = ww(i, k, j) + ww1(i, k, j);
-    }
-    if (rk_step < m.cf.rk_ord) {
-      for (int k = m.kds; k <= m.kde - 1; ++k)
-        t_2(i, k, j) = (t_2(i, k, j) + t_save(i, k, j) * (c1h(k) * mt + c2h(k))) / (c1h(k) * mts + c2h(k));
-    } else {
-      for (int k = m.kds; k <= m.kde - 1; ++k)
-        t_2(i, k, j) = (t_2(i, k, j) - st.dts_rk * float(st.nsmall) * (c1h(k) * mt + c2h(k)) * h_diabatic(i, k, j) +
-                        t_save(i, k, j) * (c1h(k) * mt + c2h(k))) / (c1h(k) * mts + c2h(k));
-    }
+    const float mt = f2(m, WRFGPU_MUT).ro(i, j), mts = MU(i, j), my = f2(m, WRFGPU_MSFTY).ro(i, j);
+    const bool last = rk_step >= m.cf.rk_ord;
+    struct LW { float w, ws, p, ps, ww, ww1, t, ts, hd; };
+    chunked_levels<6, LW>(
+        m.kds, m.kde,
+        [&](int k, LW& d) {
+          d.w = w_2(i, k, j); d.ws = w_save.ro(i, k, j); d.p = ph_2(i, k, j); d.ps = ph_save.ro(i, k, j);
+          d.ww = ww(i, k, j); d.ww1 = ww1.ro(i, k, j);
+          if (k <= m.kde - 1) {
+            d.t = t_2(i, k, j); d.ts = t_save.ro(i, k, j); d.hd = last ? h_diabatic.ro(i, k, j) : 0.f;
+          }
+        },
+        [&](int k, const LW& d) {
+          w_2(i, k, j) = (my * d.w + d.ws * (c1f(k) * mt + c2f(k))) / (c1f(k) * mts + c2f(k));
+          ph_2(i, k, j) = d.p + d.ps;
+          ww(i, k, j) = d.ww + d.ww1;
+          if (k <= m.kde - 1) {
+            if (!last)
+              t_2(i, k, j) = (d.t + d.ts * (c1h(k) * mt + c2h(k))) / (c1h(k) * mts + c2h(k));
+            else
+              t_2(i, k, j) = (d.t - st.dts_rk * float(st.nsmall) * (c1h(k) * mt + c2h(k)) * d.hd +
+                              d.ts * (c1h(k) * mt + c2h(k))) / (c1h(k) * mts + c2h(k));
+          }
+        });
     F2 mu_2 = f2(m, WRFGPU_MU_2);
     mu_2(i, j) = mu_2(i, j) + f2(m, WRFGPU_MU_SAVE)(i, j);
   }

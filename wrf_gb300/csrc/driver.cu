@@ -380,11 +380,11 @@ struct Ensemble {
         fill(j);
       }
       // rk_tendency (module_em.F:370-781)
-      mark(PH_TEND_U); launch_tend_u(l3, nb3, TF_ALL, stream);
-      mark(PH_TEND_V); launch_tend_v(l3, nb3, TF_ALL, stream);
+      mark(PH_TEND_U); launch_tend_u_col(LST(), nb_st, TF_ALL, stream);
+      mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream);
       mark(PH_TEND_W); launch_tend_w(l2, nb2, TF_ALL, stream);
-      mark(PH_TEND_T); launch_tend_t(l3, nb3, TF_ZERO | TF_ADV, stream);
-      mark(PH_TEND_PH); launch_tend_ph(l3, nb3, TF_ZERO | TF_ADV, stream);
+      mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
+      mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       if (cfl_check) { mark(PH_CFL); launch_cfl_check(l3, nb3, stream); }
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
       mark(PH_SSP); launch_small_step_prep(l2, nb2, a, stream);

@@ -21,11 +21,7 @@ namespace wrfgpu {
 
 // ---------------------------------------------------------------- ru_tend
 template <int FL>
-__global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
-  BlockPos bp = block_pos(L);
-  const Mem& m = block_member(L.mem, bp.m);
-  if (!bp.valid) return;
-  const int i = bp.i, j = bp.j, k = bp.k;
+__device__ __forceinline__ void tend_u_point(const Mem& m, const int i, const int j, const int k) {
   F3 tend = f3(m, WRFGPU_RU_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
   const int ktf = min(m.kte, m.kde - 1);
@@ -108,13 +104,47 @@ __global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
   tend(i, k, j) = t;
 }
 
-// ---------------------------------------------------------------- rv_tend
 template <int FL>
-__global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
+__global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const int i = bp.i, j = bp.j, k = bp.k;
+  tend_u_point<FL>(m, bp.i, bp.j, bp.k);
+}
+
+// column form: one thread per (i, j) of a tile, levels in order, the
+// inputs two levels ahead prefetched into L2
+template <int FL>
+__global__ void __launch_bounds__(TX* TY) k_tend_u_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  auto pf = [&](const F3& a, int kk) {
+    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
+  };
+  for (int k = m.kms; k <= m.kme; ++k) {
+    pf(f3(m, WRFGPU_U_2), k + 2);
+    pf(f3(m, WRFGPU_RU), k + 2);
+    pf(f3(m, WRFGPU_RV), k + 2);
+    pf(f3(m, WRFGPU_RW), k + 2);
+    pf(f3(m, WRFGPU_WW), k + 2);
+    pf(f3(m, WRFGPU_PH_2), k + 2);
+    pf(f3(m, WRFGPU_ALT), k + 2);
+    pf(f3(m, WRFGPU_P), k + 2);
+    pf(f3(m, WRFGPU_PB), k + 2);
+    pf(f3(m, WRFGPU_AL), k + 2);
+    pf(f3(m, WRFGPU_PHP), k + 2);
+    pf(f3(m, WRFGPU_CQU), k + 2);
+    pf(f3(m, WRFGPU_V_2), k + 2);
+    pf(f3(m, WRFGPU_RU_TEND), k + 2);
+    tend_u_point<FL>(m, i, j, k);
+  }
+}
+
+// ---------------------------------------------------------------- rv_tend
+template <int FL>
+__device__ __forceinline__ void tend_v_point(const Mem& m, const int i, const int j, const int k) {
   F3 tend = f3(m, WRFGPU_RV_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
   const int ktf = min(m.kte, m.kde - 1);
@@ -196,6 +226,44 @@ __global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
             (rw(i, k + 1, j - 1) + rw(i, k, j - 1) + rw(i, k + 1, j) + rw(i, k, j));
   }
   tend(i, k, j) = t;
+}
+
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid) return;
+  tend_v_point<FL>(m, bp.i, bp.j, bp.k);
+}
+
+// column form: one thread per (i, j) of a tile, levels in order, the
+// inputs two levels ahead prefetched into L2
+template <int FL>
+__global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  auto pf = [&](const F3& a, int kk) {
+    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
+  };
+  for (int k = m.kms; k <= m.kme; ++k) {
+    pf(f3(m, WRFGPU_V_2), k + 2);
+    pf(f3(m, WRFGPU_RU), k + 2);
+    pf(f3(m, WRFGPU_RV), k + 2);
+    pf(f3(m, WRFGPU_RW), k + 2);
+    pf(f3(m, WRFGPU_WW), k + 2);
+    pf(f3(m, WRFGPU_PH_2), k + 2);
+    pf(f3(m, WRFGPU_ALT), k + 2);
+    pf(f3(m, WRFGPU_P), k + 2);
+    pf(f3(m, WRFGPU_PB), k + 2);
+    pf(f3(m, WRFGPU_AL), k + 2);
+    pf(f3(m, WRFGPU_PHP), k + 2);
+    pf(f3(m, WRFGPU_CQV), k + 2);
+    pf(f3(m, WRFGPU_U_2), k + 2);
+    pf(f3(m, WRFGPU_RV_TEND), k + 2);
+    tend_v_point<FL>(m, i, j, k);
+  }
 }
 
 // ---------------------------------------------------------------- rw_tend
@@ -290,11 +358,7 @@ __global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
 
 // ---------------------------------------------------------------- t_tend
 template <int FL>
-__global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
-  BlockPos bp = block_pos(L);
-  const Mem& m = block_member(L.mem, bp.m);
-  if (!bp.valid) return;
-  const int i = bp.i, j = bp.j, k = bp.k;
+__device__ __forceinline__ void tend_t_point(const Mem& m, const int i, const int j, const int k) {
   F3 tend = f3(m, WRFGPU_T_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
@@ -339,13 +403,38 @@ __global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
   tend(i, k, j) = t;
 }
 
-// ---------------------------------------------------------------- ph_tend
 template <int FL>
-__global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
+__global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
-  const int i = bp.i, j = bp.j, k = bp.k;
+  tend_t_point<FL>(m, bp.i, bp.j, bp.k);
+}
+
+// column form: one thread per (i, j) of a tile, levels in order, the
+// inputs two levels ahead prefetched into L2
+template <int FL>
+__global__ void __launch_bounds__(TX* TY) k_tend_t_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  auto pf = [&](const F3& a, int kk) {
+    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
+  };
+  for (int k = m.kms; k <= m.kme; ++k) {
+    pf(f3(m, WRFGPU_T_2), k + 2);
+    pf(f3(m, WRFGPU_RU), k + 2);
+    pf(f3(m, WRFGPU_RV), k + 2);
+    pf(f3(m, WRFGPU_WW), k + 2);
+    pf(f3(m, WRFGPU_T_TEND), k + 2);
+    tend_t_point<FL>(m, i, j, k);
+  }
+}
+
+// ---------------------------------------------------------------- ph_tend
+template <int FL>
+__device__ __forceinline__ void tend_ph_point(const Mem& m, const int i, const int j, const int k) {
   F3 tend = f3(m, WRFGPU_PH_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte && k >= m.kts && k <= m.kte;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1);
@@ -411,6 +500,37 @@ __global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
   tend(i, k, j) = t;
 }
 
+template <int FL>
+__global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid) return;
+  tend_ph_point<FL>(m, bp.i, bp.j, bp.k);
+}
+
+// column form: one thread per (i, j) of a tile, levels in order, the
+// inputs two levels ahead prefetched into L2
+template <int FL>
+__global__ void __launch_bounds__(TX* TY) k_tend_ph_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  auto pf = [&](const F3& a, int kk) {
+    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
+  };
+  for (int k = m.kms; k <= m.kme; ++k) {
+    pf(f3(m, WRFGPU_PH_2), k + 2);
+    pf(f3(m, WRFGPU_PHB), k + 2);
+    pf(f3(m, WRFGPU_U_2), k + 2);
+    pf(f3(m, WRFGPU_V_2), k + 2);
+    pf(f3(m, WRFGPU_WW), k + 2);
+    pf(f3(m, WRFGPU_W_2), k + 2);
+    pf(f3(m, WRFGPU_PH_TEND), k + 2);
+    tend_ph_point<FL>(m, i, j, k);
+  }
+}
+
 // ---------------------------------------------------------------- launchers
 #define DISPATCH_FL(KERNEL, GRID, BLOCK, S, FLAGS)                                       \
   switch (FLAGS) {                                                                      \
@@ -429,5 +549,9 @@ void launch_tend_v(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATC
 void launch_tend_w(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_w, nb, dim3(BX, BY), s, flags) }
 void launch_tend_t(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t, nb, dim3(BX, BY), s, flags) }
 void launch_tend_ph(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph, nb, dim3(BX, BY), s, flags) }
+void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_u_col, nb, dim3(TX, TY), s, flags) }
+void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_v_col, nb, dim3(TX, TY), s, flags) }
+void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t_col, nb, dim3(TX, TY), s, flags) }
+void launch_tend_ph_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph_col, nb, dim3(TX, TY), s, flags) }
 
 }  // namespace wrfgpu

@@ -48,6 +48,11 @@ void launch_tend_w(const Launch& L2, int nblocks, int flags, cudaStream_t s);
 void launch_tend_t(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_zero_save(const Launch& L3, int nblocks, cudaStream_t s);
+// column forms over tiles of the staggered extents
+void launch_tend_u_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
+void launch_tend_v_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
+void launch_tend_t_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
+void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 
 // acoustic steps
 void launch_small_step_prep(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s);

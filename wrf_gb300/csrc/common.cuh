@@ -20,6 +20,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include "../../include/wrfgpu.h"
+#include "cdiv.h"
 
 namespace wrfgpu {
 
@@ -101,58 +102,56 @@ __host__ __device__ inline Stage stage_of(const Mem& m, int rk_step) {
 // ro(): read through the read-only (non-coherent) path, for arrays a kernel
 // never writes: such loads do not alias the kernel's stores, so they can be
 // issued ahead of them instead of waiting behind every store.
+//
+// Offsets are 32-bit: a field holds fewer than 2^31 elements (checked when a
+// member is created), so one index costs an integer multiply-add per distinct
+// (k, j) and a single wide add per field instead of 64-bit products.
 struct F3 {
-  float* __restrict__ p; long long sk, sj; int ims, kms, jms;
-  __device__ __forceinline__ float& operator()(int i, int k, int j) const {
-    return p[(long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj];
-  }
-  __device__ __forceinline__ float ro(int i, int k, int j) const {
-    return __ldg(p + ((long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj));
-  }
+  float* __restrict__ p; int sk, sj, ims, kms, jms;
+  __device__ __forceinline__ int off(int i, int k, int j) const { return (i - ims) + (k - kms) * sk + (j - jms) * sj; }
+  __device__ __forceinline__ float& operator()(int i, int k, int j) const { return p[off(i, k, j)]; }
+  __device__ __forceinline__ float ro(int i, int k, int j) const { return __ldg(p + off(i, k, j)); }
 };
 struct F2 {
-  float* __restrict__ p; long long sj; int ims, jms;
-  __device__ __forceinline__ float& operator()(int i, int j) const {
-    return p[(long long)(i - ims) + (long long)(j - jms) * sj];
-  }
-  __device__ __forceinline__ float ro(int i, int j) const {
-    return __ldg(p + ((long long)(i - ims) + (long long)(j - jms) * sj));
-  }
+  float* __restrict__ p; int sj, ims, jms;
+  __device__ __forceinline__ float& operator()(int i, int j) const { return p[(i - ims) + (j - jms) * sj]; }
+  __device__ __forceinline__ float ro(int i, int j) const { return __ldg(p + ((i - ims) + (j - jms) * sj)); }
 };
 struct F1 {
   const float* __restrict__ p; int kms;
   __device__ __forceinline__ float operator()(int k) const { return __ldg(p + (k - kms)); }
 };
 struct D3 {
-  double* __restrict__ p; long long sk, sj; int ims, kms, jms;
+  double* __restrict__ p; int sk, sj, ims, kms, jms;
   __device__ __forceinline__ double& operator()(int i, int k, int j) const {
-    return p[(long long)(i - ims) + (long long)(k - kms) * sk + (long long)(j - jms) * sj];
+    return p[(i - ims) + (k - kms) * sk + (j - jms) * sj];
   }
 };
-__device__ __forceinline__ F3 f3(const Mem& m, int id) { return F3{m.f3[id], m.sk, m.sj, m.ims, m.kms, m.jms}; }
-__device__ __forceinline__ F3 f3p(const Mem& m, float* p) { return F3{p, m.sk, m.sj, m.ims, m.kms, m.jms}; }
+__device__ __forceinline__ F3 f3(const Mem& m, int id) { return F3{m.f3[id], (int)m.sk, (int)m.sj, m.ims, m.kms, m.jms}; }
+__device__ __forceinline__ F3 f3p(const Mem& m, float* p) { return F3{p, (int)m.sk, (int)m.sj, m.ims, m.kms, m.jms}; }
 __device__ __forceinline__ F2 f2(const Mem& m, int id) {
-  return F2{m.f2[id - WRFGPU_F2D_BASE], m.s2, m.ims, m.jms};
+  return F2{m.f2[id - WRFGPU_F2D_BASE], (int)m.s2, m.ims, m.jms};
 }
 __device__ __forceinline__ F1 f1(const Mem& m, int id) { return F1{m.f1[id - WRFGPU_F1D_BASE], m.kms}; }
-__device__ __forceinline__ D3 d3(const Mem& m, double* p) { return D3{p, m.sk, m.sj, m.ims, m.kms, m.jms}; }
+__device__ __forceinline__ D3 d3(const Mem& m, double* p) { return D3{p, (int)m.sk, (int)m.sj, m.ims, m.kms, m.jms}; }
 
 // ---------------------------------------------------------------------------
 // Flux operators (module_advect_em.F:172-186; advect_scalar_pd's pre-divided
 // coefficients :6165-6185).  sign(1,time_step) == 1 for forward runs.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float sgn1(float a) { return copysignf(1.f, a); }
+// The divisions by 12 and 60 round exactly as IEEE division (cdiv.h).
 __device__ __forceinline__ float flux4(float qm2, float qm1, float q, float qp1) {
-  return (7.f * (q + qm1) - (qp1 + qm2)) / 12.0f;
+  return wrfgpu_div12(7.f * (q + qm1) - (qp1 + qm2));
 }
 __device__ __forceinline__ float flux3(float qm2, float qm1, float q, float qp1, float ua) {
-  return flux4(qm2, qm1, q, qp1) + 1.f * sgn1(ua) * ((qp1 - qm2) - 3.f * (q - qm1)) / 12.0f;
+  return flux4(qm2, qm1, q, qp1) + wrfgpu_div12(1.f * sgn1(ua) * ((qp1 - qm2) - 3.f * (q - qm1)));
 }
 __device__ __forceinline__ float flux6(float qm3, float qm2, float qm1, float q, float qp1, float qp2) {
-  return (37.f * (q + qm1) - 8.f * (qp1 + qm2) + (qp2 + qm3)) / 60.0f;
+  return wrfgpu_div60(37.f * (q + qm1) - 8.f * (qp1 + qm2) + (qp2 + qm3));
 }
 __device__ __forceinline__ float flux5(float qm3, float qm2, float qm1, float q, float qp1, float qp2, float ua) {
-  return flux6(qm3, qm2, qm1, q, qp1, qp2) - 1.f * sgn1(ua) * ((qp2 - qm3) - 5.f * (qp1 - qm2) + 10.f * (q - qm1)) / 60.0f;
+  return flux6(qm3, qm2, qm1, q, qp1, qp2) - wrfgpu_div60(1.f * sgn1(ua) * ((qp2 - qm3) - 5.f * (qp1 - qm2) + 10.f * (q - qm1)));
 }
 __device__ __forceinline__ float pflux4(float qm2, float qm1, float q, float qp1) {
   return (7.f / 12.f) * (q + qm1) - (1.f / 12.f) * (qp1 + qm2);

@@ -68,6 +68,9 @@ static int check_desc(const WrfGpuDomainDesc& d) {
   if (c.open_xs || c.open_xe || c.open_ys || c.open_ye || c.specified || c.nested || c.polar) return WRFGPU_E_ARG;
   if (c.hypsometric_opt != 1 && c.hypsometric_opt != 2) return WRFGPU_E_ARG;
   if (d.scalars.dt <= 0 || d.scalars.dx <= 0 || d.scalars.dy <= 0) return WRFGPU_E_ARG;
+  // the kernels index a field with 32-bit offsets
+  const long long pts = (long long)(d.ide + 2 * WRFGPU_HALO + 4) * d.kde * (d.jde + 2 * WRFGPU_HALO);
+  if (pts >= (1ll << 31)) return WRFGPU_E_ARG;
   return WRFGPU_OK;
 }
 

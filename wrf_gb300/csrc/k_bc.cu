@@ -57,22 +57,26 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
   const int nyr = yr1 - yr0 + 1;
   const int xj0 = m.jds, xj1 = m.jde + jstag;
   const int yi0 = m.ims, yi1 = us ? m.ime : m.ide + 3;
-  const long long nxpts = px ? (long long)(nxl + nxr) * (xj1 - xj0 + 1) : 0;
-  const long long nypts = (py || sy) ? (long long)(WRFGPU_HALO + nyr) * (yi1 - yi0 + 1) : 0;
-  const long long total = (nxpts + nypts) * nk;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    long long pt = t / nk;
-    int k = (int)(t % nk) + m.kts;
+  // 32-bit index space (a member's field holds < 2^31 points); points of a
+  // level are consecutive, i (or the x-halo column) fastest
+  const int nxw = nxl + nxr, nyi = yi1 - yi0 + 1;
+  const int nxpts = px ? nxw * (xj1 - xj0 + 1) : 0;
+  const int nypts = (py || sy) ? (WRFGPU_HALO + nyr) * nyi : 0;
+  const int npts = nxpts + nypts;
+  const int total = npts * nk;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int kk = t / npts;
+    const int pt = t - kk * npts;
+    const int k = kk + m.kts;
     int ti, tj;
     if (pt < nxpts) {
-      int c = (int)(pt % (nxl + nxr));
-      tj = xj0 + (int)(pt / (nxl + nxr));
+      const int r = pt / nxw, c = pt - r * nxw;
+      tj = xj0 + r;
       ti = c < nxl ? m.ids - nxl + c : xr0 + (c - nxl);
     } else {
-      long long q = pt - nxpts;
-      int r = (int)(q % (WRFGPU_HALO + nyr));
-      ti = yi0 + (int)(q / (WRFGPU_HALO + nyr));
+      const int q = pt - nxpts;
+      const int r = q / nyi;
+      ti = yi0 + (q - r * nyi);
       tj = r < WRFGPU_HALO ? m.jds - WRFGPU_HALO + r : yr0 + (r - WRFGPU_HALO);
     }
     bool neg = false;
@@ -83,7 +87,7 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
       float val = a(si, k, sj);
       a(ti, k, tj) = neg ? -val : val;
     } else {
-      F2 a{base, m.s2, m.ims, m.jms};
+      F2 a{base, (int)m.s2, m.ims, m.jms};
       float val = a(si, sj);
       a(ti, tj) = neg ? -val : val;
     }

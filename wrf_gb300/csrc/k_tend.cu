@@ -112,35 +112,6 @@ __global__ void __launch_bounds__(BX* BY) k_tend_u(Launch L) {
   tend_u_point<FL>(m, bp.i, bp.j, bp.k);
 }
 
-// column form: one thread per (i, j) of a tile, levels in order, the
-// inputs two levels ahead prefetched into L2
-template <int FL>
-__global__ void __launch_bounds__(TX* TY) k_tend_u_col(TileLaunch L) {
-  const TilePos tp = tile_pos(L, false, true);
-  const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
-  auto pf = [&](const F3& a, int kk) {
-    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
-  };
-  for (int k = m.kms; k <= m.kme; ++k) {
-    pf(f3(m, WRFGPU_U_2), k + 2);
-    pf(f3(m, WRFGPU_RU), k + 2);
-    pf(f3(m, WRFGPU_RV), k + 2);
-    pf(f3(m, WRFGPU_RW), k + 2);
-    pf(f3(m, WRFGPU_WW), k + 2);
-    pf(f3(m, WRFGPU_PH_2), k + 2);
-    pf(f3(m, WRFGPU_ALT), k + 2);
-    pf(f3(m, WRFGPU_P), k + 2);
-    pf(f3(m, WRFGPU_PB), k + 2);
-    pf(f3(m, WRFGPU_AL), k + 2);
-    pf(f3(m, WRFGPU_PHP), k + 2);
-    pf(f3(m, WRFGPU_CQU), k + 2);
-    pf(f3(m, WRFGPU_V_2), k + 2);
-    pf(f3(m, WRFGPU_RU_TEND), k + 2);
-    tend_u_point<FL>(m, i, j, k);
-  }
-}
 
 // ---------------------------------------------------------------- rv_tend
 template <int FL>
@@ -236,42 +207,13 @@ __global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
   tend_v_point<FL>(m, bp.i, bp.j, bp.k);
 }
 
-// column form: one thread per (i, j) of a tile, levels in order, the
-// inputs two levels ahead prefetched into L2
-template <int FL>
-__global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
-  const TilePos tp = tile_pos(L, false, true);
-  const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
-  auto pf = [&](const F3& a, int kk) {
-    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
-  };
-  for (int k = m.kms; k <= m.kme; ++k) {
-    pf(f3(m, WRFGPU_V_2), k + 2);
-    pf(f3(m, WRFGPU_RU), k + 2);
-    pf(f3(m, WRFGPU_RV), k + 2);
-    pf(f3(m, WRFGPU_RW), k + 2);
-    pf(f3(m, WRFGPU_WW), k + 2);
-    pf(f3(m, WRFGPU_PH_2), k + 2);
-    pf(f3(m, WRFGPU_ALT), k + 2);
-    pf(f3(m, WRFGPU_P), k + 2);
-    pf(f3(m, WRFGPU_PB), k + 2);
-    pf(f3(m, WRFGPU_AL), k + 2);
-    pf(f3(m, WRFGPU_PHP), k + 2);
-    pf(f3(m, WRFGPU_CQV), k + 2);
-    pf(f3(m, WRFGPU_U_2), k + 2);
-    pf(f3(m, WRFGPU_RV_TEND), k + 2);
-    tend_v_point<FL>(m, i, j, k);
-  }
-}
 
 // ---------------------------------------------------------------- rw_tend
 // Column kernel: pg_buoy_w overwrites cqw(k) with 1/(1+cqw(k)) after the
 // k = kde point has read the original cqw(kde-1), so each column is walked
 // in order by one thread.
 template <int FL>
-__global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
+__global__ void __launch_bounds__(BX* BY, 5) k_tend_w(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
@@ -298,7 +240,21 @@ __global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
     float vel = 0.5f * (rom(i, kk, j) + rom(i, kk - 1, j));
     return vel * flux3(w(i, kk - 2, j), w(i, kk - 1, j), w(i, kk, j), w(i, kk + 1, j), -vel);
   };
+  // column constants, formed in the order of the per-level expressions
   const float mrdy = msftx(i, j) * rdy, mrdx = msftx(i, j) * rdx;
+  const float rmg = (1.f / msfty(i, j)) * G;
+  const float ratio = msftx(i, j) / msfty(i, j);
+  float e_c = 0.f, cosa05 = 0.f, rsina05 = 0.f;
+  if (FL & TF_COR) {
+    e_c = f2(m, WRFGPU_E)(i, j);
+    cosa05 = f2(m, WRFGPU_COSA)(i, j) * 0.5f;
+    rsina05 = ratio * f2(m, WRFGPU_SINA)(i, j) * 0.5f;
+  }
+  const float ratio05 = ratio * 0.5f;
+  float muf_c = 0.f, mub_c = 0.f;
+  if (FL & TF_PG) { muf_c = f2(m, WRFGPU_MU_2)(i, j); mub_c = f2(m, WRFGPU_MUB)(i, j); }
+  // the vertical flux of face k+1 is the lower face of level k+1
+  float vf_lo = (FL & TF_ADV) && m.kts + 1 <= ktf + 1 ? vf(m.kts + 1) : 0.f;
   for (int k = m.kts; k <= m.kte; ++k) {
     float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
     if (k >= m.kts + 1 && k <= ktf + 1) {
@@ -315,31 +271,32 @@ __global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
           return vel * flux5(w(ii - 3, k, j), w(ii - 2, k, j), w(ii - 1, k, j), w(ii, k, j), w(ii + 1, k, j), w(ii + 2, k, j), vel);
         };
         t = t - mrdx * (fx(i + 1) - fx(i));
-        if (k <= ktf) t = t - rdzu(k) * (vf(k + 1) - vf(k));
-        else t = t + 2.f * rdzu(k - 1) * (vf(k));
+        if (k <= ktf) {
+          const float vf_hi = vf(k + 1);
+          t = t - rdzu(k) * (vf_hi - vf_lo);
+          vf_lo = vf_hi;
+        } else {
+          t = t + 2.f * rdzu(k - 1) * (vf_lo);
+        }
       }
     }
     if (FL & TF_PG) {
-      F2 muf = f2(m, WRFGPU_MU_2), mubf = f2(m, WRFGPU_MUB);
       if (k == kde) {
         float cq1 = 1.f / (1.f + cqw_top);
         float cq2 = cqw_top * cq1;
-        t = t + (1.f / msfty(i, j)) * G *
-                    (cq1 * 2.f * rdnw(k - 1) * (-p(i, k - 1, j)) - (c1f(k) * muf(i, j)) - cq2 * (c1f(k) * mubf(i, j) + c2f(k)));
+        t = t + rmg * (cq1 * 2.f * rdnw(k - 1) * (-p(i, k - 1, j)) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       } else if (k >= 2) {
-        float cq1 = 1.f / (1.f + cqw(i, k, j));
-        float cq2 = cqw(i, k, j) * cq1;
+        const float cqk = cqw(i, k, j);
+        float cq1 = 1.f / (1.f + cqk);
+        float cq2 = cqk * cq1;
         cqw(i, k, j) = cq1;
-        t = t + (1.f / msfty(i, j)) * G *
-                    (cq1 * rdzu(k) * (p(i, k, j) - p(i, k - 1, j)) - (c1f(k) * muf(i, j)) - cq2 * (c1f(k) * mubf(i, j) + c2f(k)));
+        t = t + rmg * (cq1 * rdzu(k) * (p(i, k, j) - p(i, k - 1, j)) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       }
     }
     if (k >= m.kts + 1 && k <= ktf) {
       if (FL & TF_COR) {
-        F2 e = f2(m, WRFGPU_E), sina = f2(m, WRFGPU_SINA), cosa = f2(m, WRFGPU_COSA);
-        t = t + e(i, j) * (cosa(i, j) * 0.5f * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) -
-                           (msftx(i, j) / msfty(i, j)) * sina(i, j) * 0.5f *
-                               (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))));
+        t = t + e_c * (cosa05 * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) -
+                       rsina05 * (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))));
       }
     }
     if (k >= max(2, m.kts) && k <= ktf) {
@@ -347,7 +304,7 @@ __global__ void __launch_bounds__(BX* BY) k_tend_w(Launch L) {
         F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
         t = t + RERADIUS * (0.5f * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) *
                                 0.5f * (fzm(k) * (u(i, k, j) + u(i + 1, k, j)) + fzp(k) * (u(i, k - 1, j) + u(i + 1, k - 1, j))) +
-                            (msftx(i, j) / msfty(i, j)) * 0.5f *
+                            ratio05 *
                                 (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))) *
                                 0.5f * (fzm(k) * (v(i, k, j) + v(i, k, j + 1)) + fzp(k) * (v(i, k - 1, j) + v(i, k - 1, j + 1))));
       }
@@ -549,8 +506,6 @@ void launch_tend_v(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATC
 void launch_tend_w(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_w, nb, dim3(BX, BY), s, flags) }
 void launch_tend_t(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t, nb, dim3(BX, BY), s, flags) }
 void launch_tend_ph(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph, nb, dim3(BX, BY), s, flags) }
-void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_u_col, nb, dim3(TX, TY), s, flags) }
-void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_v_col, nb, dim3(TX, TY), s, flags) }
 void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t_col, nb, dim3(TX, TY), s, flags) }
 void launch_tend_ph_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph_col, nb, dim3(TX, TY), s, flags) }
 

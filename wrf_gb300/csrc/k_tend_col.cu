@@ -1,0 +1,308 @@
+// Column-marching forms of the u and v large-step tendencies (rk_tendency,
+// module_em.F:129-560 with advect_u / advect_v, module_advect_em.F:205-1700
+// for 5th/3rd order; horizontal_pressure_gradient, module_big_step_utilities_em.F:1585-1718;
+// coriolis :3106-3215; curvature :3234-3363).
+//
+// One thread per (i, j) column of a 32 x 8 tile of the staggered extents,
+// levels kts..kte in order.  The per-point arithmetic is that of the point
+// kernels in k_tend.cu, term for term and in the same order, with three
+// exact reuses across levels:
+//   * the vertical flux of face k+1 is the lower face of level k+1,
+//   * dpn(k+1) of the pressure-gradient correction is dpn(k) one level up,
+//   * values at level k+1 (p, ph, rw of the two columns) carry down,
+// and the column-invariant products of map factors, Coriolis parameters and
+// grid constants are formed once per column, in the reference's order of
+// operations (so every rounding is unchanged).  The next levels' own-column
+// inputs are prefetched into L2 two levels ahead.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wrfgpu {
+
+// ---------------------------------------------------------------- ru_tend
+template <int FL>
+__global__ void __launch_bounds__(TX* TY) k_tend_u_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  const F3 tend = f3(m, WRFGPU_RU_TEND);
+  const int kts = m.kts, kte = m.kte, kde = m.kde, kme = m.kme, ktf = min(kte, kde - 1);
+  const bool acc = j <= min(m.jte, m.jde - 1);
+  if (!acc) {
+    if (FL & TF_ZERO)
+      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+    return;
+  }
+  const F3 u = f3(m, WRFGPU_U_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rw = f3(m, WRFGPU_RW),
+           rom = f3(m, WRFGPU_WW);
+  const F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
+           al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqu = f3(m, WRFGPU_CQU), v = f3(m, WRFGPU_V_2);
+  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW), c1h = f1(m, WRFGPU_C1H),
+           c2h = f1(m, WRFGPU_C2H);
+  const float rdx = m.rdx, rdy = m.rdy;
+  // column constants
+  const F2 msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY);
+  const float msfux_c = msfux(i, j), msfuy_c = msfuy(i, j);
+  const float mrdy = msfux_c * rdy, mrdx = msfux_c * rdx;
+  const float ratio = msfux_c / msfuy_c;
+  const float pgA = ratio * .5f * rdx, pgB = ratio * rdx;
+  float muu_c = 0.f, mu_l = 0.f, mu_r = 0.f;
+  if (FL & TF_PG) {
+    muu_c = f2(m, WRFGPU_MUU)(i, j);
+    mu_l = f2(m, WRFGPU_MU_2)(i - 1, j);
+    mu_r = f2(m, WRFGPU_MU_2)(i, j);
+  }
+  float corA = 0.f, corB = 0.f;
+  if (FL & TF_COR) {
+    const F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), cosa = f2(m, WRFGPU_COSA);
+    corA = ratio * 0.5f * (f(i, j) + f(i - 1, j)) * 0.25f;
+    corB = 0.5f * (e(i, j) + e(i - 1, j)) * 0.5f * (cosa(i, j) + cosa(i - 1, j)) * 0.25f;
+  }
+  float dvx_l = 0.f, dvx_r = 0.f, duy_l = 0.f, duy_r = 0.f;
+  if (FL & TF_CURV) {
+    const F2 msfvx = f2(m, WRFGPU_MSFVX);
+    dvx_r = msfvx(i, j + 1) - msfvx(i, j);
+    dvx_l = msfvx(i - 1, j + 1) - msfvx(i - 1, j);
+    duy_r = msfuy(i + 1, j) - msfuy(i, j);
+    duy_l = msfuy(i, j) - msfuy(i - 1, j);
+  }
+  // own-column window of u for the vertical flux: u(k-1 .. k+2)
+  float um1 = 0.f, u0 = u(i, kts, j), up1 = u(i, kts + 1, j), up2 = (kts + 2 <= kme) ? u(i, kts + 2, j) : 0.f;
+  float vf_lo = 0.f;  // vf(kts) = 0
+  // pressure-gradient carries: p, ph at level k of columns i-1, i; dpn(k)
+  float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f;
+  if (FL & TF_PG) {
+    p_l = p(i - 1, kts, j); p_r = p(i, kts, j);
+    ph_l = ph(i - 1, kts, j); ph_r = ph(i, kts, j);
+    if (kts == 1)
+      dpn_lo = .5f * (m.cf1 * (p(i - 1, 1, j) + p(i, 1, j)) + m.cf2 * (p(i - 1, 2, j) + p(i, 2, j)) +
+                      m.cf3 * (p(i - 1, 3, j) + p(i, 3, j)));
+    else
+      dpn_lo = .5f * (fzm(kts) * (p_l + p_r) + fzp(kts) * (p(i - 1, kts - 1, j) + p(i, kts - 1, j)));
+  }
+  float rw_l = 0.f, rw_r = 0.f;
+  if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i - 1, kts, j); rw_r = rw(i, kts, j); }
+
+  for (int k = kts; k <= ktf; ++k) {
+    if (k + 2 <= kme) {
+      prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
+      prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
+      prefetch_l2(&alt(i, k + 2, j)); prefetch_l2(&al(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
+      prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqu(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
+      prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
+    }
+    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    const float up3 = (k + 3 <= kme) ? u(i, k + 3, j) : 0.f;
+    if (FL & TF_ADV) {
+      auto fy = [&](int jj) {
+        float vel = 0.5f * (rv(i, k, jj) + rv(i - 1, k, jj));
+        return vel * flux5(u(i, k, jj - 3), u(i, k, jj - 2), u(i, k, jj - 1), u(i, k, jj), u(i, k, jj + 1), u(i, k, jj + 2), vel);
+      };
+      t = t - mrdy * (fy(j + 1) - fy(j));
+      auto fx = [&](int ii) {
+        float vel = 0.5f * (ru(ii, k, j) + ru(ii - 1, k, j));
+        return vel * flux5(u(ii - 3, k, j), u(ii - 2, k, j), u(ii - 1, k, j), u(ii, k, j), u(ii + 1, k, j), u(ii + 2, k, j), vel);
+      };
+      t = t - mrdx * (fx(i + 1) - fx(i));
+      // vertical flux of face k+1
+      const int kk = k + 1;
+      float vf_hi;
+      if (kk == kts || kk == kte) vf_hi = 0.f;
+      else if (kk == kts + 1 || kk == ktf)
+        vf_hi = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * up1 + fzp(kk) * u0);
+      else {
+        const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
+        vf_hi = vel * flux3(um1, u0, up1, up2, -vel);
+      }
+      t = t - rdzw(k) * (vf_hi - vf_lo);
+      vf_lo = vf_hi;
+    }
+    float rw_l1 = 0.f, rw_r1 = 0.f;
+    if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i - 1, k + 1, j); rw_r1 = rw(i, k + 1, j); }
+    if (FL & TF_PG) {
+      const int kk = k + 1;
+      float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
+      if (kk == kde) {
+        if (m.cf.top_lid)
+          dpn_hi = .5f * (m.cfn * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) + m.cfn1 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)));
+        else dpn_hi = 0.f;
+      } else {
+        p_l1 = p(i - 1, kk, j); p_r1 = p(i, kk, j);
+        dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+      }
+      const float ph_l1 = ph(i - 1, k + 1, j), ph_r1 = ph(i, k + 1, j);
+      float dpx = pgA * (c1h(k) * muu_c + c2h(k)) *
+                  ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i - 1, k, j)) * (p_r - p_l) +
+                   (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
+      dpx = dpx + pgB * (php(i, k, j) - php(i - 1, k, j)) *
+                      (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
+      t = t - cqu(i, k, j) * dpx;
+      dpn_lo = dpn_hi;
+      p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
+    }
+    if (FL & (TF_COR | TF_CURV)) {
+      const float rvsum = rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j);
+      const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
+      if (FL & TF_COR) t = t + corA * rvsum - corB * rwsum;
+      if (FL & TF_CURV) {
+        const float vx_r = 0.5f * (u0 + u(i + 1, k, j)) * dvx_r * rdy - 0.5f * (v(i, k, j) + v(i, k, j + 1)) * duy_r * rdx;
+        const float vx_l = 0.5f * (u(i - 1, k, j) + u0) * dvx_l * rdy - 0.5f * (v(i - 1, k, j) + v(i - 1, k, j + 1)) * duy_l * rdx;
+        t = t + 0.5f * (vx_r + vx_l) * 0.25f * rvsum - u0 * RERADIUS * 0.25f * rwsum;
+      }
+    }
+    rw_l = rw_l1; rw_r = rw_r1;
+    tend(i, k, j) = t;
+    um1 = u0; u0 = up1; up1 = up2; up2 = up3;
+  }
+  if (FL & TF_ZERO)
+    for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
+}
+
+// ---------------------------------------------------------------- rv_tend
+template <int FL>
+__global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  const F3 tend = f3(m, WRFGPU_RV_TEND);
+  const int kts = m.kts, kte = m.kte, kde = m.kde, kme = m.kme, ktf = min(kte, kde - 1);
+  const bool acc = i <= min(m.ite, m.ide - 1);
+  if (!acc) {
+    if (FL & TF_ZERO)
+      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+    return;
+  }
+  const F3 v = f3(m, WRFGPU_V_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rw = f3(m, WRFGPU_RW),
+           rom = f3(m, WRFGPU_WW);
+  const F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
+           al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqv = f3(m, WRFGPU_CQV), u = f3(m, WRFGPU_U_2);
+  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW), c1h = f1(m, WRFGPU_C1H),
+           c2h = f1(m, WRFGPU_C2H);
+  const float rdx = m.rdx, rdy = m.rdy;
+  const F2 msfvx = f2(m, WRFGPU_MSFVX), msfvy = f2(m, WRFGPU_MSFVY);
+  const float msfvy_c = msfvy(i, j), msfvx_c = msfvx(i, j);
+  const float mrdy = msfvy_c * rdy, mrdx = msfvy_c * rdx;
+  const float ratio = msfvy_c / msfvx_c;
+  const float pgA = ratio * .5f * rdy, pgB = ratio * rdy;
+  float muv_c = 0.f, mu_l = 0.f, mu_r = 0.f;
+  if (FL & TF_PG) {
+    muv_c = f2(m, WRFGPU_MUV)(i, j);
+    mu_l = f2(m, WRFGPU_MU_2)(i, j - 1);
+    mu_r = f2(m, WRFGPU_MU_2)(i, j);
+  }
+  float corA = 0.f, corB = 0.f;
+  if (FL & TF_COR) {
+    const F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), sina = f2(m, WRFGPU_SINA);
+    corA = ratio * 0.5f * (f(i, j) + f(i, j - 1)) * 0.25f;
+    corB = ratio * 0.5f * (e(i, j) + e(i, j - 1)) * 0.5f * (sina(i, j) + sina(i, j - 1)) * 0.25f;
+  }
+  float dvx_r = 0.f, dvx_l = 0.f, duy_r = 0.f, duy_l = 0.f;
+  if (FL & TF_CURV) {
+    const F2 msfuy = f2(m, WRFGPU_MSFUY);
+    dvx_r = msfvx(i, j + 1) - msfvx(i, j);
+    dvx_l = msfvx(i, j) - msfvx(i, j - 1);
+    duy_r = msfuy(i + 1, j) - msfuy(i, j);
+    duy_l = msfuy(i + 1, j - 1) - msfuy(i, j - 1);
+  }
+  float vm1 = 0.f, v0 = v(i, kts, j), vp1 = v(i, kts + 1, j), vp2 = (kts + 2 <= kme) ? v(i, kts + 2, j) : 0.f;
+  float vf_lo = 0.f;
+  float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f;
+  if (FL & TF_PG) {
+    p_l = p(i, kts, j - 1); p_r = p(i, kts, j);
+    ph_l = ph(i, kts, j - 1); ph_r = ph(i, kts, j);
+    if (kts == 1)
+      dpn_lo = .5f * (m.cf1 * (p(i, 1, j - 1) + p(i, 1, j)) + m.cf2 * (p(i, 2, j - 1) + p(i, 2, j)) +
+                      m.cf3 * (p(i, 3, j - 1) + p(i, 3, j)));
+    else
+      dpn_lo = .5f * (fzm(kts) * (p_l + p_r) + fzp(kts) * (p(i, kts - 1, j - 1) + p(i, kts - 1, j)));
+  }
+  float rw_l = 0.f, rw_r = 0.f;
+  if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i, kts, j - 1); rw_r = rw(i, kts, j); }
+
+  for (int k = kts; k <= ktf; ++k) {
+    if (k + 2 <= kme) {
+      prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
+      prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
+      prefetch_l2(&alt(i, k + 2, j)); prefetch_l2(&al(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
+      prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqv(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
+      prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
+    }
+    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    const float vp3 = (k + 3 <= kme) ? v(i, k + 3, j) : 0.f;
+    if (FL & TF_ADV) {
+      auto fy = [&](int jj) {
+        float vel = 0.5f * (rv(i, k, jj) + rv(i, k, jj - 1));
+        return vel * flux5(v(i, k, jj - 3), v(i, k, jj - 2), v(i, k, jj - 1), v(i, k, jj), v(i, k, jj + 1), v(i, k, jj + 2), vel);
+      };
+      t = t - mrdy * (fy(j + 1) - fy(j));
+      auto fx = [&](int ii) {
+        float vel = 0.5f * (ru(ii, k, j) + ru(ii, k, j - 1));
+        return vel * flux5(v(ii - 3, k, j), v(ii - 2, k, j), v(ii - 1, k, j), v(ii, k, j), v(ii + 1, k, j), v(ii + 2, k, j), vel);
+      };
+      t = t - mrdx * (fx(i + 1) - fx(i));
+      const int kk = k + 1;
+      float vf_hi;
+      if (kk == kts || kk == kte) vf_hi = 0.f;
+      else if (kk == kts + 1 || kk == ktf)
+        vf_hi = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * vp1 + fzp(kk) * v0);
+      else {
+        const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
+        vf_hi = vel * flux3(vm1, v0, vp1, vp2, -vel);
+      }
+      t = t - ratio * rdzw(k) * (vf_hi - vf_lo);
+      vf_lo = vf_hi;
+    }
+    float rw_l1 = 0.f, rw_r1 = 0.f;
+    if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i, k + 1, j - 1); rw_r1 = rw(i, k + 1, j); }
+    if (FL & TF_PG) {
+      const int kk = k + 1;
+      float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
+      if (kk == kde) {
+        if (m.cf.top_lid)
+          dpn_hi = .5f * (m.cfn * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) + m.cfn1 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)));
+        else dpn_hi = 0.f;
+      } else {
+        p_l1 = p(i, kk, j - 1); p_r1 = p(i, kk, j);
+        dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+      }
+      const float ph_l1 = ph(i, k + 1, j - 1), ph_r1 = ph(i, k + 1, j);
+      float dpy = pgA * (c1h(k) * muv_c + c2h(k)) *
+                  ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i, k, j - 1)) * (p_r - p_l) +
+                   (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
+      dpy = dpy + pgB * (php(i, k, j) - php(i, k, j - 1)) *
+                      (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
+      t = t - cqv(i, k, j) * dpy;
+      dpn_lo = dpn_hi;
+      p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
+    }
+    if (FL & (TF_COR | TF_CURV)) {
+      const float rusum = ru(i, k, j) + ru(i + 1, k, j) + ru(i, k, j - 1) + ru(i + 1, k, j - 1);
+      const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
+      if (FL & TF_COR) t = t - corA * rusum + corB * rwsum;
+      if (FL & TF_CURV) {
+        const float vx_r = 0.5f * (u(i, k, j) + u(i + 1, k, j)) * dvx_r * rdy - 0.5f * (v0 + v(i, k, j + 1)) * duy_r * rdx;
+        const float vx_l = 0.5f * (u(i, k, j - 1) + u(i + 1, k, j - 1)) * dvx_l * rdy - 0.5f * (v(i, k, j - 1) + v0) * duy_l * rdx;
+        t = t - 0.5f * (vx_r + vx_l) * 0.25f * rusum - ratio * v0 * RERADIUS * 0.25f * rwsum;
+      }
+    }
+    rw_l = rw_l1; rw_r = rw_r1;
+    tend(i, k, j) = t;
+    vm1 = v0; v0 = vp1; vp1 = vp2; vp2 = vp3;
+  }
+  if (FL & TF_ZERO)
+    for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
+}
+
+#define DISPATCH_COL(KERNEL, GRID, S, FLAGS)                                                  \
+  switch (FLAGS) {                                                                            \
+    case TF_ALL: KERNEL<TF_ALL><<<GRID, dim3(TX, TY), 0, S>>>(L); break;                      \
+    case TF_ZERO | TF_ADV | TF_PG: KERNEL<TF_ZERO | TF_ADV | TF_PG><<<GRID, dim3(TX, TY), 0, S>>>(L); break; \
+    default: break;                                                                           \
+  }
+
+void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_COL(k_tend_u_col, nb, s, flags) }
+void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_COL(k_tend_v_col, nb, s, flags) }
+
+}  // namespace wrfgpu

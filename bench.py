@@ -76,6 +76,12 @@ def alg_bytes_per_cell_step(phase, s_pd, s_all, n_acoustic=7):
     return 4 * per.get(phase, 0)
 
 
+PHASE_NAMES = ["step_prep", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",
+               "small_step_prep", "calc_p_rho_0", "calc_coef_w", "advance_uv", "advance_mu_t", "advance_w",
+               "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "scalar_adv_update",
+               "scalar_pd_update", "calc_p_rho_phi"]
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -220,13 +226,154 @@ def cpu_baseline(case, seconds_budget=25.0):
                       "of the reference's FP32 solve_em path)" % (steps, case.name, cores)}
 
 
+def _copy_member_state(src, ms, dst, md, nsp):
+    """Copy every field of member ms of one ensemble into member md of
+    another (same domain description), through host memory."""
+    from wrf_gb300 import abi
+    ids = list(abi.FIELD_ID.values()) + [abi.species_id(s) for s in range(nsp)] + \
+        [abi.species_id(s, True) for s in range(nsp)]
+    for fid in ids:
+        if src.field_size(ms, fid) > 0:
+            dst.set(md, fid, src.get(ms, fid))
+
+
+def ensemble_accuracy(n_members=2, steps=(1, 10, 30, 60)):
+    """FP64-oracle error of the batched mixed form (and of the plain FP32
+    form) on the smallest members of the uneven ensemble: diffwrf relative L2
+    per field after each of `steps` large steps (identical FP32 initial state)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _harness import OracleDomain, interior, serr
+    from wrf_gb300 import abi, cases
+    from wrf_gb300 import gpu as G
+    specs = cases.ensemble_members(seed=4)
+    order = sorted(range(len(specs)), key=lambda q: specs[q][0] * specs[q][1] * specs[q][2])[:n_members]
+    mcases = [cases.ensemble_member(specs[q]) for q in order]
+    cores = os.cpu_count() or 1
+    oracles = [OracleDomain(c, "f64", nthreads=cores, load=False) for c in mcases]
+    for c, o in zip(mcases, oracles):
+        for fid, arr in c.field_items():
+            o.set(fid, arr, as_f32=True)
+    mixed = G.Ensemble.from_cases(mcases, flags=G.FLAG_MIXED)
+    plain = G.Ensemble.from_cases(mcases, flags=0)
+    names = ["u_2", "v_2", "w_2", "t_2", "ph_2", "mu_2", "p", "al"]
+    out = {"members": [c.name for c in mcases], "oracle": "FP64 restatement, same FP32-rounded initial state",
+           "serr": {}}
+    done = 0
+    for n in steps:
+        for o in oracles:
+            o.step(n - done)
+        mixed.step(n - done)
+        plain.step(n - done)
+        done = n
+        mixed.sync()
+        plain.sync()
+        row = {"mixed": {}, "plain": {}}
+        for label, e in (("mixed", mixed), ("plain", plain)):
+            for nm in names + ["qv"]:
+                fid = abi.species_id(0) if nm == "qv" else abi.FIELD_ID[nm]
+                a = [interior(c, fid, e.get(m, fid)) for m, c in enumerate(mcases)]
+                b = [interior(c, fid, o.get(fid)) for c, o in zip(mcases, oracles)]
+                import numpy as np
+                row[label][nm] = float(serr(np.concatenate([x.ravel() for x in a]),
+                                            np.concatenate([x.ravel() for x in b])))
+        out["serr"][str(n)] = row
+    mixed.close()
+    plain.close()
+    return out
+
+
+def ensemble_bench(steps, warmup, n_members=64):
+    """Uneven 64-member ensemble (nx, ny ~ U[64, 256], 41..80 levels, 3 PD
+    scalars, dx = 2 km, dt = 12 s): cell-steps/s of the batched forms (all
+    members in one graph-captured step, FP32 and mixed FP32 + FP64 columns)
+    and of the plain single-domain form run member after member."""
+    from wrf_gb300 import cases
+    from wrf_gb300 import gpu as G
+    specs = cases.ensemble_members(seed=4)[:n_members]
+    descs = [cases.ensemble_member_desc(s) for s in specs]
+    cells_m = [(d.ide - 1) * (d.jde - 1) * (d.kde - 1) for d in descs]
+    cells = sum(cells_m)
+    nsp = descs[0].n_moist + descs[0].n_scalar
+    t0 = time.perf_counter()
+    ens = G.Ensemble(descs, flags=G.FLAG_MIXED)
+    for m, sp in enumerate(specs):
+        ens.load_case(m, cases.ensemble_member(sp))
+    build_s = time.perf_counter() - t0
+    res = {"workload": "c4_ensemble_%d_members" % len(specs), "cells": cells, "species": nsp,
+           "members": len(specs), "state_build_s": round(build_s, 1),
+           "device_gb_mixed": round(ens.device_bytes() / 1e9, 2)}
+    ens.step(warmup)
+    ens.sync()
+    ms = ens.time_steps(steps)
+    res["batched_mixed"] = cells * steps / (ms / 1e3)
+    res["batched_mixed_ms_per_step"] = ms / steps
+    res["batched_mixed_phases_ms"] = {k: round(v[0], 3) for k, v in ens.profile_phases(1).items()}
+    # batched FP32: same members, same state
+    f32 = G.Ensemble(descs, flags=0)
+    for m in range(len(specs)):
+        _copy_member_state(ens, m, f32, m, nsp)
+    f32.step(warmup)
+    f32.sync()
+    ms32 = f32.time_steps(steps)
+    res["batched_f32"] = cells * steps / (ms32 / 1e3)
+    res["batched_f32_phases_ms"] = {k: round(v[0], 3) for k, v in f32.profile_phases(1).items()}
+    f32.close()
+    # plain single-domain form: every member alone, one after another
+    tot_ms = 0.0
+    for m, d in enumerate(descs):
+        dom = G.Ensemble([d], flags=0)
+        _copy_member_state(ens, m, dom, 0, nsp)
+        dom.step(warmup)
+        dom.sync()
+        tot_ms += dom.time_steps(steps)
+        dom.close()
+    res["plain_sequential"] = cells * steps / (tot_ms / 1e3)
+    res["plain_ms_per_step"] = tot_ms / steps
+    res["batched_mixed_over_plain"] = res["batched_mixed"] / res["plain_sequential"]
+    ens.close()
+    return res
+
+
+def run_ensemble_line(args, world, rank, local, pg):
+    """--workload c4: the uneven 64-member ensemble on its own line (value =
+    batched mixed form), with the plain sequential form and the FP64 error."""
+    sampler = ClockSampler(local)
+    sampler.start()
+    res = ensemble_bench(args.steps, args.warmup)
+    clocks = sampler.stop()
+    hbm, hbm_kind = peaks()
+    alg = sum(alg_bytes_per_cell_step(k, 3, 3) for k in PHASE_NAMES)
+    acc = ensemble_accuracy()
+    if rank == 0:
+        line = {
+            "metric": "cell-steps/s", "value": res["batched_mixed"] * world, "unit": "cell-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": res["batched_mixed_ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64-columns",
+            "data": "synthetic (seeded Weisman-Klemp supercell members, uneven sizes)",
+            "config": {"workload": res["workload"], "form": "batched+mixed", "cells": res["cells"],
+                       "global_batch": res["members"], "seq_len": None,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (%.1f GB device state)" % res["device_gb_mixed"]},
+            "roofline": {"bound": "hbm", "achieved": alg * res["batched_mixed"] / 1e9, "peak": hbm,
+                         "peak_kind": hbm_kind, "unit": "GB/s",
+                         "frac": alg * res["batched_mixed"] / 1e9 / hbm, "traffic": None,
+                         "note": "whole-step algorithmic bytes per cell-step (%d B, FP64 column arrays not counted) "
+                                 "x cell-steps/s" % alg},
+            "ensemble": res, "accuracy": acc, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4"])
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the uneven-ensemble comparison (batched+mixed vs plain) added to the default line")
     ap.add_argument("--mixed", action="store_true", help="mixed-precision form (FP64 column steps)")
     ap.add_argument("--nx", type=int, default=None, help="horizontal size of the supercell workload (profiling runs)")
     ap.add_argument("--ref-steps", type=int, default=3)
@@ -242,6 +389,9 @@ def main():
 
     from wrf_gb300 import abi
     from wrf_gb300 import gpu as G
+    if args.workload == "c4":
+        run_ensemble_line(args, world, rank, local, pg)
+        return
     case = make_case(args.workload, args.nx)
     flags = G.FLAG_MIXED if args.mixed else 0
     dom = G.Domain(case, flags=flags)
@@ -266,6 +416,7 @@ def main():
     ms = allreduce_max(pg, ms)
     value = cells * args.steps * world / (ms / 1e3)
 
+    dev_gb = dom.device_bytes() / 1e9
     # per-kernel phases (events between launches, outside the timed region)
     phases = dom.profile_phases(1)
     launches = dom.launches_per_step()
@@ -323,6 +474,19 @@ def main():
                "what": "per step: H2D of the prognostic state (u,v,w,theta,ph,mu,p,al + %d species) from pinned "
                        "host memory, one large step, D2H of the same fields, through the C ABI" % nsp}
 
+    ensemble = None
+    if args.workload == "c2" and not args.nx and not args.no_ensemble:
+        dom.close()
+        try:
+            ensemble = ensemble_bench(max(2, min(args.steps, 3)), 3)
+            hbm_e, _ = peaks()
+            ens_alg = sum(alg_bytes_per_cell_step(k, 3, 3) for k in phases)
+            ensemble["step_alg_bytes_per_cell"] = ens_alg
+            ensemble["batched_mixed_hbm_frac"] = ens_alg * ensemble["batched_mixed"] / 1e9 / hbm_e
+            ensemble["accuracy"] = ensemble_accuracy()
+        except Exception as ex:  # reported, never required
+            ensemble = {"error": repr(ex)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
@@ -341,11 +505,12 @@ def main():
                        "cells": cells, "species": case.desc.n_moist + case.desc.n_scalar,
                        "global_batch": world, "seq_len": None,
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (%.1f GB device state)" % (dom.device_bytes() / 1e9)},
+                       "l2": "inputs larger than L2 (%.1f GB device state)" % (dev_gb)},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches * args.steps,
             "clocks": clocks,
             "phases_ms_per_step": {k: round(v[0], 4) for k, v in phases.items()},
+            "ensemble": ensemble,
         }
         print(json.dumps(line), flush=True)
     if pg is not None:

@@ -394,6 +394,12 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
         qm = mem3(qs, nkm)
         species.append((qm, qm.copy()))
 
+    desc = _make_desc(ide, jde, kde, n_scalar, cfg, dt, dx, m, p_top)
+    meta = dict(dx=dx, dt=dt, ztop=ztop, bubbles=bubbles, n_scalar=n_scalar)
+    return Case(name, desc, f, species, meta)
+
+
+def _make_desc(ide, jde, kde, n_scalar, cfg, dt, dx, m, p_top):
     desc = abi.WrfGpuDomainDesc()
     desc.ide, desc.jde, desc.kde = ide, jde, kde
     desc.n_moist, desc.n_scalar = 1, n_scalar
@@ -404,8 +410,19 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     s.cf1, s.cf2, s.cf3, s.cfn, s.cfn1 = m["cf1"], m["cf2"], m["cf3"], m["cfn"], m["cfn1"]
     s.epssm, s.smdiv, s.emdiv = 0.1, 0.1, 0.01
     s.p_top = p_top
-    meta = dict(dx=dx, dt=dt, ztop=ztop, bubbles=bubbles, n_scalar=n_scalar)
-    return Case(name, desc, f, species, meta)
+    return desc
+
+
+def supercell_desc(nx, ny, kde, dx, dt, ztop, n_scalar=0, hypsometric_opt=2, hodo_radius=15.0):
+    """The domain description supercell_state gives, without building the
+    fields (so that an ensemble can be created before its members' states
+    are built and streamed in one at a time)."""
+    cfg = abi.default_config(periodic_x=True, periodic_y=True)
+    cfg.hypsometric_opt = hypsometric_opt
+    m = eta_metrics(kde)
+    zd, pdry, _, _, _, _, _ = wk_sounding(ztop, hodo_radius=hodo_radius, dry=True)
+    p_top = float(_interp(ztop, zd, pdry))
+    return _make_desc(nx + 1, ny + 1, kde, n_scalar, cfg, dt, dx, m, p_top)
 
 
 # ---------------------------------------------------------------------------
@@ -460,6 +477,11 @@ def ensemble_member(spec, dx=2000.0, dt=12.0, n_scalar=3):
     return supercell_state(nx, ny, kde, dx, dt, 20000.0,
                            [(xc, yc, 1500.0, 10000.0, 10000.0, 1500.0, amp)], rng,
                            n_scalar=n_scalar, name="member_%dx%dx%d" % (nx, ny, kde))
+
+
+def ensemble_member_desc(spec, dx=2000.0, dt=12.0, n_scalar=3):
+    nx, ny, kde = spec[0], spec[1], spec[2]
+    return supercell_desc(nx, ny, kde, dx, dt, 20000.0, n_scalar=n_scalar)
 
 
 def small_case(nx=12, ny=10, kde=12, n_scalar=1, seed=7, dx=2000.0, dt=12.0):

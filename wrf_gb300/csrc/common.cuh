@@ -127,6 +127,23 @@ struct D3 {
     return p[(i - ims) + (k - kms) * sk + (j - jms) * sj];
   }
 };
+// 1 / d for the FP64 column arithmetic of the mixed form: an FP32 seed and
+// two Newton-Raphson steps r <- r + r (1 - d r) in FP64 fma (each squares the
+// relative error: 2^-24 -> 2^-48 -> below the FP64 rounding).  GB300 runs
+// FP64 at 1/64 of the FP32 rate, so this replaces the longer IEEE double
+// division in the per-level recursions; d is well inside the FP32 range.
+__device__ __forceinline__ double drcp(double d) {
+  double r = (double)(1.0f / (float)d);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+// 1 / d in the column precision RC: IEEE division for the plain FP32 form
+// (the reference's rounding), drcp for FP64.
+template <typename RC> __device__ __forceinline__ RC rcp_rc(RC d) { return RC(1.) / d; }
+template <> __device__ __forceinline__ double rcp_rc<double>(double d) { return drcp(d); }
+
 __device__ __forceinline__ F3 f3(const Mem& m, int id) { return F3{m.f3[id], (int)m.sk, (int)m.sj, m.ims, m.kms, m.jms}; }
 __device__ __forceinline__ F3 f3p(const Mem& m, float* p) { return F3{p, (int)m.sk, (int)m.sj, m.ims, m.kms, m.jms}; }
 __device__ __forceinline__ F2 f2(const Mem& m, int id) {

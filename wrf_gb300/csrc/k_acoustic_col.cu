@@ -346,6 +346,7 @@ __global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int r
   MUTS(i, j) = MUT.ro(i, j) + mu;
   MUAVE(i, j) = .5f * ((1.f + epssm) * mu + (1.f - epssm) * muave);
   const float my = msfty.ro(i, j), mx = msftx.ro(i, j);
+  const RC rmy = rcp_rc<RC>((RC)my);  // mixed form only
   // pass 2: omega (recursion one level ahead of theta) and theta
   struct D2 { float ww1, t, ft, t1, t1xm, t1xp, t1ym, t1yp, u0, u1, v0, v1; };
   auto load2 = [&](int k, D2& d) {
@@ -366,7 +367,10 @@ __global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int r
     float wwf_kp1 = 0.f;
     if (k + 1 <= k_end) {
       const int kk = k + 1, kl = kk - 1;
-      wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(kl) * dmdt) + (RC)dv[kk - 1] + ((RC)c1h(kl) * (RC)mu_tend)) / (RC)my;
+      if (sizeof(RC) == 8)
+        wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(kl) * dmdt) + (RC)dv[kk - 1] + ((RC)c1h(kl) * (RC)mu_tend)) * rmy;
+      else
+        wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(kl) * dmdt) + (RC)dv[kk - 1] + ((RC)c1h(kl) * (RC)mu_tend)) / (RC)my;
       wwf_kp1 = (float)wwk - nxt.ww1;
     }
     ww(i, k, j) = wwf_k;
@@ -421,33 +425,32 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
   auto Acoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[0])(i, k, j)) : (RC)f3(m, WRFGPU_A).ro(i, k, j); };
   auto ALcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[1])(i, k, j)) : (RC)f3(m, WRFGPU_ALPHA).ro(i, k, j); };
   auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[2])(i, k, j)) : (RC)f3(m, WRFGPU_GAMMA).ro(i, k, j); };
-  const RC eps1 = RC(1.) + (RC)epssm, eps0 = RC(1.) - (RC)epssm;
+  const float eps1 = 1.f + epssm, eps0 = 1.f - epssm;
 
   // surface w (needs only u, v of the lowest levels)
   const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
-  const RC w1 = (RC)(my * .5f * rdy *
+  const float w1 = (my * .5f * rdy *
                          ((ht.ro(i, j + 1) - ht.ro(i, j)) * (cf1 * v.ro(i, 1, j + 1) + cf2 * v.ro(i, 2, j + 1) + cf3 * v.ro(i, 3, j + 1)) +
                           (ht.ro(i, j) - ht.ro(i, j - 1)) * (cf1 * v.ro(i, 1, j) + cf2 * v.ro(i, 2, j) + cf3 * v.ro(i, 3, j))) +
                      mx * .5f * rdx *
                          ((ht.ro(i + 1, j) - ht.ro(i, j)) * (cf1 * u.ro(i + 1, 1, j) + cf2 * u.ro(i + 1, 2, j) + cf3 * u.ro(i + 1, 3, j)) +
                           (ht.ro(i, j) - ht.ro(i - 1, j)) * (cf1 * u.ro(i, 1, j) + cf2 * u.ro(i, 2, j) + cf3 * u.ro(i, 3, j))));
 
-  // explicit w of level k and forward elimination (the reference's upward loop body)
-  RC wprev = w1;
+  // explicit w of level k (FP32, the reference's expression) and forward
+  // elimination (RC: FP64 in the mixed form)
+  RC wprev = (RC)w1;
   RC wcol[KCOL];
   auto sweep = [&](int k, float wk_in, float rwt, float cqwk, float c2ak, float altk, RC ak, RC alk, float tak,
-                   float c2am, float altm, float tam, RC r_p1, RC r_0, RC r_m1, float ph_p1, float ph_0, float ph_m1) {
-    RC wk = (RC)wk_in + (RC)dts * (RC)rwt +
-            (RC)msft_inv * (RC)cqwk *
-                (+RC(.5) * (RC)dts * (RC)G * (RC)rdn(k) *
-                 ((RC)c2ak * (RC)rdnw(k) / ((RC)c1h(k) * (RC)mutij + (RC)c2h(k)) *
-                      (eps1 * (r_p1 - r_0) + eps0 * ((RC)ph_p1 - (RC)ph_0)) -
-                  (RC)c2am * (RC)rdnw(k - 1) / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) *
-                      (eps1 * (r_0 - r_m1) + eps0 * ((RC)ph_0 - (RC)ph_m1)))) +
-            (RC)dts * (RC)G * (RC)msft_inv *
-                ((RC)rdn(k) * ((RC)c2ak * (RC)altk * (RC)tak - (RC)c2am * (RC)altm * (RC)tam) - ((RC)c1f(k) * (RC)mua));
-    if (!fp64) wk = (RC)(float)wk;
-    wk = (wk - ak * wprev) * alk;
+                   float c2am, float altm, float tam, float r_p1, float r_0, float r_m1, float ph_p1, float ph_0,
+                   float ph_m1) {
+    const float wkf = wk_in + dts * rwt +
+                      msft_inv * cqwk *
+                          (+.5f * dts * G * rdn(k) *
+                           (c2ak * rdnw(k) / (c1h(k) * mutij + c2h(k)) * (eps1 * (r_p1 - r_0) + eps0 * (ph_p1 - ph_0)) -
+                            c2am * rdnw(k - 1) / (c1h(k - 1) * mutij + c2h(k - 1)) *
+                                (eps1 * (r_0 - r_m1) + eps0 * (ph_0 - ph_m1)))) +
+                      dts * G * msft_inv * (rdn(k) * (c2ak * altk * tak - c2am * altm * tam) - (c1f(k) * mua));
+    const RC wk = ((RC)wkf - ak * wprev) * alk;
     wcol[k] = wk;
     wprev = wk;
   };
@@ -464,10 +467,10 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
     d.pht1 = ph_tend.ro(i, k + 1, j); d.w1 = w(i, k + 1, j); d.ww1 = ww.ro(i, k + 1, j);
     d.ph11 = ph_1.ro(i, k + 1, j); d.phb1 = phb.ro(i, k + 1, j);
   };
-  RC rhs[KCOL];
-  rhs[1] = RC(0.);
+  float rhs[KCOL];
+  rhs[1] = 0.f;
   // windows: level L-1 and L-2 values of what the elimination reads
-  RC r_m1 = RC(0.), r_m2 = RC(0.);       // rhs(L-1), rhs(L-2)
+  float r_m1 = 0.f, r_m2 = 0.f;          // rhs(L-1), rhs(L-2)
   float ph_m1 = 0.f, ph_m2 = 0.f;        // ph(L-1), ph(L-2)
   float ta_m1 = 0.f, ta_m2 = 0.f;        // t_2ave(L-1), t_2ave(L-2)
   float c2a_m1 = 0.f, c2a_m2 = 0.f, alt_m1 = 0.f, alt_m2 = 0.f;
@@ -475,7 +478,7 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
   RC a_m1 = RC(0.), al_m1 = RC(0.);
   float ww_k = ww.ro(i, 1, j), ph1_k = ph_1.ro(i, 1, j), phb_k = phb.ro(i, 1, j);
   float wd_k = 0.f;   // wdwn(L)
-  RC rr_k = RC(0.);   // raw rhs(L)
+  float rr_k = 0.f;   // raw rhs(L)
   Lv cur, nxt;
   load(1, cur);
   for (int Lk = 1; Lk <= k_end; ++Lk) {
@@ -485,17 +488,17 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
     tav = (tav + (c1h(Lk) * mua) * T0) / ((c1h(Lk) * mts + c2h(Lk)) * (T0 + cur.t1));
     t_2ave(i, Lk, j) = tav;
     // raw rhs(L+1), wdwn(L+1)
-    const RC rr_next = (RC)(dts * (cur.pht1 + .5f * G * (1.f - epssm) * cur.w1));
+    const float rr_next = dts * (cur.pht1 + .5f * G * (1.f - epssm) * cur.w1);
     float wd_hi;
     if (adv2) wd_hi = rdnw(Lk) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
     else wd_hi = .5f * (cur.ww1 + ww_k) * rdnw(Lk) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
     // rhs(L) complete
-    RC r_0 = RC(0.);
+    float r_0 = 0.f;
     if (Lk >= 2) {
-      RC r = rr_k;
-      if (adv2) r = r - (RC)(dts * ww_k * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
-      else r = r - (RC)(dts * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
-      r = (RC)cur.ph + (RC)my * r / ((RC)c1f(Lk) * (RC)mutij + (RC)c2f(Lk));
+      float r = rr_k;
+      if (adv2) r = r - (dts * ww_k * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
+      else r = r - (dts * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
+      r = cur.ph + my * r / (c1f(Lk) * mutij + c2f(Lk));
       rhs[Lk] = r;
       r_0 = r;
     }
@@ -516,37 +519,35 @@ __global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_s
   // top: rhs(kde) has no omega term
   const int kt = k_end + 1;
   const float ph_top = ph(i, kt, j);
-  RC r_top = (RC)ph_top + (RC)my * rr_k / ((RC)c1f(kt) * (RC)mutij + (RC)c2f(kt));
-  if (m.cf.top_lid) r_top = RC(0.);
+  float r_top = ph_top + my * rr_k / (c1f(kt) * mutij + c2f(kt));
+  if (m.cf.top_lid) r_top = 0.f;
   rhs[kt] = r_top;
   // elimination of level k_end
   sweep(k_end, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_top, r_m1, r_m2,
         ph_top, ph_m1, ph_m2);
   {  // level kde
     const int k = kt;
-    const RC r = (RC)rdnw(k - 1);
-    RC wk = (RC)w(i, k, j) + (RC)dts * (RC)rw_tend.ro(i, k, j) +
-            (RC)msft_inv * (-RC(.5) * (RC)dts * (RC)G / ((RC)c1h(k - 1) * (RC)mutij + (RC)c2h(k - 1)) * (r * r) * RC(2.) *
-                                (RC)c2a_m1 * (eps1 * (r_top - r_m1) + eps0 * ((RC)ph_top - (RC)ph_m1)) -
-                            (RC)dts * (RC)G * (RC(2.) * (RC)rdnw(k - 1) * (RC)c2a_m1 * (RC)alt_m1 * (RC)ta_m1 +
-                                               ((RC)c1f(k) * (RC)mua)));
-    if (m.cf.top_lid) wk = RC(0.);
-    if (!fp64) wk = (RC)(float)wk;
-    wk = (wk - Acoef(k) * wprev) * ALcoef(k);
+    const float r = rdnw(k - 1);
+    float wkf = w(i, k, j) + dts * rw_tend.ro(i, k, j) +
+                msft_inv * (-.5f * dts * G / (c1h(k - 1) * mutij + c2h(k - 1)) * (r * r) * 2.f * c2a_m1 *
+                                (eps1 * (r_top - r_m1) + eps0 * (ph_top - ph_m1)) -
+                            dts * G * (2.f * rdnw(k - 1) * c2a_m1 * alt_m1 * ta_m1 + (c1f(k) * mua)));
+    if (m.cf.top_lid) wkf = 0.f;
+    const RC wk = ((RC)wkf - Acoef(k) * wprev) * ALcoef(k);
     wcol[k] = wk;
   }
-  w(i, 1, j) = (float)w1;
-  // ---- back substitution and geopotential (down)
+  w(i, 1, j) = w1;
+  // ---- back substitution (RC) and geopotential (FP32, from the new w)
   RC wup = wcol[kt];
   w(i, kt, j) = (float)wup;
-  ph(i, kt, j) = (float)(rhs[kt] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wup / ((RC)c1f(kt) * (RC)mts + (RC)c2f(kt)));
+  ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * (float)wup / (c1f(kt) * mts + c2f(kt));
   RC g_nxt = GAcoef(k_end);
   for (int k = k_end; k >= 2; --k) {
     const RC g = g_nxt;
     if (k - 1 >= 2) g_nxt = GAcoef(k - 1);
     const RC wk = wcol[k] - g * wup;
     w(i, k, j) = (float)wk;
-    ph(i, k, j) = (float)(rhs[k] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wk / ((RC)c1f(k) * (RC)mts + (RC)c2f(k)));
+    ph(i, k, j) = rhs[k] + my * .5f * dts * G * eps1 * (float)wk / (c1f(k) * mts + c2f(k));
     wup = wk;
   }
 }

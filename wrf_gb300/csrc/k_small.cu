@@ -156,10 +156,12 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
      rdn = f1(m, WRFGPU_RDN), rdnw = f1(m, WRFGPU_RDNW);
   const int kde = m.kde;
-  const RC MUT = (RC)MUTf(i, j);
-  const RC lid_flag = m.cf.top_lid ? RC(0) : RC(1);
-  const RC tt = (RC(.5) * (RC)st.dts_rk * (RC)G * (RC(1.) + (RC)m.epssm));
-  const RC cof = tt * tt;
+  // a, b, c in FP32 (the reference's expressions and rounding); the
+  // recursion alpha = 1 / (b - a gamma), gamma = c alpha in RC
+  const float MUT = MUTf(i, j);
+  const float lid_flag = m.cf.top_lid ? 0.f : 1.f;
+  const float tt = (.5f * st.dts_rk * G * (1.f + m.epssm));
+  const float cof = tt * tt;
   auto A = [&](int k) -> RC& {
     if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[0])(i, k, j);
     return *(RC*)&f3(m, WRFGPU_A)(i, k, j);
@@ -172,46 +174,46 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
     if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[2])(i, k, j);
     return *(RC*)&f3(m, WRFGPU_GAMMA)(i, k, j);
   };
-  RC a_loc[KMAX + 1];  // A of this column, re-read by the elimination below
+  float a_loc[KMAX + 1];  // A of this column, re-read by the elimination below
   {
     int k = kde - 1;
     A(2) = RC(0.);
-    a_loc[2] = RC(0.);
-    RC r = (RC)rdnw(kde - 1);
-    A(kde) = -RC(2.) * cof * (r * r) * (RC)c2a.ro(i, kde - 1, j) * lid_flag /
-             (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
-    a_loc[kde] = A(kde);
+    a_loc[2] = 0.f;
+    float r = rdnw(kde - 1);
+    const float av = -2.f * cof * (r * r) * c2a.ro(i, kde - 1, j) * lid_flag /
+                     ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k)));
+    A(kde) = (RC)av;
+    a_loc[kde] = av;
     GA(1) = RC(0.);
   }
   for (int kk = 3; kk <= kde - 1; ++kk) {
     int k = kk - 1;
-    const RC av = -(RC)cqw.ro(i, kk, j) * cof * (RC)rdn(kk) * (RC)rdnw(kk - 1) * (RC)c2a.ro(i, kk - 1, j) /
-                  (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
-    A(kk) = av;
+    const float av = -cqw.ro(i, kk, j) * cof * rdn(kk) * rdnw(kk - 1) * c2a.ro(i, kk - 1, j) /
+                     ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k)));
+    A(kk) = (RC)av;
     a_loc[kk] = av;
   }
   RC gprev = GA(1);
   for (int k = 2; k <= kde - 1; ++k) {
-    RC b = RC(1.) + (RC)cqw.ro(i, k, j) * cof * (RC)rdn(k) *
-                        ((RC)rdnw(k) * (RC)c2a.ro(i, k, j) / (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k) * MUT + (RC)c2f(k))) +
-                         (RC)rdnw(k - 1) * (RC)c2a.ro(i, k - 1, j) /
-                             (((RC)c1h(k - 1) * MUT + (RC)c2h(k - 1)) * ((RC)c1f(k) * MUT + (RC)c2f(k))));
-    RC c = -(RC)cqw.ro(i, k, j) * cof * (RC)rdn(k) * (RC)rdnw(k) * (RC)c2a.ro(i, k, j) /
-           (((RC)c1h(k) * MUT + (RC)c2h(k)) * ((RC)c1f(k + 1) * MUT + (RC)c2f(k + 1)));
-    RC al = RC(1.) / (b - a_loc[k] * gprev);
+    const float b = 1.f + cqw.ro(i, k, j) * cof * rdn(k) *
+                              (rdnw(k) * c2a.ro(i, k, j) / ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k))) +
+                               rdnw(k - 1) * c2a.ro(i, k - 1, j) /
+                                   ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k))));
+    const float c = -cqw.ro(i, k, j) * cof * rdn(k) * rdnw(k) * c2a.ro(i, k, j) /
+                    ((c1h(k) * MUT + c2h(k)) * (c1f(k + 1) * MUT + c2f(k + 1)));
+    RC al = rcp_rc<RC>((RC)b - (RC)a_loc[k] * gprev);
     AL(k) = al;
-    gprev = c * al;
+    gprev = (RC)c * al;
     GA(k) = gprev;
   }
   {
     int k = kde;
-    RC r = (RC)rdnw(kde - 1);
-    RC b = RC(1.) + RC(2.) * cof * (r * r) * (RC)c2a.ro(i, kde - 1, j) /
-                        (((RC)c1h(k - 1) * MUT + (RC)c2h(k - 1)) * ((RC)c1f(k) * MUT + (RC)c2f(k)));
-    RC c = RC(0.);
-    RC al = RC(1.) / (b - a_loc[kde] * gprev);
+    float r = rdnw(kde - 1);
+    const float b = 1.f + 2.f * cof * (r * r) * c2a.ro(i, kde - 1, j) /
+                              ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k)));
+    RC al = rcp_rc<RC>((RC)b - (RC)a_loc[kde] * gprev);
     AL(kde) = al;
-    GA(kde) = c * al;
+    GA(kde) = RC(0.) * al;
   }
 }
 

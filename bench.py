@@ -153,7 +153,8 @@ def dist_setup(args):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         pg = dist
     return world, rank, local, pg
@@ -165,12 +166,8 @@ def barrier(pg):
 
 
 def allreduce_max(pg, x):
-    if pg is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    return float(t.item())
+    from wrf_gb300.replicas import reduce_max
+    return reduce_max(pg, x)
 
 
 def run_reference(args, world, rank):
@@ -282,31 +279,38 @@ def ensemble_accuracy(n_members=2, steps=(1, 10, 30, 60)):
     return out
 
 
-def ensemble_bench(steps, warmup, n_members=64):
+def ensemble_bench(steps, warmup, n_members=64, world=1, rank=0, pg=None):
     """Uneven 64-member ensemble (nx, ny ~ U[64, 256], 41..80 levels, 3 PD
     scalars, dx = 2 km, dt = 12 s): cell-steps/s of the batched forms (all
     members in one graph-captured step, FP32 and mixed FP32 + FP64 columns)
-    and of the plain single-domain form run member after member."""
+    and of the plain single-domain form run member after member.  With N
+    ranks the members are sharded by size (no collective on the data path)
+    and the rates are whole-job: all ranks' cells / the slowest rank's time."""
     from wrf_gb300 import cases
     from wrf_gb300 import gpu as G
-    specs = cases.ensemble_members(seed=4)[:n_members]
-    descs = [cases.ensemble_member_desc(s) for s in specs]
-    cells_m = [(d.ide - 1) * (d.jde - 1) * (d.kde - 1) for d in descs]
-    cells = sum(cells_m)
+    from wrf_gb300.replicas import shard_members, job_rate
+    all_specs = cases.ensemble_members(seed=4)[:n_members]
+    all_descs = [cases.ensemble_member_desc(s) for s in all_specs]
+    all_cells = [(d.ide - 1) * (d.jde - 1) * (d.kde - 1) for d in all_descs]
+    mine = shard_members(all_cells, world)[rank]
+    specs = [all_specs[q] for q in mine]
+    descs = [all_descs[q] for q in mine]
+    cells = sum(all_cells[q] for q in mine)
     nsp = descs[0].n_moist + descs[0].n_scalar
     t0 = time.perf_counter()
     ens = G.Ensemble(descs, flags=G.FLAG_MIXED)
     for m, sp in enumerate(specs):
         ens.load_case(m, cases.ensemble_member(sp))
     build_s = time.perf_counter() - t0
-    res = {"workload": "c4_ensemble_%d_members" % len(specs), "cells": cells, "species": nsp,
-           "members": len(specs), "state_build_s": round(build_s, 1),
-           "device_gb_mixed": round(ens.device_bytes() / 1e9, 2)}
+    res = {"workload": "c4_ensemble_%d_members" % len(all_specs), "cells": sum(all_cells), "species": nsp,
+           "members": len(all_specs), "members_per_rank": [len(x) for x in shard_members(all_cells, world)],
+           "state_build_s": round(build_s, 1), "device_gb_mixed": round(ens.device_bytes() / 1e9, 2)}
     ens.step(warmup)
     ens.sync()
+    barrier(pg)
     ms = ens.time_steps(steps)
-    res["batched_mixed"] = cells * steps / (ms / 1e3)
-    res["batched_mixed_ms_per_step"] = ms / steps
+    res["batched_mixed"], _, slow = job_rate(pg, cells * steps, ms / 1e3)
+    res["batched_mixed_ms_per_step"] = 1e3 * slow / steps
     res["batched_mixed_phases_ms"] = {k: round(v[0], 3) for k, v in ens.profile_phases(1).items()}
     # batched FP32: same members, same state
     f32 = G.Ensemble(descs, flags=0)
@@ -314,8 +318,9 @@ def ensemble_bench(steps, warmup, n_members=64):
         _copy_member_state(ens, m, f32, m, nsp)
     f32.step(warmup)
     f32.sync()
+    barrier(pg)
     ms32 = f32.time_steps(steps)
-    res["batched_f32"] = cells * steps / (ms32 / 1e3)
+    res["batched_f32"], _, _ = job_rate(pg, cells * steps, ms32 / 1e3)
     res["batched_f32_phases_ms"] = {k: round(v[0], 3) for k, v in f32.profile_phases(1).items()}
     f32.close()
     # plain single-domain form: every member alone, one after another
@@ -327,8 +332,8 @@ def ensemble_bench(steps, warmup, n_members=64):
         dom.sync()
         tot_ms += dom.time_steps(steps)
         dom.close()
-    res["plain_sequential"] = cells * steps / (tot_ms / 1e3)
-    res["plain_ms_per_step"] = tot_ms / steps
+    res["plain_sequential"], _, slow = job_rate(pg, cells * steps, tot_ms / 1e3)
+    res["plain_ms_per_step"] = 1e3 * slow / steps
     res["batched_mixed_over_plain"] = res["batched_mixed"] / res["plain_sequential"]
     ens.close()
     return res
@@ -339,14 +344,14 @@ def run_ensemble_line(args, world, rank, local, pg):
     batched mixed form), with the plain sequential form and the FP64 error."""
     sampler = ClockSampler(local)
     sampler.start()
-    res = ensemble_bench(args.steps, args.warmup)
+    res = ensemble_bench(args.steps, args.warmup, world=world, rank=rank, pg=pg)
     clocks = sampler.stop()
     hbm, hbm_kind = peaks()
     alg = sum(alg_bytes_per_cell_step(k, 3, 3) for k in PHASE_NAMES)
-    acc = ensemble_accuracy()
+    acc = ensemble_accuracy() if rank == 0 else None
     if rank == 0:
         line = {
-            "metric": "cell-steps/s", "value": res["batched_mixed"] * world, "unit": "cell-steps/s",
+            "metric": "cell-steps/s", "value": res["batched_mixed"], "unit": "cell-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": res["batched_mixed_ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64-columns",
@@ -383,15 +388,22 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
     world, rank, local, pg = dist_setup(args)
-    if args.impl == "reference":
-        run_reference(args, world, rank)
-        return
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank)
+        elif args.workload == "c4":
+            run_ensemble_line(args, world, rank, local, pg)
+        else:
+            run_single(args, world, rank, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
 
+
+def run_single(args, world, rank, local, pg):
+    """One domain per rank (replicas for N > 1): the default line."""
     from wrf_gb300 import abi
     from wrf_gb300 import gpu as G
-    if args.workload == "c4":
-        run_ensemble_line(args, world, rank, local, pg)
-        return
     case = make_case(args.workload, args.nx)
     flags = G.FLAG_MIXED if args.mixed else 0
     dom = G.Domain(case, flags=flags)
@@ -475,7 +487,7 @@ def main():
                        "host memory, one large step, D2H of the same fields, through the C ABI" % nsp}
 
     ensemble = None
-    if args.workload == "c2" and not args.nx and not args.no_ensemble:
+    if args.workload == "c2" and not args.nx and not args.no_ensemble and world == 1:
         dom.close()
         try:
             ensemble = ensemble_bench(max(2, min(args.steps, 3)), 3)
@@ -513,8 +525,6 @@ def main():
             "ensemble": ensemble,
         }
         print(json.dumps(line), flush=True)
-    if pg is not None:
-        pg.destroy_process_group()
 
 
 if __name__ == "__main__":

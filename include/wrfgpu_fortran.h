@@ -108,6 +108,21 @@ int wrfgpu_advect_scalar_pd(const float *field, const float *field_old, float *t
                             const float *rdx, const float *rdy, const float *rdzw, const float *dt,
                             WRFGPU_DIMS_ARGS);
 
+/* No counterpart in the reference: advect_scalar_pd on DEVICE arrays (same
+ * layout and meaning as above, unused arguments dropped; tendency
+ * accumulates), enqueued on `stream` (a cudaStream_t, NULL = default stream)
+ * without allocating device memory.  For callers whose state is already on
+ * the GPU and that cannot allocate there.  The limiter-factor scratch is a
+ * fixed static device array: the memory shape may hold at most 8 Mi points
+ * (WRFGPU_E_SIZE otherwise); the first call on a device does a one-time
+ * setup; calls that overlap in time race on the shared scratch. */
+int wrfgpu_advect_scalar_pd_noalloc(const float *field, const float *field_old, float *tendency,
+                                    const float *ru, const float *rv, const float *rom, const float *c1,
+                                    const float *c2, const float *mut, const float *mub, const float *mu_old,
+                                    const WrfDynConfig *config_flags, const float *msftx, const float *msfty,
+                                    const float *fzm, const float *fzp, const float *rdx, const float *rdy,
+                                    const float *rdzw, const float *dt, WRFGPU_DIMS_ARGS, void *stream);
+
 /* dyn_em/module_small_step_em.F:16 small_step_prep */
 int wrfgpu_small_step_prep(float *u_1, float *u_2, float *v_1, float *v_2, float *w_1, float *w_2, float *t_1,
                            float *t_2, float *ph_1, float *ph_2, const float *mub, float *mu_1, float *mu_2,

@@ -76,6 +76,15 @@ def alg_bytes_per_cell_step(phase, s_pd, s_all, n_acoustic=7):
     return 4 * per.get(phase, 0)
 
 
+# DRAM bytes (read + write) per mass cell of one launch, from the ncu
+# captures summarised in profiles/ (256x256x80 case, inputs far larger than
+# L2; traffic grows with the cells processed, so it scales to other sizes).
+NCU_DRAM_BYTES_PER_CELL = {
+    "scalar_pd_update": 938.6e6 / 5177344,   # k_scalar_pd_update_c2_256x256x80.md
+    "rk_tend_v": 331.0e6 / 5177344,          # k_tend_v_col_c2_256x256x80.md
+    "advance_w": 450.1e6 / 5177344,          # k_advance_w_col_c2_256x256x80.md
+}
+
 PHASE_NAMES = ["step_prep", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",
                "small_step_prep", "calc_p_rho_0", "calc_coef_w", "advance_uv", "advance_mu_t", "advance_w",
                "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "scalar_adv_update",
@@ -441,8 +450,12 @@ def run_single(args, world, rank, local, pg):
     achieved = alg[dom_name] / (dom_ms / 1e3) / 1e9
     step_alg = sum(alg.values())
     step_ms = ms / args.steps
+    traffic = None
+    if dom_name in NCU_DRAM_BYTES_PER_CELL and case.desc.n_scalar == 10:
+        traffic = NCU_DRAM_BYTES_PER_CELL[dom_name] * cells
     roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "peak_kind": hbm_kind,
-                "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                "traffic_note": "DRAM bytes per launch from the ncu capture of the 256x256x80 case, scaled by cells",
                 "alg_bytes_per_step": alg[dom_name], "ms_per_step": dom_ms, "launches_per_step": dom_n,
                 "step_alg_bytes": step_alg, "step_achieved": step_alg / (step_ms / 1e3) / 1e9,
                 "step_frac": step_alg / (step_ms / 1e3) / 1e9 / hbm,

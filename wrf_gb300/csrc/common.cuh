@@ -38,10 +38,14 @@ constexpr float RERADIUS = 1.f / 6370.0e03f;
 
 // Tensor maps (TMA descriptors) of every 3-D field buffer of a member: slot
 // f < WRFGPU_N3D for the fields, WRFGPU_N3D + 3 s + {0, 1, 2} for species s's
-// buffers (first current, old, first spare).  Two boxes per slot: the
-// tile plus a 4-point halo, (TX + 8) x 1 x (TY + 8), and the tile alone.
+// buffers (first current, old, first spare).  Three boxes per slot: the
+// tile plus a 4-point halo, (TX + 8) x 1 x (TY + 8) from (i0 - 4, j0 - 4);
+// the tile alone, TX x 1 x TY from (i0, j0); and the tile plus one point on
+// every side, NEAR_W x 1 x NEAR_H from (i0 - 4, j0 - 1) (x starts 4 points
+// early so that it stays 16-byte aligned).
 constexpr int NMAPSLOT = WRFGPU_N3D + 3 * NSPMAX;
-constexpr int BOX_HALO = 0, BOX_TILE = 1;
+constexpr int BOX_HALO = 0, BOX_TILE = 1, BOX_NEAR = 2, NBOX = 3;
+constexpr int NEAR_W = 40, NEAR_H = 10;
 
 // Error word bits (Mem::err): set by kernels, read by the host between steps.
 constexpr unsigned ERR_NONFINITE = 1u;
@@ -78,6 +82,11 @@ struct alignas(16) Mem {
   float pad1;
   float* cfl_out;         // [2]: max vertical, max horizontal CFL (atomic max)
 };
+
+// Tensor map of buffer slot `slot` (field id or species slot), box `box`.
+__host__ __device__ inline const CUtensorMap* tmap_of(const Mem& m, int slot, int box) {
+  return m.tmap + NBOX * slot + box;
+}
 
 // Stage constants of solve_em.F:601-615 for one member.
 struct Stage {
@@ -332,6 +341,45 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, 
       "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
+
+// A ring of level slots for column kernels: each slot holds NF planes of one
+// level, all of one TMA box (PW x PH floats, row by row) and completes on its
+// own mbarrier.  Thread 0 issues; every thread waits.  A slot is reused for
+// level k + NSLOT only after a block barrier that follows the last read of
+// level k (the caller's loop places it).
+// Every plane starts on a 128-byte boundary (the TMA destination rule), and
+// SMEM is a multiple of 128 bytes so that rings can be stacked.
+template <int NF, int NSLOT, int PW = TX, int PH = TY>
+struct LevelRing {
+  float* buf;      // [NSLOT][NF][PSTRIDE]
+  uint64_t* bar;   // [NSLOT]
+  int k0;          // first level staged
+  static constexpr unsigned PLANE = PW * PH;               // floats a box delivers
+  static constexpr unsigned PSTRIDE = (PLANE + 31) / 32 * 32;  // floats between planes
+  static constexpr size_t DATA = (size_t)NSLOT * NF * PSTRIDE * 4;
+  static constexpr size_t SMEM = DATA + (NSLOT * 8 + 127) / 128 * 128;
+  __device__ int slot_of(int k) const { return (k - k0) % NSLOT; }
+  __device__ const float* plane(int k, int f) const { return buf + (slot_of(k) * NF + f) * PSTRIDE; }
+  // carve the ring out of shared memory at `smem` (128-byte aligned)
+  __device__ void init(unsigned char* smem, int first_level) {
+    buf = (float*)smem;
+    bar = (uint64_t*)(smem + DATA);
+    k0 = first_level;
+  }
+  __device__ void init_barriers() const {
+    for (int q = 0; q < NSLOT; ++q) mbar_init(&bar[q], 1);
+  }
+  // thread 0: level k of the NF fields into its slot (box origin x0, z0)
+  __device__ void issue(int k, const CUtensorMap* const* maps, int x0, int z0, int kms) const {
+    const int sl = slot_of(k);
+    fence_proxy_async_smem();
+    mbar_expect_tx(&bar[sl], NF * PLANE * 4);
+    for (int f = 0; f < NF; ++f) tma_load_3d(buf + (sl * NF + f) * PSTRIDE, maps[f], x0, k - kms, z0, &bar[sl]);
+  }
+  __device__ bool wait(int k) const { return mbar_wait(&bar[slot_of(k)], ((k - k0) / NSLOT) & 1); }
+};
+template <int NF, int NSLOT> using TileRing = LevelRing<NF, NSLOT, TX, TY>;
+template <int NF, int NSLOT> using NearRing = LevelRing<NF, NSLOT, NEAR_W, NEAR_H>;
 
 struct TileLaunch {
   const Mem* mem;

@@ -268,19 +268,21 @@ struct Ensemble {
       btm[m + 1] = btm[m] + tiles_x(M) * tiles_y(M);
     }
     nb2 = bs2[n]; nb3 = bs3[n]; nb_sc = bss[n]; nb_st = bst[n]; nb_tm = btm[n];
-    {  // tensor maps of every 3-D buffer: halo box and tile box
+    {  // tensor maps of every 3-D buffer: halo, tile and near boxes
       int rc = get_tensor_map_encoder();
       if (rc) return rc;
-      std::vector<CUtensorMap> maps((size_t)n * NMAPSLOT * 2);
+      std::vector<CUtensorMap> maps((size_t)n * NMAPSLOT * NBOX);
       std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
       for (int m = 0; m < n; ++m) {
         Mem& M = hm[m];
-        CUtensorMap* mm = maps.data() + (size_t)m * NMAPSLOT * 2;
+        CUtensorMap* mm = maps.data() + (size_t)m * NMAPSLOT * NBOX;
         auto enc = [&](int slot, float* base) -> int {
-          int r1 = encode_field_map(&mm[2 * slot + BOX_HALO], base, ni_[m], pitch_[m], nk_[m], nj_[m],
+          int r1 = encode_field_map(&mm[NBOX * slot + BOX_HALO], base, ni_[m], pitch_[m], nk_[m], nj_[m],
                                     TX + 2 * TMA_HALO, TY + 2 * TMA_HALO);
-          int r2 = encode_field_map(&mm[2 * slot + BOX_TILE], base, ni_[m], pitch_[m], nk_[m], nj_[m], TX, TY);
-          return r1 ? r1 : r2;
+          int r2 = encode_field_map(&mm[NBOX * slot + BOX_TILE], base, ni_[m], pitch_[m], nk_[m], nj_[m], TX, TY);
+          int r3 = encode_field_map(&mm[NBOX * slot + BOX_NEAR], base, ni_[m], pitch_[m], nk_[m], nj_[m], NEAR_W,
+                                    NEAR_H);
+          return r1 ? r1 : (r2 ? r2 : r3);
         };
         for (int f = 0; f < WRFGPU_N3D; ++f) { rc = enc(f, M.f3[f]); if (rc) return rc; }
         for (int sp = 0; sp < M.nsp; ++sp) {
@@ -291,7 +293,7 @@ struct Ensemble {
       }
       CK(cudaMalloc(&d_tmaps, maps.size() * sizeof(CUtensorMap)));
       CK(cudaMemcpy(d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
-      for (int m = 0; m < n; ++m) hm[m].tmap = d_tmaps + (size_t)m * NMAPSLOT * 2;
+      for (int m = 0; m < n; ++m) hm[m].tmap = d_tmaps + (size_t)m * NMAPSLOT * NBOX;
     }
     CK(cudaMalloc(&d_mems, sizeof(Mem) * n));
     CK(cudaMemcpyAsync(d_mems, hm.data(), sizeof(Mem) * n, cudaMemcpyHostToDevice, stream));
@@ -388,7 +390,7 @@ struct Ensemble {
       mark(PH_TEND_W); launch_tend_w(l2, nb2, TF_ALL, stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
-      if (cfl_check) { mark(PH_CFL); launch_cfl_check(l3, nb3, stream); }
+      if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream); }
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
       mark(PH_SSP); launch_small_step_prep(l2, nb2, a, stream);
       mark(PH_CPR0); launch_calc_p_rho(l3, nb3, StepArgs{rk_step, 0, 0, 0}, stream);
@@ -611,7 +613,7 @@ int fortran_call(const FCall& c) {
   int rc = e->run_routine(c.routine, c.rk_step, c.iteration, c.species);
   if (rc) return rc;
   if (c.max_vert_cfl || c.max_horiz_cfl) {
-    launch_cfl_check(e->L3(), e->nb3, e->stream);
+    launch_cfl_check_col(e->LTM(), e->nb_tm, e->stream);
     float cfl[2] = {0.f, 0.f};
     CK(cudaMemcpyAsync(cfl, e->d_cfl, sizeof(cfl), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));

@@ -399,156 +399,197 @@ __global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int r
 // back substitution and the geopotential update.  RC as above (the mixed
 // form keeps a, alpha, gamma in FP64).
 // ---------------------------------------------------------------------------
+// Level inputs of advance_w staged by TMA: plane index of each field in a
+// ring slot (the FP64 a / alpha of the mixed form are read from global
+// memory instead, so that form stages the first 13).
+enum AwPlane { AW_T2 = 0, AW_T2A, AW_T1, AW_PH, AW_W, AW_RWT, AW_CQW, AW_C2A, AW_ALT, AW_PHT, AW_WW, AW_PH1, AW_PHB,
+               AW_A, AW_AL, AW_NPLANE };
+constexpr int AW_RING = 4;  // levels L, L+1 resident, L+2, L+3 in flight
+template <typename RC> struct AwCfg {
+  static constexpr int NF = sizeof(RC) == 8 ? AW_A : AW_NPLANE;
+  using Ring = TileRing<NF, AW_RING>;
+};
+
 template <typename RC>
-__global__ void __launch_bounds__(TX* TY) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
+__global__ void __launch_bounds__(TX* TY, 3) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
+  using Ring = typename AwCfg<RC>::Ring;
+  constexpr int NF = AwCfg<RC>::NF;
+  extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
   const Stage st = stage_of(m, rk_step);
   if (iteration > st.nsmall) return;
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx, po = ty * TX + tx;
+  const int i = tp.i0 + tx, j = tp.j0 + ty;
   const int i_end = min(m.ite, m.ide - 1), j_end = min(m.jte, m.jde - 1);
-  if (i > i_end || j > j_end) return;
+  // every thread takes part in the ring's barriers; only columns of the
+  // domain compute and store
+  const bool act = i <= i_end && j <= j_end;
+  const int ic = act ? i : tp.i0, jc = act ? j : tp.j0;  // in-range indices for the column loads
   const int k_end = m.kte - 1, kde = m.kde;
   const float dts = st.dts_rk, epssm = m.epssm, rdx = m.rdx, rdy = m.rdy;
-  F3 w = f3(m, WRFGPU_W_2), rw_tend = f3(m, WRFGPU_RW_TEND), ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2),
-     v = f3(m, WRFGPU_V_2), t_2ave = f3(m, WRFGPU_T_2SAVE), t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE),
-     ph = f3(m, WRFGPU_PH_2), ph_1 = f3(m, WRFGPU_PH_SAVE), phb = f3(m, WRFGPU_PHB), ph_tend = f3(m, WRFGPU_PH_TEND),
-     c2a = f3(m, WRFGPU_C2A), cqw = f3(m, WRFGPU_CQW), alt = f3(m, WRFGPU_ALT);
-  F2 mut = f2(m, WRFGPU_MUT), muave = f2(m, WRFGPU_MUAVE), muts = f2(m, WRFGPU_MUTS), ht = f2(m, WRFGPU_HT),
-     msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
-  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
-     fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW), rdn = f1(m, WRFGPU_RDN);
-  const bool fp64 = sizeof(RC) == 8;
-  const bool adv2 = m.cf.phi_adv_z == 2;
-  const float msft_inv = 1.f / msfty.ro(i, j);
-  const float my = msfty.ro(i, j), mx = msftx.ro(i, j), mutij = mut.ro(i, j), mua = muave.ro(i, j), mts = muts.ro(i, j);
-  auto Acoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[0])(i, k, j)) : (RC)f3(m, WRFGPU_A).ro(i, k, j); };
-  auto ALcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[1])(i, k, j)) : (RC)f3(m, WRFGPU_ALPHA).ro(i, k, j); };
-  auto GAcoef = [&](int k) -> RC { return fp64 ? (RC)__ldg(&d3(m, m.wd[2])(i, k, j)) : (RC)f3(m, WRFGPU_GAMMA).ro(i, k, j); };
-  const float eps1 = 1.f + epssm, eps0 = 1.f - epssm;
 
-  // surface w (needs only u, v of the lowest levels)
-  const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
-  const float w1 = (my * .5f * rdy *
-                         ((ht.ro(i, j + 1) - ht.ro(i, j)) * (cf1 * v.ro(i, 1, j + 1) + cf2 * v.ro(i, 2, j + 1) + cf3 * v.ro(i, 3, j + 1)) +
-                          (ht.ro(i, j) - ht.ro(i, j - 1)) * (cf1 * v.ro(i, 1, j) + cf2 * v.ro(i, 2, j) + cf3 * v.ro(i, 3, j))) +
-                     mx * .5f * rdx *
-                         ((ht.ro(i + 1, j) - ht.ro(i, j)) * (cf1 * u.ro(i + 1, 1, j) + cf2 * u.ro(i + 1, 2, j) + cf3 * u.ro(i + 1, 3, j)) +
-                          (ht.ro(i, j) - ht.ro(i - 1, j)) * (cf1 * u.ro(i, 1, j) + cf2 * u.ro(i, 2, j) + cf3 * u.ro(i, 3, j))));
-
-  // explicit w of level k (FP32, the reference's expression) and forward
-  // elimination (RC: FP64 in the mixed form)
-  RC wprev = (RC)w1;
-  RC wcol[KCOL];
-  auto sweep = [&](int k, float wk_in, float rwt, float cqwk, float c2ak, float altk, RC ak, RC alk, float tak,
-                   float c2am, float altm, float tam, float r_p1, float r_0, float r_m1, float ph_p1, float ph_0,
-                   float ph_m1) {
-    const float wkf = wk_in + dts * rwt +
-                      msft_inv * cqwk *
-                          (+.5f * dts * G * rdn(k) *
-                           (c2ak * rdnw(k) / (c1h(k) * mutij + c2h(k)) * (eps1 * (r_p1 - r_0) + eps0 * (ph_p1 - ph_0)) -
-                            c2am * rdnw(k - 1) / (c1h(k - 1) * mutij + c2h(k - 1)) *
-                                (eps1 * (r_0 - r_m1) + eps0 * (ph_0 - ph_m1)))) +
-                      dts * G * msft_inv * (rdn(k) * (c2ak * altk * tak - c2am * altm * tam) - (c1f(k) * mua));
-    const RC wk = ((RC)wkf - ak * wprev) * alk;
-    wcol[k] = wk;
-    wprev = wk;
-  };
-
-  struct Lv {
-    float t2, t2a, t1, ph, w, rwt, cqw, c2a, alt;  // level L
-    RC a, al;
-    float pht1, w1, ww1, ph11, phb1;               // level L+1
-  };
-  auto load = [&](int k, Lv& d) {
-    d.t2 = t_2.ro(i, k, j); d.t2a = t_2ave(i, k, j); d.t1 = t_1.ro(i, k, j); d.ph = ph(i, k, j);
-    d.w = w(i, k, j); d.rwt = rw_tend.ro(i, k, j); d.cqw = cqw.ro(i, k, j); d.c2a = c2a.ro(i, k, j);
-    d.alt = alt.ro(i, k, j); d.a = Acoef(k); d.al = ALcoef(k);
-    d.pht1 = ph_tend.ro(i, k + 1, j); d.w1 = w(i, k + 1, j); d.ww1 = ww.ro(i, k + 1, j);
-    d.ph11 = ph_1.ro(i, k + 1, j); d.phb1 = phb.ro(i, k + 1, j);
-  };
-  float rhs[KCOL];
-  rhs[1] = 0.f;
-  // windows: level L-1 and L-2 values of what the elimination reads
-  float r_m1 = 0.f, r_m2 = 0.f;          // rhs(L-1), rhs(L-2)
-  float ph_m1 = 0.f, ph_m2 = 0.f;        // ph(L-1), ph(L-2)
-  float ta_m1 = 0.f, ta_m2 = 0.f;        // t_2ave(L-1), t_2ave(L-2)
-  float c2a_m1 = 0.f, c2a_m2 = 0.f, alt_m1 = 0.f, alt_m2 = 0.f;
-  float w_m1 = 0.f, rwt_m1 = 0.f, cqw_m1 = 0.f;
-  RC a_m1 = RC(0.), al_m1 = RC(0.);
-  float ww_k = ww.ro(i, 1, j), ph1_k = ph_1.ro(i, 1, j), phb_k = phb.ro(i, 1, j);
-  float wd_k = 0.f;   // wdwn(L)
-  float rr_k = 0.f;   // raw rhs(L)
-  Lv cur, nxt;
-  load(1, cur);
-  for (int Lk = 1; Lk <= k_end; ++Lk) {
-    if (Lk + 1 <= k_end) load(Lk + 1, nxt);
-    // t_2ave(L)
-    float tav = .5f * ((1.f + epssm) * cur.t2 + (1.f - epssm) * cur.t2a);
-    tav = (tav + (c1h(Lk) * mua) * T0) / ((c1h(Lk) * mts + c2h(Lk)) * (T0 + cur.t1));
-    t_2ave(i, Lk, j) = tav;
-    // raw rhs(L+1), wdwn(L+1)
-    const float rr_next = dts * (cur.pht1 + .5f * G * (1.f - epssm) * cur.w1);
-    float wd_hi;
-    if (adv2) wd_hi = rdnw(Lk) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
-    else wd_hi = .5f * (cur.ww1 + ww_k) * rdnw(Lk) * (cur.ph11 - ph1_k + cur.phb1 - phb_k);
-    // rhs(L) complete
-    float r_0 = 0.f;
-    if (Lk >= 2) {
-      float r = rr_k;
-      if (adv2) r = r - (dts * ww_k * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
-      else r = r - (dts * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
-      r = cur.ph + my * r / (c1f(Lk) * mutij + c2f(Lk));
-      rhs[Lk] = r;
-      r_0 = r;
+  Ring ring;
+  ring.init(smem, 1);
+  {
+    const int ids[AW_NPLANE] = {WRFGPU_T_2, WRFGPU_T_2SAVE, WRFGPU_T_SAVE, WRFGPU_PH_2, WRFGPU_W_2, WRFGPU_RW_TEND,
+                                WRFGPU_CQW, WRFGPU_C2A, WRFGPU_ALT, WRFGPU_PH_TEND, WRFGPU_WW, WRFGPU_PH_SAVE,
+                                WRFGPU_PHB, WRFGPU_A, WRFGPU_ALPHA};
+    const CUtensorMap* maps[NF];
+    for (int f = 0; f < NF; ++f) maps[f] = tmap_of(m, ids[f], BOX_TILE);
+    const int x0 = tp.i0 - m.ims, z0 = tp.j0 - m.jms;
+    if (tid == 0) {
+      ring.init_barriers();
+      mbar_fence_init();
     }
-    // elimination of level L-1
-    if (Lk >= 3)
-      sweep(Lk - 1, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_0, r_m1, r_m2,
-            cur.ph, ph_m1, ph_m2);
-    // slide
-    r_m2 = r_m1; r_m1 = r_0;
-    ph_m2 = ph_m1; ph_m1 = cur.ph;
-    ta_m2 = ta_m1; ta_m1 = tav;
-    c2a_m2 = c2a_m1; c2a_m1 = cur.c2a; alt_m2 = alt_m1; alt_m1 = cur.alt;
-    w_m1 = cur.w; rwt_m1 = cur.rwt; cqw_m1 = cur.cqw; a_m1 = cur.a; al_m1 = cur.al;
-    ww_k = cur.ww1; ph1_k = cur.ph11; phb_k = cur.phb1;
-    wd_k = wd_hi; rr_k = rr_next;
-    cur = nxt;
-  }
-  // top: rhs(kde) has no omega term
-  const int kt = k_end + 1;
-  const float ph_top = ph(i, kt, j);
-  float r_top = ph_top + my * rr_k / (c1f(kt) * mutij + c2f(kt));
-  if (m.cf.top_lid) r_top = 0.f;
-  rhs[kt] = r_top;
-  // elimination of level k_end
-  sweep(k_end, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_top, r_m1, r_m2,
-        ph_top, ph_m1, ph_m2);
-  {  // level kde
-    const int k = kt;
-    const float r = rdnw(k - 1);
-    float wkf = w(i, k, j) + dts * rw_tend.ro(i, k, j) +
-                msft_inv * (-.5f * dts * G / (c1h(k - 1) * mutij + c2h(k - 1)) * (r * r) * 2.f * c2a_m1 *
-                                (eps1 * (r_top - r_m1) + eps0 * (ph_top - ph_m1)) -
-                            dts * G * (2.f * rdnw(k - 1) * c2a_m1 * alt_m1 * ta_m1 + (c1f(k) * mua)));
-    if (m.cf.top_lid) wkf = 0.f;
-    const RC wk = ((RC)wkf - Acoef(k) * wprev) * ALcoef(k);
-    wcol[k] = wk;
-  }
-  w(i, 1, j) = w1;
-  // ---- back substitution (RC) and geopotential (FP32, from the new w)
-  RC wup = wcol[kt];
-  w(i, kt, j) = (float)wup;
-  ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * (float)wup / (c1f(kt) * mts + c2f(kt));
-  RC g_nxt = GAcoef(k_end);
-  for (int k = k_end; k >= 2; --k) {
-    const RC g = g_nxt;
-    if (k - 1 >= 2) g_nxt = GAcoef(k - 1);
-    const RC wk = wcol[k] - g * wup;
-    w(i, k, j) = (float)wk;
-    ph(i, k, j) = rhs[k] + my * .5f * dts * G * eps1 * (float)wk / (c1f(k) * mts + c2f(k));
-    wup = wk;
+    __syncthreads();
+    if (tid == 0)
+      for (int k = 1; k <= min(AW_RING - 1, kde); ++k) ring.issue(k, maps, x0, z0, m.kms);
+    bool ok = true;
+
+    F3 w = f3(m, WRFGPU_W_2), t_2ave = f3(m, WRFGPU_T_2SAVE), ph = f3(m, WRFGPU_PH_2), u = f3(m, WRFGPU_U_2),
+       v = f3(m, WRFGPU_V_2);
+    F2 ht = f2(m, WRFGPU_HT), msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
+    F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F),
+       fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP), rdnw = f1(m, WRFGPU_RDNW), rdn = f1(m, WRFGPU_RDN);
+    const bool fp64 = sizeof(RC) == 8;
+    const bool adv2 = m.cf.phi_adv_z == 2;
+    const float msft_inv = 1.f / msfty.ro(ic, jc);
+    const float my = msfty.ro(ic, jc), mx = msftx.ro(ic, jc), mutij = f2(m, WRFGPU_MUT).ro(ic, jc),
+                mua = f2(m, WRFGPU_MUAVE).ro(ic, jc), mts = f2(m, WRFGPU_MUTS).ro(ic, jc);
+    auto P = [&](int k, int f) -> float { return ring.plane(k, f)[po]; };
+    auto Acoef = [&](int k) -> RC {
+      if (fp64) return (RC)__ldg(&d3(m, m.wd[0])(ic, k, jc));
+      return (RC)P(k, AW_A < NF ? AW_A : 0);
+    };
+    auto ALcoef = [&](int k) -> RC {
+      if (fp64) return (RC)__ldg(&d3(m, m.wd[1])(ic, k, jc));
+      return (RC)P(k, AW_AL < NF ? AW_AL : 0);
+    };
+    auto GAcoef = [&](int k) -> RC {
+      return fp64 ? (RC)__ldg(&d3(m, m.wd[2])(ic, k, jc)) : (RC)f3(m, WRFGPU_GAMMA).ro(ic, k, jc);
+    };
+    const float eps1 = 1.f + epssm, eps0 = 1.f - epssm;
+
+    // surface w (needs only u, v of the lowest levels)
+    const float cf1 = m.cf1, cf2 = m.cf2, cf3 = m.cf3;
+    const int I = ic, J = jc;
+    const float w1 = (my * .5f * rdy *
+                          ((ht.ro(I, J + 1) - ht.ro(I, J)) * (cf1 * v.ro(I, 1, J + 1) + cf2 * v.ro(I, 2, J + 1) + cf3 * v.ro(I, 3, J + 1)) +
+                           (ht.ro(I, J) - ht.ro(I, J - 1)) * (cf1 * v.ro(I, 1, J) + cf2 * v.ro(I, 2, J) + cf3 * v.ro(I, 3, J))) +
+                      mx * .5f * rdx *
+                          ((ht.ro(I + 1, J) - ht.ro(I, J)) * (cf1 * u.ro(I + 1, 1, J) + cf2 * u.ro(I + 1, 2, J) + cf3 * u.ro(I + 1, 3, J)) +
+                           (ht.ro(I, J) - ht.ro(I - 1, J)) * (cf1 * u.ro(I, 1, J) + cf2 * u.ro(I, 2, J) + cf3 * u.ro(I, 3, J))));
+
+    // explicit w of level k (FP32, the reference's expression) and forward
+    // elimination (RC: FP64 in the mixed form)
+    RC wprev = (RC)w1;
+    RC wcol[KCOL];
+    auto sweep = [&](int k, float wk_in, float rwt, float cqwk, float c2ak, float altk, RC ak, RC alk, float tak,
+                     float c2am, float altm, float tam, float r_p1, float r_0, float r_m1, float ph_p1, float ph_0,
+                     float ph_m1) {
+      const float wkf = wk_in + dts * rwt +
+                        msft_inv * cqwk *
+                            (+.5f * dts * G * rdn(k) *
+                             (c2ak * rdnw(k) / (c1h(k) * mutij + c2h(k)) * (eps1 * (r_p1 - r_0) + eps0 * (ph_p1 - ph_0)) -
+                              c2am * rdnw(k - 1) / (c1h(k - 1) * mutij + c2h(k - 1)) *
+                                  (eps1 * (r_0 - r_m1) + eps0 * (ph_0 - ph_m1)))) +
+                        dts * G * msft_inv * (rdn(k) * (c2ak * altk * tak - c2am * altm * tam) - (c1f(k) * mua));
+      const RC wk = ((RC)wkf - ak * wprev) * alk;
+      wcol[k] = wk;
+      wprev = wk;
+    };
+    float rhs[KCOL];
+    rhs[1] = 0.f;
+    // windows: level L-1 and L-2 values of what the elimination reads
+    float r_m1 = 0.f, r_m2 = 0.f;          // rhs(L-1), rhs(L-2)
+    float ph_m1 = 0.f, ph_m2 = 0.f;        // ph(L-1), ph(L-2)
+    float ta_m1 = 0.f, ta_m2 = 0.f;        // t_2ave(L-1), t_2ave(L-2)
+    float c2a_m1 = 0.f, c2a_m2 = 0.f, alt_m1 = 0.f, alt_m2 = 0.f;
+    float w_m1 = 0.f, rwt_m1 = 0.f, cqw_m1 = 0.f;
+    RC a_m1 = RC(0.), al_m1 = RC(0.);
+    float wd_k = 0.f;   // wdwn(L)
+    float rr_k = 0.f;   // raw rhs(L)
+    ok = ring.wait(1) && ok;
+    float ww_k = P(1, AW_WW), ph1_k = P(1, AW_PH1), phb_k = P(1, AW_PHB);
+    for (int Lk = 1; Lk <= k_end; ++Lk) {
+      __syncthreads();  // level Lk-1's slot is free
+      if (tid == 0 && Lk + AW_RING - 1 <= kde) ring.issue(Lk + AW_RING - 1, maps, x0, z0, m.kms);
+      ok = ring.wait(Lk + 1) && ok;
+      const float c_t2 = P(Lk, AW_T2), c_t2a = P(Lk, AW_T2A), c_t1 = P(Lk, AW_T1), c_ph = P(Lk, AW_PH);
+      const float c_w = P(Lk, AW_W), c_rwt = P(Lk, AW_RWT), c_cqw = P(Lk, AW_CQW), c_c2a = P(Lk, AW_C2A),
+                  c_alt = P(Lk, AW_ALT);
+      const RC c_a = Acoef(Lk), c_al = ALcoef(Lk);
+      const float c_pht1 = P(Lk + 1, AW_PHT), c_w1 = P(Lk + 1, AW_W), c_ww1 = P(Lk + 1, AW_WW),
+                  c_ph11 = P(Lk + 1, AW_PH1), c_phb1 = P(Lk + 1, AW_PHB);
+      // t_2ave(L)
+      float tav = .5f * ((1.f + epssm) * c_t2 + (1.f - epssm) * c_t2a);
+      tav = (tav + (c1h(Lk) * mua) * T0) / ((c1h(Lk) * mts + c2h(Lk)) * (T0 + c_t1));
+      if (act) t_2ave(i, Lk, j) = tav;
+      // raw rhs(L+1), wdwn(L+1)
+      const float rr_next = dts * (c_pht1 + .5f * G * (1.f - epssm) * c_w1);
+      float wd_hi;
+      if (adv2) wd_hi = rdnw(Lk) * (c_ph11 - ph1_k + c_phb1 - phb_k);
+      else wd_hi = .5f * (c_ww1 + ww_k) * rdnw(Lk) * (c_ph11 - ph1_k + c_phb1 - phb_k);
+      // rhs(L) complete
+      float r_0 = 0.f;
+      if (Lk >= 2) {
+        float r = rr_k;
+        if (adv2) r = r - (dts * ww_k * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
+        else r = r - (dts * (fnm(Lk) * wd_hi + fnp(Lk) * wd_k));
+        r = c_ph + my * r / (c1f(Lk) * mutij + c2f(Lk));
+        rhs[Lk] = r;
+        r_0 = r;
+      }
+      // elimination of level L-1
+      if (Lk >= 3)
+        sweep(Lk - 1, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_0, r_m1,
+              r_m2, c_ph, ph_m1, ph_m2);
+      // slide
+      r_m2 = r_m1; r_m1 = r_0;
+      ph_m2 = ph_m1; ph_m1 = c_ph;
+      ta_m2 = ta_m1; ta_m1 = tav;
+      c2a_m2 = c2a_m1; c2a_m1 = c_c2a; alt_m2 = alt_m1; alt_m1 = c_alt;
+      w_m1 = c_w; rwt_m1 = c_rwt; cqw_m1 = c_cqw; a_m1 = c_a; al_m1 = c_al;
+      ww_k = c_ww1; ph1_k = c_ph11; phb_k = c_phb1;
+      wd_k = wd_hi; rr_k = rr_next;
+    }
+    // top: rhs(kde) has no omega term (level kde is resident: waited at Lk = k_end)
+    const int kt = k_end + 1;
+    const float ph_top = P(kt, AW_PH);
+    float r_top = ph_top + my * rr_k / (c1f(kt) * mutij + c2f(kt));
+    if (m.cf.top_lid) r_top = 0.f;
+    rhs[kt] = r_top;
+    // elimination of level k_end
+    sweep(k_end, w_m1, rwt_m1, cqw_m1, c2a_m1, alt_m1, a_m1, al_m1, ta_m1, c2a_m2, alt_m2, ta_m2, r_top, r_m1, r_m2,
+          ph_top, ph_m1, ph_m2);
+    {  // level kde
+      const int k = kt;
+      const float r = rdnw(k - 1);
+      float wkf = P(k, AW_W) + dts * P(k, AW_RWT) +
+                  msft_inv * (-.5f * dts * G / (c1h(k - 1) * mutij + c2h(k - 1)) * (r * r) * 2.f * c2a_m1 *
+                                  (eps1 * (r_top - r_m1) + eps0 * (ph_top - ph_m1)) -
+                              dts * G * (2.f * rdnw(k - 1) * c2a_m1 * alt_m1 * ta_m1 + (c1f(k) * mua)));
+      if (m.cf.top_lid) wkf = 0.f;
+      const RC wk = ((RC)wkf - Acoef(k) * wprev) * ALcoef(k);
+      wcol[k] = wk;
+    }
+    if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
+    if (!act) return;
+    w(i, 1, j) = w1;
+    // ---- back substitution (RC) and geopotential (FP32, from the new w)
+    RC wup = wcol[kt];
+    w(i, kt, j) = (float)wup;
+    ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * (float)wup / (c1f(kt) * mts + c2f(kt));
+    RC g_nxt = GAcoef(k_end);
+    for (int k = k_end; k >= 2; --k) {
+      const RC g = g_nxt;
+      if (k - 1 >= 2) g_nxt = GAcoef(k - 1);
+      const RC wk = wcol[k] - g * wup;
+      w(i, k, j) = (float)wk;
+      ph(i, k, j) = rhs[k] + my * .5f * dts * G * eps1 * (float)wk / (c1f(k) * mts + c2f(k));
+      wup = wk;
+    }
   }
 }
 
@@ -557,8 +598,15 @@ void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int 
   else k_advance_mu_t_col<float><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s) {
-  if (fp64) k_advance_w_col<double><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
-  else k_advance_w_col<float><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  static bool attr = false;
+  constexpr size_t S32 = AwCfg<float>::Ring::SMEM, S64 = AwCfg<double>::Ring::SMEM;
+  if (!attr) {
+    cudaFuncSetAttribute(k_advance_w_col<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
+    cudaFuncSetAttribute(k_advance_w_col<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
+    attr = true;
+  }
+  if (fp64) k_advance_w_col<double><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+  else k_advance_w_col<float><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
 }
 
 }  // namespace wrfgpu

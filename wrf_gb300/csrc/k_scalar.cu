@@ -327,7 +327,56 @@ __global__ void __launch_bounds__(BX* BY) k_cfl_check(Launch L) {
   }
 }
 
+// Column form of the same diagnostics: one thread per mass column of a 32x8
+// tile, levels 2..kde-1 in order, the maxima kept in registers and reduced
+// once per block (warp shuffles, then shared memory).  A maximum does not
+// depend on the order it is taken in, so the result equals the point form's.
+__global__ void __launch_bounds__(TX* TY) k_cfl_check_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  float vmax = 0.f, hmax = 0.f;
+  bool bad = false;
+  if (mass_pt(m, i, j)) {
+    F3 ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), w = f3(m, WRFGPU_W_2), t = f3(m, WRFGPU_T_2);
+    F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), rdnw = f1(m, WRFGPU_RDNW);
+    const float mutc = f2(m, WRFGPU_MUT)(i, j), mux = f2(m, WRFGPU_MSFUX)(i, j), mvy = f2(m, WRFGPU_MSFVY)(i, j);
+    const float dt = m.dt, rdx = m.rdx, rdy = m.rdy;
+#pragma unroll 4
+    for (int k = 2; k <= m.kde - 1; ++k) {
+      const float vc = fabsf(ww.ro(i, k, j) / (c1f(k) * mutc + c2f(k)) * rdnw(k) * dt);
+      const float hc = fmaxf_f(fabsf(u.ro(i, k, j) * rdx * mux * dt), fabsf(v.ro(i, k, j) * rdy * mvy * dt));
+      bad = bad || !isfinite(vc) || !isfinite(hc) || !isfinite(w.ro(i, k, j)) || !isfinite(t.ro(i, k, j));
+      vmax = fmaxf_f(vmax, isfinite(vc) ? vc : 0.f);
+      hmax = fmaxf_f(hmax, isfinite(hc) ? hc : 0.f);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    vmax = fmaxf_f(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    hmax = fmaxf_f(hmax, __shfl_xor_sync(0xffffffffu, hmax, o));
+  }
+  const bool wbad = __any_sync(0xffffffffu, bad);
+  __shared__ float sv[TY], sh[TY];
+  __shared__ int sb[TY];
+  if (threadIdx.x == 0) { sv[threadIdx.y] = vmax; sh[threadIdx.y] = hmax; sb[threadIdx.y] = wbad ? 1 : 0; }
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    float bv = 0.f, bh = 0.f;
+    int bb = 0;
+    for (int q = 0; q < TY; ++q) { bv = fmaxf_f(bv, sv[q]); bh = fmaxf_f(bh, sh[q]); bb |= sb[q]; }
+    if (m.cfl_out) {
+      atomicMax((unsigned*)&m.cfl_out[0], __float_as_uint(bv));
+      atomicMax((unsigned*)&m.cfl_out[1], __float_as_uint(bh));
+    }
+    unsigned bits = 0;
+    if (bb) bits |= ERR_NONFINITE;
+    if (m.cfl_limit > 0.f && bv > m.cfl_limit) bits |= ERR_CFL;
+    if (bits) raise_err(m, bits);
+  }
+}
+
 // ------------------------------------------------------------ launchers
+void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s) { k_cfl_check_col<<<nb, dim3(TX, TY), 0, s>>>(L); }
 void launch_update_scalar_pd(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar_pd<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
 }

@@ -80,8 +80,8 @@ __global__ void __launch_bounds__(TX* TY, 4) k_scalar_adv_update(TileLaunch L, i
   float* fy_base = fx_base + 2 * TY * (TX + 1);                      // [2][TY+1][TX]
   ring.bar = (uint64_t*)(fy_base + 2 * (TY + 1) * TX);
   ring.kts = kts;
-  const CUtensorMap* maps[ADV_NPL] = {m.tmap + 2 * m.qmap[s] + BOX_HALO, m.tmap + 2 * WRFGPU_RU_M + BOX_HALO,
-                                      m.tmap + 2 * WRFGPU_RV_M + BOX_HALO};
+  const CUtensorMap* maps[ADV_NPL] = {tmap_of(m, m.qmap[s], BOX_HALO), tmap_of(m, WRFGPU_RU_M, BOX_HALO),
+                                      tmap_of(m, WRFGPU_RV_M, BOX_HALO)};
   const int x0 = i0 - TMA_HALO - m.ims, z0 = j0 - TMA_HALO - m.jms;
   if (tid == 0) {
     for (int q = 0; q < ADV_RING; ++q) mbar_init(&ring.bar[q], 1);
@@ -247,9 +247,9 @@ __global__ void __launch_bounds__(TX* TY, 2) k_scalar_pd_update(TileLaunch L, in
   float* sSC = p; p += 2 * P::SN;
   ring.bar = (uint64_t*)p;
   ring.kts = kts;
-  const CUtensorMap* maps[PD_NPL] = {m.tmap + 2 * m.qmap[s] + BOX_HALO,
-                                     m.tmap + 2 * (WRFGPU_N3D + 3 * s + 1) + BOX_HALO,
-                                     m.tmap + 2 * WRFGPU_RU_M + BOX_HALO, m.tmap + 2 * WRFGPU_RV_M + BOX_HALO};
+  const CUtensorMap* maps[PD_NPL] = {tmap_of(m, m.qmap[s], BOX_HALO),
+                                     tmap_of(m, WRFGPU_N3D + 3 * s + 1, BOX_HALO),
+                                     tmap_of(m, WRFGPU_RU_M, BOX_HALO), tmap_of(m, WRFGPU_RV_M, BOX_HALO)};
   const int x0 = i0 - TMA_HALO - m.ims, z0 = j0 - TMA_HALO - m.jms;
   if (tid == 0) {
     for (int q = 0; q < PD_RING; ++q) mbar_init(&ring.bar[q], 1);

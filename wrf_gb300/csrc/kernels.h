@@ -73,6 +73,7 @@ void launch_update_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_
 void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_cfl_check(const Launch& L3, int nblocks, cudaStream_t s);
+void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s);  // mass-extent tiles
 
 // fused scalar transport (k_scalar_fused.cu): one block per (tile, species)
 void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s);

@@ -392,7 +392,7 @@ struct Ensemble {
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream); }
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
-      mark(PH_SSP); launch_small_step_prep(l2, nb2, a, stream);
+      mark(PH_SSP); launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream);
       mark(PH_CPR0); launch_calc_p_rho(l3, nb3, StepArgs{rk_step, 0, 0, 0}, stream);
       mark(PH_COEFW); launch_calc_coef_w(l2, nb2, a, fp64, stream);
       {  // solve_em.F:1176-1264
@@ -506,7 +506,7 @@ struct Ensemble {
         launch_tend_u(l3, nb3, TF_CURV, stream); launch_tend_v(l3, nb3, TF_CURV, stream);
         launch_tend_w(l2, nb2, TF_CURV, stream);
         break;
-      case 12: launch_small_step_prep(l2, nb2, a, stream); break;
+      case 12: launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream); break;
       case 13: launch_calc_p_rho(l3, nb3, a, stream); break;
       case 14: launch_calc_coef_w(l2, nb2, a, fp64, stream); break;
       case 15: launch_advance_uv(l3, nb3, a, stream); break;

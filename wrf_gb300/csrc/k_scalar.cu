@@ -328,25 +328,31 @@ __global__ void __launch_bounds__(BX* BY) k_cfl_check(Launch L) {
 }
 
 // Column form of the same diagnostics: one thread per mass column of a 32x8
-// tile, levels 2..kde-1 in order, the maxima kept in registers and reduced
-// once per block (warp shuffles, then shared memory).  A maximum does not
-// depend on the order it is taken in, so the result equals the point form's.
+// tile and one block per (tile, chunk of levels 2..kde-1: gridDim.y chunks),
+// the maxima kept in registers and reduced once per block (warp shuffles,
+// then shared memory).  A maximum does not depend on the order it is taken
+// in, so the result equals the point form's.
 __global__ void __launch_bounds__(TX* TY) k_cfl_check_col(TileLaunch L) {
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
   const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  const int per = (m.kde - 2 + gridDim.y - 1) / gridDim.y;
+  const int k0 = 2 + blockIdx.y * per, k1 = min(m.kde - 1, k0 + per - 1);
   float vmax = 0.f, hmax = 0.f;
   bool bad = false;
-  if (mass_pt(m, i, j)) {
+  if (mass_pt(m, i, j) && k0 <= k1) {
     F3 ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), w = f3(m, WRFGPU_W_2), t = f3(m, WRFGPU_T_2);
     F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), rdnw = f1(m, WRFGPU_RDNW);
     const float mutc = f2(m, WRFGPU_MUT)(i, j), mux = f2(m, WRFGPU_MSFUX)(i, j), mvy = f2(m, WRFGPU_MSFVY)(i, j);
     const float dt = m.dt, rdx = m.rdx, rdy = m.rdy;
 #pragma unroll 4
-    for (int k = 2; k <= m.kde - 1; ++k) {
+    for (int k = k0; k <= k1; ++k) {
       const float vc = fabsf(ww.ro(i, k, j) / (c1f(k) * mutc + c2f(k)) * rdnw(k) * dt);
       const float hc = fmaxf_f(fabsf(u.ro(i, k, j) * rdx * mux * dt), fabsf(v.ro(i, k, j) * rdy * mvy * dt));
-      bad = bad || !isfinite(vc) || !isfinite(hc) || !isfinite(w.ro(i, k, j)) || !isfinite(t.ro(i, k, j));
+      // every load unconditional: a short-circuit || would hold the w and t
+      // loads back until the other checks are known
+      const float wv = w.ro(i, k, j), tv = t.ro(i, k, j);
+      bad = bad | !isfinite(vc) | !isfinite(hc) | !isfinite(wv) | !isfinite(tv);
       vmax = fmaxf_f(vmax, isfinite(vc) ? vc : 0.f);
       hmax = fmaxf_f(hmax, isfinite(hc) ? hc : 0.f);
     }
@@ -376,7 +382,9 @@ __global__ void __launch_bounds__(TX* TY) k_cfl_check_col(TileLaunch L) {
 }
 
 // ------------------------------------------------------------ launchers
-void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s) { k_cfl_check_col<<<nb, dim3(TX, TY), 0, s>>>(L); }
+void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s) {
+  k_cfl_check_col<<<dim3(nb, 8), dim3(TX, TY), 0, s>>>(L);
+}
 void launch_update_scalar_pd(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar_pd<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
 }

@@ -20,19 +20,51 @@ namespace wrfgpu {
 constexpr int KMAX = 128;  // column scratch (kde <= KMAX, checked at domain creation)
 
 // ------------------------------------------------------------ small_step_prep
-__global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_step) {
+// Two kernels.  The 2-D part (mu_1, mu_2, muts, muus, muvs, mu_save, mudf)
+// runs once per column; the 3-D part is elementwise in k and runs one block
+// per (staggered tile, chunk of levels), reading muts / muus / muvs as the
+// 2-D kernel stored them (the same values the reference's loops use).
+__global__ void __launch_bounds__(BX* BY) k_small_step_prep_2d(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
   const int i = bp.i, j = bp.j;
   const int i_start = m.its, i_end = min(m.ite, m.ide - 1), j_start = m.jts, j_end = min(m.jte, m.jde - 1);
-  const int k_start = m.kts, k_end = min(m.kte, m.kde - 1), i_endu = m.ite, j_endv = m.jte, kde = m.kde;
+  const int i_endu = m.ite, j_endv = m.jte;
   if (i < i_start || i > i_endu || j < j_start || j > j_endv) return;
   const bool mass = i <= i_end && j <= j_end, upt = i <= i_endu && j <= j_end, vpt = i <= i_end && j <= j_endv;
   F2 mub = f2(m, WRFGPU_MUB), MU_1 = f2(m, WRFGPU_MU_1), MU_2 = f2(m, WRFGPU_MU_2), MUU = f2(m, WRFGPU_MUU),
-     MUUS = f2(m, WRFGPU_MUUS), MUV = f2(m, WRFGPU_MUV), MUVS = f2(m, WRFGPU_MUVS), mut = f2(m, WRFGPU_MUT),
-     MUTS = f2(m, WRFGPU_MUTS), MUDF = f2(m, WRFGPU_MUDF), MU_SAVE = f2(m, WRFGPU_MU_SAVE),
-     msfuy = f2(m, WRFGPU_MSFUY), msfvx_inv = f2(m, WRFGPU_MSFVX_INV), msfty = f2(m, WRFGPU_MSFTY);
+     MUUS = f2(m, WRFGPU_MUUS), MUV = f2(m, WRFGPU_MUV), MUVS = f2(m, WRFGPU_MUVS), MUTS = f2(m, WRFGPU_MUTS),
+     MUDF = f2(m, WRFGPU_MUDF), MU_SAVE = f2(m, WRFGPU_MU_SAVE);
+  if (rk_step == 1) {
+    if (mass) { MU_1(i, j) = MU_2(i, j); MUDF(i, j) = 0.f; }
+    if (mass) MUTS(i, j) = mub.ro(i, j) + MU_2(i, j);
+    if (upt) MUUS(i, j) = MUU.ro(i, j);
+    if (vpt) MUVS(i, j) = MUV.ro(i, j);
+    if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = 0.f; }
+  } else {
+    if (mass) MUTS(i, j) = mub.ro(i, j) + MU_1(i, j);
+    if (upt) MUUS(i, j) = 0.5f * (mub.ro(i, j) + MU_1(i, j) + mub.ro(i - 1, j) + MU_1(i - 1, j));
+    if (vpt) MUVS(i, j) = 0.5f * (mub.ro(i, j) + MU_1(i, j) + mub.ro(i, j - 1) + MU_1(i, j - 1));
+    if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = MU_1(i, j) - MU_2(i, j); }
+  }
+}
+
+// levels [k0, k1] split into gridDim.y chunks: this block's part
+__device__ __forceinline__ void level_chunk(int k0, int k1, int* c0, int* c1) {
+  const int per = (k1 - k0 + 1 + gridDim.y - 1) / gridDim.y;
+  *c0 = k0 + blockIdx.y * per;
+  *c1 = min(k1, *c0 + per - 1);
+}
+
+__global__ void __launch_bounds__(TX* TY) k_small_step_prep_3d(TileLaunch L, int rk_step) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  const int i_end = min(m.ite, m.ide - 1), j_end = min(m.jte, m.jde - 1);
+  const int k_start = m.kts, k_end = min(m.kte, m.kde - 1), i_endu = m.ite, j_endv = m.jte, kde = m.kde;
+  if (i > i_endu || j > j_endv) return;
+  const bool mass = i <= i_end && j <= j_end, upt = i <= i_endu && j <= j_end, vpt = i <= i_end && j <= j_endv;
   F3 u_1 = f3(m, WRFGPU_U_1), u_2 = f3(m, WRFGPU_U_2), v_1 = f3(m, WRFGPU_V_1), v_2 = f3(m, WRFGPU_V_2),
      w_1 = f3(m, WRFGPU_W_1), w_2 = f3(m, WRFGPU_W_2), t_1 = f3(m, WRFGPU_T_1), t_2 = f3(m, WRFGPU_T_2),
      ph_1 = f3(m, WRFGPU_PH_1), ph_2 = f3(m, WRFGPU_PH_2), u_save = f3(m, WRFGPU_U_SAVE),
@@ -40,27 +72,16 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_ste
      ph_save = f3(m, WRFGPU_PH_SAVE), ww = f3(m, WRFGPU_WW), ww_save = f3(m, WRFGPU_WW1), c2a = f3(m, WRFGPU_C2A),
      pb = f3(m, WRFGPU_PB), p = f3(m, WRFGPU_P), alt = f3(m, WRFGPU_ALT);
   F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
-  float muts = 0.f, muus = 0.f, muvs = 0.f;
   const bool rk1 = rk_step == 1;
-  if (rk1) {
-    if (mass) { MU_1(i, j) = MU_2(i, j); MUDF(i, j) = 0.f; }
-    if (mass) { muts = mub.ro(i, j) + MU_2(i, j); MUTS(i, j) = muts; }
-    if (upt) { muus = MUU.ro(i, j); MUUS(i, j) = muus; }
-    if (vpt) { muvs = MUV.ro(i, j); MUVS(i, j) = muvs; }
-    if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = 0.f; }
-  } else {
-    if (mass) { muts = mub.ro(i, j) + MU_1(i, j); MUTS(i, j) = muts; }
-    if (upt) { muus = 0.5f * (mub.ro(i, j) + MU_1(i, j) + mub.ro(i - 1, j) + MU_1(i - 1, j)); MUUS(i, j) = muus; }
-    if (vpt) { muvs = 0.5f * (mub.ro(i, j) + MU_1(i, j) + mub.ro(i, j - 1) + MU_1(i, j - 1)); MUVS(i, j) = muvs; }
-    if (mass) { MU_SAVE(i, j) = MU_2(i, j); MU_2(i, j) = MU_1(i, j) - MU_2(i, j); }
-  }
+  int c0, c1;
+  level_chunk(k_start, k_end, &c0, &c1);
   // levels are independent: inputs of a chunk of levels are loaded first.
   // At the first stage *_1 = *_2 (the copies the reference makes first).
   struct L2 { float x2, x1; };
   if (upt) {
-    const float muu = MUU.ro(i, j), my = msfuy.ro(i, j);
+    const float muus = f2(m, WRFGPU_MUUS)(i, j), muu = f2(m, WRFGPU_MUU).ro(i, j), my = f2(m, WRFGPU_MSFUY).ro(i, j);
     chunked_levels<8, L2>(
-        k_start, k_end, [&](int k, L2& d) { d.x2 = u_2(i, k, j); d.x1 = rk1 ? d.x2 : u_1(i, k, j); },
+        c0, c1, [&](int k, L2& d) { d.x2 = u_2(i, k, j); d.x1 = rk1 ? d.x2 : u_1(i, k, j); },
         [&](int k, const L2& d) {
           if (rk1) u_1(i, k, j) = d.x2;
           u_save(i, k, j) = d.x2;
@@ -68,9 +89,10 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_ste
         });
   }
   if (vpt) {
-    const float muv = MUV.ro(i, j), mxi = msfvx_inv.ro(i, j);
+    const float muvs = f2(m, WRFGPU_MUVS)(i, j), muv = f2(m, WRFGPU_MUV).ro(i, j),
+                mxi = f2(m, WRFGPU_MSFVX_INV).ro(i, j);
     chunked_levels<8, L2>(
-        k_start, k_end, [&](int k, L2& d) { d.x2 = v_2(i, k, j); d.x1 = rk1 ? d.x2 : v_1(i, k, j); },
+        c0, c1, [&](int k, L2& d) { d.x2 = v_2(i, k, j); d.x1 = rk1 ? d.x2 : v_1(i, k, j); },
         [&](int k, const L2& d) {
           if (rk1) v_1(i, k, j) = d.x2;
           v_save(i, k, j) = d.x2;
@@ -78,10 +100,10 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_ste
         });
   }
   if (mass) {
-    const float mt = mut.ro(i, j), my = msfty.ro(i, j);
+    const float muts = f2(m, WRFGPU_MUTS)(i, j), mt = f2(m, WRFGPU_MUT).ro(i, j), my = f2(m, WRFGPU_MSFTY).ro(i, j);
     struct LT { float t2, t1, pb, p, alt; };
     chunked_levels<8, LT>(
-        k_start, k_end,
+        c0, c1,
         [&](int k, LT& d) {
           d.t2 = t_2(i, k, j); d.t1 = rk1 ? d.t2 : t_1(i, k, j);
           d.pb = pb.ro(i, k, j); d.p = p.ro(i, k, j); d.alt = alt.ro(i, k, j);
@@ -92,9 +114,11 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_prep(Launch L, int rk_ste
           t_save(i, k, j) = d.t2;
           t_2(i, k, j) = (c1h(k) * muts + c2h(k)) * d.t1 - (c1h(k) * mt + c2h(k)) * d.t2;
         });
+    int w0, w1;
+    level_chunk(k_start, kde, &w0, &w1);
     struct LW { float w2, w1, p2, p1, ww; };
     chunked_levels<6, LW>(
-        k_start, kde,
+        w0, w1,
         [&](int k, LW& d) {
           d.w2 = w_2(i, k, j); d.w1 = rk1 ? d.w2 : w_1(i, k, j);
           d.p2 = ph_2(i, k, j); d.p1 = rk1 ? d.p2 : ph_1(i, k, j);
@@ -610,8 +634,9 @@ __global__ void __launch_bounds__(BX* BY) k_small_step_finish(Launch L, int rk_s
 }
 
 // ------------------------------------------------------------ launchers
-void launch_small_step_prep(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
-  k_small_step_prep<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, int nb_st, StepArgs a, cudaStream_t s) {
+  k_small_step_prep_2d<<<nb2, dim3(BX, BY), 0, s>>>(L2, a.rk_step);
+  k_small_step_prep_3d<<<dim3(nb_st, 4), dim3(TX, TY), 0, s>>>(LST, a.rk_step);
 }
 void launch_calc_p_rho(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_calc_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.iteration);

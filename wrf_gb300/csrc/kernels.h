@@ -55,7 +55,8 @@ void launch_tend_t_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t
 void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 
 // acoustic steps
-void launch_small_step_prep(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s);
+// 2-D part over column blocks, then the 3-D part over staggered tiles x level chunks
+void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, int nb_st, StepArgs a, cudaStream_t s);
 void launch_calc_p_rho(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_calc_coef_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
 void launch_advance_uv(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);

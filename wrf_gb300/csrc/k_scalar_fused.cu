@@ -215,7 +215,7 @@ __device__ __forceinline__ void zface(const Mem& m, const ZCell& c, int kk, floa
   *lo = l; *hi = h - l;
 }
 
-__global__ void __launch_bounds__(TX* TY, 2) k_scalar_pd_update(TileLaunch L, int rk_step) {
+__global__ void __launch_bounds__(TX* TY, 3) k_scalar_pd_update(TileLaunch L, int rk_step) {
   using P = PDPlanes;
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, true);

@@ -27,7 +27,7 @@ struct SFLevel {
 };
 }  // namespace
 
-__global__ void __launch_bounds__(TX* TY) k_sumflux_p_rho_col(TileLaunch L, int rk_step, int iteration) {
+__global__ void __launch_bounds__(TX* TY, 3) k_sumflux_p_rho_col(TileLaunch L, int rk_step, int iteration) {
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
   const Stage st = stage_of(m, rk_step);
@@ -132,7 +132,7 @@ struct UVLevel {
 };
 }  // namespace
 
-__global__ void __launch_bounds__(TX* TY, 2) k_advance_uv_col(TileLaunch L, int rk_step, int iteration) {
+__global__ void __launch_bounds__(TX* TY, 3) k_advance_uv_col(TileLaunch L, int rk_step, int iteration) {
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
   const Stage st = stage_of(m, rk_step);

@@ -8,7 +8,7 @@
 
 namespace wrfgpu {
 
-__global__ void __launch_bounds__(BX* BY) k_rk_step_prep(Launch L) {
+__global__ void __launch_bounds__(BX* BY, 5) k_rk_step_prep(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;

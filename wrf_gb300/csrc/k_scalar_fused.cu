@@ -63,7 +63,7 @@ constexpr int ADV_NPL = 3;   // q, ru_m, rv_m
 constexpr size_t ADV_SMEM = (size_t)ADV_RING * ADV_NPL * HPLANE_BYTES + 2 * (TY * (TX + 1) + (TY + 1) * TX) * 4 +
                             ADV_RING * 8;
 
-__global__ void __launch_bounds__(TX* TY, 4) k_scalar_adv_update(TileLaunch L, int rk_step) {
+__global__ void __launch_bounds__(TX* TY, 5) k_scalar_adv_update(TileLaunch L, int rk_step) {
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, true);
   const Mem& m = block_member(L.mem, tp.m);

@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step,
 }
 
 // ------------------------------------------------------------ small_step_finish
-__global__ void __launch_bounds__(BX* BY) k_small_step_finish(Launch L, int rk_step) {
+__global__ void __launch_bounds__(BX* BY, 6) k_small_step_finish(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;

@@ -311,9 +311,11 @@ def ensemble_bench(steps, warmup, n_members=64, world=1, rank=0, pg=None):
     for m, sp in enumerate(specs):
         ens.load_case(m, cases.ensemble_member(sp))
     build_s = time.perf_counter() - t0
+    tune_mixed = ens.autotune(2)
     res = {"workload": "c4_ensemble_%d_members" % len(all_specs), "cells": sum(all_cells), "species": nsp,
            "members": len(all_specs), "members_per_rank": [len(x) for x in shard_members(all_cells, world)],
-           "state_build_s": round(build_s, 1), "device_gb_mixed": round(ens.device_bytes() / 1e9, 2)}
+           "state_build_s": round(build_s, 1), "device_gb_mixed": round(ens.device_bytes() / 1e9, 2),
+           "tuning_mixed": {f: t["param"] for f, t in tune_mixed.items()}}
     ens.step(warmup)
     ens.sync()
     barrier(pg)
@@ -325,6 +327,7 @@ def ensemble_bench(steps, warmup, n_members=64, world=1, rank=0, pg=None):
     f32 = G.Ensemble(descs, flags=0)
     for m in range(len(specs)):
         _copy_member_state(ens, m, f32, m, nsp)
+    f32.autotune(2)
     f32.step(warmup)
     f32.sync()
     barrier(pg)
@@ -337,6 +340,7 @@ def ensemble_bench(steps, warmup, n_members=64, world=1, rank=0, pg=None):
     for m, d in enumerate(descs):
         dom = G.Ensemble([d], flags=0)
         _copy_member_state(ens, m, dom, 0, nsp)
+        dom.autotune(1)
         dom.step(warmup)
         dom.sync()
         tot_ms += dom.time_steps(steps)
@@ -417,6 +421,8 @@ def run_single(args, world, rank, local, pg):
     flags = G.FLAG_MIXED if args.mixed else 0
     dom = G.Domain(case, flags=flags)
     cells = case.cells()
+    # online autotuning of the launch variants (advances the model 8 steps)
+    tuning = dom.autotune(2)
 
     # warm-up (also builds the CUDA graph)
     dom.step(args.warmup)
@@ -530,7 +536,8 @@ def run_single(args, world, rank, local, pg):
                        "cells": cells, "species": case.desc.n_moist + case.desc.n_scalar,
                        "global_batch": world, "seq_len": None,
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (%.1f GB device state)" % (dev_gb)},
+                       "l2": "inputs larger than L2 (%.1f GB device state)" % (dev_gb),
+                       "tuning": {f: t["param"] for f, t in tuning.items()}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches * args.steps,
             "clocks": clocks,

@@ -176,6 +176,20 @@ int wrfgpu_kernel_launches_per_step(WrfGpuEnsemble* h);
  * between kernel launches (the reference's BENCH_START/BENCH_END timers,
  * inc/bench_solve_em_def.h).  Returns the number of phases filled. */
 int wrfgpu_profile_phases(WrfGpuEnsemble* h, int nsteps, double* ms_out, int* launches_out, int nphase);
+
+/* No counterpart in the reference (its tiling is fixed by the namelist).
+ * Online autotuning of the launch configuration: runs rounds x 4 real large
+ * steps (the model advances), trying for each of the 10 tuned kernel
+ * families (WRFGPU_TUNE_*) its launch variants — blocks per SM of the column
+ * and scalar-transport kernels, level chunks of the split column kernels —
+ * and keeps the fastest per family for the captured step.  Every variant
+ * computes the same bits. */
+#define WRFGPU_NTUNE 10
+int wrfgpu_autotune(WrfGpuEnsemble* h, int rounds);
+/* The chosen variant of each family, the parameter it stands for (blocks per
+ * SM or chunks), and the measured ms per step of every variant
+ * (ms[f * 4 + v], -1 when not timed).  Returns WRFGPU_NTUNE. */
+int wrfgpu_tuning(WrfGpuEnsemble* h, int* variant, int* param, float* ms, int nfamily);
 const char* wrfgpu_phase_name(int phase);
 const char* wrfgpu_version(void);
 

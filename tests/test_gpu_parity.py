@@ -267,6 +267,31 @@ def test_full_step_bitwise_rotating(gpulib, nsteps):
     assert not bad, "\n".join(bad)
 
 
+def test_autotune_keeps_bits(gpulib, small):
+    """The autotuner's variants compute the same bits: 4 tuning steps (every
+    variant of every family in turn) plus 1 graph step with the choice equal
+    the oracle's 5 steps."""
+    case = small
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    tun = ge.autotune(1)
+    assert set(tun) == set(G.Ensemble.TUNE_FAMILIES)
+    for f, t in tun.items():
+        assert 0 <= t["variant"] < 4 and t["param"] > 0 and len(t["ms"]) >= 2, (f, t)
+    ge.step(1)
+    ge.sync()
+    od.step(5)
+    bad = []
+    nsp = case.desc.n_moist + case.desc.n_scalar
+    ids = [abi.FIELD_ID[nm] for nm in STATE_FIELDS] + [abi.species_id(s) for s in range(nsp)]
+    for fid in ids:
+        a = interior(case, fid, ge.get(0, fid), halo=3)
+        b = interior(case, fid, od.get(fid), halo=3)
+        if max_abs(a, b) != 0.0:
+            bad.append(id_name(fid))
+    assert not bad, bad
+
+
 def test_graph_equals_direct(gpulib, small):
     a = G.Domain(small, flags=G.FLAG_NO_GRAPH)
     b = G.Domain(small, flags=0)

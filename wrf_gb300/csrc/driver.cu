@@ -130,6 +130,16 @@ struct Ensemble {
   cudaGraphExec_t gexec = nullptr;
   bool cfl_check = true;
   int halo_blocks = 64;
+  // launch variant of each tuned kernel family (kernels.h), and what the
+  // autotuner measured: ms per step of family f with variant v (-1: not timed)
+  int tune[NTUNE];
+  float tune_ms[NTUNE][TUNE_MAXVAR];
+  Ensemble() {
+    for (int f = 0; f < NTUNE; ++f) {
+      tune[f] = TUNE_DEFAULT[f];
+      for (int v = 0; v < TUNE_MAXVAR; ++v) tune_ms[f][v] = -1.f;
+    }
+  }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<std::pair<int, cudaEvent_t>>* prof = nullptr;  // per-launch marks when profiling
 
@@ -375,7 +385,7 @@ struct Ensemble {
     for (int rk_step = 1; rk_step <= 3; ++rk_step) {
       StepArgs a{rk_step, 0, 0, 0};
       mark(PH_PREP);
-      launch_rk_step_prep(l2, nb2, stream);
+      launch_rk_step_prep(l2, nb2, stream, tune[TU_PREP]);
       {  // rk_phys_bc_dry_1 + al, ph_2 (solve_em.F:726-754)
         JobList j;
         j.f3(WRFGPU_RU, 'u'); j.f3(WRFGPU_RV, 'v'); j.f3(WRFGPU_RW, 'w'); j.f3(WRFGPU_WW, 'w');
@@ -387,12 +397,12 @@ struct Ensemble {
       // rk_tendency (module_em.F:370-781)
       mark(PH_TEND_U); launch_tend_u_col(LST(), nb_st, TF_ALL, stream);
       mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream);
-      mark(PH_TEND_W); launch_tend_w(l2, nb2, TF_ALL, stream);
+      mark(PH_TEND_W); launch_tend_w_all(l2, nb2, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
-      if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream); }
+      if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream, tune[TU_CFL]); }
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
-      mark(PH_SSP); launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream);
+      mark(PH_SSP); launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream, tune[TU_SSP]);
       mark(PH_CPR0); launch_calc_p_rho(l3, nb3, StepArgs{rk_step, 0, 0, 0}, stream);
       mark(PH_COEFW); launch_calc_coef_w(l2, nb2, a, fp64, stream);
       {  // solve_em.F:1176-1264
@@ -406,16 +416,16 @@ struct Ensemble {
       for (int m = 0; m < nmem; ++m) nsmall_max = std::max(nsmall_max, stage_of(hm[m], rk_step).nsmall);
       for (int it = 1; it <= nsmall_max; ++it) {
         StepArgs ai{rk_step, it, 0, 0};
-        mark(PH_AUV); launch_advance_uv_col(LST(), nb_st, rk_step, it, stream);
+        mark(PH_AUV); launch_advance_uv_col(LST(), nb_st, rk_step, it, stream, tune[TU_AUV]);
         mark(PH_AMUT); launch_advance_mu_t_col(LTM(), nb_tm, rk_step, it, fp64, stream);
-        mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream);
-        mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream);
+        mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AW]);
+        mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream, tune[TU_SUMF]);
         JobList j;  // solve_em.F:1659-1716
         j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_P, 'p');
         j.f2(WRFGPU_MUTS, 't'); j.f2(WRFGPU_MU_2, 't'); j.f2(WRFGPU_MUDF, 't');
         fill(j);
       }
-      mark(PH_SSF); launch_small_step_finish(l2, nb2, a, stream);
+      mark(PH_SSF); launch_small_step_finish(l2, nb2, a, stream, tune[TU_SSF]);
       if (rk_step == 3) {
         JobList j;  // solve_em.F:1754-1800
         j.f3(WRFGPU_RU_M, 'u'); j.f3(WRFGPU_RV_M, 'v'); j.f3(WRFGPU_WW_M, 'w');
@@ -428,8 +438,8 @@ struct Ensemble {
       }
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
-      mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream);
-      if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, rk_step, stream); }
+      mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV]);
+      if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, rk_step, stream, tune[TU_PD]); }
       swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi(l3, nb3, stream);
       if (rk_step < 3) {
@@ -477,6 +487,51 @@ struct Ensemble {
         for (int q = 0; q < capture_swaps; ++q) host_flip();
       }
     }
+    CK(cudaGetLastError());
+    return WRFGPU_OK;
+  }
+
+  // Online autotuning: `rounds` x TUNE_MAXVAR real large steps, launched
+  // directly with event marks; step q runs variant q % nvar of every family.
+  // Each family keeps the variant with the least time, taking for each
+  // variant the minimum over rounds (the first use of a variant also pays
+  // its module load).  Variants compute the same bits, so the model
+  // advances exactly as it would untuned.  The graph is rebuilt afterwards.
+  int autotune(int rounds) {
+    static const int fam_phase[NTUNE] = {PH_PD, PH_ADVS, PH_AW, PH_AUV, PH_SUMF, PH_PREP, PH_SSF, PH_SSP, PH_CFL,
+                                         PH_TEND_W};
+    for (int f = 0; f < NTUNE; ++f)
+      for (int v = 0; v < TUNE_MAXVAR; ++v) tune_ms[f][v] = -1.f;
+    for (int r = 0; r < rounds; ++r) {
+      for (int q = 0; q < TUNE_MAXVAR; ++q) {
+        for (int f = 0; f < NTUNE; ++f) tune[f] = q % TUNE_NVAR[f];
+        std::vector<std::pair<int, cudaEvent_t>> marks;
+        prof = &marks;
+        enqueue_step();
+        prof = nullptr;
+        CK(cudaStreamSynchronize(stream));
+        float ph_ms[NPHASE] = {0.f};
+        for (size_t k = 0; k + 1 < marks.size(); ++k) {
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, marks[k].second, marks[k + 1].second);
+          ph_ms[marks[k].first] += ms;
+        }
+        for (auto& mk : marks) cudaEventDestroy(mk.second);
+        for (int f = 0; f < NTUNE; ++f) {
+          const int v = q % TUNE_NVAR[f];
+          const float t = ph_ms[fam_phase[f]];
+          if (tune_ms[f][v] < 0.f || t < tune_ms[f][v]) tune_ms[f][v] = t;
+        }
+      }
+    }
+    for (int f = 0; f < NTUNE; ++f) {
+      int best = TUNE_DEFAULT[f];
+      for (int v = 0; v < TUNE_NVAR[f]; ++v)
+        if (tune_ms[f][v] >= 0.f && tune_ms[f][v] < tune_ms[f][best]) best = v;
+      tune[f] = best;
+    }
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
     CK(cudaGetLastError());
     return WRFGPU_OK;
   }
@@ -803,6 +858,23 @@ int wrfgpu_kernel_launches_per_step(WrfGpuEnsemble* h) {
   if (cudaGraphGetNodes(e.graph, nullptr, &n) != cudaSuccess) return WRFGPU_E_CUDA;
   (void)g;
   return (int)n;
+}
+
+int wrfgpu_autotune(WrfGpuEnsemble* h, int rounds) {
+  if (!h || rounds < 1 || rounds > 16) return WRFGPU_E_ARG;
+  return h->e.autotune(rounds);
+}
+
+int wrfgpu_tuning(WrfGpuEnsemble* h, int* variant, int* param, float* ms, int nfamily) {
+  if (!h || !variant || nfamily < (int)wrfgpu::NTUNE) return WRFGPU_E_ARG;
+  Ensemble& e = h->e;
+  for (int f = 0; f < (int)wrfgpu::NTUNE; ++f) {
+    variant[f] = e.tune[f];
+    if (param) param[f] = wrfgpu::TUNE_PARAM[f][e.tune[f]];
+    if (ms)
+      for (int v = 0; v < wrfgpu::TUNE_MAXVAR; ++v) ms[f * wrfgpu::TUNE_MAXVAR + v] = e.tune_ms[f][v];
+  }
+  return (int)wrfgpu::NTUNE;
 }
 
 int wrfgpu_profile_phases(WrfGpuEnsemble* h, int nsteps, double* ms_out, int* launches_out, int nphase) {

@@ -27,7 +27,8 @@ struct SFLevel {
 };
 }  // namespace
 
-__global__ void __launch_bounds__(TX* TY, 3) k_sumflux_p_rho_col(TileLaunch L, int rk_step, int iteration) {
+template <int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L, int rk_step, int iteration) {
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
   const Stage st = stage_of(m, rk_step);
@@ -113,8 +114,9 @@ __global__ void __launch_bounds__(TX* TY, 3) k_sumflux_p_rho_col(TileLaunch L, i
   }
 }
 
-void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s) {
-  k_sumflux_p_rho_col<<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s, int var) {
+  if (var == 0) k_sumflux_p_rho_col<2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  else k_sumflux_p_rho_col<3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
 // ---------------------------------------------------------------------------
@@ -132,7 +134,8 @@ struct UVLevel {
 };
 }  // namespace
 
-__global__ void __launch_bounds__(TX* TY, 3) k_advance_uv_col(TileLaunch L, int rk_step, int iteration) {
+template <int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_advance_uv_col(TileLaunch L, int rk_step, int iteration) {
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
   const Stage st = stage_of(m, rk_step);
@@ -279,8 +282,9 @@ __global__ void __launch_bounds__(TX* TY, 3) k_advance_uv_col(TileLaunch L, int 
   }
 }
 
-void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s) {
-  k_advance_uv_col<<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s, int var) {
+  if (var == 0) k_advance_uv_col<2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  else k_advance_uv_col<3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
 
@@ -410,8 +414,8 @@ template <typename RC> struct AwCfg {
   using Ring = TileRing<NF, AW_RING>;
 };
 
-template <typename RC>
-__global__ void __launch_bounds__(TX* TY, 3) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
+template <typename RC, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
   using Ring = typename AwCfg<RC>::Ring;
   constexpr int NF = AwCfg<RC>::NF;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -597,16 +601,24 @@ void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int 
   if (fp64) k_advance_mu_t_col<double><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
   else k_advance_mu_t_col<float><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
-void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s) {
+void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
+                          int var) {
   static bool attr = false;
   constexpr size_t S32 = AwCfg<float>::Ring::SMEM, S64 = AwCfg<double>::Ring::SMEM;
   if (!attr) {
-    cudaFuncSetAttribute(k_advance_w_col<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
-    cudaFuncSetAttribute(k_advance_w_col<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
+    cudaFuncSetAttribute(k_advance_w_col<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
+    cudaFuncSetAttribute(k_advance_w_col<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
+    cudaFuncSetAttribute(k_advance_w_col<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
+    cudaFuncSetAttribute(k_advance_w_col<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
     attr = true;
   }
-  if (fp64) k_advance_w_col<double><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
-  else k_advance_w_col<float><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+  if (fp64) {
+    if (var == 0) k_advance_w_col<double, 2><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+    else k_advance_w_col<double, 3><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+  } else {
+    if (var == 0) k_advance_w_col<float, 2><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+    else k_advance_w_col<float, 3><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+  }
 }
 
 }  // namespace wrfgpu

@@ -8,7 +8,8 @@
 
 namespace wrfgpu {
 
-__global__ void __launch_bounds__(BX* BY, 5) k_rk_step_prep(Launch L) {
+template <int MINB>
+__global__ void __launch_bounds__(BX* BY, MINB) k_rk_step_prep(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
@@ -145,8 +146,9 @@ __global__ void __launch_bounds__(BX* BY, 5) k_rk_step_prep(Launch L) {
   }
 }
 
-void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s) {
-  k_rk_step_prep<<<nblocks, dim3(BX, BY), 0, s>>>(L);
+void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s, int var) {
+  if (var == 0) k_rk_step_prep<3><<<nblocks, dim3(BX, BY), 0, s>>>(L);
+  else k_rk_step_prep<5><<<nblocks, dim3(BX, BY), 0, s>>>(L);
 }
 
 }  // namespace wrfgpu

@@ -382,8 +382,8 @@ __global__ void __launch_bounds__(TX* TY) k_cfl_check_col(TileLaunch L) {
 }
 
 // ------------------------------------------------------------ launchers
-void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s) {
-  k_cfl_check_col<<<dim3(nb, 8), dim3(TX, TY), 0, s>>>(L);
+void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s, int var) {
+  k_cfl_check_col<<<dim3(nb, TUNE_PARAM[TU_CFL][var]), dim3(TX, TY), 0, s>>>(L);
 }
 void launch_update_scalar_pd(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar_pd<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);

@@ -63,7 +63,8 @@ constexpr int ADV_NPL = 3;   // q, ru_m, rv_m
 constexpr size_t ADV_SMEM = (size_t)ADV_RING * ADV_NPL * HPLANE_BYTES + 2 * (TY * (TX + 1) + (TY + 1) * TX) * 4 +
                             ADV_RING * 8;
 
-__global__ void __launch_bounds__(TX* TY, 5) k_scalar_adv_update(TileLaunch L, int rk_step) {
+template <int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L, int rk_step) {
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, true);
   const Mem& m = block_member(L.mem, tp.m);
@@ -215,7 +216,8 @@ __device__ __forceinline__ void zface(const Mem& m, const ZCell& c, int kk, floa
   *lo = l; *hi = h - l;
 }
 
-__global__ void __launch_bounds__(TX* TY, 3) k_scalar_pd_update(TileLaunch L, int rk_step) {
+template <int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L, int rk_step) {
   using P = PDPlanes;
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, true);
@@ -483,21 +485,31 @@ __global__ void k_swap_species(Mem* mems, int nmem) {
   }
 }
 
-void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_scalar_adv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ADV_SMEM);
-    attr = true;
-  }
-  k_scalar_adv_update<<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+template <typename K>
+static void set_smem(K kernel, size_t bytes) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
-void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s) {
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_scalar_pd_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PD_SMEM);
+    set_smem(k_scalar_adv_update<4>, ADV_SMEM);
+    set_smem(k_scalar_adv_update<5>, ADV_SMEM);
+    set_smem(k_scalar_adv_update<6>, ADV_SMEM);
     attr = true;
   }
-  k_scalar_pd_update<<<nblocks, dim3(TX, TY), PD_SMEM, s>>>(L, rk_step);
+  if (var == 0) k_scalar_adv_update<4><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  else if (var == 1) k_scalar_adv_update<5><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  else k_scalar_adv_update<6><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+}
+void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var) {
+  static bool attr = false;
+  if (!attr) {
+    set_smem(k_scalar_pd_update<2>, PD_SMEM);
+    set_smem(k_scalar_pd_update<3>, PD_SMEM);
+    attr = true;
+  }
+  if (var == 0) k_scalar_pd_update<2><<<nblocks, dim3(TX, TY), PD_SMEM, s>>>(L, rk_step);
+  else k_scalar_pd_update<3><<<nblocks, dim3(TX, TY), PD_SMEM, s>>>(L, rk_step);
 }
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
   k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);

@@ -557,7 +557,8 @@ __global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step,
 }
 
 // ------------------------------------------------------------ small_step_finish
-__global__ void __launch_bounds__(BX* BY, 6) k_small_step_finish(Launch L, int rk_step) {
+template <int MINB>
+__global__ void __launch_bounds__(BX* BY, MINB) k_small_step_finish(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
@@ -634,9 +635,10 @@ __global__ void __launch_bounds__(BX* BY, 6) k_small_step_finish(Launch L, int r
 }
 
 // ------------------------------------------------------------ launchers
-void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, int nb_st, StepArgs a, cudaStream_t s) {
+void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, int nb_st, StepArgs a, cudaStream_t s,
+                            int var) {
   k_small_step_prep_2d<<<nb2, dim3(BX, BY), 0, s>>>(L2, a.rk_step);
-  k_small_step_prep_3d<<<dim3(nb_st, 4), dim3(TX, TY), 0, s>>>(LST, a.rk_step);
+  k_small_step_prep_3d<<<dim3(nb_st, TUNE_PARAM[TU_SSP][var]), dim3(TX, TY), 0, s>>>(LST, a.rk_step);
 }
 void launch_calc_p_rho(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_calc_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.iteration);
@@ -660,8 +662,9 @@ void launch_sumflux_p_rho(const Launch& L, int nb, StepArgs a, bool do_p_rho, cu
   k_sumflux_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration, do_p_rho ? 1 : 0);
 }
 void launch_sumflux(const Launch& L, int nb, StepArgs a, cudaStream_t s) { launch_sumflux_p_rho(L, nb, a, false, s); }
-void launch_small_step_finish(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
-  k_small_step_finish<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+void launch_small_step_finish(const Launch& L, int nb, StepArgs a, cudaStream_t s, int var) {
+  if (var == 0) k_small_step_finish<4><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+  else k_small_step_finish<6><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
 }
 
 }  // namespace wrfgpu

@@ -38,13 +38,26 @@ enum : int {
   TF_ALL = 31
 };
 
-void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s);
+// Run-time tuned launch variants (the autotuner in driver.cu times them on
+// the real step and keeps the fastest).  Every variant of a family computes
+// the same bits: they differ only in launch bounds (registers per thread,
+// so blocks per SM) or in how many level chunks a column kernel is split into.
+enum Tune { TU_PD = 0, TU_ADV, TU_AW, TU_AUV, TU_SUMF, TU_PREP, TU_SSF, TU_SSP, TU_CFL, TU_TENDW, NTUNE };
+constexpr int TUNE_MAXVAR = 4;
+constexpr int TUNE_NVAR[NTUNE] = {2, 3, 2, 2, 2, 2, 2, 4, 4, 3};
+constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 1, 1, 1, 1, 2, 2, 1};
+// the parameter each variant stands for (blocks per SM, or level chunks)
+constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{2, 3, 0, 0}, {4, 5, 6, 0}, {2, 3, 0, 0}, {2, 3, 0, 0}, {2, 3, 0, 0},
+                                                {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {4, 5, 6, 0}};
+
+void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_PREP]);
 void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s);
 
 // rk_tendency
 void launch_tend_u(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_v(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_w(const Launch& L2, int nblocks, int flags, cudaStream_t s);
+void launch_tend_w_all(const Launch& L2, int nblocks, int var, cudaStream_t s);  // TF_ALL, tuned
 void launch_tend_t(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_zero_save(const Launch& L3, int nblocks, cudaStream_t s);
@@ -56,7 +69,8 @@ void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_
 
 // acoustic steps
 // 2-D part over column blocks, then the 3-D part over staggered tiles x level chunks
-void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, int nb_st, StepArgs a, cudaStream_t s);
+void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, int nb_st, StepArgs a, cudaStream_t s,
+                            int var = TUNE_DEFAULT[TU_SSP]);
 void launch_calc_p_rho(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_calc_coef_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
 void launch_advance_uv(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
@@ -64,7 +78,7 @@ void launch_advance_mu_t(const Launch& L2, int nblocks, StepArgs a, bool fp64, c
 void launch_advance_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
 void launch_sumflux_p_rho(const Launch& L3, int nblocks, StepArgs a, bool do_p_rho, cudaStream_t s);
 void launch_sumflux(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
-void launch_small_step_finish(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s);
+void launch_small_step_finish(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s, int var = TUNE_DEFAULT[TU_SSF]);
 
 // scalars and diagnosis
 void launch_update_scalar_pd(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
@@ -74,19 +88,22 @@ void launch_update_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_
 void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_cfl_check(const Launch& L3, int nblocks, cudaStream_t s);
-void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s);  // mass-extent tiles
+void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CFL]);  // mass tiles
 
 // fused scalar transport (k_scalar_fused.cu): one block per (tile, species)
-void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s);
-void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s);
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var = TUNE_DEFAULT[TU_ADV]);
+void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var = TUNE_DEFAULT[TU_PD]);
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s);
 
 // column-marching acoustic kernels (k_acoustic_col.cu): one block per tile
 // of the staggered extents
-void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s);
-void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s);
+void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s,
+                              int var = TUNE_DEFAULT[TU_SUMF]);
+void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s,
+                           int var = TUNE_DEFAULT[TU_AUV]);
 // one block per tile of mass columns
 void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s);
-void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s);
+void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
+                          int var = TUNE_DEFAULT[TU_AW]);
 
 }  // namespace wrfgpu

@@ -53,6 +53,8 @@ def load():
     L.wrfgpu_device_bytes.restype = C.c_longlong
     L.wrfgpu_kernel_launches_per_step.argtypes = [vp]
     L.wrfgpu_profile_phases.argtypes = [vp, C.c_int, P(C.c_double), P(C.c_int), C.c_int]
+    L.wrfgpu_autotune.argtypes = [vp, C.c_int]
+    L.wrfgpu_tuning.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_float), C.c_int]
     L.wrfgpu_phase_name.argtypes = [C.c_int]
     L.wrfgpu_phase_name.restype = C.c_char_p
     L.wrfgpu_version.restype = C.c_char_p
@@ -164,6 +166,26 @@ class Ensemble:
         if got < 0:
             _check(got, "profile_phases")
         return {self.L.wrfgpu_phase_name(p).decode(): (ms[p], cnt[p]) for p in range(got)}
+
+    TUNE_FAMILIES = ["scalar_pd_update", "scalar_adv_update", "advance_w", "advance_uv", "sumflux_calc_p_rho",
+                     "step_prep", "small_step_finish", "small_step_prep", "cfl_check", "rk_tend_w"]
+
+    def autotune(self, rounds=2):
+        """Online autotuning (advances the model rounds x 4 steps); returns tuning()."""
+        _check(self.L.wrfgpu_autotune(self.h, rounds), "wrfgpu_autotune")
+        return self.tuning()
+
+    def tuning(self):
+        """{family: {"variant", "param", "ms": [per-variant ms per step]}}."""
+        n = len(self.TUNE_FAMILIES)
+        var = (C.c_int * n)()
+        par = (C.c_int * n)()
+        ms = (C.c_float * (4 * n))()
+        got = self.L.wrfgpu_tuning(self.h, var, par, ms, n)
+        if got < 0:
+            _check(got, "wrfgpu_tuning")
+        return {f: {"variant": var[q], "param": par[q], "ms": [round(ms[4 * q + v], 4) for v in range(4) if ms[4 * q + v] >= 0]}
+                for q, f in enumerate(self.TUNE_FAMILIES)}
 
     def launches_per_step(self):
         return int(self.L.wrfgpu_kernel_launches_per_step(self.h))

@@ -2,24 +2,34 @@
 //
 // Fast path: float-float ("double-float") arithmetic on FP32 units, built on
 // Dekker's error-free transformations (TwoSum, and TwoProduct with a fused
-// multiply-add), with truncated Taylor series of atanh (log) and exp after
-// the usual reduction exp(z) = 2^n exp(z - n ln2).  Its relative error is a
-// few 1e-15, far below half an FP32 ulp (6e-8).
+// multiply-add), with table-driven reductions in the manner of Tang
+// ("Table-driven implementation of the logarithm / exponential function",
+// ACM TOMS 1989/1990):
+//   log x = E log 2 + T_j + log1p(r),  r = m rc_j - 1 exactly, |r| < 2^-8,
+//           T_j = -log(rc_j) (128 entries), log1p to r^6;
+//   exp z = 2^k 2^(j/64) exp(r),  r = z - (64k + j) log2/64, |r| < 2^-7,
+//           exp(r) to r^5;
+// the tables are in ffmath_tables.h (gen_ffmath_tables.py, 50-digit decimal
+// arithmetic).  Relative error below 1e-13 for log and pow (measured by
+// tests/native/ffmath_check.cpp against long double).
 // Rounding test (Ziv's strategy): the float-float result hi + lo rounds to hi
-// unless |lo| sits within the error bound of half an ulp of hi; only then is
-// the value recomputed in FP64 with the CUDA / libm double functions and
-// rounded once.  That happens for ~1e-5 of the inputs.
+// unless |lo| sits within 1e-12 |hi| of half an ulp of hi; only then is the
+// value recomputed in FP64 with the CUDA / libm double functions and rounded
+// once (~1e-5 of the inputs).
 //
 // They replace the libm calls of calc_p_rho_phi (the reference's LOG and
 // x**cpovcv through vspow, frame/libmassv.F:383), so that the GPU rounds
 // like a correctly rounded libm.
 #pragma once
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 #ifdef __CUDACC__
 #define FFM_HD __host__ __device__ __forceinline__
 #else
 #define FFM_HD inline
 #endif
+#include "ffmath_tables.h"
 
 namespace wrfgpu_ff {
 
@@ -86,65 +96,108 @@ FFM_HD ff ff_mulf(ff a, float b) {
   float e = p.lo + a.lo * b;
   return fast_two_sum(p.hi, e);
 }
-FFM_HD ff ff_div(ff a, ff b) {  // a / b with two correction steps
-  float q1 = a.hi / b.hi;
-  ff r = ff_add(a, ff_mulf(ff{-b.hi, -b.lo}, q1));
-  float q2 = r.hi / b.hi;
-  r = ff_add(r, ff_mulf(ff{-b.hi, -b.lo}, q2));
-  float q3 = r.hi / b.hi;
-  ff q = fast_two_sum(q1, q2);
-  return ff_add(q, ff{q3, 0.f});
+
+// tables: global memory on the device (read through the non-coherent cache),
+// ordinary arrays on the host
+#ifdef __CUDACC__
+static __device__ __align__(16) const float LOG_TAB_DEV[128][4] = WRFGPU_FF_LOG_TAB;
+static __device__ __align__(8) const float EXP_TAB_DEV[64][2] = WRFGPU_FF_EXP_TAB;
+#endif
+static const float LOG_TAB_HOST[128][4] = WRFGPU_FF_LOG_TAB;
+static const float EXP_TAB_HOST[64][2] = WRFGPU_FF_EXP_TAB;
+
+FFM_HD uint32_t f2u(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t u; std::memcpy(&u, &x, 4); return u;
+#endif
+}
+FFM_HD float u2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float x; std::memcpy(&x, &u, 4); return x;
+#endif
+}
+// hi + lo with |lo| small: add one float
+FFM_HD ff ff_addf(ff a, float b) {
+  ff s = two_sum(a.hi, b);
+  s.lo += a.lo;
+  return fast_two_sum(s.hi, s.lo);
 }
 
-// ln 2 and 1/n as (nearest float, float remainder) pairs.
-constexpr float LN2_HI = 0.6931471824645996f;
-constexpr float LN2_LO = -1.9046542121259336e-09f;
-constexpr float INV_LN2 = 1.4426950408889634f;
-#define WRFGPU_FF(h, l) ff { h##f, l##f }
-
-// natural log of x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)),
-// log m = 2 atanh(t) = 2t (1 + t^2/3 + t^4/5 + ...), t = (m-1)/(m+1), |t| <= 0.172.
-// Terms from t^8 on are summed in float (their float error is < 1e-14 of the
-// result); the series is cut after t^18 (truncation < 1e-15).
-FFM_HD ff ff_log(float x) {
-  int e = 0;
-  float m = frexpf_(x, &e);
-  if (m < 0.70710678f) { m = m * 2.f; e -= 1; }
-  ff num = {m - 1.f, 0.f};  // exact (Sterbenz)
-  ff den = two_sum(m, 1.f);
-  ff t = ff_div(num, den);
-  ff t2 = ff_mul(t, t);
-  const float s = t2.hi;
-  const float f8 = 1.f / 9.f + s * (1.f / 11.f + s * (1.f / 13.f + s * (1.f / 15.f + s * (1.f / 17.f + s * (1.f / 19.f)))));
-  ff a = ff_add(WRFGPU_FF(0.1428571492433548, -6.38621200366174e-09), ff_mulf(t2, f8));  // 1/7 + ...
-  a = ff_add(WRFGPU_FF(0.20000000298023224, -2.9802322831784522e-09), ff_mul(t2, a));     // 1/5 + ...
-  a = ff_add(WRFGPU_FF(0.3333333432674408, -9.934107758624577e-09), ff_mul(t2, a));      // 1/3 + ...
-  a = ff_add(ff{1.f, 0.f}, ff_mul(t2, a));
-  ff lm = ff_mul(ff{2.f * t.hi, 2.f * t.lo}, a);
-  const float ef = (float)e;
-  ff el = ff_add(two_prod(ef, LN2_HI), ff{ef * LN2_LO, 0.f});
-  return ff_add(el, lm);
+// log x for a positive normal float, as a float pair
+FFM_HD ff ff_log_t(float x) {
+  const uint32_t b = f2u(x);
+  int e = (int)(b >> 23) - 127;
+  const int j = (int)((b >> 16) & 127u);
+  const float m = u2f((b & 0x007FFFFFu) | 0x3F800000u);  // [1, 2)
+#ifdef __CUDA_ARCH__
+  const float4 t = __ldg(reinterpret_cast<const float4*>(LOG_TAB_DEV[j]));
+  const float rc = t.x, th = t.y, tl = t.z;
+#else
+  const float rc = LOG_TAB_HOST[j][0], th = LOG_TAB_HOST[j][1], tl = LOG_TAB_HOST[j][2];
+#endif
+  if (j >= 64) e += 1;  // m in [1.5, 2) counts as m/2 (the table holds -log(rc) - log 2)
+  // r = m rc - 1 exactly: m rc = p.hi + p.lo, p.hi - 1 exact (p.hi near 1)
+  const ff p = two_prod(m, rc);
+  const ff r = two_sum(p.hi - 1.f, p.lo);
+  // log1p(r) = r - r^2/2 + r^3/3 + r^4 (-1/4 + r/5 - r^2/6) + O(r^7): the
+  // terms through r^3 in float-float (r^3/3 is ~r^2/3 of the result, so its
+  // float rounding alone would cost up to 1e-12), the rest in float
+  const float rh = r.hi;
+  ff r2 = two_prod(rh, rh);
+  r2.lo += 2.f * rh * r.lo;
+  ff r3 = ff_mulf(r2, rh);
+  r3.lo += rh * (rh * r.lo);
+  const ff t3 = ff_mul(r3, ff{THIRD_HI, THIRD_LO});
+  const float r4 = r2.hi * r2.hi;
+  const float d4 = r4 * (-0.25f + rh * (0.2f - rh * (1.f / 6.f)));
+  ff l = ff_add(r, ff{-0.5f * r2.hi, -0.5f * r2.lo});
+  l = ff_add(l, t3);
+  l = ff_addf(l, d4);
+  l = ff_add(ff{th, tl}, l);
+  if (e != 0) {
+    const float ef = (float)e;
+    const float h = ef * LN2F_HI;
+    const ff el = fast_two_sum(h, fmaf_(ef, LN2F_HI, -h) + ef * LN2F_LO);
+    l = ff_add(el, l);
+  }
+  return l;
 }
 
-// exp(r) for |r| <= ~0.35: Horner in float-float down to the r^6/720 term,
-// the r^7.. r^13 terms in float (their float error is < 2e-14 of the
-// result; truncation < 2e-16).
-FFM_HD ff ff_exp_reduced(ff r) {
-  const float s = r.hi;
-  const float g = 1.f / 5040.f + s * (1.f / 40320.f + s * (1.f / 362880.f + s * (1.f / 3628800.f +
-                  s * (1.f / 39916800.f + s * (1.f / 479001600.f + s * (1.f / 6227020800.f))))));
-  ff a = ff_add(WRFGPU_FF(0.0013888889225199819, -3.3631094437103215e-11), ff_mulf(r, g));  // 1/720
-  a = ff_add(WRFGPU_FF(0.008333333767950535, -4.34617203337595e-10), ff_mul(r, a));         // 1/120
-  a = ff_add(WRFGPU_FF(0.0416666679084301, -1.2417634698280722e-09), ff_mul(r, a));         // 1/24
-  a = ff_add(WRFGPU_FF(0.1666666716337204, -4.967053879312289e-09), ff_mul(r, a));          // 1/6
-  a = ff_add(ff{0.5f, 0.f}, ff_mul(r, a));
-  a = ff_add(ff{1.f, 0.f}, ff_mul(r, a));
-  return ff_add(ff{1.f, 0.f}, ff_mul(r, a));
+// exp z for |z| < ~80, as 2^k times a float pair in [0.7, 1.5)
+FFM_HD ff ff_exp_t(ff z, int* k) {
+  const float nf = rintf_(z.hi * INV_LN2_64);
+  const int n = (int)nf;
+  // r = z - n log2/64: n * LN2_64_HI is exact (13-bit constant, |n| < 2^11)
+  // and so is z.hi minus it (the two are within a factor of two)
+  const float a = z.hi - nf * LN2_64_HI;
+  const ff bm = two_prod(nf, LN2_64_MID);
+  ff r = two_sum(a, -bm.hi);
+  r.lo += (z.lo - bm.lo) - nf * LN2_64_LO;
+  r = fast_two_sum(r.hi, r.lo);
+  // exp(r) - 1 = r + r^2/2 + r^3 (1/6 + r/24 + r^2/120) + O(r^6)
+  const float rh = r.hi;
+  ff r2 = two_prod(rh, rh);
+  r2.lo += 2.f * rh * r.lo;
+  const float c3 = rh * r2.hi * (1.f / 6.f + rh * (1.f / 24.f + rh * (1.f / 120.f)));
+  ff q = ff_add(r, ff{0.5f * r2.hi, 0.5f * r2.lo});
+  q = ff_addf(q, c3);
+  const ff e1 = ff_add(ff{1.f, 0.f}, q);
+  const int j = n & 63;
+  *k = n >> 6;  // floor(n / 64)
+#ifdef __CUDA_ARCH__
+  const float2 t = __ldg(reinterpret_cast<const float2*>(EXP_TAB_DEV[j]));
+  return ff_mul(e1, ff{t.x, t.y});
+#else
+  return ff_mul(e1, ff{EXP_TAB_HOST[j][0], EXP_TAB_HOST[j][1]});
+#endif
 }
-#undef WRFGPU_FF
 
 // Ziv's rounding test for a normalised float-float v = hi + lo (|lo| <= ulp(hi)/2)
-// known to relative accuracy ~1e-14: hi is the correctly rounded value unless
+// known to relative accuracy 1e-13 or better: hi is the correctly rounded value unless
 // |lo| lies within 1e-12 |hi| of half an ulp of hi, or hi is a power of two.
 FFM_HD bool rounds_safely(ff v) {
   int e;
@@ -154,24 +207,32 @@ FFM_HD bool rounds_safely(ff v) {
   return fabsf(fabsf(v.lo) - half_ulp) > 1e-12f * fabsf(v.hi);
 }
 
+FFM_HD bool normal_positive(float x) {
+  const uint32_t b = f2u(x);
+  return b >= 0x00800000u && b < 0x7F800000u;  // positive, normal, finite
+}
+
 // log(x) for x > 0, correctly rounded to float.
 FFM_HD float logf_cr(float x) {
-  ff l = ff_log(x);
-  l = fast_two_sum(l.hi, l.lo);
-  if (rounds_safely(l)) return l.hi;
+  if (normal_positive(x)) {
+    ff l = ff_log_t(x);
+    l = fast_two_sum(l.hi, l.lo);
+    if (l.hi != 0.f && rounds_safely(l)) return l.hi;
+  }
   return (float)::log((double)x);
 }
 
 // x^y for x > 0 (finite, normal result), correctly rounded to float.
 FFM_HD float powf_cr(float x, float y) {
-  ff z = ff_mulf(ff_log(x), y);
-  const float n = rintf_(z.hi * INV_LN2);
-  const ff nl = two_prod(n, LN2_HI);  // n ln2_hi exactly
-  ff r = ff_add(z, ff{-nl.hi, -nl.lo});
-  r = ff_add(r, ff{-n * LN2_LO, 0.f});
-  ff v = ff_exp_reduced(r);
-  v = fast_two_sum(v.hi, v.lo);
-  if (rounds_safely(v)) return ldexpf_(v.hi, (int)n);
+  if (normal_positive(x)) {
+    const ff z = ff_mulf(ff_log_t(x), y);
+    if (fabsf(z.hi) < 80.f) {
+      int k = 0;
+      ff v = ff_exp_t(z, &k);
+      v = fast_two_sum(v.hi, v.lo);
+      if (k > -120 && k < 120 && rounds_safely(v)) return ldexpf_(v.hi, k);
+    }
+  }
   return (float)::pow((double)x, (double)y);
 }
 

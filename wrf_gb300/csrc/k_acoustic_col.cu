@@ -328,20 +328,16 @@ __global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int r
   };
   float dv[KCOL];
   RC dmdt = RC(0.);
-  {
-    D1 cur, nxt;
-    load1(k_start, cur);
-    for (int k = k_start; k <= k_end; ++k) {
-      if (k + 1 <= k_end) load1(k + 1, nxt);
-      const float d = mxy * (rdy * ((cur.v1 + (c1h(k) * muv1 + c2h(k)) * cur.vo1 * vi1) -
-                                    (cur.v0 + (c1h(k) * muv0 + c2h(k)) * cur.vo0 * vi0)) +
-                             rdx * ((cur.u1 + (c1h(k) * muu1 + c2h(k)) * cur.uo1 / uy1) -
-                                    (cur.u0 + (c1h(k) * muu0 + c2h(k)) * cur.uo0 / uy0)));
-      dv[k] = d;
-      dmdt = dmdt + (RC)dnw(k) * (RC)d;
-      cur = nxt;
-    }
-  }
+  // the levels' loads are independent: four levels in flight at a time; the
+  // sum is still taken in k order
+  chunked_levels<4, D1>(k_start, k_end, load1, [&](int k, const D1& cur) {
+    const float d = mxy * (rdy * ((cur.v1 + (c1h(k) * muv1 + c2h(k)) * cur.vo1 * vi1) -
+                                  (cur.v0 + (c1h(k) * muv0 + c2h(k)) * cur.vo0 * vi0)) +
+                           rdx * ((cur.u1 + (c1h(k) * muu1 + c2h(k)) * cur.uo1 / uy1) -
+                                  (cur.u0 + (c1h(k) * muu0 + c2h(k)) * cur.uo0 / uy0)));
+    dv[k] = d;
+    dmdt = dmdt + (RC)dnw(k) * (RC)d;
+  });
   const float mu_tend = MU_TEND.ro(i, j);
   const float muave = MU(i, j);
   const float mu = (float)((RC)muave + (RC)dts * (dmdt + (RC)mu_tend));

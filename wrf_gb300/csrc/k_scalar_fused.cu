@@ -182,9 +182,12 @@ constexpr int PD_NPL = 4;    // q, q_old, ru_m, rv_m
 constexpr int PD_FSLOT = 3;  // face planes kept for three levels
 constexpr size_t PD_SMEM =
     (size_t)PD_RING * PD_NPL * HPLANE_BYTES +
-    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 4 * PDPlanes::GN + 2 * (PDPlanes::XN + PDPlanes::YN) +
-         2 * PDPlanes::SN) +
-    PD_RING * 8;
+    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 4 * PDPlanes::GN + 2 * PDPlanes::SN) + PD_RING * 8;
+// One thread per limiter cell of the 34 x 10 region (tile + 1), plus one
+// thread per face the cells' left / bottom faces leave out (the 10 x faces of
+// column i0 + 33 and the 34 y faces of row j0 + 9): every thread computes at
+// most one x face and one y face per level, with no loop.
+constexpr int PD_THREADS = PDPlanes::SN + PDPlanes::XH + PDPlanes::YW;  // 384
 
 // One cell of the limiter region (tile + 1): its column's vertical window.
 struct ZCell {
@@ -217,14 +220,14 @@ __device__ __forceinline__ void zface(const Mem& m, const ZCell& c, int kk, floa
 }
 
 template <int MINB>
-__global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L, int rk_step) {
+__global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunch L, int rk_step) {
   using P = PDPlanes;
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, true);
   const Mem& m = block_member(L.mem, tp.m);
   const int s = tp.sub;
   if (!pd_scheme(m, s, rk_step)) return;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int tid = threadIdx.x;
   const int i0 = tp.i0, j0 = tp.j0;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
   const int kts = m.kts, kme = m.kme;
@@ -242,10 +245,6 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
   float* sMSX = p; p += P::GN;
   float* sMSY = p; p += P::GN;
   float* sCM = p; p += P::GN;   // c1(L) mut + c2(L) of the level being staged
-  float* sDX = p; p += P::XN;   // 2 / (msfty(i) + msfty(i-1)) / rdx
-  float* sDXT = p; p += P::XN;  // dx / dt
-  float* sDY = p; p += P::YN;
-  float* sDYT = p; p += P::YN;
   float* sSC = p; p += 2 * P::SN;
   ring.bar = (uint64_t*)p;
   ring.kts = kts;
@@ -266,11 +265,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
   F2 mub2 = f2(m, WRFGPU_MUB), mu1 = f2(m, WRFGPU_MU_1), mu2 = f2(m, WRFGPU_MU_2);
   F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
   auto in_mem = [&](int ii, int jj) { return ii >= m.ims && ii <= m.ime && jj >= m.jms && jj <= m.jme; };
-  auto xface_ok = [&](int ii, int jj) { return ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1; };
-  auto yface_ok = [&](int ii, int jj) { return ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2; };
 
-  // 2-D planes (halo 2) and the level-independent face metrics
-  for (int q = tid; q < P::GN; q += TX * TY) {
+  // 2-D planes (halo 2)
+  for (int q = tid; q < P::GN; q += PD_THREADS) {
     const int r = q / P::GW, c = q - r * P::GW;
     const int ii = i0 - 2 + c, jj = j0 - 2 + r;
     const bool okm = in_mem(ii, jj);
@@ -279,51 +276,64 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
     sMSY[q] = okm ? msy2(ii, jj) : 1.f;
   }
   __syncthreads();
-  for (int q = tid; q < P::XN; q += TX * TY) {
-    const int r = q / P::XW, c = q - r * P::XW;
-    const int g = (r + 1) * P::GW + (c + 1);  // 2-D index of (i0-1+c, j0-1+r)
-    const float dxv = 2.f / (sMSY[g] + sMSY[g - 1]) / rdx;
-    sDX[q] = dxv; sDXT[q] = dxv / dt;
+
+  // this thread's limiter cell (sx, sy) of the region, and its faces
+  const bool has_cell = tid < P::SN;
+  const int sx = has_cell ? tid % P::SW : 0, sy = has_cell ? tid / P::SW : 0;
+  int xq = -1, yq = -1;  // x / y face this thread computes (index in the face planes)
+  if (has_cell) {
+    xq = sy * P::XW + sx;  // left face of the cell
+    yq = sy * P::YW + sx;  // bottom face of the cell
+  } else {
+    const int q = tid - P::SN;
+    if (q < P::XH) xq = q * P::XW + (P::XW - 1);     // column i0 + TX + 1
+    else yq = (P::YH - 1) * P::YW + (q - P::XH);     // row j0 + TY + 1
   }
-  for (int q = tid; q < P::YN; q += TX * TY) {
-    const int r = q / P::YW, c = q - r * P::YW;
-    const int g = (r + 1) * P::GW + (c + 1);
-    const float dyv = 2.f / (sMSX[g] + sMSX[g - P::GW]) / rdy;
-    sDY[q] = dyv; sDYT[q] = dyv / dt;
+  // level-independent data of the faces: halo-plane offset, 2-D offset, dx
+  bool xok = false, yok = false;
+  int xo = 0, xg = 0, yo = 0, yg = 0;
+  float xdx = 0.f, xdxt = 0.f, ydy = 0.f, ydyt = 0.f;
+  if (xq >= 0) {
+    const int r = xq / P::XW, c = xq - r * P::XW;
+    const int ii = i0 - 1 + c, jj = j0 - 1 + r;
+    xok = ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1;
+    xo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
+    xg = (r + 1) * P::GW + (c + 1);
+    xdx = 2.f / (sMSY[xg] + sMSY[xg - 1]) / rdx;
+    xdxt = xdx / dt;
   }
-  // limiter cells owned by this thread: its tile column, and one ring cell for tid < 84
-  ZCell zc[2];
-  const int nring = 2 * P::SW + 2 * TY;
-  const int ncell = 1 + (tid < nring ? 1 : 0);
-  for (int q = 0; q < 2; ++q) {
-    ZCell& c = zc[q];
-    if (q == 0) { c.sx = tx + 1; c.sy = ty + 1; }
-    else if (tid < nring) {
-      const int r = tid;
-      if (r < P::SW) { c.sx = r; c.sy = 0; }
-      else if (r < 2 * P::SW) { c.sx = r - P::SW; c.sy = P::SH - 1; }
-      else if (r < 2 * P::SW + TY) { c.sx = 0; c.sy = 1 + (r - 2 * P::SW); }
-      else { c.sx = P::SW - 1; c.sy = 1 + (r - 2 * P::SW - TY); }
-    } else { c.sx = 0; c.sy = 0; }
-    c.i = i0 - 1 + c.sx; c.j = j0 - 1 + c.sy;
-    c.valid = (q < ncell) && c.i >= m.its - 1 && c.i <= itf + 1 && c.j >= m.jts - 1 && c.j <= jtf + 1;
-    c.mut = c.mub = c.mu_old = 0.f; c.mx = c.my = 1.f;
-    c.fm1 = c.f0 = c.fp1 = c.fp2 = c.fo0 = c.fop1 = c.fom1 = c.romp1 = 0.f;
-    c.hz0 = c.lz0 = c.hz1 = c.lz1 = c.hzm = c.lzm = 0.f;
-    if (c.valid) {
-      c.mut = mut2(c.i, c.j); c.mub = mub2(c.i, c.j); c.mu_old = mu1(c.i, c.j);
-      c.mx = msx2(c.i, c.j); c.my = msy2(c.i, c.j);
-      // window for L = kts (f(L-1) unused: face kts+1 is second order); z face kts = 0
-      c.f0 = fld(c.i, kts, c.j);
-      c.fp1 = fld(c.i, kts + 1, c.j);
-      c.fp2 = (kts + 2 <= kme) ? fld(c.i, kts + 2, c.j) : 0.f;
-      c.fo0 = fold(c.i, kts, c.j);
-      c.fop1 = fold(c.i, kts + 1, c.j);
-      c.romp1 = rom(c.i, kts + 1, c.j);
-    }
+  if (yq >= 0) {
+    const int r = yq / P::YW, c = yq - r * P::YW;
+    const int ii = i0 - 1 + c, jj = j0 - 1 + r;
+    yok = ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2;
+    yo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
+    yg = (r + 1) * P::GW + (c + 1);
+    ydy = 2.f / (sMSX[yg] + sMSX[yg - P::GW]) / rdy;
+    ydyt = ydy / dt;
   }
-  const int i = i0 + tx, j = j0 + ty;
-  const bool own = i <= itf && j <= jtf;
+
+  // the limiter cell's vertical window
+  ZCell c;
+  c.sx = sx; c.sy = sy;
+  c.i = i0 - 1 + sx; c.j = j0 - 1 + sy;
+  c.valid = has_cell && c.i >= m.its - 1 && c.i <= itf + 1 && c.j >= m.jts - 1 && c.j <= jtf + 1;
+  c.mut = c.mub = c.mu_old = 0.f; c.mx = c.my = 1.f;
+  c.fm1 = c.f0 = c.fp1 = c.fp2 = c.fo0 = c.fop1 = c.fom1 = c.romp1 = 0.f;
+  c.hz0 = c.lz0 = c.hz1 = c.lz1 = c.hzm = c.lzm = 0.f;
+  if (c.valid) {
+    c.mut = mut2(c.i, c.j); c.mub = mub2(c.i, c.j); c.mu_old = mu1(c.i, c.j);
+    c.mx = msx2(c.i, c.j); c.my = msy2(c.i, c.j);
+    // window for L = kts (f(L-1) unused: face kts+1 is second order); z face kts = 0
+    c.f0 = fld(c.i, kts, c.j);
+    c.fp1 = fld(c.i, kts + 1, c.j);
+    c.fp2 = (kts + 2 <= kme) ? fld(c.i, kts + 2, c.j) : 0.f;
+    c.fo0 = fold(c.i, kts, c.j);
+    c.fop1 = fold(c.i, kts + 1, c.j);
+    c.romp1 = rom(c.i, kts + 1, c.j);
+  }
+  // interior cells of the region are the tile's cells: they also update
+  const int i = c.i, j = c.j;
+  const bool own = has_cell && sx >= 1 && sx <= TX && sy >= 1 && sy <= TY && i <= itf && j <= jtf;
   float muold_u = 0.f, munew_u = 0.f, msfty_o = 1.f, msftx_o = 1.f;
   if (own) {
     muold_u = mu1(i, j) + mub2(i, j);
@@ -332,6 +342,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
     msftx_o = msx2(i, j);
   }
   float sc_m1 = -1.f, sc_0 = -1.f, sc_p1 = -1.f;  // own column factors at levels L-2, L-1, L
+  const int so = sy * P::SW + sx;                // own cell in the factor planes
+  const int xoc = sy * P::XW + sx, yoc = sy * P::YW + sx;  // own cell's left / bottom faces
   bool ok = true;
 
   for (int Lv = kts; Lv <= ktf + 1; ++Lv) {
@@ -339,7 +351,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
     if (Lv <= ktf) {
       if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
       const float c1k = c1(Lv), c2k = c2(Lv);
-      for (int q = tid; q < P::GN; q += TX * TY) sCM[q] = c1k * sMUT[q] + c2k;
+      for (int q = tid; q < P::GN; q += PD_THREADS) sCM[q] = c1k * sMUT[q] + c2k;
       ok = ring.wait(Lv) && ok;
       __syncthreads();
       const int rs = ring.slot_of(Lv);
@@ -350,59 +362,46 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
       const int fs = Lv % PD_FSLOT;
       float* XH = sXH + fs * P::XN; float* XL = sXL + fs * P::XN;
       float* YH = sYH + fs * P::YN; float* YL = sYL + fs * P::YN;
-      // ---- horizontal faces of level Lv (each once)
-      for (int q = tid; q < P::XN; q += TX * TY) {
-        const int r = q / P::XW, c = q - r * P::XW;
+      // ---- this thread's x and y faces of level Lv
+      if (xq >= 0) {
         float hi = 0.f, lo = 0.f;
-        if (xface_ok(i0 - 1 + c, j0 - 1 + r)) {
-          const int o = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
-          const int g = (r + 1) * P::GW + (c + 1);
-          const float dx = sDX[q];
-          const float mu = 0.5f * (sCM[g] + sCM[g - 1]);
+        if (xok) {
+          const int o = xo;
+          const float mu = 0.5f * (sCM[xg] + sCM[xg - 1]);
           const float vel = RU[o];
-          const float cr = vel * dt / dx / mu;
-          lo = mu * sDXT[q] * flux_upwind(FO[o - 1], FO[o], cr);
+          const float cr = vel * dt / xdx / mu;
+          lo = mu * xdxt * flux_upwind(FO[o - 1], FO[o], cr);
           const float h = vel * pflux5(F[o - 3], F[o - 2], F[o - 1], F[o], F[o + 1], F[o + 2], vel);
           hi = h - lo;
         }
-        XH[q] = hi; XL[q] = lo;
+        XH[xq] = hi; XL[xq] = lo;
       }
-      for (int q = tid; q < P::YN; q += TX * TY) {
-        const int r = q / P::YW, c = q - r * P::YW;
+      if (yq >= 0) {
         float hi = 0.f, lo = 0.f;
-        if (yface_ok(i0 - 1 + c, j0 - 1 + r)) {
-          const int o = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
-          const int g = (r + 1) * P::GW + (c + 1);
-          const float dy = sDY[q];
-          const float mu = 0.5f * (sCM[g] + sCM[g - P::GW]);
+        if (yok) {
+          const int o = yo;
+          const float mu = 0.5f * (sCM[yg] + sCM[yg - P::GW]);
           const float vel = RV[o];
-          const float cr = vel * dt / dy / mu;
-          lo = mu * sDYT[q] * flux_upwind(FO[o - HW], FO[o], cr);
+          const float cr = vel * dt / ydy / mu;
+          lo = mu * ydyt * flux_upwind(FO[o - HW], FO[o], cr);
           const float h = vel * pflux5(F[o - 3 * HW], F[o - 2 * HW], F[o - HW], F[o], F[o + HW], F[o + 2 * HW], vel);
           hi = h - lo;
         }
-        YH[q] = hi; YL[q] = lo;
+        YH[yq] = hi; YL[yq] = lo;
       }
-      // ---- vertical face Lv+1 of every owned limiter cell
-      {
+      // ---- vertical face Lv+1 of this thread's limiter cell
+      if (c.valid) {
         const int kk = Lv + 1;
         float dz = 0.f, dzdt = 0.f;
         if (kk > 1 && kk < m.kde) { dz = 2.f / (rdzw(kk) + rdzw(kk - 1)); dzdt = dz / dt; }
-        for (int q = 0; q < 2; ++q) {
-          ZCell& c = zc[q];
-          if (!c.valid) continue;
-          zface(m, c, kk, dz, dzdt, dt, ktf, &c.hz1, &c.lz1);
-        }
+        zface(m, c, kk, dz, dzdt, dt, ktf, &c.hz1, &c.lz1);
       }
       __syncthreads();
       // ---- limiter factor of level Lv (advect_scalar_pd ph_low / flux_out)
-      const float rdzwk = rdzw(Lv);
-      for (int q = 0; q < 2; ++q) {
-        ZCell& c = zc[q];
-        if (!c.valid) continue;
-        const int xo = c.sy * P::XW + c.sx, yo = c.sy * P::YW + c.sx;
-        const float hx0 = XH[xo], hx1 = XH[xo + 1], lx0 = XL[xo], lx1 = XL[xo + 1];
-        const float hy0 = YH[yo], hy1 = YH[yo + P::YW], ly0 = YL[yo], ly1 = YL[yo + P::YW];
+      if (c.valid) {
+        const float rdzwk = rdzw(Lv);
+        const float hx0 = XH[xoc], hx1 = XH[xoc + 1], lx0 = XL[xoc], lx1 = XL[xoc + 1];
+        const float hy0 = YH[yoc], hy1 = YH[yoc + P::YW], ly0 = YL[yoc], ly1 = YL[yoc + P::YW];
         const float mx = c.mx, my = c.my;
         const float ph_low = ((c1k * c.mub + c2k) + (c1k * c.mu_old)) * c.fo0 -
                              dt * (mx * my * (rdx * (lx1 - lx0) + rdy * (ly1 - ly0)) + my * rdzwk * (c.lz1 - c.lz0));
@@ -411,8 +410,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
                                      my * rdzwk * (fminf_f(0.f, c.hz1) - fmaxf_f(0.f, c.hz0)));
         float sc = -1.f;
         if (flux_out > ph_low) sc = fmaxf_f(0.f, ph_low / (flux_out + 1.e-20f));
-        sSC[slot * P::SN + c.sy * P::SW + c.sx] = sc;
-        if (q == 0) sc_p1 = sc;
+        sSC[slot * P::SN + so] = sc;
+        sc_p1 = sc;
       }
       __syncthreads();
     }
@@ -423,13 +422,11 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
       const float* XH = sXH + fs * P::XN; const float* XL = sXL + fs * P::XN;
       const float* YH = sYH + fs * P::YN; const float* YL = sYL + fs * P::YN;
       const float* SC = sSC + (k & 1) * P::SN;
-      const ZCell& c = zc[0];
-      const int xo = c.sy * P::XW + c.sx, yo = c.sy * P::YW + c.sx, so = c.sy * P::SW + c.sx;
       auto lim = [](float v, float sc) { return sc >= 0.f ? sc * v : v; };
-      float hx0 = XH[xo], hx1 = XH[xo + 1];
-      const float lx0 = XL[xo], lx1 = XL[xo + 1];
-      float hy0 = YH[yo], hy1 = YH[yo + P::YW];
-      const float ly0 = YL[yo], ly1 = YL[yo + P::YW];
+      float hx0 = XH[xoc], hx1 = XH[xoc + 1];
+      const float lx0 = XL[xoc], lx1 = XL[xoc + 1];
+      float hy0 = YH[yoc], hy1 = YH[yoc + P::YW];
+      const float ly0 = YL[yoc], ly1 = YL[yoc + P::YW];
       // z faces k (hzm) and k+1 (hz0) of the own column, as of this iteration
       float hz0 = c.hzm, hz1 = c.hz0;
       const float lz0 = c.lzm, lz1 = c.lz0;
@@ -452,9 +449,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_pd_update(TileLaunch L,
     }
     // ---- slide the windows to level Lv+1 (loads for the next level issued now)
     sc_m1 = sc_0; sc_0 = sc_p1;
-    for (int q = 0; q < 2; ++q) {
-      ZCell& c = zc[q];
-      if (!c.valid) continue;
+    if (c.valid) {
       c.hzm = c.hz0; c.lzm = c.lz0;
       c.hz0 = c.hz1; c.lz0 = c.lz1;
       c.fom1 = c.fo0;
@@ -504,12 +499,12 @@ void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cud
 void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var) {
   static bool attr = false;
   if (!attr) {
+    set_smem(k_scalar_pd_update<1>, PD_SMEM);
     set_smem(k_scalar_pd_update<2>, PD_SMEM);
-    set_smem(k_scalar_pd_update<3>, PD_SMEM);
     attr = true;
   }
-  if (var == 0) k_scalar_pd_update<2><<<nblocks, dim3(TX, TY), PD_SMEM, s>>>(L, rk_step);
-  else k_scalar_pd_update<3><<<nblocks, dim3(TX, TY), PD_SMEM, s>>>(L, rk_step);
+  if (var == 0) k_scalar_pd_update<1><<<nblocks, PD_THREADS, PD_SMEM, s>>>(L, rk_step);
+  else k_scalar_pd_update<2><<<nblocks, PD_THREADS, PD_SMEM, s>>>(L, rk_step);
 }
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
   k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);

@@ -198,44 +198,47 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
     if (sizeof(RC) == 8) return *(RC*)&d3(m, m.wd[2])(i, k, j);
     return *(RC*)&f3(m, WRFGPU_GAMMA)(i, k, j);
   };
-  float a_loc[KMAX + 1];  // A of this column, re-read by the elimination below
+  // one pass up the column: A(k) (the reference forms all of A first; A
+  // does not depend on the recursion, so the values are the same), B, C and
+  // the recursion, with the loads of four levels in flight
+  A(2) = RC(0.);
+  GA(1) = RC(0.);
+  RC gprev = RC(0.);
+  struct LC { float cqw, c2a, c2am; };
+  chunked_levels<4, LC>(
+      2, kde - 1,
+      [&](int k, LC& d) { d.cqw = cqw.ro(i, k, j); d.c2a = c2a.ro(i, k, j); d.c2am = c2a.ro(i, k - 1, j); },
+      [&](int k, const LC& d) {
+        float a_k = 0.f;
+        if (k >= 3) {
+          const int kl = k - 1;
+          a_k = -d.cqw * cof * rdn(k) * rdnw(k - 1) * d.c2am / ((c1h(kl) * MUT + c2h(kl)) * (c1f(kl) * MUT + c2f(kl)));
+          A(k) = (RC)a_k;
+        }
+        const float b = 1.f + d.cqw * cof * rdn(k) *
+                                  (rdnw(k) * d.c2a / ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k))) +
+                                   rdnw(k - 1) * d.c2am / ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k))));
+        const float c = -d.cqw * cof * rdn(k) * rdnw(k) * d.c2a /
+                        ((c1h(k) * MUT + c2h(k)) * (c1f(k + 1) * MUT + c2f(k + 1)));
+        RC al = rcp_rc<RC>((RC)b - (RC)a_k * gprev);
+        AL(k) = al;
+        gprev = (RC)c * al;
+        GA(k) = gprev;
+      });
+  float a_top;
   {
     int k = kde - 1;
-    A(2) = RC(0.);
-    a_loc[2] = 0.f;
     float r = rdnw(kde - 1);
-    const float av = -2.f * cof * (r * r) * c2a.ro(i, kde - 1, j) * lid_flag /
-                     ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k)));
-    A(kde) = (RC)av;
-    a_loc[kde] = av;
-    GA(1) = RC(0.);
-  }
-  for (int kk = 3; kk <= kde - 1; ++kk) {
-    int k = kk - 1;
-    const float av = -cqw.ro(i, kk, j) * cof * rdn(kk) * rdnw(kk - 1) * c2a.ro(i, kk - 1, j) /
-                     ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k)));
-    A(kk) = (RC)av;
-    a_loc[kk] = av;
-  }
-  RC gprev = GA(1);
-  for (int k = 2; k <= kde - 1; ++k) {
-    const float b = 1.f + cqw.ro(i, k, j) * cof * rdn(k) *
-                              (rdnw(k) * c2a.ro(i, k, j) / ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k))) +
-                               rdnw(k - 1) * c2a.ro(i, k - 1, j) /
-                                   ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k))));
-    const float c = -cqw.ro(i, k, j) * cof * rdn(k) * rdnw(k) * c2a.ro(i, k, j) /
-                    ((c1h(k) * MUT + c2h(k)) * (c1f(k + 1) * MUT + c2f(k + 1)));
-    RC al = rcp_rc<RC>((RC)b - (RC)a_loc[k] * gprev);
-    AL(k) = al;
-    gprev = (RC)c * al;
-    GA(k) = gprev;
+    a_top = -2.f * cof * (r * r) * c2a.ro(i, kde - 1, j) * lid_flag /
+            ((c1h(k) * MUT + c2h(k)) * (c1f(k) * MUT + c2f(k)));
+    A(kde) = (RC)a_top;
   }
   {
     int k = kde;
     float r = rdnw(kde - 1);
     const float b = 1.f + 2.f * cof * (r * r) * c2a.ro(i, kde - 1, j) /
                               ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k)));
-    RC al = rcp_rc<RC>((RC)b - (RC)a_loc[kde] * gprev);
+    RC al = rcp_rc<RC>((RC)b - (RC)a_top * gprev);
     AL(kde) = al;
     GA(kde) = RC(0.) * al;
   }

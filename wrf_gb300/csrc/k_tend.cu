@@ -255,22 +255,31 @@ __global__ void __launch_bounds__(BX* BY, MINB) k_tend_w(Launch L) {
   if (FL & TF_PG) { muf_c = f2(m, WRFGPU_MU_2)(i, j); mub_c = f2(m, WRFGPU_MUB)(i, j); }
   // the vertical flux of face k+1 is the lower face of level k+1
   float vf_lo = (FL & TF_ADV) && m.kts + 1 <= ktf + 1 ? vf(m.kts + 1) : 0.f;
+  // values of levels k, k-1, k-2 of the mass fluxes (and of u, v, p) at the
+  // points the w-point stencils read, carried down the column instead of
+  // re-read (the same values, so the same bits)
+  F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
+  float ru0 = 0.f, ru1 = 0.f, ru0m = 0.f, ru1m = 0.f, ru0mm = 0.f, ru1mm = 0.f;  // ru(i | i+1, k | k-1 | k-2, j)
+  float rv0 = 0.f, rv1 = 0.f, rv0m = 0.f, rv1m = 0.f, rv0mm = 0.f, rv1mm = 0.f;  // rv(i, k.., j | j+1)
+  float u0 = 0.f, u1 = 0.f, u0m = 0.f, u1m = 0.f, v0 = 0.f, v1 = 0.f, v0m = 0.f, v1m = 0.f;
+  float pk = 0.f, pkm = 0.f;
   for (int k = m.kts; k <= m.kte; ++k) {
+    ru0 = ru(i, k, j); ru1 = ru(i + 1, k, j); rv0 = rv(i, k, j); rv1 = rv(i, k, j + 1);
+    if (FL & TF_CURV) { u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1); }
+    if (FL & TF_PG) pk = p(i, k, j);
     float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
     if (k >= m.kts + 1 && k <= ktf + 1) {
       if (FL & TF_ADV) {
-        auto fy = [&](int jj) {
-          float vel = (k <= ktf) ? fzm(k) * rv(i, k, jj) + fzp(k) * rv(i, k - 1, jj)
-                                 : (2.f - fzm(k - 1)) * rv(i, k - 1, jj) - fzp(k - 1) * rv(i, k - 2, jj);
+        auto fy = [&](int jj, float r_k, float r_km, float r_kmm) {
+          float vel = (k <= ktf) ? fzm(k) * r_k + fzp(k) * r_km : (2.f - fzm(k - 1)) * r_km - fzp(k - 1) * r_kmm;
           return vel * flux5(w(i, k, jj - 3), w(i, k, jj - 2), w(i, k, jj - 1), w(i, k, jj), w(i, k, jj + 1), w(i, k, jj + 2), vel);
         };
-        t = t - mrdy * (fy(j + 1) - fy(j));
-        auto fx = [&](int ii) {
-          float vel = (k <= ktf) ? fzm(k) * ru(ii, k, j) + fzp(k) * ru(ii, k - 1, j)
-                                 : (2.f - fzm(k - 1)) * ru(ii, k - 1, j) - fzp(k - 1) * ru(ii, k - 2, j);
+        t = t - mrdy * (fy(j + 1, rv1, rv1m, rv1mm) - fy(j, rv0, rv0m, rv0mm));
+        auto fx = [&](int ii, float r_k, float r_km, float r_kmm) {
+          float vel = (k <= ktf) ? fzm(k) * r_k + fzp(k) * r_km : (2.f - fzm(k - 1)) * r_km - fzp(k - 1) * r_kmm;
           return vel * flux5(w(ii - 3, k, j), w(ii - 2, k, j), w(ii - 1, k, j), w(ii, k, j), w(ii + 1, k, j), w(ii + 2, k, j), vel);
         };
-        t = t - mrdx * (fx(i + 1) - fx(i));
+        t = t - mrdx * (fx(i + 1, ru1, ru1m, ru1mm) - fx(i, ru0, ru0m, ru0mm));
         if (k <= ktf) {
           const float vf_hi = vf(k + 1);
           t = t - rdzu(k) * (vf_hi - vf_lo);
@@ -284,32 +293,34 @@ __global__ void __launch_bounds__(BX* BY, MINB) k_tend_w(Launch L) {
       if (k == kde) {
         float cq1 = 1.f / (1.f + cqw_top);
         float cq2 = cqw_top * cq1;
-        t = t + rmg * (cq1 * 2.f * rdnw(k - 1) * (-p(i, k - 1, j)) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
+        t = t + rmg * (cq1 * 2.f * rdnw(k - 1) * (-pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       } else if (k >= 2) {
         const float cqk = cqw(i, k, j);
         float cq1 = 1.f / (1.f + cqk);
         float cq2 = cqk * cq1;
         cqw(i, k, j) = cq1;
-        t = t + rmg * (cq1 * rdzu(k) * (p(i, k, j) - p(i, k - 1, j)) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
+        t = t + rmg * (cq1 * rdzu(k) * (pk - pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       }
     }
     if (k >= m.kts + 1 && k <= ktf) {
       if (FL & TF_COR) {
-        t = t + e_c * (cosa05 * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) -
-                       rsina05 * (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))));
+        t = t + e_c * (cosa05 * (fzm(k) * (ru0 + ru1) + fzp(k) * (ru0m + ru1m)) -
+                       rsina05 * (fzm(k) * (rv0 + rv1) + fzp(k) * (rv0m + rv1m)));
       }
     }
     if (k >= max(2, m.kts) && k <= ktf) {
       if (FL & TF_CURV) {
-        F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
-        t = t + RERADIUS * (0.5f * (fzm(k) * (ru(i, k, j) + ru(i + 1, k, j)) + fzp(k) * (ru(i, k - 1, j) + ru(i + 1, k - 1, j))) *
-                                0.5f * (fzm(k) * (u(i, k, j) + u(i + 1, k, j)) + fzp(k) * (u(i, k - 1, j) + u(i + 1, k - 1, j))) +
-                            ratio05 *
-                                (fzm(k) * (rv(i, k, j) + rv(i, k, j + 1)) + fzp(k) * (rv(i, k - 1, j) + rv(i, k - 1, j + 1))) *
-                                0.5f * (fzm(k) * (v(i, k, j) + v(i, k, j + 1)) + fzp(k) * (v(i, k - 1, j) + v(i, k - 1, j + 1))));
+        t = t + RERADIUS * (0.5f * (fzm(k) * (ru0 + ru1) + fzp(k) * (ru0m + ru1m)) *
+                                0.5f * (fzm(k) * (u0 + u1) + fzp(k) * (u0m + u1m)) +
+                            ratio05 * (fzm(k) * (rv0 + rv1) + fzp(k) * (rv0m + rv1m)) *
+                                0.5f * (fzm(k) * (v0 + v1) + fzp(k) * (v0m + v1m)));
       }
     }
     tend(i, k, j) = t;
+    ru0mm = ru0m; ru1mm = ru1m; ru0m = ru0; ru1m = ru1;
+    rv0mm = rv0m; rv1mm = rv1m; rv0m = rv0; rv1m = rv1;
+    u0m = u0; u1m = u1; v0m = v0; v1m = v1;
+    pkm = pk;
   }
 }
 

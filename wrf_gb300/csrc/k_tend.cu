@@ -379,26 +379,6 @@ __global__ void __launch_bounds__(BX* BY) k_tend_t(Launch L) {
   tend_t_point<FL>(m, bp.i, bp.j, bp.k);
 }
 
-// column form: one thread per (i, j) of a tile, levels in order, the
-// inputs two levels ahead prefetched into L2
-template <int FL>
-__global__ void __launch_bounds__(TX* TY) k_tend_t_col(TileLaunch L) {
-  const TilePos tp = tile_pos(L, false, true);
-  const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
-  auto pf = [&](const F3& a, int kk) {
-    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
-  };
-  for (int k = m.kms; k <= m.kme; ++k) {
-    pf(f3(m, WRFGPU_T_2), k + 2);
-    pf(f3(m, WRFGPU_RU), k + 2);
-    pf(f3(m, WRFGPU_RV), k + 2);
-    pf(f3(m, WRFGPU_WW), k + 2);
-    pf(f3(m, WRFGPU_T_TEND), k + 2);
-    tend_t_point<FL>(m, i, j, k);
-  }
-}
 
 // ---------------------------------------------------------------- ph_tend
 template <int FL>
@@ -476,28 +456,6 @@ __global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
   tend_ph_point<FL>(m, bp.i, bp.j, bp.k);
 }
 
-// column form: one thread per (i, j) of a tile, levels in order, the
-// inputs two levels ahead prefetched into L2
-template <int FL>
-__global__ void __launch_bounds__(TX* TY) k_tend_ph_col(TileLaunch L) {
-  const TilePos tp = tile_pos(L, false, true);
-  const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
-  auto pf = [&](const F3& a, int kk) {
-    if (kk <= m.kme) prefetch_l2(&a(i, kk, j));
-  };
-  for (int k = m.kms; k <= m.kme; ++k) {
-    pf(f3(m, WRFGPU_PH_2), k + 2);
-    pf(f3(m, WRFGPU_PHB), k + 2);
-    pf(f3(m, WRFGPU_U_2), k + 2);
-    pf(f3(m, WRFGPU_V_2), k + 2);
-    pf(f3(m, WRFGPU_WW), k + 2);
-    pf(f3(m, WRFGPU_W_2), k + 2);
-    pf(f3(m, WRFGPU_PH_TEND), k + 2);
-    tend_ph_point<FL>(m, i, j, k);
-  }
-}
 
 // ---------------------------------------------------------------- launchers
 #define DISPATCH_FL(KERNEL, GRID, BLOCK, S, FLAGS)                                       \
@@ -522,7 +480,5 @@ void launch_tend_w_all(const Launch& L, int nb, int var, cudaStream_t s) {
 }
 void launch_tend_t(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t, nb, dim3(BX, BY), s, flags) }
 void launch_tend_ph(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph, nb, dim3(BX, BY), s, flags) }
-void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t_col, nb, dim3(TX, TY), s, flags) }
-void launch_tend_ph_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph_col, nb, dim3(TX, TY), s, flags) }
 
 }  // namespace wrfgpu

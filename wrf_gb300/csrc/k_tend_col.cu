@@ -295,6 +295,175 @@ __global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
+// ---------------------------------------------------------------- t_tend
+// advect_scalar of theta (module_advect_em.F:3394-3650, :4306-4333) plus the
+// zero_tend of the *_save arrays at the points small_step_prep leaves alone
+// (module_em.F:395-428); the vertical flux and the own-column window of
+// theta carry down the column.
+template <int FL>
+__global__ void __launch_bounds__(TX* TY, 4) k_tend_t_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  const F3 tend = f3(m, WRFGPU_T_TEND);
+  const int kts = m.kts, kte = m.kte, kme = m.kme;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(kte, m.kde - 1);
+  if (FL & TF_ZERO) {
+    const bool ie = i == m.ide, je = j == m.jde;
+    const F3 us = f3(m, WRFGPU_U_SAVE), vs = f3(m, WRFGPU_V_SAVE), ts = f3(m, WRFGPU_T_SAVE),
+             ws = f3(m, WRFGPU_W_SAVE), phs = f3(m, WRFGPU_PH_SAVE);
+    for (int k = kts; k <= kte; ++k) {
+      const bool kt = k == m.kde;
+      if (kt || je) us(i, k, j) = 0.f;
+      if (kt || ie) vs(i, k, j) = 0.f;
+      if (kt || ie || je) ts(i, k, j) = 0.f;
+      if (ie || je) { ws(i, k, j) = 0.f; phs(i, k, j) = 0.f; }
+    }
+    if (ie || je) f2(m, WRFGPU_MU_SAVE)(i, j) = 0.f;
+  }
+  const bool acc = i <= itf && j <= jtf;
+  if (!acc) {
+    if (FL & TF_ZERO)
+      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+    return;
+  }
+  const F3 fld = f3(m, WRFGPU_T_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rom = f3(m, WRFGPU_WW);
+  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+  const float msftx_c = f2(m, WRFGPU_MSFTX)(i, j);
+  const float mrdy = msftx_c * m.rdy, mrdx = msftx_c * m.rdx;
+  float fm1 = 0.f, f0 = fld(i, kts, j), fp1 = fld(i, kts + 1, j), fp2 = (kts + 2 <= kme) ? fld(i, kts + 2, j) : 0.f;
+  float vf_lo = 0.f;  // vf(kts) = 0
+  for (int k = kts; k <= ktf; ++k) {
+    if (k + 2 <= kme) {
+      prefetch_l2(&fld(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
+      prefetch_l2(&rom(i, k + 2, j));
+    }
+    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    const float fp3 = (k + 3 <= kme) ? fld(i, k + 3, j) : 0.f;
+    if (FL & TF_ADV) {
+      auto fy = [&](int jj) {
+        float vel = rv(i, k, jj);
+        return vel * flux5(fld(i, k, jj - 3), fld(i, k, jj - 2), fld(i, k, jj - 1), fld(i, k, jj), fld(i, k, jj + 1), fld(i, k, jj + 2), vel);
+      };
+      t = t - mrdy * (fy(j + 1) - fy(j));
+      auto fx = [&](int ii) {
+        float vel = ru(ii, k, j);
+        return vel * flux5(fld(ii - 3, k, j), fld(ii - 2, k, j), fld(ii - 1, k, j), fld(ii, k, j), fld(ii + 1, k, j), fld(ii + 2, k, j), vel);
+      };
+      t = t - mrdx * (fx(i + 1) - fx(i));
+      const int kk = k + 1;
+      float vf_hi;
+      if (kk == kts || kk == kte) vf_hi = 0.f;
+      else if (kk == kts + 1 || kk == ktf) vf_hi = rom(i, kk, j) * (fzm(kk) * fp1 + fzp(kk) * f0);
+      else {
+        const float vel = rom(i, kk, j);
+        vf_hi = vel * flux3(fm1, f0, fp1, fp2, -vel);
+      }
+      t = t - rdzw(k) * (vf_hi - vf_lo);
+      vf_lo = vf_hi;
+    }
+    tend(i, k, j) = t;
+    fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = fp3;
+  }
+  if (FL & TF_ZERO)
+    for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
+}
+
+// ---------------------------------------------------------------- ph_tend
+// rhs_ph (module_big_step_utilities_em.F:1365-2178, 5th/6th order branch):
+// the vertical term's wdwn(k+1) is wdwn(k) one level up, u and v of levels
+// k, k-1 carry down, the column's map factors and mass terms are read once.
+template <int FL>
+__global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > m.ite || j > m.jte) return;
+  const F3 tend = f3(m, WRFGPU_PH_TEND);
+  const int kts = m.kts, kte = m.kte, kde = m.kde;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1);
+  const bool acc = i <= itf && j <= jtf;
+  if (!acc || !(FL & TF_ADV)) {
+    if ((FL & TF_ZERO) && !acc)
+      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+    if ((FL & TF_ZERO) && acc)
+      for (int k = kts; k <= min(kte, 1); ++k) tend(i, k, j) = 0.f;
+    return;
+  }
+  const F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), ww = f3(m, WRFGPU_WW), ph = f3(m, WRFGPU_PH_2),
+           phb = f3(m, WRFGPU_PHB), w = f3(m, WRFGPU_W_2);
+  const F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
+           rdnw = f1(m, WRFGPU_RDNW);
+  // column constants
+  const float mut_c = f2(m, WRFGPU_MUT)(i, j), msfty_c = f2(m, WRFGPU_MSFTY)(i, j);
+  const float muv1 = f2(m, WRFGPU_MUV)(i, j + 1), muv0 = f2(m, WRFGPU_MUV)(i, j);
+  const float muu1 = f2(m, WRFGPU_MUU)(i + 1, j), muu0 = f2(m, WRFGPU_MUU)(i, j);
+  const float mvy1 = f2(m, WRFGPU_MSFVY)(i, j + 1), mvy0 = f2(m, WRFGPU_MSFVY)(i, j);
+  const float mux1 = f2(m, WRFGPU_MSFUX)(i + 1, j), mux0 = f2(m, WRFGPU_MSFUX)(i, j);
+  const float cy4 = 0.25f * m.rdy / msfty_c, cx4 = 0.25f * m.rdx / msfty_c;
+  const float cy2 = 0.5f * m.rdy / msfty_c, cx2 = 0.5f * m.rdx / msfty_c;
+  const float cfn = m.cfn, cfn1 = m.cfn1;
+  const bool adv2 = m.cf.phi_adv_z == 2;
+  // carried: wdwn(k) and u, v of levels k-1, k-2 at (i, i+1) / (j, j+1)
+  auto wdwn = [&](int kk) {
+    if (adv2) return rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
+    return .5f * (ww(i, kk, j) + ww(i, kk - 1, j)) * rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
+  };
+  float u0m = u(i, 1, j), u1m = u(i + 1, 1, j), v0m = v(i, 1, j), v1m = v(i, 1, j + 1);  // level k-1 = 1
+  float u0mm = 0.f, u1mm = 0.f, v0mm = 0.f, v1mm = 0.f;
+  float wd_lo = (2 <= kte - 1) ? wdwn(2) : 0.f;  // wdwn(k) at k = 2
+  for (int k = kts; k <= kte; ++k) {
+    if (k + 2 <= kte) {
+      prefetch_l2(&ph(i, k + 2, j)); prefetch_l2(&phb(i, k + 2, j)); prefetch_l2(&u(i, k + 2, j));
+      prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ww(i, k + 2, j)); prefetch_l2(&w(i, k + 2, j));
+    }
+    if (k < 2) {
+      if (FL & TF_ZERO) tend(i, k, j) = 0.f;
+      continue;
+    }
+    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    // vertical advection of ph (:1396-1428)
+    if (k <= kte - 1) {
+      const float wd_hi = wdwn(k + 1);
+      if (adv2) t = t - ww(i, k, j) * (fnm(k) * wd_hi + fnp(k) * wd_lo);
+      else t = t - (fnm(k) * wd_hi + fnp(k) * wd_lo);
+      wd_lo = wd_hi;
+    }
+    // "gw" term (:1432-1446)
+    if (m.cf.non_hydrostatic) {
+      if (k == kde) t = 0.f;
+      t = t + (c1f(k) * mut_c + c2f(k)) * G * w(i, k, j) / msfty_c;
+    }
+    auto S = [&](int di, int dj) {  // 6th-order centred difference of ph + phb
+      return 45.f * (ph(i + di, k, j + dj) - ph(i - di, k, j - dj)) -
+             9.f * (ph(i + 2 * di, k, j + 2 * dj) - ph(i - 2 * di, k, j - 2 * dj)) +
+             (ph(i + 3 * di, k, j + 3 * dj) - ph(i - 3 * di, k, j - 3 * dj)) +
+             45.f * (phb(i + di, k, j + dj) - phb(i - di, k, j - dj)) -
+             9.f * (phb(i + 2 * di, k, j + 2 * dj) - phb(i - 2 * di, k, j - 2 * dj)) +
+             (phb(i + 3 * di, k, j + 3 * dj) - phb(i - 3 * di, k, j - 3 * dj));
+    };
+    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f;
+    if (k <= kte - 1) {
+      u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1);
+      t = t - cy4 * (((c1f(k) * muv1 + c2f(k)) * (v1 + v1m) * mvy1 + (c1f(k) * muv0 + c2f(k)) * (v0 + v0m) * mvy0) *
+                     (1.f / 60.f) * S(0, 1));
+      t = t - cx4 * (((c1f(k) * muu1 + c2f(k)) * (u1 + u1m) * mux1 + (c1f(k) * muu0 + c2f(k)) * (u0 + u0m) * mux0) *
+                     (1.f / 60.f) * S(1, 0));
+    } else {
+      t = t - cy2 * (((c1f(k) * muv1 + c2f(k)) * (cfn * v1m + cfn1 * v1mm) * mvy1 +
+                      (c1f(k) * muv0 + c2f(k)) * (cfn * v0m + cfn1 * v0mm) * mvy0) *
+                     (1.f / 60.f) * S(0, 1));
+      t = t - cx2 * (((c1f(k) * muu1 + c2f(k)) * (cfn * u1m + cfn1 * u1mm) * mux1 +
+                      (c1f(k) * muu0 + c2f(k)) * (cfn * u0m + cfn1 * u0mm) * mux0) *
+                     (1.f / 60.f) * S(1, 0));
+    }
+    tend(i, k, j) = t;
+    u0mm = u0m; u1mm = u1m; v0mm = v0m; v1mm = v1m;
+    u0m = u0; u1m = u1; v0m = v0; v1m = v1;
+  }
+}
+
 #define DISPATCH_COL(KERNEL, GRID, S, FLAGS)                                                  \
   switch (FLAGS) {                                                                            \
     case TF_ALL: KERNEL<TF_ALL><<<GRID, dim3(TX, TY), 0, S>>>(L); break;                      \
@@ -304,5 +473,11 @@ __global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
 
 void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_COL(k_tend_u_col, nb, s, flags) }
 void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_COL(k_tend_v_col, nb, s, flags) }
+void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
+  if (flags == (TF_ZERO | TF_ADV)) k_tend_t_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);
+}
+void launch_tend_ph_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
+  if (flags == (TF_ZERO | TF_ADV)) k_tend_ph_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);
+}
 
 }  // namespace wrfgpu

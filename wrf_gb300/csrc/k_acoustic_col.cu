@@ -27,6 +27,9 @@ struct SFLevel {
 };
 }  // namespace
 
+// One block per (staggered tile, chunk of levels: gridDim.y chunks); the
+// levels are independent but for ph(k), carried from the level below within
+// a chunk and read at a chunk's first level.
 template <int MINB>
 __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L, int rk_step, int iteration) {
   const TilePos tp = tile_pos(L, false, true);
@@ -71,11 +74,14 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
       v.ph1 = v.alt = v.t2 = v.t1 = v.c2a = v.pm1 = 0.f;
     }
   };
+  const int per = (kte - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = kts + (int)blockIdx.y * per, k1 = min(kte, k0 + per - 1);
+  if (k0 > k1) return;
   SFLevel cur, nxt;
-  load(kts, cur);
-  float ph_k = mcol ? ph.ro(i, kts, j) : 0.f;
-  for (int k = kts; k <= kte; ++k) {
-    if (k + 1 <= kte) load(k + 1, nxt);
+  load(k0, cur);
+  float ph_k = mcol ? ph.ro(i, k0, j) : 0.f;
+  for (int k = k0; k <= k1; ++k) {
+    if (k + 1 <= k1) load(k + 1, nxt);
     const bool ru_acc = ucol && k <= mink, rv_acc = vcol && k <= mink;
     // sumflux
     float rum = cur.rum, rvm = cur.rvm, wwm = cur.wwm;
@@ -115,8 +121,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
 }
 
 void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s, int var) {
-  if (var == 0) k_sumflux_p_rho_col<2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
-  else k_sumflux_p_rho_col<3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  k_sumflux_p_rho_col<3><<<dim3(nblocks, TUNE_PARAM[TU_SUMF][var]), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
 // ---------------------------------------------------------------------------
@@ -217,18 +222,29 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_uv_col(TileLaunch L, i
       d.pby = pb.ro(i, k, j - 1); d.phpy = php.ro(i, k, j - 1); d.alty = alt.ro(i, k, j - 1); d.aly = al.ro(i, k, j - 1);
     }
   };
-  // level k_start values of p and ph, and dpn(k_start) = dpn(1)
+  // this block's chunk of levels (gridDim.y chunks); the levels are
+  // independent but for the carried p, ph and dpn of the level below
+  const int per = (k_end - k_start + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = k_start + (int)blockIdx.y * per, k1 = min(k_end, k0 + per - 1);
+  if (k0 > k1) return;
+  // level k0 values of p and ph, and dpn(k0) (dpn(1) has its own formula)
   float p0 = 0.f, ph0 = 0.f, p0x = 0.f, ph0x = 0.f, p0y = 0.f, ph0y = 0.f, dpn_u = 0.f, dpn_v = 0.f;
-  if (need_c) { p0 = p.ro(i, k_start, j); ph0 = ph.ro(i, k_start, j); }
+  if (need_c) { p0 = p.ro(i, k0, j); ph0 = ph.ro(i, k0, j); }
   if (need_x) {
-    p0x = p.ro(i - 1, k_start, j); ph0x = ph.ro(i - 1, k_start, j);
-    dpn_u = .5f * (cf1 * (p.ro(i, 1, j) + p.ro(i - 1, 1, j)) + cf2 * (p.ro(i, 2, j) + p.ro(i - 1, 2, j)) +
-                   cf3 * (p.ro(i, 3, j) + p.ro(i - 1, 3, j)));
+    p0x = p.ro(i - 1, k0, j); ph0x = ph.ro(i - 1, k0, j);
+    if (k0 == 1)
+      dpn_u = .5f * (cf1 * (p.ro(i, 1, j) + p.ro(i - 1, 1, j)) + cf2 * (p.ro(i, 2, j) + p.ro(i - 1, 2, j)) +
+                     cf3 * (p.ro(i, 3, j) + p.ro(i - 1, 3, j)));
+    else
+      dpn_u = .5f * (fnm(k0) * (p0 + p0x) + fnp(k0) * (p.ro(i, k0 - 1, j) + p.ro(i - 1, k0 - 1, j)));
   }
   if (need_y) {
-    p0y = p.ro(i, k_start, j - 1); ph0y = ph.ro(i, k_start, j - 1);
-    dpn_v = .5f * (cf1 * (p.ro(i, 1, j) + p.ro(i, 1, j - 1)) + cf2 * (p.ro(i, 2, j) + p.ro(i, 2, j - 1)) +
-                   cf3 * (p.ro(i, 3, j) + p.ro(i, 3, j - 1)));
+    p0y = p.ro(i, k0, j - 1); ph0y = ph.ro(i, k0, j - 1);
+    if (k0 == 1)
+      dpn_v = .5f * (cf1 * (p.ro(i, 1, j) + p.ro(i, 1, j - 1)) + cf2 * (p.ro(i, 2, j) + p.ro(i, 2, j - 1)) +
+                     cf3 * (p.ro(i, 3, j) + p.ro(i, 3, j - 1)));
+    else
+      dpn_v = .5f * (fnm(k0) * (p0 + p0y) + fnp(k0) * (p.ro(i, k0 - 1, j) + p.ro(i, k0 - 1, j - 1)));
   }
   // top value of dpn (kde): zero unless the lid is rigid
   float dpn_u_top = 0.f, dpn_v_top = 0.f;
@@ -241,9 +257,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_uv_col(TileLaunch L, i
                          cf3 * (p.ro(i, kde - 3, j - 1) + p.ro(i, kde - 3, j)));
   }
   UVLevel cur, nxt;
-  load(k_start, cur);
-  for (int k = k_start; k <= k_end; ++k) {
-    if (k + 1 <= k_end) load(k + 1, nxt);
+  load(k0, cur);
+  for (int k = k0; k <= k1; ++k) {
+    if (k + 1 <= k1) load(k + 1, nxt);
     const int kk = k + 1;
     // u
     if (upt) {
@@ -283,8 +299,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_uv_col(TileLaunch L, i
 }
 
 void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s, int var) {
-  if (var == 0) k_advance_uv_col<2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
-  else k_advance_uv_col<3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  k_advance_uv_col<3><<<dim3(nblocks, TUNE_PARAM[TU_AUV][var]), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
 

@@ -395,8 +395,8 @@ struct Ensemble {
         fill(j);
       }
       // rk_tendency (module_em.F:370-781)
-      mark(PH_TEND_U); launch_tend_u_col(LST(), nb_st, TF_ALL, stream);
-      mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream);
+      mark(PH_TEND_U); launch_tend_u_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDU]);
+      mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDV]);
       mark(PH_TEND_W); launch_tend_w_all(l2, nb2, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
@@ -499,7 +499,7 @@ struct Ensemble {
   // advances exactly as it would untuned.  The graph is rebuilt afterwards.
   int autotune(int rounds) {
     static const int fam_phase[NTUNE] = {PH_PD, PH_ADVS, PH_AW, PH_AUV, PH_SUMF, PH_PREP, PH_SSF, PH_SSP, PH_CFL,
-                                         PH_TEND_W};
+                                         PH_TEND_W, PH_TEND_U, PH_TEND_V};
     for (int f = 0; f < NTUNE; ++f)
       for (int v = 0; v < TUNE_MAXVAR; ++v) tune_ms[f][v] = -1.f;
     for (int r = 0; r < rounds; ++r) {

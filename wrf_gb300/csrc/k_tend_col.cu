@@ -67,24 +67,40 @@ __global__ void __launch_bounds__(TX* TY) k_tend_u_col(TileLaunch L) {
     duy_r = msfuy(i + 1, j) - msfuy(i, j);
     duy_l = msfuy(i, j) - msfuy(i - 1, j);
   }
+  // this block's chunk of levels (gridDim.y chunks): the carried values
+  // below are formed afresh at the chunk's first level k0
+  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = kts + (int)blockIdx.y * per, k1 = min(ktf, k0 + per - 1);
   // own-column window of u for the vertical flux: u(k-1 .. k+2)
-  float um1 = 0.f, u0 = u(i, kts, j), up1 = u(i, kts + 1, j), up2 = (kts + 2 <= kme) ? u(i, kts + 2, j) : 0.f;
-  float vf_lo = 0.f;  // vf(kts) = 0
+  float um1 = (k0 - 1 >= kts) ? u(i, k0 - 1, j) : 0.f, u0 = u(i, k0, j), up1 = u(i, k0 + 1, j),
+        up2 = (k0 + 2 <= kme) ? u(i, k0 + 2, j) : 0.f;
+  // vertical flux of face k0 (the same expression as at the level below)
+  float vf_lo = 0.f;
+  if ((FL & TF_ADV) && k0 <= k1) {
+    const int kk = k0;
+    if (kk == kts || kk == kte) vf_lo = 0.f;
+    else if (kk == kts + 1 || kk == ktf)
+      vf_lo = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * u0 + fzp(kk) * um1);
+    else {
+      const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
+      vf_lo = vel * flux3(u(i, kk - 2, j), um1, u0, up1, -vel);
+    }
+  }
   // pressure-gradient carries: p, ph at level k of columns i-1, i; dpn(k)
   float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f;
-  if (FL & TF_PG) {
-    p_l = p(i - 1, kts, j); p_r = p(i, kts, j);
-    ph_l = ph(i - 1, kts, j); ph_r = ph(i, kts, j);
-    if (kts == 1)
+  if ((FL & TF_PG) && k0 <= k1) {
+    p_l = p(i - 1, k0, j); p_r = p(i, k0, j);
+    ph_l = ph(i - 1, k0, j); ph_r = ph(i, k0, j);
+    if (k0 == 1)
       dpn_lo = .5f * (m.cf1 * (p(i - 1, 1, j) + p(i, 1, j)) + m.cf2 * (p(i - 1, 2, j) + p(i, 2, j)) +
                       m.cf3 * (p(i - 1, 3, j) + p(i, 3, j)));
     else
-      dpn_lo = .5f * (fzm(kts) * (p_l + p_r) + fzp(kts) * (p(i - 1, kts - 1, j) + p(i, kts - 1, j)));
+      dpn_lo = .5f * (fzm(k0) * (p_l + p_r) + fzp(k0) * (p(i - 1, k0 - 1, j) + p(i, k0 - 1, j)));
   }
   float rw_l = 0.f, rw_r = 0.f;
-  if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i - 1, kts, j); rw_r = rw(i, kts, j); }
+  if ((FL & (TF_COR | TF_CURV)) && k0 <= k1) { rw_l = rw(i - 1, k0, j); rw_r = rw(i, k0, j); }
 
-  for (int k = kts; k <= ktf; ++k) {
+  for (int k = k0; k <= k1; ++k) {
     if (k + 2 <= kme) {
       prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
       prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
@@ -155,7 +171,7 @@ __global__ void __launch_bounds__(TX* TY) k_tend_u_col(TileLaunch L) {
     tend(i, k, j) = t;
     um1 = u0; u0 = up1; up1 = up2; up2 = up3;
   }
-  if (FL & TF_ZERO)
+  if ((FL & TF_ZERO) && blockIdx.y == gridDim.y - 1)
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
@@ -206,22 +222,35 @@ __global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
     duy_r = msfuy(i + 1, j) - msfuy(i, j);
     duy_l = msfuy(i + 1, j - 1) - msfuy(i, j - 1);
   }
-  float vm1 = 0.f, v0 = v(i, kts, j), vp1 = v(i, kts + 1, j), vp2 = (kts + 2 <= kme) ? v(i, kts + 2, j) : 0.f;
+  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = kts + (int)blockIdx.y * per, k1 = min(ktf, k0 + per - 1);
+  float vm1 = (k0 - 1 >= kts) ? v(i, k0 - 1, j) : 0.f, v0 = v(i, k0, j), vp1 = v(i, k0 + 1, j),
+        vp2 = (k0 + 2 <= kme) ? v(i, k0 + 2, j) : 0.f;
   float vf_lo = 0.f;
+  if ((FL & TF_ADV) && k0 <= k1) {
+    const int kk = k0;
+    if (kk == kts || kk == kte) vf_lo = 0.f;
+    else if (kk == kts + 1 || kk == ktf)
+      vf_lo = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * v0 + fzp(kk) * vm1);
+    else {
+      const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
+      vf_lo = vel * flux3(v(i, kk - 2, j), vm1, v0, vp1, -vel);
+    }
+  }
   float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f;
-  if (FL & TF_PG) {
-    p_l = p(i, kts, j - 1); p_r = p(i, kts, j);
-    ph_l = ph(i, kts, j - 1); ph_r = ph(i, kts, j);
-    if (kts == 1)
+  if ((FL & TF_PG) && k0 <= k1) {
+    p_l = p(i, k0, j - 1); p_r = p(i, k0, j);
+    ph_l = ph(i, k0, j - 1); ph_r = ph(i, k0, j);
+    if (k0 == 1)
       dpn_lo = .5f * (m.cf1 * (p(i, 1, j - 1) + p(i, 1, j)) + m.cf2 * (p(i, 2, j - 1) + p(i, 2, j)) +
                       m.cf3 * (p(i, 3, j - 1) + p(i, 3, j)));
     else
-      dpn_lo = .5f * (fzm(kts) * (p_l + p_r) + fzp(kts) * (p(i, kts - 1, j - 1) + p(i, kts - 1, j)));
+      dpn_lo = .5f * (fzm(k0) * (p_l + p_r) + fzp(k0) * (p(i, k0 - 1, j - 1) + p(i, k0 - 1, j)));
   }
   float rw_l = 0.f, rw_r = 0.f;
-  if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i, kts, j - 1); rw_r = rw(i, kts, j); }
+  if ((FL & (TF_COR | TF_CURV)) && k0 <= k1) { rw_l = rw(i, k0, j - 1); rw_r = rw(i, k0, j); }
 
-  for (int k = kts; k <= ktf; ++k) {
+  for (int k = k0; k <= k1; ++k) {
     if (k + 2 <= kme) {
       prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
       prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
@@ -291,7 +320,7 @@ __global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
     tend(i, k, j) = t;
     vm1 = v0; v0 = vp1; vp1 = vp2; vp2 = vp3;
   }
-  if (FL & TF_ZERO)
+  if ((FL & TF_ZERO) && blockIdx.y == gridDim.y - 1)
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
@@ -464,15 +493,12 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
   }
 }
 
-#define DISPATCH_COL(KERNEL, GRID, S, FLAGS)                                                  \
-  switch (FLAGS) {                                                                            \
-    case TF_ALL: KERNEL<TF_ALL><<<GRID, dim3(TX, TY), 0, S>>>(L); break;                      \
-    case TF_ZERO | TF_ADV | TF_PG: KERNEL<TF_ZERO | TF_ADV | TF_PG><<<GRID, dim3(TX, TY), 0, S>>>(L); break; \
-    default: break;                                                                           \
-  }
-
-void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_COL(k_tend_u_col, nb, s, flags) }
-void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) { DISPATCH_COL(k_tend_v_col, nb, s, flags) }
+void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, int var) {
+  if (flags == TF_ALL) k_tend_u_col<TF_ALL><<<dim3(nb, TUNE_PARAM[TU_TENDU][var]), dim3(TX, TY), 0, s>>>(L);
+}
+void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, int var) {
+  if (flags == TF_ALL) k_tend_v_col<TF_ALL><<<dim3(nb, TUNE_PARAM[TU_TENDV][var]), dim3(TX, TY), 0, s>>>(L);
+}
 void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
   if (flags == (TF_ZERO | TF_ADV)) k_tend_t_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);
 }

@@ -42,13 +42,15 @@ enum : int {
 // the real step and keeps the fastest).  Every variant of a family computes
 // the same bits: they differ only in launch bounds (registers per thread,
 // so blocks per SM) or in how many level chunks a column kernel is split into.
-enum Tune { TU_PD = 0, TU_ADV, TU_AW, TU_AUV, TU_SUMF, TU_PREP, TU_SSF, TU_SSP, TU_CFL, TU_TENDW, NTUNE };
+enum Tune { TU_PD = 0, TU_ADV, TU_AW, TU_AUV, TU_SUMF, TU_PREP, TU_SSF, TU_SSP, TU_CFL, TU_TENDW, TU_TENDU, TU_TENDV,
+            NTUNE };
 constexpr int TUNE_MAXVAR = 4;
-constexpr int TUNE_NVAR[NTUNE] = {2, 3, 2, 3, 4, 2, 2, 4, 4, 3};
-constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 0, 0, 1, 1, 2, 2, 1};
+constexpr int TUNE_NVAR[NTUNE] = {2, 3, 2, 3, 4, 2, 2, 4, 4, 3, 3, 3};
+constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 0, 0};
 // the parameter each variant stands for (blocks per SM, or level chunks)
 constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 0, 0}, {4, 5, 6, 0}, {2, 3, 0, 0}, {1, 2, 4, 0}, {1, 2, 4, 8},
-                                                {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {4, 5, 6, 0}};
+                                                {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {4, 5, 6, 0},
+                                                {1, 2, 4, 0}, {1, 2, 4, 0}};
 
 void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_PREP]);
 void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s);
@@ -62,8 +64,8 @@ void launch_tend_t(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_zero_save(const Launch& L3, int nblocks, cudaStream_t s);
 // column forms over tiles of the staggered extents
-void launch_tend_u_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
-void launch_tend_v_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
+void launch_tend_u_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s, int var = 0);
+void launch_tend_v_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s, int var = 0);
 void launch_tend_t_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 

@@ -168,7 +168,8 @@ class Ensemble:
         return {self.L.wrfgpu_phase_name(p).decode(): (ms[p], cnt[p]) for p in range(got)}
 
     TUNE_FAMILIES = ["scalar_pd_update", "scalar_adv_update", "advance_w", "advance_uv", "sumflux_calc_p_rho",
-                     "step_prep", "small_step_finish", "small_step_prep", "cfl_check", "rk_tend_w"]
+                     "step_prep", "small_step_finish", "small_step_prep", "cfl_check", "rk_tend_w", "rk_tend_u",
+                     "rk_tend_v"]
 
     def autotune(self, rounds=2):
         """Online autotuning (advances the model rounds x 4 steps); returns tuning()."""

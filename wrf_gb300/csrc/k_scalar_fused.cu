@@ -182,7 +182,7 @@ constexpr int PD_NPL = 4;    // q, q_old, ru_m, rv_m
 constexpr int PD_FSLOT = 3;  // face planes kept for three levels
 constexpr size_t PD_SMEM =
     (size_t)PD_RING * PD_NPL * HPLANE_BYTES +
-    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 4 * PDPlanes::GN + 2 * PDPlanes::SN) + PD_RING * 8;
+    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 3 * PDPlanes::GN + 2 * PDPlanes::SN) + PD_RING * 8;
 // One thread per limiter cell of the 34 x 10 region (tile + 1), plus one
 // thread per face the cells' left / bottom faces leave out (the 10 x faces of
 // column i0 + 33 and the 34 y faces of row j0 + 9): every thread computes at
@@ -244,7 +244,6 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   float* sMUT = p; p += P::GN;
   float* sMSX = p; p += P::GN;
   float* sMSY = p; p += P::GN;
-  float* sCM = p; p += P::GN;   // c1(L) mut + c2(L) of the level being staged
   float* sSC = p; p += 2 * P::SN;
   ring.bar = (uint64_t*)p;
   ring.kts = kts;
@@ -289,27 +288,30 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     if (q < P::XH) xq = q * P::XW + (P::XW - 1);     // column i0 + TX + 1
     else yq = (P::YH - 1) * P::YW + (q - P::XH);     // row j0 + TY + 1
   }
-  // level-independent data of the faces: halo-plane offset, 2-D offset, dx
+  // level-independent data of the faces: halo-plane offset, dx, and the
+  // column masses on either side (mut of the face's two cells)
   bool xok = false, yok = false;
-  int xo = 0, xg = 0, yo = 0, yg = 0;
-  float xdx = 0.f, xdxt = 0.f, ydy = 0.f, ydyt = 0.f;
+  int xo = 0, yo = 0;
+  float xdx = 0.f, xdxt = 0.f, ydy = 0.f, ydyt = 0.f, xma = 0.f, xmb = 0.f, yma = 0.f, ymb = 0.f;
   if (xq >= 0) {
     const int r = xq / P::XW, c = xq - r * P::XW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     xok = ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1;
     xo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
-    xg = (r + 1) * P::GW + (c + 1);
+    const int xg = (r + 1) * P::GW + (c + 1);
     xdx = 2.f / (sMSY[xg] + sMSY[xg - 1]) / rdx;
     xdxt = xdx / dt;
+    xma = sMUT[xg]; xmb = sMUT[xg - 1];
   }
   if (yq >= 0) {
     const int r = yq / P::YW, c = yq - r * P::YW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     yok = ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2;
     yo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
-    yg = (r + 1) * P::GW + (c + 1);
+    const int yg = (r + 1) * P::GW + (c + 1);
     ydy = 2.f / (sMSX[yg] + sMSX[yg - P::GW]) / rdy;
     ydyt = ydy / dt;
+    yma = sMUT[yg]; ymb = sMUT[yg - P::GW];
   }
 
   // the limiter cell's vertical window
@@ -346,14 +348,23 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   const int xoc = sy * P::XW + sx, yoc = sy * P::YW + sx;  // own cell's left / bottom faces
   bool ok = true;
 
+  // One barrier per level.  Iteration Lv: faces of level Lv (face slot Lv % 3)
+  // and the z face Lv+1 of the own cell; barrier; limiter factor of level Lv
+  // (factor slot Lv & 1); divergence of level Lv-1, which reads face slot
+  // (Lv-1) % 3, the neighbours' factors of level Lv-1 (written before this
+  // barrier) and its own factor of level Lv (this thread's).  A slot is
+  // rewritten only after a later barrier that every reader of its previous
+  // level has passed: face slot (Lv+1) % 3 held level Lv-2, last read before
+  // this barrier; factor slot (Lv+1) & 1 holds level Lv-1, read before the
+  // next one; the ring slot of level Lv+3 (issued after this barrier) held
+  // level Lv, read before it.
   for (int Lv = kts; Lv <= ktf + 1; ++Lv) {
     const int slot = Lv & 1;
+    float c1k = 0.f, c2k = 0.f;
     if (Lv <= ktf) {
       if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
-      const float c1k = c1(Lv), c2k = c2(Lv);
-      for (int q = tid; q < P::GN; q += PD_THREADS) sCM[q] = c1k * sMUT[q] + c2k;
+      c1k = c1(Lv); c2k = c2(Lv);
       ok = ring.wait(Lv) && ok;
-      __syncthreads();
       const int rs = ring.slot_of(Lv);
       const float* F = ring.plane(rs, 0);
       const float* FO = ring.plane(rs, 1);
@@ -367,7 +378,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         float hi = 0.f, lo = 0.f;
         if (xok) {
           const int o = xo;
-          const float mu = 0.5f * (sCM[xg] + sCM[xg - 1]);
+          const float mu = 0.5f * ((c1k * xma + c2k) + (c1k * xmb + c2k));
           const float vel = RU[o];
           const float cr = vel * dt / xdx / mu;
           lo = mu * xdxt * flux_upwind(FO[o - 1], FO[o], cr);
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         float hi = 0.f, lo = 0.f;
         if (yok) {
           const int o = yo;
-          const float mu = 0.5f * (sCM[yg] + sCM[yg - P::GW]);
+          const float mu = 0.5f * ((c1k * yma + c2k) + (c1k * ymb + c2k));
           const float vel = RV[o];
           const float cr = vel * dt / ydy / mu;
           lo = mu * ydyt * flux_upwind(FO[o - HW], FO[o], cr);
@@ -396,7 +407,12 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         if (kk > 1 && kk < m.kde) { dz = 2.f / (rdzw(kk) + rdzw(kk - 1)); dzdt = dz / dt; }
         zface(m, c, kk, dz, dzdt, dt, ktf, &c.hz1, &c.lz1);
       }
-      __syncthreads();
+    }
+    __syncthreads();
+    if (Lv <= ktf) {
+      const int fs = Lv % PD_FSLOT;
+      const float* XH = sXH + fs * P::XN; const float* XL = sXL + fs * P::XN;
+      const float* YH = sYH + fs * P::YN; const float* YL = sYL + fs * P::YN;
       // ---- limiter factor of level Lv (advect_scalar_pd ph_low / flux_out)
       if (c.valid) {
         const float rdzwk = rdzw(Lv);
@@ -413,7 +429,6 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         sSC[slot * P::SN + so] = sc;
         sc_p1 = sc;
       }
-      __syncthreads();
     }
     // ---- divergence + update of level k = Lv - 1
     const int k = Lv - 1;

@@ -397,6 +397,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tune-rounds", type=int, default=2,
+                    help="autotuning rounds before the warm-up (0: default launch variants; profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -421,8 +423,8 @@ def run_single(args, world, rank, local, pg):
     flags = G.FLAG_MIXED if args.mixed else 0
     dom = G.Domain(case, flags=flags)
     cells = case.cells()
-    # online autotuning of the launch variants (advances the model 8 steps)
-    tuning = dom.autotune(2)
+    # online autotuning of the launch variants (advances the model 4 x rounds steps)
+    tuning = dom.autotune(args.tune_rounds) if args.tune_rounds > 0 else dom.tuning()
 
     # warm-up (also builds the CUDA graph)
     dom.step(args.warmup)

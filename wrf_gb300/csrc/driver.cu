@@ -116,7 +116,7 @@ struct Ensemble {
   int nb2 = 0, nb3 = 0, nb_sc = 0, nb_st = 0, nb_tm = 0;
   bool capturing = false;
   int capture_swaps = 0;               // species-buffer swaps in one captured step
-  int nsp_max = 0, ns_max = 0;
+  int nsp_max = 0, ns_max = 0, nlev_max = 0;
   std::vector<size_t> n3, n2, n1;      // element counts per member (padded rows)
   std::vector<size_t> ni_, nk_, nj_, pitch_;  // Fortran extents and the padded row pitch
   CUtensorMap* d_tmaps = nullptr;      // [nmem][NMAPSLOT][2]
@@ -271,6 +271,7 @@ struct Ensemble {
       M.cfl_limit = 0.f;
       nsp_max = std::max(nsp_max, M.nsp);
       ns_max = std::max(ns_max, M.ns_total);
+      nlev_max = std::max(nlev_max, M.kme - M.kms + 1);
       bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
       bss[m + 1] = bss[m] + tiles_x(M) * tiles_y(M) * M.nsp;
@@ -439,7 +440,7 @@ struct Ensemble {
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
       mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV]);
-      if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, rk_step, stream, tune[TU_PD]); }
+      if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, nlev_max, rk_step, stream, tune[TU_PD]); }
       swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi(l3, nb3, stream);
       if (rk_step < 3) {

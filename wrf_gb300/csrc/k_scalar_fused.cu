@@ -124,20 +124,24 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L
     const float* V = ring.plane(sl, 2);
     float* FX = fx_base + (k & 1) * TY * (TX + 1);
     float* FY = fy_base + (k & 1) * (TY + 1) * TX;
-    // x faces i0 .. i0+TX of rows j0 .. j0+TY-1
-    for (int q = tid; q < TY * (TX + 1); q += TX * TY) {
-      const int r = q / (TX + 1), c = q - r * (TX + 1);
-      const int o = (r + TMA_HALO) * HW + c + TMA_HALO;  // face (i0 + c, j0 + r)
+    // x faces i0 .. i0+TX of rows j0 .. j0+TY-1 and y faces j0 .. j0+TY of
+    // columns i0 .. i0+TX-1: every thread its cell's left and bottom faces;
+    // the TY right faces of the last column go to warp TY-1 and the TX top
+    // faces of the last row to warp TY-2, so no warp computes more than three
+    auto xface = [&](int r, int c) {  // face (i0 + c, j0 + r)
+      const int o = (r + TMA_HALO) * HW + c + TMA_HALO;
       const float vel = U[o];
-      FX[q] = vel * flux5(Q[o - 3], Q[o - 2], Q[o - 1], Q[o], Q[o + 1], Q[o + 2], vel);
-    }
-    // y faces j0 .. j0+TY of columns i0 .. i0+TX-1
-    for (int q = tid; q < (TY + 1) * TX; q += TX * TY) {
-      const int r = q / TX, c = q - r * TX;
+      FX[r * (TX + 1) + c] = vel * flux5(Q[o - 3], Q[o - 2], Q[o - 1], Q[o], Q[o + 1], Q[o + 2], vel);
+    };
+    auto yface = [&](int r, int c) {
       const int o = (r + TMA_HALO) * HW + c + TMA_HALO;
       const float vel = V[o];
-      FY[q] = vel * flux5(Q[o - 3 * HW], Q[o - 2 * HW], Q[o - HW], Q[o], Q[o + HW], Q[o + 2 * HW], vel);
-    }
+      FY[r * TX + c] = vel * flux5(Q[o - 3 * HW], Q[o - 2 * HW], Q[o - HW], Q[o], Q[o + HW], Q[o + 2 * HW], vel);
+    };
+    xface(ty, tx);
+    yface(ty, tx);
+    if (ty == TY - 1 && tx < TY) xface(tx, TX);
+    if (ty == TY - 2) yface(TY, tx);
     __syncthreads();
     if (own) {
       // prefetch the next level's own-column values
@@ -203,18 +207,21 @@ struct ZCell {
   float romp1;              // ww_m at face L+1
 };
 
+// Column constants of level k, staged in shared memory once per block:
+// a = {c1h, c2h, rdnw, dz}, b = {dz / dt, fnm, fnp, 0}, with
+// dz = 2 / (rdnw(k) + rdnw(k-1)) for 1 < k < kde (else 0).
+struct LevelConst { float4 a, b; };
+
 // z face kk = L+1 of a limiter cell (advect_scalar_pd's fqz, fqzl).
-__device__ __forceinline__ void zface(const Mem& m, const ZCell& c, int kk, float dz, float dzdt, float dt, int ktf,
+__device__ __forceinline__ void zface(const ZCell& c, int kk, const LevelConst& t, float dt, int kts, int kde, int ktf,
                                       float* hi, float* lo) {
-  if (kk == 1 || kk == m.kde) { *hi = 0.f; *lo = 0.f; return; }
-  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
-  F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP);
-  const float mu = 0.5f * ((c1(kk) * c.mut + c2(kk)) + (c1(kk) * c.mut + c2(kk)));
+  if (kk == 1 || kk == kde) { *hi = 0.f; *lo = 0.f; return; }
+  const float mu = 0.5f * ((t.a.x * c.mut + t.a.y) + (t.a.x * c.mut + t.a.y));
   const float vel = c.romp1;
-  const float cr = vel * dt / dz / mu;
-  const float l = mu * dzdt * flux_upwind(c.fo0, c.fop1, cr);
+  const float cr = vel * dt / t.a.w / mu;
+  const float l = mu * t.b.x * flux_upwind(c.fo0, c.fop1, cr);
   float h;
-  if (kk == m.kts + 1 || kk == ktf) h = vel * (fzm(kk) * c.fp1 + fzp(kk) * c.f0);
+  if (kk == kts + 1 || kk == ktf) h = vel * (t.b.y * c.fp1 + t.b.z * c.f0);
   else h = vel * pflux3(c.fm1, c.f0, c.fp1, c.fp2, -vel);
   *lo = l; *hi = h - l;
 }
@@ -245,6 +252,8 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   float* sMSX = p; p += P::GN;
   float* sMSY = p; p += P::GN;
   float* sSC = p; p += 2 * P::SN;
+  const int nlev = m.kme - m.kms + 1;
+  LevelConst* sLV = reinterpret_cast<LevelConst*>(p); p += 8 * nlev;  // [k - kms]
   ring.bar = (uint64_t*)p;
   ring.kts = kts;
   const CUtensorMap* maps[PD_NPL] = {tmap_of(m, m.qmap[s], BOX_HALO),
@@ -262,8 +271,18 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   F3 fld = f3p(m, m.q[s]), fold = f3p(m, m.qo[s]), out = f3p(m, m.qa[s]), rom = f3(m, WRFGPU_WW_M);
   F2 mut2 = f2(m, WRFGPU_MUTS), msx2 = f2(m, WRFGPU_MSFTX), msy2 = f2(m, WRFGPU_MSFTY);
   F2 mub2 = f2(m, WRFGPU_MUB), mu1 = f2(m, WRFGPU_MU_1), mu2 = f2(m, WRFGPU_MU_2);
-  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
   auto in_mem = [&](int ii, int jj) { return ii >= m.ims && ii <= m.ime && jj >= m.jms && jj <= m.jme; };
+  {
+    F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
+    F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP);
+    for (int q = tid; q < nlev; q += PD_THREADS) {
+      const int k = m.kms + q;
+      float dz = 0.f, dzdt = 0.f;
+      if (k > 1 && k < m.kde && k - 1 >= m.kms) { dz = 2.f / (rdzw(k) + rdzw(k - 1)); dzdt = dz / dt; }
+      sLV[q].a = make_float4(c1(k), c2(k), rdzw(k), dz);
+      sLV[q].b = make_float4(dzdt, fzm(k), fzp(k), 0.f);
+    }
+  }
 
   // 2-D planes (halo 2)
   for (int q = tid; q < P::GN; q += PD_THREADS) {
@@ -360,10 +379,11 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   // level Lv, read before it.
   for (int Lv = kts; Lv <= ktf + 1; ++Lv) {
     const int slot = Lv & 1;
-    float c1k = 0.f, c2k = 0.f;
+    float c1k = 0.f, c2k = 0.f, rdzwk = 0.f;
     if (Lv <= ktf) {
       if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
-      c1k = c1(Lv); c2k = c2(Lv);
+      const float4 tl = sLV[Lv - m.kms].a;
+      c1k = tl.x; c2k = tl.y; rdzwk = tl.z;
       ok = ring.wait(Lv) && ok;
       const int rs = ring.slot_of(Lv);
       const float* F = ring.plane(rs, 0);
@@ -401,12 +421,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         YH[yq] = hi; YL[yq] = lo;
       }
       // ---- vertical face Lv+1 of this thread's limiter cell
-      if (c.valid) {
-        const int kk = Lv + 1;
-        float dz = 0.f, dzdt = 0.f;
-        if (kk > 1 && kk < m.kde) { dz = 2.f / (rdzw(kk) + rdzw(kk - 1)); dzdt = dz / dt; }
-        zface(m, c, kk, dz, dzdt, dt, ktf, &c.hz1, &c.lz1);
-      }
+      if (c.valid) zface(c, Lv + 1, sLV[Lv + 1 - m.kms], dt, kts, m.kde, ktf, &c.hz1, &c.lz1);
     }
     __syncthreads();
     if (Lv <= ktf) {
@@ -415,7 +430,6 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
       const float* YH = sYH + fs * P::YN; const float* YL = sYL + fs * P::YN;
       // ---- limiter factor of level Lv (advect_scalar_pd ph_low / flux_out)
       if (c.valid) {
-        const float rdzwk = rdzw(Lv);
         const float hx0 = XH[xoc], hx1 = XH[xoc + 1], lx0 = XL[xoc], lx1 = XL[xoc + 1];
         const float hy0 = YH[yoc], hy1 = YH[yoc + P::YW], ly0 = YL[yoc], ly1 = YL[yoc + P::YW];
         const float mx = c.mx, my = c.my;
@@ -453,14 +467,15 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
       if (k > 1) { if (hz0 < 0.f) hz0 = lim(hz0, sc_m1); else if (hz0 > 0.f) hz0 = lim(hz0, s_own); }
       if (k + 1 < m.kde) { if (hz1 < 0.f) hz1 = lim(hz1, s_own); else if (hz1 > 0.f) hz1 = lim(hz1, sc_p1); }
       const float mx = msftx_o;
+      const float4 tk = sLV[k - m.kms].a;  // c1h, c2h, rdnw of level k
       float t = 0.f;
-      t = t - rdzw(k) * (hz1 - hz0 + lz1 - lz0);
+      t = t - tk.z * (hz1 - hz0 + lz1 - lz0);
       t = t - mx * (rdx * (hx1 - hx0 + lx1 - lx0));
       t = t - mx * (rdy * (hy1 - hy0 + ly1 - ly0));
       // rk_update_scalar (last stage: q1 = q_old)
       const float tendency = t * msfty_o;
       const float q1 = c.fom1;
-      out(i, k, j) = ((c1(k) * muold_u + c2(k)) * q1 + dt * tendency) / (c1(k) * munew_u + c2(k));
+      out(i, k, j) = ((tk.x * muold_u + tk.y) * q1 + dt * tendency) / (tk.x * munew_u + tk.y);
     }
     // ---- slide the windows to level Lv+1 (loads for the next level issued now)
     sc_m1 = sc_0; sc_0 = sc_p1;
@@ -511,15 +526,16 @@ void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cud
   else if (var == 1) k_scalar_adv_update<5><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
   else k_scalar_adv_update<6><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
 }
-void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var) {
-  static bool attr = false;
-  if (!attr) {
-    set_smem(k_scalar_pd_update<1>, PD_SMEM);
-    set_smem(k_scalar_pd_update<2>, PD_SMEM);
-    attr = true;
+void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int rk_step, cudaStream_t s, int var) {
+  static size_t attr = 0;
+  const size_t bytes = PD_SMEM + sizeof(LevelConst) * (size_t)nlev_max;
+  if (bytes > attr) {
+    set_smem(k_scalar_pd_update<1>, bytes);
+    set_smem(k_scalar_pd_update<2>, bytes);
+    attr = bytes;
   }
-  if (var == 0) k_scalar_pd_update<1><<<nblocks, PD_THREADS, PD_SMEM, s>>>(L, rk_step);
-  else k_scalar_pd_update<2><<<nblocks, PD_THREADS, PD_SMEM, s>>>(L, rk_step);
+  if (var == 0) k_scalar_pd_update<1><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
+  else k_scalar_pd_update<2><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
 }
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
   k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);

@@ -4,7 +4,11 @@
 // coriolis :3106-3215; curvature :3234-3363).
 //
 // One thread per (i, j) column of a 32 x 8 tile of the staggered extents,
-// levels kts..kte in order.  The per-point arithmetic is that of the point
+// levels kts..kte in order (or one chunk of them per block along y).  For u
+// and v, the advected field and the mass fluxes ru, rv of each level arrive
+// by TMA as halo planes, several levels ahead, and every horizontal face
+// flux is formed once, in shared memory, instead of once by each of the two
+// columns it separates.  The per-point arithmetic is that of the point
 // kernels in k_tend.cu, term for term and in the same order, with three
 // exact reuses across levels:
 //   * the vertical flux of face k+1 is the lower face of level k+1,
@@ -19,308 +23,395 @@
 
 namespace wrfgpu {
 
+// Staged planes of the advected field and the two mass fluxes: the tile plus
+// a 4-point halo, (TX + 8) x (TY + 8) from (i0 - 4, j0 - 4), TEND_RING levels
+// in flight; the x and y face fluxes of a level are formed once each into
+// shared memory (double-buffered), so one block barrier per level suffices.
+constexpr int HALO_W = TX + 2 * TMA_HALO, HALO_H = TY + 2 * TMA_HALO;
+constexpr int TEND_RING = 4;
+using HaloRing = LevelRing<3, TEND_RING, HALO_W, HALO_H>;
+constexpr int FXN = TY * (TX + 1), FYN = (TY + 1) * TX;
+constexpr size_t TEND_SMEM = HaloRing::SMEM + 2 * (FXN + FYN) * 4;
+
+// The tile's x faces (columns i0 .. i0+TX of rows j0 .. j0+TY-1) and y faces
+// (rows j0 .. j0+TY of columns i0 .. i0+TX-1) of one level: 5th-order fluxes
+// of Q with the face velocity vx(o) / vy(o), o the face's upper point in the
+// halo plane.  Each thread forms its cell's left and bottom faces; the last
+// column's right faces go to warp TY-1, the last row's top faces to warp TY-2.
+template <class VX, class VY>
+__device__ __forceinline__ void tile_faces(const float* Q, float* FX, float* FY, VX vx, VY vy, int tx, int ty) {
+  auto xface = [&](int r, int c) {
+    const int o = (r + TMA_HALO) * HALO_W + c + TMA_HALO;
+    const float vel = vx(o);
+    FX[r * (TX + 1) + c] = vel * flux5(Q[o - 3], Q[o - 2], Q[o - 1], Q[o], Q[o + 1], Q[o + 2], vel);
+  };
+  auto yface = [&](int r, int c) {
+    const int o = (r + TMA_HALO) * HALO_W + c + TMA_HALO;
+    const float vel = vy(o);
+    FY[r * TX + c] = vel * flux5(Q[o - 3 * HALO_W], Q[o - 2 * HALO_W], Q[o - HALO_W], Q[o], Q[o + HALO_W],
+                                 Q[o + 2 * HALO_W], vel);
+  };
+  xface(ty, tx);
+  yface(ty, tx);
+  if (ty == TY - 1 && tx < TY) xface(tx, TX);
+  if (ty == TY - 2) yface(TY, tx);
+}
+
+// Level chunk of this block (gridDim.y chunks of kts..ktf).
+struct Chunk { int k0, k1; };
+__device__ __forceinline__ Chunk level_chunk_of(int kts, int ktf) {
+  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = kts + (int)blockIdx.y * per;
+  return Chunk{k0, min(ktf, k0 + per - 1)};
+}
+
 // ---------------------------------------------------------------- ru_tend
-template <int FL>
-__global__ void __launch_bounds__(TX* TY) k_tend_u_col(TileLaunch L) {
+template <int FL, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_tend_u_col(TileLaunch L) {
+  static_assert(FL & TF_ADV, "the staged form includes advection");
+  extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i = tp.i0 + tx, j = tp.j0 + ty;
   const F3 tend = f3(m, WRFGPU_RU_TEND);
   const int kts = m.kts, kte = m.kte, kde = m.kde, kme = m.kme, ktf = min(kte, kde - 1);
-  const bool acc = j <= min(m.jte, m.jde - 1);
-  if (!acc) {
-    if (FL & TF_ZERO)
-      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
-    return;
-  }
-  const F3 u = f3(m, WRFGPU_U_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rw = f3(m, WRFGPU_RW),
-           rom = f3(m, WRFGPU_WW);
-  const F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
-           al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqu = f3(m, WRFGPU_CQU), v = f3(m, WRFGPU_V_2);
-  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW), c1h = f1(m, WRFGPU_C1H),
-           c2h = f1(m, WRFGPU_C2H);
-  const float rdx = m.rdx, rdy = m.rdy;
-  // column constants
-  const F2 msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY);
-  const float msfux_c = msfux(i, j), msfuy_c = msfuy(i, j);
-  const float mrdy = msfux_c * rdy, mrdx = msfux_c * rdx;
-  const float ratio = msfux_c / msfuy_c;
-  const float pgA = ratio * .5f * rdx, pgB = ratio * rdx;
-  float muu_c = 0.f, mu_l = 0.f, mu_r = 0.f;
-  if (FL & TF_PG) {
-    muu_c = f2(m, WRFGPU_MUU)(i, j);
-    mu_l = f2(m, WRFGPU_MU_2)(i - 1, j);
-    mu_r = f2(m, WRFGPU_MU_2)(i, j);
-  }
-  float corA = 0.f, corB = 0.f;
-  if (FL & TF_COR) {
-    const F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), cosa = f2(m, WRFGPU_COSA);
-    corA = ratio * 0.5f * (f(i, j) + f(i - 1, j)) * 0.25f;
-    corB = 0.5f * (e(i, j) + e(i - 1, j)) * 0.5f * (cosa(i, j) + cosa(i - 1, j)) * 0.25f;
-  }
-  float dvx_l = 0.f, dvx_r = 0.f, duy_l = 0.f, duy_r = 0.f;
-  if (FL & TF_CURV) {
-    const F2 msfvx = f2(m, WRFGPU_MSFVX);
-    dvx_r = msfvx(i, j + 1) - msfvx(i, j);
-    dvx_l = msfvx(i - 1, j + 1) - msfvx(i - 1, j);
-    duy_r = msfuy(i + 1, j) - msfuy(i, j);
-    duy_l = msfuy(i, j) - msfuy(i - 1, j);
-  }
-  // this block's chunk of levels (gridDim.y chunks): the carried values
-  // below are formed afresh at the chunk's first level k0
-  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
-  const int k0 = kts + (int)blockIdx.y * per, k1 = min(ktf, k0 + per - 1);
-  // own-column window of u for the vertical flux: u(k-1 .. k+2)
-  float um1 = (k0 - 1 >= kts) ? u(i, k0 - 1, j) : 0.f, u0 = u(i, k0, j), up1 = u(i, k0 + 1, j),
-        up2 = (k0 + 2 <= kme) ? u(i, k0 + 2, j) : 0.f;
-  // vertical flux of face k0 (the same expression as at the level below)
-  float vf_lo = 0.f;
-  if ((FL & TF_ADV) && k0 <= k1) {
-    const int kk = k0;
-    if (kk == kts || kk == kte) vf_lo = 0.f;
-    else if (kk == kts + 1 || kk == ktf)
-      vf_lo = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * u0 + fzp(kk) * um1);
-    else {
-      const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
-      vf_lo = vel * flux3(u(i, kk - 2, j), um1, u0, up1, -vel);
+  const int jacc = min(m.jte, m.jde - 1);
+  const bool inside = i <= m.ite && j <= m.jte;
+  const bool acc = inside && j <= jacc;
+  if ((FL & TF_ZERO) && inside && !acc && blockIdx.y == 0)
+    for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+  const Chunk ch = level_chunk_of(kts, ktf);
+  const int k0 = ch.k0, k1 = ch.k1;
+  if (tp.i0 <= m.ite && tp.j0 <= jacc && k0 <= k1) {  // block-uniform
+    const F3 u = f3(m, WRFGPU_U_2), rw = f3(m, WRFGPU_RW), rom = f3(m, WRFGPU_WW);
+    const F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
+             al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqu = f3(m, WRFGPU_CQU), v = f3(m, WRFGPU_V_2);
+    const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW), c1h = f1(m, WRFGPU_C1H),
+             c2h = f1(m, WRFGPU_C2H);
+    const float rdx = m.rdx, rdy = m.rdy;
+    HaloRing ring;
+    ring.init(smem, k0);
+    float* FXb = (float*)(smem + HaloRing::SMEM);
+    float* FYb = FXb + 2 * FXN;
+    const CUtensorMap* maps[3] = {tmap_of(m, WRFGPU_U_2, BOX_HALO), tmap_of(m, WRFGPU_RU, BOX_HALO),
+                                  tmap_of(m, WRFGPU_RV, BOX_HALO)};
+    const int x0 = tp.i0 - TMA_HALO - m.ims, z0 = tp.j0 - TMA_HALO - m.jms;
+    if (tid == 0) {
+      ring.init_barriers();
+      mbar_fence_init();
     }
-  }
-  // pressure-gradient carries: p, ph at level k of columns i-1, i; dpn(k)
-  float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f;
-  if ((FL & TF_PG) && k0 <= k1) {
-    p_l = p(i - 1, k0, j); p_r = p(i, k0, j);
-    ph_l = ph(i - 1, k0, j); ph_r = ph(i, k0, j);
-    if (k0 == 1)
-      dpn_lo = .5f * (m.cf1 * (p(i - 1, 1, j) + p(i, 1, j)) + m.cf2 * (p(i - 1, 2, j) + p(i, 2, j)) +
-                      m.cf3 * (p(i - 1, 3, j) + p(i, 3, j)));
-    else
-      dpn_lo = .5f * (fzm(k0) * (p_l + p_r) + fzp(k0) * (p(i - 1, k0 - 1, j) + p(i, k0 - 1, j)));
-  }
-  float rw_l = 0.f, rw_r = 0.f;
-  if ((FL & (TF_COR | TF_CURV)) && k0 <= k1) { rw_l = rw(i - 1, k0, j); rw_r = rw(i, k0, j); }
-
-  for (int k = k0; k <= k1; ++k) {
-    if (k + 2 <= kme) {
-      prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
-      prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
-      prefetch_l2(&alt(i, k + 2, j)); prefetch_l2(&al(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
-      prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqu(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
-      prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
-    }
-    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
-    const float up3 = (k + 3 <= kme) ? u(i, k + 3, j) : 0.f;
-    if (FL & TF_ADV) {
-      auto fy = [&](int jj) {
-        float vel = 0.5f * (rv(i, k, jj) + rv(i - 1, k, jj));
-        return vel * flux5(u(i, k, jj - 3), u(i, k, jj - 2), u(i, k, jj - 1), u(i, k, jj), u(i, k, jj + 1), u(i, k, jj + 2), vel);
-      };
-      t = t - mrdy * (fy(j + 1) - fy(j));
-      auto fx = [&](int ii) {
-        float vel = 0.5f * (ru(ii, k, j) + ru(ii - 1, k, j));
-        return vel * flux5(u(ii - 3, k, j), u(ii - 2, k, j), u(ii - 1, k, j), u(ii, k, j), u(ii + 1, k, j), u(ii + 2, k, j), vel);
-      };
-      t = t - mrdx * (fx(i + 1) - fx(i));
-      // vertical flux of face k+1
-      const int kk = k + 1;
-      float vf_hi;
-      if (kk == kts || kk == kte) vf_hi = 0.f;
-      else if (kk == kts + 1 || kk == ktf)
-        vf_hi = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * up1 + fzp(kk) * u0);
-      else {
-        const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
-        vf_hi = vel * flux3(um1, u0, up1, up2, -vel);
+    __syncthreads();
+    if (tid == 0)
+      for (int d = 0; d < TEND_RING - 1 && k0 + d <= k1; ++d) ring.issue(k0 + d, maps, x0, z0, m.kms);
+    // column constants
+    float mrdy = 0.f, mrdx = 0.f, ratio = 0.f, pgA = 0.f, pgB = 0.f;
+    float muu_c = 0.f, mu_l = 0.f, mu_r = 0.f, corA = 0.f, corB = 0.f;
+    float dvx_l = 0.f, dvx_r = 0.f, duy_l = 0.f, duy_r = 0.f;
+    // own-column window of u for the vertical flux u(k-1 .. k+2), the vertical
+    // flux of face k, and the pressure-gradient / rw carries (formed afresh at
+    // the chunk's first level k0, with the same expressions as one level down)
+    float um1 = 0.f, u0 = 0.f, up1 = 0.f, up2 = 0.f, vf_lo = 0.f;
+    float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f, rw_l = 0.f, rw_r = 0.f;
+    if (acc) {
+      const F2 msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY);
+      const float msfux_c = msfux(i, j), msfuy_c = msfuy(i, j);
+      mrdy = msfux_c * rdy; mrdx = msfux_c * rdx;
+      ratio = msfux_c / msfuy_c;
+      pgA = ratio * .5f * rdx; pgB = ratio * rdx;
+      if (FL & TF_PG) {
+        muu_c = f2(m, WRFGPU_MUU)(i, j);
+        mu_l = f2(m, WRFGPU_MU_2)(i - 1, j);
+        mu_r = f2(m, WRFGPU_MU_2)(i, j);
       }
-      t = t - rdzw(k) * (vf_hi - vf_lo);
-      vf_lo = vf_hi;
-    }
-    float rw_l1 = 0.f, rw_r1 = 0.f;
-    if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i - 1, k + 1, j); rw_r1 = rw(i, k + 1, j); }
-    if (FL & TF_PG) {
-      const int kk = k + 1;
-      float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
-      if (kk == kde) {
-        if (m.cf.top_lid)
-          dpn_hi = .5f * (m.cfn * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) + m.cfn1 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)));
-        else dpn_hi = 0.f;
-      } else {
-        p_l1 = p(i - 1, kk, j); p_r1 = p(i, kk, j);
-        dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+      if (FL & TF_COR) {
+        const F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), cosa = f2(m, WRFGPU_COSA);
+        corA = ratio * 0.5f * (f(i, j) + f(i - 1, j)) * 0.25f;
+        corB = 0.5f * (e(i, j) + e(i - 1, j)) * 0.5f * (cosa(i, j) + cosa(i - 1, j)) * 0.25f;
       }
-      const float ph_l1 = ph(i - 1, k + 1, j), ph_r1 = ph(i, k + 1, j);
-      float dpx = pgA * (c1h(k) * muu_c + c2h(k)) *
-                  ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i - 1, k, j)) * (p_r - p_l) +
-                   (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
-      dpx = dpx + pgB * (php(i, k, j) - php(i - 1, k, j)) *
-                      (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
-      t = t - cqu(i, k, j) * dpx;
-      dpn_lo = dpn_hi;
-      p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
-    }
-    if (FL & (TF_COR | TF_CURV)) {
-      const float rvsum = rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j);
-      const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
-      if (FL & TF_COR) t = t + corA * rvsum - corB * rwsum;
       if (FL & TF_CURV) {
-        const float vx_r = 0.5f * (u0 + u(i + 1, k, j)) * dvx_r * rdy - 0.5f * (v(i, k, j) + v(i, k, j + 1)) * duy_r * rdx;
-        const float vx_l = 0.5f * (u(i - 1, k, j) + u0) * dvx_l * rdy - 0.5f * (v(i - 1, k, j) + v(i - 1, k, j + 1)) * duy_l * rdx;
-        t = t + 0.5f * (vx_r + vx_l) * 0.25f * rvsum - u0 * RERADIUS * 0.25f * rwsum;
+        const F2 msfvx = f2(m, WRFGPU_MSFVX);
+        dvx_r = msfvx(i, j + 1) - msfvx(i, j);
+        dvx_l = msfvx(i - 1, j + 1) - msfvx(i - 1, j);
+        duy_r = msfuy(i + 1, j) - msfuy(i, j);
+        duy_l = msfuy(i, j) - msfuy(i - 1, j);
       }
+      um1 = (k0 - 1 >= kts) ? u(i, k0 - 1, j) : 0.f; u0 = u(i, k0, j); up1 = u(i, k0 + 1, j);
+      up2 = (k0 + 2 <= kme) ? u(i, k0 + 2, j) : 0.f;
+      {
+        const int kk = k0;
+        if (kk == kts || kk == kte) vf_lo = 0.f;
+        else if (kk == kts + 1 || kk == ktf)
+          vf_lo = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * u0 + fzp(kk) * um1);
+        else {
+          const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
+          vf_lo = vel * flux3(u(i, kk - 2, j), um1, u0, up1, -vel);
+        }
+      }
+      if (FL & TF_PG) {
+        p_l = p(i - 1, k0, j); p_r = p(i, k0, j);
+        ph_l = ph(i - 1, k0, j); ph_r = ph(i, k0, j);
+        if (k0 == 1)
+          dpn_lo = .5f * (m.cf1 * (p(i - 1, 1, j) + p(i, 1, j)) + m.cf2 * (p(i - 1, 2, j) + p(i, 2, j)) +
+                          m.cf3 * (p(i - 1, 3, j) + p(i, 3, j)));
+        else
+          dpn_lo = .5f * (fzm(k0) * (p_l + p_r) + fzp(k0) * (p(i - 1, k0 - 1, j) + p(i, k0 - 1, j)));
+      }
+      if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i - 1, k0, j); rw_r = rw(i, k0, j); }
     }
-    rw_l = rw_l1; rw_r = rw_r1;
-    tend(i, k, j) = t;
-    um1 = u0; u0 = up1; up1 = up2; up2 = up3;
+    const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;  // own point in the halo planes
+    bool ok = true;
+    for (int k = k0; k <= k1; ++k) {
+      ok = ring.wait(k) && ok;
+      const float* U = ring.plane(k, 0);
+      const float* RU = ring.plane(k, 1);
+      const float* RV = ring.plane(k, 2);
+      float* FX = FXb + (k & 1) * FXN;
+      float* FY = FYb + (k & 1) * FYN;
+      tile_faces(U, FX, FY, [&](int q) { return 0.5f * (RU[q] + RU[q - 1]); },
+                 [&](int q) { return 0.5f * (RV[q] + RV[q - 1]); }, tx, ty);
+      __syncthreads();
+      // the slot of level k-1, which every thread has finished with
+      if (tid == 0 && k + TEND_RING - 1 <= k1) ring.issue(k + TEND_RING - 1, maps, x0, z0, m.kms);
+      if (!acc) continue;
+      if (k + 2 <= kme) {
+        prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
+        prefetch_l2(&alt(i, k + 2, j)); prefetch_l2(&al(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
+        prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqu(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
+        prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
+      }
+      float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+      const float up3 = (k + 3 <= kme) ? u(i, k + 3, j) : 0.f;
+      t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
+      t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
+      {  // vertical flux of face k+1
+        const int kk = k + 1;
+        float vf_hi;
+        if (kk == kts || kk == kte) vf_hi = 0.f;
+        else if (kk == kts + 1 || kk == ktf)
+          vf_hi = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * up1 + fzp(kk) * u0);
+        else {
+          const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
+          vf_hi = vel * flux3(um1, u0, up1, up2, -vel);
+        }
+        t = t - rdzw(k) * (vf_hi - vf_lo);
+        vf_lo = vf_hi;
+      }
+      float rw_l1 = 0.f, rw_r1 = 0.f;
+      if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i - 1, k + 1, j); rw_r1 = rw(i, k + 1, j); }
+      if (FL & TF_PG) {
+        const int kk = k + 1;
+        float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
+        if (kk == kde) {
+          if (m.cf.top_lid)
+            dpn_hi = .5f * (m.cfn * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) +
+                            m.cfn1 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)));
+          else dpn_hi = 0.f;
+        } else {
+          p_l1 = p(i - 1, kk, j); p_r1 = p(i, kk, j);
+          dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+        }
+        const float ph_l1 = ph(i - 1, k + 1, j), ph_r1 = ph(i, k + 1, j);
+        float dpx = pgA * (c1h(k) * muu_c + c2h(k)) *
+                    ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i - 1, k, j)) * (p_r - p_l) +
+                     (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
+        dpx = dpx + pgB * (php(i, k, j) - php(i - 1, k, j)) *
+                        (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
+        t = t - cqu(i, k, j) * dpx;
+        dpn_lo = dpn_hi;
+        p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
+      }
+      if (FL & (TF_COR | TF_CURV)) {
+        const float rvsum = RV[o + HALO_W - 1] + RV[o + HALO_W] + RV[o - 1] + RV[o];
+        const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
+        if (FL & TF_COR) t = t + corA * rvsum - corB * rwsum;
+        if (FL & TF_CURV) {
+          const float vx_r = 0.5f * (u0 + U[o + 1]) * dvx_r * rdy - 0.5f * (v(i, k, j) + v(i, k, j + 1)) * duy_r * rdx;
+          const float vx_l =
+              0.5f * (U[o - 1] + u0) * dvx_l * rdy - 0.5f * (v(i - 1, k, j) + v(i - 1, k, j + 1)) * duy_l * rdx;
+          t = t + 0.5f * (vx_r + vx_l) * 0.25f * rvsum - u0 * RERADIUS * 0.25f * rwsum;
+        }
+      }
+      rw_l = rw_l1; rw_r = rw_r1;
+      tend(i, k, j) = t;
+      um1 = u0; u0 = up1; up1 = up2; up2 = up3;
+    }
+    if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
   }
-  if ((FL & TF_ZERO) && blockIdx.y == gridDim.y - 1)
+  if ((FL & TF_ZERO) && acc && blockIdx.y == gridDim.y - 1)
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
 // ---------------------------------------------------------------- rv_tend
-template <int FL>
-__global__ void __launch_bounds__(TX* TY) k_tend_v_col(TileLaunch L) {
+template <int FL, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_tend_v_col(TileLaunch L) {
+  static_assert(FL & TF_ADV, "the staged form includes advection");
+  extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i = tp.i0 + tx, j = tp.j0 + ty;
   const F3 tend = f3(m, WRFGPU_RV_TEND);
   const int kts = m.kts, kte = m.kte, kde = m.kde, kme = m.kme, ktf = min(kte, kde - 1);
-  const bool acc = i <= min(m.ite, m.ide - 1);
-  if (!acc) {
-    if (FL & TF_ZERO)
-      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
-    return;
-  }
-  const F3 v = f3(m, WRFGPU_V_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rw = f3(m, WRFGPU_RW),
-           rom = f3(m, WRFGPU_WW);
-  const F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
-           al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqv = f3(m, WRFGPU_CQV), u = f3(m, WRFGPU_U_2);
-  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW), c1h = f1(m, WRFGPU_C1H),
-           c2h = f1(m, WRFGPU_C2H);
-  const float rdx = m.rdx, rdy = m.rdy;
-  const F2 msfvx = f2(m, WRFGPU_MSFVX), msfvy = f2(m, WRFGPU_MSFVY);
-  const float msfvy_c = msfvy(i, j), msfvx_c = msfvx(i, j);
-  const float mrdy = msfvy_c * rdy, mrdx = msfvy_c * rdx;
-  const float ratio = msfvy_c / msfvx_c;
-  const float pgA = ratio * .5f * rdy, pgB = ratio * rdy;
-  float muv_c = 0.f, mu_l = 0.f, mu_r = 0.f;
-  if (FL & TF_PG) {
-    muv_c = f2(m, WRFGPU_MUV)(i, j);
-    mu_l = f2(m, WRFGPU_MU_2)(i, j - 1);
-    mu_r = f2(m, WRFGPU_MU_2)(i, j);
-  }
-  float corA = 0.f, corB = 0.f;
-  if (FL & TF_COR) {
-    const F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), sina = f2(m, WRFGPU_SINA);
-    corA = ratio * 0.5f * (f(i, j) + f(i, j - 1)) * 0.25f;
-    corB = ratio * 0.5f * (e(i, j) + e(i, j - 1)) * 0.5f * (sina(i, j) + sina(i, j - 1)) * 0.25f;
-  }
-  float dvx_r = 0.f, dvx_l = 0.f, duy_r = 0.f, duy_l = 0.f;
-  if (FL & TF_CURV) {
-    const F2 msfuy = f2(m, WRFGPU_MSFUY);
-    dvx_r = msfvx(i, j + 1) - msfvx(i, j);
-    dvx_l = msfvx(i, j) - msfvx(i, j - 1);
-    duy_r = msfuy(i + 1, j) - msfuy(i, j);
-    duy_l = msfuy(i + 1, j - 1) - msfuy(i, j - 1);
-  }
-  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
-  const int k0 = kts + (int)blockIdx.y * per, k1 = min(ktf, k0 + per - 1);
-  float vm1 = (k0 - 1 >= kts) ? v(i, k0 - 1, j) : 0.f, v0 = v(i, k0, j), vp1 = v(i, k0 + 1, j),
-        vp2 = (k0 + 2 <= kme) ? v(i, k0 + 2, j) : 0.f;
-  float vf_lo = 0.f;
-  if ((FL & TF_ADV) && k0 <= k1) {
-    const int kk = k0;
-    if (kk == kts || kk == kte) vf_lo = 0.f;
-    else if (kk == kts + 1 || kk == ktf)
-      vf_lo = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * v0 + fzp(kk) * vm1);
-    else {
-      const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
-      vf_lo = vel * flux3(v(i, kk - 2, j), vm1, v0, vp1, -vel);
+  const int iacc = min(m.ite, m.ide - 1);
+  const bool inside = i <= m.ite && j <= m.jte;
+  const bool acc = inside && i <= iacc;
+  if ((FL & TF_ZERO) && inside && !acc && blockIdx.y == 0)
+    for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+  const Chunk ch = level_chunk_of(kts, ktf);
+  const int k0 = ch.k0, k1 = ch.k1;
+  if (tp.i0 <= iacc && tp.j0 <= m.jte && k0 <= k1) {  // block-uniform
+    const F3 v = f3(m, WRFGPU_V_2), rw = f3(m, WRFGPU_RW), rom = f3(m, WRFGPU_WW);
+    const F3 ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT), p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB),
+             al = f3(m, WRFGPU_AL), php = f3(m, WRFGPU_PHP), cqv = f3(m, WRFGPU_CQV), u = f3(m, WRFGPU_U_2);
+    const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW), c1h = f1(m, WRFGPU_C1H),
+             c2h = f1(m, WRFGPU_C2H);
+    const float rdx = m.rdx, rdy = m.rdy;
+    HaloRing ring;
+    ring.init(smem, k0);
+    float* FXb = (float*)(smem + HaloRing::SMEM);
+    float* FYb = FXb + 2 * FXN;
+    const CUtensorMap* maps[3] = {tmap_of(m, WRFGPU_V_2, BOX_HALO), tmap_of(m, WRFGPU_RU, BOX_HALO),
+                                  tmap_of(m, WRFGPU_RV, BOX_HALO)};
+    const int x0 = tp.i0 - TMA_HALO - m.ims, z0 = tp.j0 - TMA_HALO - m.jms;
+    if (tid == 0) {
+      ring.init_barriers();
+      mbar_fence_init();
     }
-  }
-  float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f;
-  if ((FL & TF_PG) && k0 <= k1) {
-    p_l = p(i, k0, j - 1); p_r = p(i, k0, j);
-    ph_l = ph(i, k0, j - 1); ph_r = ph(i, k0, j);
-    if (k0 == 1)
-      dpn_lo = .5f * (m.cf1 * (p(i, 1, j - 1) + p(i, 1, j)) + m.cf2 * (p(i, 2, j - 1) + p(i, 2, j)) +
-                      m.cf3 * (p(i, 3, j - 1) + p(i, 3, j)));
-    else
-      dpn_lo = .5f * (fzm(k0) * (p_l + p_r) + fzp(k0) * (p(i, k0 - 1, j - 1) + p(i, k0 - 1, j)));
-  }
-  float rw_l = 0.f, rw_r = 0.f;
-  if ((FL & (TF_COR | TF_CURV)) && k0 <= k1) { rw_l = rw(i, k0, j - 1); rw_r = rw(i, k0, j); }
-
-  for (int k = k0; k <= k1; ++k) {
-    if (k + 2 <= kme) {
-      prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
-      prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
-      prefetch_l2(&alt(i, k + 2, j)); prefetch_l2(&al(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
-      prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqv(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
-      prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
-    }
-    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
-    const float vp3 = (k + 3 <= kme) ? v(i, k + 3, j) : 0.f;
-    if (FL & TF_ADV) {
-      auto fy = [&](int jj) {
-        float vel = 0.5f * (rv(i, k, jj) + rv(i, k, jj - 1));
-        return vel * flux5(v(i, k, jj - 3), v(i, k, jj - 2), v(i, k, jj - 1), v(i, k, jj), v(i, k, jj + 1), v(i, k, jj + 2), vel);
-      };
-      t = t - mrdy * (fy(j + 1) - fy(j));
-      auto fx = [&](int ii) {
-        float vel = 0.5f * (ru(ii, k, j) + ru(ii, k, j - 1));
-        return vel * flux5(v(ii - 3, k, j), v(ii - 2, k, j), v(ii - 1, k, j), v(ii, k, j), v(ii + 1, k, j), v(ii + 2, k, j), vel);
-      };
-      t = t - mrdx * (fx(i + 1) - fx(i));
-      const int kk = k + 1;
-      float vf_hi;
-      if (kk == kts || kk == kte) vf_hi = 0.f;
-      else if (kk == kts + 1 || kk == ktf)
-        vf_hi = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * vp1 + fzp(kk) * v0);
-      else {
-        const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
-        vf_hi = vel * flux3(vm1, v0, vp1, vp2, -vel);
+    __syncthreads();
+    if (tid == 0)
+      for (int d = 0; d < TEND_RING - 1 && k0 + d <= k1; ++d) ring.issue(k0 + d, maps, x0, z0, m.kms);
+    float mrdy = 0.f, mrdx = 0.f, ratio = 0.f, pgA = 0.f, pgB = 0.f;
+    float muv_c = 0.f, mu_l = 0.f, mu_r = 0.f, corA = 0.f, corB = 0.f;
+    float dvx_l = 0.f, dvx_r = 0.f, duy_l = 0.f, duy_r = 0.f;
+    float vm1 = 0.f, v0 = 0.f, vp1 = 0.f, vp2 = 0.f, vf_lo = 0.f;
+    float p_l = 0.f, p_r = 0.f, ph_l = 0.f, ph_r = 0.f, dpn_lo = 0.f, rw_l = 0.f, rw_r = 0.f;
+    if (acc) {
+      const F2 msfvx = f2(m, WRFGPU_MSFVX), msfvy = f2(m, WRFGPU_MSFVY);
+      const float msfvy_c = msfvy(i, j), msfvx_c = msfvx(i, j);
+      mrdy = msfvy_c * rdy; mrdx = msfvy_c * rdx;
+      ratio = msfvy_c / msfvx_c;
+      pgA = ratio * .5f * rdy; pgB = ratio * rdy;
+      if (FL & TF_PG) {
+        muv_c = f2(m, WRFGPU_MUV)(i, j);
+        mu_l = f2(m, WRFGPU_MU_2)(i, j - 1);
+        mu_r = f2(m, WRFGPU_MU_2)(i, j);
       }
-      t = t - ratio * rdzw(k) * (vf_hi - vf_lo);
-      vf_lo = vf_hi;
-    }
-    float rw_l1 = 0.f, rw_r1 = 0.f;
-    if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i, k + 1, j - 1); rw_r1 = rw(i, k + 1, j); }
-    if (FL & TF_PG) {
-      const int kk = k + 1;
-      float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
-      if (kk == kde) {
-        if (m.cf.top_lid)
-          dpn_hi = .5f * (m.cfn * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) + m.cfn1 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)));
-        else dpn_hi = 0.f;
-      } else {
-        p_l1 = p(i, kk, j - 1); p_r1 = p(i, kk, j);
-        dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+      if (FL & TF_COR) {
+        const F2 f = f2(m, WRFGPU_F), e = f2(m, WRFGPU_E), sina = f2(m, WRFGPU_SINA);
+        corA = ratio * 0.5f * (f(i, j) + f(i, j - 1)) * 0.25f;
+        corB = ratio * 0.5f * (e(i, j) + e(i, j - 1)) * 0.5f * (sina(i, j) + sina(i, j - 1)) * 0.25f;
       }
-      const float ph_l1 = ph(i, k + 1, j - 1), ph_r1 = ph(i, k + 1, j);
-      float dpy = pgA * (c1h(k) * muv_c + c2h(k)) *
-                  ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i, k, j - 1)) * (p_r - p_l) +
-                   (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
-      dpy = dpy + pgB * (php(i, k, j) - php(i, k, j - 1)) *
-                      (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
-      t = t - cqv(i, k, j) * dpy;
-      dpn_lo = dpn_hi;
-      p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
-    }
-    if (FL & (TF_COR | TF_CURV)) {
-      const float rusum = ru(i, k, j) + ru(i + 1, k, j) + ru(i, k, j - 1) + ru(i + 1, k, j - 1);
-      const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
-      if (FL & TF_COR) t = t - corA * rusum + corB * rwsum;
       if (FL & TF_CURV) {
-        const float vx_r = 0.5f * (u(i, k, j) + u(i + 1, k, j)) * dvx_r * rdy - 0.5f * (v0 + v(i, k, j + 1)) * duy_r * rdx;
-        const float vx_l = 0.5f * (u(i, k, j - 1) + u(i + 1, k, j - 1)) * dvx_l * rdy - 0.5f * (v(i, k, j - 1) + v0) * duy_l * rdx;
-        t = t - 0.5f * (vx_r + vx_l) * 0.25f * rusum - ratio * v0 * RERADIUS * 0.25f * rwsum;
+        const F2 msfuy = f2(m, WRFGPU_MSFUY);
+        dvx_r = msfvx(i, j + 1) - msfvx(i, j);
+        dvx_l = msfvx(i, j) - msfvx(i, j - 1);
+        duy_r = msfuy(i + 1, j) - msfuy(i, j);
+        duy_l = msfuy(i + 1, j - 1) - msfuy(i, j - 1);
       }
+      vm1 = (k0 - 1 >= kts) ? v(i, k0 - 1, j) : 0.f; v0 = v(i, k0, j); vp1 = v(i, k0 + 1, j);
+      vp2 = (k0 + 2 <= kme) ? v(i, k0 + 2, j) : 0.f;
+      {
+        const int kk = k0;
+        if (kk == kts || kk == kte) vf_lo = 0.f;
+        else if (kk == kts + 1 || kk == ktf)
+          vf_lo = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * v0 + fzp(kk) * vm1);
+        else {
+          const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
+          vf_lo = vel * flux3(v(i, kk - 2, j), vm1, v0, vp1, -vel);
+        }
+      }
+      if (FL & TF_PG) {
+        p_l = p(i, k0, j - 1); p_r = p(i, k0, j);
+        ph_l = ph(i, k0, j - 1); ph_r = ph(i, k0, j);
+        if (k0 == 1)
+          dpn_lo = .5f * (m.cf1 * (p(i, 1, j - 1) + p(i, 1, j)) + m.cf2 * (p(i, 2, j - 1) + p(i, 2, j)) +
+                          m.cf3 * (p(i, 3, j - 1) + p(i, 3, j)));
+        else
+          dpn_lo = .5f * (fzm(k0) * (p_l + p_r) + fzp(k0) * (p(i, k0 - 1, j - 1) + p(i, k0 - 1, j)));
+      }
+      if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i, k0, j - 1); rw_r = rw(i, k0, j); }
     }
-    rw_l = rw_l1; rw_r = rw_r1;
-    tend(i, k, j) = t;
-    vm1 = v0; v0 = vp1; vp1 = vp2; vp2 = vp3;
+    const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
+    bool ok = true;
+    for (int k = k0; k <= k1; ++k) {
+      ok = ring.wait(k) && ok;
+      const float* V = ring.plane(k, 0);
+      const float* RU = ring.plane(k, 1);
+      const float* RV = ring.plane(k, 2);
+      float* FX = FXb + (k & 1) * FXN;
+      float* FY = FYb + (k & 1) * FYN;
+      tile_faces(V, FX, FY, [&](int q) { return 0.5f * (RU[q] + RU[q - HALO_W]); },
+                 [&](int q) { return 0.5f * (RV[q] + RV[q - HALO_W]); }, tx, ty);
+      __syncthreads();
+      if (tid == 0 && k + TEND_RING - 1 <= k1) ring.issue(k + TEND_RING - 1, maps, x0, z0, m.kms);
+      if (!acc) continue;
+      if (k + 2 <= kme) {
+        prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&p(i, k + 2, j)); prefetch_l2(&ph(i, k + 2, j));
+        prefetch_l2(&alt(i, k + 2, j)); prefetch_l2(&al(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
+        prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqv(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
+        prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
+      }
+      float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+      const float vp3 = (k + 3 <= kme) ? v(i, k + 3, j) : 0.f;
+      t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
+      t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
+      {
+        const int kk = k + 1;
+        float vf_hi;
+        if (kk == kts || kk == kte) vf_hi = 0.f;
+        else if (kk == kts + 1 || kk == ktf)
+          vf_hi = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * vp1 + fzp(kk) * v0);
+        else {
+          const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
+          vf_hi = vel * flux3(vm1, v0, vp1, vp2, -vel);
+        }
+        t = t - ratio * rdzw(k) * (vf_hi - vf_lo);
+        vf_lo = vf_hi;
+      }
+      float rw_l1 = 0.f, rw_r1 = 0.f;
+      if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i, k + 1, j - 1); rw_r1 = rw(i, k + 1, j); }
+      if (FL & TF_PG) {
+        const int kk = k + 1;
+        float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
+        if (kk == kde) {
+          if (m.cf.top_lid)
+            dpn_hi = .5f * (m.cfn * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) +
+                            m.cfn1 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)));
+          else dpn_hi = 0.f;
+        } else {
+          p_l1 = p(i, kk, j - 1); p_r1 = p(i, kk, j);
+          dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+        }
+        const float ph_l1 = ph(i, k + 1, j - 1), ph_r1 = ph(i, k + 1, j);
+        float dpy = pgA * (c1h(k) * muv_c + c2h(k)) *
+                    ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i, k, j - 1)) * (p_r - p_l) +
+                     (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
+        dpy = dpy + pgB * (php(i, k, j) - php(i, k, j - 1)) *
+                        (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
+        t = t - cqv(i, k, j) * dpy;
+        dpn_lo = dpn_hi;
+        p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
+      }
+      if (FL & (TF_COR | TF_CURV)) {
+        const float rusum = RU[o] + RU[o + 1] + RU[o - HALO_W] + RU[o - HALO_W + 1];
+        const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
+        if (FL & TF_COR) t = t - corA * rusum + corB * rwsum;
+        if (FL & TF_CURV) {
+          const float vx_r =
+              0.5f * (u(i, k, j) + u(i + 1, k, j)) * dvx_r * rdy - 0.5f * (v0 + V[o + HALO_W]) * duy_r * rdx;
+          const float vx_l =
+              0.5f * (u(i, k, j - 1) + u(i + 1, k, j - 1)) * dvx_l * rdy - 0.5f * (V[o - HALO_W] + v0) * duy_l * rdx;
+          t = t - 0.5f * (vx_r + vx_l) * 0.25f * rusum - ratio * v0 * RERADIUS * 0.25f * rwsum;
+        }
+      }
+      rw_l = rw_l1; rw_r = rw_r1;
+      tend(i, k, j) = t;
+      vm1 = v0; v0 = vp1; vp1 = vp2; vp2 = vp3;
+    }
+    if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
   }
-  if ((FL & TF_ZERO) && blockIdx.y == gridDim.y - 1)
+  if ((FL & TF_ZERO) && acc && blockIdx.y == gridDim.y - 1)
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
@@ -493,11 +584,14 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
   }
 }
 
+constexpr int TEND_MINB = 3;
 void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, int var) {
-  if (flags == TF_ALL) k_tend_u_col<TF_ALL><<<dim3(nb, TUNE_PARAM[TU_TENDU][var]), dim3(TX, TY), 0, s>>>(L);
+  if (flags == TF_ALL)
+    k_tend_u_col<TF_ALL, TEND_MINB><<<dim3(nb, TUNE_PARAM[TU_TENDU][var]), dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
 void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, int var) {
-  if (flags == TF_ALL) k_tend_v_col<TF_ALL><<<dim3(nb, TUNE_PARAM[TU_TENDV][var]), dim3(TX, TY), 0, s>>>(L);
+  if (flags == TF_ALL)
+    k_tend_v_col<TF_ALL, TEND_MINB><<<dim3(nb, TUNE_PARAM[TU_TENDV][var]), dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
 void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
   if (flags == (TF_ZERO | TF_ADV)) k_tend_t_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);

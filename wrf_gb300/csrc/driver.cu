@@ -398,7 +398,7 @@ struct Ensemble {
       // rk_tendency (module_em.F:370-781)
       mark(PH_TEND_U); launch_tend_u_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDU]);
       mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDV]);
-      mark(PH_TEND_W); launch_tend_w_all(l2, nb2, tune[TU_TENDW], stream);
+      mark(PH_TEND_W); launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream, tune[TU_CFL]); }

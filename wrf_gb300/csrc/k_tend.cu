@@ -212,8 +212,8 @@ __global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
 // Column kernel: pg_buoy_w overwrites cqw(k) with 1/(1+cqw(k)) after the
 // k = kde point has read the original cqw(kde-1), so each column is walked
 // in order by one thread.
-template <int FL, int MINB = 5>
-__global__ void __launch_bounds__(BX* BY, MINB) k_tend_w(Launch L) {
+template <int FL>
+__global__ void __launch_bounds__(BX* BY, 5) k_tend_w(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
@@ -473,11 +473,6 @@ __global__ void __launch_bounds__(BX* BY) k_tend_ph(Launch L) {
 void launch_tend_u(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_u, nb, dim3(BX, BY), s, flags) }
 void launch_tend_v(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_v, nb, dim3(BX, BY), s, flags) }
 void launch_tend_w(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_w, nb, dim3(BX, BY), s, flags) }
-void launch_tend_w_all(const Launch& L, int nb, int var, cudaStream_t s) {
-  if (var == 0) k_tend_w<TF_ALL, 4><<<nb, dim3(BX, BY), 0, s>>>(L);
-  else if (var == 1) k_tend_w<TF_ALL, 5><<<nb, dim3(BX, BY), 0, s>>>(L);
-  else k_tend_w<TF_ALL, 6><<<nb, dim3(BX, BY), 0, s>>>(L);
-}
 void launch_tend_t(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_t, nb, dim3(BX, BY), s, flags) }
 void launch_tend_ph(const Launch& L, int nb, int flags, cudaStream_t s) { DISPATCH_FL(k_tend_ph, nb, dim3(BX, BY), s, flags) }
 

@@ -415,21 +415,178 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_v_col(TileLaunch L) {
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
+// ---------------------------------------------------------------- rw_tend
+// advect_w (module_advect_em.F:4364-6064), pg_buoy_w, coriolis and curvature
+// (module_big_step_utilities_em.F) on the w levels.  pg_buoy_w overwrites
+// cqw(k) with 1/(1+cqw(k)) after the k = kde point has read the original
+// cqw(kde-1), so each column is walked in order by one thread (no level
+// chunks).  The face velocities interpolate ru, rv between levels k and k-1
+// (k-1 and k-2 at the top), so the ring keeps the two levels below the
+// current one: after the barrier of level k the slot of level k-3 is free.
+constexpr int W_RING = 6;
+using HaloRingW = LevelRing<3, W_RING, HALO_W, HALO_H>;
+constexpr size_t TENDW_SMEM = HaloRingW::SMEM + 2 * (FXN + FYN) * 4;
+
+template <int FL, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
+  static_assert(FL & TF_ADV, "the staged form includes advection");
+  extern __shared__ __align__(128) unsigned char smem[];
+  const TilePos tp = tile_pos(L, false, true);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i = tp.i0 + tx, j = tp.j0 + ty;
+  const F3 tend = f3(m, WRFGPU_RW_TEND);
+  const int kts = m.kts, kte = m.kte, kde = m.kde;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(kte, kde - 1);
+  const bool inside = i <= m.ite && j <= m.jte;
+  const bool acc = inside && i <= itf && j <= jtf;
+  if ((FL & TF_ZERO) && inside && !acc)
+    for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+  if (!(tp.i0 <= itf && tp.j0 <= jtf)) return;  // block-uniform
+  const F3 w = f3(m, WRFGPU_W_2), rom = f3(m, WRFGPU_WW), p = f3(m, WRFGPU_P), cqw = f3(m, WRFGPU_CQW);
+  const F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
+  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzu = f1(m, WRFGPU_RDN), rdnw = f1(m, WRFGPU_RDNW),
+           c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+  const float rdx = m.rdx, rdy = m.rdy;
+  HaloRingW ring;
+  ring.init(smem, kts);
+  float* FXb = (float*)(smem + HaloRingW::SMEM);
+  float* FYb = FXb + 2 * FXN;
+  const CUtensorMap* maps[3] = {tmap_of(m, WRFGPU_W_2, BOX_HALO), tmap_of(m, WRFGPU_RU, BOX_HALO),
+                                tmap_of(m, WRFGPU_RV, BOX_HALO)};
+  const int x0 = tp.i0 - TMA_HALO - m.ims, z0 = tp.j0 - TMA_HALO - m.jms;
+  if (tid == 0) {
+    ring.init_barriers();
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int d = 0; d < W_RING - 3 && kts + d <= kte; ++d) ring.issue(kts + d, maps, x0, z0, m.kms);
+  auto vf = [&](int kk) -> float {
+    if (kk == kts + 1 || kk == ktf + 1) return 0.25f * (rom(i, kk, j) + rom(i, kk - 1, j)) * (w(i, kk, j) + w(i, kk - 1, j));
+    float vel = 0.5f * (rom(i, kk, j) + rom(i, kk - 1, j));
+    return vel * flux3(w(i, kk - 2, j), w(i, kk - 1, j), w(i, kk, j), w(i, kk + 1, j), -vel);
+  };
+  // column constants, formed in the order of the per-level expressions
+  float mrdy = 0.f, mrdx = 0.f, rmg = 0.f, ratio = 0.f, e_c = 0.f, cosa05 = 0.f, rsina05 = 0.f, ratio05 = 0.f;
+  float muf_c = 0.f, mub_c = 0.f, cqw_top = 0.f, vf_lo = 0.f;
+  if (acc) {
+    const F2 msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
+    mrdy = msftx(i, j) * rdy; mrdx = msftx(i, j) * rdx;
+    rmg = (1.f / msfty(i, j)) * G;
+    ratio = msftx(i, j) / msfty(i, j);
+    if (FL & TF_COR) {
+      e_c = f2(m, WRFGPU_E)(i, j);
+      cosa05 = f2(m, WRFGPU_COSA)(i, j) * 0.5f;
+      rsina05 = ratio * f2(m, WRFGPU_SINA)(i, j) * 0.5f;
+    }
+    ratio05 = ratio * 0.5f;
+    if (FL & TF_PG) { muf_c = f2(m, WRFGPU_MU_2)(i, j); mub_c = f2(m, WRFGPU_MUB)(i, j); }
+    cqw_top = cqw(i, kde - 1, j);  // read before the k = kde-1 overwrite below
+    // the vertical flux of face k+1 is the lower face of level k+1
+    vf_lo = kts + 1 <= ktf + 1 ? vf(kts + 1) : 0.f;
+  }
+  // levels k-1 (and k-2) of the mass fluxes at the own point and its +i / +j
+  // neighbours, and of u, v, p, carried down the column
+  float ru0m = 0.f, ru1m = 0.f, rv0m = 0.f, rv1m = 0.f;
+  float u0m = 0.f, u1m = 0.f, v0m = 0.f, v1m = 0.f, pkm = 0.f;
+  const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
+  bool ok = true;
+  for (int k = kts; k <= kte; ++k) {
+    ok = ring.wait(k) && ok;
+    const float* Wk = ring.plane(k, 0);
+    const float* RUk = ring.plane(k, 1);
+    const float* RVk = ring.plane(k, 2);
+    float* FX = FXb + (k & 1) * FXN;
+    float* FY = FYb + (k & 1) * FYN;
+    const bool adv = k >= kts + 1 && k <= ktf + 1;  // block-uniform
+    if (adv) {
+      const float* RUm = ring.plane(k - 1, 1);
+      const float* RVm = ring.plane(k - 1, 2);
+      if (k <= ktf) {
+        const float a = fzm(k), b = fzp(k);
+        tile_faces(Wk, FX, FY, [&](int q) { return a * RUk[q] + b * RUm[q]; },
+                   [&](int q) { return a * RVk[q] + b * RVm[q]; }, tx, ty);
+      } else {
+        const float* RUmm = ring.plane(k - 2, 1);
+        const float* RVmm = ring.plane(k - 2, 2);
+        const float a = fzm(k - 1), b = fzp(k - 1);
+        tile_faces(Wk, FX, FY, [&](int q) { return (2.f - a) * RUm[q] - b * RUmm[q]; },
+                   [&](int q) { return (2.f - a) * RVm[q] - b * RVmm[q]; }, tx, ty);
+      }
+    }
+    __syncthreads();
+    if (tid == 0 && k - 3 + W_RING <= kte) ring.issue(k - 3 + W_RING, maps, x0, z0, m.kms);
+    if (!acc) continue;
+    const float ru0 = RUk[o], ru1 = RUk[o + 1], rv0 = RVk[o], rv1 = RVk[o + HALO_W];
+    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f, pk = 0.f;
+    if (FL & TF_CURV) { u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1); }
+    if (FL & TF_PG) pk = p(i, k, j);
+    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    if (adv) {
+      t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
+      t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
+      if (k <= ktf) {
+        const float vf_hi = vf(k + 1);
+        t = t - rdzu(k) * (vf_hi - vf_lo);
+        vf_lo = vf_hi;
+      } else {
+        t = t + 2.f * rdzu(k - 1) * (vf_lo);
+      }
+    }
+    if (FL & TF_PG) {
+      if (k == kde) {
+        float cq1 = 1.f / (1.f + cqw_top);
+        float cq2 = cqw_top * cq1;
+        t = t + rmg * (cq1 * 2.f * rdnw(k - 1) * (-pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
+      } else if (k >= 2) {
+        const float cqk = cqw(i, k, j);
+        float cq1 = 1.f / (1.f + cqk);
+        float cq2 = cqk * cq1;
+        cqw(i, k, j) = cq1;
+        t = t + rmg * (cq1 * rdzu(k) * (pk - pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
+      }
+    }
+    if (k >= kts + 1 && k <= ktf) {
+      if (FL & TF_COR) {
+        t = t + e_c * (cosa05 * (fzm(k) * (ru0 + ru1) + fzp(k) * (ru0m + ru1m)) -
+                       rsina05 * (fzm(k) * (rv0 + rv1) + fzp(k) * (rv0m + rv1m)));
+      }
+    }
+    if (k >= max(2, kts) && k <= ktf) {
+      if (FL & TF_CURV) {
+        t = t + RERADIUS * (0.5f * (fzm(k) * (ru0 + ru1) + fzp(k) * (ru0m + ru1m)) *
+                                0.5f * (fzm(k) * (u0 + u1) + fzp(k) * (u0m + u1m)) +
+                            ratio05 * (fzm(k) * (rv0 + rv1) + fzp(k) * (rv0m + rv1m)) *
+                                0.5f * (fzm(k) * (v0 + v1) + fzp(k) * (v0m + v1m)));
+      }
+    }
+    tend(i, k, j) = t;
+    ru0m = ru0; ru1m = ru1; rv0m = rv0; rv1m = rv1;
+    u0m = u0; u1m = u1; v0m = v0; v1m = v1;
+    pkm = pk;
+  }
+  if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
+}
+
 // ---------------------------------------------------------------- t_tend
 // advect_scalar of theta (module_advect_em.F:3394-3650, :4306-4333) plus the
 // zero_tend of the *_save arrays at the points small_step_prep leaves alone
 // (module_em.F:395-428); the vertical flux and the own-column window of
 // theta carry down the column.
-template <int FL>
-__global__ void __launch_bounds__(TX* TY, 4) k_tend_t_col(TileLaunch L) {
+template <int FL, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_tend_t_col(TileLaunch L) {
+  static_assert(FL & TF_ADV, "the staged form includes advection");
+  extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i = tp.i0 + tx, j = tp.j0 + ty;
   const F3 tend = f3(m, WRFGPU_T_TEND);
   const int kts = m.kts, kte = m.kte, kme = m.kme;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(kte, m.kde - 1);
-  if (FL & TF_ZERO) {
+  const bool inside = i <= m.ite && j <= m.jte;
+  if ((FL & TF_ZERO) && inside) {
     const bool ie = i == m.ide, je = j == m.jde;
     const F3 us = f3(m, WRFGPU_U_SAVE), vs = f3(m, WRFGPU_V_SAVE), ts = f3(m, WRFGPU_T_SAVE),
              ws = f3(m, WRFGPU_W_SAVE), phs = f3(m, WRFGPU_PH_SAVE);
@@ -442,36 +599,50 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_t_col(TileLaunch L) {
     }
     if (ie || je) f2(m, WRFGPU_MU_SAVE)(i, j) = 0.f;
   }
-  const bool acc = i <= itf && j <= jtf;
-  if (!acc) {
-    if (FL & TF_ZERO)
-      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
-    return;
-  }
-  const F3 fld = f3(m, WRFGPU_T_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rom = f3(m, WRFGPU_WW);
-  const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
-  const float msftx_c = f2(m, WRFGPU_MSFTX)(i, j);
-  const float mrdy = msftx_c * m.rdy, mrdx = msftx_c * m.rdx;
-  float fm1 = 0.f, f0 = fld(i, kts, j), fp1 = fld(i, kts + 1, j), fp2 = (kts + 2 <= kme) ? fld(i, kts + 2, j) : 0.f;
-  float vf_lo = 0.f;  // vf(kts) = 0
-  for (int k = kts; k <= ktf; ++k) {
-    if (k + 2 <= kme) {
-      prefetch_l2(&fld(i, k + 2, j)); prefetch_l2(&ru(i, k + 2, j)); prefetch_l2(&rv(i, k + 2, j));
-      prefetch_l2(&rom(i, k + 2, j));
+  const bool acc = inside && i <= itf && j <= jtf;
+  if ((FL & TF_ZERO) && inside && !acc)
+    for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+  if (tp.i0 <= itf && tp.j0 <= jtf) {  // block-uniform
+    const F3 fld = f3(m, WRFGPU_T_2), rom = f3(m, WRFGPU_WW);
+    const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
+    HaloRing ring;
+    ring.init(smem, kts);
+    float* FXb = (float*)(smem + HaloRing::SMEM);
+    float* FYb = FXb + 2 * FXN;
+    const CUtensorMap* maps[3] = {tmap_of(m, WRFGPU_T_2, BOX_HALO), tmap_of(m, WRFGPU_RU, BOX_HALO),
+                                  tmap_of(m, WRFGPU_RV, BOX_HALO)};
+    const int x0 = tp.i0 - TMA_HALO - m.ims, z0 = tp.j0 - TMA_HALO - m.jms;
+    if (tid == 0) {
+      ring.init_barriers();
+      mbar_fence_init();
     }
-    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
-    const float fp3 = (k + 3 <= kme) ? fld(i, k + 3, j) : 0.f;
-    if (FL & TF_ADV) {
-      auto fy = [&](int jj) {
-        float vel = rv(i, k, jj);
-        return vel * flux5(fld(i, k, jj - 3), fld(i, k, jj - 2), fld(i, k, jj - 1), fld(i, k, jj), fld(i, k, jj + 1), fld(i, k, jj + 2), vel);
-      };
-      t = t - mrdy * (fy(j + 1) - fy(j));
-      auto fx = [&](int ii) {
-        float vel = ru(ii, k, j);
-        return vel * flux5(fld(ii - 3, k, j), fld(ii - 2, k, j), fld(ii - 1, k, j), fld(ii, k, j), fld(ii + 1, k, j), fld(ii + 2, k, j), vel);
-      };
-      t = t - mrdx * (fx(i + 1) - fx(i));
+    __syncthreads();
+    if (tid == 0)
+      for (int d = 0; d < TEND_RING - 1 && kts + d <= ktf; ++d) ring.issue(kts + d, maps, x0, z0, m.kms);
+    float mrdy = 0.f, mrdx = 0.f, fm1 = 0.f, f0 = 0.f, fp1 = 0.f, fp2 = 0.f;
+    if (acc) {
+      const float msftx_c = f2(m, WRFGPU_MSFTX)(i, j);
+      mrdy = msftx_c * m.rdy; mrdx = msftx_c * m.rdx;
+      f0 = fld(i, kts, j); fp1 = fld(i, kts + 1, j); fp2 = (kts + 2 <= kme) ? fld(i, kts + 2, j) : 0.f;
+    }
+    float vf_lo = 0.f;  // vf(kts) = 0
+    bool ok = true;
+    for (int k = kts; k <= ktf; ++k) {
+      ok = ring.wait(k) && ok;
+      const float* T = ring.plane(k, 0);
+      const float* RU = ring.plane(k, 1);
+      const float* RV = ring.plane(k, 2);
+      float* FX = FXb + (k & 1) * FXN;
+      float* FY = FYb + (k & 1) * FYN;
+      tile_faces(T, FX, FY, [&](int q) { return RU[q]; }, [&](int q) { return RV[q]; }, tx, ty);
+      __syncthreads();
+      if (tid == 0 && k + TEND_RING - 1 <= ktf) ring.issue(k + TEND_RING - 1, maps, x0, z0, m.kms);
+      if (!acc) continue;
+      if (k + 2 <= kme) { prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j)); }
+      float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+      const float fp3 = (k + 3 <= kme) ? fld(i, k + 3, j) : 0.f;
+      t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
+      t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
       const int kk = k + 1;
       float vf_hi;
       if (kk == kts || kk == kte) vf_hi = 0.f;
@@ -482,11 +653,12 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_t_col(TileLaunch L) {
       }
       t = t - rdzw(k) * (vf_hi - vf_lo);
       vf_lo = vf_hi;
+      tend(i, k, j) = t;
+      fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = fp3;
     }
-    tend(i, k, j) = t;
-    fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = fp3;
+    if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
   }
-  if (FL & TF_ZERO)
+  if ((FL & TF_ZERO) && acc)
     for (int k = ktf + 1; k <= kte; ++k) tend(i, k, j) = 0.f;
 }
 
@@ -593,8 +765,21 @@ void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, i
   if (flags == TF_ALL)
     k_tend_v_col<TF_ALL, TEND_MINB><<<dim3(nb, TUNE_PARAM[TU_TENDV][var]), dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
+void launch_tend_w_col(const TileLaunch& L, int nb, int var, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_tend_w_col<TF_ALL, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TENDW_SMEM);
+    cudaFuncSetAttribute(k_tend_w_col<TF_ALL, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TENDW_SMEM);
+    cudaFuncSetAttribute(k_tend_w_col<TF_ALL, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TENDW_SMEM);
+    attr = true;
+  }
+  const int minb = TUNE_PARAM[TU_TENDW][var];
+  if (minb == 2) k_tend_w_col<TF_ALL, 2><<<nb, dim3(TX, TY), TENDW_SMEM, s>>>(L);
+  else if (minb == 3) k_tend_w_col<TF_ALL, 3><<<nb, dim3(TX, TY), TENDW_SMEM, s>>>(L);
+  else k_tend_w_col<TF_ALL, 4><<<nb, dim3(TX, TY), TENDW_SMEM, s>>>(L);
+}
 void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
-  if (flags == (TF_ZERO | TF_ADV)) k_tend_t_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);
+  if (flags == (TF_ZERO | TF_ADV)) k_tend_t_col<TF_ZERO | TF_ADV, 4><<<nb, dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
 void launch_tend_ph_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
   if (flags == (TF_ZERO | TF_ADV)) k_tend_ph_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);

@@ -49,7 +49,7 @@ constexpr int TUNE_NVAR[NTUNE] = {2, 3, 2, 3, 4, 2, 2, 4, 4, 3, 3, 3};
 constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 0, 0};
 // the parameter each variant stands for (blocks per SM, or level chunks)
 constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 0, 0}, {4, 5, 6, 0}, {2, 3, 0, 0}, {1, 2, 4, 0}, {1, 2, 4, 8},
-                                                {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {4, 5, 6, 0},
+                                                {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {2, 3, 4, 0},
                                                 {1, 2, 4, 0}, {1, 2, 4, 0}};
 
 void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_PREP]);
@@ -59,7 +59,7 @@ void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blo
 void launch_tend_u(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_v(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_w(const Launch& L2, int nblocks, int flags, cudaStream_t s);
-void launch_tend_w_all(const Launch& L2, int nblocks, int var, cudaStream_t s);  // TF_ALL, tuned
+void launch_tend_w_col(const TileLaunch& L, int nblocks, int var, cudaStream_t s);  // TF_ALL, staggered tiles, tuned
 void launch_tend_t(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_zero_save(const Launch& L3, int nblocks, cudaStream_t s);

@@ -442,7 +442,7 @@ struct Ensemble {
       mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV]);
       if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, nlev_max, rk_step, stream, tune[TU_PD]); }
       swap_species();
-      mark(PH_CPRP); launch_calc_p_rho_phi(l3, nb3, stream);
+      mark(PH_CPRP); launch_calc_p_rho_phi_col(LTM(), nb_tm, stream, tune[TU_CPRP]);
       if (rk_step < 3) {
         JobList j;  // rk_phys_bc_dry_2 + species (solve_em.F:3240-3330)
         j.f3(WRFGPU_U_2, 'u'); j.f3(WRFGPU_V_2, 'v'); j.f3(WRFGPU_W_2, 'w'); j.f3(WRFGPU_T_2, 'p');
@@ -500,7 +500,7 @@ struct Ensemble {
   // advances exactly as it would untuned.  The graph is rebuilt afterwards.
   int autotune(int rounds) {
     static const int fam_phase[NTUNE] = {PH_PD, PH_ADVS, PH_AW, PH_AUV, PH_SUMF, PH_PREP, PH_SSF, PH_SSP, PH_CFL,
-                                         PH_TEND_W, PH_TEND_U, PH_TEND_V};
+                                         PH_TEND_W, PH_TEND_U, PH_TEND_V, PH_CPRP};
     for (int f = 0; f < NTUNE; ++f)
       for (int v = 0; v < TUNE_MAXVAR; ++v) tune_ms[f][v] = -1.f;
     for (int r = 0; r < rounds; ++r) {

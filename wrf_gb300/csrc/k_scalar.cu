@@ -262,6 +262,61 @@ __global__ void __launch_bounds__(BX* BY) k_calc_p_rho_phi(Launch L) {
   p(i, k, j) = pv * P0 - pb(i, k, j);
 }
 
+// Column form over mass tiles x level chunks (gridDim.y chunks of
+// kts..ktf): ph and phb of level k+1 carry down as level k of the next level,
+// and so does the full-level pressure above (pfu(k) is pfd(k+1), the same
+// expression), so each level reads ph and phb once.
+__global__ void __launch_bounds__(TX* TY) k_calc_p_rho_phi_col(TileLaunch L) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (!mass_pt(m, i, j)) return;
+  const int kts = m.kts, ktf = min(m.kte, m.kde - 1), kme = m.kme;
+  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = kts + (int)blockIdx.y * per, k1 = min(ktf, k0 + per - 1);
+  if (k0 > k1) return;
+  const F3 al = f3(m, WRFGPU_AL), alb = f3(m, WRFGPU_ALB), ph = f3(m, WRFGPU_PH_2), phb = f3(m, WRFGPU_PHB),
+           p = f3(m, WRFGPU_P), pb = f3(m, WRFGPU_PB), t = f3(m, WRFGPU_T_2), qv = f3p(m, m.q[0]);
+  const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), c3h = f1(m, WRFGPU_C3H), c4h = f1(m, WRFGPU_C4H),
+           c3f = f1(m, WRFGPU_C3F), c4f = f1(m, WRFGPU_C4F), rdnw = f1(m, WRFGPU_RDNW);
+  const float ptop = m.p_top;
+  const float muts_c = f2(m, WRFGPU_MUTS)(i, j), mu_c = f2(m, WRFGPU_MU_2)(i, j);
+  const bool hyps1 = m.cf.hypsometric_opt == 1, theta_m = m.cf.use_theta_m == 1;
+  float ph_lo = ph(i, k0, j), phb_lo = hyps1 ? 0.f : phb(i, k0, j);
+  float pfd = hyps1 ? 0.f : c3f(k0) * muts_c + c4f(k0) + ptop;
+  for (int k = k0; k <= k1; ++k) {
+    if (k + 3 <= kme) {
+      prefetch_l2(&ph(i, k + 3, j)); prefetch_l2(&phb(i, k + 3, j)); prefetch_l2(&alb(i, k + 2, j));
+      prefetch_l2(&t(i, k + 2, j)); prefetch_l2(&pb(i, k + 2, j));
+      if (!theta_m) prefetch_l2(&qv(i, k + 2, j));
+    }
+    const float ph_hi = ph(i, k + 1, j);
+    const float albk = alb(i, k, j);
+    float alv;
+    if (hyps1) {
+      alv = -1.f / (c1(k) * muts_c + c2(k)) * (albk * (c1(k) * mu_c) + rdnw(k) * (ph_hi - ph_lo));
+    } else {
+      const float phb_hi = phb(i, k + 1, j);
+      const float pfu = c3f(k + 1) * muts_c + c4f(k + 1) + ptop;
+      const float phm = c3h(k) * muts_c + c4h(k) + ptop;
+      alv = (ph_hi - ph_lo + phb_hi - phb_lo) / phm / wrfgpu_ff::logf_cr(pfd / pfu) - albk;
+      pfd = pfu;
+      phb_lo = phb_hi;
+    }
+    al(i, k, j) = alv;
+    float temp;
+    if (theta_m) {
+      temp = (R_D * (T0 + t(i, k, j))) / (P0 * (alv + albk));
+    } else {
+      float qvf = 1.f + (461.6f / 287.f) * qv(i, k, j);
+      temp = (R_D * (T0 + t(i, k, j)) * qvf) / (P0 * (alv + albk));
+    }
+    const float pv = wrfgpu_ff::powf_cr(temp, CPOVCV);
+    p(i, k, j) = pv * P0 - pb(i, k, j);
+    ph_lo = ph_hi;
+  }
+}
+
 // ------------------------------------------------------------ set_w_surface
 __global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
   BlockPos bp = block_pos(L);
@@ -399,6 +454,9 @@ void launch_update_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step);
 }
 void launch_calc_p_rho_phi(const Launch& L, int nb, cudaStream_t s) { k_calc_p_rho_phi<<<nb, dim3(BX, BY), 0, s>>>(L); }
+void launch_calc_p_rho_phi_col(const TileLaunch& L, int nb, cudaStream_t s, int var) {
+  k_calc_p_rho_phi_col<<<dim3(nb, TUNE_PARAM[TU_CPRP][var]), dim3(TX, TY), 0, s>>>(L);
+}
 void launch_set_w_surface(const Launch& L, int nb, cudaStream_t s) { k_set_w_surface<<<nb, dim3(BX, BY), 0, s>>>(L); }
 void launch_cfl_check(const Launch& L, int nb, cudaStream_t s) { k_cfl_check<<<nb, dim3(BX, BY), 0, s>>>(L); }
 

@@ -666,55 +666,80 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_t_col(TileLaunch L) {
 // rhs_ph (module_big_step_utilities_em.F:1365-2178, 5th/6th order branch):
 // the vertical term's wdwn(k+1) is wdwn(k) one level up, u and v of levels
 // k, k-1 carry down, the column's map factors and mass terms are read once.
+constexpr int PH_RING = 4;
+using PhRing = LevelRing<2, PH_RING, HALO_W, HALO_H>;  // ph, phb halo planes
+
 template <int FL>
 __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
+  static_assert((FL & TF_ADV) && (FL & TF_ZERO), "the staged form starts from zero and advects");
+  extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
-  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
-  if (i > m.ite || j > m.jte) return;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i = tp.i0 + tx, j = tp.j0 + ty;
   const F3 tend = f3(m, WRFGPU_PH_TEND);
   const int kts = m.kts, kte = m.kte, kde = m.kde;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1);
-  const bool acc = i <= itf && j <= jtf;
-  if (!acc || !(FL & TF_ADV)) {
-    if ((FL & TF_ZERO) && !acc)
-      for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
-    if ((FL & TF_ZERO) && acc)
-      for (int k = kts; k <= min(kte, 1); ++k) tend(i, k, j) = 0.f;
-    return;
-  }
+  const bool inside = i <= m.ite && j <= m.jte;
+  const bool acc = inside && i <= itf && j <= jtf;
+  if (inside && !acc)
+    for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
+  if (!(tp.i0 <= itf && tp.j0 <= jtf)) return;  // block-uniform
+  if (acc)
+    for (int k = kts; k <= min(kte, 1); ++k) tend(i, k, j) = 0.f;
+  const int ks = max(kts, 2);
+  if (ks > kte) return;
   const F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), ww = f3(m, WRFGPU_WW), ph = f3(m, WRFGPU_PH_2),
            phb = f3(m, WRFGPU_PHB), w = f3(m, WRFGPU_W_2);
   const F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), fnm = f1(m, WRFGPU_FNM), fnp = f1(m, WRFGPU_FNP),
            rdnw = f1(m, WRFGPU_RDNW);
+  PhRing ring;
+  ring.init(smem, ks);
+  const CUtensorMap* maps[2] = {tmap_of(m, WRFGPU_PH_2, BOX_HALO), tmap_of(m, WRFGPU_PHB, BOX_HALO)};
+  const int x0 = tp.i0 - TMA_HALO - m.ims, z0 = tp.j0 - TMA_HALO - m.jms;
+  if (tid == 0) {
+    ring.init_barriers();
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int d = 0; d < PH_RING - 1 && ks + d <= kte; ++d) ring.issue(ks + d, maps, x0, z0, m.kms);
   // column constants
-  const float mut_c = f2(m, WRFGPU_MUT)(i, j), msfty_c = f2(m, WRFGPU_MSFTY)(i, j);
-  const float muv1 = f2(m, WRFGPU_MUV)(i, j + 1), muv0 = f2(m, WRFGPU_MUV)(i, j);
-  const float muu1 = f2(m, WRFGPU_MUU)(i + 1, j), muu0 = f2(m, WRFGPU_MUU)(i, j);
-  const float mvy1 = f2(m, WRFGPU_MSFVY)(i, j + 1), mvy0 = f2(m, WRFGPU_MSFVY)(i, j);
-  const float mux1 = f2(m, WRFGPU_MSFUX)(i + 1, j), mux0 = f2(m, WRFGPU_MSFUX)(i, j);
-  const float cy4 = 0.25f * m.rdy / msfty_c, cx4 = 0.25f * m.rdx / msfty_c;
-  const float cy2 = 0.5f * m.rdy / msfty_c, cx2 = 0.5f * m.rdx / msfty_c;
+  float mut_c = 0.f, msfty_c = 0.f, muv1 = 0.f, muv0 = 0.f, muu1 = 0.f, muu0 = 0.f, mvy1 = 0.f, mvy0 = 0.f;
+  float mux1 = 0.f, mux0 = 0.f, cy4 = 0.f, cx4 = 0.f, cy2 = 0.f, cx2 = 0.f;
   const float cfn = m.cfn, cfn1 = m.cfn1;
   const bool adv2 = m.cf.phi_adv_z == 2;
-  // carried: wdwn(k) and u, v of levels k-1, k-2 at (i, i+1) / (j, j+1)
   auto wdwn = [&](int kk) {
     if (adv2) return rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
     return .5f * (ww(i, kk, j) + ww(i, kk - 1, j)) * rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
   };
-  float u0m = u(i, 1, j), u1m = u(i + 1, 1, j), v0m = v(i, 1, j), v1m = v(i, 1, j + 1);  // level k-1 = 1
-  float u0mm = 0.f, u1mm = 0.f, v0mm = 0.f, v1mm = 0.f;
-  float wd_lo = (2 <= kte - 1) ? wdwn(2) : 0.f;  // wdwn(k) at k = 2
-  for (int k = kts; k <= kte; ++k) {
+  // carried: wdwn(k) and u, v of levels k-1, k-2 at (i, i+1) / (j, j+1)
+  float u0m = 0.f, u1m = 0.f, v0m = 0.f, v1m = 0.f, u0mm = 0.f, u1mm = 0.f, v0mm = 0.f, v1mm = 0.f, wd_lo = 0.f;
+  if (acc) {
+    mut_c = f2(m, WRFGPU_MUT)(i, j); msfty_c = f2(m, WRFGPU_MSFTY)(i, j);
+    muv1 = f2(m, WRFGPU_MUV)(i, j + 1); muv0 = f2(m, WRFGPU_MUV)(i, j);
+    muu1 = f2(m, WRFGPU_MUU)(i + 1, j); muu0 = f2(m, WRFGPU_MUU)(i, j);
+    mvy1 = f2(m, WRFGPU_MSFVY)(i, j + 1); mvy0 = f2(m, WRFGPU_MSFVY)(i, j);
+    mux1 = f2(m, WRFGPU_MSFUX)(i + 1, j); mux0 = f2(m, WRFGPU_MSFUX)(i, j);
+    cy4 = 0.25f * m.rdy / msfty_c; cx4 = 0.25f * m.rdx / msfty_c;
+    cy2 = 0.5f * m.rdy / msfty_c; cx2 = 0.5f * m.rdx / msfty_c;
+    u0m = u(i, 1, j); u1m = u(i + 1, 1, j); v0m = v(i, 1, j); v1m = v(i, 1, j + 1);  // level k-1 = 1
+    wd_lo = (2 <= kte - 1) ? wdwn(2) : 0.f;  // wdwn(k) at k = 2
+  }
+  const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
+  bool ok = true;
+  for (int k = ks; k <= kte; ++k) {
+    __syncthreads();  // every thread is done with level k-1's slot
+    if (tid == 0 && k + PH_RING - 1 <= kte) ring.issue(k + PH_RING - 1, maps, x0, z0, m.kms);
+    ok = ring.wait(k) && ok;
+    if (!acc) continue;
+    const float* PH = ring.plane(k, 0);
+    const float* PHB = ring.plane(k, 1);
     if (k + 2 <= kte) {
       prefetch_l2(&ph(i, k + 2, j)); prefetch_l2(&phb(i, k + 2, j)); prefetch_l2(&u(i, k + 2, j));
       prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ww(i, k + 2, j)); prefetch_l2(&w(i, k + 2, j));
     }
-    if (k < 2) {
-      if (FL & TF_ZERO) tend(i, k, j) = 0.f;
-      continue;
-    }
-    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    float t = 0.f;
     // vertical advection of ph (:1396-1428)
     if (k <= kte - 1) {
       const float wd_hi = wdwn(k + 1);
@@ -727,33 +752,31 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
       if (k == kde) t = 0.f;
       t = t + (c1f(k) * mut_c + c2f(k)) * G * w(i, k, j) / msfty_c;
     }
-    auto S = [&](int di, int dj) {  // 6th-order centred difference of ph + phb
-      return 45.f * (ph(i + di, k, j + dj) - ph(i - di, k, j - dj)) -
-             9.f * (ph(i + 2 * di, k, j + 2 * dj) - ph(i - 2 * di, k, j - 2 * dj)) +
-             (ph(i + 3 * di, k, j + 3 * dj) - ph(i - 3 * di, k, j - 3 * dj)) +
-             45.f * (phb(i + di, k, j + dj) - phb(i - di, k, j - dj)) -
-             9.f * (phb(i + 2 * di, k, j + 2 * dj) - phb(i - 2 * di, k, j - 2 * dj)) +
-             (phb(i + 3 * di, k, j + 3 * dj) - phb(i - 3 * di, k, j - 3 * dj));
+    auto S = [&](int d) {  // 6th-order centred difference of ph + phb, stride d in the halo plane
+      return 45.f * (PH[o + d] - PH[o - d]) - 9.f * (PH[o + 2 * d] - PH[o - 2 * d]) + (PH[o + 3 * d] - PH[o - 3 * d]) +
+             45.f * (PHB[o + d] - PHB[o - d]) - 9.f * (PHB[o + 2 * d] - PHB[o - 2 * d]) +
+             (PHB[o + 3 * d] - PHB[o - 3 * d]);
     };
     float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f;
     if (k <= kte - 1) {
       u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1);
       t = t - cy4 * (((c1f(k) * muv1 + c2f(k)) * (v1 + v1m) * mvy1 + (c1f(k) * muv0 + c2f(k)) * (v0 + v0m) * mvy0) *
-                     (1.f / 60.f) * S(0, 1));
+                     (1.f / 60.f) * S(HALO_W));
       t = t - cx4 * (((c1f(k) * muu1 + c2f(k)) * (u1 + u1m) * mux1 + (c1f(k) * muu0 + c2f(k)) * (u0 + u0m) * mux0) *
-                     (1.f / 60.f) * S(1, 0));
+                     (1.f / 60.f) * S(1));
     } else {
       t = t - cy2 * (((c1f(k) * muv1 + c2f(k)) * (cfn * v1m + cfn1 * v1mm) * mvy1 +
                       (c1f(k) * muv0 + c2f(k)) * (cfn * v0m + cfn1 * v0mm) * mvy0) *
-                     (1.f / 60.f) * S(0, 1));
+                     (1.f / 60.f) * S(HALO_W));
       t = t - cx2 * (((c1f(k) * muu1 + c2f(k)) * (cfn * u1m + cfn1 * u1mm) * mux1 +
                       (c1f(k) * muu0 + c2f(k)) * (cfn * u0m + cfn1 * u0mm) * mux0) *
-                     (1.f / 60.f) * S(1, 0));
+                     (1.f / 60.f) * S(1));
     }
     tend(i, k, j) = t;
     u0mm = u0m; u1mm = u1m; v0mm = v0m; v1mm = v1m;
     u0m = u0; u1m = u1; v0m = v0; v1m = v1;
   }
+  if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
 }
 
 constexpr int TEND_MINB = 3;
@@ -782,7 +805,7 @@ void launch_tend_t_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
   if (flags == (TF_ZERO | TF_ADV)) k_tend_t_col<TF_ZERO | TF_ADV, 4><<<nb, dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
 void launch_tend_ph_col(const TileLaunch& L, int nb, int flags, cudaStream_t s) {
-  if (flags == (TF_ZERO | TF_ADV)) k_tend_ph_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), 0, s>>>(L);
+  if (flags == (TF_ZERO | TF_ADV)) k_tend_ph_col<TF_ZERO | TF_ADV><<<nb, dim3(TX, TY), PhRing::SMEM, s>>>(L);
 }
 
 }  // namespace wrfgpu

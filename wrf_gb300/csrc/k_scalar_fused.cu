@@ -532,10 +532,13 @@ void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int
   if (bytes > attr) {
     set_smem(k_scalar_pd_update<1>, bytes);
     set_smem(k_scalar_pd_update<2>, bytes);
+    set_smem(k_scalar_pd_update<3>, bytes);
     attr = bytes;
   }
-  if (var == 0) k_scalar_pd_update<1><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
-  else k_scalar_pd_update<2><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
+  const int minb = TUNE_PARAM[TU_PD][var];
+  if (minb == 1) k_scalar_pd_update<1><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
+  else if (minb == 2) k_scalar_pd_update<2><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
+  else k_scalar_pd_update<3><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
 }
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
   k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);

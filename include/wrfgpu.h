@@ -179,15 +179,15 @@ int wrfgpu_profile_phases(WrfGpuEnsemble* h, int nsteps, double* ms_out, int* la
 
 /* No counterpart in the reference (its tiling is fixed by the namelist).
  * Online autotuning of the launch configuration: runs rounds x 4 real large
- * steps (the model advances), trying for each of the 13 tuned kernel
+ * steps (the model advances), trying for each of the 14 tuned kernel
  * families its launch variants — blocks per SM of the column and
  * scalar-transport kernels, level chunks of the split column kernels — and
  * keeps the fastest per family for the captured step.  Every variant
  * computes the same bits.  Family order: scalar_pd_update,
  * scalar_adv_update, advance_w, advance_uv, sumflux_calc_p_rho, step_prep,
  * small_step_finish, small_step_prep, cfl_check, rk_tend_w, rk_tend_u,
- * rk_tend_v, calc_p_rho_phi. */
-#define WRFGPU_NTUNE 13
+ * rk_tend_v, calc_p_rho_phi, advance_mu_t. */
+#define WRFGPU_NTUNE 14
 int wrfgpu_autotune(WrfGpuEnsemble* h, int rounds);
 /* The chosen variant of each family, the parameter it stands for (blocks per
  * SM or chunks), and the measured ms per step of every variant

@@ -404,7 +404,7 @@ struct Ensemble {
       if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream, tune[TU_CFL]); }
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
       mark(PH_SSP); launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream, tune[TU_SSP]);
-      mark(PH_CPR0); launch_calc_p_rho(l3, nb3, StepArgs{rk_step, 0, 0, 0}, stream);
+      mark(PH_CPR0); launch_calc_p_rho_col(LTM(), nb_tm, StepArgs{rk_step, 0, 0, 0}, stream);
       mark(PH_COEFW); launch_calc_coef_w(l2, nb2, a, fp64, stream);
       {  // solve_em.F:1176-1264
         JobList j;
@@ -418,7 +418,7 @@ struct Ensemble {
       for (int it = 1; it <= nsmall_max; ++it) {
         StepArgs ai{rk_step, it, 0, 0};
         mark(PH_AUV); launch_advance_uv_col(LST(), nb_st, rk_step, it, stream, tune[TU_AUV]);
-        mark(PH_AMUT); launch_advance_mu_t_col(LTM(), nb_tm, rk_step, it, fp64, stream);
+        mark(PH_AMUT); launch_advance_mu_t_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AMUT]);
         mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AW]);
         mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream, tune[TU_SUMF]);
         JobList j;  // solve_em.F:1659-1716
@@ -432,7 +432,7 @@ struct Ensemble {
         j.f3(WRFGPU_RU_M, 'u'); j.f3(WRFGPU_RV_M, 'v'); j.f3(WRFGPU_WW_M, 'w');
         j.f2(WRFGPU_MUT, 't'); j.f2(WRFGPU_MUTS, 't');
         fill(j);
-        mark(PH_USPD); launch_update_scalar_pd(l3, nb3, a, stream);
+        mark(PH_USPD); launch_update_scalar_pd_col(LTM(), nb_tm, a, stream);
         JobList jo;
         for (int s = 0; s < nsp_max; ++s) jo.sp(s, 1, 'p');
         fill(jo);
@@ -500,7 +500,7 @@ struct Ensemble {
   // advances exactly as it would untuned.  The graph is rebuilt afterwards.
   int autotune(int rounds) {
     static const int fam_phase[NTUNE] = {PH_PD, PH_ADVS, PH_AW, PH_AUV, PH_SUMF, PH_PREP, PH_SSF, PH_SSP, PH_CFL,
-                                         PH_TEND_W, PH_TEND_U, PH_TEND_V, PH_CPRP};
+                                         PH_TEND_W, PH_TEND_U, PH_TEND_V, PH_CPRP, PH_AMUT};
     for (int f = 0; f < NTUNE; ++f)
       for (int v = 0; v < TUNE_MAXVAR; ++v) tune_ms[f][v] = -1.f;
     for (int r = 0; r < rounds; ++r) {

@@ -312,8 +312,8 @@ void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int it
 // ---------------------------------------------------------------------------
 constexpr int KCOL = 129;  // column scratch (kde <= 128)
 
-template <typename RC>
-__global__ void __launch_bounds__(TX* TY) k_advance_mu_t_col(TileLaunch L, int rk_step, int iteration) {
+template <typename RC, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L, int rk_step, int iteration) {
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
   const Stage st = stage_of(m, rk_step);
@@ -608,9 +608,18 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
   }
 }
 
-void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s) {
-  if (fp64) k_advance_mu_t_col<double><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
-  else k_advance_mu_t_col<float><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
+                             int var) {
+  const int minb = TUNE_PARAM[TU_AMUT][var];
+  if (fp64) {
+    if (minb == 2) k_advance_mu_t_col<double, 2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else if (minb == 3) k_advance_mu_t_col<double, 3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else k_advance_mu_t_col<double, 4><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  } else {
+    if (minb == 2) k_advance_mu_t_col<float, 2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else if (minb == 3) k_advance_mu_t_col<float, 3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else k_advance_mu_t_col<float, 4><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  }
 }
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
                           int var) {

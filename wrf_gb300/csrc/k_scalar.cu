@@ -43,6 +43,33 @@ __global__ void __launch_bounds__(BX* BY) k_update_scalar_pd(Launch L, int rk_st
   }
 }
 
+// Column form over mass tiles x level chunks (gridDim.y), species outermost,
+// eight levels of loads in flight.
+__global__ void __launch_bounds__(TX* TY) k_update_scalar_pd_col(TileLaunch L, int rk_step) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (!mass_pt(m, i, j)) return;
+  const int kts = m.kts, ktf = min(m.kte, m.kde - 1);
+  const int per = (ktf - kts + 1 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int k0 = kts + (int)blockIdx.y * per, k1 = min(ktf, k0 + per - 1);
+  const Stage st = stage_of(m, rk_step);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  const float muold = f2(m, WRFGPU_MU_1)(i, j) + f2(m, WRFGPU_MUB)(i, j);
+  const float munew = f2(m, WRFGPU_MU_1)(i, j) + f2(m, WRFGPU_MUB)(i, j);
+  const float tendency = 0.f;
+  for (int s = 0; s < m.nsp; ++s) {
+    int adv = s < m.n_moist ? m.cf.moist_adv_opt : m.cf.scalar_adv_opt;
+    if (adv != 1) continue;
+    F3 q = f3p(m, m.qo[s]);
+    chunked_levels<8, float>(
+        k0, k1, [&](int k, float& v) { v = q(i, k, j); },
+        [&](int k, const float& v) {
+          q(i, k, j) = ((c1(k) * muold + c2(k)) * v + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+        });
+  }
+}
+
 // ------------------------------------------------------------ advect_scalar (+ zero_tend)
 __device__ __forceinline__ bool pd_applies(const Mem& m, int species, int rk_step) {
   int adv = species < m.n_moist ? m.cf.moist_adv_opt : m.cf.scalar_adv_opt;
@@ -442,6 +469,9 @@ void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s, int var) 
 }
 void launch_update_scalar_pd(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar_pd<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+}
+void launch_update_scalar_pd_col(const TileLaunch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_update_scalar_pd_col<<<dim3(nb, 4), dim3(TX, TY), 0, s>>>(L, a.rk_step);
 }
 void launch_advect_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_advect_scalar<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags);

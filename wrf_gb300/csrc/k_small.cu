@@ -166,6 +166,42 @@ __global__ void __launch_bounds__(BX* BY) k_calc_p_rho(Launch L, int step) {
   calc_p_rho_point(m, i, k, j, step);
 }
 
+// Column form over mass tiles x level chunks: the levels of a chunk are
+// independent, so their loads go out four levels at a time; the arithmetic
+// of each point is calc_p_rho_point's.
+__global__ void __launch_bounds__(TX* TY) k_calc_p_rho_col(TileLaunch L, int step) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > min(m.ite, m.ide - 1) || j > min(m.jte, m.jde - 1)) return;
+  int c0, c1;
+  level_chunk(m.kts, min(m.kte, m.kde - 1), &c0, &c1);
+  F3 al = f3(m, WRFGPU_AL), p = f3(m, WRFGPU_P), ph = f3(m, WRFGPU_PH_2), alt = f3(m, WRFGPU_ALT),
+     t_2 = f3(m, WRFGPU_T_2), t_1 = f3(m, WRFGPU_T_SAVE), c2a = f3(m, WRFGPU_C2A), pm1 = f3(m, WRFGPU_PM1);
+  F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), rdnw = f1(m, WRFGPU_RDNW);
+  const float muij = f2(m, WRFGPU_MU_2).ro(i, j), mutij = f2(m, WRFGPU_MUTS).ro(i, j), smdiv = m.smdiv;
+  struct LP { float a, t1, t2, c2a, ph0, ph1, pm1; };
+  chunked_levels<4, LP>(
+      c0, c1,
+      [&](int k, LP& d) {
+        d.a = alt.ro(i, k, j); d.t1 = t_1.ro(i, k, j); d.t2 = t_2.ro(i, k, j); d.c2a = c2a.ro(i, k, j);
+        d.ph0 = ph.ro(i, k, j); d.ph1 = ph.ro(i, k + 1, j); d.pm1 = step == 0 ? 0.f : pm1(i, k, j);
+      },
+      [&](int k, const LP& d) {
+        const float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (d.a * (c1h(k) * muij) + rdnw(k) * (d.ph1 - d.ph0));
+        al(i, k, j) = alv;
+        float pv = d.c2a * (d.a * (d.t2 - (c1h(k) * muij) * d.t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + d.t1)) - alv);
+        if (step == 0) {
+          pm1(i, k, j) = pv;
+        } else {
+          const float ptmp = pv;
+          pv = pv + smdiv * (pv - d.pm1);
+          pm1(i, k, j) = ptmp;
+        }
+        p(i, k, j) = pv;
+      });
+}
+
 // ------------------------------------------------------------ calc_coef_w
 template <typename RC>
 __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
@@ -645,6 +681,9 @@ void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, in
 }
 void launch_calc_p_rho(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_calc_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.iteration);
+}
+void launch_calc_p_rho_col(const TileLaunch& L, int nb, StepArgs a, cudaStream_t s) {
+  k_calc_p_rho_col<<<dim3(nb, 4), dim3(TX, TY), 0, s>>>(L, a.iteration);
 }
 void launch_calc_coef_w(const Launch& L, int nb, StepArgs a, bool fp64, cudaStream_t s) {
   if (fp64) k_calc_coef_w<double><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);

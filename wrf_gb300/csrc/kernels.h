@@ -43,14 +43,14 @@ enum : int {
 // the same bits: they differ only in launch bounds (registers per thread,
 // so blocks per SM) or in how many level chunks a column kernel is split into.
 enum Tune { TU_PD = 0, TU_ADV, TU_AW, TU_AUV, TU_SUMF, TU_PREP, TU_SSF, TU_SSP, TU_CFL, TU_TENDW, TU_TENDU, TU_TENDV,
-            TU_CPRP, NTUNE };
+            TU_CPRP, TU_AMUT, NTUNE };
 constexpr int TUNE_MAXVAR = 4;
-constexpr int TUNE_NVAR[NTUNE] = {3, 3, 2, 3, 4, 2, 2, 4, 4, 3, 3, 3, 4};
-constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 0, 0, 2};
+constexpr int TUNE_NVAR[NTUNE] = {3, 3, 2, 3, 4, 2, 2, 4, 4, 3, 3, 3, 4, 3};
+constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 0, 0, 2, 0};
 // the parameter each variant stands for (blocks per SM, or level chunks)
 constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 3, 0}, {4, 5, 6, 0}, {2, 3, 0, 0}, {1, 2, 4, 0}, {1, 2, 4, 8},
                                                 {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {2, 3, 4, 0},
-                                                {1, 2, 4, 0}, {1, 2, 4, 0}, {1, 2, 4, 8}};
+                                                {1, 2, 4, 0}, {1, 2, 4, 0}, {1, 2, 4, 8}, {2, 3, 4, 0}};
 
 void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_PREP]);
 void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s);
@@ -88,6 +88,8 @@ void launch_advect_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_
 void launch_advect_scalar_pd2(const Launch& L3, int nblocks, StepArgs a, float* const* d_scratch, cudaStream_t s);
 void launch_update_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
+void launch_calc_p_rho_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);        // mass tiles
+void launch_update_scalar_pd_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);  // mass tiles
 void launch_calc_p_rho_phi_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CPRP]);  // mass tiles
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_cfl_check(const Launch& L3, int nblocks, cudaStream_t s);
@@ -107,7 +109,8 @@ void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int
 void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s,
                            int var = TUNE_DEFAULT[TU_AUV]);
 // one block per tile of mass columns
-void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s);
+void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
+                             int var = TUNE_DEFAULT[TU_AMUT]);
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
                           int var = TUNE_DEFAULT[TU_AW]);
 

@@ -169,7 +169,7 @@ class Ensemble:
 
     TUNE_FAMILIES = ["scalar_pd_update", "scalar_adv_update", "advance_w", "advance_uv", "sumflux_calc_p_rho",
                      "step_prep", "small_step_finish", "small_step_prep", "cfl_check", "rk_tend_w", "rk_tend_u",
-                     "rk_tend_v", "calc_p_rho_phi"]
+                     "rk_tend_v", "calc_p_rho_phi", "advance_mu_t"]
 
     def autotune(self, rounds=2):
         """Online autotuning (advances the model rounds x 4 steps); returns tuning()."""

@@ -370,3 +370,34 @@ def test_mixed_precision_close_to_fp64(gpulib):
         em = serr(interior(case, fid, mixed.get(0, fid)), ref)
         assert em <= 1e-4, (nm, em, ep)
         assert em <= 3 * ep + 1e-7, (nm, em, ep)
+
+
+@pytest.mark.parametrize("bc", ["periodic", "symmetric_y"])
+def test_halo_fill_bitwise(gpulib, bc):
+    """The halo fill of every variable kind against the oracle's restatement
+    of set_physical_bc3d / set_physical_bc2d (periodic x; periodic or
+    symmetric y, where the normal velocity changes sign), on random fields."""
+    case = cases.small_case(nx=16, ny=12, kde=14, n_scalar=1, seed=5)
+    if bc == "symmetric_y":
+        c = case.desc.config
+        c.periodic_y = 0
+        c.symmetric_ys = 1
+        c.symmetric_ye = 1
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    rng = np.random.default_rng(3)
+    jobs = [("u_2", "u"), ("v_2", "v"), ("w_2", "w"), ("t_2", "t"), ("p", "p"), ("ph_2", "w"),
+            ("mu_2", "t"), ("muu", "u"), ("muv", "v")]
+    bad = []
+    for nm, var in jobs:
+        fid = abi.FIELD_ID[nm]
+        x = rng.standard_normal(od.get(fid).size).astype(np.float32)
+        od.set(fid, x)
+        ge.set(0, fid, x)
+        od.fill_halo(fid, var)
+        ge.fill_halo(fid, var)
+        a = interior(case, fid, ge.get(0, fid), halo=3)
+        b = interior(case, fid, od.get(fid), halo=3)
+        if max_abs(a, b) != 0.0:
+            bad.append("%s (%s): max|diff| %.3e" % (nm, var, max_abs(a, b)))
+    assert not bad, "\n".join(bad)

@@ -614,11 +614,13 @@ void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int 
   if (fp64) {
     if (minb == 2) k_advance_mu_t_col<double, 2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
     else if (minb == 3) k_advance_mu_t_col<double, 3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
-    else k_advance_mu_t_col<double, 4><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else if (minb == 4) k_advance_mu_t_col<double, 4><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else k_advance_mu_t_col<double, 5><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
   } else {
     if (minb == 2) k_advance_mu_t_col<float, 2><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
     else if (minb == 3) k_advance_mu_t_col<float, 3><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
-    else k_advance_mu_t_col<float, 4><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else if (minb == 4) k_advance_mu_t_col<float, 4><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+    else k_advance_mu_t_col<float, 5><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
   }
 }
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,

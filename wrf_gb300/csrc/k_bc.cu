@@ -18,9 +18,12 @@
 
 namespace wrfgpu {
 
+// Source index along one direction of halo index t (1-based domain extent
+// n, nper = n - 1 interior mass points).  Periodic: the image one period
+// away (|halo| <= 5 < nper, so one conditional add replaces the modulo).
 __device__ __forceinline__ int bc_src(int t, int n, bool stag, bool periodic, bool normal_flip, bool* neg) {
   const int nper = n - 1;
-  if (periodic) return ((t - 1) % nper + nper) % nper + 1;
+  if (periodic) return t < 1 ? t + nper : (t > nper ? t - nper : t);
   if (!stag) {
     if (t < 1) return 1 - t;                  // dat(ids-i) = dat(ids+i-1)
     if (t > nper) return 2 * nper + 1 - t;    // dat(ide+i-1) = dat(ide-i)
@@ -31,7 +34,15 @@ __device__ __forceinline__ int bc_src(int t, int n, bool stag, bool periodic, bo
   return t;
 }
 
-// grid: (blocks per job, jobs, members)
+// grid: (blocks per job, jobs, members).  Work units: for the x halo
+// (periodic x) one (level, row) segment of nxw <= 9 points per thread, for
+// the y halo one (level, halo row, 128 points of i) piece per warp, four
+// points per lane.  A unit's loads are all issued before its stores (a store
+// may alias a later load as far as the compiler knows, so copying point by
+// point would wait out one memory latency per point).  The points written by
+// the two kinds of unit are disjoint and every source point is an interior
+// point (or, without periodic x, a point no unit writes), so the units need
+// no ordering.
 __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
   const Mem& m = block_member(mems, blockIdx.z);
   const HaloJob& J = jobs.job[blockIdx.y];
@@ -49,47 +60,76 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
   const int nk = (J.kind == 3) ? (k_end - m.kts + 1) : 1;
   const bool px = m.cf.periodic_x, py = m.cf.periodic_y;
   const bool sy = m.cf.symmetric_ys && m.cf.symmetric_ye;
+  constexpr int NXW_MAX = 2 * WRFGPU_HALO + 1;
   const int nxl = WRFGPU_HALO;
   const int xr0 = m.ide, xr1 = m.ide + 4 + istag;  // periodic x only
-  const int nxr = xr1 - xr0 + 1;
+  const int nxw = nxl + (xr1 - xr0 + 1);           // <= NXW_MAX
   const int yr0 = py ? m.jde : (vs ? m.jde + 1 : m.jde);
   const int yr1 = py ? m.jde + 4 + jstag : (vs ? m.jde + 4 : m.jde + 3);
-  const int nyr = yr1 - yr0 + 1;
+  const int nyrows = WRFGPU_HALO + (yr1 - yr0 + 1);
   const int xj0 = m.jds, xj1 = m.jde + jstag;
   const int yi0 = m.ims, yi1 = us ? m.ime : m.ide + 3;
-  // 32-bit index space (a member's field holds < 2^31 points); points of a
-  // level are consecutive, i (or the x-halo column) fastest
-  const int nxw = nxl + nxr, nyi = yi1 - yi0 + 1;
-  const int nxpts = px ? nxw * (xj1 - xj0 + 1) : 0;
-  const int nypts = (py || sy) ? (WRFGPU_HALO + nyr) * nyi : 0;
-  const int npts = nxpts + nypts;
-  const int total = npts * nk;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    const int kk = t / npts;
-    const int pt = t - kk * npts;
-    const int k = kk + m.kts;
-    int ti, tj;
-    if (pt < nxpts) {
-      const int r = pt / nxw, c = pt - r * nxw;
-      tj = xj0 + r;
-      ti = c < nxl ? m.ids - nxl + c : xr0 + (c - nxl);
-    } else {
-      const int q = pt - nxpts;
-      const int r = q / nyi;
-      ti = yi0 + (q - r * nyi);
-      tj = r < WRFGPU_HALO ? m.jds - WRFGPU_HALO + r : yr0 + (r - WRFGPU_HALO);
+  const int nxj = xj1 - xj0 + 1, nyi = yi1 - yi0 + 1;
+  // 32-bit offsets of (i, k, j) / (i, j) in the field
+  const bool f3d = J.kind == 3;
+  const int sk = (int)m.sk, sj = f3d ? (int)m.sj : (int)m.s2;
+  auto off = [&](int i, int k, int j) { return (i - m.ims) + (f3d ? (k - m.kms) * sk : 0) + (j - m.jms) * sj; };
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+  if (px) {
+    const int nunits = nk * nxj;
+    for (int u = tid; u < nunits; u += nthr) {
+      const int kk = u / nxj;
+      const int tj = xj0 + (u - kk * nxj), k = kk + m.kts;
+      bool negj = false;
+      const int sjj = (py || sy) ? bc_src(tj, m.jde, vs, py, var == 'v', &negj) : tj;
+      float val[NXW_MAX];
+#pragma unroll
+      for (int c = 0; c < NXW_MAX; ++c) {
+        if (c < nxw) {
+          const int ti = c < nxl ? m.ids - nxl + c : xr0 + (c - nxl);
+          bool neg = false;
+          const int si = bc_src(ti, m.ide, us, true, false, &neg);
+          val[c] = base[off(si, k, sjj)];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NXW_MAX; ++c) {
+        if (c < nxw) {
+          const int ti = c < nxl ? m.ids - nxl + c : xr0 + (c - nxl);
+          base[off(ti, k, tj)] = negj ? -val[c] : val[c];
+        }
+      }
     }
-    bool neg = false;
-    int si = px ? bc_src(ti, m.ide, us, true, false, &neg) : ti;
-    int sj = (py || sy) ? bc_src(tj, m.jde, vs, py, var == 'v', &neg) : tj;
-    if (J.kind == 3) {
-      F3 a = f3p(m, base);
-      float val = a(si, k, sj);
-      a(ti, k, tj) = neg ? -val : val;
-    } else {
-      F2 a{base, (int)m.s2, m.ims, m.jms};
-      float val = a(si, sj);
-      a(ti, tj) = neg ? -val : val;
+  }
+  if (py || sy) {
+    constexpr int PER = 4;  // points per lane
+    const int lane = threadIdx.x & 31, warp = tid >> 5, nwarps = nthr >> 5;
+    const int npiece = (nyi + 32 * PER - 1) / (32 * PER);
+    const int nunits = nk * nyrows * npiece;
+    for (int w = warp; w < nunits; w += nwarps) {
+      const int row = w / npiece, pc = w - row * npiece;
+      const int kk = row / nyrows, r = row - kk * nyrows;
+      const int k = kk + m.kts;
+      const int tj = r < WRFGPU_HALO ? m.jds - WRFGPU_HALO + r : yr0 + (r - WRFGPU_HALO);
+      bool negj = false;
+      const int sjj = bc_src(tj, m.jde, vs, py, var == 'v', &negj);
+      float val[PER];
+      bool neg[PER];
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int ii = pc * 32 * PER + q * 32 + lane;
+        neg[q] = negj;
+        if (ii < nyi) {
+          const int ti = yi0 + ii;
+          const int si = px ? bc_src(ti, m.ide, us, true, false, &neg[q]) : ti;
+          val[q] = base[off(si, k, sjj)];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int ii = pc * 32 * PER + q * 32 + lane;
+        if (ii < nyi) base[off(yi0 + ii, k, tj)] = neg[q] ? -val[q] : val[q];
+      }
     }
   }
 }

@@ -57,7 +57,8 @@ __device__ __forceinline__ void level_chunk(int k0, int k1, int* c0, int* c1) {
   *c1 = min(k1, *c0 + per - 1);
 }
 
-__global__ void __launch_bounds__(TX* TY) k_small_step_prep_3d(TileLaunch L, int rk_step) {
+// (a minimum of three blocks per SM holds it to 63 registers, four resident blocks)
+__global__ void __launch_bounds__(TX* TY, 3) k_small_step_prep_3d(TileLaunch L, int rk_step) {
   const TilePos tp = tile_pos(L, false, true);
   const Mem& m = block_member(L.mem, tp.m);
   const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;

@@ -190,7 +190,8 @@ int wrfgpu_profile_phases(WrfGpuEnsemble* h, int nsteps, double* ms_out, int* la
 #define WRFGPU_NTUNE 14
 int wrfgpu_autotune(WrfGpuEnsemble* h, int rounds);
 /* The chosen variant of each family, the parameter it stands for (blocks per
- * SM or chunks), and the measured ms per step of every variant
+ * SM, level chunks, or 10 x blocks per SM + level chunks for advance_uv,
+ * sumflux_calc_p_rho, rk_tend_u and rk_tend_v), and the measured ms per step of every variant
  * (ms[f * 4 + v], -1 when not timed).  Returns WRFGPU_NTUNE. */
 int wrfgpu_tuning(WrfGpuEnsemble* h, int* variant, int* param, float* ms, int nfamily);
 const char* wrfgpu_phase_name(int phase);

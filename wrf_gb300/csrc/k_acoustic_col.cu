@@ -120,8 +120,11 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
   }
 }
 
+// variant parameter: 10 x blocks per SM + level chunks
 void launch_sumflux_p_rho_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s, int var) {
-  k_sumflux_p_rho_col<3><<<dim3(nblocks, TUNE_PARAM[TU_SUMF][var]), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  const int p = TUNE_PARAM[TU_SUMF][var], chunks = p % 10;
+  if (p / 10 == 4) k_sumflux_p_rho_col<4><<<dim3(nblocks, chunks), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  else k_sumflux_p_rho_col<3><<<dim3(nblocks, chunks), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
 // ---------------------------------------------------------------------------
@@ -298,8 +301,11 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_uv_col(TileLaunch L, i
   }
 }
 
+// variant parameter: 10 x blocks per SM + level chunks
 void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, cudaStream_t s, int var) {
-  k_advance_uv_col<3><<<dim3(nblocks, TUNE_PARAM[TU_AUV][var]), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  const int p = TUNE_PARAM[TU_AUV][var], chunks = p % 10;
+  if (p / 10 == 4) k_advance_uv_col<4><<<dim3(nblocks, chunks), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
+  else k_advance_uv_col<3><<<dim3(nblocks, chunks), dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
 }
 
 

@@ -779,14 +779,20 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
   if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
 }
 
-constexpr int TEND_MINB = 3;
+// variant parameter: 10 x blocks per SM + level chunks
 void launch_tend_u_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, int var) {
-  if (flags == TF_ALL)
-    k_tend_u_col<TF_ALL, TEND_MINB><<<dim3(nb, TUNE_PARAM[TU_TENDU][var]), dim3(TX, TY), TEND_SMEM, s>>>(L);
+  const int p = TUNE_PARAM[TU_TENDU][var];
+  const dim3 grid(nb, p % 10);
+  if (flags != TF_ALL) return;
+  if (p / 10 == 4) k_tend_u_col<TF_ALL, 4><<<grid, dim3(TX, TY), TEND_SMEM, s>>>(L);
+  else k_tend_u_col<TF_ALL, 3><<<grid, dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
 void launch_tend_v_col(const TileLaunch& L, int nb, int flags, cudaStream_t s, int var) {
-  if (flags == TF_ALL)
-    k_tend_v_col<TF_ALL, TEND_MINB><<<dim3(nb, TUNE_PARAM[TU_TENDV][var]), dim3(TX, TY), TEND_SMEM, s>>>(L);
+  const int p = TUNE_PARAM[TU_TENDV][var];
+  const dim3 grid(nb, p % 10);
+  if (flags != TF_ALL) return;
+  if (p / 10 == 4) k_tend_v_col<TF_ALL, 4><<<grid, dim3(TX, TY), TEND_SMEM, s>>>(L);
+  else k_tend_v_col<TF_ALL, 3><<<grid, dim3(TX, TY), TEND_SMEM, s>>>(L);
 }
 void launch_tend_w_col(const TileLaunch& L, int nb, int var, cudaStream_t s) {
   static bool attr = false;

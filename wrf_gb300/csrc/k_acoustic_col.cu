@@ -425,16 +425,19 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L,
 // memory instead, so that form stages the first 13).
 enum AwPlane { AW_T2 = 0, AW_T2A, AW_T1, AW_PH, AW_W, AW_RWT, AW_CQW, AW_C2A, AW_ALT, AW_PHT, AW_WW, AW_PH1, AW_PHB,
                AW_A, AW_AL, AW_NPLANE };
-constexpr int AW_RING = 4;  // levels L, L+1 resident, L+2, L+3 in flight
-template <typename RC> struct AwCfg {
+// Ring depth: levels L, L+1 resident and L+2, L+3 in flight; at four
+// blocks per SM (which the shared memory of four slots does not allow) only
+// L+2 is in flight.
+template <typename RC, int NSLOT> struct AwCfg {
   static constexpr int NF = sizeof(RC) == 8 ? AW_A : AW_NPLANE;
-  using Ring = TileRing<NF, AW_RING>;
+  using Ring = TileRing<NF, NSLOT>;
 };
 
 template <typename RC, int MINB>
 __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
-  using Ring = typename AwCfg<RC>::Ring;
-  constexpr int NF = AwCfg<RC>::NF;
+  constexpr int AW_RING = MINB >= 4 ? 3 : 4;
+  using Ring = typename AwCfg<RC, AW_RING>::Ring;
+  constexpr int NF = AwCfg<RC, AW_RING>::NF;
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
@@ -632,20 +635,26 @@ void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int 
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
                           int var) {
   static bool attr = false;
-  constexpr size_t S32 = AwCfg<float>::Ring::SMEM, S64 = AwCfg<double>::Ring::SMEM;
+  constexpr size_t S32 = AwCfg<float, 4>::Ring::SMEM, S64 = AwCfg<double, 4>::Ring::SMEM;
+  constexpr size_t S32_3 = AwCfg<float, 3>::Ring::SMEM, S64_3 = AwCfg<double, 3>::Ring::SMEM;
   if (!attr) {
     cudaFuncSetAttribute(k_advance_w_col<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
     cudaFuncSetAttribute(k_advance_w_col<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
+    cudaFuncSetAttribute(k_advance_w_col<float, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32_3);
     cudaFuncSetAttribute(k_advance_w_col<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
     cudaFuncSetAttribute(k_advance_w_col<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
+    cudaFuncSetAttribute(k_advance_w_col<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64_3);
     attr = true;
   }
+  const int minb = TUNE_PARAM[TU_AW][var];
   if (fp64) {
-    if (var == 0) k_advance_w_col<double, 2><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
-    else k_advance_w_col<double, 3><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+    if (minb == 2) k_advance_w_col<double, 2><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+    else if (minb == 3) k_advance_w_col<double, 3><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+    else k_advance_w_col<double, 4><<<nblocks, dim3(TX, TY), S64_3, s>>>(L, rk_step, iteration);
   } else {
-    if (var == 0) k_advance_w_col<float, 2><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
-    else k_advance_w_col<float, 3><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+    if (minb == 2) k_advance_w_col<float, 2><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+    else if (minb == 3) k_advance_w_col<float, 3><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+    else k_advance_w_col<float, 4><<<nblocks, dim3(TX, TY), S32_3, s>>>(L, rk_step, iteration);
   }
 }
 

@@ -45,11 +45,11 @@ enum : int {
 enum Tune { TU_PD = 0, TU_ADV, TU_AW, TU_AUV, TU_SUMF, TU_PREP, TU_SSF, TU_SSP, TU_CFL, TU_TENDW, TU_TENDU, TU_TENDV,
             TU_CPRP, TU_AMUT, NTUNE };
 constexpr int TUNE_MAXVAR = 4;
-constexpr int TUNE_NVAR[NTUNE] = {3, 3, 2, 4, 4, 2, 2, 4, 4, 3, 4, 4, 4, 4};
+constexpr int TUNE_NVAR[NTUNE] = {3, 3, 3, 4, 4, 2, 2, 4, 4, 3, 4, 4, 4, 4};
 constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 0, 0, 1, 1, 2, 2, 1, 0, 0, 2, 0};
 // the parameter each variant stands for: blocks per SM, level chunks, or
 // (advance_uv, sumflux, rk_tend_u, rk_tend_v) 10 x blocks per SM + level chunks
-constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 3, 0}, {4, 5, 6, 0}, {2, 3, 0, 0}, {32, 42, 34, 44}, {32, 42, 34, 44},
+constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 3, 0}, {4, 5, 6, 0}, {2, 3, 4, 0}, {32, 42, 34, 44}, {32, 42, 34, 44},
                                                 {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {2, 3, 4, 0},
                                                 {32, 42, 34, 44}, {32, 42, 34, 44}, {1, 2, 4, 8}, {2, 3, 4, 5}};
 

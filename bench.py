@@ -80,7 +80,7 @@ def alg_bytes_per_cell_step(phase, s_pd, s_all, n_acoustic=7):
 # captures summarised in profiles/ (256x256x80 case, inputs far larger than
 # L2; traffic grows with the cells processed, so it scales to other sizes).
 NCU_DRAM_BYTES_PER_CELL = {
-    "scalar_pd_update": 938.6e6 / 5177344,   # k_scalar_pd_update_c2_256x256x80.md
+    "scalar_pd_update": 941.5e6 / 5177344,   # k_scalar_pd_update_c2_256x256x80.md
     "rk_tend_v": 331.0e6 / 5177344,          # k_tend_v_col_c2_256x256x80.md
     "advance_w": 450.1e6 / 5177344,          # k_advance_w_col_c2_256x256x80.md
 }

@@ -357,7 +357,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L,
                            rdx * ((cur.u1 + (c1h(k) * muu1 + c2h(k)) * cur.uo1 / uy1) -
                                   (cur.u0 + (c1h(k) * muu0 + c2h(k)) * cur.uo0 / uy0)));
     dv[k] = d;
-    dmdt = dmdt + (RC)dnw(k) * (RC)d;
+    if constexpr (sizeof(RC) == 8) dmdt = fma((RC)dnw(k), (RC)d, dmdt);  // mixed form: one FP64 fma per level
+    else dmdt = dmdt + (RC)dnw(k) * (RC)d;
   });
   const float mu_tend = MU_TEND.ro(i, j);
   const float muave = MU(i, j);
@@ -377,6 +378,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L,
     d.u0 = u.ro(i, k, j); d.u1 = u.ro(i + 1, k, j); d.v0 = v.ro(i, k, j); d.v1 = v.ro(i, k, j + 1);
   };
   RC wwk = (RC)ww(i, 1, j);
+  // mixed form: the recursion factored into fmas, c1h (dmdt + mu_tend) + dv
+  // times dnw / my (FP64 runs at 1/64 of the FP32 rate on this part)
+  const RC dm_mt = (RC)dmdt + (RC)mu_tend;
   // final omega of level 1 (the recursion starts from the unchanged ww(1))
   float wwf_k = ww(i, 1, j) - ww_1.ro(i, 1, j);
   float wdtn_lo = 0.f;  // wdtn(1) = 0
@@ -388,8 +392,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L,
     float wwf_kp1 = 0.f;
     if (k + 1 <= k_end) {
       const int kk = k + 1, kl = kk - 1;
-      if (sizeof(RC) == 8)
-        wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(kl) * dmdt) + (RC)dv[kk - 1] + ((RC)c1h(kl) * (RC)mu_tend)) * rmy;
+      if constexpr (sizeof(RC) == 8)
+        wwk = fma(-fma((RC)c1h(kl), dm_mt, (RC)dv[kk - 1]), (RC)dnw(kk - 1) * rmy, wwk);
       else
         wwk = wwk - (RC)dnw(kk - 1) * (((RC)c1h(kl) * dmdt) + (RC)dv[kk - 1] + ((RC)c1h(kl) * (RC)mu_tend)) / (RC)my;
       wwf_kp1 = (float)wwk - nxt.ww1;

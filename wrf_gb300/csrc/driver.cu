@@ -173,7 +173,24 @@ struct Ensemble {
     if (capturing) ++capture_swaps;
   }
 
+  // Contiguous device staging buffer of the host <-> device field copies
+  // (allocated on first use, sized to the largest field): a field crosses the
+  // host link as one contiguous copy, and a kernel moves it between the
+  // caller's contiguous rows and the device's padded rows.
+  float* d_stage = nullptr;
+  size_t stage_n = 0;
+  int ensure_stage(size_t n) {
+    if (n <= stage_n) return WRFGPU_OK;
+    if (d_stage) cudaFree(d_stage);
+    d_stage = nullptr;
+    stage_n = 0;
+    if (cudaMalloc(&d_stage, n * 4) != cudaSuccess) return WRFGPU_E_CUDA;
+    stage_n = n;
+    return WRFGPU_OK;
+  }
+
   ~Ensemble() {
+    if (d_stage) cudaFree(d_stage);
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     if (pool) cudaFree(pool);
@@ -730,15 +747,19 @@ int wrfgpu_set_field_f32(WrfGpuEnsemble* h, int member, int id, const float* src
   size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
   float* p = h->e.field_ptr(member, id, &cnt, &cols, &rows, &pitch);
   if (!p || (long long)cnt != n) return WRFGPU_E_ARG;
-  if (cudaMemcpy2DAsync(p, pitch * 4, src, cols * 4, cols * 4, rows, cudaMemcpyHostToDevice, h->e.stream) != cudaSuccess)
-    return WRFGPU_E_CUDA;
   // a species' spare buffer gets the same values, so points the solver never
   // writes (halo corners, level kde) agree whichever buffer is current
-  if (float* q = h->e.spare_ptr(member, id))
-    if (cudaMemcpy2DAsync(q, pitch * 4, src, cols * 4, cols * 4, rows, cudaMemcpyHostToDevice, h->e.stream) !=
-        cudaSuccess)
-      return WRFGPU_E_CUDA;
-  if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  float* q = h->e.spare_ptr(member, id);
+  cudaStream_t s = h->e.stream;
+  if (pitch == cols) {
+    if (cudaMemcpyAsync(p, src, cnt * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return WRFGPU_E_CUDA;
+    if (q && cudaMemcpyAsync(q, p, cnt * 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return WRFGPU_E_CUDA;
+  } else {
+    if (int rc = h->e.ensure_stage(cnt)) return rc;
+    if (cudaMemcpyAsync(h->e.d_stage, src, cnt * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return WRFGPU_E_CUDA;
+    wrfgpu::launch_unpack_rows(h->e.d_stage, p, q, (int)cols, (int)rows, (int)pitch, s);
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return WRFGPU_E_CUDA;
   return WRFGPU_OK;
 }
 
@@ -747,9 +768,15 @@ int wrfgpu_get_field_f32(WrfGpuEnsemble* h, int member, int id, float* dst, long
   size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
   float* p = h->e.field_ptr(member, id, &cnt, &cols, &rows, &pitch);
   if (!p || (long long)cnt != n) return WRFGPU_E_ARG;
-  if (cudaMemcpy2DAsync(dst, cols * 4, p, pitch * 4, cols * 4, rows, cudaMemcpyDeviceToHost, h->e.stream) != cudaSuccess)
-    return WRFGPU_E_CUDA;
-  if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return WRFGPU_E_CUDA;
+  cudaStream_t s = h->e.stream;
+  if (pitch == cols) {
+    if (cudaMemcpyAsync(dst, p, cnt * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return WRFGPU_E_CUDA;
+  } else {
+    if (int rc = h->e.ensure_stage(cnt)) return rc;
+    wrfgpu::launch_pack_rows(p, h->e.d_stage, (int)cols, (int)rows, (int)pitch, s);
+    if (cudaMemcpyAsync(dst, h->e.d_stage, cnt * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return WRFGPU_E_CUDA;
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return WRFGPU_E_CUDA;
   return WRFGPU_OK;
 }
 

@@ -134,6 +134,31 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
   }
 }
 
+// Row copies between a contiguous buffer (rows of `cols` values, the
+// caller's Fortran layout) and a field's padded device rows (`pitch` apart);
+// `dst2`, when given, receives the same rows (a species' spare buffer).
+__global__ void k_unpack_rows(const float* __restrict__ src, float* __restrict__ dst, float* __restrict__ dst2,
+                              int cols, int rows, int pitch) {
+  for (int r = blockIdx.y; r < rows; r += gridDim.y)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+      const float v = src[(size_t)r * cols + c];
+      dst[(size_t)r * pitch + c] = v;
+      if (dst2) dst2[(size_t)r * pitch + c] = v;
+    }
+}
+__global__ void k_pack_rows(const float* __restrict__ src, float* __restrict__ dst, int cols, int rows, int pitch) {
+  for (int r = blockIdx.y; r < rows; r += gridDim.y)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
+      dst[(size_t)r * cols + c] = src[(size_t)r * pitch + c];
+}
+static dim3 rows_grid(int cols, int rows) { return dim3((cols + 255) / 256, rows < 65535 ? rows : 65535); }
+void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s) {
+  if (cols > 0 && rows > 0) k_unpack_rows<<<rows_grid(cols, rows), 256, 0, s>>>(src, dst, dst2, cols, rows, pitch);
+}
+void launch_pack_rows(const float* src, float* dst, int cols, int rows, int pitch, cudaStream_t s) {
+  if (cols > 0 && rows > 0) k_pack_rows<<<rows_grid(cols, rows), 256, 0, s>>>(src, dst, cols, rows, pitch);
+}
+
 void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s) {
   if (jobs.n <= 0 || nmem <= 0) return;
   k_fill_halo<<<dim3(blocks_per_job, jobs.n, nmem), 256, 0, s>>>(d_mems, jobs);

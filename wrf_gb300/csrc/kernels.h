@@ -89,6 +89,9 @@ void launch_advect_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_
 void launch_advect_scalar_pd2(const Launch& L3, int nblocks, StepArgs a, float* const* d_scratch, cudaStream_t s);
 void launch_update_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
+// host <-> device field copies through a contiguous staging buffer
+void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s);
+void launch_pack_rows(const float* src, float* dst, int cols, int rows, int pitch, cudaStream_t s);
 void launch_calc_p_rho_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);        // mass tiles
 void launch_update_scalar_pd_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);  // mass tiles
 void launch_calc_p_rho_phi_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CPRP]);  // mass tiles

@@ -34,3 +34,19 @@ WRFGPU_HD float wrfgpu_div_const(float x, float c, float zh) {
 
 WRFGPU_HD float wrfgpu_div12(float x) { return wrfgpu_div_const(x, 12.0f, 1.0f / 12.0f); }
 WRFGPU_HD float wrfgpu_div60(float x) { return wrfgpu_div_const(x, 60.0f, 1.0f / 60.0f); }
+
+/* x / c + s y / c with both quotients rounded as IEEE division (s = +1 or
+ * -1), one range test for the pair: the fast path is taken when neither
+ * numerator is below 2^-110 in magnitude or infinite (a NaN propagates
+ * through either path).  The 5th- and 3rd-order fluxes each divide two
+ * numerators by the same constant. */
+WRFGPU_HD float wrfgpu_div_const_pair(float x, float y, float s, float c, float zh) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float lo = ax < ay ? ax : ay, hi = ax < ay ? ay : ax;
+  if (!(lo >= 0x1p-110f && hi <= 3.40282347e38f)) return x / c + s * (y / c);
+  const float qx = x * zh, qy = y * zh;
+  const float rx = fmaf(-qx, c, x), ry = fmaf(-qy, c, y);
+  return fmaf(rx, zh, qx) + s * fmaf(ry, zh, qy);
+}
+WRFGPU_HD float wrfgpu_div12_add(float x, float y) { return wrfgpu_div_const_pair(x, y, 1.0f, 12.0f, 1.0f / 12.0f); }
+WRFGPU_HD float wrfgpu_div60_sub(float x, float y) { return wrfgpu_div_const_pair(x, y, -1.0f, 60.0f, 1.0f / 60.0f); }

@@ -170,14 +170,17 @@ __device__ __forceinline__ float sgn1(float a) { return copysignf(1.f, a); }
 __device__ __forceinline__ float flux4(float qm2, float qm1, float q, float qp1) {
   return wrfgpu_div12(7.f * (q + qm1) - (qp1 + qm2));
 }
+// flux4(...) + (1 sign(ua) (...)) / 12, the two quotients under one range test
 __device__ __forceinline__ float flux3(float qm2, float qm1, float q, float qp1, float ua) {
-  return flux4(qm2, qm1, q, qp1) + wrfgpu_div12(1.f * sgn1(ua) * ((qp1 - qm2) - 3.f * (q - qm1)));
+  return wrfgpu_div12_add(7.f * (q + qm1) - (qp1 + qm2), 1.f * sgn1(ua) * ((qp1 - qm2) - 3.f * (q - qm1)));
 }
 __device__ __forceinline__ float flux6(float qm3, float qm2, float qm1, float q, float qp1, float qp2) {
   return wrfgpu_div60(37.f * (q + qm1) - 8.f * (qp1 + qm2) + (qp2 + qm3));
 }
+// flux6(...) - (1 sign(ua) (...)) / 60, the two quotients under one range test
 __device__ __forceinline__ float flux5(float qm3, float qm2, float qm1, float q, float qp1, float qp2, float ua) {
-  return flux6(qm3, qm2, qm1, q, qp1, qp2) - wrfgpu_div60(1.f * sgn1(ua) * ((qp2 - qm3) - 5.f * (qp1 - qm2) + 10.f * (q - qm1)));
+  return wrfgpu_div60_sub(37.f * (q + qm1) - 8.f * (qp1 + qm2) + (qp2 + qm3),
+                          1.f * sgn1(ua) * ((qp2 - qm3) - 5.f * (qp1 - qm2) + 10.f * (q - qm1)));
 }
 __device__ __forceinline__ float pflux4(float qm2, float qm1, float q, float qp1) {
   return (7.f / 12.f) * (q + qm1) - (1.f / 12.f) * (qp1 + qm2);

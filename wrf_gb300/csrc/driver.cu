@@ -422,7 +422,7 @@ struct Ensemble {
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
       mark(PH_SSP); launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream, tune[TU_SSP]);
       mark(PH_CPR0); launch_calc_p_rho_col(LTM(), nb_tm, StepArgs{rk_step, 0, 0, 0}, stream);
-      mark(PH_COEFW); launch_calc_coef_w(l2, nb2, a, fp64, stream);
+      mark(PH_COEFW); launch_calc_coef_w_col(LTM(), nb_tm, a, fp64, stream);
       {  // solve_em.F:1176-1264
         JobList j;
         j.f3(WRFGPU_RU_TEND, 'u'); j.f3(WRFGPU_RV_TEND, 'v'); j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p');

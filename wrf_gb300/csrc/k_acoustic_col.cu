@@ -609,14 +609,26 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
     RC wup = wcol[kt];
     w(i, kt, j) = (float)wup;
     ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * (float)wup / (c1f(kt) * mts + c2f(kt));
-    RC g_nxt = GAcoef(k_end);
-    for (int k = k_end; k >= 2; --k) {
-      const RC g = g_nxt;
-      if (k - 1 >= 2) g_nxt = GAcoef(k - 1);
-      const RC wk = wcol[k] - g * wup;
-      w(i, k, j) = (float)wk;
-      ph(i, k, j) = rhs[k] + my * .5f * dts * G * eps1 * (float)wk / (c1f(k) * mts + c2f(k));
-      wup = wk;
+    // four levels at a time: their gamma, eliminated w and rhs (global and
+    // local-memory loads, independent of the recursion) go out first
+    for (int kb = k_end; kb >= 2; kb -= 4) {
+      RC gv[4], wv[4];
+      float rv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = kb - q;
+        if (k >= 2) { gv[q] = GAcoef(k); wv[q] = wcol[k]; rv[q] = rhs[k]; }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = kb - q;
+        if (k >= 2) {
+          const RC wk = wv[q] - gv[q] * wup;
+          w(i, k, j) = (float)wk;
+          ph(i, k, j) = rv[q] + my * .5f * dts * G * eps1 * (float)wk / (c1f(k) * mts + c2f(k));
+          wup = wk;
+        }
+      }
     }
   }
 }

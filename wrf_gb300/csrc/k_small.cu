@@ -204,13 +204,9 @@ __global__ void __launch_bounds__(TX* TY) k_calc_p_rho_col(TileLaunch L, int ste
 }
 
 // ------------------------------------------------------------ calc_coef_w
+// One column of calc_coef_w at (i, j).
 template <typename RC>
-__global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
-  BlockPos bp = block_pos(L);
-  const Mem& m = block_member(L.mem, bp.m);
-  if (!bp.valid) return;
-  const int i = bp.i, j = bp.j;
-  if (i < m.its || i > min(m.ite, m.ide - 1) || j < m.jts || j > min(m.jte, m.jde - 1)) return;
+__device__ __forceinline__ void coef_w_column(const Mem& m, int i, int j, int rk_step) {
   const Stage st = stage_of(m, rk_step);
   F3 cqw = f3(m, WRFGPU_CQW), c2a = f3(m, WRFGPU_C2A);
   F2 MUTf = f2(m, WRFGPU_MUT);
@@ -279,6 +275,26 @@ __global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
     AL(kde) = al;
     GA(kde) = RC(0.) * al;
   }
+}
+
+template <typename RC>
+__global__ void __launch_bounds__(BX* BY) k_calc_coef_w(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid) return;
+  const int i = bp.i, j = bp.j;
+  if (i < m.its || i > min(m.ite, m.ide - 1) || j < m.jts || j > min(m.jte, m.jde - 1)) return;
+  coef_w_column<RC>(m, i, j, rk_step);
+}
+
+// the same over mass tiles (32 x 8 columns per block)
+template <typename RC>
+__global__ void __launch_bounds__(TX* TY) k_calc_coef_w_col(TileLaunch L, int rk_step) {
+  const TilePos tp = tile_pos(L, false, false);
+  const Mem& m = block_member(L.mem, tp.m);
+  const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;
+  if (i > min(m.ite, m.ide - 1) || j > min(m.jte, m.jde - 1)) return;
+  coef_w_column<RC>(m, i, j, rk_step);
 }
 
 // ------------------------------------------------------------ advance_uv
@@ -685,6 +701,10 @@ void launch_calc_p_rho(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
 }
 void launch_calc_p_rho_col(const TileLaunch& L, int nb, StepArgs a, cudaStream_t s) {
   k_calc_p_rho_col<<<dim3(nb, 4), dim3(TX, TY), 0, s>>>(L, a.iteration);
+}
+void launch_calc_coef_w_col(const TileLaunch& L, int nb, StepArgs a, bool fp64, cudaStream_t s) {
+  if (fp64) k_calc_coef_w_col<double><<<nb, dim3(TX, TY), 0, s>>>(L, a.rk_step);
+  else k_calc_coef_w_col<float><<<nb, dim3(TX, TY), 0, s>>>(L, a.rk_step);
 }
 void launch_calc_coef_w(const Launch& L, int nb, StepArgs a, bool fp64, cudaStream_t s) {
   if (fp64) k_calc_coef_w<double><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);

@@ -76,6 +76,7 @@ void launch_small_step_prep(const Launch& L2, int nb2, const TileLaunch& LST, in
                             int var = TUNE_DEFAULT[TU_SSP]);
 void launch_calc_p_rho(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_calc_coef_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
+void launch_calc_coef_w_col(const TileLaunch& L, int nblocks, StepArgs a, bool fp64, cudaStream_t s);  // mass tiles
 void launch_advance_uv(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_advance_mu_t(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
 void launch_advance_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);

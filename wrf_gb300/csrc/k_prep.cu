@@ -115,10 +115,13 @@ __global__ void __launch_bounds__(BX* BY, MINB) k_rk_step_prep(Launch L) {
           dmdt = dmdt + dvv;
         });
     float wwk = 0.f;  // ww(i, 1, j), set to zero above by this thread
-    for (int k = 2; k <= ktf; ++k) {
-      wwk = wwk - dnw(k - 1) * c1h(k - 1) * dmdt - dv[k - 1];
-      ww(i, k, j) = wwk;
-    }
+    // the recursion's loads (dv sits in local memory) go out eight levels at a time
+    chunked_levels<8, float>(
+        2, ktf, [&](int k, float& d) { d = dv[k - 1]; },
+        [&](int k, const float& d) {
+          wwk = wwk - dnw(k - 1) * c1h(k - 1) * dmdt - d;
+          ww(i, k, j) = wwk;
+        });
     // couple_momentum rw (:329-391), calc_cq cqw, calc_alt (:910-950), calc_php (:1227-1262)
     const float my = msfty.ro(i, j);
     struct LT { float w, q0, qm, al, alb, phb0, phb1, ph0, ph1; };

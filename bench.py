@@ -81,8 +81,8 @@ def alg_bytes_per_cell_step(phase, s_pd, s_all, n_acoustic=7):
 # L2; traffic grows with the cells processed, so it scales to other sizes).
 NCU_DRAM_BYTES_PER_CELL = {
     "scalar_pd_update": 941.5e6 / 5177344,   # k_scalar_pd_update_c2_256x256x80.md
-    "rk_tend_v": 331.0e6 / 5177344,          # k_tend_v_col_c2_256x256x80.md
-    "advance_w": 450.1e6 / 5177344,          # k_advance_w_col_c2_256x256x80.md
+    "scalar_adv_update": 779.3e6 / 5177344,  # k_scalar_adv_update_c2_256x256x80.md (stage 1)
+    "advance_w": 451.3e6 / 5177344,          # k_acoustic_cols_c2_256x256x80.md
 }
 
 PHASE_NAMES = ["step_prep", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",

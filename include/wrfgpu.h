@@ -57,7 +57,7 @@ typedef struct WrfDynConfig {
   int32_t non_hydrostatic, top_lid, use_theta_m, hypsometric_opt, phi_adv_z;
   int32_t w_damping, damp_opt, diff_opt, zadvect_implicit, map_proj;
   int32_t time_step_sound;
-  int32_t pad0;
+  float w_crit_cfl;       /* namelist w_crit_cfl (Registry default 1.0); enters the w_damping = 1 term */
 } WrfDynConfig;
 
 /* Domain scalars that solve_em reads from grid% (double on the ABI; each

@@ -445,14 +445,19 @@ void pg_buoy_w(R* rw_tend_p, R* p_p, R* cqw_p, R* muf_p, R* mubf_p, R* c1f_p, R*
   }
 }
 
-// module_big_step_utilities_em.F:2503-2712 w_damp: CFL diagnostics only
-// (w_damping=0 leaves rw_tend untouched on this path).
+// module_big_step_utilities_em.F:2503-2712 w_damp: the CFL diagnostics, and
+// with w_damping = 1 the damping of rw_tend where the vertical Courant
+// number exceeds w_beta (:2689; zadvect_implicit = 0 on this path, so the
+// activation number is w_beta, module_model_constants.F:88-89).
 template <typename R>
-void w_damp_cfl(R* u_p, R* v_p, R* ww_p, R* mut_p, R* c1f_p, R* c2f_p, R* rdnw_p, R rdx, R rdy, R* msfux_p,
-                R* msfvy_p, R dt, R* max_vert_cfl, R* max_horiz_cfl, const Dims& d) {
-  A3<R> u(u_p, d), v(v_p, d), ww(ww_p, d);
+void w_damp_cfl(R* rw_tend_p, R* u_p, R* v_p, R* ww_p, R* w_p, R* mut_p, R* c1f_p, R* c2f_p, R* rdnw_p, R rdx,
+                R rdy, R* msfux_p, R* msfvy_p, R dt, const WrfDynConfig& cf, R* max_vert_cfl, R* max_horiz_cfl,
+                const Dims& d) {
+  A3<R> rw_tend(rw_tend_p, d), u(u_p, d), v(v_p, d), ww(ww_p, d), w(w_p, d);
   A2<R> mut(mut_p, d), msfux(msfux_p, d), msfvy(msfvy_p, d);
   A1<R> c1f(c1f_p, d), c2f(c2f_p, d), rdnw(rdnw_p, d);
+  const R w_alpha = R(0.3), w_beta = R(1.0);
+  const R w_crit_cfl = (R)cf.w_crit_cfl;
   int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1);
   R mv = 0, mh = 0;
   for (int j = d.jts; j <= jtf; ++j)
@@ -462,6 +467,9 @@ void w_damp_cfl(R* u_p, R* v_p, R* ww_p, R* mut_p, R* c1f_p, R* c2f_p, R* rdnw_p
         if (vert_cfl > mv) mv = vert_cfl;
         R horiz_cfl = fmaxr(std::fabs(u(i, k, j) * rdx * msfux(i, j) * dt), std::fabs(v(i, k, j) * rdy * msfvy(i, j) * dt));
         if (horiz_cfl > mh) mh = horiz_cfl;
+        if (vert_cfl > w_beta && cf.w_damping == 1)
+          rw_tend(i, k, j) = rw_tend(i, k, j) - std::copysign(R(1.), w(i, k, j)) * w_alpha * (vert_cfl - w_crit_cfl) *
+                                                    (c1f(k) * mut(i, j) + c2f(k));
       }
   *max_vert_cfl = mv; *max_horiz_cfl = mh;
 }

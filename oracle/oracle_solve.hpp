@@ -234,8 +234,9 @@ struct Domain {
         pg_buoy_w(p3(WRFGPU_RW_TEND), p3(WRFGPU_P), p3(WRFGPU_CQW), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), p1(WRFGPU_C1F),
                   p1(WRFGPU_C2F), p1(WRFGPU_RDNW), p1(WRFGPU_RDN), KR::g, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), td);
         R a = 0, b = 0;
-        w_damp_cfl(p3(WRFGPU_U_2), p3(WRFGPU_V_2), p3(WRFGPU_WW), p2(WRFGPU_MUT), p1(WRFGPU_C1F), p1(WRFGPU_C2F),
-                   p1(WRFGPU_RDNW), rdx, rdy, p2(WRFGPU_MSFUX), p2(WRFGPU_MSFVY), dt, &a, &b, td);
+        w_damp_cfl(p3(WRFGPU_RW_TEND), p3(WRFGPU_U_2), p3(WRFGPU_V_2), p3(WRFGPU_WW), p3(WRFGPU_W_2), p2(WRFGPU_MUT),
+                   p1(WRFGPU_C1F), p1(WRFGPU_C2F), p1(WRFGPU_RDNW), rdx, rdy, p2(WRFGPU_MSFUX), p2(WRFGPU_MSFVY), dt, cf,
+                   &a, &b, td);
 #ifdef _OPENMP
         int tid = omp_get_thread_num();
 #else

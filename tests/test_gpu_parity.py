@@ -427,3 +427,47 @@ def test_full_step_bitwise_symmetric_y(gpulib, nsteps):
         if d != 0.0:
             bad.append("%s: max|diff| %.3e serr %.2e" % (nm, d, serr(a, b)))
     assert not bad, "\n".join(bad)
+
+
+def damping_case():
+    """Strong convergence (a 60 m/s wave in u over 8 points) on 40 levels
+    with dt = 30 s: vertical Courant numbers reach ~2, so w_damp's term is
+    active at many points (measured on the oracle)."""
+    case = cases.small_case(nx=16, ny=12, kde=40, n_scalar=1, seed=17, dt=30.0)
+    F = case.fields
+    ni = F["u_2"].shape[-1]
+    pert = (60.0 * np.sin(2 * np.pi * np.arange(ni) / 8.0)).astype(F["u_2"].dtype)
+    for nm in ("u_1", "u_2"):
+        F[nm][...] = F[nm] + pert
+    c = case.desc.config
+    c.w_damping = 1
+    c.w_crit_cfl = 1.2
+    return case
+
+
+@pytest.mark.parametrize("nsteps", [1, 2])
+def test_full_step_bitwise_w_damping(gpulib, nsteps):
+    """w_damping = 1 (module_big_step_utilities_em.F:2687-2691): rw_tend
+    loses sign(w) w_alpha (cfl - w_crit_cfl) mu wherever the vertical Courant
+    number passes w_beta; bit for bit with the oracle, and the term is
+    active (the oracle's state differs from its w_damping = 0 run)."""
+    case = damping_case()
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(nsteps)
+    ge.step(nsteps)
+    ge.sync()
+    bad = []
+    for nm in STATE_FIELDS:
+        fid = abi.FIELD_ID[nm]
+        a = interior(case, fid, ge.get(0, fid), halo=3)
+        b = interior(case, fid, od.get(fid), halo=3)
+        d = max_abs(a, b)
+        if d != 0.0:
+            bad.append("%s: max|diff| %.3e serr %.2e" % (nm, d, serr(a, b)))
+    assert not bad, "\n".join(bad)
+    case.desc.config.w_damping = 0
+    o0 = OracleDomain(case, "f32")
+    o0.step(nsteps)
+    fid = abi.FIELD_ID["w_2"]
+    assert max_abs(o0.get(fid), od.get(fid)) > 0.0

@@ -35,6 +35,8 @@ constexpr float CPOVCV = CP / (CP - R_D);
 constexpr float T0 = 300.f;
 constexpr float P0 = 100000.f;
 constexpr float RERADIUS = 1.f / 6370.0e03f;
+constexpr float W_ALPHA = 0.3f;  // w_damp strength (m/s/s), module_model_constants.F:88
+constexpr float W_BETA = 1.0f;   // w_damp activation Courant number, :89
 
 // Tensor maps (TMA descriptors) of every 3-D field buffer of a member: slot
 // f < WRFGPU_N3D for the fields, WRFGPU_N3D + 3 s + {0, 1, 2} for species s's

@@ -61,7 +61,7 @@ static int check_desc(const WrfGpuDomainDesc& d) {
   if (c.rk_ord != 3 || c.h_mom_adv_order != 5 || c.h_sca_adv_order != 5 || c.v_mom_adv_order != 3 ||
       c.v_sca_adv_order != 3)
     return WRFGPU_E_ARG;
-  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || c.damp_opt == 3 || c.w_damping != 0 || c.diff_opt != 0)
+  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || c.damp_opt == 3 || (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
     return WRFGPU_E_ARG;
   if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
   if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;

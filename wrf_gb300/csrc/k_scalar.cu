@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
 }
 
 // ------------------------------------------------------------ w_damp CFL diagnostics + health
-// module_big_step_utilities_em.F:2503-2712 (w_damping = 0: diagnostics only).
+// module_big_step_utilities_em.F:2503-2712 (the diagnostics; the w_damping = 1
+// term of rw_tend is applied by the w-tendency kernels, in rk_tendency's order).
 __global__ void __launch_bounds__(BX* BY) k_cfl_check(Launch L) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);

@@ -302,6 +302,15 @@ __global__ void __launch_bounds__(BX* BY, 5) k_tend_w(Launch L) {
         t = t + rmg * (cq1 * rdzu(k) * (pk - pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       }
     }
+    // w_damp with w_damping = 1 (module_big_step_utilities_em.F:2687-2691),
+    // after pg_buoy_w and before coriolis as rk_tendency calls them; part of
+    // the whole rk_tendency only (the single-routine calls leave it out)
+    if (FL == TF_ALL && m.cf.w_damping == 1 && k >= 2 && k <= kde - 1) {
+      const float mutw = f2(m, WRFGPU_MUT)(i, j);
+      const float vert_cfl = fabsf(rom(i, k, j) / (c1f(k) * mutw + c2f(k)) * rdnw(k) * m.dt);
+      if (vert_cfl > W_BETA)
+        t = t - sgn1(w(i, k, j)) * W_ALPHA * (vert_cfl - m.cf.w_crit_cfl) * (c1f(k) * mutw + c2f(k));
+    }
     if (k >= m.kts + 1 && k <= ktf) {
       if (FL & TF_COR) {
         t = t + e_c * (cosa05 * (fzm(k) * (ru0 + ru1) + fzp(k) * (ru0m + ru1m)) -

@@ -469,8 +469,10 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
   };
   // column constants, formed in the order of the per-level expressions
   float mrdy = 0.f, mrdx = 0.f, rmg = 0.f, ratio = 0.f, e_c = 0.f, cosa05 = 0.f, rsina05 = 0.f, ratio05 = 0.f;
-  float muf_c = 0.f, mub_c = 0.f, cqw_top = 0.f, vf_lo = 0.f;
+  float muf_c = 0.f, mub_c = 0.f, cqw_top = 0.f, vf_lo = 0.f, mut_w = 0.f;
+  const bool wdamp = m.cf.w_damping == 1;
   if (acc) {
+    if (wdamp) mut_w = f2(m, WRFGPU_MUT)(i, j);
     const F2 msftx = f2(m, WRFGPU_MSFTX), msfty = f2(m, WRFGPU_MSFTY);
     mrdy = msftx(i, j) * rdy; mrdx = msftx(i, j) * rdx;
     rmg = (1.f / msfty(i, j)) * G;
@@ -546,6 +548,14 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
         cqw(i, k, j) = cq1;
         t = t + rmg * (cq1 * rdzu(k) * (pk - pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       }
+    }
+    // w_damp with w_damping = 1 (module_big_step_utilities_em.F:2687-2691),
+    // after pg_buoy_w and before coriolis as rk_tendency calls them
+    // (module_em.F:729-745); activation at w_beta (zadvect_implicit = 0)
+    if (FL == TF_ALL && wdamp && k >= 2 && k <= kde - 1) {
+      const float vert_cfl = fabsf(rom(i, k, j) / (c1f(k) * mut_w + c2f(k)) * rdnw(k) * m.dt);
+      if (vert_cfl > W_BETA)
+        t = t - sgn1(Wk[o]) * W_ALPHA * (vert_cfl - m.cf.w_crit_cfl) * (c1f(k) * mut_w + c2f(k));
     }
     if (k >= kts + 1 && k <= ktf) {
       if (FL & TF_COR) {

@@ -370,51 +370,12 @@ __global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
 // ------------------------------------------------------------ w_damp CFL diagnostics + health
 // module_big_step_utilities_em.F:2503-2712 (the diagnostics; the w_damping = 1
 // term of rw_tend is applied by the w-tendency kernels, in rk_tendency's order).
-__global__ void __launch_bounds__(BX* BY) k_cfl_check(Launch L) {
-  BlockPos bp = block_pos(L);
-  const Mem& m = block_member(L.mem, bp.m);
-  float vmax = 0.f, hmax = 0.f;
-  bool bad = false;
-  if (bp.valid && mass_pt(m, bp.i, bp.j) && bp.k >= 2 && bp.k <= m.kde - 1) {
-    const int i = bp.i, j = bp.j, k = bp.k;
-    F3 ww = f3(m, WRFGPU_WW), u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2), w = f3(m, WRFGPU_W_2), t = f3(m, WRFGPU_T_2);
-    F2 mut = f2(m, WRFGPU_MUT), msfux = f2(m, WRFGPU_MSFUX), msfvy = f2(m, WRFGPU_MSFVY);
-    F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F), rdnw = f1(m, WRFGPU_RDNW);
-    float vc = fabsf(ww(i, k, j) / (c1f(k) * mut(i, j) + c2f(k)) * rdnw(k) * m.dt);
-    float hc = fmaxf_f(fabsf(u(i, k, j) * m.rdx * msfux(i, j) * m.dt), fabsf(v(i, k, j) * m.rdy * msfvy(i, j) * m.dt));
-    bad = !isfinite(vc) || !isfinite(hc) || !isfinite(w(i, k, j)) || !isfinite(t(i, k, j));
-    vmax = isfinite(vc) ? vc : 0.f;
-    hmax = isfinite(hc) ? hc : 0.f;
-  }
-  // block max (all members of a block share one member)
-  __shared__ float sv[BX * BY], sh[BX * BY];
-  __shared__ int sb;
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  if (tid == 0) sb = 0;
-  sv[tid] = vmax; sh[tid] = hmax;
-  __syncthreads();
-  if (bad) atomicOr(&sb, 1);
-  for (int s = (BX * BY) / 2; s > 0; s >>= 1) {
-    if (tid < s) { sv[tid] = fmaxf_f(sv[tid], sv[tid + s]); sh[tid] = fmaxf_f(sh[tid], sh[tid + s]); }
-    __syncthreads();
-  }
-  if (tid == 0) {
-    if (m.cfl_out) {
-      atomicMax((unsigned*)&m.cfl_out[0], __float_as_uint(sv[0]));
-      atomicMax((unsigned*)&m.cfl_out[1], __float_as_uint(sh[0]));
-    }
-    unsigned bits = 0;
-    if (sb) bits |= ERR_NONFINITE;
-    if (m.cfl_limit > 0.f && sv[0] > m.cfl_limit) bits |= ERR_CFL;
-    if (bits) raise_err(m, bits);
-  }
-}
-
-// Column form of the same diagnostics: one thread per mass column of a 32x8
-// tile and one block per (tile, chunk of levels 2..kde-1: gridDim.y chunks),
-// the maxima kept in registers and reduced once per block (warp shuffles,
-// then shared memory).  A maximum does not depend on the order it is taken
-// in, so the result equals the point form's.
+// One thread per mass column of a 32x8 tile and one block per (tile, chunk
+// of levels 2..kde-1: gridDim.y chunks), the maxima kept in registers and
+// reduced once per block (warp shuffles, then shared memory).  A maximum does
+// not depend on the order it is taken in, so the result equals the
+// reference's loop order's.  Also the health check: any non-finite u, v, w,
+// theta or Courant number raises ERR_NONFINITE.
 __global__ void __launch_bounds__(TX* TY) k_cfl_check_col(TileLaunch L) {
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
@@ -489,6 +450,5 @@ void launch_calc_p_rho_phi_col(const TileLaunch& L, int nb, cudaStream_t s, int 
   k_calc_p_rho_phi_col<<<dim3(nb, TUNE_PARAM[TU_CPRP][var]), dim3(TX, TY), 0, s>>>(L);
 }
 void launch_set_w_surface(const Launch& L, int nb, cudaStream_t s) { k_set_w_surface<<<nb, dim3(BX, BY), 0, s>>>(L); }
-void launch_cfl_check(const Launch& L, int nb, cudaStream_t s) { k_cfl_check<<<nb, dim3(BX, BY), 0, s>>>(L); }
 
 }  // namespace wrfgpu

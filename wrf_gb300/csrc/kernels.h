@@ -63,7 +63,6 @@ void launch_tend_w(const Launch& L2, int nblocks, int flags, cudaStream_t s);
 void launch_tend_w_col(const TileLaunch& L, int nblocks, int var, cudaStream_t s);  // TF_ALL, staggered tiles, tuned
 void launch_tend_t(const Launch& L3, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph(const Launch& L3, int nblocks, int flags, cudaStream_t s);
-void launch_zero_save(const Launch& L3, int nblocks, cudaStream_t s);
 // column forms over tiles of the staggered extents
 void launch_tend_u_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s, int var = 0);
 void launch_tend_v_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s, int var = 0);
@@ -97,7 +96,6 @@ void launch_calc_p_rho_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStr
 void launch_update_scalar_pd_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);  // mass tiles
 void launch_calc_p_rho_phi_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CPRP]);  // mass tiles
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
-void launch_cfl_check(const Launch& L3, int nblocks, cudaStream_t s);
 void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CFL]);  // mass tiles
 
 // fused scalar transport (k_scalar_fused.cu): one block per (tile, species)

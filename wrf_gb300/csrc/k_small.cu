@@ -726,8 +726,9 @@ void launch_sumflux_p_rho(const Launch& L, int nb, StepArgs a, bool do_p_rho, cu
 }
 void launch_sumflux(const Launch& L, int nb, StepArgs a, cudaStream_t s) { launch_sumflux_p_rho(L, nb, a, false, s); }
 void launch_small_step_finish(const Launch& L, int nb, StepArgs a, cudaStream_t s, int var) {
+  // 4 blocks of 128 threads per SM leave the registers free (~80); 8 hold them to 64
   if (var == 0) k_small_step_finish<4><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
-  else k_small_step_finish<6><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+  else k_small_step_finish<8><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
 }
 
 }  // namespace wrfgpu

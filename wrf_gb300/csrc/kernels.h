@@ -50,7 +50,7 @@ constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 0, 0, 1, 1, 2, 2, 1, 0, 0, 2, 0};
 // the parameter each variant stands for: blocks per SM, level chunks, or
 // (advance_uv, sumflux, rk_tend_u, rk_tend_v) 10 x blocks per SM + level chunks
 constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 3, 0}, {4, 5, 6, 0}, {2, 3, 4, 0}, {32, 42, 34, 44}, {32, 42, 34, 44},
-                                                {3, 5, 0, 0}, {4, 6, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {2, 3, 4, 0},
+                                                {3, 8, 0, 0}, {4, 8, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {2, 3, 4, 0},
                                                 {32, 42, 34, 44}, {32, 42, 34, 44}, {1, 2, 4, 8}, {2, 3, 4, 5}};
 
 void launch_rk_step_prep(const Launch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_PREP]);

@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(BX* BY) k_set_w_surface(Launch L) {
 // not depend on the order it is taken in, so the result equals the
 // reference's loop order's.  Also the health check: any non-finite u, v, w,
 // theta or Courant number raises ERR_NONFINITE.
-__global__ void __launch_bounds__(TX* TY) k_cfl_check_col(TileLaunch L) {
+__global__ void __launch_bounds__(TX* TY, 4) k_cfl_check_col(TileLaunch L) {
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
   const int i = tp.i0 + threadIdx.x, j = tp.j0 + threadIdx.y;

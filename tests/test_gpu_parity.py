@@ -471,3 +471,27 @@ def test_full_step_bitwise_w_damping(gpulib, nsteps):
     o0.step(nsteps)
     fid = abi.FIELD_ID["w_2"]
     assert max_abs(o0.get(fid), od.get(fid)) > 0.0
+
+
+def test_field_copies_pinned_and_pageable(gpulib, small):
+    """wrfgpu_set_field_f32 / wrfgpu_get_field_f32 move the same bits whether
+    the host array is pageable (staged copy) or page-locked (read and written
+    in place by the copy kernels)."""
+    torch = pytest.importorskip("torch")
+    ge = G.Domain(small)
+    rng = np.random.default_rng(1)
+    for fid in (abi.FIELD_ID["u_2"], abi.FIELD_ID["w_2"], abi.FIELD_ID["mu_2"], abi.FIELD_ID["c1h"],
+                abi.species_id(0)):
+        n = ge.field_size(0, fid)
+        x = rng.standard_normal(n).astype(np.float32)
+        pin = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+        pin[:] = x
+        ge.set(0, fid, pin)
+        assert np.array_equal(ge.get(0, fid), x)
+        out = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+        assert ge.L.wrfgpu_get_field_f32(ge.h, 0, fid, out.ctypes.data, n) == 0
+        assert np.array_equal(out, x)
+        y = (x + 1.0).astype(np.float32)
+        ge.set(0, fid, y)
+        assert ge.L.wrfgpu_get_field_f32(ge.h, 0, fid, out.ctypes.data, n) == 0
+        assert np.array_equal(out, y)

@@ -58,6 +58,7 @@ typedef struct WrfDynConfig {
   int32_t w_damping, damp_opt, diff_opt, zadvect_implicit, map_proj;
   int32_t time_step_sound;
   float w_crit_cfl;       /* namelist w_crit_cfl (Registry default 1.0); enters the w_damping = 1 term */
+  float dampcoef, zdamp;  /* namelist dampcoef, zdamp (Registry defaults 0.2, 5000 m): damp_opt = 3 */
 } WrfDynConfig;
 
 /* Domain scalars that solve_em reads from grid% (double on the ABI; each

@@ -396,15 +396,17 @@ void advance_w(R* w_p, R* rw_tend_p, R* ww_p, R* w_save_p, R* u_p, R* v_p, R* mu
                R* alpha_p, R* gamma_p, R rdx, R rdy, R dts, R t0, R epssm, R* dnw_p, R* fnm_p, R* fnp_p,
                R* rdnw_p, R* rdn_p, R cf1, R cf2, R cf3, R* msftx_p, R* msfty_p, const WrfDynConfig& cf,
                int top_lid, const Dims& d) {
-  (void)w_save_p; (void)mu1_p; (void)alb_p; (void)dnw_p;
+  (void)mu1_p; (void)alb_p; (void)dnw_p;
   A3<R> w(w_p, d), rw_tend(rw_tend_p, d), ww(ww_p, d), u(u_p, d), v(v_p, d), t_2ave(t_2ave_p, d), t_2(t_2_p, d),
       t_1(t_1_p, d), ph(ph_p, d), ph_1(ph_1_p, d), phb(phb_p, d), ph_tend(ph_tend_p, d), c2a(c2a_p, d),
-      cqw(cqw_p, d), alt(alt_p, d), a(a_p, d), alpha(alpha_p, d), gamma(gamma_p, d);
+      cqw(cqw_p, d), alt(alt_p, d), a(a_p, d), alpha(alpha_p, d), gamma(gamma_p, d), w_save(w_save_p, d);
   A2<R> mut(mut_p, d), muave(muave_p, d), muts(muts_p, d), ht(ht_p, d), msftx(msftx_p, d), msfty(msfty_p, d);
   A1<R> c1h(c1h_p, d), c2h(c2h_p, d), c1f(c1f_p, d), c2f(c2f_p, d), fnm(fnm_p, d), fnp(fnp_p, d),
       rdnw(rdnw_p, d), rdn(rdn_p, d);
   const R g = K<R>::g;
-  if (cf.damp_opt == 3) throw std::runtime_error("damp_opt=3 not supported");
+  // damp_opt = 3 (:1283-1285): pi = 4 atan(1) in the working precision
+  const R pi = R(4.) * std::atan(R(1.));
+  const R dampmag = dts * (R)cf.dampcoef, hdepth = (R)cf.zdamp;
   int i_start = d.its, i_end = std::min(d.ite, d.ide - 1), j_start = d.jts, j_end = std::min(d.jte, d.jde - 1);
   int k_end = d.kte - 1;
   const int nx = d.ime - d.ims + 1, nk = d.kme - d.kms + 1;
@@ -473,6 +475,23 @@ void advance_w(R* w_p, R* rw_tend_p, R* ww_p, R* w_save_p, R* u_p, R* v_p, R* mu
       for (int i = i_start; i <= i_end; ++i) w(i, k, j) = (w(i, k, j) - a(i, k, j) * w(i, k - 1, j)) * alpha(i, k, j);
     for (k = k_end; k >= 2; --k)
       for (int i = i_start; i <= i_end; ++i) w(i, k, j) = w(i, k, j) - gamma(i, k, j) * w(i, k + 1, j);
+    // implicit Rayleigh damping of w toward w_save in the top zdamp metres
+    // (:1445-1458); sin in the working precision, correctly rounded (FP64
+    // sine rounded once for the FP32 restatement)
+    if (cf.damp_opt == 3) {
+      for (k = k_end + 1; k >= 2; --k)
+        for (int i = i_start; i <= i_end; ++i) {
+          const R htop = (ph_1(i, k_end + 1, j) + phb(i, k_end + 1, j)) / g;
+          const R hk = (ph_1(i, k, j) + phb(i, k, j)) / g;
+          const R hbot = htop - hdepth;
+          R dampwt = R(0.);
+          if (hk >= hbot) {
+            const R s = (R)std::sin((double)(R(.5) * pi * (hk - hbot) / hdepth));
+            dampwt = dampmag * s * s;
+          }
+          w(i, k, j) = (w(i, k, j) - dampwt * (c1f(k) * mut(i, j) + c2f(k)) * w_save(i, k, j)) / (R(1.) + dampwt);
+        }
+    }
     for (k = k_end + 1; k >= 2; --k)
       for (int i = i_start; i <= i_end; ++i)
         ph(i, k, j) = rhs(i, k) + msfty(i, j) * R(.5) * dts * g * (R(1.) + epssm) * w(i, k, j) / (c1f(k) * muts(i, j) + c2f(k));

@@ -5,7 +5,9 @@
 //    logf_cr(x) == (float)log((double)x);
 //  * a strided sample of x in [1e-3, 4]: powf_cr(x, 1.4) == (float)pow(x, 1.4);
 //  * the float-float approximations' relative error against long double,
-//    which must stay below the rounding test's 1e-12 bound.
+//    which must stay below the rounding test's 1e-12 bound;
+//  * sinf_cr on every 32nd float of [0, pi/2] against long double sin rounded
+//    to float, and its double-double series alone on a sparser sample.
 // Prints the counts; exit status 1 on any mismatch or error above 5e-13.
 #include <cmath>
 #include <cstdint>
@@ -47,7 +49,22 @@ int main() {
     const double e = (double)fabsl((ldexpl((long double)v.hi + (long double)v.lo, k) - ex) / ex);
     if (e > maxe_pow) maxe_pow = e;
   }
+  long long nsin = 0, badsin = 0, nser = 0, badser = 0;
+  for (uint32_t u = 0; u <= to_bits(1.5707964f); u += 32) {
+    const float x = from_bits(u);
+    ++nsin;
+    if (to_bits(sinf_cr(x)) != to_bits((float)sinl((long double)x))) ++badsin;
+  }
+  for (uint32_t u = to_bits(1e-6f); u <= to_bits(1.5707964f); u += 1021) {
+    const float x = from_bits(u);
+    ++nser;
+    const dd v = sin_dd_small((double)x);
+    const long double ex = sinl((long double)x);
+    const long double e = fabsl(((long double)v.hi + (long double)v.lo - ex) / ex);
+    if (e > 1e-18L) ++badser;
+  }
   std::printf("log: %lld inputs, %lld mismatches, max rel error %.3e\n", nlog, badlog, maxe_log);
   std::printf("pow: %lld inputs, %lld mismatches, max rel error %.3e\n", npow, badpow, maxe_pow);
-  return (badlog || badpow || maxe_log > 5e-13 || maxe_pow > 5e-13) ? 1 : 0;
+  std::printf("sin: %lld inputs, %lld mismatches; series: %lld inputs, %lld above 1e-18\n", nsin, badsin, nser, badser);
+  return (badlog || badpow || badsin || badser || maxe_log > 5e-13 || maxe_pow > 5e-13) ? 1 : 0;
 }

@@ -495,3 +495,59 @@ def test_field_copies_pinned_and_pageable(gpulib, small):
         ge.set(0, fid, y)
         assert ge.L.wrfgpu_get_field_f32(ge.h, 0, fid, out.ctypes.data, n) == 0
         assert np.array_equal(out, y)
+
+
+def rayleigh_case():
+    """damp_opt = 3 with the Registry's dampcoef 0.2 and zdamp 5000 m under
+    the 20 km lid of the small case: the top levels are damped."""
+    case = cases.small_case(nx=16, ny=12, kde=20, n_scalar=1, seed=19)
+    c = case.desc.config
+    c.damp_opt = 3
+    c.dampcoef = 0.2
+    c.zdamp = 5000.0
+    return case
+
+
+@pytest.mark.parametrize("nsteps", [1, 2])
+def test_full_step_bitwise_damp_opt_3(gpulib, nsteps):
+    """The implicit Rayleigh damping of w in advance_w
+    (module_small_step_em.F:1445-1458), whose weight takes a correctly rounded
+    sine: bit for bit with the oracle, and active (the oracle's state differs
+    from its damp_opt = 0 run)."""
+    case = rayleigh_case()
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(nsteps)
+    ge.step(nsteps)
+    ge.sync()
+    bad = []
+    for nm in STATE_FIELDS:
+        fid = abi.FIELD_ID[nm]
+        a = interior(case, fid, ge.get(0, fid), halo=3)
+        b = interior(case, fid, od.get(fid), halo=3)
+        d = max_abs(a, b)
+        if d != 0.0:
+            bad.append("%s: max|diff| %.3e serr %.2e" % (nm, d, serr(a, b)))
+    assert not bad, "\n".join(bad)
+    case.desc.config.damp_opt = 0
+    o0 = OracleDomain(case, "f32")
+    o0.step(nsteps)
+    fid = abi.FIELD_ID["w_2"]
+    assert max_abs(o0.get(fid), od.get(fid)) > 0.0
+
+
+def test_routine_advance_w_damp_opt_3(gpulib):
+    """The routine-level advance_w with damp_opt = 3 against the oracle's,
+    after the routines that precede it in the first acoustic step."""
+    case = rayleigh_case()
+    od = OracleDomain(case, "f32")
+    od.step(1)
+    ge = G.Ensemble([case.desc], flags=G.FLAG_NO_GRAPH)
+    sync(od, ge, case)
+    for name, it in (("rk_step_prep", 1), ("rk_tendency", 1), ("small_step_prep", 1), ("calc_p_rho", 0),
+                     ("calc_coef_w", 1), ("advance_uv", 1), ("advance_mu_t", 1)):
+        od.run(name, 1, it, 0)
+    sync(od, ge, case)
+    od.run("advance_w", 1, 1, 0)
+    ge.run_routine("advance_w", 1, 1, 0)
+    compare(od, ge, case, "advance_w with damp_opt = 3")

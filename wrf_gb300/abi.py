@@ -39,7 +39,7 @@ class WrfDynConfig(C.Structure):
         "moist_adv_opt", "scalar_adv_opt",
         "non_hydrostatic", "top_lid", "use_theta_m", "hypsometric_opt", "phi_adv_z",
         "w_damping", "damp_opt", "diff_opt", "zadvect_implicit", "map_proj",
-        "time_step_sound")] + [("w_crit_cfl", C.c_float)]
+        "time_step_sound")] + [("w_crit_cfl", C.c_float), ("dampcoef", C.c_float), ("zdamp", C.c_float)]
 
 
 class WrfGpuScalars(C.Structure):
@@ -135,4 +135,6 @@ def default_config(periodic_x=True, periodic_y=True, symmetric_y=False):
     c.map_proj = 0
     c.time_step_sound = 0
     c.w_crit_cfl = 1.0
+    c.dampcoef = 0.2
+    c.zdamp = 5000.0
     return c

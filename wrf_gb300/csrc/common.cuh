@@ -35,6 +35,7 @@ constexpr float CPOVCV = CP / (CP - R_D);
 constexpr float T0 = 300.f;
 constexpr float P0 = 100000.f;
 constexpr float RERADIUS = 1.f / 6370.0e03f;
+constexpr float PI_F = 3.14159274f;  // 4 atan(1) in FP32 (module_small_step_em.F:1283)
 constexpr float W_ALPHA = 0.3f;  // w_damp strength (m/s/s), module_model_constants.F:88
 constexpr float W_BETA = 1.0f;   // w_damp activation Courant number, :89
 

@@ -61,7 +61,7 @@ static int check_desc(const WrfGpuDomainDesc& d) {
   if (c.rk_ord != 3 || c.h_mom_adv_order != 5 || c.h_sca_adv_order != 5 || c.v_mom_adv_order != 3 ||
       c.v_sca_adv_order != 3)
     return WRFGPU_E_ARG;
-  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || c.damp_opt == 3 || (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
+  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || (c.damp_opt != 0 && c.damp_opt != 3) || (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
     return WRFGPU_E_ARG;
   if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
   if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;
@@ -117,6 +117,7 @@ struct Ensemble {
   bool capturing = false;
   int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0, nlev_max = 0;
+  bool damp3 = false;  // some member uses damp_opt = 3
   std::vector<size_t> n3, n2, n1;      // element counts per member (padded rows)
   std::vector<size_t> ni_, nk_, nj_, pitch_;  // Fortran extents and the padded row pitch
   CUtensorMap* d_tmaps = nullptr;      // [nmem][NMAPSLOT][2]
@@ -289,6 +290,7 @@ struct Ensemble {
       nsp_max = std::max(nsp_max, M.nsp);
       ns_max = std::max(ns_max, M.ns_total);
       nlev_max = std::max(nlev_max, M.kme - M.kms + 1);
+      damp3 = damp3 || M.cf.damp_opt == 3;
       bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
       bss[m + 1] = bss[m] + tiles_x(M) * tiles_y(M) * M.nsp;
@@ -436,7 +438,7 @@ struct Ensemble {
         StepArgs ai{rk_step, it, 0, 0};
         mark(PH_AUV); launch_advance_uv_col(LST(), nb_st, rk_step, it, stream, tune[TU_AUV]);
         mark(PH_AMUT); launch_advance_mu_t_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AMUT]);
-        mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AW]);
+        mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AW], damp3);
         mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream, tune[TU_SUMF]);
         JobList j;  // solve_em.F:1659-1716
         j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_P, 'p');

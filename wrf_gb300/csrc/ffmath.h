@@ -236,4 +236,73 @@ FFM_HD float powf_cr(float x, float y) {
   return (float)::pow((double)x, (double)y);
 }
 
+// ---------------------------------------------------------------- sin
+// Double-double helpers (Dekker / Knuth error-free transformations in FP64).
+struct dd { double hi, lo; };
+FFM_HD double fma_d(double a, double b, double c) {
+#ifdef __CUDA_ARCH__
+  return __fma_rn(a, b, c);
+#else
+  return std::fma(a, b, c);
+#endif
+}
+FFM_HD dd dd_fast_two_sum(double a, double b) { const double s = a + b; return {s, b - (s - a)}; }
+FFM_HD dd dd_add(dd a, dd b) {
+  const double s = a.hi + b.hi, bb = s - a.hi, e = (a.hi - (s - bb)) + (b.hi - bb);
+  return dd_fast_two_sum(s, e + a.lo + b.lo);
+}
+FFM_HD dd dd_mul(dd a, dd b) {
+  const double p = a.hi * b.hi, e = fma_d(a.hi, b.hi, -p);
+  return dd_fast_two_sum(p, e + (a.hi * b.lo + a.lo * b.hi));
+}
+FFM_HD dd dd_div_d(dd a, double b) {  // a / b, b an exact small integer here
+  const double q1 = a.hi / b;
+  const double p = q1 * b, pe = fma_d(q1, b, -p);
+  const double r = ((a.hi - p) - pe) + a.lo;
+  return dd_fast_two_sum(q1, r / b);
+}
+
+// sin x for a float |x| <= 2 as a double-double (relative error below
+// 2^-95): the Taylor series x - x^3/3! + x^5/5! - ... summed to x^33/33!
+// (below 2^-100 of the sum for |x| <= 2).
+FFM_HD dd sin_dd_small(double x) {
+  const dd x2 = {x * x, 0.0};  // exact: x has 24 significant bits
+  dd term = {x, 0.0}, sum = {x, 0.0};
+  for (int n = 1; n <= 16; ++n) {
+    term = dd_div_d(dd_mul(term, x2), (double)(2 * n) * (double)(2 * n + 1));
+    term.hi = -term.hi;
+    term.lo = -term.lo;
+    sum = dd_add(sum, term);
+  }
+  return sum;
+}
+
+// sin(x) for |x| <= 2, correctly rounded to float.  Fast path: the FP64 sine
+// (libm on the host, CUDA's double sin on the device; both within 2 ulp of
+// FP64) rounded once, accepted when it lies farther than 2^-45 of its value
+// from a float rounding boundary; otherwise the double-double series decides
+// (the same code on host and device).  Used by the w Rayleigh damping of
+// advance_w (damp_opt = 3), whose argument lies in [0, pi/2].
+FFM_HD float sinf_cr(float x) {
+  const double d = (double)x;
+  const double s = ::sin(d);
+  const float f = (float)s;
+  const double e = s - (double)f;          // exact
+  int ex;
+  const float mant = frexpf_(fabsf(f), &ex);
+  const double half_ulp = (double)ldexpf_(1.f, ex - 25);
+  if (f != 0.f && mant != 0.5f && fabs(fabs(e) - half_ulp) > 0x1p-45 * fabs(s)) return f;
+  if (x == 0.f) return x;
+  const dd v = sin_dd_small(d);
+  // round hi + lo to float: hi's rounding, moved one float step when lo
+  // carries the sum past the midpoint with a neighbour (the midpoints of
+  // adjacent floats are exact doubles, and hi - midpoint is exact)
+  float r = (float)v.hi;
+  const double up = 0.5 * ((double)r + (double)nextafterf(r, INFINITY));
+  const double dn = 0.5 * ((double)r + (double)nextafterf(r, -INFINITY));
+  if ((v.hi - up) + v.lo > 0.0) r = nextafterf(r, INFINITY);
+  else if ((v.hi - dn) + v.lo < 0.0) r = nextafterf(r, -INFINITY);
+  return r;
+}
+
 }  // namespace wrfgpu_ff

@@ -15,6 +15,7 @@
 //                        point j = jde are included.
 #include "common.cuh"
 #include "kernels.h"
+#include "ffmath.h"
 
 namespace wrfgpu {
 
@@ -437,7 +438,7 @@ template <typename RC, int NSLOT> struct AwCfg {
   using Ring = TileRing<NF, NSLOT>;
 };
 
-template <typename RC, int MINB>
+template <typename RC, int MINB, bool DAMP>
 __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, int rk_step, int iteration) {
   constexpr int AW_RING = MINB >= 4 ? 3 : 4;
   using Ring = typename AwCfg<RC, AW_RING>::Ring;
@@ -605,27 +606,55 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
     if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
     if (!act) return;
     w(i, 1, j) = w1;
+    // ---- damp_opt = 3 (module_small_step_em.F:1445-1458): after the back
+    // substitution, w relaxes toward w_save in the top zdamp metres with
+    // weight dampmag sin^2(pi/2 (h - hbot) / zdamp); the geopotential then
+    // takes the damped w.  The recursion itself runs on the undamped values.
+    // DAMP: compiled in only when some member uses it (the launcher's choice)
+    const bool damp3 = DAMP && m.cf.damp_opt == 3;
+    const F3 w_save = f3(m, WRFGPU_W_SAVE), ph_1 = f3(m, WRFGPU_PH_SAVE), phb = f3(m, WRFGPU_PHB);
+    const float hdepth = m.cf.zdamp, dampmag = dts * m.cf.dampcoef;
+    const float htop = damp3 ? (ph_1.ro(i, kt, j) + phb.ro(i, kt, j)) / G : 0.f;
+    auto damped = [&](int k, float wk, float ph1k, float phbk, float wsk) -> float {
+      const float hk = (ph1k + phbk) / G;
+      const float hbot = htop - hdepth;
+      float dampwt = 0.f;
+      if (hk >= hbot) {
+        const float sn = wrfgpu_ff::sinf_cr(.5f * PI_F * (hk - hbot) / hdepth);
+        dampwt = dampmag * sn * sn;
+      }
+      return (wk - dampwt * (c1f(k) * mutij + c2f(k)) * wsk) / (1.f + dampwt);
+    };
     // ---- back substitution (RC) and geopotential (FP32, from the new w)
     RC wup = wcol[kt];
-    w(i, kt, j) = (float)wup;
-    ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * (float)wup / (c1f(kt) * mts + c2f(kt));
+    {
+      float wst = (float)wup;
+      if (damp3) wst = damped(kt, wst, ph_1.ro(i, kt, j), phb.ro(i, kt, j), w_save.ro(i, kt, j));
+      w(i, kt, j) = wst;
+      ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * wst / (c1f(kt) * mts + c2f(kt));
+    }
     // four levels at a time: their gamma, eliminated w and rhs (global and
     // local-memory loads, independent of the recursion) go out first
     for (int kb = k_end; kb >= 2; kb -= 4) {
       RC gv[4], wv[4];
-      float rv[4];
+      float rv[4], p1v[4], pbv[4], wsv[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int k = kb - q;
-        if (k >= 2) { gv[q] = GAcoef(k); wv[q] = wcol[k]; rv[q] = rhs[k]; }
+        if (k >= 2) {
+          gv[q] = GAcoef(k); wv[q] = wcol[k]; rv[q] = rhs[k];
+          if (damp3) { p1v[q] = ph_1.ro(i, k, j); pbv[q] = phb.ro(i, k, j); wsv[q] = w_save.ro(i, k, j); }
+        }
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int k = kb - q;
         if (k >= 2) {
           const RC wk = wv[q] - gv[q] * wup;
-          w(i, k, j) = (float)wk;
-          ph(i, k, j) = rv[q] + my * .5f * dts * G * eps1 * (float)wk / (c1f(k) * mts + c2f(k));
+          float wst = (float)wk;
+          if (damp3) wst = damped(k, wst, p1v[q], pbv[q], wsv[q]);
+          w(i, k, j) = wst;
+          ph(i, k, j) = rv[q] + my * .5f * dts * G * eps1 * wst / (c1f(k) * mts + c2f(k));
           wup = wk;
         }
       }
@@ -648,30 +677,36 @@ void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int 
     else k_advance_mu_t_col<float, 5><<<nblocks, dim3(TX, TY), 0, s>>>(L, rk_step, iteration);
   }
 }
-void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
-                          int var) {
+template <bool DAMP>
+static void launch_advance_w_var(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64,
+                                 cudaStream_t s, int minb) {
   static bool attr = false;
   constexpr size_t S32 = AwCfg<float, 4>::Ring::SMEM, S64 = AwCfg<double, 4>::Ring::SMEM;
   constexpr size_t S32_3 = AwCfg<float, 3>::Ring::SMEM, S64_3 = AwCfg<double, 3>::Ring::SMEM;
   if (!attr) {
-    cudaFuncSetAttribute(k_advance_w_col<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
-    cudaFuncSetAttribute(k_advance_w_col<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
-    cudaFuncSetAttribute(k_advance_w_col<float, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32_3);
-    cudaFuncSetAttribute(k_advance_w_col<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
-    cudaFuncSetAttribute(k_advance_w_col<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
-    cudaFuncSetAttribute(k_advance_w_col<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64_3);
+    cudaFuncSetAttribute(k_advance_w_col<float, 2, DAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
+    cudaFuncSetAttribute(k_advance_w_col<float, 3, DAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32);
+    cudaFuncSetAttribute(k_advance_w_col<float, 4, DAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S32_3);
+    cudaFuncSetAttribute(k_advance_w_col<double, 2, DAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
+    cudaFuncSetAttribute(k_advance_w_col<double, 3, DAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64);
+    cudaFuncSetAttribute(k_advance_w_col<double, 4, DAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S64_3);
     attr = true;
   }
-  const int minb = TUNE_PARAM[TU_AW][var];
   if (fp64) {
-    if (minb == 2) k_advance_w_col<double, 2><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
-    else if (minb == 3) k_advance_w_col<double, 3><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
-    else k_advance_w_col<double, 4><<<nblocks, dim3(TX, TY), S64_3, s>>>(L, rk_step, iteration);
+    if (minb == 2) k_advance_w_col<double, 2, DAMP><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+    else if (minb == 3) k_advance_w_col<double, 3, DAMP><<<nblocks, dim3(TX, TY), S64, s>>>(L, rk_step, iteration);
+    else k_advance_w_col<double, 4, DAMP><<<nblocks, dim3(TX, TY), S64_3, s>>>(L, rk_step, iteration);
   } else {
-    if (minb == 2) k_advance_w_col<float, 2><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
-    else if (minb == 3) k_advance_w_col<float, 3><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
-    else k_advance_w_col<float, 4><<<nblocks, dim3(TX, TY), S32_3, s>>>(L, rk_step, iteration);
+    if (minb == 2) k_advance_w_col<float, 2, DAMP><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+    else if (minb == 3) k_advance_w_col<float, 3, DAMP><<<nblocks, dim3(TX, TY), S32, s>>>(L, rk_step, iteration);
+    else k_advance_w_col<float, 4, DAMP><<<nblocks, dim3(TX, TY), S32_3, s>>>(L, rk_step, iteration);
   }
+}
+void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
+                          int var, bool damp) {
+  const int minb = TUNE_PARAM[TU_AW][var];
+  if (damp) launch_advance_w_var<true>(L, nblocks, rk_step, iteration, fp64, s, minb);
+  else launch_advance_w_var<false>(L, nblocks, rk_step, iteration, fp64, s, minb);
 }
 
 }  // namespace wrfgpu

@@ -14,6 +14,7 @@
 // largest acoustic kernel.
 #include "common.cuh"
 #include "kernels.h"
+#include "ffmath.h"
 
 namespace wrfgpu {
 
@@ -560,15 +561,37 @@ __global__ void __launch_bounds__(BX* BY) k_advance_w(Launch L, int rk_step, int
     wk = (wk - Acoef(k) * wprev) * ALcoef(k);
     wcol[k] = wk;
   }
+  // damp_opt = 3 (module_small_step_em.F:1445-1458): w relaxes toward w_save
+  // in the top zdamp metres after the back substitution (which runs on the
+  // undamped values); the geopotential takes the damped w
+  const bool damp3 = m.cf.damp_opt == 3;
+  const F3 w_save = f3(m, WRFGPU_W_SAVE);
+  const float hdepth = m.cf.zdamp, dampmag = dts * m.cf.dampcoef;
+  const float htop = damp3 ? (ph_1.ro(i, k_end + 1, j) + phb.ro(i, k_end + 1, j)) / G : 0.f;
+  auto damped = [&](int k, RC wk) -> RC {
+    if (!damp3) return wk;
+    const float hk = (ph_1.ro(i, k, j) + phb.ro(i, k, j)) / G;
+    const float hbot = htop - hdepth;
+    float dampwt = 0.f;
+    if (hk >= hbot) {
+      const float sn = wrfgpu_ff::sinf_cr(.5f * PI_F * (hk - hbot) / hdepth);
+      dampwt = dampmag * sn * sn;
+    }
+    return (RC)(((float)wk - dampwt * (c1f(k) * mutij + c2f(k)) * w_save.ro(i, k, j)) / (1.f + dampwt));
+  };
   // back substitution and geopotential update (downward)
   RC wup = wcol[k_end + 1];
-  w(i, k_end + 1, j) = (float)wup;
-  ph(i, k_end + 1, j) = (float)(rhs[k_end + 1] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wup /
-                                                     ((RC)c1f(k_end + 1) * (RC)mts + (RC)c2f(k_end + 1)));
+  {
+    const RC wd = damped(k_end + 1, wup);
+    w(i, k_end + 1, j) = (float)wd;
+    ph(i, k_end + 1, j) = (float)(rhs[k_end + 1] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wd /
+                                                       ((RC)c1f(k_end + 1) * (RC)mts + (RC)c2f(k_end + 1)));
+  }
   for (int k = k_end; k >= 2; --k) {
     RC wk = wcol[k] - GAcoef(k) * wup;
-    w(i, k, j) = (float)wk;
-    ph(i, k, j) = (float)(rhs[k] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wk / ((RC)c1f(k) * (RC)mts + (RC)c2f(k)));
+    const RC wd = damped(k, wk);
+    w(i, k, j) = (float)wd;
+    ph(i, k, j) = (float)(rhs[k] + (RC)my * RC(.5) * (RC)dts * (RC)G * eps1 * wd / ((RC)c1f(k) * (RC)mts + (RC)c2f(k)));
     wup = wk;
   }
 }

@@ -114,7 +114,8 @@ void launch_advance_uv_col(const TileLaunch& L, int nblocks, int rk_step, int it
 // one block per tile of mass columns
 void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
                              int var = TUNE_DEFAULT[TU_AMUT]);
+// damp: some member uses damp_opt = 3 (compiles the damping into the kernel)
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
-                          int var = TUNE_DEFAULT[TU_AW]);
+                          int var = TUNE_DEFAULT[TU_AW], bool damp = false);
 
 }  // namespace wrfgpu

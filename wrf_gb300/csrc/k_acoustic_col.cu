@@ -524,7 +524,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
                               c2am * rdnw(k - 1) / (c1h(k - 1) * mutij + c2h(k - 1)) *
                                   (eps1 * (r_0 - r_m1) + eps0 * (ph_0 - ph_m1)))) +
                         dts * G * msft_inv * (rdn(k) * (c2ak * altk * tak - c2am * altm * tam) - (c1f(k) * mua));
-      const RC wk = ((RC)wkf - ak * wprev) * alk;
+      RC wk;
+      if constexpr (sizeof(RC) == 8) wk = fma(-ak, wprev, (RC)wkf) * alk;  // mixed form: one FP64 fma
+      else wk = ((RC)wkf - ak * wprev) * alk;
       wcol[k] = wk;
       wprev = wk;
     };
@@ -600,7 +602,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
                                   (eps1 * (r_top - r_m1) + eps0 * (ph_top - ph_m1)) -
                               dts * G * (2.f * rdnw(k - 1) * c2a_m1 * alt_m1 * ta_m1 + (c1f(k) * mua)));
       if (m.cf.top_lid) wkf = 0.f;
-      const RC wk = ((RC)wkf - Acoef(k) * wprev) * ALcoef(k);
+      RC wk;
+      if constexpr (sizeof(RC) == 8) wk = fma(-Acoef(k), wprev, (RC)wkf) * ALcoef(k);
+      else wk = ((RC)wkf - Acoef(k) * wprev) * ALcoef(k);
       wcol[k] = wk;
     }
     if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
@@ -650,7 +654,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
       for (int q = 0; q < 4; ++q) {
         const int k = kb - q;
         if (k >= 2) {
-          const RC wk = wv[q] - gv[q] * wup;
+          RC wk;
+          if constexpr (sizeof(RC) == 8) wk = fma(-gv[q], wup, wv[q]);
+          else wk = wv[q] - gv[q] * wup;
           float wst = (float)wk;
           if (damp3) wst = damped(k, wst, p1v[q], pbv[q], wsv[q]);
           w(i, k, j) = wst;

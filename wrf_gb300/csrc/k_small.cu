@@ -254,7 +254,11 @@ __device__ __forceinline__ void coef_w_column(const Mem& m, int i, int j, int rk
                                    rdnw(k - 1) * d.c2am / ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k))));
         const float c = -d.cqw * cof * rdn(k) * rdnw(k) * d.c2a /
                         ((c1h(k) * MUT + c2h(k)) * (c1f(k + 1) * MUT + c2f(k + 1)));
-        RC al = rcp_rc<RC>((RC)b - (RC)a_k * gprev);
+        // the mixed form fuses b - a gamma into one FP64 fma
+        RC den;
+        if constexpr (sizeof(RC) == 8) den = fma(-(RC)a_k, gprev, (RC)b);
+        else den = (RC)b - (RC)a_k * gprev;
+        RC al = rcp_rc<RC>(den);
         AL(k) = al;
         gprev = (RC)c * al;
         GA(k) = gprev;
@@ -272,7 +276,10 @@ __device__ __forceinline__ void coef_w_column(const Mem& m, int i, int j, int rk
     float r = rdnw(kde - 1);
     const float b = 1.f + 2.f * cof * (r * r) * c2a.ro(i, kde - 1, j) /
                               ((c1h(k - 1) * MUT + c2h(k - 1)) * (c1f(k) * MUT + c2f(k)));
-    RC al = rcp_rc<RC>((RC)b - (RC)a_top * gprev);
+    RC den;
+    if constexpr (sizeof(RC) == 8) den = fma(-(RC)a_top, gprev, (RC)b);
+    else den = (RC)b - (RC)a_top * gprev;
+    RC al = rcp_rc<RC>(den);
     AL(kde) = al;
     GA(kde) = RC(0.) * al;
   }

@@ -551,3 +551,28 @@ def test_routine_advance_w_damp_opt_3(gpulib):
     od.run("advance_w", 1, 1, 0)
     ge.run_routine("advance_w", 1, 1, 0)
     compare(od, ge, case, "advance_w with damp_opt = 3")
+
+
+def test_batched_mixed_options_equals_plain(gpulib):
+    """An ensemble whose members differ in the damping options (w_damping = 1,
+    damp_opt = 3, symmetric y) gives each member the bits it gets alone: the
+    launches compile the options in when any member uses them and each member
+    applies its own."""
+    a = damping_case()
+    b = rayleigh_case()
+    c = cases.small_case(nx=12, ny=20, kde=16, n_scalar=1, seed=5)
+    cf = c.desc.config
+    cf.periodic_y = 0
+    cf.symmetric_ys = 1
+    cf.symmetric_ye = 1
+    members = [a, b, c]
+    ens = G.Ensemble.from_cases(members)
+    ens.step(2)
+    ens.sync()
+    for m, cs in enumerate(members):
+        d = G.Domain(cs)
+        d.step(2)
+        d.sync()
+        for nm in STATE_FIELDS:
+            fid = abi.FIELD_ID[nm]
+            assert np.array_equal(ens.get(m, fid), d.get(0, fid)), (m, nm)

@@ -41,14 +41,11 @@ constexpr float W_BETA = 1.0f;   // w_damp activation Courant number, :89
 
 // Tensor maps (TMA descriptors) of every 3-D field buffer of a member: slot
 // f < WRFGPU_N3D for the fields, WRFGPU_N3D + 3 s + {0, 1, 2} for species s's
-// buffers (first current, old, first spare).  Three boxes per slot: the
-// tile plus a 4-point halo, (TX + 8) x 1 x (TY + 8) from (i0 - 4, j0 - 4);
-// the tile alone, TX x 1 x TY from (i0, j0); and the tile plus one point on
-// every side, NEAR_W x 1 x NEAR_H from (i0 - 4, j0 - 1) (x starts 4 points
-// early so that it stays 16-byte aligned).
+// buffers (first current, old, first spare).  Two boxes per slot: the
+// tile plus a 4-point halo, (TX + 8) x 1 x (TY + 8) from (i0 - 4, j0 - 4),
+// and the tile alone, TX x 1 x TY from (i0, j0).
 constexpr int NMAPSLOT = WRFGPU_N3D + 3 * NSPMAX;
-constexpr int BOX_HALO = 0, BOX_TILE = 1, BOX_NEAR = 2, NBOX = 3;
-constexpr int NEAR_W = 40, NEAR_H = 10;
+constexpr int BOX_HALO = 0, BOX_TILE = 1, NBOX = 2;
 
 // Error word bits (Mem::err): set by kernels, read by the host between steps.
 constexpr unsigned ERR_NONFINITE = 1u;
@@ -385,7 +382,6 @@ struct LevelRing {
   __device__ bool wait(int k) const { return mbar_wait(&bar[slot_of(k)], ((k - k0) / NSLOT) & 1); }
 };
 template <int NF, int NSLOT> using TileRing = LevelRing<NF, NSLOT, TX, TY>;
-template <int NF, int NSLOT> using NearRing = LevelRing<NF, NSLOT, NEAR_W, NEAR_H>;
 
 struct TileLaunch {
   const Mem* mem;

@@ -298,7 +298,7 @@ struct Ensemble {
       btm[m + 1] = btm[m] + tiles_x(M) * tiles_y(M);
     }
     nb2 = bs2[n]; nb3 = bs3[n]; nb_sc = bss[n]; nb_st = bst[n]; nb_tm = btm[n];
-    {  // tensor maps of every 3-D buffer: halo, tile and near boxes
+    {  // tensor maps of every 3-D buffer: halo and tile boxes
       int rc = get_tensor_map_encoder();
       if (rc) return rc;
       std::vector<CUtensorMap> maps((size_t)n * NMAPSLOT * NBOX);
@@ -310,9 +310,7 @@ struct Ensemble {
           int r1 = encode_field_map(&mm[NBOX * slot + BOX_HALO], base, ni_[m], pitch_[m], nk_[m], nj_[m],
                                     TX + 2 * TMA_HALO, TY + 2 * TMA_HALO);
           int r2 = encode_field_map(&mm[NBOX * slot + BOX_TILE], base, ni_[m], pitch_[m], nk_[m], nj_[m], TX, TY);
-          int r3 = encode_field_map(&mm[NBOX * slot + BOX_NEAR], base, ni_[m], pitch_[m], nk_[m], nj_[m], NEAR_W,
-                                    NEAR_H);
-          return r1 ? r1 : (r2 ? r2 : r3);
+          return r1 ? r1 : r2;
         };
         for (int f = 0; f < WRFGPU_N3D; ++f) { rc = enc(f, M.f3[f]); if (rc) return rc; }
         for (int sp = 0; sp < M.nsp; ++sp) {

@@ -242,6 +242,7 @@ struct Ensemble {
       b += (size_t)WRFGPU_N2D * al256(n2[m] * 4);
       b += (size_t)WRFGPU_N1D * al256(n1[m] * 4);
       b += al256(n3[m] * 4);  // limiter scratch
+      b += 3 * al256(n3[m] * 4);  // face Courant numbers of the PD transport
       if (fp64) b += 3 * al256(n3[m] * 8);
       off[m] = total;
       total += b;
@@ -277,6 +278,7 @@ struct Ensemble {
       for (int f = 0; f < WRFGPU_N2D; ++f) { M.f2[f] = (float*)p; p += al256(n2[m] * 4); }
       for (int f = 0; f < WRFGPU_N1D; ++f) { M.f1[f] = (float*)p; p += al256(n1[m] * 4); }
       scr[m] = (float*)p; p += al256(n3[m] * 4);
+      for (int q = 0; q < 3; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
       if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
       M.ns_total = num_sound_steps(d);
       const WrfGpuScalars& s = d.scalars;
@@ -457,7 +459,11 @@ struct Ensemble {
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
       mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV]);
-      if (rk_step == 3) { mark(PH_PD); launch_scalar_pd_update(LS(), nb_sc, nlev_max, rk_step, stream, tune[TU_PD]); }
+      if (rk_step == 3) {
+        mark(PH_PD);
+        launch_pd_courant(l3, nb3, rk_step, stream);
+        launch_scalar_pd_update(LS(), nb_sc, nlev_max, rk_step, stream, tune[TU_PD]);
+      }
       swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi_col(LTM(), nb_tm, stream, tune[TU_CPRP]);
       if (rk_step < 3) {

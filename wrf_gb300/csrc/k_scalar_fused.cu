@@ -173,6 +173,49 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L
   if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
 }
 
+// ------------------------------------------------------------------ PD Courant numbers
+// The Courant numbers of advect_scalar_pd's low-order fluxes
+// (module_advect_em.F:6505-6779, :7595-7645) depend on the mass fluxes and
+// column masses only, not on the species: formed once per step here, for the
+// x face between columns i-1 and i (pdc[0]), the y face between rows j-1 and
+// j (pdc[1]) and the z face k of column (i, j) (pdc[2]), over the faces the
+// PD kernel's limiter region reads (columns its-1 .. itf+2, rows
+// jts-1 .. jtf+2), with the PD kernel's expressions (the same bits).
+// Point layout: one thread per (i, j, k) of the memory extent.
+__global__ void __launch_bounds__(BX* BY) k_pd_courant(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid || !m.pdc[0]) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
+  if (i < m.its - 1 || i > itf + 2 || j < m.jts - 1 || j > jtf + 2 || k < m.kts) return;
+  const Stage st = stage_of(m, rk_step);
+  const float dt = st.dt_rk, rdx = m.rdx, rdy = m.rdy;
+  const F2 mut = f2(m, WRFGPU_MUTS), msx = f2(m, WRFGPU_MSFTX), msy = f2(m, WRFGPU_MSFTY);
+  const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
+  if (k <= ktf) {
+    const float c1k = c1(k), c2k = c2(k);
+    {  // x face
+      const float xdx = 2.f / (msy(i, j) + msy(i - 1, j)) / rdx;
+      const float mu = 0.5f * ((c1k * mut(i, j) + c2k) + (c1k * mut(i - 1, j) + c2k));
+      const float vel = f3(m, WRFGPU_RU_M)(i, k, j);
+      f3p(m, m.pdc[0])(i, k, j) = vel * dt / xdx / mu;
+    }
+    {  // y face
+      const float ydy = 2.f / (msx(i, j) + msx(i, j - 1)) / rdy;
+      const float mu = 0.5f * ((c1k * mut(i, j) + c2k) + (c1k * mut(i, j - 1) + c2k));
+      const float vel = f3(m, WRFGPU_RV_M)(i, k, j);
+      f3p(m, m.pdc[1])(i, k, j) = vel * dt / ydy / mu;
+    }
+  }
+  if (k > 1 && k < m.kde && k - 1 >= m.kms) {  // z face k
+    const float dz = 2.f / (rdzw(k) + rdzw(k - 1));
+    const float mu = 0.5f * ((c1(k) * mut(i, j) + c2(k)) + (c1(k) * mut(i, j) + c2(k)));
+    const float vel = f3(m, WRFGPU_WW_M)(i, k, j);
+    f3p(m, m.pdc[2])(i, k, j) = vel * dt / dz / mu;
+  }
+}
+
 // ------------------------------------------------------------------ PD
 struct PDPlanes {
   static constexpr int GW = TX + 4, GH = TY + 4;  // 2-D fields, halo 2
@@ -213,12 +256,11 @@ struct ZCell {
 struct LevelConst { float4 a, b; };
 
 // z face kk = L+1 of a limiter cell (advect_scalar_pd's fqz, fqzl).
-__device__ __forceinline__ void zface(const ZCell& c, int kk, const LevelConst& t, float dt, int kts, int kde, int ktf,
+__device__ __forceinline__ void zface(const ZCell& c, int kk, const LevelConst& t, float cr, int kts, int kde, int ktf,
                                       float* hi, float* lo) {
   if (kk == 1 || kk == kde) { *hi = 0.f; *lo = 0.f; return; }
   const float mu = 0.5f * ((t.a.x * c.mut + t.a.y) + (t.a.x * c.mut + t.a.y));
   const float vel = c.romp1;
-  const float cr = vel * dt / t.a.w / mu;
   const float l = mu * t.b.x * flux_upwind(c.fo0, c.fop1, cr);
   float h;
   if (kk == kts + 1 || kk == ktf) h = vel * (t.b.y * c.fp1 + t.b.z * c.f0);
@@ -269,6 +311,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     for (int d = 0; d < PD_RING - 1 && kts + d <= ktf; ++d) ring.issue(kts + d, maps, x0, z0, m.kms);
 
   F3 fld = f3p(m, m.q[s]), fold = f3p(m, m.qo[s]), out = f3p(m, m.qa[s]), rom = f3(m, WRFGPU_WW_M);
+  const F3 crxa = f3p(m, m.pdc[0]), crya = f3p(m, m.pdc[1]), crza = f3p(m, m.pdc[2]);
   F2 mut2 = f2(m, WRFGPU_MUTS), msx2 = f2(m, WRFGPU_MSFTX), msy2 = f2(m, WRFGPU_MSFTY);
   F2 mub2 = f2(m, WRFGPU_MUB), mu1 = f2(m, WRFGPU_MU_1), mu2 = f2(m, WRFGPU_MU_2);
   auto in_mem = [&](int ii, int jj) { return ii >= m.ims && ii <= m.ime && jj >= m.jms && jj <= m.jme; };
@@ -310,12 +353,13 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   // level-independent data of the faces: halo-plane offset, dx, and the
   // column masses on either side (mut of the face's two cells)
   bool xok = false, yok = false;
-  int xo = 0, yo = 0;
+  int xo = 0, yo = 0, xii = 0, xjj = 0, yii = 0, yjj = 0;
   float xdx = 0.f, xdxt = 0.f, ydy = 0.f, ydyt = 0.f, xma = 0.f, xmb = 0.f, yma = 0.f, ymb = 0.f;
   if (xq >= 0) {
     const int r = xq / P::XW, c = xq - r * P::XW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     xok = ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1;
+    xii = ii; xjj = jj;
     xo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
     const int xg = (r + 1) * P::GW + (c + 1);
     xdx = 2.f / (sMSY[xg] + sMSY[xg - 1]) / rdx;
@@ -326,6 +370,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     const int r = yq / P::YW, c = yq - r * P::YW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     yok = ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2;
+    yii = ii; yjj = jj;
     yo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
     const int yg = (r + 1) * P::GW + (c + 1);
     ydy = 2.f / (sMSX[yg] + sMSX[yg - P::GW]) / rdy;
@@ -381,6 +426,11 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     const int slot = Lv & 1;
     float c1k = 0.f, c2k = 0.f, rdzwk = 0.f;
     if (Lv <= ktf) {
+      // this thread's faces' Courant numbers (k_pd_courant), loaded before
+      // the ring wait so that their latency overlaps it
+      const float crx = xok ? crxa.ro(xii, Lv, xjj) : 0.f;
+      const float cry = yok ? crya.ro(yii, Lv, yjj) : 0.f;
+      const float crz = (c.valid && Lv + 1 > 1 && Lv + 1 < m.kde) ? crza.ro(c.i, Lv + 1, c.j) : 0.f;
       if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
       const float4 tl = sLV[Lv - m.kms].a;
       c1k = tl.x; c2k = tl.y; rdzwk = tl.z;
@@ -400,7 +450,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
           const int o = xo;
           const float mu = 0.5f * ((c1k * xma + c2k) + (c1k * xmb + c2k));
           const float vel = RU[o];
-          const float cr = vel * dt / xdx / mu;
+          const float cr = crx;
           lo = mu * xdxt * flux_upwind(FO[o - 1], FO[o], cr);
           const float h = vel * pflux5(F[o - 3], F[o - 2], F[o - 1], F[o], F[o + 1], F[o + 2], vel);
           hi = h - lo;
@@ -413,7 +463,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
           const int o = yo;
           const float mu = 0.5f * ((c1k * yma + c2k) + (c1k * ymb + c2k));
           const float vel = RV[o];
-          const float cr = vel * dt / ydy / mu;
+          const float cr = cry;
           lo = mu * ydyt * flux_upwind(FO[o - HW], FO[o], cr);
           const float h = vel * pflux5(F[o - 3 * HW], F[o - 2 * HW], F[o - HW], F[o], F[o + HW], F[o + 2 * HW], vel);
           hi = h - lo;
@@ -421,7 +471,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         YH[yq] = hi; YL[yq] = lo;
       }
       // ---- vertical face Lv+1 of this thread's limiter cell
-      if (c.valid) zface(c, Lv + 1, sLV[Lv + 1 - m.kms], dt, kts, m.kde, ktf, &c.hz1, &c.lz1);
+      if (c.valid) zface(c, Lv + 1, sLV[Lv + 1 - m.kms], crz, kts, m.kde, ktf, &c.hz1, &c.lz1);
     }
     __syncthreads();
     if (Lv <= ktf) {
@@ -539,6 +589,9 @@ void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int
   if (minb == 1) k_scalar_pd_update<1><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
   else if (minb == 2) k_scalar_pd_update<2><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
   else k_scalar_pd_update<3><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
+}
+void launch_pd_courant(const Launch& L3, int nblocks, int rk_step, cudaStream_t s) {
+  k_pd_courant<<<nblocks, dim3(BX, BY), 0, s>>>(L3, rk_step);
 }
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
   k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);

@@ -461,7 +461,7 @@ struct Ensemble {
       mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV]);
       if (rk_step == 3) {
         mark(PH_PD);
-        launch_pd_courant(l3, nb3, rk_step, stream);
+        launch_pd_courant(l2, nb2, rk_step, stream);
         launch_scalar_pd_update(LS(), nb_sc, nlev_max, rk_step, stream, tune[TU_PD]);
       }
       swap_species();

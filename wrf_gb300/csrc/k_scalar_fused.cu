@@ -181,39 +181,47 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L
 // j (pdc[1]) and the z face k of column (i, j) (pdc[2]), over the faces the
 // PD kernel's limiter region reads (columns its-1 .. itf+2, rows
 // jts-1 .. jtf+2), with the PD kernel's expressions (the same bits).
-// Point layout: one thread per (i, j, k) of the memory extent.
+// Column layout: one thread per (i, j) of the memory extent, levels in
+// chunks of four with their loads issued first.
 __global__ void __launch_bounds__(BX* BY) k_pd_courant(Launch L, int rk_step) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid || !m.pdc[0]) return;
-  const int i = bp.i, j = bp.j, k = bp.k;
+  const int i = bp.i, j = bp.j;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
-  if (i < m.its - 1 || i > itf + 2 || j < m.jts - 1 || j > jtf + 2 || k < m.kts) return;
+  if (i < m.its - 1 || i > itf + 2 || j < m.jts - 1 || j > jtf + 2) return;
   const Stage st = stage_of(m, rk_step);
   const float dt = st.dt_rk, rdx = m.rdx, rdy = m.rdy;
   const F2 mut = f2(m, WRFGPU_MUTS), msx = f2(m, WRFGPU_MSFTX), msy = f2(m, WRFGPU_MSFTY);
   const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
-  if (k <= ktf) {
-    const float c1k = c1(k), c2k = c2(k);
-    {  // x face
-      const float xdx = 2.f / (msy(i, j) + msy(i - 1, j)) / rdx;
-      const float mu = 0.5f * ((c1k * mut(i, j) + c2k) + (c1k * mut(i - 1, j) + c2k));
-      const float vel = f3(m, WRFGPU_RU_M)(i, k, j);
-      f3p(m, m.pdc[0])(i, k, j) = vel * dt / xdx / mu;
-    }
-    {  // y face
-      const float ydy = 2.f / (msx(i, j) + msx(i, j - 1)) / rdy;
-      const float mu = 0.5f * ((c1k * mut(i, j) + c2k) + (c1k * mut(i, j - 1) + c2k));
-      const float vel = f3(m, WRFGPU_RV_M)(i, k, j);
-      f3p(m, m.pdc[1])(i, k, j) = vel * dt / ydy / mu;
-    }
-  }
-  if (k > 1 && k < m.kde && k - 1 >= m.kms) {  // z face k
-    const float dz = 2.f / (rdzw(k) + rdzw(k - 1));
-    const float mu = 0.5f * ((c1(k) * mut(i, j) + c2(k)) + (c1(k) * mut(i, j) + c2(k)));
-    const float vel = f3(m, WRFGPU_WW_M)(i, k, j);
-    f3p(m, m.pdc[2])(i, k, j) = vel * dt / dz / mu;
-  }
+  const F3 ru = f3(m, WRFGPU_RU_M), rv = f3(m, WRFGPU_RV_M), rw = f3(m, WRFGPU_WW_M);
+  const F3 crx = f3p(m, m.pdc[0]), cry = f3p(m, m.pdc[1]), crz = f3p(m, m.pdc[2]);
+  const float mt = mut(i, j), mtx = mut(i - 1, j), mty = mut(i, j - 1);
+  const float xdx = 2.f / (msy(i, j) + msy(i - 1, j)) / rdx;
+  const float ydy = 2.f / (msx(i, j) + msx(i, j - 1)) / rdy;
+  const int klast = max(ktf, m.kde - 1);
+  struct V { float u, v, w; };
+  chunked_levels<4, V>(
+      m.kts, klast,
+      [&](int k, V& d) {
+        d.u = k <= ktf ? ru.ro(i, k, j) : 0.f;
+        d.v = k <= ktf ? rv.ro(i, k, j) : 0.f;
+        d.w = rw.ro(i, k, j);
+      },
+      [&](int k, const V& d) {
+        if (k <= ktf) {
+          const float c1k = c1(k), c2k = c2(k);
+          const float mux = 0.5f * ((c1k * mt + c2k) + (c1k * mtx + c2k));
+          crx(i, k, j) = d.u * dt / xdx / mux;
+          const float muy = 0.5f * ((c1k * mt + c2k) + (c1k * mty + c2k));
+          cry(i, k, j) = d.v * dt / ydy / muy;
+        }
+        if (k > 1 && k < m.kde && k - 1 >= m.kms) {  // z face k
+          const float dz = 2.f / (rdzw(k) + rdzw(k - 1));
+          const float muz = 0.5f * ((c1(k) * mt + c2(k)) + (c1(k) * mt + c2(k)));
+          crz(i, k, j) = d.w * dt / dz / muz;
+        }
+      });
 }
 
 // ------------------------------------------------------------------ PD
@@ -590,8 +598,8 @@ void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int
   else if (minb == 2) k_scalar_pd_update<2><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
   else k_scalar_pd_update<3><<<nblocks, PD_THREADS, bytes, s>>>(L, rk_step);
 }
-void launch_pd_courant(const Launch& L3, int nblocks, int rk_step, cudaStream_t s) {
-  k_pd_courant<<<nblocks, dim3(BX, BY), 0, s>>>(L3, rk_step);
+void launch_pd_courant(const Launch& L2, int nblocks, int rk_step, cudaStream_t s) {
+  k_pd_courant<<<nblocks, dim3(BX, BY), 0, s>>>(L2, rk_step);
 }
 void launch_swap_species(Mem* d_mems, int nmem, cudaStream_t s) {
   k_swap_species<<<(nmem + 63) / 64, 64, 0, s>>>(d_mems, nmem);

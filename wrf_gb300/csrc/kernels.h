@@ -100,8 +100,8 @@ void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s, int 
 
 // fused scalar transport (k_scalar_fused.cu): one block per (tile, species)
 void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var = TUNE_DEFAULT[TU_ADV]);
-// the face Courant numbers of the PD transport, once per step before it (point layout)
-void launch_pd_courant(const Launch& L3, int nblocks, int rk_step, cudaStream_t s);
+// the face Courant numbers of the PD transport, once per step before it (column layout)
+void launch_pd_courant(const Launch& L2, int nblocks, int rk_step, cudaStream_t s);
 // nlev_max: the largest kme - kms + 1 of the members (sizes a per-level table in shared memory)
 void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int rk_step, cudaStream_t s,
                              int var = TUNE_DEFAULT[TU_PD]);

@@ -68,7 +68,7 @@ struct alignas(16) Mem {
   int qamap[NSPMAX];
   const CUtensorMap* tmap;  // this member's tensor maps [NMAPSLOT][2] (device memory)
   double* wd[3];          // FP64 a/alpha/gamma of the mixed-precision form (or null)
-  float* pdc[3];          // Courant numbers of the PD transport's x, y, z faces (k_pd_courant)
+  float* pdc[6];          // PD transport's x, y, z faces: Courant numbers, then mu dx / dt (k_pd_courant)
   int nsp, n_moist;
   int ns_total;           // acoustic steps per large step
   int pad0;

@@ -242,7 +242,7 @@ struct Ensemble {
       b += (size_t)WRFGPU_N2D * al256(n2[m] * 4);
       b += (size_t)WRFGPU_N1D * al256(n1[m] * 4);
       b += al256(n3[m] * 4);  // limiter scratch
-      b += 3 * al256(n3[m] * 4);  // face Courant numbers of the PD transport
+      b += 6 * al256(n3[m] * 4);  // face Courant numbers and low-order factors of the PD transport
       if (fp64) b += 3 * al256(n3[m] * 8);
       off[m] = total;
       total += b;
@@ -278,7 +278,7 @@ struct Ensemble {
       for (int f = 0; f < WRFGPU_N2D; ++f) { M.f2[f] = (float*)p; p += al256(n2[m] * 4); }
       for (int f = 0; f < WRFGPU_N1D; ++f) { M.f1[f] = (float*)p; p += al256(n1[m] * 4); }
       scr[m] = (float*)p; p += al256(n3[m] * 4);
-      for (int q = 0; q < 3; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
+      for (int q = 0; q < 6; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
       if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
       M.ns_total = num_sound_steps(d);
       const WrfGpuScalars& s = d.scalars;

@@ -196,9 +196,11 @@ __global__ void __launch_bounds__(BX* BY) k_pd_courant(Launch L, int rk_step) {
   const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
   const F3 ru = f3(m, WRFGPU_RU_M), rv = f3(m, WRFGPU_RV_M), rw = f3(m, WRFGPU_WW_M);
   const F3 crx = f3p(m, m.pdc[0]), cry = f3p(m, m.pdc[1]), crz = f3p(m, m.pdc[2]);
+  const F3 lfx = f3p(m, m.pdc[3]), lfy = f3p(m, m.pdc[4]), lfz = f3p(m, m.pdc[5]);
   const float mt = mut(i, j), mtx = mut(i - 1, j), mty = mut(i, j - 1);
   const float xdx = 2.f / (msy(i, j) + msy(i - 1, j)) / rdx;
   const float ydy = 2.f / (msx(i, j) + msx(i, j - 1)) / rdy;
+  const float xdxt = xdx / dt, ydyt = ydy / dt;
   const int klast = max(ktf, m.kde - 1);
   struct V { float u, v, w; };
   chunked_levels<4, V>(
@@ -213,13 +215,16 @@ __global__ void __launch_bounds__(BX* BY) k_pd_courant(Launch L, int rk_step) {
           const float c1k = c1(k), c2k = c2(k);
           const float mux = 0.5f * ((c1k * mt + c2k) + (c1k * mtx + c2k));
           crx(i, k, j) = d.u * dt / xdx / mux;
+          lfx(i, k, j) = mux * xdxt;
           const float muy = 0.5f * ((c1k * mt + c2k) + (c1k * mty + c2k));
           cry(i, k, j) = d.v * dt / ydy / muy;
+          lfy(i, k, j) = muy * ydyt;
         }
         if (k > 1 && k < m.kde && k - 1 >= m.kms) {  // z face k
           const float dz = 2.f / (rdzw(k) + rdzw(k - 1));
           const float muz = 0.5f * ((c1(k) * mt + c2(k)) + (c1(k) * mt + c2(k)));
           crz(i, k, j) = d.w * dt / dz / muz;
+          lfz(i, k, j) = muz * (dz / dt);
         }
       });
 }
@@ -237,7 +242,7 @@ constexpr int PD_NPL = 4;    // q, q_old, ru_m, rv_m
 constexpr int PD_FSLOT = 3;  // face planes kept for three levels
 constexpr size_t PD_SMEM =
     (size_t)PD_RING * PD_NPL * HPLANE_BYTES +
-    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 3 * PDPlanes::GN + 2 * PDPlanes::SN) + PD_RING * 8;
+    4 * (PD_FSLOT * 2 * (PDPlanes::XN + PDPlanes::YN) + 2 * PDPlanes::SN) + PD_RING * 8;
 // One thread per limiter cell of the 34 x 10 region (tile + 1), plus one
 // thread per face the cells' left / bottom faces leave out (the 10 x faces of
 // column i0 + 33 and the 34 y faces of row j0 + 9): every thread computes at
@@ -259,17 +264,15 @@ struct ZCell {
 };
 
 // Column constants of level k, staged in shared memory once per block:
-// a = {c1h, c2h, rdnw, dz}, b = {dz / dt, fnm, fnp, 0}, with
-// dz = 2 / (rdnw(k) + rdnw(k-1)) for 1 < k < kde (else 0).
+// a = {c1h, c2h, rdnw, 0}, b = {0, fnm, fnp, 0}.
 struct LevelConst { float4 a, b; };
 
 // z face kk = L+1 of a limiter cell (advect_scalar_pd's fqz, fqzl).
-__device__ __forceinline__ void zface(const ZCell& c, int kk, const LevelConst& t, float cr, int kts, int kde, int ktf,
-                                      float* hi, float* lo) {
+__device__ __forceinline__ void zface(const ZCell& c, int kk, const LevelConst& t, float cr, float lf, int kts, int kde,
+                                      int ktf, float* hi, float* lo) {
   if (kk == 1 || kk == kde) { *hi = 0.f; *lo = 0.f; return; }
-  const float mu = 0.5f * ((t.a.x * c.mut + t.a.y) + (t.a.x * c.mut + t.a.y));
   const float vel = c.romp1;
-  const float l = mu * t.b.x * flux_upwind(c.fo0, c.fop1, cr);
+  const float l = lf * flux_upwind(c.fo0, c.fop1, cr);
   float h;
   if (kk == kts + 1 || kk == ktf) h = vel * (t.b.y * c.fp1 + t.b.z * c.f0);
   else h = vel * pflux3(c.fm1, c.f0, c.fp1, c.fp2, -vel);
@@ -298,9 +301,6 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   float* sXL = p; p += PD_FSLOT * P::XN;
   float* sYH = p; p += PD_FSLOT * P::YN;
   float* sYL = p; p += PD_FSLOT * P::YN;
-  float* sMUT = p; p += P::GN;
-  float* sMSX = p; p += P::GN;
-  float* sMSY = p; p += P::GN;
   float* sSC = p; p += 2 * P::SN;
   const int nlev = m.kme - m.kms + 1;
   LevelConst* sLV = reinterpret_cast<LevelConst*>(p); p += 8 * nlev;  // [k - kms]
@@ -320,31 +320,19 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
 
   F3 fld = f3p(m, m.q[s]), fold = f3p(m, m.qo[s]), out = f3p(m, m.qa[s]), rom = f3(m, WRFGPU_WW_M);
   const F3 crxa = f3p(m, m.pdc[0]), crya = f3p(m, m.pdc[1]), crza = f3p(m, m.pdc[2]);
+  const F3 lfxa = f3p(m, m.pdc[3]), lfya = f3p(m, m.pdc[4]), lfza = f3p(m, m.pdc[5]);
   F2 mut2 = f2(m, WRFGPU_MUTS), msx2 = f2(m, WRFGPU_MSFTX), msy2 = f2(m, WRFGPU_MSFTY);
   F2 mub2 = f2(m, WRFGPU_MUB), mu1 = f2(m, WRFGPU_MU_1), mu2 = f2(m, WRFGPU_MU_2);
-  auto in_mem = [&](int ii, int jj) { return ii >= m.ims && ii <= m.ime && jj >= m.jms && jj <= m.jme; };
   {
     F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H), rdzw = f1(m, WRFGPU_RDNW);
     F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP);
     for (int q = tid; q < nlev; q += PD_THREADS) {
       const int k = m.kms + q;
-      float dz = 0.f, dzdt = 0.f;
-      if (k > 1 && k < m.kde && k - 1 >= m.kms) { dz = 2.f / (rdzw(k) + rdzw(k - 1)); dzdt = dz / dt; }
-      sLV[q].a = make_float4(c1(k), c2(k), rdzw(k), dz);
-      sLV[q].b = make_float4(dzdt, fzm(k), fzp(k), 0.f);
+      sLV[q].a = make_float4(c1(k), c2(k), rdzw(k), 0.f);
+      sLV[q].b = make_float4(0.f, fzm(k), fzp(k), 0.f);
     }
   }
-
-  // 2-D planes (halo 2)
-  for (int q = tid; q < P::GN; q += PD_THREADS) {
-    const int r = q / P::GW, c = q - r * P::GW;
-    const int ii = i0 - 2 + c, jj = j0 - 2 + r;
-    const bool okm = in_mem(ii, jj);
-    sMUT[q] = okm ? mut2(ii, jj) : 0.f;
-    sMSX[q] = okm ? msx2(ii, jj) : 1.f;
-    sMSY[q] = okm ? msy2(ii, jj) : 1.f;
-  }
-  __syncthreads();
+  __syncthreads();  // the level table is complete
 
   // this thread's limiter cell (sx, sy) of the region, and its faces
   const bool has_cell = tid < P::SN;
@@ -358,21 +346,16 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     if (q < P::XH) xq = q * P::XW + (P::XW - 1);     // column i0 + TX + 1
     else yq = (P::YH - 1) * P::YW + (q - P::XH);     // row j0 + TY + 1
   }
-  // level-independent data of the faces: halo-plane offset, dx, and the
-  // column masses on either side (mut of the face's two cells)
+  // level-independent data of the faces: the face's point and its offset in
+  // the halo plane
   bool xok = false, yok = false;
   int xo = 0, yo = 0, xii = 0, xjj = 0, yii = 0, yjj = 0;
-  float xdx = 0.f, xdxt = 0.f, ydy = 0.f, ydyt = 0.f, xma = 0.f, xmb = 0.f, yma = 0.f, ymb = 0.f;
   if (xq >= 0) {
     const int r = xq / P::XW, c = xq - r * P::XW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     xok = ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1;
     xii = ii; xjj = jj;
     xo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
-    const int xg = (r + 1) * P::GW + (c + 1);
-    xdx = 2.f / (sMSY[xg] + sMSY[xg - 1]) / rdx;
-    xdxt = xdx / dt;
-    xma = sMUT[xg]; xmb = sMUT[xg - 1];
   }
   if (yq >= 0) {
     const int r = yq / P::YW, c = yq - r * P::YW;
@@ -380,10 +363,6 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     yok = ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2;
     yii = ii; yjj = jj;
     yo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
-    const int yg = (r + 1) * P::GW + (c + 1);
-    ydy = 2.f / (sMSX[yg] + sMSX[yg - P::GW]) / rdy;
-    ydyt = ydy / dt;
-    yma = sMUT[yg]; ymb = sMUT[yg - P::GW];
   }
 
   // the limiter cell's vertical window
@@ -436,9 +415,10 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     if (Lv <= ktf) {
       // this thread's faces' Courant numbers (k_pd_courant), loaded before
       // the ring wait so that their latency overlaps it
-      const float crx = xok ? crxa.ro(xii, Lv, xjj) : 0.f;
-      const float cry = yok ? crya.ro(yii, Lv, yjj) : 0.f;
-      const float crz = (c.valid && Lv + 1 > 1 && Lv + 1 < m.kde) ? crza.ro(c.i, Lv + 1, c.j) : 0.f;
+      const float crx = xok ? crxa.ro(xii, Lv, xjj) : 0.f, lfx = xok ? lfxa.ro(xii, Lv, xjj) : 0.f;
+      const float cry = yok ? crya.ro(yii, Lv, yjj) : 0.f, lfy = yok ? lfya.ro(yii, Lv, yjj) : 0.f;
+      const bool zin = c.valid && Lv + 1 > 1 && Lv + 1 < m.kde;
+      const float crz = zin ? crza.ro(c.i, Lv + 1, c.j) : 0.f, lfz = zin ? lfza.ro(c.i, Lv + 1, c.j) : 0.f;
       if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
       const float4 tl = sLV[Lv - m.kms].a;
       c1k = tl.x; c2k = tl.y; rdzwk = tl.z;
@@ -456,10 +436,8 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         float hi = 0.f, lo = 0.f;
         if (xok) {
           const int o = xo;
-          const float mu = 0.5f * ((c1k * xma + c2k) + (c1k * xmb + c2k));
           const float vel = RU[o];
-          const float cr = crx;
-          lo = mu * xdxt * flux_upwind(FO[o - 1], FO[o], cr);
+          lo = lfx * flux_upwind(FO[o - 1], FO[o], crx);
           const float h = vel * pflux5(F[o - 3], F[o - 2], F[o - 1], F[o], F[o + 1], F[o + 2], vel);
           hi = h - lo;
         }
@@ -469,17 +447,15 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         float hi = 0.f, lo = 0.f;
         if (yok) {
           const int o = yo;
-          const float mu = 0.5f * ((c1k * yma + c2k) + (c1k * ymb + c2k));
           const float vel = RV[o];
-          const float cr = cry;
-          lo = mu * ydyt * flux_upwind(FO[o - HW], FO[o], cr);
+          lo = lfy * flux_upwind(FO[o - HW], FO[o], cry);
           const float h = vel * pflux5(F[o - 3 * HW], F[o - 2 * HW], F[o - HW], F[o], F[o + HW], F[o + 2 * HW], vel);
           hi = h - lo;
         }
         YH[yq] = hi; YL[yq] = lo;
       }
       // ---- vertical face Lv+1 of this thread's limiter cell
-      if (c.valid) zface(c, Lv + 1, sLV[Lv + 1 - m.kms], crz, kts, m.kde, ktf, &c.hz1, &c.lz1);
+      if (c.valid) zface(c, Lv + 1, sLV[Lv + 1 - m.kms], crz, lfz, kts, m.kde, ktf, &c.hz1, &c.lz1);
     }
     __syncthreads();
     if (Lv <= ktf) {

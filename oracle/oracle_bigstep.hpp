@@ -633,4 +633,154 @@ void calc_p_rho_phi(R* qv_p, int n_moist_species, int hypsometric_opt, R* al_p, 
   }
 }
 
+// module_big_step_utilities_em.F:6220-6636 sixth_order_diffusion: Xue's
+// sixth-order flux, dropped where it runs up-gradient (diff_6th_opt = 2),
+// tapered over steep terrain (diff_6th_slopeopt >= 1), weighted by the column
+// mass, added to `tendency`.  name: 'u', 'v', 'w' or 'm' (mass-point
+// scalars).  The loop limits are those of periodic / symmetric boundaries
+// (:6330-6443 without the open / specified branches).
+template <typename R>
+void sixth_order_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R dt, const WrfDynConfig& cf, R* c1_p,
+                           R* c2_p, R* phb_p, R rdx, R rdy, R* msftx_p, R* msfty_p, R* msfux_p, R* msfuy_p,
+                           R* msfvx_p, R* msfvy_p, const Dims& d) {
+  A3<R> field(field_p, d), tendency(tendency_p, d), phb(phb_p, d);
+  A2<R> mut(mut_p, d), msftx(msftx_p, d), msfty(msfty_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d),
+      msfvx(msfvx_p, d), msfvy(msfvy_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d);
+  const R coef = R(cf.diff_6th_factor) * R(0.015625) / (R(2.0) * dt);
+  const int ktf = std::min(d.kte, d.kde - 1);
+  int i_end = std::min(d.ide - 1, d.ite), j_end = std::min(d.jde - 1, d.jte), k_start = d.kts;
+  if (name == 'u') i_end = d.ite;
+  if (name == 'v') j_end = d.jte;
+  if (name == 'w') k_start = d.kts + 1;
+  auto mass = [&](int k, int i, int j) { return c1(k) * mut(i, j) + c2(k); };
+  // the sixth-order flux through the face between f(-1) and f(0) of a row
+  auto flux6 = [](R fm3, R fm2, R fm1, R f0, R fp1, R fp2) {
+    return R(10.0) * (f0 - fm1) - R(5.0) * (fp1 - fm2) + (fp2 - fm3);
+  };
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = k_start; k <= ktf; ++k)
+      for (int i = d.its; i <= i_end; ++i) {
+        // x
+        R fx0 = flux6(field(i - 3, k, j), field(i - 2, k, j), field(i - 1, k, j), field(i, k, j), field(i + 1, k, j),
+                      field(i + 2, k, j));
+        R fx1 = flux6(field(i - 2, k, j), field(i - 1, k, j), field(i, k, j), field(i + 1, k, j), field(i + 2, k, j),
+                      field(i + 3, k, j));
+        if (cf.diff_6th_opt == 2) {
+          if (fx0 * (field(i, k, j) - field(i - 1, k, j)) <= R(0.)) fx0 = R(0.);
+          if (fx1 * (field(i + 1, k, j) - field(i, k, j)) <= R(0.)) fx1 = R(0.);
+        }
+        R sd0 = R(1.), sd1 = R(1.);
+        if (cf.diff_6th_slopeopt >= 1) {
+          const R dx = R(1.) / rdx;
+          const R thresh = R(cf.diff_6th_thresh) * R(9.81) * dx;
+          R z0, z1;
+          if (name == 'u') {
+            z0 = std::max(std::fabs(phb(i, k, j) - phb(i - 1, k, j)) * msfux(i, j),
+                          std::fabs(phb(i - 1, k, j) - phb(i - 2, k, j)) * msfux(i - 1, j));
+            z1 = std::max(std::fabs(phb(i + 1, k, j) - phb(i, k, j)) * msfux(i + 1, j),
+                          std::fabs(phb(i, k, j) - phb(i - 1, k, j)) * msfux(i, j));
+          } else if (name == 'v') {
+            z0 = std::max(std::fabs(phb(i, k, j) - phb(i - 1, k, j)) * msfux(i, j),
+                          std::fabs(phb(i, k, j - 1) - phb(i - 1, k, j - 1)) * msfux(i, j - 1));
+            z1 = std::max(std::fabs(phb(i + 1, k, j) - phb(i, k, j)) * msfux(i + 1, j),
+                          std::fabs(phb(i + 1, k, j - 1) - phb(i, k, j - 1)) * msfux(i + 1, j - 1));
+          } else {
+            z0 = std::fabs(phb(i, k, j) - phb(i - 1, k, j)) * msfux(i, j);
+            z1 = std::fabs(phb(i + 1, k, j) - phb(i, k, j)) * msfux(i + 1, j);
+          }
+          sd0 = std::max(R(1.) - (z0 / thresh), R(0.));
+          sd1 = std::max(R(1.) - (z1 / thresh), R(0.));
+        }
+        R m0, m1, msf;
+        if (name == 'u') {
+          m0 = mass(k, i - 1, j); m1 = mass(k, i, j); msf = msfux(i, j);
+        } else if (name == 'v') {
+          m0 = R(0.25) * (mass(k, i - 1, j - 1) + mass(k, i, j - 1) + mass(k, i - 1, j) + mass(k, i, j));
+          m1 = R(0.25) * (mass(k, i, j - 1) + mass(k, i + 1, j - 1) + mass(k, i, j) + mass(k, i + 1, j));
+          msf = msfvx(i, j);
+        } else {
+          m0 = R(0.5) * (mass(k, i - 1, j) + mass(k, i, j));
+          m1 = R(0.5) * (mass(k, i, j) + mass(k, i + 1, j));
+          msf = msftx(i, j);
+        }
+        const R tx = coef * msf * ((sd1 * m1 * fx1) - (sd0 * m0 * fx0));
+        // y
+        R fy0 = flux6(field(i, k, j - 3), field(i, k, j - 2), field(i, k, j - 1), field(i, k, j), field(i, k, j + 1),
+                      field(i, k, j + 2));
+        R fy1 = flux6(field(i, k, j - 2), field(i, k, j - 1), field(i, k, j), field(i, k, j + 1), field(i, k, j + 2),
+                      field(i, k, j + 3));
+        if (cf.diff_6th_opt == 2) {
+          if (fy0 * (field(i, k, j) - field(i, k, j - 1)) <= R(0.)) fy0 = R(0.);
+          if (fy1 * (field(i, k, j + 1) - field(i, k, j)) <= R(0.)) fy1 = R(0.);
+        }
+        sd0 = R(1.); sd1 = R(1.);
+        if (cf.diff_6th_slopeopt >= 1) {
+          const R dy = R(1.) / rdy;
+          const R thresh = R(cf.diff_6th_thresh) * R(9.81) * dy;
+          R z0, z1;
+          if (name == 'u') {
+            z0 = std::max(std::fabs(phb(i, k, j) - phb(i, k, j - 1)) * msfvy(i, j),
+                          std::fabs(phb(i - 1, k, j) - phb(i - 1, k, j - 1)) * msfvy(i - 1, j));
+            z1 = std::max(std::fabs(phb(i, k, j + 1) - phb(i, k, j)) * msfvy(i, j + 1),
+                          std::fabs(phb(i - 1, k, j + 1) - phb(i - 1, k, j)) * msfvy(i - 1, j + 1));
+          } else if (name == 'v') {
+            z0 = std::max(std::fabs(phb(i, k, j) - phb(i, k, j - 1)) * msfvy(i, j),
+                          std::fabs(phb(i, k, j - 1) - phb(i, k, j - 2)) * msfvy(i, j - 1));
+            z1 = std::max(std::fabs(phb(i, k, j + 1) - phb(i, k, j)) * msfvy(i, j + 1),
+                          std::fabs(phb(i, k, j) - phb(i, k, j - 1)) * msfvy(i, j));
+          } else {
+            z0 = std::fabs(phb(i, k, j) - phb(i, k, j - 1)) * msfvy(i, j);
+            z1 = std::fabs(phb(i, k, j + 1) - phb(i, k, j)) * msfvy(i, j + 1);
+          }
+          sd0 = std::max(R(1.) - (z0 / thresh), R(0.));
+          sd1 = std::max(R(1.) - (z1 / thresh), R(0.));
+        }
+        if (name == 'u') {
+          m0 = R(0.25) * (mass(k, i - 1, j - 1) + mass(k, i, j - 1) + mass(k, i - 1, j) + mass(k, i, j));
+          m1 = R(0.25) * (mass(k, i - 1, j) + mass(k, i, j) + mass(k, i - 1, j + 1) + mass(k, i, j + 1));
+          msf = msfuy(i, j);
+        } else if (name == 'v') {
+          m0 = mass(k, i, j - 1); m1 = mass(k, i, j); msf = msfvy(i, j);
+        } else {
+          m0 = R(0.5) * (mass(k, i, j - 1) + mass(k, i, j));
+          m1 = R(0.5) * (mass(k, i, j) + mass(k, i, j + 1));
+          msf = msfty(i, j);
+        }
+        const R ty = coef * msf * ((sd1 * m1 * fy1) - (sd0 * m0 * fy0));
+        tendency(i, k, j) = tendency(i, k, j) + tx + ty;
+      }
+}
+
+// module_em.F:959-1092 rk_addtend_dry for the forward-in-time tendencies this
+// path forms (ru_tendf .. t_tendf: the sixth-order diffusion).  With physics
+// off the saved tendencies (u_save .. t_save, ph_save), h_diabatic, ph_tendf
+// and mu_tendf are zero: the stage-1 "tendf + save * msf" steps add +0 to a
+// tendency that is never -0, and the ph / mu additions are left out; the
+// h_diabatic term of theta is kept, as it can turn a -0 sum into +0.
+template <typename R>
+void rk_addtend_dry(R* ru_tend_p, R* rv_tend_p, R* rw_tend_p, R* t_tend_p, R* ru_tendf_p, R* rv_tendf_p,
+                    R* rw_tendf_p, R* t_tendf_p, R* c1_p, R* c2_p, R* mut_p, R* msfty_p, R* msfuy_p,
+                    R* msfvx_inv_p, const Dims& d) {
+  A3<R> ru_tend(ru_tend_p, d), rv_tend(rv_tend_p, d), rw_tend(rw_tend_p, d), t_tend(t_tend_p, d),
+      ru_tendf(ru_tendf_p, d), rv_tendf(rv_tendf_p, d), rw_tendf(rw_tendf_p, d), t_tendf(t_tendf_p, d);
+  A2<R> mut(mut_p, d), msfty(msfty_p, d), msfuy(msfuy_p, d), msfvx_inv(msfvx_inv_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d);
+  const int i_end = std::min(d.ite, d.ide - 1), j_end = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = d.kts; k <= d.kte - 1; ++k)
+      for (int i = d.its; i <= d.ite; ++i) ru_tend(i, k, j) = ru_tend(i, k, j) + ru_tendf(i, k, j) / msfuy(i, j);
+  for (int j = d.jts; j <= d.jte; ++j)
+    for (int k = d.kts; k <= d.kte - 1; ++k)
+      for (int i = d.its; i <= i_end; ++i) rv_tend(i, k, j) = rv_tend(i, k, j) + rv_tendf(i, k, j) * msfvx_inv(i, j);
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = d.kts; k <= d.kte; ++k)
+      for (int i = d.its; i <= i_end; ++i) rw_tend(i, k, j) = rw_tend(i, k, j) + rw_tendf(i, k, j) / msfty(i, j);
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = d.kts; k <= d.kte - 1; ++k)
+      for (int i = d.its; i <= i_end; ++i)
+        t_tend(i, k, j) = t_tend(i, k, j) + t_tendf(i, k, j) / msfty(i, j) +
+                          (c1(k) * mut(i, j) + c2(k)) * R(0.) / msfty(i, j);
+}
+
 }  // namespace wrforacle

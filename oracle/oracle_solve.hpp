@@ -91,6 +91,7 @@ struct Domain {
   int n_moist = 1, n_scalar = 0;
   std::vector<std::vector<R>> f3, f2, f1;   // indexed by WrfGpuFieldId ranges
   std::vector<std::vector<R>> qs;           // moist then passive: [2*s] current, [2*s+1] old
+  std::vector<std::vector<R>> tendf;        // ru_tendf, rv_tendf, rw_tendf, t_tendf (diff_6th_opt != 0)
   long n3 = 0, n2 = 0, n1 = 0;
   int nthreads = 1;
   R max_vert_cfl = 0, max_horiz_cfl = 0;
@@ -112,6 +113,7 @@ struct Domain {
     f2.assign(WRFGPU_N2D, std::vector<R>(n2, R(0)));
     f1.assign(WRFGPU_N1D, std::vector<R>(n1, R(0)));
     qs.assign(2 * (n_moist + n_scalar), std::vector<R>(n3, R(0)));
+    tendf.assign(cf.diff_6th_opt != 0 ? 4 : 0, std::vector<R>(n3, R(0)));
   }
   R* p3(int id) { return f3[id].data(); }
   R* p2(int id) { return f2[id - WRFGPU_F2D_BASE].data(); }
@@ -195,8 +197,13 @@ struct Domain {
       bc2(WRFGPU_MUU, 'u'); bc2(WRFGPU_MUV, 'v'); bc2(WRFGPU_MUT, 't');
       bc3(WRFGPU_AL, 'p'); bc3(WRFGPU_PH_2, 'w');
 
-      // rk_tendency (module_em.F:370-781); rk_addtend_dry then adds zero physics tendencies.
+      // rk_tendency (module_em.F:370-781); rk_addtend_dry then adds the
+      // forward-in-time tendencies formed at stage 1 (the sixth-order
+      // diffusion; zero physics tendencies otherwise).
       std::vector<R> tmv(64, R(0)), tmh(64, R(0));
+      const bool diff6 = cf.diff_6th_opt != 0;
+      if (diff6 && rk_step == 1)
+        for (auto& t : tendf) std::fill(t.begin(), t.end(), R(0));
       tiles([&](const Dims& td) {
         zero_tend(p3(WRFGPU_RU_TEND), td); zero_tend(p3(WRFGPU_RV_TEND), td); zero_tend(p3(WRFGPU_RW_TEND), td);
         zero_tend(p3(WRFGPU_T_TEND), td); zero_tend(p3(WRFGPU_PH_TEND), td);
@@ -251,8 +258,26 @@ struct Domain {
                   p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), cf, p2(WRFGPU_MSFUX),
                   p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
                   (R*)nullptr, p1(WRFGPU_FNM), p1(WRFGPU_FNP), rdx, rdy, td);
+        if (diff6 && rk_step == 1) {
+          // module_em.F:879-932, with the state of stage 1
+          const int fld[4] = {WRFGPU_U_2, WRFGPU_V_2, WRFGPU_W_2, WRFGPU_T_2};
+          const char nm[4] = {'u', 'v', 'w', 'm'};
+          for (int q = 0; q < 4; ++q) {
+            const bool wl = q == 2;  // w sits on full levels
+            sixth_order_diffusion(nm[q], p3(fld[q]), tendf[q].data(), p2(WRFGPU_MUT), dt, cf,
+                                  p1(wl ? WRFGPU_C1F : WRFGPU_C1H), p1(wl ? WRFGPU_C2F : WRFGPU_C2H), p3(WRFGPU_PHB),
+                                  rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY),
+                                  p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
+          }
+        }
       });
       for (int t = 0; t < 64; ++t) { mvc = std::max(mvc, tmv[t]); mhc = std::max(mhc, tmh[t]); }
+      if (diff6)
+        tiles([&](const Dims& td) {
+          rk_addtend_dry(p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), p3(WRFGPU_T_TEND),
+                         tendf[0].data(), tendf[1].data(), tendf[2].data(), tendf[3].data(), p1(WRFGPU_C1H),
+                         p1(WRFGPU_C2H), p2(WRFGPU_MUT), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX_INV), td);
+        });
 
       tiles([&](const Dims& td) {
         small_step_prep(p3(WRFGPU_U_1), p3(WRFGPU_U_2), p3(WRFGPU_V_1), p3(WRFGPU_V_2), p3(WRFGPU_W_1),

@@ -576,3 +576,60 @@ def test_batched_mixed_options_equals_plain(gpulib):
         for nm in STATE_FIELDS:
             fid = abi.FIELD_ID[nm]
             assert np.array_equal(ens.get(m, fid), d.get(0, fid)), (m, nm)
+
+
+def diffusion_case(opt, slopeopt):
+    """Sixth-order diffusion of the dry state (species mixing off) on the
+    small case with a 60 m/s wave in u over 8 points."""
+    case = cases.small_case(nx=16, ny=12, kde=20, n_scalar=1, seed=23)
+    F = case.fields
+    ni = F["u_2"].shape[-1]
+    pert = (60.0 * np.sin(2 * np.pi * np.arange(ni) / 8.0)).astype(F["u_2"].dtype)
+    for nm in ("u_1", "u_2"):
+        F[nm][...] = F[nm] + pert
+    c = case.desc.config
+    c.diff_6th_opt = opt
+    c.diff_6th_slopeopt = slopeopt
+    c.diff_6th_factor = 0.12
+    c.diff_6th_thresh = 0.10
+    c.moist_mix6_off = 1
+    c.scalar_mix6_off = 1
+    return case
+
+
+@pytest.mark.parametrize("opt,slopeopt", [(1, 0), (2, 0), (2, 1)])
+def test_full_step_bitwise_diff_6th(gpulib, opt, slopeopt):
+    """Sixth-order diffusion of u, v, w and theta at stage 1
+    (module_big_step_utilities_em.F:6220-6636) added at every stage by
+    rk_addtend_dry (module_em.F:959-1092): bit for bit with the oracle over
+    two steps, and active (the oracle's state differs from its
+    diff_6th_opt = 0 run)."""
+    case = diffusion_case(opt, slopeopt)
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(2)
+    ge.step(2)
+    ge.sync()
+    bad = []
+    for nm in STATE_FIELDS:
+        fid = abi.FIELD_ID[nm]
+        a = interior(case, fid, ge.get(0, fid), halo=3)
+        b = interior(case, fid, od.get(fid), halo=3)
+        d = max_abs(a, b)
+        if d != 0.0:
+            bad.append("%s: max|diff| %.3e serr %.2e" % (nm, d, serr(a, b)))
+    assert not bad, "\n".join(bad)
+    case.desc.config.diff_6th_opt = 0
+    o0 = OracleDomain(case, "f32")
+    o0.step(2)
+    fid = abi.FIELD_ID["u_2"]
+    assert max_abs(interior(case, fid, o0.get(fid), halo=3), interior(case, fid, od.get(fid), halo=3)) > 0
+
+
+def test_diff_6th_species_mixing_refused(gpulib):
+    """The species' sixth-order diffusion is not built: a member that asks for
+    it is refused at creation."""
+    case = diffusion_case(2, 0)
+    case.desc.config.moist_mix6_off = 0
+    with pytest.raises(G.WrfGpuError):
+        G.Domain(case)

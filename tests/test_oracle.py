@@ -279,3 +279,50 @@ def test_f32_tracks_f64():
         assert e < 1e-3
         assert e >= 0.2 * prev
         prev = e
+
+
+# ---------------------------------------------------------------------------
+# sixth-order numerical diffusion (diff_6th_opt)
+# ---------------------------------------------------------------------------
+def _theta_wave_case(opt, amp=0.5):
+    """The rest state plus a 2 dx wave of theta along x (12 columns, periodic)."""
+    case = rest_case()
+    F = case.fields
+    ni = F["t_2"].shape[-1]
+    wave = (amp * (-1.0) ** np.arange(ni)).astype(F["t_2"].dtype)
+    for nm in ("t_1", "t_2"):
+        F[nm][...] = F[nm] + wave
+    c = case.desc.config
+    c.diff_6th_opt = opt
+    c.diff_6th_factor = 0.12
+    c.moist_mix6_off = 1
+    c.scalar_mix6_off = 1
+    return case
+
+
+@pytest.mark.parametrize("opt", [1, 2])
+def test_sixth_order_diffusion_damps_2dx_wave(opt):
+    """For a 2 dx wave of amplitude A the sixth-order flux is +-32 A at every
+    face (module_big_step_utilities_em.F:6455-6461) and runs down-gradient
+    (diff_6th_opt = 2 keeps it), so the stage-1 tendency is
+    -(diff_6th_factor / (2 dt)) (c1 mut + c2) A and one large step scales the
+    wave by 1 - diff_6th_factor / 2 relative to the undiffused step."""
+    amp = {}
+    for o in (0, opt):
+        case = _theta_wave_case(o)
+        od = OracleDomain(case, "f64")
+        od.step(1)
+        t = mass_interior(case, od.get(abi.FIELD_ID["t_2"]))
+        sign = (-1.0) ** np.arange(t.shape[-1])
+        amp[o] = abs(float(np.mean(t * sign)))
+    assert amp[0] > 0.45
+    assert abs(amp[opt] / amp[0] - (1.0 - 0.12 / 2)) < 0.01
+
+
+def test_sixth_order_diffusion_of_species_is_refused():
+    """Species diffusion is not restated: the oracle refuses it, as the
+    library does (WRFGPU_E_ARG)."""
+    case = _theta_wave_case(1)
+    case.desc.config.moist_mix6_off = 0
+    with pytest.raises(Exception):
+        OracleDomain(case, "f64")

@@ -39,7 +39,10 @@ class WrfDynConfig(C.Structure):
         "moist_adv_opt", "scalar_adv_opt",
         "non_hydrostatic", "top_lid", "use_theta_m", "hypsometric_opt", "phi_adv_z",
         "w_damping", "damp_opt", "diff_opt", "zadvect_implicit", "map_proj",
-        "time_step_sound")] + [("w_crit_cfl", C.c_float), ("dampcoef", C.c_float), ("zdamp", C.c_float)]
+        "time_step_sound")] + [("w_crit_cfl", C.c_float), ("dampcoef", C.c_float), ("zdamp", C.c_float),
+                               ("diff_6th_opt", C.c_int32), ("diff_6th_slopeopt", C.c_int32),
+                               ("diff_6th_factor", C.c_float), ("diff_6th_thresh", C.c_float),
+                               ("moist_mix6_off", C.c_int32), ("scalar_mix6_off", C.c_int32)]
 
 
 class WrfGpuScalars(C.Structure):
@@ -137,4 +140,10 @@ def default_config(periodic_x=True, periodic_y=True, symmetric_y=False):
     c.w_crit_cfl = 1.0
     c.dampcoef = 0.2
     c.zdamp = 5000.0
+    c.diff_6th_opt = 0
+    c.diff_6th_slopeopt = 0
+    c.diff_6th_factor = 0.12
+    c.diff_6th_thresh = 0.10
+    c.moist_mix6_off = 0
+    c.scalar_mix6_off = 0
     return c

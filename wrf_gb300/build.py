@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(HERE, "libwrfgpu.so")
 
-SOURCES = ["k_prep.cu", "k_bc.cu", "k_tend.cu", "k_tend_col.cu", "k_small.cu", "k_scalar.cu", "k_scalar_fused.cu", "fortran_abi.cu", "k_acoustic_col.cu", "driver.cu", "noalloc.cu"]
+SOURCES = ["k_prep.cu", "k_bc.cu", "k_tend.cu", "k_tend_col.cu", "k_small.cu", "k_scalar.cu", "k_scalar_fused.cu", "fortran_abi.cu", "k_acoustic_col.cu", "k_diff.cu", "driver.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "--expt-relaxed-constexpr", "-Xptxas", "-O3"]

@@ -69,6 +69,7 @@ struct alignas(16) Mem {
   const CUtensorMap* tmap;  // this member's tensor maps [NMAPSLOT][2] (device memory)
   double* wd[3];          // FP64 a/alpha/gamma of the mixed-precision form (or null)
   float* pdc[6];          // PD transport's x, y, z faces: Courant numbers, then mu dx / dt (k_pd_courant)
+  float* tendf[4];        // ru_tendf, rv_tendf, rw_tendf, t_tendf of the sixth-order diffusion (or null)
   int nsp, n_moist;
   int ns_total;           // acoustic steps per large step
   int pad0;

@@ -46,13 +46,13 @@ namespace wrfgpu {
 enum Phase {
   PH_PREP = 0, PH_FILL, PH_TEND_U, PH_TEND_V, PH_TEND_W, PH_TEND_T, PH_TEND_PH, PH_CFL, PH_SSP, PH_CPR0,
   PH_COEFW, PH_AUV, PH_AMUT, PH_AW, PH_SUMF, PH_SSF, PH_USPD, PH_PD, PH_ADVS, PH_UPDS, PH_CPRP, PH_WSURF,
-  PH_END, NPHASE
+  PH_DIFF, PH_END, NPHASE
 };
 static const char* PHASE_NAMES[NPHASE] = {
     "step_prep", "bc_fill", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",
     "small_step_prep", "calc_p_rho_0", "calc_coef_w", "advance_uv", "advance_mu_t", "advance_w",
     "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "scalar_pd_update", "scalar_adv_update",
-    "rk_update_scalar", "calc_p_rho_phi", "set_w_surface", "end"};
+    "rk_update_scalar", "calc_p_rho_phi", "set_w_surface", "sixth_order_diffusion", "end"};
 
 static int check_desc(const WrfGpuDomainDesc& d) {
   const WrfDynConfig& c = d.config;
@@ -63,6 +63,9 @@ static int check_desc(const WrfGpuDomainDesc& d) {
     return WRFGPU_E_ARG;
   if (!c.non_hydrostatic || c.zadvect_implicit != 0 || (c.damp_opt != 0 && c.damp_opt != 3) || (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
     return WRFGPU_E_ARG;
+  // sixth-order diffusion of the dry state; the species' is not built
+  if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) return WRFGPU_E_ARG;
+  if (c.diff_6th_opt != 0 && !(c.moist_mix6_off && c.scalar_mix6_off)) return WRFGPU_E_ARG;
   if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
   if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;
   if (c.open_xs || c.open_xe || c.open_ys || c.open_ye || c.specified || c.nested || c.polar) return WRFGPU_E_ARG;
@@ -118,6 +121,7 @@ struct Ensemble {
   int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0, nlev_max = 0;
   bool damp3 = false;  // some member uses damp_opt = 3
+  bool diff6 = false;  // some member uses diff_6th_opt != 0
   std::vector<size_t> n3, n2, n1;      // element counts per member (padded rows)
   std::vector<size_t> ni_, nk_, nj_, pitch_;  // Fortran extents and the padded row pitch
   CUtensorMap* d_tmaps = nullptr;      // [nmem][NMAPSLOT][2]
@@ -244,6 +248,7 @@ struct Ensemble {
       b += al256(n3[m] * 4);  // limiter scratch
       b += 6 * al256(n3[m] * 4);  // face Courant numbers and low-order factors of the PD transport
       if (fp64) b += 3 * al256(n3[m] * 8);
+      if (d.config.diff_6th_opt != 0) b += 4 * al256(n3[m] * 4);  // ru_tendf, rv_tendf, rw_tendf, t_tendf
       off[m] = total;
       total += b;
     }
@@ -280,6 +285,8 @@ struct Ensemble {
       scr[m] = (float*)p; p += al256(n3[m] * 4);
       for (int q = 0; q < 6; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
       if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
+      if (d.config.diff_6th_opt != 0)  // zero outside the diffusion's loop limits (the pool is cleared)
+        for (int q = 0; q < 4; ++q) { M.tendf[q] = (float*)p; p += al256(n3[m] * 4); }
       M.ns_total = num_sound_steps(d);
       const WrfGpuScalars& s = d.scalars;
       M.dt = (float)s.dt; M.rdx = (float)s.rdx; M.rdy = (float)s.rdy;
@@ -293,6 +300,7 @@ struct Ensemble {
       ns_max = std::max(ns_max, M.ns_total);
       nlev_max = std::max(nlev_max, M.kme - M.kms + 1);
       damp3 = damp3 || M.cf.damp_opt == 3;
+      diff6 = diff6 || M.cf.diff_6th_opt != 0;
       bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
       bss[m + 1] = bss[m] + tiles_x(M) * tiles_y(M) * M.nsp;
@@ -420,6 +428,11 @@ struct Ensemble {
       mark(PH_TEND_W); launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
+      if (diff6) {  // module_em.F:879-932 (stage 1), then rk_addtend_dry (solve_em.F:967)
+        mark(PH_DIFF);
+        if (rk_step == 1) launch_sixth_diff(l3, nb3, stream);
+        launch_addtend_dry(l3, nb3, stream);
+      }
       if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream, tune[TU_CFL]); }
       // small_step_prep, calc_p_rho(step 0), calc_coef_w (solve_em.F:1089-1140)
       mark(PH_SSP); launch_small_step_prep(l2, nb2, LST(), nb_st, a, stream, tune[TU_SSP]);

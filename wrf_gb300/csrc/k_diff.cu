@@ -1,0 +1,207 @@
+// Sixth-order numerical diffusion of the dry state at the first RK stage
+// (sixth_order_diffusion, dyn_em/module_big_step_utilities_em.F:6220-6636,
+// called from rk_tendency's forward step, dyn_em/module_em.F:879-932) and
+// the addition of those forward-in-time tendencies to the large-step
+// tendencies at every stage (rk_addtend_dry, dyn_em/module_em.F:959-1092).
+//
+// Both are point kernels over (i, j) x level blocks.  The diffusion runs once
+// per large step on inputs that L2 holds for its 7-point stencils; the
+// addition is one read of the stored tendency per point and stage.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wrfgpu {
+
+namespace {
+
+enum { DV_U = 0, DV_V = 1, DV_W = 2, DV_M = 3 };
+
+// Xue's sixth-order flux through the face between f(-1) and f(0)
+// (:6455-6461): 10 (f0 - f-1) - 5 (f+1 - f-2) + (f+2 - f-3).
+__device__ __forceinline__ float flux6(float fm3, float fm2, float fm1, float f0, float fp1, float fp2) {
+  return 10.0f * (f0 - fm1) - 5.0f * (fp1 - fm2) + (fp2 - fm3);
+}
+
+// max(1 - dzmax / dzthresh, 0): the terrain-slope taper (:6481-6497).
+__device__ __forceinline__ float taper(float dzmax, float thresh) { return fmaxf(1.f - (dzmax / thresh), 0.f); }
+
+// One point of sixth_order_diffusion for variable kind V at (i, k, j), with
+// the column constants c1, c2 of level k: returns 0 + tendency_x +
+// tendency_y in the reference's order (the tendency starts at zero).
+template <int V>
+__device__ float diff6_point(const Mem& m, const F3& f, int i, int k, int j, float c1, float c2, float coef) {
+  const F2 mut = f2(m, WRFGPU_MUT);
+  const F3 phb = f3(m, WRFGPU_PHB);
+  const int opt = m.cf.diff_6th_opt;
+  const bool slope = m.cf.diff_6th_slopeopt >= 1;
+  auto mass = [&](int ii, int jj) { return c1 * mut.ro(ii, jj) + c2; };
+  const float q0 = f.ro(i, k, j);
+
+  // ---- x (:6452-6538)
+  const float xm3 = f.ro(i - 3, k, j), xm2 = f.ro(i - 2, k, j), xm1 = f.ro(i - 1, k, j);
+  const float xp1 = f.ro(i + 1, k, j), xp2 = f.ro(i + 2, k, j), xp3 = f.ro(i + 3, k, j);
+  float d0 = flux6(xm3, xm2, xm1, q0, xp1, xp2), d1 = flux6(xm2, xm1, q0, xp1, xp2, xp3);
+  if (opt == 2) {
+    if (d0 * (q0 - xm1) <= 0.f) d0 = 0.f;
+    if (d1 * (xp1 - q0) <= 0.f) d1 = 0.f;
+  }
+  float s0 = 1.f, s1 = 1.f;
+  if (slope) {
+    const F2 msfux = f2(m, WRFGPU_MSFUX);
+    const float dx = 1.f / m.rdx;
+    const float thresh = m.cf.diff_6th_thresh * 9.81f * dx;
+    float z0, z1;
+    if (V == DV_U) {
+      z0 = fmaxf(fabsf(phb.ro(i, k, j) - phb.ro(i - 1, k, j)) * msfux.ro(i, j),
+                 fabsf(phb.ro(i - 1, k, j) - phb.ro(i - 2, k, j)) * msfux.ro(i - 1, j));
+      z1 = fmaxf(fabsf(phb.ro(i + 1, k, j) - phb.ro(i, k, j)) * msfux.ro(i + 1, j),
+                 fabsf(phb.ro(i, k, j) - phb.ro(i - 1, k, j)) * msfux.ro(i, j));
+    } else if (V == DV_V) {
+      z0 = fmaxf(fabsf(phb.ro(i, k, j) - phb.ro(i - 1, k, j)) * msfux.ro(i, j),
+                 fabsf(phb.ro(i, k, j - 1) - phb.ro(i - 1, k, j - 1)) * msfux.ro(i, j - 1));
+      z1 = fmaxf(fabsf(phb.ro(i + 1, k, j) - phb.ro(i, k, j)) * msfux.ro(i + 1, j),
+                 fabsf(phb.ro(i + 1, k, j - 1) - phb.ro(i, k, j - 1)) * msfux.ro(i + 1, j - 1));
+    } else {
+      z0 = fabsf(phb.ro(i, k, j) - phb.ro(i - 1, k, j)) * msfux.ro(i, j);
+      z1 = fabsf(phb.ro(i + 1, k, j) - phb.ro(i, k, j)) * msfux.ro(i + 1, j);
+    }
+    s0 = taper(z0, thresh);
+    s1 = taper(z1, thresh);
+  }
+  float m0, m1, msf;
+  if (V == DV_U) {
+    m0 = mass(i - 1, j); m1 = mass(i, j); msf = f2(m, WRFGPU_MSFUX).ro(i, j);
+  } else if (V == DV_V) {
+    m0 = 0.25f * (mass(i - 1, j - 1) + mass(i, j - 1) + mass(i - 1, j) + mass(i, j));
+    m1 = 0.25f * (mass(i, j - 1) + mass(i + 1, j - 1) + mass(i, j) + mass(i + 1, j));
+    msf = f2(m, WRFGPU_MSFVX).ro(i, j);
+  } else {
+    m0 = 0.5f * (mass(i - 1, j) + mass(i, j));
+    m1 = 0.5f * (mass(i, j) + mass(i + 1, j));
+    msf = f2(m, WRFGPU_MSFTX).ro(i, j);
+  }
+  const float tx = coef * msf * ((s1 * m1 * d1) - (s0 * m0 * d0));
+
+  // ---- y (:6543-6628)
+  const float ym3 = f.ro(i, k, j - 3), ym2 = f.ro(i, k, j - 2), ym1 = f.ro(i, k, j - 1);
+  const float yp1 = f.ro(i, k, j + 1), yp2 = f.ro(i, k, j + 2), yp3 = f.ro(i, k, j + 3);
+  d0 = flux6(ym3, ym2, ym1, q0, yp1, yp2);
+  d1 = flux6(ym2, ym1, q0, yp1, yp2, yp3);
+  if (opt == 2) {
+    if (d0 * (q0 - ym1) <= 0.f) d0 = 0.f;
+    if (d1 * (yp1 - q0) <= 0.f) d1 = 0.f;
+  }
+  s0 = 1.f; s1 = 1.f;
+  if (slope) {
+    const F2 msfvy = f2(m, WRFGPU_MSFVY);
+    const float dy = 1.f / m.rdy;
+    const float thresh = m.cf.diff_6th_thresh * 9.81f * dy;
+    float z0, z1;
+    if (V == DV_U) {
+      z0 = fmaxf(fabsf(phb.ro(i, k, j) - phb.ro(i, k, j - 1)) * msfvy.ro(i, j),
+                 fabsf(phb.ro(i - 1, k, j) - phb.ro(i - 1, k, j - 1)) * msfvy.ro(i - 1, j));
+      z1 = fmaxf(fabsf(phb.ro(i, k, j + 1) - phb.ro(i, k, j)) * msfvy.ro(i, j + 1),
+                 fabsf(phb.ro(i - 1, k, j + 1) - phb.ro(i - 1, k, j)) * msfvy.ro(i - 1, j + 1));
+    } else if (V == DV_V) {
+      z0 = fmaxf(fabsf(phb.ro(i, k, j) - phb.ro(i, k, j - 1)) * msfvy.ro(i, j),
+                 fabsf(phb.ro(i, k, j - 1) - phb.ro(i, k, j - 2)) * msfvy.ro(i, j - 1));
+      z1 = fmaxf(fabsf(phb.ro(i, k, j + 1) - phb.ro(i, k, j)) * msfvy.ro(i, j + 1),
+                 fabsf(phb.ro(i, k, j) - phb.ro(i, k, j - 1)) * msfvy.ro(i, j));
+    } else {
+      z0 = fabsf(phb.ro(i, k, j) - phb.ro(i, k, j - 1)) * msfvy.ro(i, j);
+      z1 = fabsf(phb.ro(i, k, j + 1) - phb.ro(i, k, j)) * msfvy.ro(i, j + 1);
+    }
+    s0 = taper(z0, thresh);
+    s1 = taper(z1, thresh);
+  }
+  if (V == DV_U) {
+    m0 = 0.25f * (mass(i - 1, j - 1) + mass(i, j - 1) + mass(i - 1, j) + mass(i, j));
+    m1 = 0.25f * (mass(i - 1, j) + mass(i, j) + mass(i - 1, j + 1) + mass(i, j + 1));
+    msf = f2(m, WRFGPU_MSFUY).ro(i, j);
+  } else if (V == DV_V) {
+    m0 = mass(i, j - 1); m1 = mass(i, j); msf = f2(m, WRFGPU_MSFVY).ro(i, j);
+  } else {
+    m0 = 0.5f * (mass(i, j - 1) + mass(i, j));
+    m1 = 0.5f * (mass(i, j) + mass(i, j + 1));
+    msf = f2(m, WRFGPU_MSFTY).ro(i, j);
+  }
+  const float ty = coef * msf * ((s1 * m1 * d1) - (s0 * m0 * d0));
+  float t = 0.f;
+  t = t + tx;
+  t = t + ty;
+  return t;
+}
+
+// Stage 1: the forward-in-time tendencies ru_tendf, rv_tendf, rw_tendf and
+// t_tendf of the sixth-order diffusion of u_2, v_2, w_2 and t_2, over the
+// loop limits of periodic / symmetric boundaries (:6330-6443).  Points
+// outside those limits keep the zero the buffers were created with.
+__global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid || m.tendf[0] == nullptr) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  const int ktf = min(m.kte, m.kde - 1);
+  if (i < m.its || j < m.jts || k < m.kts || k > ktf) return;
+  const int i_end = min(m.ide - 1, m.ite), j_end = min(m.jde - 1, m.jte);
+  const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * m.dt);
+  const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H);
+  const float c1 = c1h(k), c2 = c2h(k);
+  if (i <= m.ite && j <= j_end)
+    f3p(m, m.tendf[0])(i, k, j) = diff6_point<DV_U>(m, f3(m, WRFGPU_U_2), i, k, j, c1, c2, coef);
+  if (i <= i_end && j <= m.jte)
+    f3p(m, m.tendf[1])(i, k, j) = diff6_point<DV_V>(m, f3(m, WRFGPU_V_2), i, k, j, c1, c2, coef);
+  if (i <= i_end && j <= j_end) {
+    if (k >= m.kts + 1) {
+      const F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+      f3p(m, m.tendf[2])(i, k, j) = diff6_point<DV_W>(m, f3(m, WRFGPU_W_2), i, k, j, c1f(k), c2f(k), coef);
+    }
+    f3p(m, m.tendf[3])(i, k, j) = diff6_point<DV_M>(m, f3(m, WRFGPU_T_2), i, k, j, c1, c2, coef);
+  }
+}
+
+// Every stage: rk_addtend_dry for the stored tendencies.  With physics off
+// the saved tendencies, h_diabatic, ph_tendf and mu_tendf are zero: the
+// stage-1 "tendf + save * msf" steps add +0 to a tendency that is never -0
+// and the ph / mu additions are left out; theta keeps its h_diabatic term,
+// which can turn a -0 sum into +0.
+__global__ void __launch_bounds__(BX* BY) k_addtend_dry(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid || m.tendf[0] == nullptr) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (i < m.its || j < m.jts || k < m.kts || k > m.kte) return;
+  const int i_end = min(m.ite, m.ide - 1), j_end = min(m.jte, m.jde - 1);
+  if (k <= m.kte - 1) {
+    if (i <= m.ite && j <= j_end) {
+      F3 t = f3(m, WRFGPU_RU_TEND);
+      t(i, k, j) = t(i, k, j) + f3p(m, m.tendf[0]).ro(i, k, j) / f2(m, WRFGPU_MSFUY).ro(i, j);
+    }
+    if (i <= i_end && j <= m.jte) {
+      F3 t = f3(m, WRFGPU_RV_TEND);
+      t(i, k, j) = t(i, k, j) + f3p(m, m.tendf[1]).ro(i, k, j) * f2(m, WRFGPU_MSFVX_INV).ro(i, j);
+    }
+    if (i <= i_end && j <= j_end) {
+      F3 t = f3(m, WRFGPU_T_TEND);
+      const float msfty = f2(m, WRFGPU_MSFTY).ro(i, j);
+      const float mass = f1(m, WRFGPU_C1H)(k) * f2(m, WRFGPU_MUT).ro(i, j) + f1(m, WRFGPU_C2H)(k);
+      t(i, k, j) = t(i, k, j) + f3p(m, m.tendf[3]).ro(i, k, j) / msfty + mass * 0.f / msfty;
+    }
+  }
+  if (i <= i_end && j <= j_end) {
+    F3 t = f3(m, WRFGPU_RW_TEND);
+    t(i, k, j) = t(i, k, j) + f3p(m, m.tendf[2]).ro(i, k, j) / f2(m, WRFGPU_MSFTY).ro(i, j);
+  }
+}
+
+}  // namespace
+
+void launch_sixth_diff(const Launch& L, int nblocks, cudaStream_t s) {
+  k_sixth_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L);
+}
+
+void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s) {
+  k_addtend_dry<<<nblocks, dim3(BX, BY), 0, s>>>(L);
+}
+
+}  // namespace wrfgpu

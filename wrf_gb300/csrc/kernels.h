@@ -68,6 +68,9 @@ void launch_tend_u_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t
 void launch_tend_v_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s, int var = 0);
 void launch_tend_t_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
+// sixth-order diffusion of the dry state at stage 1, and rk_addtend_dry (k_diff.cu)
+void launch_sixth_diff(const Launch& L, int nblocks, cudaStream_t s);
+void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s);
 
 // acoustic steps
 // 2-D part over column blocks, then the 3-D part over staggered tiles x level chunks

@@ -10,7 +10,8 @@
 //
 // Two calls of the reference that provably leave the state unchanged are not
 // issued: rk_addtend_dry adds physics tendencies that are identically zero
-// with physics off (module_em.F:959-1092), and the post-RK calc_p_rho_phi
+// with physics off unless the sixth-order diffusion is on (module_em.F:959-1092;
+// k_diff.cu issues it then), and the post-RK calc_p_rho_phi
 // (solve_em.F:4180-4203) recomputes al and p from the same inputs as the
 // stage-3 call.  initialize_moist_old (solve_em.F:517-527) is also skipped:
 // moist_old is overwritten by rk_update_scalar before any read.

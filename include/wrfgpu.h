@@ -62,8 +62,8 @@ typedef struct WrfDynConfig {
   /* sixth-order numerical diffusion (Registry.EM_COMMON:2860-2863): diff_6th_opt
    * 0 off, 1 on, 2 on with up-gradient fluxes dropped; diff_6th_slopeopt 1 tapers
    * it over steep terrain (threshold diff_6th_thresh, Registry default 0.10);
-   * diff_6th_factor (Registry default 0.12).  The species' diffusion is not
-   * built: with diff_6th_opt != 0, moist_mix6_off and scalar_mix6_off must be 1. */
+   * diff_6th_factor (Registry default 0.12); moist_mix6_off / scalar_mix6_off 1
+   * leave the moist / passive species undiffused. */
   int32_t diff_6th_opt, diff_6th_slopeopt;
   float diff_6th_factor, diff_6th_thresh;
   int32_t moist_mix6_off, scalar_mix6_off;

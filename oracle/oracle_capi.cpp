@@ -161,7 +161,7 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
       return 0;
     case ORACLE_R_UPDATE_SCALAR_PD:
       rk_update_scalar_pd(D.qold(species), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_1),
-                          p2(WRFGPU_MUB), dt_rk, td);
+                          p2(WRFGPU_MUB), dt_rk, (R*)nullptr, td);
       return 0;
     case ORACLE_R_ADVECT_SCALAR:
       zero_tend(p3(WRFGPU_ADVECT_TEND), td);
@@ -180,7 +180,8 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
       return 0;
     case ORACLE_R_UPDATE_SCALAR:
       rk_update_scalar(D.qold(species), D.q(species), p3(WRFGPU_ADVECT_TEND), p2(WRFGPU_MSFTY), p1(WRFGPU_C1H),
-                       p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), rk_step, dt_rk, td);
+                       p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), rk_step, dt_rk,
+                       (R*)nullptr, td);
       return 0;
     case ORACLE_R_CALC_P_RHO_PHI:
       calc_p_rho_phi(D.q(0), D.n_moist, cf.hypsometric_opt, p3(WRFGPU_AL), p3(WRFGPU_ALB), p2(WRFGPU_MU_2),

@@ -19,12 +19,14 @@
 
 namespace wrforacle {
 
-// module_em.F:1587-1799 rk_update_scalar (physics tendency sc_tend == 0, so
-// the "+ sc_tend" step of :1700-1706 adds an exact zero and is left out).
+// module_em.F:1587-1799 rk_update_scalar.  sc_tend (:1700-1706) holds the
+// stage-1 sixth-order diffusion of a diffused species; sc_tend_p is null for
+// the others, whose sc_tend is zero (the "+ sc_tend" step then adds an exact
+// zero and is left out).
 template <typename R>
 void rk_update_scalar(R* scalar_1_p, R* scalar_2_p, R* advect_tend_p, R* msfty_p, R* c1_p, R* c2_p, R* mu_old_p,
-                      R* mu_new_p, R* mu_base_p, int rk_step, R dt, const Dims& d) {
-  A3<R> scalar_1(scalar_1_p, d), scalar_2(scalar_2_p, d), advect_tend(advect_tend_p, d);
+                      R* mu_new_p, R* mu_base_p, int rk_step, R dt, R* sc_tend_p, const Dims& d) {
+  A3<R> scalar_1(scalar_1_p, d), scalar_2(scalar_2_p, d), advect_tend(advect_tend_p, d), sc_tend(sc_tend_p, d);
   A2<R> msfty(msfty_p, d), mu_old(mu_old_p, d), mu_new(mu_new_p, d), mu_base(mu_base_p, d);
   A1<R> c1(c1_p, d), c2(c2_p, d);
   const int i_end = std::min(d.ite, d.ide - 1), j_end = std::min(d.jte, d.jde - 1), k_end = std::min(d.kte, d.kde - 1);
@@ -34,16 +36,20 @@ void rk_update_scalar(R* scalar_1_p, R* scalar_2_p, R* advect_tend_p, R* msfty_p
       R munew = mu_new(i, j) + mu_base(i, j);
       for (int k = d.kts; k <= k_end; ++k) {
         R tendency = advect_tend(i, k, j) * msfty(i, j);
+        if (sc_tend_p) tendency = tendency + sc_tend(i, k, j);
         if (rk_step == 1) scalar_1(i, k, j) = scalar_2(i, k, j);
         scalar_2(i, k, j) = ((c1(k) * muold + c2(k)) * scalar_1(i, k, j) + dt * tendency) / (c1(k) * munew + c2(k));
       }
     }
 }
 
-// module_em.F:1803-1916 rk_update_scalar_pd with sc_tend == 0.
+// module_em.F:1803-1916 rk_update_scalar_pd: tendency = 0 + sc_tend (null:
+// zero).  The reference then zeroes sc_tend (:1893); the caller passes null
+// to the last stage's rk_update_scalar of these species instead.
 template <typename R>
-void rk_update_scalar_pd(R* scalar_p, R* c1_p, R* c2_p, R* mu_old_p, R* mu_new_p, R* mu_base_p, R dt, const Dims& d) {
-  A3<R> scalar(scalar_p, d);
+void rk_update_scalar_pd(R* scalar_p, R* c1_p, R* c2_p, R* mu_old_p, R* mu_new_p, R* mu_base_p, R dt, R* sc_tend_p,
+                         const Dims& d) {
+  A3<R> scalar(scalar_p, d), sc_tend(sc_tend_p, d);
   A2<R> mu_old(mu_old_p, d), mu_new(mu_new_p, d), mu_base(mu_base_p, d);
   A1<R> c1(c1_p, d), c2(c2_p, d);
   const int i_end = std::min(d.ite, d.ide - 1), j_end = std::min(d.jte, d.jde - 1), k_end = std::min(d.kte, d.kde - 1);
@@ -53,6 +59,7 @@ void rk_update_scalar_pd(R* scalar_p, R* c1_p, R* c2_p, R* mu_old_p, R* mu_new_p
       R munew = mu_new(i, j) + mu_base(i, j);
       for (int k = d.kts; k <= k_end; ++k) {
         R tendency = R(0.);
+        if (sc_tend_p) tendency = tendency + sc_tend(i, k, j);
         scalar(i, k, j) = ((c1(k) * muold + c2(k)) * scalar(i, k, j) + dt * tendency) / (c1(k) * munew + c2(k));
       }
     }
@@ -92,6 +99,7 @@ struct Domain {
   std::vector<std::vector<R>> f3, f2, f1;   // indexed by WrfGpuFieldId ranges
   std::vector<std::vector<R>> qs;           // moist then passive: [2*s] current, [2*s+1] old
   std::vector<std::vector<R>> tendf;        // ru_tendf, rv_tendf, rw_tendf, t_tendf (diff_6th_opt != 0)
+  std::vector<std::vector<R>> sctend;       // species' sc_tend (diff_6th_opt != 0)
   long n3 = 0, n2 = 0, n1 = 0;
   int nthreads = 1;
   R max_vert_cfl = 0, max_horiz_cfl = 0;
@@ -114,6 +122,13 @@ struct Domain {
     f1.assign(WRFGPU_N1D, std::vector<R>(n1, R(0)));
     qs.assign(2 * (n_moist + n_scalar), std::vector<R>(n3, R(0)));
     tendf.assign(cf.diff_6th_opt != 0 ? 4 : 0, std::vector<R>(n3, R(0)));
+    sctend.assign(cf.diff_6th_opt != 0 ? n_moist + n_scalar : 0, std::vector<R>(n3, R(0)));
+  }
+  // species s's sc_tend, or null where it is not diffused
+  R* sct_of(int s) {
+    if (cf.diff_6th_opt == 0) return nullptr;
+    if (s < n_moist ? cf.moist_mix6_off : cf.scalar_mix6_off) return nullptr;
+    return sctend[s].data();
   }
   R* p3(int id) { return f3[id].data(); }
   R* p2(int id) { return f2[id - WRFGPU_F2D_BASE].data(); }
@@ -363,7 +378,7 @@ struct Domain {
           if (adv != 1) continue;
           tiles([&](const Dims& td) {
             rk_update_scalar_pd(qold(s), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_1),
-                                p2(WRFGPU_MUB), dt_rk, td);
+                                p2(WRFGPU_MUB), dt_rk, sct_of(s), td);
           });
           bc3p(qold(s), 'p');
         }
@@ -371,8 +386,16 @@ struct Domain {
       // moist_variable_loop / scalar_variable_loop (solve_em.F:2198-2364, :2772-2955).
       for (int s = 0; s < nsp; ++s) {
         int adv = s < n_moist ? cf.moist_adv_opt : cf.scalar_adv_opt;
+        R* sct = sct_of(s);
+        if (sct && rk_step == 1) std::fill(sctend[s].begin(), sctend[s].end(), R(0));
         tiles([&](const Dims& td) {
           zero_tend(p3(WRFGPU_ADVECT_TEND), td);
+          // rk_scalar_tend's stage-1 sixth-order diffusion (module_em.F:1421-1435):
+          // muts and the stage's dt
+          if (sct && rk_step == 1)
+            sixth_order_diffusion('m', q(s), sct, p2(WRFGPU_MUTS), dt_rk, cf, p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                                  p3(WRFGPU_PHB), rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUX),
+                                  p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
           if (rk_step == rk_order && adv == 1)
             advect_scalar_pd(q(s), qold(s), p3(WRFGPU_ADVECT_TEND), p3(WRFGPU_RU_M), p3(WRFGPU_RV_M),
                              p3(WRFGPU_WW_M), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MUTS), p2(WRFGPU_MUB),
@@ -387,7 +410,8 @@ struct Domain {
         });
         tiles([&](const Dims& td) {
           rk_update_scalar(qold(s), q(s), p3(WRFGPU_ADVECT_TEND), p2(WRFGPU_MSFTY), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
-                           p2(WRFGPU_MU_1), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), rk_step, dt_rk, td);
+                           p2(WRFGPU_MU_1), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), rk_step, dt_rk,
+                           (rk_step == rk_order && adv == 1) ? nullptr : sct, td);
         });
       }
       tiles([&](const Dims& td) {

@@ -136,8 +136,6 @@ inline void check_config(const WrfDynConfig& c) {
     throw std::runtime_error("open/specified/nested/polar boundaries not supported");
   if (c.zadvect_implicit != 0) throw std::runtime_error("IEVA not supported");
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) throw std::runtime_error("diff_6th_opt must be 0, 1 or 2");
-  if (c.diff_6th_opt != 0 && !(c.moist_mix6_off && c.scalar_mix6_off))
-    throw std::runtime_error("sixth-order diffusion of the species is not restated");
 }
 
 // ===========================================================================

@@ -578,10 +578,11 @@ def test_batched_mixed_options_equals_plain(gpulib):
             assert np.array_equal(ens.get(m, fid), d.get(0, fid)), (m, nm)
 
 
-def diffusion_case(opt, slopeopt):
-    """Sixth-order diffusion of the dry state (species mixing off) on the
-    small case with a 60 m/s wave in u over 8 points."""
-    case = cases.small_case(nx=16, ny=12, kde=20, n_scalar=1, seed=23)
+def diffusion_case(opt, slopeopt, species=True):
+    """Sixth-order diffusion on the small case with a 60 m/s wave in u over
+    8 points; the moist and passive species diffused too unless species is
+    False."""
+    case = cases.small_case(nx=16, ny=12, kde=20, n_scalar=2, seed=23)
     F = case.fields
     ni = F["u_2"].shape[-1]
     pert = (60.0 * np.sin(2 * np.pi * np.arange(ni) / 8.0)).astype(F["u_2"].dtype)
@@ -592,27 +593,29 @@ def diffusion_case(opt, slopeopt):
     c.diff_6th_slopeopt = slopeopt
     c.diff_6th_factor = 0.12
     c.diff_6th_thresh = 0.10
-    c.moist_mix6_off = 1
-    c.scalar_mix6_off = 1
+    c.moist_mix6_off = 0 if species else 1
+    c.scalar_mix6_off = 0 if species else 1
     return case
 
 
-@pytest.mark.parametrize("opt,slopeopt", [(1, 0), (2, 0), (2, 1)])
-def test_full_step_bitwise_diff_6th(gpulib, opt, slopeopt):
+@pytest.mark.parametrize("opt,slopeopt,species", [(1, 0, False), (1, 0, True), (2, 0, True), (2, 1, True)])
+def test_full_step_bitwise_diff_6th(gpulib, opt, slopeopt, species):
     """Sixth-order diffusion of u, v, w and theta at stage 1
     (module_big_step_utilities_em.F:6220-6636) added at every stage by
-    rk_addtend_dry (module_em.F:959-1092): bit for bit with the oracle over
-    two steps, and active (the oracle's state differs from its
+    rk_addtend_dry (module_em.F:959-1092), and of the species at stage 1
+    into sc_tend (module_em.F:1421-1435) added by rk_update_scalar and the
+    positive-definite pre-update: bit for bit with the oracle over two steps
+    (state and species), and active (the oracle's state differs from its
     diff_6th_opt = 0 run)."""
-    case = diffusion_case(opt, slopeopt)
+    case = diffusion_case(opt, slopeopt, species)
     od = OracleDomain(case, "f32")
     ge = G.Domain(case)
     od.step(2)
     ge.step(2)
     ge.sync()
     bad = []
-    for nm in STATE_FIELDS:
-        fid = abi.FIELD_ID[nm]
+    nsp = case.desc.n_moist + case.desc.n_scalar
+    for nm, fid in [(n, abi.FIELD_ID[n]) for n in STATE_FIELDS] + [("q%d" % s, abi.species_id(s)) for s in range(nsp)]:
         a = interior(case, fid, ge.get(0, fid), halo=3)
         b = interior(case, fid, od.get(fid), halo=3)
         d = max_abs(a, b)
@@ -622,14 +625,8 @@ def test_full_step_bitwise_diff_6th(gpulib, opt, slopeopt):
     case.desc.config.diff_6th_opt = 0
     o0 = OracleDomain(case, "f32")
     o0.step(2)
+    if species:
+        fid = abi.species_id(0)
+        assert max_abs(interior(case, fid, o0.get(fid), halo=3), interior(case, fid, od.get(fid), halo=3)) > 0
     fid = abi.FIELD_ID["u_2"]
     assert max_abs(interior(case, fid, o0.get(fid), halo=3), interior(case, fid, od.get(fid), halo=3)) > 0
-
-
-def test_diff_6th_species_mixing_refused(gpulib):
-    """The species' sixth-order diffusion is not built: a member that asks for
-    it is refused at creation."""
-    case = diffusion_case(2, 0)
-    case.desc.config.moist_mix6_off = 0
-    with pytest.raises(G.WrfGpuError):
-        G.Domain(case)

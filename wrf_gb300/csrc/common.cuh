@@ -70,6 +70,8 @@ struct alignas(16) Mem {
   double* wd[3];          // FP64 a/alpha/gamma of the mixed-precision form (or null)
   float* pdc[6];          // PD transport's x, y, z faces: Courant numbers, then mu dx / dt (k_pd_courant)
   float* tendf[4];        // ru_tendf, rv_tendf, rw_tendf, t_tendf of the sixth-order diffusion (or null)
+  float* sctend;          // species s's sc_tend at sctend + s * sct_n (sixth-order diffusion, or null)
+  long long sct_n;
   int nsp, n_moist;
   int ns_total;           // acoustic steps per large step
   int pad0;
@@ -84,6 +86,14 @@ struct alignas(16) Mem {
   float pad1;
   float* cfl_out;         // [2]: max vertical, max horizontal CFL (atomic max)
 };
+
+// Species s's stored sixth-order diffusion tendency sc_tend, or null where the
+// species is not diffused (diff_6th_opt = 0, or its class's mix6_off).
+__host__ __device__ inline float* sc_tend_of(const Mem& m, int s) {
+  if (m.sctend == nullptr) return nullptr;
+  const bool on = s < m.n_moist ? !m.cf.moist_mix6_off : !m.cf.scalar_mix6_off;
+  return on ? m.sctend + (long long)s * m.sct_n : nullptr;
+}
 
 // Tensor map of buffer slot `slot` (field id or species slot), box `box`.
 __host__ __device__ inline const CUtensorMap* tmap_of(const Mem& m, int slot, int box) {

@@ -64,9 +64,7 @@ static int check_desc(const WrfGpuDomainDesc& d) {
     return WRFGPU_E_ARG;
   if (!c.non_hydrostatic || c.zadvect_implicit != 0 || (c.damp_opt != 0 && c.damp_opt != 3) || (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
     return WRFGPU_E_ARG;
-  // sixth-order diffusion of the dry state; the species' is not built
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) return WRFGPU_E_ARG;
-  if (c.diff_6th_opt != 0 && !(c.moist_mix6_off && c.scalar_mix6_off)) return WRFGPU_E_ARG;
   if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
   if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;
   if (c.open_xs || c.open_xe || c.open_ys || c.open_ye || c.specified || c.nested || c.polar) return WRFGPU_E_ARG;
@@ -249,7 +247,7 @@ struct Ensemble {
       b += al256(n3[m] * 4);  // limiter scratch
       b += 6 * al256(n3[m] * 4);  // face Courant numbers and low-order factors of the PD transport
       if (fp64) b += 3 * al256(n3[m] * 8);
-      if (d.config.diff_6th_opt != 0) b += 4 * al256(n3[m] * 4);  // ru_tendf, rv_tendf, rw_tendf, t_tendf
+      if (d.config.diff_6th_opt != 0) b += (4 + nsp) * al256(n3[m] * 4);  // ru_tendf .. t_tendf, sc_tend
       off[m] = total;
       total += b;
     }
@@ -287,7 +285,10 @@ struct Ensemble {
       for (int q = 0; q < 6; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
       if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
       if (d.config.diff_6th_opt != 0)  // zero outside the diffusion's loop limits (the pool is cleared)
+      {
         for (int q = 0; q < 4; ++q) { M.tendf[q] = (float*)p; p += al256(n3[m] * 4); }
+        M.sctend = (float*)p; M.sct_n = (long long)(al256(n3[m] * 4) / 4); p += M.nsp * al256(n3[m] * 4);
+      }
       M.ns_total = num_sound_steps(d);
       const WrfGpuScalars& s = d.scalars;
       M.dt = (float)s.dt; M.rdx = (float)s.rdx; M.rdy = (float)s.rdy;
@@ -431,7 +432,7 @@ struct Ensemble {
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       if (diff6) {  // module_em.F:879-932 (stage 1), then rk_addtend_dry (solve_em.F:967)
         mark(PH_DIFF);
-        if (rk_step == 1) launch_sixth_diff(l3, nb3, stream);
+        if (rk_step == 1) launch_sixth_diff(l3, nb3, 0, stream);
         launch_addtend_dry(l3, nb3, stream);
       }
       if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream, tune[TU_CFL]); }
@@ -465,14 +466,15 @@ struct Ensemble {
         j.f3(WRFGPU_RU_M, 'u'); j.f3(WRFGPU_RV_M, 'v'); j.f3(WRFGPU_WW_M, 'w');
         j.f2(WRFGPU_MUT, 't'); j.f2(WRFGPU_MUTS, 't');
         fill(j);
-        mark(PH_USPD); launch_update_scalar_pd_col(LTM(), nb_tm, a, stream);
+        mark(PH_USPD); launch_update_scalar_pd_col(LTM(), nb_tm, a, stream, diff6);
         JobList jo;
         for (int s = 0; s < nsp_max; ++s) jo.sp(s, 1, 'p');
         fill(jo);
       }
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
-      mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV]);
+      if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_sixth_diff(l3, nb3, 1, stream); }  // module_em.F:1421-1435
+      mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV], diff6);
       if (rk_step == 3) {
         mark(PH_PD);
         launch_pd_courant(l2, nb2, rk_step, stream);

@@ -29,8 +29,8 @@ __device__ __forceinline__ float taper(float dzmax, float thresh) { return fmaxf
 // the column constants c1, c2 of level k: returns 0 + tendency_x +
 // tendency_y in the reference's order (the tendency starts at zero).
 template <int V>
-__device__ float diff6_point(const Mem& m, const F3& f, int i, int k, int j, float c1, float c2, float coef) {
-  const F2 mut = f2(m, WRFGPU_MUT);
+__device__ float diff6_point(const Mem& m, const F3& f, const F2& mut, int i, int k, int j, float c1, float c2,
+                             float coef) {
   const F3 phb = f3(m, WRFGPU_PHB);
   const int opt = m.cf.diff_6th_opt;
   const bool slope = m.cf.diff_6th_slopeopt >= 1;
@@ -132,11 +132,14 @@ __device__ float diff6_point(const Mem& m, const F3& f, int i, int k, int j, flo
   return t;
 }
 
-// Stage 1: the forward-in-time tendencies ru_tendf, rv_tendf, rw_tendf and
-// t_tendf of the sixth-order diffusion of u_2, v_2, w_2 and t_2, over the
-// loop limits of periodic / symmetric boundaries (:6330-6443).  Points
-// outside those limits keep the zero the buffers were created with.
-__global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L) {
+// Stage 1, mode 0 (rk_tendency): the forward-in-time tendencies ru_tendf,
+// rv_tendf, rw_tendf and t_tendf of the sixth-order diffusion of u_2, v_2,
+// w_2 and t_2 with mut and the large step dt.  Mode 1 (rk_scalar_tend,
+// module_em.F:1421-1435, after the acoustic steps): each diffused species'
+// sc_tend, with muts and the stage's dt (dt / 3).  Loop limits of periodic /
+// symmetric boundaries (:6330-6443); points outside them keep the zero the
+// buffers were created with.
+__global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L, int mode) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid || m.tendf[0] == nullptr) return;
@@ -144,19 +147,30 @@ __global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L) {
   const int ktf = min(m.kte, m.kde - 1);
   if (i < m.its || j < m.jts || k < m.kts || k > ktf) return;
   const int i_end = min(m.ide - 1, m.ite), j_end = min(m.jde - 1, m.jte);
-  const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * m.dt);
   const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H);
   const float c1 = c1h(k), c2 = c2h(k);
+  if (mode == 1) {
+    if (i > i_end || j > j_end) return;
+    const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * stage_of(m, 1).dt_rk);
+    const F2 muts = f2(m, WRFGPU_MUTS);
+    for (int s = 0; s < m.nsp; ++s) {
+      float* sc = sc_tend_of(m, s);
+      if (sc) f3p(m, sc)(i, k, j) = diff6_point<DV_M>(m, f3p(m, m.q[s]), muts, i, k, j, c1, c2, coef);
+    }
+    return;
+  }
+  const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * m.dt);
+  const F2 mut = f2(m, WRFGPU_MUT);
   if (i <= m.ite && j <= j_end)
-    f3p(m, m.tendf[0])(i, k, j) = diff6_point<DV_U>(m, f3(m, WRFGPU_U_2), i, k, j, c1, c2, coef);
+    f3p(m, m.tendf[0])(i, k, j) = diff6_point<DV_U>(m, f3(m, WRFGPU_U_2), mut, i, k, j, c1, c2, coef);
   if (i <= i_end && j <= m.jte)
-    f3p(m, m.tendf[1])(i, k, j) = diff6_point<DV_V>(m, f3(m, WRFGPU_V_2), i, k, j, c1, c2, coef);
+    f3p(m, m.tendf[1])(i, k, j) = diff6_point<DV_V>(m, f3(m, WRFGPU_V_2), mut, i, k, j, c1, c2, coef);
   if (i <= i_end && j <= j_end) {
     if (k >= m.kts + 1) {
       const F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
-      f3p(m, m.tendf[2])(i, k, j) = diff6_point<DV_W>(m, f3(m, WRFGPU_W_2), i, k, j, c1f(k), c2f(k), coef);
+      f3p(m, m.tendf[2])(i, k, j) = diff6_point<DV_W>(m, f3(m, WRFGPU_W_2), mut, i, k, j, c1f(k), c2f(k), coef);
     }
-    f3p(m, m.tendf[3])(i, k, j) = diff6_point<DV_M>(m, f3(m, WRFGPU_T_2), i, k, j, c1, c2, coef);
+    f3p(m, m.tendf[3])(i, k, j) = diff6_point<DV_M>(m, f3(m, WRFGPU_T_2), mut, i, k, j, c1, c2, coef);
   }
 }
 
@@ -196,8 +210,8 @@ __global__ void __launch_bounds__(BX* BY) k_addtend_dry(Launch L) {
 
 }  // namespace
 
-void launch_sixth_diff(const Launch& L, int nblocks, cudaStream_t s) {
-  k_sixth_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L);
+void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s) {
+  k_sixth_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L, mode);
 }
 
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s) {

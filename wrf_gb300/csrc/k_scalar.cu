@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(BX* BY) k_update_scalar_pd(Launch L, int rk_st
 
 // Column form over mass tiles x level chunks (gridDim.y), species outermost,
 // eight levels of loads in flight.
+template <bool SCT>
 __global__ void __launch_bounds__(TX* TY) k_update_scalar_pd_col(TileLaunch L, int rk_step) {
   const TilePos tp = tile_pos(L, false, false);
   const Mem& m = block_member(L.mem, tp.m);
@@ -57,16 +58,28 @@ __global__ void __launch_bounds__(TX* TY) k_update_scalar_pd_col(TileLaunch L, i
   F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
   const float muold = f2(m, WRFGPU_MU_1)(i, j) + f2(m, WRFGPU_MUB)(i, j);
   const float munew = f2(m, WRFGPU_MU_1)(i, j) + f2(m, WRFGPU_MUB)(i, j);
-  const float tendency = 0.f;
   for (int s = 0; s < m.nsp; ++s) {
     int adv = s < m.n_moist ? m.cf.moist_adv_opt : m.cf.scalar_adv_opt;
     if (adv != 1) continue;
     F3 q = f3p(m, m.qo[s]);
-    chunked_levels<8, float>(
-        k0, k1, [&](int k, float& v) { v = q(i, k, j); },
-        [&](int k, const float& v) {
-          q(i, k, j) = ((c1(k) * muold + c2(k)) * v + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
-        });
+    // tendency = 0 + sc_tend (the stage-1 sixth-order diffusion, if any);
+    // the reference zeroes sc_tend here (:1893), so no later stage adds it
+    float* sc = SCT ? sc_tend_of(m, s) : nullptr;
+    if (sc == nullptr) {
+      const float tendency = 0.f;
+      chunked_levels<8, float>(
+          k0, k1, [&](int k, float& v) { v = q(i, k, j); },
+          [&](int k, const float& v) {
+            q(i, k, j) = ((c1(k) * muold + c2(k)) * v + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+          });
+    } else {
+      F3 sct = f3p(m, sc);
+      for (int k = k0; k <= k1; ++k) {
+        float tendency = 0.f;
+        tendency = tendency + sct(i, k, j);
+        q(i, k, j) = ((c1(k) * muold + c2(k)) * q(i, k, j) + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+      }
+    }
   }
 }
 
@@ -432,8 +445,9 @@ void launch_cfl_check_col(const TileLaunch& L, int nb, cudaStream_t s, int var) 
 void launch_update_scalar_pd(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar_pd<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
 }
-void launch_update_scalar_pd_col(const TileLaunch& L, int nb, StepArgs a, cudaStream_t s) {
-  k_update_scalar_pd_col<<<dim3(nb, 4), dim3(TX, TY), 0, s>>>(L, a.rk_step);
+void launch_update_scalar_pd_col(const TileLaunch& L, int nb, StepArgs a, cudaStream_t s, bool sct) {
+  if (sct) k_update_scalar_pd_col<true><<<dim3(nb, 4), dim3(TX, TY), 0, s>>>(L, a.rk_step);
+  else k_update_scalar_pd_col<false><<<dim3(nb, 4), dim3(TX, TY), 0, s>>>(L, a.rk_step);
 }
 void launch_advect_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_advect_scalar<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags);

@@ -63,7 +63,9 @@ constexpr int ADV_NPL = 3;   // q, ru_m, rv_m
 constexpr size_t ADV_SMEM = (size_t)ADV_RING * ADV_NPL * HPLANE_BYTES + 2 * (TY * (TX + 1) + (TY + 1) * TX) * 4 +
                             ADV_RING * 8;
 
-template <int MINB>
+// SCT: some member stores sc_tend (the species' sixth-order diffusion); the
+// variant without it keeps the common case free of its load and test.
+template <int MINB, bool SCT>
 __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L, int rk_step) {
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, true);
@@ -98,6 +100,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L
   F3 fld = f3p(m, m.q[s]), old = f3p(m, m.qo[s]), out = f3p(m, m.qa[s]), rom = f3(m, WRFGPU_WW_M);
   F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
   F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  // sc_tend of this species (null unless it is diffused); at the last stage a
+  // positive-definite species' sc_tend was spent (and zeroed) by the PD pre-update
+  const F3 sct = f3p(m, (!SCT || pd_scheme(m, s, rk_step)) ? nullptr : sc_tend_of(m, s));
   float msftx = 0.f, msfty = 0.f, muold = 0.f, munew = 0.f;
   // own-column registers: scalar window fld(k-1 .. k+2), next values of old and rom
   float wm1 = 0.f, w0 = 0.f, wp1 = 0.f, wp2 = 0.f, old_k = 0.f, rom_k1 = 0.f;
@@ -159,8 +164,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L
       t = t - msftx * rdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
       t = t - rdzw(k) * (vf_hi - vf_lo);
       vf_lo = vf_hi;
-      // rk_update_scalar
-      const float tendency = t * msfty;
+      // rk_update_scalar (+ sc_tend: the species' stage-1 sixth-order diffusion)
+      float tendency = t * msfty;
+      if (SCT && sct.p) tendency = tendency + sct(i, k, j);
       float q1;
       if (rk_step == 1) { q1 = w0; old(i, k, j) = q1; }
       else q1 = old_k;
@@ -548,17 +554,19 @@ template <typename K>
 static void set_smem(K kernel, size_t bytes) {
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
-void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var) {
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var, bool sct) {
   static bool attr = false;
   if (!attr) {
-    set_smem(k_scalar_adv_update<4>, ADV_SMEM);
-    set_smem(k_scalar_adv_update<5>, ADV_SMEM);
-    set_smem(k_scalar_adv_update<6>, ADV_SMEM);
+    set_smem(k_scalar_adv_update<4, false>, ADV_SMEM);
+    set_smem(k_scalar_adv_update<5, false>, ADV_SMEM);
+    set_smem(k_scalar_adv_update<6, false>, ADV_SMEM);
+    set_smem(k_scalar_adv_update<4, true>, ADV_SMEM);
     attr = true;
   }
-  if (var == 0) k_scalar_adv_update<4><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
-  else if (var == 1) k_scalar_adv_update<5><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
-  else k_scalar_adv_update<6><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  if (sct) k_scalar_adv_update<4, true><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  else if (var == 0) k_scalar_adv_update<4, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  else if (var == 1) k_scalar_adv_update<5, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  else k_scalar_adv_update<6, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
 }
 void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int rk_step, cudaStream_t s, int var) {
   static size_t attr = 0;

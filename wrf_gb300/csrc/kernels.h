@@ -69,7 +69,8 @@ void launch_tend_v_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t
 void launch_tend_t_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 // sixth-order diffusion of the dry state at stage 1, and rk_addtend_dry (k_diff.cu)
-void launch_sixth_diff(const Launch& L, int nblocks, cudaStream_t s);
+// mode 0: u, v, w, theta into ru_tendf .. t_tendf; 1: the species into sc_tend
+void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s);
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s);
 
 // acoustic steps
@@ -96,13 +97,15 @@ void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
 void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s);
 void launch_pack_rows(const float* src, float* dst, int cols, int rows, int pitch, cudaStream_t s);
 void launch_calc_p_rho_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);        // mass tiles
-void launch_update_scalar_pd_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);  // mass tiles
+// sct: some member stores the species' sixth-order diffusion tendency sc_tend
+void launch_update_scalar_pd_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s, bool sct = false);  // mass tiles
 void launch_calc_p_rho_phi_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CPRP]);  // mass tiles
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CFL]);  // mass tiles
 
 // fused scalar transport (k_scalar_fused.cu): one block per (tile, species)
-void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var = TUNE_DEFAULT[TU_ADV]);
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var = TUNE_DEFAULT[TU_ADV],
+                              bool sct = false);
 // the face Courant numbers of the PD transport, once per step before it (column layout)
 void launch_pd_courant(const Launch& L2, int nblocks, int rk_step, cudaStream_t s);
 // nlev_max: the largest kme - kms + 1 of the members (sizes a per-level table in shared memory)

@@ -76,13 +76,26 @@ def alg_bytes_per_cell_step(phase, s_pd, s_all, n_acoustic=7):
     return 4 * per.get(phase, 0)
 
 
+# Contract bytes per cell-step: unique 3-D arrays read plus written between
+# the reference's global sync points of one large step (halo exchanges and
+# boundary fills of solve_em), N = 553 + 3 n_moist + 8 S array passes of 4 B
+# with S species in all (qv included), plus 4 B per access of each array the
+# mixed form keeps in FP64 (a, alpha, gamma: 30 accesses).  Re-reads between
+# kernels that the reference would also do between its own loops are not
+# counted, so this is the floor a fully fused step could reach.
+def contract_bytes_per_cell_step(n_moist, n_species, mixed=False):
+    return 4 * (553 + 3 * n_moist + 8 * n_species) + (120 if mixed else 0)
+
+
 # DRAM bytes (read + write) per mass cell of one launch, from the ncu
 # captures summarised in profiles/ (256x256x80 case, inputs far larger than
-# L2; traffic grows with the cells processed, so it scales to other sizes).
+# L2; traffic grows with the cells processed, so it scales to other sizes):
+# the capture of k_scalar_pd_update, of k_scalar_adv_update (stage 1) and of
+# the acoustic column kernels.
 NCU_DRAM_BYTES_PER_CELL = {
-    "scalar_pd_update": 941.5e6 / 5177344,   # k_scalar_pd_update_c2_256x256x80.md
-    "scalar_adv_update": 779.3e6 / 5177344,  # k_scalar_adv_update_c2_256x256x80.md (stage 1)
-    "advance_w": 451.3e6 / 5177344,          # k_acoustic_cols_c2_256x256x80.md
+    "scalar_pd_update": 941.5e6 / 5177344,
+    "scalar_adv_update": 779.3e6 / 5177344,
+    "advance_w": 451.3e6 / 5177344,
 }
 
 PHASE_NAMES = ["step_prep", "rk_tend_u", "rk_tend_v", "rk_tend_w", "rk_tend_t", "rk_tend_ph", "cfl_check",
@@ -151,6 +164,8 @@ def make_case(workload, nx=None):
         return cases.config1()
     if workload == "c2":
         return cases.config2() if not nx else cases.config2(nx=nx)
+    if workload == "c3":
+        return cases.config3() if not nx else cases.config3(nx=nx)
     raise ValueError(workload)
 
 
@@ -189,18 +204,22 @@ def run_reference(args, world, rank):
     case = make_case(args.workload, args.nx)
     cores = os.cpu_count() or 1
     od = OracleDomain(case, "f32", nthreads=cores)
-    steps = max(1, min(args.steps, args.ref_steps))
-    for _ in range(min(args.warmup, 1)):
-        od.step(1)
+    # one warm-up step (also sizes the sample), then the same K steps as the
+    # GPU arm unless they would exceed the time budget
+    t0 = time.perf_counter()
+    od.step(1)
+    t_step = time.perf_counter() - t0
+    steps = args.steps if args.ref_steps is None else args.ref_steps
+    steps = max(1, min(steps, int(args.ref_budget_s / max(t_step, 1e-3))))
     t0 = time.perf_counter()
     od.step(steps)
     el = time.perf_counter() - t0
     val = case.cells() * steps / el
-    sample = "%d of %d steps of the %s workload (after %d warm-up), %d OpenMP threads" % (
-        steps, args.steps, case.name, min(args.warmup, 1), cores)
+    sample = "%d of the %d timed steps of the %s workload (after 1 warm-up step; budget %.0f s), " \
+             "%d OpenMP threads" % (steps, args.steps, case.name, args.ref_budget_s, cores)
     line = {
         "impl": "reference", "metric": "cell-steps/s", "value": val, "unit": "cell-steps/s",
-        "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps,
+        "n_gpus": args.gpus, "steps": steps, "warmup": 1, "ms_per_step": 1e3 * el / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Weisman-Klemp supercell state)",
         "config": {"workload": case.name, "global_batch": 1, "seq_len": None, "parallelism": "cpu-openmp",
@@ -211,7 +230,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(case, seconds_budget=25.0):
+def cpu_baseline(case, seconds_budget=25.0, max_steps=10):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from _harness import OracleDomain
     cores = os.cpu_count() or 1
@@ -222,7 +241,7 @@ def cpu_baseline(case, seconds_budget=25.0):
     steps = 1
     if el1 < seconds_budget / 3:
         n = max(1, int((seconds_budget - el1) / max(el1, 1e-3)))
-        n = min(n, 5)
+        n = min(n, max_steps)
         t0 = time.perf_counter()
         od.step(n)
         el1 = (time.perf_counter() - t0) / n
@@ -245,47 +264,72 @@ def _copy_member_state(src, ms, dst, md, nsp):
 
 def ensemble_accuracy(n_members=2, steps=(1, 10, 30, 60)):
     """FP64-oracle error of the batched mixed form (and of the plain FP32
-    form) on the smallest members of the uneven ensemble: diffwrf relative L2
-    per field after each of `steps` large steps (identical FP32 initial state)."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from _harness import OracleDomain, interior, serr
-    from wrf_gb300 import abi, cases
-    from wrf_gb300 import gpu as G
+    form and the FP32 oracle) on the smallest members of the uneven
+    ensemble, after each of `steps` large steps."""
+    from wrf_gb300 import cases
     specs = cases.ensemble_members(seed=4)
     order = sorted(range(len(specs)), key=lambda q: specs[q][0] * specs[q][1] * specs[q][2])[:n_members]
-    mcases = [cases.ensemble_member(specs[q]) for q in order]
+    res = accuracy_vs_fp64([cases.ensemble_member(specs[q]) for q in order], steps)
+    res["members"] = res.pop("cases")
+    return res
+
+
+def accuracy_vs_fp64(mcases, steps=(1, 10, 30, 60), names=("u_2", "v_2", "w_2", "t_2", "ph_2", "mu_2", "p", "al")):
+    """diffwrf relative L2 (serr) per field of the GPU plain FP32 form, the
+    GPU mixed form and the FP32 oracle (the reference's own arithmetic)
+    against the FP64 oracle, all from the same FP32-rounded initial state,
+    after each of `steps` large steps; fields of several cases are pooled."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    from _harness import OracleDomain, interior, serr
+    from wrf_gb300 import abi
+    from wrf_gb300 import gpu as G
     cores = os.cpu_count() or 1
-    oracles = [OracleDomain(c, "f64", nthreads=cores, load=False) for c in mcases]
-    for c, o in zip(mcases, oracles):
+    o64 = [OracleDomain(c, "f64", nthreads=cores, load=False) for c in mcases]
+    for c, o in zip(mcases, o64):
         for fid, arr in c.field_items():
             o.set(fid, arr, as_f32=True)
+    o32 = [OracleDomain(c, "f32", nthreads=cores) for c in mcases]
     mixed = G.Ensemble.from_cases(mcases, flags=G.FLAG_MIXED)
     plain = G.Ensemble.from_cases(mcases, flags=0)
-    names = ["u_2", "v_2", "w_2", "t_2", "ph_2", "mu_2", "p", "al"]
-    out = {"members": [c.name for c in mcases], "oracle": "FP64 restatement, same FP32-rounded initial state",
+    out = {"cases": [c.name for c in mcases], "oracle": "FP64 restatement, same FP32-rounded initial state",
            "serr": {}}
     done = 0
     for n in steps:
-        for o in oracles:
+        for o in o64 + o32:
             o.step(n - done)
         mixed.step(n - done)
         plain.step(n - done)
         done = n
         mixed.sync()
         plain.sync()
-        row = {"mixed": {}, "plain": {}}
-        for label, e in (("mixed", mixed), ("plain", plain)):
-            for nm in names + ["qv"]:
+        row = {}
+        getters = (("mixed", lambda m, c, f: mixed.get(m, f)), ("plain", lambda m, c, f: plain.get(m, f)),
+                   ("oracle_f32", lambda m, c, f: o32[m].get(f)))
+        for label, get in getters:
+            row[label] = {}
+            for nm in list(names) + ["qv"]:
                 fid = abi.species_id(0) if nm == "qv" else abi.FIELD_ID[nm]
-                a = [interior(c, fid, e.get(m, fid)) for m, c in enumerate(mcases)]
-                b = [interior(c, fid, o.get(fid)) for c, o in zip(mcases, oracles)]
-                import numpy as np
+                a = [interior(c, fid, get(m, c, fid)) for m, c in enumerate(mcases)]
+                b = [interior(c, fid, o.get(fid)) for c, o in zip(mcases, o64)]
                 row[label][nm] = float(serr(np.concatenate([x.ravel() for x in a]),
                                             np.concatenate([x.ravel() for x in b])))
         out["serr"][str(n)] = row
     mixed.close()
     plain.close()
     return out
+
+
+def c3_accuracy(nx=128, kde=96):
+    """The C3 precision configuration's accuracy against the FP64 oracle:
+    the f-plane jet channel at nx x nx x kde (dx = 4 km, dt = 20 s, top 25 km;
+    the full 1024 x 1024 channel's FP64 run would take tens of minutes on the
+    host), after 1, 10, 30 and 60 steps."""
+    from wrf_gb300 import cases
+    c = cases.config3(nx=nx, kde=kde)
+    res = accuracy_vs_fp64([c])
+    res["size"] = "%dx%dx%d (the 1024x1024x96 channel's dx, dt, levels and jet; narrower channel)" % (nx, nx, kde)
+    return res
 
 
 def ensemble_bench(steps, warmup, n_members=64, world=1, rank=0, pg=None):
@@ -360,7 +404,7 @@ def run_ensemble_line(args, world, rank, local, pg):
     res = ensemble_bench(args.steps, args.warmup, world=world, rank=rank, pg=pg)
     clocks = sampler.stop()
     hbm, hbm_kind = peaks()
-    alg = sum(alg_bytes_per_cell_step(k, 3, 3) for k in PHASE_NAMES)
+    alg = contract_bytes_per_cell_step(1, 4, mixed=True)
     acc = ensemble_accuracy() if rank == 0 else None
     if rank == 0:
         line = {
@@ -376,8 +420,8 @@ def run_ensemble_line(args, world, rank, local, pg):
             "roofline": {"bound": "hbm", "achieved": alg * res["batched_mixed"] / 1e9, "peak": hbm,
                          "peak_kind": hbm_kind, "unit": "GB/s",
                          "frac": alg * res["batched_mixed"] / 1e9 / hbm, "traffic": None,
-                         "note": "whole-step algorithmic bytes per cell-step (%d B, FP64 column arrays not counted) "
-                                 "x cell-steps/s" % alg},
+                         "note": "whole step at the contract bytes per cell-step (%d B: unique arrays between the "
+                                 "reference's sync points, FP64 a/alpha/gamma included) x cell-steps/s" % alg},
             "ensemble": res, "accuracy": acc, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
@@ -389,12 +433,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--no-c3-accuracy", action="store_true",
+                    help="skip the C3 channel's FP64-oracle accuracy block")
     ap.add_argument("--no-ensemble", action="store_true",
                     help="skip the uneven-ensemble comparison (batched+mixed vs plain) added to the default line")
     ap.add_argument("--mixed", action="store_true", help="mixed-precision form (FP64 column steps)")
     ap.add_argument("--nx", type=int, default=None, help="horizontal size of the supercell workload (profiling runs)")
-    ap.add_argument("--ref-steps", type=int, default=3)
+    ap.add_argument("--ref-steps", type=int, default=None,
+                    help="reference arm: steps to time (default: the same --steps as the GPU arm, within the budget)")
+    ap.add_argument("--ref-budget-s", type=float, default=150.0,
+                    help="reference arm: time budget of the timed steps (seconds)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tune-rounds", type=int, default=2,
@@ -458,6 +507,7 @@ def run_single(args, world, rank, local, pg):
     achieved = alg[dom_name] / (dom_ms / 1e3) / 1e9
     step_alg = sum(alg.values())
     step_ms = ms / args.steps
+    contract = contract_bytes_per_cell_step(case.desc.n_moist, nsp, args.mixed) * cells
     traffic = None
     if dom_name in NCU_DRAM_BYTES_PER_CELL and case.desc.n_scalar == 10:
         traffic = NCU_DRAM_BYTES_PER_CELL[dom_name] * cells
@@ -465,8 +515,13 @@ def run_single(args, world, rank, local, pg):
                 "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
                 "traffic_note": "DRAM bytes per launch from the ncu capture of the 256x256x80 case, scaled by cells",
                 "alg_bytes_per_step": alg[dom_name], "ms_per_step": dom_ms, "launches_per_step": dom_n,
-                "step_alg_bytes": step_alg, "step_achieved": step_alg / (step_ms / 1e3) / 1e9,
-                "step_frac": step_alg / (step_ms / 1e3) / 1e9 / hbm,
+                "step_contract_bytes": contract, "step_achieved": contract / (step_ms / 1e3) / 1e9,
+                "step_frac": contract / (step_ms / 1e3) / 1e9 / hbm,
+                "step_frac_note": "whole step at the contract bytes (unique arrays between the reference's sync "
+                                  "points: %d B per cell-step)" % (contract // cells),
+                "step_kernel_bytes": step_alg, "step_kernel_frac": step_alg / (step_ms / 1e3) / 1e9 / hbm,
+                "step_kernel_note": "whole step at the sum of every kernel's own unique arrays (%d B per "
+                                    "cell-step; counts re-reads between kernels)" % (step_alg // cells),
                 "note": "frac of %s HBM copy bandwidth; kernel times from CUDA events between launches" % hbm_kind}
 
     # end to end through the C ABI with host buffers (pinned)
@@ -513,12 +568,19 @@ def run_single(args, world, rank, local, pg):
         try:
             ensemble = ensemble_bench(max(2, min(args.steps, 3)), 3)
             hbm_e, _ = peaks()
-            ens_alg = sum(alg_bytes_per_cell_step(k, 3, 3) for k in phases)
-            ensemble["step_alg_bytes_per_cell"] = ens_alg
+            ens_alg = contract_bytes_per_cell_step(1, 4, mixed=True)
+            ensemble["step_contract_bytes_per_cell"] = ens_alg
             ensemble["batched_mixed_hbm_frac"] = ens_alg * ensemble["batched_mixed"] / 1e9 / hbm_e
             ensemble["accuracy"] = ensemble_accuracy()
         except Exception as ex:  # reported, never required
             ensemble = {"error": repr(ex)}
+
+    c3acc = None
+    if rank == 0 and world == 1 and args.workload in ("c2", "c3") and not args.nx and not args.no_c3_accuracy:
+        try:
+            c3acc = c3_accuracy()
+        except Exception as ex:  # reported, never required
+            c3acc = {"error": repr(ex)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -533,7 +595,9 @@ def run_single(args, world, rank, local, pg):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if not args.mixed else "f32+f64-columns",
-            "data": "synthetic (seeded Weisman-Klemp supercell state, 16 bubbles, log-normal scalars)",
+            "data": ("synthetic (seeded f-plane jet channel in thermal-wind balance, +-1 K noise, qv at 80% RH)"
+                     if args.workload == "c3" else
+                     "synthetic (seeded Weisman-Klemp supercell state, 16 bubbles, log-normal scalars)"),
             "config": {"workload": case.name, "form": "mixed" if args.mixed else "plain",
                        "cells": cells, "species": case.desc.n_moist + case.desc.n_scalar,
                        "global_batch": world, "seq_len": None,
@@ -545,6 +609,7 @@ def run_single(args, world, rank, local, pg):
             "clocks": clocks,
             "phases_ms_per_step": {k: round(v[0], 4) for k, v in phases.items()},
             "ensemble": ensemble,
+            "c3_accuracy": c3acc,
         }
         print(json.dumps(line), flush=True)
 

@@ -177,6 +177,14 @@ int wrfgpu_fill_halo(WrfGpuEnsemble* h, int id, char var);
  * Returns WRFGPU_E_NONFINITE / WRFGPU_E_CFL when the bits are set. */
 int wrfgpu_status(WrfGpuEnsemble* h, int member, unsigned* err_bits, double* max_vert_cfl, double* max_horiz_cfl);
 int wrfgpu_clear_status(WrfGpuEnsemble* h);
+/* Self-test of the bounded device wait every TMA-ring kernel uses (no
+ * counterpart in the reference, whose loops have no device waits): one
+ * block waits on an mbarrier phase for at most `polls` polls (1 .. 2^22).
+ * With arrive != 0 the phase is completed first and the call returns 0;
+ * with arrive = 0 nothing completes it, the wait gives up, the block records
+ * the timeout bit in *status_bits and the call returns WRFGPU_E_TIMEOUT —
+ * the device context stays usable. */
+int wrfgpu_selftest_bounded_wait(int polls, int arrive, unsigned* status_bits);
 int wrfgpu_set_cfl_limit(WrfGpuEnsemble* h, double limit);
 int wrfgpu_num_sound_steps(WrfGpuEnsemble* h, int member);
 long long wrfgpu_device_bytes(WrfGpuEnsemble* h);

@@ -3,8 +3,9 @@
  *
  * One entry point per model-layer routine of the physics-off solve_em path,
  * with the reference's Fortran argument order and meaning, so that a Fortran
- * shim can bind each with an ISO_C_BINDING interface and call it in place of
- * the original (INTEGRATION.md shows the interfaces):
+ * shim can bind each with an ISO_C_BINDING interface (an INTERFACE block of
+ * BIND(C) declarations with the same dummy arguments) and call it in place
+ * of the original:
  *
  *   - every argument is passed by reference (a pointer), as Fortran does
  *     without the VALUE attribute;
@@ -114,8 +115,11 @@ int wrfgpu_advect_scalar_pd(const float *field, const float *field_old, float *t
  * without allocating device memory.  For callers whose state is already on
  * the GPU and that cannot allocate there.  The limiter-factor scratch is a
  * fixed static device array: the memory shape may hold at most 8 Mi points
- * (WRFGPU_E_SIZE otherwise); the first call on a device does a one-time
- * setup; calls that overlap in time race on the shared scratch. */
+ * (WRFGPU_E_SIZE otherwise).  Options a device domain does not accept
+ * return WRFGPU_E_ARG.  The first call on a device (or after its context
+ * was re-created) does a one-time setup and should come before any stream
+ * capture; calls that overlap in time race on the shared scratch.  The
+ * kernels have no device-side failure: the return code is the whole status. */
 int wrfgpu_advect_scalar_pd_noalloc(const float *field, const float *field_old, float *tendency,
                                     const float *ru, const float *rv, const float *rom, const float *c1,
                                     const float *c2, const float *mut, const float *mub, const float *mu_old,
@@ -210,10 +214,9 @@ int wrfgpu_small_step_finish(float *u_2, const float *u_1, float *v_2, const flo
                              const float *h_diabatic, const int *number_of_small_timesteps, const float *dts,
                              const int *rk_step, const int *rk_order, WRFGPU_DIMS_ARGS);
 
-/* dyn_em/module_em.F:1587 rk_update_scalar.  scalar_1 / scalar_2:
- * (ims:ime,kms:kme,jms:jme,*) arrays of which species scs..sce are updated;
- * sc_tend, advh_t, advz_t, h_tendency, z_tendency unused (physics off,
- * tenddec = .false.) */
+/* dyn_em/module_em.F:1587 rk_update_scalar.  scalar_1, scalar_2, sc_tend:
+ * (ims:ime,kms:kme,jms:jme,scs:sce) arrays (sc_tend may be NULL: zero);
+ * advh_t, advz_t, h_tendency, z_tendency unused (tenddec = .false.) */
 int wrfgpu_rk_update_scalar(const int *scs, const int *sce, float *scalar_1, float *scalar_2, const float *sc_tend,
                             const float *advh_t, const float *advz_t, const float *advect_tend,
                             const float *h_tendency, const float *z_tendency, const float *msftx,
@@ -221,6 +224,40 @@ int wrfgpu_rk_update_scalar(const int *scs, const int *sce, float *scalar_1, flo
                             const float *mu_new, const float *mu_base, const int *rk_step, const float *dt,
                             const int *spec_zone, const WrfDynConfig *config_flags, const int *tenddec,
                             WRFGPU_DIMS_ARGS);
+
+/* dyn_em/module_em.F:1803 rk_update_scalar_pd: scalar (the old species,
+ * updated in place) and sc_tend are (ims:ime,kms:kme,jms:jme,scs:sce);
+ * sc_tend is added and then zeroed, as the reference does (spec_zone
+ * unused: no specified boundaries). */
+int wrfgpu_rk_update_scalar_pd(const int *scs, const int *sce, float *scalar, float *sc_tend, const float *c1,
+                               const float *c2, const float *mu_old, const float *mu_new, const float *mu_base,
+                               const int *rk_step, const float *dt, const int *spec_zone,
+                               const WrfDynConfig *config_flags, WRFGPU_DIMS_ARGS);
+
+/* dyn_em/module_em.F:1096 rk_scalar_tend: for each species scs..sce
+ * (scalar, scalar_old, scalar_tends: (ims:ime,kms:kme,jms:jme,scs:sce)),
+ * advect_tend is zeroed over the tile and receives advect_scalar_pd at the
+ * last stage when adv_opt = 1 (positive definite), else advect_scalar; at
+ * stage 1, with diff_6th_opt != 0 and mix6_off false, the species'
+ * sixth-order diffusion is added to scalar_tends.  adv_opt other than 0 / 1,
+ * tenddec, and the explicit-diffusion options return WRFGPU_E_ARG; ww, wwI,
+ * u_old, v_old, c1f, c2f, alt, h_tendency, z_tendency, RQVFTEN, base,
+ * moist_step, rdn, khdif, kvdif, xkmhd, ph, mix2_off are unused on this path
+ * (IEVA off, no cumulus tendency, diff_opt = 0). */
+int wrfgpu_rk_scalar_tend(const int *scs, const int *sce, const WrfDynConfig *config_flags, const int *tenddec,
+                          const int *rk_step, const float *dt_step, const float *ru, const float *rv,
+                          const float *ww, const float *wwE, const float *wwI, const float *u_old,
+                          const float *v_old, const float *mut, const float *mub, const float *mu_old,
+                          const float *c1h, const float *c2h, const float *c1f, const float *c2f,
+                          const float *alt, const float *scalar_old, const float *scalar, float *scalar_tends,
+                          float *advect_tend, float *h_tendency, float *z_tendency, const float *RQVFTEN,
+                          const float *base, const int *moist_step, const float *fnm, const float *fnp,
+                          const float *msfux, const float *msfuy, const float *msfvx, const float *msfvx_inv,
+                          const float *msfvy, const float *msftx, const float *msfty, const float *rdx,
+                          const float *rdy, const float *rdn, const float *rdnw, const float *khdif,
+                          const float *kvdif, const float *xkmhd, const int *diff_6th_opt,
+                          const float *diff_6th_factor, const int *adv_opt, const float *phb, const float *ph,
+                          const int *mix2_off, const int *mix6_off, WRFGPU_DIMS_ARGS);
 
 /* dyn_em/module_big_step_utilities_em.F:953 calc_p_rho_phi (non-hydrostatic,
  * hypsometric_opt 1 or 2; moist: (ims:ime,kms:kme,jms:jme,n_moist)) */

@@ -163,6 +163,20 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
       rk_update_scalar_pd(D.qold(species), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_1),
                           p2(WRFGPU_MUB), dt_rk, (R*)nullptr, td);
       return 0;
+    case ORACLE_R_UPDATE_SCALAR_PD_ARGS:
+      rk_update_scalar_pd(D.qold(species), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_2),
+                          p2(WRFGPU_MUB), dt_rk, p3(WRFGPU_H_DIABATIC), td);
+      return 0;
+    case ORACLE_R_UPDATE_SCALAR_ARGS:
+      rk_update_scalar(D.qold(species), D.q(species), p3(WRFGPU_ADVECT_TEND), p2(WRFGPU_MSFTY), p1(WRFGPU_C1H),
+                       p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), rk_step, dt_rk,
+                       p3(WRFGPU_H_DIABATIC), td);
+      return 0;
+    case ORACLE_R_SIXTH_DIFF_SPECIES:
+      sixth_order_diffusion('m', D.q(species), p3(WRFGPU_H_DIABATIC), p2(WRFGPU_MUTS), dt_rk, cf, p1(WRFGPU_C1H),
+                            p1(WRFGPU_C2H), p3(WRFGPU_PHB), rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
+                            p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
+      return 0;
     case ORACLE_R_ADVECT_SCALAR:
       zero_tend(p3(WRFGPU_ADVECT_TEND), td);
       advect_scalar(D.q(species), D.q(species), p3(WRFGPU_ADVECT_TEND), p3(WRFGPU_RU_M), p3(WRFGPU_RV_M),

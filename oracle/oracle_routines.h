@@ -29,6 +29,11 @@ enum {
   ORACLE_R_UPDATE_SCALAR = 23,
   ORACLE_R_CALC_P_RHO_PHI = 24,
   ORACLE_R_SET_W_SURFACE = 25,
-  ORACLE_R_RK_TENDENCY = 26
+  ORACLE_R_RK_TENDENCY = 26,
+  /* the routine-level C entry points' forms: sc_tend (and rk_scalar_tend's
+   * scalar_tends) carried in the H_DIABATIC field, mu_new in MU_2 */
+  ORACLE_R_UPDATE_SCALAR_PD_ARGS = 30,
+  ORACLE_R_UPDATE_SCALAR_ARGS = 31,
+  ORACLE_R_SIXTH_DIFF_SPECIES = 32
 };
 #endif

@@ -106,7 +106,7 @@ ROUTINES["advect_scalar_pd"] = (
      F("muts"), F("mub"), F("mu_1"), I(1), CFG, I(0)] + _MSF
     + [F("fnm"), F("fnp"), S("rdx"), S("rdy"), F("rdnw"), S("dtrk"), DIMS], ["advect_tend"])
 ROUTINES["rk_update_scalar"] = (
-    [I(1), I(1), F("qv_old"), F("qv"), NUL, NUL, NUL, F("advect_tend"), NUL, NUL, F("msftx"), F("msfty"),
+    [I(1), I(1), F("qv_old"), F("qv"), Z("h_diabatic"), NUL, NUL, F("advect_tend"), NUL, NUL, F("msftx"), F("msfty"),
      F("c1h"), F("c2h"), F("mu_1"), F("mu_2"), F("mub"), I("rk"), S("dtrk"), I(0), CFG, I(0), DIMS],
     ["qv_old", "qv"])
 STAGE = {"advect_scalar_pd": 3}
@@ -258,3 +258,195 @@ def test_routine_abi_rejects_tiles(gpulib, case):
                 v = C.c_int(d); keep.append(v); args.append(C.cast(C.pointer(v), C.c_void_p))
     fn.argtypes = [C.c_void_p] * len(args)
     assert fn(*args) == abi.WRFGPU_E_ARG
+
+
+# --------------------------------------------------------------------------
+# Scalar entry points over several species: 4-D (ims:ime,kms:kme,jms:jme,
+# scs:sce) arrays, sc_tend carried through, rk_scalar_tend's dispatch.
+# --------------------------------------------------------------------------
+class _Argv:
+    """ctypes arguments by reference, kept alive for the call."""
+
+    def __init__(self):
+        self.keep, self.args = [], []
+
+    def arr(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        self.keep.append(a)
+        self.args.append(a.ctypes.data_as(C.c_void_p))
+        return a
+
+    def ptr(self, a, offset_elems=0):
+        self.keep.append(a)
+        self.args.append(C.c_void_p(a.ctypes.data + 4 * offset_elems))
+
+    def null(self):
+        self.args.append(C.c_void_p(None))
+
+    def f32(self, v):
+        x = C.c_float(v); self.keep.append(x); self.args.append(C.cast(C.pointer(x), C.c_void_p))
+
+    def i32(self, v):
+        x = C.c_int(v); self.keep.append(x); self.args.append(C.cast(C.pointer(x), C.c_void_p))
+
+    def cfg(self, cf):
+        p = C.pointer(cf); self.keep.append(p); self.args.append(C.cast(p, C.c_void_p))
+
+    def dims(self, case):
+        h = abi.HALO
+        for d in [1, case.ide, 1, case.jde, 1, case.kde, 1 - h, case.ide + h, 1 - h, case.jde + h, 1, case.kde,
+                  1, case.ide, 1, case.jde, 1, case.kde]:
+            self.i32(d)
+
+    def call(self, lib, name):
+        fn = getattr(lib, name)
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_void_p] * len(self.args)
+        return fn(*self.args)
+
+
+def _stack(od, ids):
+    return np.ascontiguousarray(np.concatenate([np.asarray(od.get(f), dtype=np.float32) for f in ids]))
+
+
+@pytest.fixture(scope="module")
+def case3():
+    """Three species (qv + 2 PD scalars), sixth-order diffusion on."""
+    c = cases.small_case(nx=16, ny=12, kde=14, n_scalar=2, seed=27)
+    c.desc.config.diff_6th_opt = 2
+    c.desc.config.diff_6th_factor = 0.12
+    c.desc.config.diff_6th_thresh = 0.10
+    return c
+
+
+def _f(od, nm):
+    return np.asarray(od.get(_fid(nm)), dtype=np.float32)
+
+
+def test_rk_update_scalar_pd_abi_bitwise(gpulib, case3):
+    """wrfgpu_rk_update_scalar_pd (module_em.F:1803) over species 1..3 with a
+    non-zero sc_tend and mu_new != mu_old: each old species bit for bit with
+    the oracle's rk_update_scalar_pd; sc_tend zeroed over the update region
+    and untouched elsewhere."""
+    case = case3
+    od = _state(case)
+    nsp = 3
+    n3 = od.get(abi.species_id(0)).size
+    rng = np.random.Generator(np.random.PCG64(9))
+    sct = (1e-9 * rng.standard_normal(nsp * n3)).astype(np.float32)
+    mu_new = _f(od, "mu_2") + np.float32(3.0)
+    scal = _scalars(case, 3, 1)
+    a = _Argv()
+    a.i32(1); a.i32(nsp)
+    q = a.arr(_stack(od, [abi.species_id(s, True) for s in range(nsp)]))
+    sct_gpu = a.arr(sct.copy())
+    a.arr(_f(od, "c1h")); a.arr(_f(od, "c2h")); a.arr(_f(od, "mu_1")); a.arr(mu_new); a.arr(_f(od, "mub"))
+    a.i32(3); a.f32(scal["dtrk"]); a.i32(0); a.cfg(case.desc.config); a.dims(case)
+    assert a.call(gpulib, "wrfgpu_rk_update_scalar_pd") == 0
+    od.set(abi.FIELD_ID["mu_2"], mu_new)
+    bad = []
+    for s in range(nsp):
+        od.set(abi.FIELD_ID["h_diabatic"], sct[s * n3:(s + 1) * n3])
+        od.run("rk_update_scalar_pd_args", 3, 0, s)
+        fid = abi.species_id(s, True)
+        d = max_abs(interior(case, fid, q[s * n3:(s + 1) * n3], halo=0), interior(case, fid, od.get(fid), halo=0))
+        if d != 0.0:
+            bad.append("species %d: max|diff| %.3e" % (s, d))
+    assert not bad, bad
+    # sc_tend: zero over the update region i < ide, k < kde, j < jde, else untouched
+    h = abi.HALO
+    shape = (case.jde + 2 * h, case.kde, -1)
+    for s in range(nsp):
+        got = sct_gpu[s * n3:(s + 1) * n3].reshape(shape)
+        ref = sct[s * n3:(s + 1) * n3].reshape(shape).copy()
+        ref[h:h + case.jde - 1, 0:case.kde - 1, h:h + case.ide - 1] = 0.0
+        assert np.array_equal(got, ref), s
+
+
+@pytest.mark.parametrize("rk", [1, 2])
+def test_rk_update_scalar_abi_offset_species_bitwise(gpulib, case3, rk):
+    """wrfgpu_rk_update_scalar over species 2..3 only (arrays dimensioned
+    scs:sce, the way solve_em passes moist(ims,kms,jms,im)), with sc_tend:
+    bit for bit with the oracle's rk_update_scalar."""
+    case = case3
+    od = _state(case)
+    n3 = od.get(abi.species_id(0)).size
+    rng = np.random.Generator(np.random.PCG64(10 + rk))
+    sct = (1e-9 * rng.standard_normal(2 * n3)).astype(np.float32)
+    adv = (1e-7 * rng.standard_normal(n3)).astype(np.float32)
+    scal = _scalars(case, rk, 1)
+    a = _Argv()
+    a.i32(2); a.i32(3)
+    q1 = a.arr(_stack(od, [abi.species_id(s, True) for s in (1, 2)]))
+    q2 = a.arr(_stack(od, [abi.species_id(s) for s in (1, 2)]))
+    a.arr(sct); a.null(); a.null(); a.arr(adv); a.null(); a.null()
+    for nm in ("msftx", "msfty", "c1h", "c2h", "mu_1", "mu_2", "mub"):
+        a.arr(_f(od, nm))
+    a.i32(rk); a.f32(scal["dtrk"]); a.i32(0); a.cfg(case.desc.config); a.i32(0); a.dims(case)
+    assert a.call(gpulib, "wrfgpu_rk_update_scalar") == 0
+    od.set(abi.FIELD_ID["advect_tend"], adv)
+    bad = []
+    for n, s in enumerate((1, 2)):
+        od.set(abi.FIELD_ID["h_diabatic"], sct[n * n3:(n + 1) * n3])
+        od.run("rk_update_scalar_args", rk, 0, s)
+        for fid, got in ((abi.species_id(s, True), q1), (abi.species_id(s), q2)):
+            d = max_abs(interior(case, fid, got[n * n3:(n + 1) * n3], halo=0), interior(case, fid, od.get(fid), halo=0))
+            if d != 0.0:
+                bad.append("species %d field %d: max|diff| %.3e" % (s, fid, d))
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("rk", [1, 3])
+def test_rk_scalar_tend_abi_bitwise(gpulib, case3, rk):
+    """wrfgpu_rk_scalar_tend (module_em.F:1096) over species 1..3: advect_tend
+    zeroed over the tile and left holding the last species' tendency
+    (advect_scalar at stage 1, advect_scalar_pd at the last stage with
+    adv_opt = 1), and at stage 1 every species' sixth-order diffusion added
+    to its scalar_tends; bit for bit with the oracle's routines."""
+    case = case3
+    od = _state(case)
+    nsp = 3
+    n3 = od.get(abi.species_id(0)).size
+    rng = np.random.Generator(np.random.PCG64(20 + rk))
+    tends0 = (1e-9 * rng.standard_normal(nsp * n3)).astype(np.float32)
+    scal = _scalars(case, rk, 1)
+    a = _Argv()
+    a.i32(1); a.i32(nsp); a.cfg(case.desc.config); a.i32(0); a.i32(rk); a.f32(scal["dtrk"])
+    for nm in ("ru_m", "rv_m", "ww_m", "ww_m"):
+        a.arr(_f(od, nm))
+    a.null(); a.null(); a.null()                        # wwI, u_old, v_old
+    for nm in ("muts", "mub", "mu_1", "c1h", "c2h", "c1f", "c2f", "alt"):
+        a.arr(_f(od, nm))
+    a.arr(_stack(od, [abi.species_id(s, True) for s in range(nsp)]))
+    a.arr(_stack(od, [abi.species_id(s) for s in range(nsp)]))
+    tends = a.arr(tends0.copy())
+    adv = a.arr((1e3 * np.ones(n3)).astype(np.float32))  # garbage the call must zero
+    a.null(); a.null(); a.null(); a.null(); a.i32(1)     # h_, z_tendency, RQVFTEN, base, moist_step
+    for nm in ("fnm", "fnp", "msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy", "msftx", "msfty"):
+        a.arr(_f(od, nm))
+    a.f32(scal["rdx"]); a.f32(scal["rdy"]); a.arr(_f(od, "rdn")); a.arr(_f(od, "rdnw"))
+    a.f32(0.0); a.f32(0.0); a.null()                    # khdif, kvdif, xkmhd
+    a.i32(2); a.f32(0.12); a.i32(1); a.arr(_f(od, "phb")); a.arr(_f(od, "ph_2")); a.i32(0); a.i32(0)
+    a.dims(case)
+    assert a.call(gpulib, "wrfgpu_rk_scalar_tend") == 0
+    bad = []
+    # advect_tend: the last species' advection
+    od.run("advect_scalar_pd" if rk == 3 else "advect_scalar", rk, 0, nsp - 1)
+    fid = abi.FIELD_ID["advect_tend"]
+    d = max_abs(interior(case, fid, adv, halo=0), interior(case, fid, od.get(fid), halo=0))
+    if d != 0.0:
+        bad.append("advect_tend: max|diff| %.3e" % d)
+    for s in range(nsp):
+        got = tends[s * n3:(s + 1) * n3]
+        if rk == 1:
+            od.set(abi.FIELD_ID["h_diabatic"], tends0[s * n3:(s + 1) * n3])
+            od.run("sixth_diff_species", 1, 0, s)
+            ref = od.get(abi.FIELD_ID["h_diabatic"])
+        else:
+            ref = tends0[s * n3:(s + 1) * n3]
+        d = max_abs(interior(case, fid, got, halo=0), interior(case, fid, ref, halo=0))
+        if d != 0.0:
+            bad.append("scalar_tends %d: max|diff| %.3e" % (s, d))
+    assert not bad, bad
+    if rk == 1:  # the diffusion was active
+        assert max_abs(interior(case, fid, tends[:n3], halo=0), interior(case, fid, tends0[:n3], halo=0)) > 0.0

@@ -106,6 +106,8 @@ ROUTINES = {
     "sumflux": 18, "small_step_finish": 19, "rk_update_scalar_pd": 20,
     "advect_scalar": 21, "advect_scalar_pd": 22, "rk_update_scalar": 23,
     "calc_p_rho_phi": 24, "set_w_surface": 25, "rk_tendency": 26,
+    # oracle-only forms checked against the routine-level C entry points
+    "rk_update_scalar_pd_args": 30, "rk_update_scalar_args": 31, "sixth_diff_species": 32,
 }
 
 

@@ -211,6 +211,38 @@ def fill_halo(arr, kind, stag, ide, jde, cfg):
     return out * sign_y[:, None]
 
 
+def _column_p_al(t1, qv3, mu1_2d, mub, pb, alb, c1f, c2f, rdnw, rdn, kde):
+    """module_initialize_ideal.F:1035-1060: p, alt, al by downward integration
+    of every column (arrays (j, k, i); mub a scalar or an (j, i) array)."""
+    p = np.zeros_like(t1); alt = np.zeros_like(t1); al = np.zeros_like(t1)
+    kk = kde - 1; k = kk + 1
+    qvf1 = 0.5 * (qv3[:, kk - 1] + qv3[:, kk - 1]); qvf2 = 1.0 / (1.0 + qvf1); qvf1 = qvf1 * qvf2
+    p[:, kk - 1] = -0.5 * ((c1f[k] * mu1_2d) + qvf1 * (c1f[k] * mub + c2f[k])) / rdnw[kk] / qvf2
+    qvf = 1.0 + RVOVRD * qv3[:, kk - 1]
+    alt[:, kk - 1] = (R_D / P1000) * (t1[:, kk - 1] + T0) * qvf * (((p[:, kk - 1] + pb[kk]) / P1000) ** CVPM)
+    al[:, kk - 1] = alt[:, kk - 1] - alb[kk]
+    for kk in range(kde - 2, 0, -1):
+        k = kk + 1
+        qvf1 = 0.5 * (qv3[:, kk - 1] + qv3[:, kk]); qvf2 = 1.0 / (1.0 + qvf1); qvf1 = qvf1 * qvf2
+        p[:, kk - 1] = p[:, kk] - ((c1f[k] * mu1_2d) + qvf1 * (c1f[k] * mub + c2f[k])) / qvf2 / rdn[kk + 1]
+        qvf = 1.0 + RVOVRD * qv3[:, kk - 1]
+        alt[:, kk - 1] = (R_D / P1000) * (t1[:, kk - 1] + T0) * qvf * (((p[:, kk - 1] + pb[kk]) / P1000) ** CVPM)
+        al[:, kk - 1] = alt[:, kk - 1] - alb[kk]
+    return p, alt, al
+
+
+def _column_ph(al, mu1_2d, mub, alb, c1h, c2h, dnw, kde, ni):
+    """module_initialize_ideal.F:1063-1075: perturbation geopotential by
+    upward integration of every column."""
+    nj = al.shape[0]
+    ph = np.zeros((nj, kde, ni))
+    for kk in range(2, kde + 1):
+        k = kk - 1
+        ph[:, kk - 1] = ph[:, kk - 2] - dnw[kk - 1] * (((c1h[k] * mub + c2h[k]) + (c1h[k] * mu1_2d)) * al[:, kk - 2]
+                                                      + (c1h[k] * mu1_2d) * alb[kk - 1])
+    return ph
+
+
 # ---------------------------------------------------------------------------
 # ideal supercell-type state
 # ---------------------------------------------------------------------------
@@ -280,30 +312,10 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     mu1_2d = np.full((nj, ni), mu1)
 
     def column_p_al(t1, qv3, mu1_2d):
-        """module_initialize_ideal.F:1035-1060: p, alt, al by downward integration."""
-        p = np.zeros_like(t1); alt = np.zeros_like(t1); al = np.zeros_like(t1)
-        kk = kde - 1; k = kk + 1
-        qvf1 = 0.5 * (qv3[:, kk - 1] + qv3[:, kk - 1]); qvf2 = 1.0 / (1.0 + qvf1); qvf1 = qvf1 * qvf2
-        p[:, kk - 1] = -0.5 * ((c1f[k] * mu1_2d) + qvf1 * (c1f[k] * mub + c2f[k])) / rdnw[kk] / qvf2
-        qvf = 1.0 + RVOVRD * qv3[:, kk - 1]
-        alt[:, kk - 1] = (R_D / P1000) * (t1[:, kk - 1] + T0) * qvf * (((p[:, kk - 1] + pb[kk]) / P1000) ** CVPM)
-        al[:, kk - 1] = alt[:, kk - 1] - alb[kk]
-        for kk in range(kde - 2, 0, -1):
-            k = kk + 1
-            qvf1 = 0.5 * (qv3[:, kk - 1] + qv3[:, kk]); qvf2 = 1.0 / (1.0 + qvf1); qvf1 = qvf1 * qvf2
-            p[:, kk - 1] = p[:, kk] - ((c1f[k] * mu1_2d) + qvf1 * (c1f[k] * mub + c2f[k])) / qvf2 / rdn[kk + 1]
-            qvf = 1.0 + RVOVRD * qv3[:, kk - 1]
-            alt[:, kk - 1] = (R_D / P1000) * (t1[:, kk - 1] + T0) * qvf * (((p[:, kk - 1] + pb[kk]) / P1000) ** CVPM)
-            al[:, kk - 1] = alt[:, kk - 1] - alb[kk]
-        return p, alt, al
+        return _column_p_al(t1, qv3, mu1_2d, mub, pb, alb, c1f, c2f, rdnw, rdn, kde)
 
     def column_ph(al, mu1_2d):
-        ph = np.zeros((nj, kde, ni))
-        for kk in range(2, kde + 1):
-            k = kk - 1
-            ph[:, kk - 1] = ph[:, kk - 2] - dnw[kk - 1] * (((c1h[k] * mub + c2h[k]) + (c1h[k] * mu1_2d)) * al[:, kk - 2]
-                                                          + (c1h[k] * mu1_2d) * alb[kk - 1])
-        return ph
+        return _column_ph(al, mu1_2d, mub, alb, c1h, c2h, dnw, kde, ni)
 
     p3, alt3, al3 = column_p_al(t1, qv3, mu1_2d)
     ph1 = column_ph(al3, mu1_2d)
@@ -399,6 +411,175 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     return Case(name, desc, f, species, meta)
 
 
+def _column_sounding(z, theta, rh, dz, p_surf=P1000):
+    """Hydrostatic moist sounding on the height grid z (spacing dz) for a
+    potential-temperature profile theta and a relative-humidity profile rh:
+    full pressure p (integrated up from p_surf with the virtual potential
+    temperature, the water vapour iterated to the given humidity), dry-air
+    pressure pd (the dry-air density integrated down from the top, as
+    get_sounding_b_wave does, module_initialize_ideal.F:2072-2080) and qv."""
+    qv = np.zeros_like(z)
+    p = np.zeros_like(z)
+    for _ in range(4):
+        pi = np.empty_like(z)
+        pi[0] = (p_surf / P1000) ** (R_D / CP)
+        thv = theta * (1.0 + 0.61 * qv)
+        for k in range(1, len(z)):
+            pi[k] = pi[k - 1] - G * dz / (CP * 0.5 * (thv[k] + thv[k - 1]))
+        p = P1000 * pi ** (CP / R_D)
+        t = theta * pi
+        qv = rh * _qvs(p, t)
+    t = theta * (p / P1000) ** (R_D / CP)
+    rho = p / (R_D * t * (1.0 + 0.61 * qv))
+    rho_d = rho / (1.0 + qv)
+    pd = np.empty_like(z)
+    pd[-1] = p[-1] / (1.0 + qv[-1] * RVOVRD)
+    for k in range(len(z) - 2, -1, -1):
+        pd[k] = pd[k + 1] + G * dz * 0.5 * (rho_d[k] + rho_d[k + 1])
+    return p, pd, qv
+
+
+def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10000.0, noise=1.0,
+                  z_noise=2000.0, rh=0.8, z_moist=8000.0, n_scalar=0, name="channel", dz=20.0):
+    """Zonally periodic channel on an f-plane with a balanced zonal jet
+    (the idealised baroclinic-wave case of module_initialize_ideal.F, b_wave,
+    :240-260, :344-360, :738-760, :992-1090, restated with an analytic jet
+    instead of the tabulated input_jet):
+
+    * u(y, z) = u_max sin^2(pi y / Ly) min(z, z_jet) / z_jet;
+    * theta(y, z) = theta_ref(z) - (f theta_ref(z) / g) (u_max / z_jet) Y(y)
+      below z_jet, theta_ref(z) above, with Y(y) = y / 2 - Ly / (4 pi)
+      sin(2 pi y / Ly): thermal-wind balance f du/dz = -(g / theta) dtheta/dy
+      (cold to the north; the jump at z_jet is stable everywhere); theta_ref is
+      the Weisman-Klemp dry profile (300 K surface, 12 km / 343 K tropopause);
+    * qv from rh relative humidity below z_moist (0 above);
+    * a seeded uniform +-noise K perturbation of theta below z_noise;
+    * every row's column in hydrostatic balance from a uniform surface
+      pressure; the base state is the middle row's dry sounding (as b_wave
+      takes the middle column of its jet), flat terrain;
+    * periodic in x, symmetric (free-slip walls) in y, Coriolis f, e = 0.
+    """
+    ide, jde = nx + 1, ny + 1
+    cfg = abi.default_config(periodic_x=True, periodic_y=False, symmetric_y=True)
+    h = abi.HALO
+    nim, njm, nk = ide + 2 * h, jde + 2 * h, kde
+    m = eta_metrics(kde)
+    Ly = ny * dx
+    z = np.arange(0.0, ztop + 4000.0 + dz, dz)
+    theta_ref = np.where(z <= 12000.0, 300.0 + 43.0 * (z / 12000.0) ** 1.25,
+                         343.0 * np.exp(G / (CP * 213.0) * (z - 12000.0)))
+    yj = (np.arange(1, ny + 1) - 0.5) * dx
+    Y = yj / 2.0 - Ly / (4.0 * math.pi) * np.sin(2.0 * math.pi * yj / Ly)
+    below = z <= z_jet
+    rh_prof = np.where(z <= z_moist, rh, 0.0)
+
+    def row_theta(y_int):
+        return theta_ref - np.where(below, f * theta_ref / G * (u_max / z_jet) * y_int, 0.0)
+
+    # base state: the middle row's dry sounding
+    jmid = ny // 2
+    p_mid, pd_mid, _ = _column_sounding(z, row_theta(Y[jmid]), np.zeros_like(z), dz)
+    p_top = float(_interp(ztop, z, p_mid))
+    hc = hybrid_coefs(m, kde, p_top)
+    c1h, c2h, c1f, c2f = hc["c1h"], hc["c2h"], hc["c1f"], hc["c2f"]
+    c3h, c4h, c3f, c4f = hc["c3h"], hc["c4h"], hc["c3f"], hc["c4f"]
+    dnw, rdnw, rdn = m["dnw"], m["rdnw"], m["rdn"]
+    th_mid = row_theta(Y[jmid])
+    p_surf = float(p_mid[0])
+    mub = p_surf - p_top
+    pb = np.zeros(kde + 1); t_init = np.zeros(kde + 1); alb = np.zeros(kde + 1); phb = np.zeros(kde + 1)
+    for k in range(1, kde):
+        pl = c3h[k] * (p_surf - p_top) + c4h[k] + p_top
+        pb[k] = pl
+        t_init[k] = _interp(pl, p_mid, th_mid) - T0
+        alb[k] = (R_D / P1000) * (t_init[k] + T0) * (pb[k] / P1000) ** CVPM
+    for kk in range(2, kde + 1):
+        k = kk - 1
+        phb[kk] = phb[kk - 1] - dnw[kk - 1] * (c1h[k] * mub + c2h[k]) * alb[kk - 1]
+    zhalf = np.array([0.5 * (phb[k] + phb[k + 1]) / G if 1 <= k < kde else 0.0 for k in range(kde + 1)])
+
+    # full state, row by row (columns of a row are identical before the noise)
+    ni, nj, nkm = nx, ny, kde - 1
+    t1 = np.zeros((nj, nkm, ni)); qv3 = np.zeros((nj, nkm, ni)); u3 = np.zeros((nj, nkm, ni))
+    mu1_2d = np.zeros((nj, ni))
+    for j in range(nj):
+        th_j = row_theta(Y[j])
+        _, pd_j, qv_j = _column_sounding(z, th_j, rh_prof, dz)
+        pd_surf = float(pd_j[0])
+        mu1_2d[j, :] = pd_surf - p_top - mub
+        for k in range(1, kde):
+            pl = c3h[k] * (pd_surf - p_top) + c4h[k] + p_top
+            qv3[j, k - 1, :] = _interp(pl, pd_j, qv_j)
+            t1[j, k - 1, :] = _interp(pl, pd_j, th_j) - T0
+            u3[j, k - 1, :] = u_max * math.sin(math.pi * yj[j] / Ly) ** 2 * min(zhalf[k], z_jet) / z_jet
+
+    p3, alt3, al3 = _column_p_al(t1, qv3, mu1_2d, mub, pb, alb, c1f, c2f, rdnw, rdn, kde)
+    ph1 = _column_ph(al3, mu1_2d, mub, alb, c1h, c2h, dnw, kde, ni)
+    if noise > 0:
+        zmass = 0.5 * (ph1[:, :-1] + ph1[:, 1:] + (phb[1:kde] + phb[2:kde + 1])[None, :, None]) / G
+        t1 = t1 + np.where(zmass < z_noise, rng.uniform(-noise, noise, size=t1.shape), 0.0)
+    p3, alt3, al3 = _column_p_al(t1, qv3, mu1_2d, mub, pb, alb, c1f, c2f, rdnw, rdn, kde)
+    ph1 = _column_ph(al3, mu1_2d, mub, alb, c1h, c2h, dnw, kde, ni)
+    tm = (t1 + T0) * (1.0 + (R_V / R_D) * qv3) - T0
+    mut = mub + mu1_2d
+    al3 = np.zeros_like(tm)
+    for k in range(1, kde):
+        pfu = c3f[k + 1] * mut + c4f[k + 1] + p_top
+        pfd = c3f[k] * mut + c4f[k] + p_top
+        phm = c3h[k] * mut + c4h[k] + p_top
+        al3[:, k - 1] = (ph1[:, k] - ph1[:, k - 1] + phb[k + 1] - phb[k]) / phm / np.log(pfd / pfu) - alb[k]
+    p3 = P1000 * ((R_D * (T0 + tm)) / (P1000 * (al3 + alb[1:kde][None, :, None]))) ** CPOVCV - pb[1:kde][None, :, None]
+    alt3 = al3 + alb[1:kde][None, :, None]
+
+    def mem3(interior, nkk, stag=None):
+        a = np.zeros((njm, nk, nim))
+        a[h:h + interior.shape[0], :nkk, h:h + interior.shape[2]] = interior
+        if stag == "u":
+            a[h:h + interior.shape[0], :nkk, h + nx] = interior[:, :, 0]
+        return fill_halo(a, 3, stag, ide, jde, cfg)
+
+    def mem2(interior):
+        a = np.zeros((njm, nim))
+        a[h:h + nj, h:h + ni] = interior
+        return fill_halo(a, 2, None, ide, jde, cfg)
+
+    def col(v1d, nkk):
+        return np.broadcast_to(v1d[1:nkk + 1][None, :, None], (nj, nkk, ni))
+
+    fl = {}
+    fl["u_1"] = mem3(u3, nkm, "u"); fl["u_2"] = fl["u_1"].copy()
+    fl["v_1"] = np.zeros((njm, nk, nim)); fl["v_2"] = np.zeros((njm, nk, nim))
+    fl["w_1"] = np.zeros((njm, nk, nim)); fl["w_2"] = np.zeros((njm, nk, nim))
+    fl["t_1"] = mem3(tm, nkm); fl["t_2"] = fl["t_1"].copy()
+    fl["ph_1"] = mem3(ph1, kde); fl["ph_2"] = fl["ph_1"].copy()
+    fl["phb"] = mem3(col(phb, kde), kde)
+    fl["pb"] = mem3(col(pb, nkm), nkm)
+    fl["alb"] = mem3(col(alb, nkm), nkm)
+    fl["p"] = mem3(p3, nkm)
+    fl["al"] = mem3(al3, nkm)
+    fl["alt"] = mem3(alt3, nkm)
+    fl["mu_1"] = mem2(mu1_2d); fl["mu_2"] = fl["mu_1"].copy()
+    fl["mub"] = mem2(np.full((nj, ni), mub))
+    for nm in ("msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy", "msftx", "msfty", "cosa"):
+        fl[nm] = np.ones((njm, nim))
+    for nm in ("ht", "e", "sina"):
+        fl[nm] = np.zeros((njm, nim))
+    fl["f"] = np.full((njm, nim), f)
+    for nm in ("znw", "znu", "dnw", "rdnw", "dn", "rdn", "fnm", "fnp"):
+        fl[nm] = m[nm][1:].copy()
+    for nm in ("c1h", "c2h", "c1f", "c2f", "c3h", "c4h", "c3f", "c4f"):
+        fl[nm] = hc[nm][1:].copy()
+    qv_mem = mem3(qv3, nkm)
+    species = [(qv_mem, qv_mem.copy())]
+    for _ in range(n_scalar):
+        qs = 1.0e-6 * np.exp(rng.standard_normal(size=(nj, nkm, ni)))
+        qm = mem3(qs, nkm)
+        species.append((qm, qm.copy()))
+    desc = _make_desc(ide, jde, kde, n_scalar, cfg, dt, dx, m, p_top)
+    meta = dict(dx=dx, dt=dt, ztop=ztop, f=f, u_max=u_max, z_jet=z_jet, n_scalar=n_scalar)
+    return Case(name, desc, fl, species, meta)
+
+
 def _make_desc(ide, jde, kde, n_scalar, cfg, dt, dx, m, p_top):
     desc = abi.WrfGpuDomainDesc()
     desc.ide, desc.jde, desc.kde = ide, jde, kde
@@ -453,6 +634,18 @@ def config2(seed=2, nx=512, kde=80, n_scalar=10):
         bubbles.append((float(xc), float(yc), 1500.0, 10000.0, 10000.0, 1500.0, 3.0))
     return supercell_state(nx, nx, kde, dx, 6.0, 20000.0, bubbles, rng, n_scalar=n_scalar,
                            name="c2_%dx%dx%d" % (nx, nx, kde))
+
+
+def config3(seed=3, nx=1024, ny=None, kde=96, dx=4000.0, dt=20.0, ztop=25000.0):
+    """1024 x 1024 x 96 levels, dx = 4 km, top 25 km, dt = 20 s: the zonally
+    periodic f-plane channel (f = 1e-4) with the balanced jet
+    u = 30 sin^2(pi y / Ly) (z / 10 km), capped above 10 km, theta in
+    thermal-wind balance, +-1 K seeded noise below 2 km, qv at 80 % RH below
+    8 km; qv is the one (positive-definite) species.  nx, ny give the
+    same channel at other sizes (same dx, so a narrower channel)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ny = nx if ny is None else ny
+    return channel_state(nx, ny, kde, dx, dt, ztop, rng, name="c3_%dx%dx%d" % (nx, ny, kde))
 
 
 def ensemble_members(seed=4, n=64, nmin=64, nmax=256, kmin=41, kmax=80, n_scalar=3, dx=2000.0, dt=12.0):

@@ -334,11 +334,12 @@ __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.p
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-// Bounded wait for phase `parity` of the barrier; false after ~2^22 polls
-// (seconds), in which case the caller flags ERR_TIMEOUT and carries on.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// Bounded wait for phase `parity` of the barrier; false after `polls` polls
+// (2^22 by default: seconds), in which case the caller flags ERR_TIMEOUT and
+// carries on.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int polls = 1 << 22) {
   const unsigned a = smem_u32(bar);
-  for (int it = 0; it < (1 << 22); ++it) {
+  for (int it = 0; it < polls; ++it) {
     unsigned ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

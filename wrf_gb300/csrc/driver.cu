@@ -55,7 +55,7 @@ static const char* PHASE_NAMES[NPHASE] = {
     "sumflux_calc_p_rho", "small_step_finish", "rk_update_scalar_pd", "scalar_pd_update", "scalar_adv_update",
     "rk_update_scalar", "calc_p_rho_phi", "set_w_surface", "sixth_order_diffusion", "end"};
 
-static int check_desc(const WrfGpuDomainDesc& d) {
+int check_desc(const WrfGpuDomainDesc& d) {
   const WrfDynConfig& c = d.config;
   if (d.ide < 8 || d.jde < 8 || d.kde < 6 || d.kde > 128) return WRFGPU_E_ARG;
   if (d.n_moist != 1 || d.n_scalar < 0 || d.n_moist + d.n_scalar > NSPMAX) return WRFGPU_E_ARG;
@@ -616,6 +616,11 @@ struct Ensemble {
       case 121: launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, species, 4}, stream); break;
       case 122: launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, species, 6}, d_pd_scratch, stream); break;
       case 23: launch_update_scalar(l3, nb3, a, stream); break;
+      // routine-level C ABI forms of the scalar updates (sc_tend in H_DIABATIC)
+      // and of rk_scalar_tend's sixth-order diffusion of one species
+      case 130: launch_update_scalar_routine(l3, nb3, rk_step, 0, stream); break;
+      case 131: launch_update_scalar_routine(l3, nb3, rk_step, 1, stream); break;
+      case 132: launch_sixth_diff_species_routine(l3, nb3, stream); break;
       case 24: launch_calc_p_rho_phi(l3, nb3, stream); break;
       case 25: launch_set_w_surface(l2, nb2, stream); break;
       case 26:
@@ -632,11 +637,31 @@ struct Ensemble {
 };
 
 // ---------------------------------------------------------------------------
+// Self-test of the bounded device wait: one block waits on an mbarrier phase
+// with a poll limit.  With `arrive` thread 0 completes the phase first (the
+// wait succeeds); without it nothing ever arrives, the wait runs out after
+// `polls` polls and the block records ERR_TIMEOUT, exactly as the TMA-ring
+// kernels do when a copy never lands, and returns normally.
+// ---------------------------------------------------------------------------
+__global__ void k_selftest_bounded_wait(int polls, int arrive, unsigned* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (arrive && threadIdx.x == 0)
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&bar)) : "memory");
+  const bool ok = mbar_wait(&bar, 0, polls);
+  if (!ok) atomicOr(status, ERR_TIMEOUT);
+}
+
+// ---------------------------------------------------------------------------
 // Routine-level calls in parity mode: a cached single-member scratch domain
 // per (ide, jde, kde, species); copy in, run one routine, copy out.
 // ---------------------------------------------------------------------------
 static std::mutex g_fmu;
-static std::map<std::tuple<int, int, int, int>, Ensemble*> g_fcache;
+static std::map<std::tuple<int, int, int, int, int>, Ensemble*> g_fcache;
 
 int fortran_call(const FCall& c) {
   for (int q = 0; q < 18; ++q)
@@ -654,7 +679,9 @@ int fortran_call(const FCall& c) {
   if (its != ids || ite != ide || jts != jds || jte != jde || kts != kds || kte != kde) return WRFGPU_E_ARG;
   if (c.nsp < 1 || c.nsp > NSPMAX) return WRFGPU_E_ARG;
   std::lock_guard<std::mutex> lock(g_fmu);
-  const auto key = std::make_tuple(ide, jde, kde, c.nsp);
+  // the sixth-order diffusion's stored tendencies are allocated with the domain
+  const int diff6 = c.cfg.diff_6th_opt != 0 ? 1 : 0;
+  const auto key = std::make_tuple(ide, jde, kde, c.nsp, diff6);
   Ensemble* e = nullptr;
   auto it = g_fcache.find(key);
   if (it != g_fcache.end()) e = it->second;
@@ -704,6 +731,12 @@ int fortran_call(const FCall& c) {
     for (int f : {WRFGPU_MU_SAVE, WRFGPU_MU_TEND})
       CK(cudaMemsetAsync(M.f2[f - WRFGPU_F2D_BASE], 0, e->n2[0] * 4, e->stream));
   }
+  for (int id : c.zero_ids) {
+    size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
+    float* p = e->field_ptr(0, id, &cnt, &cols, &rows, &pitch);
+    if (!p) return WRFGPU_E_ARG;
+    CK(cudaMemsetAsync(p, 0, pitch * rows * 4, e->stream));
+  }
   if (c.max_vert_cfl || c.max_horiz_cfl) CK(cudaMemsetAsync(e->d_cfl, 0, sizeof(float) * 2, e->stream));
   int rc = e->run_routine(c.routine, c.rk_step, c.iteration, c.species);
   if (rc) return rc;
@@ -740,6 +773,22 @@ using wrfgpu::Ensemble;
 struct WrfGpuEnsemble { Ensemble e; };
 
 extern "C" {
+
+int wrfgpu_selftest_bounded_wait(int polls, int arrive, unsigned* status_bits) {
+  if (polls <= 0 || polls > (1 << 22) || !status_bits) return WRFGPU_E_ARG;
+  unsigned* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(unsigned)));
+  CK(cudaMemset(d, 0, sizeof(unsigned)));
+  wrfgpu::k_selftest_bounded_wait<<<1, 32>>>(polls, arrive, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  unsigned bits = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&bits, d, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return WRFGPU_E_CUDA;
+  *status_bits = bits;
+  return (bits & wrfgpu::ERR_TIMEOUT) ? WRFGPU_E_TIMEOUT : WRFGPU_OK;
+}
 
 int wrfgpu_ensemble_create(const WrfGpuDomainDesc* descs, int n, int flags, WrfGpuEnsemble** out) {
   if (!descs || n <= 0 || !out) return WRFGPU_E_ARG;

@@ -27,6 +27,7 @@ struct FCall {
   float p_top = -1.f;
   int nsmall = 0;
   bool zero_saves = false;          // rk_tendency: zero the *_save / mu_tend outputs
+  std::vector<int> zero_ids;        // fields set to zero before the routine (unbound inputs read as 0)
   float* max_vert_cfl = nullptr;    // rk_tendency diagnostics
   float* max_horiz_cfl = nullptr;
   std::vector<FBind> binds;
@@ -36,6 +37,8 @@ struct FCall {
 };
 
 int fortran_call(const FCall& c);
+// The options a domain (or a routine-level call) may use: 0 or WRFGPU_E_ARG.
+int check_desc(const WrfGpuDomainDesc& d);
 int fortran_release();
 
 }  // namespace wrfgpu

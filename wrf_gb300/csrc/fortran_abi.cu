@@ -423,21 +423,111 @@ int wrfgpu_rk_update_scalar(const int* scs, const int* sce, float* scalar_1, flo
                             const float* mu_new, const float* mu_base, const int* rk_step, const float* dt,
                             const int* spec_zone, const WrfDynConfig* config_flags, const int* tenddec,
                             WRFGPU_DIMS_ARGS) {
-  if (cfg_ok(config_flags) || !scs || !sce || !rk_step || !dt || (tenddec && *tenddec) || *scs < 1 || *sce < *scs)
+  if (cfg_ok(config_flags) || !scs || !sce || !rk_step || !dt || (tenddec && *tenddec) || *sce < *scs)
     return WRFGPU_E_ARG;
-  (void)sc_tend; (void)advh_t; (void)advz_t; (void)h_tendency; (void)z_tendency; (void)spec_zone;
+  (void)advh_t; (void)advz_t; (void)h_tendency; (void)z_tendency; (void)spec_zone;
+  // scalar_1, scalar_2 and sc_tend are (ims:ime,kms:kme,jms:jme,scs:sce)
   const size_t n3 = (size_t)(*ime - *ims + 1) * (size_t)(*kme - *kms + 1) * (size_t)(*jme - *jms + 1);
   for (int im = *scs; im <= *sce; ++im) {
+    const size_t off = (size_t)(im - *scs) * n3;
     FCall c;
     set_dims(c, DIMS);
-    c.cfg = *config_flags; c.routine = WRFGPU_R_RK_UPDATE_SCALAR; c.rk_step = *rk_step; c.dtrk = *dt;
-    float* s1 = scalar_1 + (size_t)(im - 1) * n3;
-    float* s2 = scalar_2 + (size_t)(im - 1) * n3;
-    RW(WRFGPU_SPECIES_BASE + 1, s1); RW(WRFGPU_SPECIES_BASE, s2); R(WRFGPU_ADVECT_TEND, advect_tend);
+    c.cfg = *config_flags; c.routine = 130; c.rk_step = *rk_step; c.dtrk = *dt;
+    RW(WRFGPU_SPECIES_BASE + 1, scalar_1 + off); RW(WRFGPU_SPECIES_BASE, scalar_2 + off);
+    R(WRFGPU_ADVECT_TEND, advect_tend);
+    if (sc_tend) R(WRFGPU_H_DIABATIC, sc_tend + off);
+    else c.zero_ids.push_back(WRFGPU_H_DIABATIC);
     R(WRFGPU_MSFTX, msftx); R(WRFGPU_MSFTY, msfty); R(WRFGPU_C1H, c1); R(WRFGPU_C2H, c2);
     R(WRFGPU_MU_1, mu_old); R(WRFGPU_MU_2, mu_new); R(WRFGPU_MUB, mu_base);
     int rc = wrfgpu::fortran_call(c);
     if (rc) return rc;
+  }
+  return WRFGPU_OK;
+}
+
+int wrfgpu_rk_update_scalar_pd(const int* scs, const int* sce, float* scalar, float* sc_tend, const float* c1,
+                               const float* c2, const float* mu_old, const float* mu_new, const float* mu_base,
+                               const int* rk_step, const float* dt, const int* spec_zone,
+                               const WrfDynConfig* config_flags, WRFGPU_DIMS_ARGS) {
+  if (cfg_ok(config_flags) || !scs || !sce || !rk_step || !dt || !scalar || !sc_tend || *sce < *scs)
+    return WRFGPU_E_ARG;
+  (void)spec_zone;
+  const size_t n3 = (size_t)(*ime - *ims + 1) * (size_t)(*kme - *kms + 1) * (size_t)(*jme - *jms + 1);
+  for (int im = *scs; im <= *sce; ++im) {
+    const size_t off = (size_t)(im - *scs) * n3;
+    FCall c;
+    set_dims(c, DIMS);
+    c.cfg = *config_flags; c.routine = 131; c.rk_step = *rk_step; c.dtrk = *dt;
+    RW(WRFGPU_SPECIES_BASE + 1, scalar + off); RW(WRFGPU_H_DIABATIC, sc_tend + off);
+    R(WRFGPU_C1H, c1); R(WRFGPU_C2H, c2);
+    R(WRFGPU_MU_1, mu_old); R(WRFGPU_MU_2, mu_new); R(WRFGPU_MUB, mu_base);
+    int rc = wrfgpu::fortran_call(c);
+    if (rc) return rc;
+  }
+  return WRFGPU_OK;
+}
+
+int wrfgpu_rk_scalar_tend(const int* scs, const int* sce, const WrfDynConfig* config_flags, const int* tenddec,
+                          const int* rk_step, const float* dt_step, const float* ru, const float* rv,
+                          const float* ww, const float* wwE, const float* wwI, const float* u_old,
+                          const float* v_old, const float* mut, const float* mub, const float* mu_old,
+                          const float* c1h, const float* c2h, const float* c1f, const float* c2f,
+                          const float* alt, const float* scalar_old, const float* scalar, float* scalar_tends,
+                          float* advect_tend, float* h_tendency, float* z_tendency, const float* RQVFTEN,
+                          const float* base, const int* moist_step, const float* fnm, const float* fnp,
+                          const float* msfux, const float* msfuy, const float* msfvx, const float* msfvx_inv,
+                          const float* msfvy, const float* msftx, const float* msfty, const float* rdx,
+                          const float* rdy, const float* rdn, const float* rdnw, const float* khdif,
+                          const float* kvdif, const float* xkmhd, const int* diff_6th_opt,
+                          const float* diff_6th_factor, const int* adv_opt, const float* phb, const float* ph,
+                          const int* mix2_off, const int* mix6_off, WRFGPU_DIMS_ARGS) {
+  if (cfg_ok(config_flags) || !scs || !sce || !rk_step || !dt_step || !rdx || !rdy || !adv_opt || !scalar ||
+      !scalar_old || !advect_tend || (tenddec && *tenddec) || *sce < *scs)
+    return WRFGPU_E_ARG;
+  // the schemes of this path: 0 (5th/3rd order) and 1 (positive definite)
+  if (*adv_opt != 0 && *adv_opt != 1) return WRFGPU_E_ARG;
+  // IEVA off (wwI unused), no cumulus moisture tendency (RQVFTEN, moist_step),
+  // no explicit diffusion (diff_opt = 0: khdif, kvdif, xkmhd, base, alt, rdn,
+  // mix2_off, c1f, c2f), tenddec off (h_tendency, z_tendency)
+  (void)ww; (void)wwI; (void)u_old; (void)v_old; (void)c1f; (void)c2f; (void)alt; (void)h_tendency;
+  (void)z_tendency; (void)RQVFTEN; (void)base; (void)moist_step; (void)rdn; (void)khdif; (void)kvdif;
+  (void)xkmhd; (void)ph; (void)mix2_off;
+  const int one = 1;
+  const size_t ni = (size_t)(*ime - *ims + 1), nk = (size_t)(*kme - *kms + 1);
+  const size_t n3 = ni * nk * (size_t)(*jme - *jms + 1);
+  for (int im = *scs; im <= *sce; ++im) {
+    const size_t off = (size_t)(im - *scs) * n3;
+    // zero_tend (module_big_step_utilities_em.F:4573): the tile, kts..kte
+    for (int j = *jts; j <= *jte; ++j)
+      for (int k = *kts; k <= *kte; ++k)
+        for (int i = *its; i <= *ite; ++i)
+          advect_tend[(size_t)(i - *ims) + ni * ((size_t)(k - *kms) + nk * (size_t)(j - *jms))] = 0.f;
+    int rc;
+    if (*rk_step == config_flags->rk_ord && *adv_opt == 1)
+      rc = wrfgpu_advect_scalar_pd(scalar + off, scalar_old + off, advect_tend, nullptr, nullptr, ru, rv, wwE, c1h,
+                                   c2h, mut, mub, mu_old, &one, config_flags, nullptr, msfux, msfuy, msfvx, msfvy,
+                                   msftx, msfty, fnm, fnp, rdx, rdy, rdnw, dt_step, DIMS);
+    else
+      rc = wrfgpu_advect_scalar(scalar + off, scalar + off, advect_tend, ru, rv, wwE, c1h, c2h, mut, &one,
+                                config_flags, msfux, msfuy, msfvx, msfvy, msftx, msfty, fnm, fnp, rdx, rdy, rdnw,
+                                DIMS);
+    if (rc) return rc;
+    const int d6 = diff_6th_opt ? *diff_6th_opt : 0;
+    const bool off6 = mix6_off && *mix6_off;
+    if (*rk_step == 1 && d6 != 0 && !off6) {  // module_em.F:1421-1435
+      if (!scalar_tends || !phb || !diff_6th_factor) return WRFGPU_E_ARG;
+      FCall c;
+      set_dims(c, DIMS);
+      c.cfg = *config_flags; c.cfg.diff_6th_opt = d6; c.cfg.diff_6th_factor = *diff_6th_factor;
+      c.routine = 132; c.rk_step = 1; c.dtrk = *dt_step; c.rdx = *rdx; c.rdy = *rdy;
+      R(WRFGPU_SPECIES_BASE, scalar + off); RW(WRFGPU_H_DIABATIC, scalar_tends + off);
+      R(WRFGPU_MUTS, mut); R(WRFGPU_C1H, c1h); R(WRFGPU_C2H, c2h); R(WRFGPU_PHB, phb);
+      R(WRFGPU_MSFUX, msfux); R(WRFGPU_MSFUY, msfuy); R(WRFGPU_MSFVX, msfvx); R(WRFGPU_MSFVY, msfvy);
+      R(WRFGPU_MSFTX, msftx); R(WRFGPU_MSFTY, msfty);
+      (void)msfvx_inv;
+      rc = wrfgpu::fortran_call(c);
+      if (rc) return rc;
+    }
   }
   return WRFGPU_OK;
 }

@@ -26,11 +26,12 @@ __device__ __forceinline__ float flux6(float fm3, float fm2, float fm1, float f0
 __device__ __forceinline__ float taper(float dzmax, float thresh) { return fmaxf(1.f - (dzmax / thresh), 0.f); }
 
 // One point of sixth_order_diffusion for variable kind V at (i, k, j), with
-// the column constants c1, c2 of level k: returns 0 + tendency_x +
-// tendency_y in the reference's order (the tendency starts at zero).
+// the column constants c1, c2 of level k: returns t0 + tendency_x +
+// tendency_y in the reference's order (t0: the tendency's value before the
+// call, zero where the tendency starts at zero).
 template <int V>
 __device__ float diff6_point(const Mem& m, const F3& f, const F2& mut, int i, int k, int j, float c1, float c2,
-                             float coef) {
+                             float coef, float t0 = 0.f) {
   const F3 phb = f3(m, WRFGPU_PHB);
   const int opt = m.cf.diff_6th_opt;
   const bool slope = m.cf.diff_6th_slopeopt >= 1;
@@ -126,7 +127,7 @@ __device__ float diff6_point(const Mem& m, const F3& f, const F2& mut, int i, in
     msf = f2(m, WRFGPU_MSFTY).ro(i, j);
   }
   const float ty = coef * msf * ((s1 * m1 * d1) - (s0 * m0 * d0));
-  float t = 0.f;
+  float t = t0;
   t = t + tx;
   t = t + ty;
   return t;
@@ -174,6 +175,24 @@ __global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L, int mode) {
   }
 }
 
+// The routine-level form of rk_scalar_tend's sixth-order diffusion
+// (module_em.F:1421-1435): species 0 of a scratch domain accumulated into
+// the caller's scalar_tends, carried in the H_DIABATIC buffer, with mut
+// (MUTS) and the caller's dt_step.
+__global__ void __launch_bounds__(BX* BY) k_sixth_diff_species_routine(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  const int ktf = min(m.kte, m.kde - 1);
+  if (i < m.its || j < m.jts || k < m.kts || k > ktf) return;
+  if (i > min(m.ide - 1, m.ite) || j > min(m.jde - 1, m.jte)) return;
+  const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H);
+  const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * stage_of(m, 1).dt_rk);
+  F3 out = f3(m, WRFGPU_H_DIABATIC);
+  out(i, k, j) = diff6_point<DV_M>(m, f3p(m, m.q[0]), f2(m, WRFGPU_MUTS), i, k, j, c1h(k), c2h(k), coef, out(i, k, j));
+}
+
 // Every stage: rk_addtend_dry for the stored tendencies.  With physics off
 // the saved tendencies, h_diabatic, ph_tendf and mu_tendf are zero: the
 // stage-1 "tendf + save * msf" steps add +0 to a tendency that is never -0
@@ -212,6 +231,10 @@ __global__ void __launch_bounds__(BX* BY) k_addtend_dry(Launch L) {
 
 void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s) {
   k_sixth_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L, mode);
+}
+
+void launch_sixth_diff_species_routine(const Launch& L, int nblocks, cudaStream_t s) {
+  k_sixth_diff_species_routine<<<nblocks, dim3(BX, BY), 0, s>>>(L);
 }
 
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s) {

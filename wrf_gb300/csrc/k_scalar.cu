@@ -268,6 +268,41 @@ __global__ void __launch_bounds__(BX* BY) k_update_scalar(Launch L, int species,
   s2(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
 }
 
+// ------------------------------------------------------------ routine-level scalar updates
+// The routine-level C entry points' form of rk_update_scalar
+// (module_em.F:1587-1799, pd = 0) and rk_update_scalar_pd (:1803-1916, pd =
+// 1) for species 0 of a scratch domain, with the caller's sc_tend carried in
+// the H_DIABATIC buffer: tendency = advect_tend msfty (rk_update_scalar only)
+// + sc_tend, in the reference's order; rk_update_scalar_pd zeroes sc_tend
+// after use and updates the old scalar with mu_old (MU_1) and mu_new (MU_2).
+// The loop limits are the periodic / symmetric ones (the spec_zone limits of
+// specified boundaries do not apply).
+__global__ void __launch_bounds__(BX* BY) k_update_scalar_routine(Launch L, int rk_step, int pd) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  F3 s1 = f3p(m, m.qo[0]), s2 = f3p(m, m.q[0]), at = f3(m, WRFGPU_ADVECT_TEND), sct = f3(m, WRFGPU_H_DIABATIC);
+  F2 msfty = f2(m, WRFGPU_MSFTY), mu_old = f2(m, WRFGPU_MU_1), mu_new = f2(m, WRFGPU_MU_2), mub = f2(m, WRFGPU_MUB);
+  F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  const float muold = mu_old(i, j) + mub(i, j), munew = mu_new(i, j) + mub(i, j);
+  if (pd) {
+    float tendency = 0.f;
+    tendency = tendency + sct(i, k, j);
+    sct(i, k, j) = 0.f;
+    s1(i, k, j) = ((c1(k) * muold + c2(k)) * s1(i, k, j) + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+    return;
+  }
+  float tendency = at(i, k, j) * msfty(i, j);
+  tendency = tendency + sct(i, k, j);
+  float q1;
+  if (rk_step == 1) { q1 = s2(i, k, j); s1(i, k, j) = q1; }
+  else q1 = s1(i, k, j);
+  s2(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+}
+
 // ------------------------------------------------------------ calc_p_rho_phi
 __global__ void __launch_bounds__(BX* BY) k_calc_p_rho_phi(Launch L) {
   BlockPos bp = block_pos(L);
@@ -455,6 +490,9 @@ void launch_advect_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
 void launch_advect_scalar_pd2(const Launch& L, int nb, StepArgs a, float* const* d_scratch, cudaStream_t s) {
   k_pd_scale<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags, d_scratch);
   k_pd_tend<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step, a.flags, d_scratch);
+}
+void launch_update_scalar_routine(const Launch& L, int nb, int rk_step, int pd, cudaStream_t s) {
+  k_update_scalar_routine<<<nb, dim3(BX, BY), 0, s>>>(L, rk_step, pd);
 }
 void launch_update_scalar(const Launch& L, int nb, StepArgs a, cudaStream_t s) {
   k_update_scalar<<<nb, dim3(BX, BY), 0, s>>>(L, a.species, a.rk_step);

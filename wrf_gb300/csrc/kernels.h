@@ -71,6 +71,7 @@ void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_
 // sixth-order diffusion of the dry state at stage 1, and rk_addtend_dry (k_diff.cu)
 // mode 0: u, v, w, theta into ru_tendf .. t_tendf; 1: the species into sc_tend
 void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s);
+void launch_sixth_diff_species_routine(const Launch& L, int nblocks, cudaStream_t s);
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s);
 
 // acoustic steps
@@ -92,6 +93,7 @@ void launch_update_scalar_pd(const Launch& L3, int nblocks, StepArgs a, cudaStre
 void launch_advect_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
 void launch_advect_scalar_pd2(const Launch& L3, int nblocks, StepArgs a, float* const* d_scratch, cudaStream_t s);
 void launch_update_scalar(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
+void launch_update_scalar_routine(const Launch& L3, int nblocks, int rk_step, int pd, cudaStream_t s);
 void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
 // host <-> device field copies through a contiguous staging buffer
 void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s);

@@ -15,20 +15,31 @@
 //   * the memory shape (ime-ims+1)(kme-kms+1)(jme-jms+1) may hold at most
 //     NOALLOC_MAX_POINTS points (8 Mi: a 256 x 256 x 120 patch); larger
 //     requests return WRFGPU_E_SIZE and launch nothing;
+//   * the options are those a device domain accepts (periodic x, periodic or
+//     symmetric y, 5th/3rd-order advection, ...): anything else returns
+//     WRFGPU_E_ARG before any device work;
 //   * nothing in the static arrays has to start at zero except the block
 //     prefix's first entry, which the one-time setup writes: the factor pass
 //     writes every factor the divergence pass reads, within the same call;
-//   * the first call on a device does the setup (symbol addresses through
-//     cudaGetSymbolAddress, one blocking copy) and should come before any
-//     stream capture; later calls only enqueue one small host-to-device copy
-//     of the member descriptor and two kernels on the caller's stream;
+//   * the first call on a device (and the first after that device's primary
+//     context was replaced, e.g. after cudaDeviceReset) does the setup —
+//     symbol addresses through cudaGetSymbolAddress and one blocking copy —
+//     so it should come before any stream capture; every call then enqueues
+//     two things on the caller's stream: a one-thread kernel that writes the
+//     member descriptor (passed by value as a kernel parameter, so no host
+//     memory is read after the call returns) and the two PD kernels;
+//   * the two PD kernels have no device-side failure (no bounded wait, no
+//     health check): the return code reports argument and launch errors, and
+//     there is no device status word to read back;
 //   * the static arrays are shared: calls that overlap in time (two host
 //     threads, or two streams without ordering between them) race on them.
 //     Serialize calls on one stream or synchronize between them.
 #include <cstring>
 #include <mutex>
+#include <cudaTypedefs.h>
 #include "common.cuh"
 #include "kernels.h"
+#include "fcall.h"
 #include "../../include/wrfgpu_fortran.h"
 
 namespace wrfgpu {
@@ -40,41 +51,65 @@ static __device__ __align__(256) float g_pd_factor[NOALLOC_MAX_POINTS];
 static __device__ __align__(16) Mem g_member;
 static __device__ int g_block_start[2];
 static __device__ float* g_factor_table[1];
-static __device__ unsigned g_err;
 
 constexpr int MAX_DEVICES = 64;
 struct DeviceSetup {
   bool done = false;
+  CUcontext ctx = nullptr;  // the context the addresses below belong to
   float* factor = nullptr;
   Mem* member = nullptr;
   int* block_start = nullptr;
   float** factor_table = nullptr;
-  unsigned* err = nullptr;
 };
 static DeviceSetup g_setup[MAX_DEVICES];
 static std::mutex g_setup_mu;
 
-// Once per device, with that device current: the addresses of the static
-// arrays, and the two table entries the kernels read (no allocation).
+// cuCtxGetCurrent from the driver (no link against libcuda): a device's
+// static arrays move when its primary context is destroyed and re-created.
+static PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+static int current_context(CUcontext* ctx) {
+  if (!g_ctx_current) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return WRFGPU_E_CUDA;
+    g_ctx_current = (PFN_cuCtxGetCurrent_v4000)fn;
+  }
+  *ctx = nullptr;
+  return g_ctx_current(ctx) == CUDA_SUCCESS && *ctx ? WRFGPU_OK : WRFGPU_E_CUDA;
+}
+
+// Once per device and context, with that device current: the addresses of
+// the static arrays, and the two table entries the kernels read (no
+// allocation).
 int setup_current_device(DeviceSetup** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return WRFGPU_E_CUDA;
+  // make the device's primary context current (initialised if need be)
+  if (cudaSetDevice(dev) != cudaSuccess) return WRFGPU_E_CUDA;
+  CUcontext ctx = nullptr;
+  if (current_context(&ctx)) return WRFGPU_E_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mu);
   DeviceSetup& s = g_setup[dev];
-  if (!s.done) {
+  if (!s.done || s.ctx != ctx) {
+    s.done = false;
     if (cudaGetSymbolAddress((void**)&s.factor, g_pd_factor) != cudaSuccess) return WRFGPU_E_CUDA;
     if (cudaGetSymbolAddress((void**)&s.member, g_member) != cudaSuccess) return WRFGPU_E_CUDA;
     if (cudaGetSymbolAddress((void**)&s.block_start, g_block_start) != cudaSuccess) return WRFGPU_E_CUDA;
     if (cudaGetSymbolAddress((void**)&s.factor_table, g_factor_table) != cudaSuccess) return WRFGPU_E_CUDA;
-    if (cudaGetSymbolAddress((void**)&s.err, g_err) != cudaSuccess) return WRFGPU_E_CUDA;
     if (cudaMemcpyToSymbol(g_factor_table, &s.factor, sizeof(float*)) != cudaSuccess) return WRFGPU_E_CUDA;
     const int zero = 0;
     if (cudaMemcpyToSymbol(g_block_start, &zero, sizeof(int)) != cudaSuccess) return WRFGPU_E_CUDA;
+    s.ctx = ctx;
     s.done = true;
   }
   *out = &s;
   return WRFGPU_OK;
 }
+
+// The member descriptor, written on the stream from a kernel parameter.
+__global__ void k_noalloc_set_member(Mem M, Mem* dst) { *dst = M; }
 
 }  // namespace
 }  // namespace wrfgpu
@@ -103,6 +138,14 @@ extern "C" int wrfgpu_advect_scalar_pd_noalloc(
   const long long ni = *ime - *ims + 1, nk = *kme - *kms + 1, nj = *jme - *jms + 1;
   if (ni * nk * nj > NOALLOC_MAX_POINTS) return WRFGPU_E_SIZE;
   if (!(*dt > 0.f) || !(*rdx > 0.f) || !(*rdy > 0.f)) return WRFGPU_E_ARG;
+  {  // the options a device domain accepts
+    WrfGpuDomainDesc d{};
+    d.ide = *ide; d.jde = *jde; d.kde = *kde; d.n_moist = 1; d.n_scalar = 0;
+    d.config = *config_flags;
+    d.scalars.dt = *dt; d.scalars.dx = 1.0 / *rdx; d.scalars.dy = 1.0 / *rdy;
+    d.scalars.rdx = *rdx; d.scalars.rdy = *rdy;
+    if (check_desc(d)) return WRFGPU_E_ARG;
+  }
 
   DeviceSetup* s = nullptr;
   int rc = setup_current_device(&s);
@@ -135,13 +178,11 @@ extern "C" int wrfgpu_advect_scalar_pd_noalloc(
   M.dt = *dt; M.dtrk_fix = *dt;
   M.rdx = *rdx; M.rdy = *rdy;
   M.cf = *config_flags;
-  M.cf.rk_ord = 3;
-  M.err = s->err;
+  M.err = nullptr;  // the PD kernels raise no device status
 
   cudaStream_t st = (cudaStream_t)stream;
-  // the descriptor goes through the driver's staging of pageable memory: the
-  // call returns after it is staged, so the stack copy may go out of scope
-  if (cudaMemcpyAsync(s->member, &M, sizeof(Mem), cudaMemcpyHostToDevice, st) != cudaSuccess) return WRFGPU_E_CUDA;
+  k_noalloc_set_member<<<1, 1, 0, st>>>(M, s->member);
+  if (cudaGetLastError() != cudaSuccess) return WRFGPU_E_CUDA;
   const int nb = blocks_for(M.ims, M.ime, M.jms, M.jme, (int)nk, 3);
   const Launch L{s->member, s->block_start, 1, 3};
   // rk_step 3 (the last stage, where the reference applies the PD scheme);

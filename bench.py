@@ -10,7 +10,7 @@ plain single-domain form (the drop-in).  Seeded synthetic initial state
 (Weisman-Klemp sounding); the device state (~6 GB) is far larger than L2.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c2|c1|c4] [--mixed]
+                  [--workload c2|c1|c3|c4|c5] [--mixed]
 
 N > 1 runs N independent replicas (one per rank, no collective on the data
 path) and reports the whole-job rate; the reference arm times the CPU
@@ -396,6 +396,114 @@ def ensemble_bench(steps, warmup, n_members=64, world=1, rank=0, pg=None):
     return res
 
 
+def _build_c5_member(spec):
+    """Worker (spawned process): one C5 member's initial state, FP32 arrays."""
+    sys.path.insert(0, ROOT)
+    from wrf_gb300 import cases
+    c = cases.c5_member(spec)
+    return [(fid, a.astype("float32")) for fid, a in c.field_items()]
+
+
+def c5_buckets(specs, nbuckets=3):
+    """Members sorted by cell count and cut into nbuckets groups of about
+    equal total cells (small, medium, large members)."""
+    cells = [sp[1] * sp[2] * (sp[3] - 1) for sp in specs]
+    order = sorted(range(len(specs)), key=lambda q: cells[q])
+    total = float(sum(cells))
+    out, cur, acc = [], [], 0.0
+    for q in order:
+        cur.append(q)
+        acc += cells[q]
+        if acc >= total * (len(out) + 1) / nbuckets and len(out) < nbuckets - 1:
+            out.append(cur)
+            cur = []
+    out.append(cur)
+    return out
+
+
+def run_c5_line(args, world, rank, local, pg):
+    """--workload c5: 256 uneven members (supercell and jet-channel states
+    mixed, qv + 7 PD scalars each, FP32 bulk with FP64 column steps).  The
+    whole ensemble's state (~1e9 cells, ~360 GB as laid out here) is larger
+    than one GB300's memory, so the members run in three size buckets of
+    about equal cells, each bucket one batched graph-captured ensemble;
+    value = all cells x steps / the buckets' summed time.  Per bucket: cell-
+    steps/s, and the FP64-oracle error of its smallest supercell and channel
+    members after 1, 10, 30, 60 and 120 steps."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from wrf_gb300 import cases
+    from wrf_gb300 import gpu as G
+    specs = cases.c5_members()
+    buckets = c5_buckets(specs)
+    # member states are built by spawned workers (started before any CUDA work here)
+    pool = cf.ProcessPoolExecutor(max_workers=max(1, min(16, (os.cpu_count() or 2) - 1)),
+                                  mp_context=mp.get_context("spawn"))
+    sampler = ClockSampler(local)
+    res = {"workload": "c5_mixed_256_members", "members": len(specs),
+           "cells": sum(sp[1] * sp[2] * (sp[3] - 1) for sp in specs), "buckets": []}
+    tot_cells_steps = 0.0
+    tot_s = 0.0
+    sampler.start()
+    for b, members in enumerate(buckets):
+        mspecs = [specs[q] for q in members]
+        descs = [cases.c5_member_desc(sp) for sp in mspecs]
+        t0 = time.perf_counter()
+        ens = G.Ensemble(descs, flags=G.FLAG_MIXED)
+        # states stream in as the workers finish them (host memory stays bounded)
+        for m, fields in enumerate(pool.map(_build_c5_member, mspecs, chunksize=1)):
+            for fid, arr in fields:
+                ens.set(m, fid, arr)
+        build_s = time.perf_counter() - t0
+        ens.autotune(1)
+        ens.step(args.warmup)
+        ens.sync()
+        bcells = sum(sp[1] * sp[2] * (sp[3] - 1) for sp in mspecs)
+        ms = ens.time_steps(args.steps)
+        dev_gb = ens.device_bytes() / 1e9
+        ens.close()
+        tot_cells_steps += bcells * args.steps
+        tot_s += ms / 1e3
+        res["buckets"].append({
+            "members": len(mspecs), "channel_members": sum(sp[0] == "channel" for sp in mspecs),
+            "cells": bcells, "cells_per_member": [min(sp[1] * sp[2] * (sp[3] - 1) for sp in mspecs),
+                                                  max(sp[1] * sp[2] * (sp[3] - 1) for sp in mspecs)],
+            "device_gb": round(dev_gb, 1), "state_build_s": round(build_s, 1),
+            "ms_per_step": ms / args.steps, "cell_steps_per_s": bcells * args.steps / (ms / 1e3)})
+    clocks = sampler.stop()
+    pool.shutdown()
+    value = tot_cells_steps / tot_s
+    # accuracy: the smallest supercell and channel member of every bucket
+    acc_steps = (1, 10, 30, 60, 120)
+    for b, members in enumerate(buckets):
+        picks = []
+        for kind in ("supercell", "channel"):
+            ks = [q for q in members if specs[q][0] == kind]
+            if ks:
+                picks.append(min(ks, key=lambda q: specs[q][1] * specs[q][2] * specs[q][3]))
+        try:
+            acc = accuracy_vs_fp64([cases.c5_member(specs[q]) for q in picks], acc_steps)
+        except Exception as ex:  # reported, never required
+            acc = {"error": repr(ex)}
+        res["buckets"][b]["accuracy"] = acc
+    hbm, hbm_kind = peaks()
+    alg = contract_bytes_per_cell_step(1, 8, mixed=True)
+    line = {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64-columns",
+        "data": "synthetic (seeded supercell and f-plane jet-channel members, uneven sizes)",
+        "config": {"workload": res["workload"], "form": "batched+mixed, three size buckets run one after another",
+                   "cells": res["cells"], "global_batch": len(specs), "seq_len": None, "parallelism": "single",
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": alg * value / 1e9, "peak": hbm, "peak_kind": hbm_kind,
+                     "unit": "GB/s", "frac": alg * value / 1e9 / hbm, "traffic": None,
+                     "note": "whole step at the contract bytes per cell-step (%d B) x cell-steps/s" % alg},
+        "c5": res, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_ensemble_line(args, world, rank, local, pg):
     """--workload c4: the uneven 64-member ensemble on its own line (value =
     batched mixed form), with the plain sequential form and the FP64 error."""
@@ -433,7 +541,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--no-c3-accuracy", action="store_true",
                     help="skip the C3 channel's FP64-oracle accuracy block")
     ap.add_argument("--no-ensemble", action="store_true",
@@ -457,6 +565,8 @@ def main():
             run_reference(args, world, rank)
         elif args.workload == "c4":
             run_ensemble_line(args, world, rank, local, pg)
+        elif args.workload == "c5":
+            run_c5_line(args, world, rank, local, pg)
         else:
             run_single(args, world, rank, local, pg)
     finally:

@@ -439,6 +439,26 @@ def _column_sounding(z, theta, rh, dz, p_surf=P1000):
     return p, pd, qv
 
 
+def _channel_profiles(ny, dx, ztop, f, u_max, z_jet, dz):
+    """The jet channel's height grid, row coordinates, the theta profile of
+    a row (thermal-wind balance) and the base state's dry sounding (the
+    middle row's) with the model-top pressure."""
+    Ly = ny * dx
+    z = np.arange(0.0, ztop + 4000.0 + dz, dz)
+    theta_ref = np.where(z <= 12000.0, 300.0 + 43.0 * (z / 12000.0) ** 1.25,
+                         343.0 * np.exp(G / (CP * 213.0) * (z - 12000.0)))
+    yj = (np.arange(1, ny + 1) - 0.5) * dx
+    Y = yj / 2.0 - Ly / (4.0 * math.pi) * np.sin(2.0 * math.pi * yj / Ly)
+    below = z <= z_jet
+
+    def row_theta(y_int):
+        return theta_ref - np.where(below, f * theta_ref / G * (u_max / z_jet) * y_int, 0.0)
+
+    p_mid, _, _ = _column_sounding(z, row_theta(Y[ny // 2]), np.zeros_like(z), dz)
+    p_top = float(_interp(ztop, z, p_mid))
+    return z, yj, Y, row_theta, p_mid, p_top
+
+
 def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10000.0, noise=1.0,
                   z_noise=2000.0, rh=0.8, z_moist=8000.0, n_scalar=0, name="channel", dz=20.0):
     """Zonally periodic channel on an f-plane with a balanced zonal jet
@@ -465,21 +485,9 @@ def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10
     nim, njm, nk = ide + 2 * h, jde + 2 * h, kde
     m = eta_metrics(kde)
     Ly = ny * dx
-    z = np.arange(0.0, ztop + 4000.0 + dz, dz)
-    theta_ref = np.where(z <= 12000.0, 300.0 + 43.0 * (z / 12000.0) ** 1.25,
-                         343.0 * np.exp(G / (CP * 213.0) * (z - 12000.0)))
-    yj = (np.arange(1, ny + 1) - 0.5) * dx
-    Y = yj / 2.0 - Ly / (4.0 * math.pi) * np.sin(2.0 * math.pi * yj / Ly)
-    below = z <= z_jet
+    z, yj, Y, row_theta, p_mid, p_top = _channel_profiles(ny, dx, ztop, f, u_max, z_jet, dz)
     rh_prof = np.where(z <= z_moist, rh, 0.0)
-
-    def row_theta(y_int):
-        return theta_ref - np.where(below, f * theta_ref / G * (u_max / z_jet) * y_int, 0.0)
-
-    # base state: the middle row's dry sounding
     jmid = ny // 2
-    p_mid, pd_mid, _ = _column_sounding(z, row_theta(Y[jmid]), np.zeros_like(z), dz)
-    p_top = float(_interp(ztop, z, p_mid))
     hc = hybrid_coefs(m, kde, p_top)
     c1h, c2h, c1f, c2f = hc["c1h"], hc["c2h"], hc["c1f"], hc["c2f"]
     c3h, c4h, c3f, c4f = hc["c3h"], hc["c4h"], hc["c3f"], hc["c4f"]
@@ -675,6 +683,53 @@ def ensemble_member(spec, dx=2000.0, dt=12.0, n_scalar=3):
 def ensemble_member_desc(spec, dx=2000.0, dt=12.0, n_scalar=3):
     nx, ny, kde = spec[0], spec[1], spec[2]
     return supercell_desc(nx, ny, kde, dx, dt, 20000.0, n_scalar=n_scalar)
+
+
+def channel_desc(nx, ny, kde, dx, dt, ztop, n_scalar=0, f=1.0e-4, u_max=30.0, z_jet=10000.0, dz=20.0):
+    """The domain description channel_state gives, without building the
+    fields (the base state's sounding alone fixes the model-top pressure)."""
+    cfg = abi.default_config(periodic_x=True, periodic_y=False, symmetric_y=True)
+    m = eta_metrics(kde)
+    p_top = _channel_profiles(ny, dx, ztop, f, u_max, z_jet, dz)[5]
+    return _make_desc(nx + 1, ny + 1, kde, n_scalar, cfg, dt, dx, m, p_top)
+
+
+def c5_members(seed=5, n=256, nmin=96, nmax=384, kmin=41, kmax=96, n_scalar=7):
+    """The large mixed ensemble: n members, nx, ny ~ U[nmin, nmax], levels
+    ~ U[kmin, kmax], each a supercell (dx = 2 km, dt = 12 s, top 20 km, one
+    bubble of seeded position and amplitude in [1, 4] K) or an f-plane jet
+    channel (dx = 4 km, dt = 20 s, top 25 km) with even odds, qv plus
+    n_scalar positive-definite scalars."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs = []
+    for _ in range(n):
+        kind = "channel" if rng.uniform() < 0.5 else "supercell"
+        nx = int(rng.integers(nmin, nmax + 1))
+        ny = int(rng.integers(nmin, nmax + 1))
+        kde = int(rng.integers(kmin, kmax + 1))
+        amp = float(rng.uniform(1.0, 4.0))
+        fx, fy = float(rng.uniform(0.25, 0.75)), float(rng.uniform(0.25, 0.75))
+        specs.append((kind, nx, ny, kde, amp, fx, fy, int(rng.integers(0, 2 ** 31)), n_scalar))
+    return specs
+
+
+def c5_member(spec):
+    kind, nx, ny, kde, amp, fx, fy, mseed, n_scalar = spec
+    rng = np.random.Generator(np.random.PCG64(mseed))
+    if kind == "channel":
+        return channel_state(nx, ny, kde, 4000.0, 20.0, 25000.0, rng, n_scalar=n_scalar,
+                             name="channel_%dx%dx%d" % (nx, ny, kde))
+    dx = 2000.0
+    return supercell_state(nx, ny, kde, dx, 12.0, 20000.0,
+                           [(fx * nx * dx, fy * ny * dx, 1500.0, 10000.0, 10000.0, 1500.0, amp)], rng,
+                           n_scalar=n_scalar, name="supercell_%dx%dx%d" % (nx, ny, kde))
+
+
+def c5_member_desc(spec):
+    kind, nx, ny, kde = spec[0], spec[1], spec[2], spec[3]
+    if kind == "channel":
+        return channel_desc(nx, ny, kde, 4000.0, 20.0, 25000.0, n_scalar=spec[8])
+    return supercell_desc(nx, ny, kde, 2000.0, 12.0, 20000.0, n_scalar=spec[8])
 
 
 def small_case(nx=12, ny=10, kde=12, n_scalar=1, seed=7, dx=2000.0, dt=12.0):

@@ -114,6 +114,9 @@ enum WrfGpuFieldId {
   WRFGPU_ZNW = WRFGPU_F1D_BASE, WRFGPU_ZNU, WRFGPU_DNW, WRFGPU_RDNW, WRFGPU_DN, WRFGPU_RDN,
   WRFGPU_FNM, WRFGPU_FNP, WRFGPU_C1H, WRFGPU_C2H, WRFGPU_C1F, WRFGPU_C2F,
   WRFGPU_C3H, WRFGPU_C4H, WRFGPU_C3F, WRFGPU_C4F,
+  /* base-state profiles of the initial column (1,1) (module_initialize_ideal.F:1578-1586),
+   * read by the Rayleigh damping toward them (damp_opt = 2) */
+  WRFGPU_U_BASE, WRFGPU_V_BASE, WRFGPU_T_BASE, WRFGPU_Z_BASE,
   WRFGPU_F1D_END,
   /* species: WRFGPU_SPECIES_BASE + 2*s is species s (moist first, then
    * passive scalars), + 1 its "old" (_1) copy */

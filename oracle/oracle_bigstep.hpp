@@ -752,6 +752,98 @@ void sixth_order_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R dt,
       }
 }
 
+// module_big_step_utilities_em.F:5836-6110 rk_rayleigh_damp (damp_opt = 2):
+// relaxation of u, v, w and theta toward the base-state profiles (u_base,
+// v_base, t_base interpolated linearly in height z_base to the column's
+// current level heights; w toward 0) in the top zdamp metres, with weight
+// sin^2(pi/2 (1 - (ztop - z)/zdamp)) dampcoef times the column mass, added to
+// the forward tendencies ru_tendf .. t_tendf.  The level searches stop at the
+// first level (the reference's loops assume zdamp lies inside the model
+// column).  sin in the working precision, correctly rounded (FP64 sine
+// rounded once for the FP32 restatement).
+template <typename R>
+void rk_rayleigh_damp(R* ru_tendf_p, R* rv_tendf_p, R* rw_tendf_p, R* t_tendf_p, R* u_p, R* v_p, R* w_p, R* t_p,
+                      R* c1h_p, R* c2h_p, R* c1f_p, R* c2f_p, R* mut_p, R* muu_p, R* muv_p, R* ph_p, R* phb_p,
+                      R* u_base_p, R* v_base_p, R* t_base_p, R* z_base_p, R dampcoef, R zdamp, const Dims& d) {
+  A3<R> ru_tendf(ru_tendf_p, d), rv_tendf(rv_tendf_p, d), rw_tendf(rw_tendf_p, d), t_tendf(t_tendf_p, d);
+  A3<R> u(u_p, d), v(v_p, d), w(w_p, d), t(t_p, d), ph(ph_p, d), phb(phb_p, d);
+  A2<R> mut(mut_p, d), muu(muu_p, d), muv(muv_p, d);
+  A1<R> c1h(c1h_p, d), c2h(c2h_p, d), c1f(c1f_p, d), c2f(c2f_p, d), u_base(u_base_p, d), v_base(v_base_p, d),
+      t_base(t_base_p, d), z_base(z_base_p, d);
+  const R g = K<R>::g;
+  const R pii = R(2.0) * std::asin(R(1.0));
+  const int ktf = std::min(d.kte, d.kde - 1);
+  std::vector<R> z00(d.kme - d.kms + 2), q00(d.kme - d.kms + 2);
+  auto Z = [&](int k) -> R& { return z00[k - d.kms]; };
+  auto Q = [&](int k) -> R& { return q00[k - d.kms]; };
+  auto weight = [&](R ztop, R z) {
+    R dcoef = R(1.0) - std::min(R(1.0), (ztop - z) / zdamp);
+    const R s = (R)std::sin((double)(R(0.5) * pii * dcoef));
+    return s * s;
+  };
+  // level heights of the top layer of a column (the search of :5903-5913),
+  // the profile interpolated to them (:5915-5930); returns the first level
+  auto top_layer = [&](R ztop, auto height, const A1<R>& prof) {
+    int k1 = ktf;
+    R z = ztop;
+    while (z >= ztop - zdamp && k1 >= d.kts) {
+      z = height(k1);
+      Z(k1) = z;
+      k1 = k1 - 1;
+    }
+    k1 = k1 + 2;
+    for (int k = k1; k <= ktf; ++k) {
+      int k2 = ktf;
+      while (z_base(k2) > Z(k) && k2 > d.kts) k2 = k2 - 1;
+      if (k2 + 1 > ktf)
+        Q(k) = prof(k2) + (prof(k2) - prof(k2 - 1)) * (Z(k) - z_base(k2)) / (z_base(k2) - z_base(k2 - 1));
+      else
+        Q(k) = prof(k2) + (prof(k2 + 1) - prof(k2)) * (Z(k) - z_base(k2)) / (z_base(k2 + 1) - z_base(k2));
+    }
+    return k1;
+  };
+  // u (:5897-5945)
+  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+    for (int i = d.its; i <= std::min(d.ite, d.ide); ++i) {
+      const R ztop = R(0.5) * (phb(i, d.kde, j) + phb(i - 1, d.kde, j) + ph(i, d.kde, j) + ph(i - 1, d.kde, j)) / g;
+      const int k1 = top_layer(ztop, [&](int k) {
+        return R(0.25) * (phb(i, k, j) + phb(i, k + 1, j) + phb(i - 1, k, j) + phb(i - 1, k + 1, j) + ph(i, k, j) +
+                          ph(i, k + 1, j) + ph(i - 1, k, j) + ph(i - 1, k + 1, j)) / g;
+      }, u_base);
+      for (int k = k1; k <= ktf; ++k)
+        ru_tendf(i, k, j) = ru_tendf(i, k, j) - (c1h(k) * muu(i, j) + c2h(k)) * (weight(ztop, Z(k)) * dampcoef) *
+                                                    (u(i, k, j) - Q(k));
+    }
+  // v (:5947-5995)
+  for (int j = d.jts; j <= std::min(d.jte, d.jde); ++j)
+    for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i) {
+      const R ztop = R(0.5) * (phb(i, d.kde, j) + phb(i, d.kde, j - 1) + ph(i, d.kde, j) + ph(i, d.kde, j - 1)) / g;
+      const int k1 = top_layer(ztop, [&](int k) {
+        return R(0.25) * (phb(i, k, j) + phb(i, k + 1, j) + phb(i, k, j - 1) + phb(i, k + 1, j - 1) + ph(i, k, j) +
+                          ph(i, k + 1, j) + ph(i, k, j - 1) + ph(i, k + 1, j - 1)) / g;
+      }, v_base);
+      for (int k = k1; k <= ktf; ++k)
+        rv_tendf(i, k, j) = rv_tendf(i, k, j) - (c1h(k) * muv(i, j) + c2h(k)) * (weight(ztop, Z(k)) * dampcoef) *
+                                                    (v(i, k, j) - Q(k));
+    }
+  // w (:5997-6013) and theta (:6015-6062)
+  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+    for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i) {
+      const R ztop = (phb(i, d.kde, j) + ph(i, d.kde, j)) / g;
+      for (int k = d.kts; k <= std::min(d.kte, d.kde); ++k) {
+        const R z = (phb(i, k, j) + ph(i, k, j)) / g;
+        if (z >= ztop - zdamp)
+          rw_tendf(i, k, j) = rw_tendf(i, k, j) - (c1f(k) * mut(i, j) + c2f(k)) * (weight(ztop, z) * dampcoef) * w(i, k, j);
+      }
+      const int k1 = top_layer(
+          ztop, [&](int k) { return R(0.5) * (phb(i, k, j) + phb(i, k + 1, j) + ph(i, k, j) + ph(i, k + 1, j)) / g; },
+          t_base);
+      for (int k = k1; k <= ktf; ++k)
+        t_tendf(i, k, j) = t_tendf(i, k, j) - (c1h(k) * mut(i, j) + c2h(k)) * (weight(ztop, Z(k)) * dampcoef) *
+                                                  (t(i, k, j) - Q(k));
+    }
+}
+
 // module_em.F:959-1092 rk_addtend_dry for the forward-in-time tendencies this
 // path forms (ru_tendf .. t_tendf: the sixth-order diffusion).  With physics
 // off the saved tendencies (u_save .. t_save, ph_save), h_diabatic, ph_tendf

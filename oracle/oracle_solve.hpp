@@ -121,7 +121,7 @@ struct Domain {
     f2.assign(WRFGPU_N2D, std::vector<R>(n2, R(0)));
     f1.assign(WRFGPU_N1D, std::vector<R>(n1, R(0)));
     qs.assign(2 * (n_moist + n_scalar), std::vector<R>(n3, R(0)));
-    tendf.assign(cf.diff_6th_opt != 0 ? 4 : 0, std::vector<R>(n3, R(0)));
+    tendf.assign(cf.diff_6th_opt != 0 || cf.damp_opt == 2 ? 4 : 0, std::vector<R>(n3, R(0)));
     sctend.assign(cf.diff_6th_opt != 0 ? n_moist + n_scalar : 0, std::vector<R>(n3, R(0)));
   }
   // species s's sc_tend, or null where it is not diffused
@@ -216,8 +216,8 @@ struct Domain {
       // forward-in-time tendencies formed at stage 1 (the sixth-order
       // diffusion; zero physics tendencies otherwise).
       std::vector<R> tmv(64, R(0)), tmh(64, R(0));
-      const bool diff6 = cf.diff_6th_opt != 0;
-      if (diff6 && rk_step == 1)
+      const bool diff6 = cf.diff_6th_opt != 0, damp2 = cf.damp_opt == 2;
+      if ((diff6 || damp2) && rk_step == 1)
         for (auto& t : tendf) std::fill(t.begin(), t.end(), R(0));
       tiles([&](const Dims& td) {
         zero_tend(p3(WRFGPU_RU_TEND), td); zero_tend(p3(WRFGPU_RV_TEND), td); zero_tend(p3(WRFGPU_RW_TEND), td);
@@ -285,9 +285,15 @@ struct Domain {
                                   p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
           }
         }
+        if (damp2 && rk_step == 1)  // module_em.F:933-944
+          rk_rayleigh_damp(tendf[0].data(), tendf[1].data(), tendf[2].data(), tendf[3].data(), p3(WRFGPU_U_2),
+                           p3(WRFGPU_V_2), p3(WRFGPU_W_2), p3(WRFGPU_T_2), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                           p1(WRFGPU_C1F), p1(WRFGPU_C2F), p2(WRFGPU_MUT), p2(WRFGPU_MUU), p2(WRFGPU_MUV),
+                           p3(WRFGPU_PH_2), p3(WRFGPU_PHB), p1(WRFGPU_U_BASE), p1(WRFGPU_V_BASE), p1(WRFGPU_T_BASE),
+                           p1(WRFGPU_Z_BASE), (R)cf.dampcoef, (R)cf.zdamp, td);
       });
       for (int t = 0; t < 64; ++t) { mvc = std::max(mvc, tmv[t]); mhc = std::max(mhc, tmh[t]); }
-      if (diff6)
+      if (diff6 || damp2)
         tiles([&](const Dims& td) {
           rk_addtend_dry(p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), p3(WRFGPU_T_TEND),
                          tendf[0].data(), tendf[1].data(), tendf[2].data(), tendf[3].data(), p1(WRFGPU_C1H),

@@ -773,3 +773,54 @@ def test_bounded_wait_times_out_without_fault(gpulib):
     d.step(1)
     rc, b, vc, hc = d.status(0)
     assert rc == 0 and b == 0
+
+
+def rayleigh2_case(diff6=False):
+    """damp_opt = 2 over the top 5 km of the small case's 20 km column,
+    dampcoef 0.01 s-1; with diff6 the sixth-order diffusion is on too, so
+    the damping accumulates onto the stored diffusion tendencies."""
+    case = diffusion_case(2, 0) if diff6 else cases.small_case(nx=16, ny=12, kde=20, n_scalar=1, seed=19)
+    c = case.desc.config
+    c.damp_opt = 2
+    c.dampcoef = 0.01
+    c.zdamp = 5000.0
+    return case
+
+
+@pytest.mark.parametrize("diff6", [False, True])
+def test_full_step_bitwise_damp_opt_2(gpulib, diff6):
+    """rk_rayleigh_damp (module_big_step_utilities_em.F:5836-6110) at stage 1
+    into ru_tendf .. t_tendf, added at every stage by rk_addtend_dry: the
+    state after two steps bit for bit the oracle's (alone and on top of the
+    sixth-order diffusion), and the term is active (the oracle's state
+    differs from its damp_opt = 0 run)."""
+    case = rayleigh2_case(diff6)
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(2)
+    ge.step(2)
+    ge.sync()
+    bad = _bitwise_diffs(case, ge, od, old_too=False)
+    assert not bad, "\n".join(bad)
+    case.desc.config.damp_opt = 0
+    o0 = OracleDomain(case, "f32")
+    o0.step(2)
+    for nm in ("u_2", "w_2", "t_2"):
+        fid = abi.FIELD_ID[nm]
+        assert max_abs(interior(case, fid, o0.get(fid), halo=3), interior(case, fid, od.get(fid), halo=3)) > 0, nm
+
+
+def test_batched_damp_opt_2_with_other_options(gpulib):
+    """An ensemble of a damp_opt = 2 member, a member with the sixth-order
+    diffusion and a plain one: each member gets the bits it gets alone."""
+    members = [rayleigh2_case(False), diffusion_case(1, 0), cases.small_case(nx=20, ny=12, kde=16, n_scalar=2, seed=6)]
+    ens = G.Ensemble.from_cases(members)
+    ens.step(2)
+    ens.sync()
+    for m, cs in enumerate(members):
+        d = G.Domain(cs)
+        d.step(2)
+        d.sync()
+        nsp = cs.desc.n_moist + cs.desc.n_scalar
+        for fid in [abi.FIELD_ID[nm] for nm in STATE_FIELDS] + [abi.species_id(s) for s in range(nsp)]:
+            assert np.array_equal(ens.get(m, fid), d.get(0, fid)), (m, id_name(fid))

@@ -20,7 +20,7 @@ import pytest
 
 from wrf_gb300 import abi, cases
 
-from _harness import OracleDomain, tophat_feeder, serr
+from _harness import OracleDomain, interior, tophat_feeder, serr
 
 H = abi.HALO
 
@@ -343,3 +343,28 @@ def test_sixth_order_diffusion_damps_2dx_wave_of_qv(adv):
         amp[mix_off] = abs(float(np.mean(qv * sign)))
     assert amp[1] > 0
     assert abs(amp[0] / amp[1] - (1.0 - 1.5 * 0.12)) < 0.02
+
+
+def test_rayleigh_damping_relaxes_top_layer():
+    """damp_opt = 2 (module_big_step_utilities_em.F:5836-6110): the Rayleigh
+    relaxation toward the base state lowers the rms w of the top 5 km (where
+    the initial state's lid adjustment lives) and leaves the lower levels as
+    they were after 3 steps; dampcoef 0.01 s-1 keeps the explicit term
+    stable at dt = 12 s."""
+    from wrf_gb300 import abi
+
+    def run(damp):
+        c = cases.small_case(nx=16, ny=12, kde=20, n_scalar=1, seed=19)
+        if damp:
+            c.desc.config.damp_opt = 2
+            c.desc.config.dampcoef = 0.01
+            c.desc.config.zdamp = 5000.0
+        od = OracleDomain(c, "f32")
+        od.step(3)
+        w = interior(c, abi.FIELD_ID["w_2"], od.get(abi.FIELD_ID["w_2"]))
+        return float(np.sqrt(np.mean(w[:, -6:, :] ** 2))), float(np.sqrt(np.mean(w[:, :8, :] ** 2)))
+
+    top0, low0 = run(False)
+    top1, low1 = run(True)
+    assert top1 < 0.97 * top0, (top0, top1)
+    assert abs(low1 - low0) <= 1e-3 * low0, (low0, low1)

@@ -68,7 +68,7 @@ F2D = ["mu_1", "mu_2", "mub", "mut", "muu", "muv", "muts", "muus", "muvs", "mudf
        "mu_save", "muave", "mu_tend", "msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy",
        "msftx", "msfty", "ht", "f", "e", "sina", "cosa"]
 F1D = ["znw", "znu", "dnw", "rdnw", "dn", "rdn", "fnm", "fnp", "c1h", "c2h", "c1f", "c2f",
-       "c3h", "c4h", "c3f", "c4f"]
+       "c3h", "c4h", "c3f", "c4f", "u_base", "v_base", "t_base", "z_base"]
 F2D_BASE = 100
 F1D_BASE = 200
 SPECIES_BASE = 300

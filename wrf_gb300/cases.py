@@ -398,6 +398,7 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     for nm in ("c1h", "c2h", "c1f", "c2f", "c3h", "c4h", "c3f", "c4f"):
         f[nm] = hc[nm][1:].copy()
 
+    _base_profiles(f, t1, ph1, phb, kde)
     species = []
     qv_mem = mem3(qv3, nkm)
     species.append((qv_mem, qv_mem.copy()))
@@ -577,6 +578,7 @@ def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10
         fl[nm] = m[nm][1:].copy()
     for nm in ("c1h", "c2h", "c1f", "c2f", "c3h", "c4h", "c3f", "c4f"):
         fl[nm] = hc[nm][1:].copy()
+    _base_profiles(fl, t1, ph1, phb, kde)
     qv_mem = mem3(qv3, nkm)
     species = [(qv_mem, qv_mem.copy())]
     for _ in range(n_scalar):
@@ -586,6 +588,21 @@ def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10
     desc = _make_desc(ide, jde, kde, n_scalar, cfg, dt, dx, m, p_top)
     meta = dict(dx=dx, dt=dt, ztop=ztop, f=f, u_max=u_max, z_jet=z_jet, n_scalar=n_scalar)
     return Case(name, desc, fl, species, meta)
+
+
+def _base_profiles(f, t1, ph1, phb, kde):
+    """u_base, v_base, t_base, z_base of column (1,1) of the initial state
+    (module_initialize_ideal.F:1578-1586): theta before the moist conversion,
+    the winds, and the mass-level heights from phb + ph_1 (1-D, kms:kme)."""
+    h = abi.HALO
+    nkm = kde - 1
+    for nm, col in (("u_base", f["u_1"][h, :nkm, h]), ("v_base", f["v_1"][h, :nkm, h]), ("t_base", t1[0, :, 0])):
+        a = np.zeros(kde)
+        a[:nkm] = col
+        f[nm] = a
+    z = np.zeros(kde)
+    z[:nkm] = 0.5 * (phb[1:kde] + phb[2:kde + 1] + ph1[0, :nkm, 0] + ph1[0, 1:kde, 0]) / G
+    f["z_base"] = z
 
 
 def _make_desc(ide, jde, kde, n_scalar, cfg, dt, dx, m, p_top):

@@ -419,14 +419,19 @@ __host__ __device__ inline int tiles_y(const Mem& m, bool stag = false) {
   return (jtf - m.jts + TY) / TY;
 }
 
-// per_species: one block per (tile, species) instead of one per tile.
-__device__ __forceinline__ TilePos tile_pos(const TileLaunch& L, bool per_species, bool stag = false) {
+// Blocks per tile: one, one per species, or one per pair of species
+// (species 2 sub and 2 sub + 1).
+enum { TILE_ONE = 0, TILE_PER_SPECIES = 1, TILE_PER_PAIR = 2 };
+__host__ __device__ inline int blocks_per_tile(int nsp, int per_mode) {
+  return per_mode == TILE_PER_SPECIES ? nsp : per_mode == TILE_PER_PAIR ? (nsp + 1) / 2 : 1;
+}
+__device__ __forceinline__ TilePos tile_pos(const TileLaunch& L, int per_mode, bool stag = false) {
   TilePos t;
   const int b = blockIdx.x;
   t.m = find_member(L.block_start, L.nmem, b);
   const Mem& m = L.mem[t.m];
   const int lb = b - __ldg(L.block_start + t.m);
-  const int per = per_species ? m.nsp : 1;
+  const int per = blocks_per_tile(m.nsp, per_mode);
   const int tile = lb / per;
   t.sub = lb - tile * per;
   const int ntx = tiles_x(m, stag);

@@ -62,8 +62,10 @@ int check_desc(const WrfGpuDomainDesc& d) {
   if (c.rk_ord != 3 || c.h_mom_adv_order != 5 || c.h_sca_adv_order != 5 || c.v_mom_adv_order != 3 ||
       c.v_sca_adv_order != 3)
     return WRFGPU_E_ARG;
-  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || (c.damp_opt != 0 && c.damp_opt != 3) || (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
+  if (!c.non_hydrostatic || c.zadvect_implicit != 0 || (c.damp_opt != 0 && c.damp_opt != 2 && c.damp_opt != 3) ||
+      (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
     return WRFGPU_E_ARG;
+  if (c.damp_opt == 2 && !(c.zdamp > 0.f)) return WRFGPU_E_ARG;
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) return WRFGPU_E_ARG;
   if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
   if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;
@@ -114,13 +116,15 @@ struct Ensemble {
   std::vector<WrfGpuDomainDesc> descs;
   std::vector<Mem> hm;                 // host copies of the member descriptors
   Mem* d_mems = nullptr;
-  int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_sc = nullptr, *d_bs_st = nullptr, *d_bs_tm = nullptr;
-  int nb2 = 0, nb3 = 0, nb_sc = 0, nb_st = 0, nb_tm = 0;
+  int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_st = nullptr, *d_bs_tm = nullptr;
+  int* d_bs_pr = nullptr;  // mass tiles x pairs of species (the scalar transport)
+  int nb2 = 0, nb3 = 0, nb_st = 0, nb_tm = 0, nb_pr = 0;
   bool capturing = false;
   int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0, nlev_max = 0;
   bool damp3 = false;  // some member uses damp_opt = 3
   bool diff6 = false;  // some member uses diff_6th_opt != 0
+  bool damp2 = false;  // some member uses damp_opt = 2 (Rayleigh damping toward the base state)
   std::vector<size_t> n3, n2, n1;      // element counts per member (padded rows)
   std::vector<size_t> ni_, nk_, nj_, pitch_;  // Fortran extents and the padded row pitch
   CUtensorMap* d_tmaps = nullptr;      // [nmem][NMAPSLOT][2]
@@ -157,7 +161,7 @@ struct Ensemble {
 
   Launch L2() const { return Launch{d_mems, d_bs2, nmem, 2}; }
   Launch L3() const { return Launch{d_mems, d_bs3, nmem, 3}; }
-  TileLaunch LS() const { return TileLaunch{d_mems, d_bs_sc, nmem}; }
+  TileLaunch LP() const { return TileLaunch{d_mems, d_bs_pr, nmem}; }  // tiles x species pairs
   TileLaunch LST() const { return TileLaunch{d_mems, d_bs_st, nmem}; }  // staggered-extent tiles
   TileLaunch LTM() const { return TileLaunch{d_mems, d_bs_tm, nmem}; }  // mass-extent tiles
 
@@ -201,7 +205,7 @@ struct Ensemble {
     if (d_mems) cudaFree(d_mems);
     if (d_bs2) cudaFree(d_bs2);
     if (d_bs3) cudaFree(d_bs3);
-    if (d_bs_sc) cudaFree(d_bs_sc);
+    if (d_bs_pr) cudaFree(d_bs_pr);
     if (d_bs_st) cudaFree(d_bs_st);
     if (d_bs_tm) cudaFree(d_bs_tm);
     if (d_tmaps) cudaFree(d_tmaps);
@@ -247,7 +251,8 @@ struct Ensemble {
       b += al256(n3[m] * 4);  // limiter scratch
       b += 6 * al256(n3[m] * 4);  // face Courant numbers and low-order factors of the PD transport
       if (fp64) b += 3 * al256(n3[m] * 8);
-      if (d.config.diff_6th_opt != 0) b += (4 + nsp) * al256(n3[m] * 4);  // ru_tendf .. t_tendf, sc_tend
+      if (d.config.diff_6th_opt != 0 || d.config.damp_opt == 2) b += 4 * al256(n3[m] * 4);  // ru_tendf .. t_tendf
+      if (d.config.diff_6th_opt != 0) b += nsp * al256(n3[m] * 4);                            // sc_tend
       off[m] = total;
       total += b;
     }
@@ -259,7 +264,7 @@ struct Ensemble {
     CK(cudaMalloc(&d_cfl, sizeof(float) * 2 * n));
     CK(cudaMemsetAsync(d_cfl, 0, sizeof(float) * 2 * n, stream));
     std::vector<float*> scr(n);
-    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bss(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0);
+    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0), bpr(n + 1, 0);
     for (int m = 0; m < n; ++m) {
       const WrfGpuDomainDesc& d = ds[m];
       Mem& M = hm[m];
@@ -284,9 +289,9 @@ struct Ensemble {
       scr[m] = (float*)p; p += al256(n3[m] * 4);
       for (int q = 0; q < 6; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
       if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
-      if (d.config.diff_6th_opt != 0)  // zero outside the diffusion's loop limits (the pool is cleared)
-      {
+      if (d.config.diff_6th_opt != 0 || d.config.damp_opt == 2)  // zero outside the loop limits (the pool is cleared)
         for (int q = 0; q < 4; ++q) { M.tendf[q] = (float*)p; p += al256(n3[m] * 4); }
+      if (d.config.diff_6th_opt != 0) {
         M.sctend = (float*)p; M.sct_n = (long long)(al256(n3[m] * 4) / 4); p += M.nsp * al256(n3[m] * 4);
       }
       M.ns_total = num_sound_steps(d);
@@ -303,13 +308,14 @@ struct Ensemble {
       nlev_max = std::max(nlev_max, M.kme - M.kms + 1);
       damp3 = damp3 || M.cf.damp_opt == 3;
       diff6 = diff6 || M.cf.diff_6th_opt != 0;
+      damp2 = damp2 || M.cf.damp_opt == 2;
       bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
-      bss[m + 1] = bss[m] + tiles_x(M) * tiles_y(M) * M.nsp;
+      bpr[m + 1] = bpr[m] + tiles_x(M) * tiles_y(M) * blocks_per_tile(M.nsp, TILE_PER_PAIR);
       bst[m + 1] = bst[m] + tiles_x(M, true) * tiles_y(M, true);
       btm[m + 1] = btm[m] + tiles_x(M) * tiles_y(M);
     }
-    nb2 = bs2[n]; nb3 = bs3[n]; nb_sc = bss[n]; nb_st = bst[n]; nb_tm = btm[n];
+    nb2 = bs2[n]; nb3 = bs3[n]; nb_st = bst[n]; nb_tm = btm[n]; nb_pr = bpr[n];
     {  // tensor maps of every 3-D buffer: halo and tile boxes
       int rc = get_tensor_map_encoder();
       if (rc) return rc;
@@ -341,8 +347,8 @@ struct Ensemble {
     CK(cudaMalloc(&d_bs3, sizeof(int) * (n + 1)));
     CK(cudaMemcpyAsync(d_bs2, bs2.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_bs3, bs3.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
-    CK(cudaMalloc(&d_bs_sc, sizeof(int) * (n + 1)));
-    CK(cudaMemcpyAsync(d_bs_sc, bss.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_bs_pr, sizeof(int) * (n + 1)));
+    CK(cudaMemcpyAsync(d_bs_pr, bpr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_bs_st, sizeof(int) * (n + 1)));
     CK(cudaMemcpyAsync(d_bs_st, bst.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_bs_tm, sizeof(int) * (n + 1)));
@@ -430,9 +436,10 @@ struct Ensemble {
       mark(PH_TEND_W); launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
-      if (diff6) {  // module_em.F:879-932 (stage 1), then rk_addtend_dry (solve_em.F:967)
+      if (diff6 || damp2) {  // module_em.F:879-944 (stage 1), then rk_addtend_dry (solve_em.F:967)
         mark(PH_DIFF);
-        if (rk_step == 1) launch_sixth_diff(l3, nb3, 0, stream);
+        if (rk_step == 1 && diff6) launch_sixth_diff(l3, nb3, 0, stream);
+        if (rk_step == 1 && damp2) launch_rayleigh_damp(l2, nb2, stream);
         launch_addtend_dry(l3, nb3, stream);
       }
       if (cfl_check) { mark(PH_CFL); launch_cfl_check_col(LTM(), nb_tm, stream, tune[TU_CFL]); }
@@ -474,11 +481,11 @@ struct Ensemble {
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
       if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_sixth_diff(l3, nb3, 1, stream); }  // module_em.F:1421-1435
-      mark(PH_ADVS); launch_scalar_adv_update(LS(), nb_sc, rk_step, stream, tune[TU_ADV], diff6);
+      mark(PH_ADVS); launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6);
       if (rk_step == 3) {
         mark(PH_PD);
         launch_pd_courant(l2, nb2, rk_step, stream);
-        launch_scalar_pd_update(LS(), nb_sc, nlev_max, rk_step, stream, tune[TU_PD]);
+        launch_scalar_pd_update(LP(), nb_pr, nlev_max, rk_step, stream, tune[TU_PD]);
       }
       swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi_col(LTM(), nb_tm, stream, tune[TU_CPRP]);

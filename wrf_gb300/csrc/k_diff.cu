@@ -1,4 +1,5 @@
 // Sixth-order numerical diffusion of the dry state at the first RK stage
+// and the Rayleigh damping toward the base state (damp_opt = 2)
 // (sixth_order_diffusion, dyn_em/module_big_step_utilities_em.F:6220-6636,
 // called from rk_tendency's forward step, dyn_em/module_em.F:879-932) and
 // the addition of those forward-in-time tendencies to the large-step
@@ -9,6 +10,7 @@
 // addition is one read of the stored tendency per point and stage.
 #include "common.cuh"
 #include "kernels.h"
+#include "ffmath.h"
 
 namespace wrfgpu {
 
@@ -143,7 +145,7 @@ __device__ float diff6_point(const Mem& m, const F3& f, const F2& mut, int i, in
 __global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L, int mode) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
-  if (!bp.valid || m.tendf[0] == nullptr) return;
+  if (!bp.valid || m.tendf[0] == nullptr || m.cf.diff_6th_opt == 0) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   const int ktf = min(m.kte, m.kde - 1);
   if (i < m.its || j < m.jts || k < m.kts || k > ktf) return;
@@ -193,6 +195,120 @@ __global__ void __launch_bounds__(BX* BY) k_sixth_diff_species_routine(Launch L)
   out(i, k, j) = diff6_point<DV_M>(m, f3p(m, m.q[0]), f2(m, WRFGPU_MUTS), i, k, j, c1h(k), c2h(k), coef, out(i, k, j));
 }
 
+// Stage 1, damp_opt = 2: rk_rayleigh_damp (module_big_step_utilities_em.F:
+// 5836-6110), relaxation of u, v, w and theta toward the base-state
+// profiles in the top zdamp metres, into ru_tendf .. t_tendf.  One thread per
+// column (i, j) of the memory extent, handling u, v, w and theta of that
+// column; the top layer's level heights are formed again where they are
+// used (the same expressions, so the same bits) instead of being stored.
+// A member that also stores the sixth-order diffusion accumulates onto it
+// (written earlier in the same stage); otherwise every level of the loop
+// range is written, the damped ones as 0 - term and the others as 0, which is
+// the reference's zeroed tendency plus its additions.  The level searches
+// stop at kts.
+__device__ __forceinline__ float rayleigh_weight(float ztop, float z, float zdamp) {
+  const float dcoef = 1.0f - fminf_f(1.0f, (ztop - z) / zdamp);
+  const float s = wrfgpu_ff::sinf_cr(0.5f * PI_F * dcoef);
+  return s * s;
+}
+template <typename HF>
+__device__ int rayleigh_top_level(float ztop, float zdamp, int kts, int ktf, HF height) {
+  int k1 = ktf;
+  float z = ztop;
+  while (z >= ztop - zdamp && k1 >= kts) {
+    z = height(k1);
+    k1 = k1 - 1;
+  }
+  return k1 + 2;
+}
+__device__ __forceinline__ float rayleigh_profile(const F1& prof, const F1& zb, float z, int kts, int ktf) {
+  int k2 = ktf;
+  while (zb(k2) > z && k2 > kts) k2 = k2 - 1;
+  if (k2 + 1 > ktf) return prof(k2) + (prof(k2) - prof(k2 - 1)) * (z - zb(k2)) / (zb(k2) - zb(k2 - 1));
+  return prof(k2) + (prof(k2 + 1) - prof(k2)) * (z - zb(k2)) / (zb(k2 + 1) - zb(k2));
+}
+__global__ void __launch_bounds__(BX* BY) k_rayleigh_damp(Launch L) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid || m.cf.damp_opt != 2 || m.tendf[0] == nullptr) return;
+  const int i = bp.i, j = bp.j;
+  if (i < m.its || j < m.jts) return;
+  const int kts = m.kts, ktf = min(m.kte, m.kde - 1), kde = m.kde;
+  const bool acc = m.cf.diff_6th_opt != 0;
+  const float dampcoef = m.cf.dampcoef, zdamp = m.cf.zdamp;
+  const F3 ph = f3(m, WRFGPU_PH_2), phb = f3(m, WRFGPU_PHB);
+  const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
+  const F1 zb = f1(m, WRFGPU_Z_BASE);
+  // u (:5897-5945)
+  if (i <= min(m.ite, m.ide) && j <= min(m.jte, m.jde - 1)) {
+    const F3 u = f3(m, WRFGPU_U_2), tend = f3p(m, m.tendf[0]);
+    const F1 prof = f1(m, WRFGPU_U_BASE);
+    const float mu = f2(m, WRFGPU_MUU)(i, j);
+    const float ztop = 0.5f * (phb(i, kde, j) + phb(i - 1, kde, j) + ph(i, kde, j) + ph(i - 1, kde, j)) / G;
+    auto height = [&](int k) {
+      return 0.25f * (phb(i, k, j) + phb(i, k + 1, j) + phb(i - 1, k, j) + phb(i - 1, k + 1, j) + ph(i, k, j) +
+                      ph(i, k + 1, j) + ph(i - 1, k, j) + ph(i - 1, k + 1, j)) / G;
+    };
+    const int k1 = rayleigh_top_level(ztop, zdamp, kts, ktf, height);
+    for (int k = kts; k <= ktf; ++k) {
+      float t = acc ? tend(i, k, j) : 0.f;
+      if (k >= k1) {
+        const float z = height(k);
+        t = t - (c1h(k) * mu + c2h(k)) * (rayleigh_weight(ztop, z, zdamp) * dampcoef) *
+                    (u(i, k, j) - rayleigh_profile(prof, zb, z, kts, ktf));
+      }
+      tend(i, k, j) = t;
+    }
+  }
+  // v (:5947-5995)
+  if (i <= min(m.ite, m.ide - 1) && j <= min(m.jte, m.jde)) {
+    const F3 v = f3(m, WRFGPU_V_2), tend = f3p(m, m.tendf[1]);
+    const F1 prof = f1(m, WRFGPU_V_BASE);
+    const float mv = f2(m, WRFGPU_MUV)(i, j);
+    const float ztop = 0.5f * (phb(i, kde, j) + phb(i, kde, j - 1) + ph(i, kde, j) + ph(i, kde, j - 1)) / G;
+    auto height = [&](int k) {
+      return 0.25f * (phb(i, k, j) + phb(i, k + 1, j) + phb(i, k, j - 1) + phb(i, k + 1, j - 1) + ph(i, k, j) +
+                      ph(i, k + 1, j) + ph(i, k, j - 1) + ph(i, k + 1, j - 1)) / G;
+    };
+    const int k1 = rayleigh_top_level(ztop, zdamp, kts, ktf, height);
+    for (int k = kts; k <= ktf; ++k) {
+      float t = acc ? tend(i, k, j) : 0.f;
+      if (k >= k1) {
+        const float z = height(k);
+        t = t - (c1h(k) * mv + c2h(k)) * (rayleigh_weight(ztop, z, zdamp) * dampcoef) *
+                    (v(i, k, j) - rayleigh_profile(prof, zb, z, kts, ktf));
+      }
+      tend(i, k, j) = t;
+    }
+  }
+  // w (:5997-6013) and theta (:6015-6062)
+  if (i <= min(m.ite, m.ide - 1) && j <= min(m.jte, m.jde - 1)) {
+    const F3 w = f3(m, WRFGPU_W_2), t3 = f3(m, WRFGPU_T_2);
+    const F3 tw = f3p(m, m.tendf[2]), tt = f3p(m, m.tendf[3]);
+    const F1 prof = f1(m, WRFGPU_T_BASE);
+    const float mt = f2(m, WRFGPU_MUT)(i, j);
+    const float ztop = (phb(i, kde, j) + ph(i, kde, j)) / G;
+    for (int k = kts; k <= min(m.kte, kde); ++k) {
+      float t = acc ? tw(i, k, j) : 0.f;
+      const float z = (phb(i, k, j) + ph(i, k, j)) / G;
+      if (z >= ztop - zdamp)
+        t = t - (c1f(k) * mt + c2f(k)) * (rayleigh_weight(ztop, z, zdamp) * dampcoef) * w(i, k, j);
+      tw(i, k, j) = t;
+    }
+    auto height = [&](int k) { return 0.5f * (phb(i, k, j) + phb(i, k + 1, j) + ph(i, k, j) + ph(i, k + 1, j)) / G; };
+    const int k1 = rayleigh_top_level(ztop, zdamp, kts, ktf, height);
+    for (int k = kts; k <= ktf; ++k) {
+      float t = acc ? tt(i, k, j) : 0.f;
+      if (k >= k1) {
+        const float z = height(k);
+        t = t - (c1h(k) * mt + c2h(k)) * (rayleigh_weight(ztop, z, zdamp) * dampcoef) *
+                    (t3(i, k, j) - rayleigh_profile(prof, zb, z, kts, ktf));
+      }
+      tt(i, k, j) = t;
+    }
+  }
+}
+
 // Every stage: rk_addtend_dry for the stored tendencies.  With physics off
 // the saved tendencies, h_diabatic, ph_tendf and mu_tendf are zero: the
 // stage-1 "tendf + save * msf" steps add +0 to a tendency that is never -0
@@ -235,6 +351,10 @@ void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s) {
 
 void launch_sixth_diff_species_routine(const Launch& L, int nblocks, cudaStream_t s) {
   k_sixth_diff_species_routine<<<nblocks, dim3(BX, BY), 0, s>>>(L);
+}
+
+void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s) {
+  k_rayleigh_damp<<<nblocks, dim3(BX, BY), 0, s>>>(L2);
 }
 
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s) {

@@ -45,11 +45,11 @@ enum : int {
 enum Tune { TU_PD = 0, TU_ADV, TU_AW, TU_AUV, TU_SUMF, TU_PREP, TU_SSF, TU_SSP, TU_CFL, TU_TENDW, TU_TENDU, TU_TENDV,
             TU_CPRP, TU_AMUT, NTUNE };
 constexpr int TUNE_MAXVAR = 4;
-constexpr int TUNE_NVAR[NTUNE] = {3, 3, 3, 4, 4, 2, 2, 4, 4, 3, 4, 4, 4, 4};
+constexpr int TUNE_NVAR[NTUNE] = {2, 3, 3, 4, 4, 2, 2, 4, 4, 3, 4, 4, 4, 4};
 constexpr int TUNE_DEFAULT[NTUNE] = {1, 1, 1, 0, 0, 1, 1, 2, 2, 1, 0, 0, 2, 0};
 // the parameter each variant stands for: blocks per SM, level chunks, or
 // (advance_uv, sumflux, rk_tend_u, rk_tend_v) 10 x blocks per SM + level chunks
-constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 3, 0}, {4, 5, 6, 0}, {2, 3, 4, 0}, {32, 42, 34, 44}, {32, 42, 34, 44},
+constexpr int TUNE_PARAM[NTUNE][TUNE_MAXVAR] = {{1, 2, 0, 0}, {2, 3, 4, 0}, {2, 3, 4, 0}, {32, 42, 34, 44}, {32, 42, 34, 44},
                                                 {3, 8, 0, 0}, {4, 8, 0, 0}, {1, 2, 4, 8}, {2, 4, 8, 16}, {2, 3, 4, 0},
                                                 {32, 42, 34, 44}, {32, 42, 34, 44}, {1, 2, 4, 8}, {2, 3, 4, 5}};
 
@@ -72,6 +72,7 @@ void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_
 // mode 0: u, v, w, theta into ru_tendf .. t_tendf; 1: the species into sc_tend
 void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s);
 void launch_sixth_diff_species_routine(const Launch& L, int nblocks, cudaStream_t s);
+void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s);
 
 // acoustic steps

@@ -67,6 +67,11 @@ typedef struct WrfDynConfig {
   int32_t diff_6th_opt, diff_6th_slopeopt;
   float diff_6th_factor, diff_6th_thresh;
   int32_t moist_mix6_off, scalar_mix6_off;
+  /* explicit diffusion (diff_opt = 1) with constant coefficients (km_opt = 1):
+   * khdif, kvdif in m2/s (Registry defaults 0); moist_mix2_off / scalar_mix2_off
+   * 1 leave the moist / passive species undiffused. */
+  int32_t km_opt, moist_mix2_off, scalar_mix2_off, pad_cfg;
+  float khdif, kvdif;
 } WrfDynConfig;
 
 /* Domain scalars that solve_em reads from grid% (double on the ABI; each
@@ -101,6 +106,7 @@ enum WrfGpuFieldId {
   WRFGPU_U_SAVE, WRFGPU_V_SAVE, WRFGPU_W_SAVE, WRFGPU_T_SAVE, WRFGPU_PH_SAVE,
   WRFGPU_C2A, WRFGPU_PM1, WRFGPU_A, WRFGPU_ALPHA, WRFGPU_GAMMA, WRFGPU_T_2SAVE,
   WRFGPU_RU_M, WRFGPU_RV_M, WRFGPU_WW_M, WRFGPU_ADVECT_TEND, WRFGPU_H_DIABATIC,
+  WRFGPU_T_INIT,  /* base-state theta perturbation (module_initialize_ideal.F:973): explicit diffusion of theta */
   WRFGPU_N3D,
   /* 2-D (ims:ime, jms:jme) */
   WRFGPU_F2D_BASE = 100,
@@ -117,6 +123,7 @@ enum WrfGpuFieldId {
   /* base-state profiles of the initial column (1,1) (module_initialize_ideal.F:1578-1586),
    * read by the Rayleigh damping toward them (damp_opt = 2) */
   WRFGPU_U_BASE, WRFGPU_V_BASE, WRFGPU_T_BASE, WRFGPU_Z_BASE,
+  WRFGPU_QV_BASE,  /* qv of column (1,1): explicit vertical diffusion of qv */
   WRFGPU_F1D_END,
   /* species: WRFGPU_SPECIES_BASE + 2*s is species s (moist first, then
    * passive scalars), + 1 its "old" (_1) copy */

@@ -234,16 +234,24 @@ int wrfgpu_rk_update_scalar_pd(const int *scs, const int *sce, float *scalar, fl
                                const int *rk_step, const float *dt, const int *spec_zone,
                                const WrfDynConfig *config_flags, WRFGPU_DIMS_ARGS);
 
+/* Index of qv in the moist array (P_QV = PARAM_FIRST_SCALAR in the
+ * Registry-generated indices): rk_scalar_tend diffuses species P_QV of a
+ * moist step vertically against its base profile. */
+#define WRFGPU_P_QV 2
+
 /* dyn_em/module_em.F:1096 rk_scalar_tend: for each species scs..sce
  * (scalar, scalar_old, scalar_tends: (ims:ime,kms:kme,jms:jme,scs:sce)),
  * advect_tend is zeroed over the tile and receives advect_scalar_pd at the
- * last stage when adv_opt = 1 (positive definite), else advect_scalar; at
- * stage 1, with diff_6th_opt != 0 and mix6_off false, the species'
- * sixth-order diffusion is added to scalar_tends.  adv_opt other than 0 / 1,
- * tenddec, and the explicit-diffusion options return WRFGPU_E_ARG; ww, wwI,
- * u_old, v_old, c1f, c2f, alt, h_tendency, z_tendency, RQVFTEN, base,
- * moist_step, rdn, khdif, kvdif, xkmhd, ph, mix2_off are unused on this path
- * (IEVA off, no cumulus tendency, diff_opt = 0). */
+ * last stage when adv_opt = 1 (positive definite), else advect_scalar.  At
+ * stage 1 scalar_tends receives the species' explicit diffusion
+ * (config_flags->diff_opt = 1 with km_opt = 1 and mix2_off false:
+ * horizontal_diffusion with khdif / prandtl, then vertical_diffusion with
+ * kvdif / prandtl, vertical_diffusion_mp against `base` for species
+ * WRFGPU_P_QV of a moist step; xkmhd, when given, must hold khdif / prandtl)
+ * and then its sixth-order diffusion (diff_6th_opt != 0, mix6_off false).
+ * adv_opt other than 0 / 1, tenddec and other diffusion options return
+ * WRFGPU_E_ARG; ww, wwI, u_old, v_old, c1f, c2f, h_tendency, z_tendency,
+ * RQVFTEN and ph are unused on this path (IEVA off, no cumulus tendency). */
 int wrfgpu_rk_scalar_tend(const int *scs, const int *sce, const WrfDynConfig *config_flags, const int *tenddec,
                           const int *rk_step, const float *dt_step, const float *ru, const float *rv,
                           const float *ww, const float *wwE, const float *wwI, const float *u_old,

@@ -752,6 +752,171 @@ void sixth_order_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R dt,
       }
 }
 
+// ---------------------------------------------------------------------------
+// Explicit diffusion (diff_opt = 1) with constant coefficients (km_opt = 1:
+// isotropic_km, module_diffusion_em.F, fills xkmh with khdif and xkhh with
+// khdif / prandtl everywhere, so each coefficient access below reads that
+// one value `xk`; every expression keeps the reference's order).  The loop
+// limits are those of periodic / symmetric boundaries.
+// ---------------------------------------------------------------------------
+// module_big_step_utilities_em.F:2715-2950 horizontal_diffusion
+template <typename R>
+void horizontal_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* c2_p, R* msfux_p,
+                          R* msfuy_p, R* msfvx_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p, R xk, R rdx,
+                          R rdy, const Dims& d) {
+  A3<R> field(field_p, d), tendency(tendency_p, d);
+  A2<R> MUT(mut_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx(msfvx_p, d), msfvx_inv(msfvx_inv_p, d),
+      msfvy(msfvy_p, d), msftx(msftx_p, d), msfty(msfty_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d);
+  const int ktf = std::min(d.kte, d.kde - 1);
+  int i_end = std::min(d.ite, d.ide - 1), j_end = std::min(d.jte, d.jde - 1), k_start = d.kts;
+  if (name == 'u') i_end = d.ite;
+  if (name == 'v') j_end = d.jte;
+  if (name == 'w') k_start = d.kts + 1;
+  auto M = [&](int k, int i, int j) { return c1(k) * MUT(i, j) + c2(k); };
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = k_start; k <= ktf; ++k)
+      for (int i = d.its; i <= i_end; ++i) {
+        R mkrdxm, mkrdxp, mrdx, mkrdym, mkrdyp, mrdy;
+        if (name == 'u') {
+          mkrdxm = (msftx(i - 1, j) / msfty(i - 1, j)) * M(k, i - 1, j) * xk * rdx;
+          mkrdxp = (msftx(i, j) / msfty(i, j)) * M(k, i, j) * xk * rdx;
+          mrdx = msfux(i, j) * msfuy(i, j) * rdx;
+          mkrdym = ((msfuy(i, j) + msfuy(i, j - 1)) / (msfux(i, j) + msfux(i, j - 1))) * R(0.25) *
+                   (M(k, i, j) + M(k, i, j - 1) + M(k, i - 1, j - 1) + M(k, i - 1, j)) * R(0.25) *
+                   (xk + xk + xk + xk) * rdy;
+          mkrdyp = ((msfuy(i, j) + msfuy(i, j + 1)) / (msfux(i, j) + msfux(i, j + 1))) * R(0.25) *
+                   (M(k, i, j) + M(k, i, j + 1) + M(k, i - 1, j + 1) + M(k, i - 1, j)) * R(0.25) *
+                   (xk + xk + xk + xk) * rdy;
+          mrdy = msfux(i, j) * msfuy(i, j) * rdy;
+        } else if (name == 'v') {
+          mkrdxm = ((msfvx(i, j) + msfvx(i - 1, j)) / (msfvy(i, j) + msfvy(i - 1, j))) * R(0.25) *
+                   (M(k, i, j) + M(k, i, j - 1) + M(k, i - 1, j - 1) + M(k, i - 1, j)) * R(0.25) *
+                   (xk + xk + xk + xk) * rdx;
+          mkrdxp = ((msfvx(i, j) + msfvx(i + 1, j)) / (msfvy(i, j) + msfvy(i + 1, j))) * R(0.25) *
+                   (M(k, i, j) + M(k, i, j - 1) + M(k, i + 1, j - 1) + M(k, i + 1, j)) * R(0.25) *
+                   (xk + xk + xk + xk) * rdx;
+          mrdx = msfvx(i, j) * msfvy(i, j) * rdx;
+          mkrdym = (msfty(i, j - 1) / msftx(i, j - 1)) * xk * rdy;
+          mkrdyp = (msfty(i, j) / msftx(i, j)) * xk * rdy;
+          mrdy = msfvx(i, j) * msfvy(i, j) * rdy;
+        } else if (name == 'w') {
+          mkrdxm = (msfux(i, j) / msfuy(i, j)) * R(0.25) *
+                   (M(k, i, j) + M(k, i - 1, j) + M(k, i, j) + M(k, i - 1, j)) * R(0.25) * (xk + xk + xk + xk) * rdx;
+          mkrdxp = (msfux(i + 1, j) / msfuy(i + 1, j)) * R(0.25) *
+                   (M(k, i + 1, j) + M(k, i, j) + M(k, i + 1, j) + M(k, i, j)) * R(0.25) * (xk + xk + xk + xk) * rdx;
+          mrdx = msftx(i, j) * msfty(i, j) * rdx;
+          mkrdym = (msfvy(i, j) * msfvx_inv(i, j)) * R(0.25) *
+                   (M(k, i, j) + M(k, i, j - 1) + M(k, i, j) + M(k, i, j - 1)) * R(0.25) * (xk + xk + xk + xk) * rdy;
+          mkrdyp = (msfvy(i, j + 1) * msfvx_inv(i, j + 1)) * R(0.25) *
+                   (M(k, i, j + 1) + M(k, i, j) + M(k, i, j + 1) + M(k, i, j)) * R(0.25) * (xk + xk + xk + xk) * rdy;
+          mrdy = msftx(i, j) * msfty(i, j) * rdy;
+        } else {
+          mkrdxm = (msfux(i, j) / msfuy(i, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i, j) + M(k, i - 1, j)) * rdx;
+          mkrdxp = (msfux(i + 1, j) / msfuy(i + 1, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i + 1, j) + M(k, i, j)) * rdx;
+          mrdx = msftx(i, j) * msfty(i, j) * rdx;
+          mkrdym = (msfvy(i, j) * msfvx_inv(i, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i, j) + M(k, i, j - 1)) * rdy;
+          mkrdyp = (msfvy(i, j + 1) * msfvx_inv(i, j + 1)) * R(0.5) * (xk + xk) * R(0.5) *
+                   (M(k, i, j + 1) + M(k, i, j)) * rdy;
+          mrdy = msftx(i, j) * msfty(i, j) * rdy;
+        }
+        tendency(i, k, j) = tendency(i, k, j) + (mrdx * (mkrdxp * (field(i + 1, k, j) - field(i, k, j)) -
+                                                         mkrdxm * (field(i, k, j) - field(i - 1, k, j))) +
+                                                 mrdy * (mkrdyp * (field(i, k, j + 1) - field(i, k, j)) -
+                                                         mkrdym * (field(i, k, j) - field(i, k, j - 1))));
+      }
+}
+
+// :2953-3060 horizontal_diffusion_3dmp: mass-point field minus its base state
+template <typename R>
+void horizontal_diffusion_3dmp(R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* c2_p, R* base_p, R* msfux_p,
+                               R* msfuy_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p, R xk, R rdx, R rdy,
+                               const Dims& d) {
+  A3<R> field(field_p, d), tendency(tendency_p, d), base(base_p, d);
+  A2<R> MUT(mut_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx_inv(msfvx_inv_p, d), msfvy(msfvy_p, d),
+      msftx(msftx_p, d), msfty(msfty_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d);
+  const int ktf = std::min(d.kte, d.kde - 1);
+  auto M = [&](int k, int i, int j) { return c1(k) * MUT(i, j) + c2(k); };
+  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+    for (int k = d.kts; k <= ktf; ++k)
+      for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i) {
+        const R mkrdxm = (msfux(i, j) / msfuy(i, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i, j) + M(k, i - 1, j)) * rdx;
+        const R mkrdxp =
+            (msfux(i + 1, j) / msfuy(i + 1, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i + 1, j) + M(k, i, j)) * rdx;
+        const R mrdx = msftx(i, j) * msfty(i, j) * rdx;
+        const R mkrdym =
+            (msfvy(i, j) * msfvx_inv(i, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i, j) + M(k, i, j - 1)) * rdy;
+        const R mkrdyp = (msfvy(i, j + 1) * msfvx_inv(i, j + 1)) * R(0.5) * (xk + xk) * R(0.5) *
+                         (M(k, i, j + 1) + M(k, i, j)) * rdy;
+        const R mrdy = msftx(i, j) * msfty(i, j) * rdy;
+        tendency(i, k, j) =
+            tendency(i, k, j) +
+            (mrdx * (mkrdxp * (field(i + 1, k, j) - field(i, k, j) - base(i + 1, k, j) + base(i, k, j)) -
+                     mkrdxm * (field(i, k, j) - field(i - 1, k, j) - base(i, k, j) + base(i - 1, k, j))) +
+             mrdy * (mkrdyp * (field(i, k, j + 1) - field(i, k, j) - base(i, k, j + 1) + base(i, k, j)) -
+                     mkrdym * (field(i, k, j) - field(i, k, j - 1) - base(i, k, j) + base(i, k, j - 1))));
+      }
+}
+
+// :3064-3581 vertical diffusion.  kind 'u' / 'v': vertical_diffusion_u / _v
+// (the wind minus its base profile, levels kts..ktf-1); 'w': vertical_diffusion
+// 'w' (levels kts+1..ktf); 'm': vertical_diffusion 'm' (no base); 'p':
+// vertical_diffusion_mp (a 1-D base profile, qv); 't': vertical_diffusion_3dmp
+// (a 3-D base state, theta).  mass: mut (u: muu, v: muv).
+template <typename R>
+void vertical_diffusion(char kind, R* field_p, R* tendency_p, R* base1_p, R* base3_p, R* c1_p, R* c2_p, R* alt_p,
+                        R* mass_p, R* rdn_p, R* rdnw_p, R kvdif, const Dims& d) {
+  A3<R> field(field_p, d), tendency(tendency_p, d), alt(alt_p, d), base3(base3_p, d);
+  A2<R> MASS(mass_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d), rdn(rdn_p, d), rdnw(rdnw_p, d), base1(base1_p, d);
+  const R g = K<R>::g;
+  const int ktf = std::min(d.kte, d.kde - 1);
+  const int i_end = kind == 'u' ? d.ite : std::min(d.ite, d.ide - 1);
+  const int j_end = std::min(d.jte, d.jde - 1);
+  std::vector<R> vf(d.kme - d.kms + 3);
+  auto V = [&](int k) -> R& { return vf[k - d.kms + 1]; };  // vflux(0:kte+1)
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int i = d.its; i <= i_end; ++i) {
+      if (kind == 'w') {
+        for (int k = d.kts; k <= ktf - 1; ++k) V(k) = (kvdif / alt(i, k, j)) * rdnw(k) * (field(i, k + 1, j) - field(i, k, j));
+        V(ktf) = R(0.);
+        for (int k = d.kts + 1; k <= ktf; ++k)
+          tendency(i, k, j) = tendency(i, k, j) + rdn(k) * g * g / (c1(k) * MASS(i, j) + c2(k)) /
+                                                      (R(0.5) * (alt(i, k, j) + alt(i, k - 1, j))) * (V(k) - V(k - 1));
+        continue;
+      }
+      for (int k = d.kts; k <= ktf - 1; ++k) {
+        if (kind == 'u')
+          V(k) = kvdif * rdn(k + 1) / (R(0.25) * (alt(i, k, j) + alt(i - 1, k, j) + alt(i, k + 1, j) + alt(i - 1, k + 1, j))) *
+                 (field(i, k + 1, j) - field(i, k, j) - base1(k + 1) + base1(k));
+        else if (kind == 'v')
+          V(k) = kvdif * rdn(k + 1) / (R(0.25) * (alt(i, k, j) + alt(i, k, j - 1) + alt(i, k + 1, j) + alt(i, k + 1, j - 1))) *
+                 (field(i, k + 1, j) - field(i, k, j) - base1(k + 1) + base1(k));
+        else if (kind == 'm')
+          V(k) = kvdif * rdn(k + 1) / (R(0.5) * (alt(i, k, j) + alt(i, k + 1, j))) * (field(i, k + 1, j) - field(i, k, j));
+        else if (kind == 'p')
+          V(k) = kvdif * rdn(k + 1) / (R(0.5) * (alt(i, k, j) + alt(i, k + 1, j))) *
+                 (field(i, k + 1, j) - field(i, k, j) - base1(k + 1) + base1(k));
+        else
+          V(k) = kvdif * rdn(k + 1) / (R(0.5) * (alt(i, k, j) + alt(i, k + 1, j))) *
+                 (field(i, k + 1, j) - field(i, k, j) - base3(i, k + 1, j) + base3(i, k, j));
+      }
+      V(d.kts - 1) = V(d.kts);
+      V(ktf) = R(0.);
+      if (kind == 'u' || kind == 'v') {
+        for (int k = d.kts; k <= ktf - 1; ++k) {
+          const R a = kind == 'u' ? R(0.5) * (alt(i - 1, k, j) + alt(i, k, j)) : R(0.5) * (alt(i, k, j - 1) + alt(i, k, j));
+          tendency(i, k, j) = tendency(i, k, j) + g * g * rdnw(k) / (c1(k) * MASS(i, j) + c2(k)) / a * (V(k) - V(k - 1));
+        }
+      } else {
+        for (int k = d.kts; k <= ktf; ++k)
+          tendency(i, k, j) = tendency(i, k, j) + g * g / (c1(k) * MASS(i, j) + c2(k)) / alt(i, k, j) * rdnw(k) *
+                                                      (V(k) - V(k - 1));
+      }
+    }
+}
+
 // module_big_step_utilities_em.F:5836-6110 rk_rayleigh_damp (damp_opt = 2):
 // relaxation of u, v, w and theta toward the base-state profiles (u_base,
 // v_base, t_base interpolated linearly in height z_base to the column's

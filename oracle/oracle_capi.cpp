@@ -173,9 +173,24 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
                        p3(WRFGPU_H_DIABATIC), td);
       return 0;
     case ORACLE_R_SIXTH_DIFF_SPECIES:
-      sixth_order_diffusion('m', D.q(species), p3(WRFGPU_H_DIABATIC), p2(WRFGPU_MUTS), dt_rk, cf, p1(WRFGPU_C1H),
-                            p1(WRFGPU_C2H), p3(WRFGPU_PHB), rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
-                            p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
+      // rk_scalar_tend's stage-1 diffusion of species `species` into the
+      // H_DIABATIC buffer (module_em.F:1378-1435): explicit (diff_opt = 1,
+      // its class's mix2_off off; iteration 1: qv against qv_base), then
+      // sixth-order (diff_6th_opt != 0, its class's mix6_off off)
+      if (cf.diff_opt == 1 && !(species < D.n_moist ? cf.moist_mix2_off : cf.scalar_mix2_off)) {
+        const R prandtl = R(1.) / R(3.0);
+        horizontal_diffusion('m', D.q(species), p3(WRFGPU_H_DIABATIC), p2(WRFGPU_MUTS), p1(WRFGPU_C1H),
+                             p1(WRFGPU_C2H), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX),
+                             p2(WRFGPU_MSFVX_INV), p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
+                             (R)cf.khdif / prandtl, rdx, rdy, td);
+        vertical_diffusion(iteration == 1 ? 'p' : 'm', D.q(species), p3(WRFGPU_H_DIABATIC), p1(WRFGPU_QV_BASE),
+                           (R*)nullptr, p1(WRFGPU_C1H), p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUTS),
+                           p1(WRFGPU_RDN), p1(WRFGPU_RDNW), (R)cf.kvdif / prandtl, td);
+      }
+      if (cf.diff_6th_opt != 0 && !(species < D.n_moist ? cf.moist_mix6_off : cf.scalar_mix6_off))
+        sixth_order_diffusion('m', D.q(species), p3(WRFGPU_H_DIABATIC), p2(WRFGPU_MUTS), dt_rk, cf, p1(WRFGPU_C1H),
+                              p1(WRFGPU_C2H), p3(WRFGPU_PHB), rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
+                              p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
       return 0;
     case ORACLE_R_ADVECT_SCALAR:
       zero_tend(p3(WRFGPU_ADVECT_TEND), td);

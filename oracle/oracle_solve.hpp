@@ -121,15 +121,15 @@ struct Domain {
     f2.assign(WRFGPU_N2D, std::vector<R>(n2, R(0)));
     f1.assign(WRFGPU_N1D, std::vector<R>(n1, R(0)));
     qs.assign(2 * (n_moist + n_scalar), std::vector<R>(n3, R(0)));
-    tendf.assign(cf.diff_6th_opt != 0 || cf.damp_opt == 2 ? 4 : 0, std::vector<R>(n3, R(0)));
-    sctend.assign(cf.diff_6th_opt != 0 ? n_moist + n_scalar : 0, std::vector<R>(n3, R(0)));
+    const bool diff1 = cf.diff_opt == 1, diff6 = cf.diff_6th_opt != 0;
+    tendf.assign(diff1 || diff6 || cf.damp_opt == 2 ? 4 : 0, std::vector<R>(n3, R(0)));
+    sctend.assign(diff1 || diff6 ? n_moist + n_scalar : 0, std::vector<R>(n3, R(0)));
   }
+  // species s's explicit (diff_opt = 1) and sixth-order diffusion switches
+  bool mix2(int s) const { return cf.diff_opt == 1 && !(s < n_moist ? cf.moist_mix2_off : cf.scalar_mix2_off); }
+  bool mix6(int s) const { return cf.diff_6th_opt != 0 && !(s < n_moist ? cf.moist_mix6_off : cf.scalar_mix6_off); }
   // species s's sc_tend, or null where it is not diffused
-  R* sct_of(int s) {
-    if (cf.diff_6th_opt == 0) return nullptr;
-    if (s < n_moist ? cf.moist_mix6_off : cf.scalar_mix6_off) return nullptr;
-    return sctend[s].data();
-  }
+  R* sct_of(int s) { return mix2(s) || mix6(s) ? sctend[s].data() : nullptr; }
   R* p3(int id) { return f3[id].data(); }
   R* p2(int id) { return f2[id - WRFGPU_F2D_BASE].data(); }
   R* p1(int id) { return f1[id - WRFGPU_F1D_BASE].data(); }
@@ -216,8 +216,8 @@ struct Domain {
       // forward-in-time tendencies formed at stage 1 (the sixth-order
       // diffusion; zero physics tendencies otherwise).
       std::vector<R> tmv(64, R(0)), tmh(64, R(0));
-      const bool diff6 = cf.diff_6th_opt != 0, damp2 = cf.damp_opt == 2;
-      if ((diff6 || damp2) && rk_step == 1)
+      const bool diff6 = cf.diff_6th_opt != 0, damp2 = cf.damp_opt == 2, diff1 = cf.diff_opt == 1;
+      if ((diff1 || diff6 || damp2) && rk_step == 1)
         for (auto& t : tendf) std::fill(t.begin(), t.end(), R(0));
       tiles([&](const Dims& td) {
         zero_tend(p3(WRFGPU_RU_TEND), td); zero_tend(p3(WRFGPU_RV_TEND), td); zero_tend(p3(WRFGPU_RW_TEND), td);
@@ -273,6 +273,34 @@ struct Domain {
                   p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), cf, p2(WRFGPU_MSFUX),
                   p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
                   (R*)nullptr, p1(WRFGPU_FNM), p1(WRFGPU_FNP), rdx, rdy, td);
+        if (diff1 && rk_step == 1) {
+          // module_em.F:801-877: explicit diffusion with the constant coefficients
+          // of km_opt = 1 (xkmh = khdif, xkhh = khdif / prandtl; theta's vertical
+          // coefficient 3 kvdif)
+          const R khdif = (R)cf.khdif, kvdif = (R)cf.kvdif, prandtl = R(1.) / R(3.0);
+          const R xkmh = khdif, xkhh = khdif / prandtl;
+          horizontal_diffusion('u', p3(WRFGPU_U_2), tendf[0].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                               p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
+                               p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
+          horizontal_diffusion('v', p3(WRFGPU_V_2), tendf[1].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                               p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
+                               p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
+          horizontal_diffusion('w', p3(WRFGPU_W_2), tendf[2].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1F), p1(WRFGPU_C2F),
+                               p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
+                               p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
+          horizontal_diffusion_3dmp(p3(WRFGPU_T_2), tendf[3].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                                    p3(WRFGPU_T_INIT), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX_INV),
+                                    p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkhh, rdx, rdy, td);
+          vertical_diffusion('u', p3(WRFGPU_U_2), tendf[0].data(), p1(WRFGPU_U_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+                             p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUU), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
+          vertical_diffusion('v', p3(WRFGPU_V_2), tendf[1].data(), p1(WRFGPU_V_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+                             p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUV), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
+          vertical_diffusion('w', p3(WRFGPU_W_2), tendf[2].data(), (R*)nullptr, (R*)nullptr, p1(WRFGPU_C1F),
+                             p1(WRFGPU_C2F), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
+          vertical_diffusion('t', p3(WRFGPU_T_2), tendf[3].data(), (R*)nullptr, p3(WRFGPU_T_INIT), p1(WRFGPU_C1H),
+                             p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW),
+                             R(3.) * kvdif, td);
+        }
         if (diff6 && rk_step == 1) {
           // module_em.F:879-932, with the state of stage 1
           const int fld[4] = {WRFGPU_U_2, WRFGPU_V_2, WRFGPU_W_2, WRFGPU_T_2};
@@ -293,7 +321,7 @@ struct Domain {
                            p1(WRFGPU_Z_BASE), (R)cf.dampcoef, (R)cf.zdamp, td);
       });
       for (int t = 0; t < 64; ++t) { mvc = std::max(mvc, tmv[t]); mhc = std::max(mhc, tmh[t]); }
-      if (diff6 || damp2)
+      if (diff1 || diff6 || damp2)
         tiles([&](const Dims& td) {
           rk_addtend_dry(p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), p3(WRFGPU_T_TEND),
                          tendf[0].data(), tendf[1].data(), tendf[2].data(), tendf[3].data(), p1(WRFGPU_C1H),
@@ -396,9 +424,20 @@ struct Domain {
         if (sct && rk_step == 1) std::fill(sctend[s].begin(), sctend[s].end(), R(0));
         tiles([&](const Dims& td) {
           zero_tend(p3(WRFGPU_ADVECT_TEND), td);
-          // rk_scalar_tend's stage-1 sixth-order diffusion (module_em.F:1421-1435):
-          // muts and the stage's dt
-          if (sct && rk_step == 1)
+          // rk_scalar_tend's stage-1 explicit diffusion (module_em.F:1378-1419; qv
+          // against its base profile, coefficients khdif / prandtl and kvdif /
+          // prandtl) and sixth-order diffusion (:1421-1435): muts and the stage's dt
+          if (rk_step == 1 && mix2(s)) {
+            const R prandtl = R(1.) / R(3.0);
+            const R khdq = (R)cf.khdif / prandtl, kvdq = (R)cf.kvdif / prandtl;
+            horizontal_diffusion('m', q(s), sct, p2(WRFGPU_MUTS), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MSFUX),
+                                 p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV), p2(WRFGPU_MSFVY),
+                                 p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), khdq, rdx, rdy, td);
+            vertical_diffusion(s == 0 ? 'p' : 'm', q(s), sct, p1(WRFGPU_QV_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+                               p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUTS), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdq,
+                               td);
+          }
+          if (rk_step == 1 && mix6(s))
             sixth_order_diffusion('m', q(s), sct, p2(WRFGPU_MUTS), dt_rk, cf, p1(WRFGPU_C1H), p1(WRFGPU_C2H),
                                   p3(WRFGPU_PHB), rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUX),
                                   p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);

@@ -450,3 +450,74 @@ def test_rk_scalar_tend_abi_bitwise(gpulib, case3, rk):
     assert not bad, bad
     if rk == 1:  # the diffusion was active
         assert max_abs(interior(case, fid, tends[:n3], halo=0), interior(case, fid, tends0[:n3], halo=0)) > 0.0
+
+
+
+@pytest.fixture(scope="module")
+def case3x():
+    """Three species (qv + 2 PD scalars), explicit diffusion (diff_opt = 1,
+    km_opt = 1) and sixth-order diffusion on."""
+    c = cases.small_case(nx=16, ny=12, kde=14, n_scalar=2, seed=29)
+    cf = c.desc.config
+    cf.diff_6th_opt = 2
+    cf.diff_6th_factor = 0.12
+    cf.diff_6th_thresh = 0.10
+    cf.diff_opt = 1
+    cf.km_opt = 1
+    cf.khdif = 800.0
+    cf.kvdif = 30.0
+    return c
+
+
+def test_rk_scalar_tend_abi_explicit_diffusion_bitwise(gpulib, case3x):
+    """wrfgpu_rk_scalar_tend at stage 1 with diff_opt = 1 over moist species
+    P_QV..P_QV+2 (module_em.F:1378-1435): every species' horizontal and
+    vertical explicit diffusion (qv's against qv_base) and then its
+    sixth-order diffusion added to scalar_tends, bit for bit with the
+    oracle's; a coefficient array that is not khdif / prandtl is refused."""
+    case = case3x
+    od = _state(case)
+    nsp = 3
+    n3 = od.get(abi.species_id(0)).size
+    cf = case.desc.config
+    rng = np.random.Generator(np.random.PCG64(41))
+    tends0 = (1e-9 * rng.standard_normal(nsp * n3)).astype(np.float32)
+    scal = _scalars(case, 1, 1)
+    xk = np.full(n3, np.float32(cf.khdif) / (np.float32(1.0) / np.float32(3.0)), dtype=np.float32)
+
+    def call(xkmhd):
+        a = _Argv()
+        a.i32(2); a.i32(1 + nsp); a.cfg(cf); a.i32(0); a.i32(1); a.f32(scal["dtrk"])
+        for nm in ("ru_m", "rv_m", "ww_m", "ww_m"):
+            a.arr(_f(od, nm))
+        a.null(); a.null(); a.null()                        # wwI, u_old, v_old
+        for nm in ("muts", "mub", "mu_1", "c1h", "c2h", "c1f", "c2f", "alt"):
+            a.arr(_f(od, nm))
+        a.arr(_stack(od, [abi.species_id(s, True) for s in range(nsp)]))
+        a.arr(_stack(od, [abi.species_id(s) for s in range(nsp)]))
+        tends = a.arr(tends0.copy())
+        a.arr(np.zeros(n3, np.float32))
+        a.null(); a.null(); a.null()                        # h_, z_tendency, RQVFTEN
+        a.arr(_f(od, "qv_base")); a.i32(1)                  # base, moist_step
+        for nm in ("fnm", "fnp", "msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy", "msftx", "msfty"):
+            a.arr(_f(od, nm))
+        a.f32(scal["rdx"]); a.f32(scal["rdy"]); a.arr(_f(od, "rdn")); a.arr(_f(od, "rdnw"))
+        a.f32(cf.khdif); a.f32(cf.kvdif); a.arr(xkmhd)
+        a.i32(2); a.f32(0.12); a.i32(1); a.arr(_f(od, "phb")); a.arr(_f(od, "ph_2")); a.i32(0); a.i32(0)
+        a.dims(case)
+        return a.call(gpulib, "wrfgpu_rk_scalar_tend"), tends
+
+    rc, tends = call(xk)
+    assert rc == 0
+    fid = abi.FIELD_ID["h_diabatic"]
+    bad = []
+    for s in range(nsp):
+        od.set(fid, tends0[s * n3:(s + 1) * n3])
+        od.run("sixth_diff_species", 1, 1 if s == 0 else 0, s)
+        got = tends[s * n3:(s + 1) * n3]
+        d = max_abs(interior(case, fid, got, halo=0), interior(case, fid, od.get(fid), halo=0))
+        if d != 0.0:
+            bad.append("scalar_tends %d: max|diff| %.3e" % (s, d))
+    assert not bad, bad
+    rc, _ = call(xk * np.float32(2.0))
+    assert rc == abi.WRFGPU_E_ARG

@@ -810,10 +810,61 @@ def test_full_step_bitwise_damp_opt_2(gpulib, diff6):
         assert max_abs(interior(case, fid, o0.get(fid), halo=3), interior(case, fid, od.get(fid), halo=3)) > 0, nm
 
 
+def explicit_case(variant):
+    """Explicit diffusion with constant coefficients (diff_opt = 1, km_opt = 1,
+    khdif 1500 m2/s, kvdif 40 m2/s) on the small case.  "with_diff6": on
+    top of the sixth-order diffusion's wave case, with damp_opt = 2 too, so
+    every stored tendency accumulates three terms; "mix2_off": the moist
+    species left out of the explicit diffusion."""
+    if variant == "with_diff6":
+        case = diffusion_case(2, 0)
+        case.desc.config.damp_opt = 2
+        case.desc.config.dampcoef = 0.01
+        case.desc.config.zdamp = 5000.0
+    else:
+        case = cases.small_case(nx=16, ny=12, kde=20, n_scalar=2, seed=31)
+    c = case.desc.config
+    c.diff_opt = 1
+    c.km_opt = 1
+    c.khdif = 1500.0
+    c.kvdif = 40.0
+    c.moist_mix2_off = 1 if variant == "mix2_off" else 0
+    return case
+
+
+@pytest.mark.parametrize("variant", ["alone", "with_diff6", "mix2_off"])
+def test_full_step_bitwise_explicit_diffusion(gpulib, variant):
+    """diff_opt = 1 (module_em.F:801-877 in rk_tendency's forward step and
+    1378-1419 in rk_scalar_tend): horizontal and vertical diffusion of u, v,
+    w, theta (against t_init) and the species (qv against qv_base) into the
+    stored tendencies at stage 1, ahead of the sixth-order diffusion and the
+    Rayleigh damping: every state field and species after two steps bit for
+    bit the oracle's, and the term is active (the oracle's state differs from
+    its diff_opt = 0 run)."""
+    case = explicit_case(variant)
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(2)
+    ge.step(2)
+    ge.sync()
+    bad = _bitwise_diffs(case, ge, od, old_too=False)
+    assert not bad, "\n".join(bad)
+    case.desc.config.diff_opt = 0
+    o0 = OracleDomain(case, "f32")
+    o0.step(2)
+    for fid in [abi.FIELD_ID[nm] for nm in ("u_2", "v_2", "w_2", "t_2")] + [abi.species_id(0), abi.species_id(2)]:
+        d = max_abs(interior(case, fid, o0.get(fid), halo=3), interior(case, fid, od.get(fid), halo=3))
+        if fid == abi.species_id(0) and variant == "mix2_off":
+            continue  # qv still feels the diffused winds; only its own term is off
+        assert d > 0, id_name(fid)
+
+
 def test_batched_damp_opt_2_with_other_options(gpulib):
     """An ensemble of a damp_opt = 2 member, a member with the sixth-order
-    diffusion and a plain one: each member gets the bits it gets alone."""
-    members = [rayleigh2_case(False), diffusion_case(1, 0), cases.small_case(nx=20, ny=12, kde=16, n_scalar=2, seed=6)]
+    diffusion, one with the explicit diffusion and a plain one: each member
+    gets the bits it gets alone."""
+    members = [rayleigh2_case(False), diffusion_case(1, 0), explicit_case("alone"),
+               cases.small_case(nx=20, ny=12, kde=16, n_scalar=2, seed=6)]
     ens = G.Ensemble.from_cases(members)
     ens.step(2)
     ens.sync()

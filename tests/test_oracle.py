@@ -368,3 +368,59 @@ def test_rayleigh_damping_relaxes_top_layer():
     top1, low1 = run(True)
     assert top1 < 0.97 * top0, (top0, top1)
     assert abs(low1 - low0) <= 1e-3 * low0, (low0, low1)
+
+
+def _level_deviation_rms(c, od, name):
+    """rms over the interior of a field's deviation from its level means."""
+    x = interior(c, abi.FIELD_ID[name], od.get(abi.FIELD_ID[name]))
+    return float(np.sqrt(np.mean((x - x.mean(axis=(0, 2), keepdims=True)) ** 2)))
+
+
+def test_explicit_diffusion_smooths_the_bubble():
+    """diff_opt = 1, km_opt = 1 (module_em.F:801-877 and 1378-1419): constant
+    khdif / kvdif diffusion lowers the horizontal deviation of theta and of
+    the species from their level means after 3 steps, against the same run
+    without it; with khdif = kvdif = 0 the step equals the undiffused one
+    bit for bit (the tendencies are exact zeros added)."""
+    def run(khdif, kvdif, on=True):
+        c = cases.small_case(nx=16, ny=12, kde=16, n_scalar=1, seed=23)
+        if on:
+            c.desc.config.diff_opt = 1
+            c.desc.config.km_opt = 1
+            c.desc.config.khdif = khdif
+            c.desc.config.kvdif = kvdif
+        od = OracleDomain(c, "f32")
+        od.step(3)
+        return c, od
+
+    c0, od0 = run(0.0, 0.0, on=False)
+    c1, od1 = run(2000.0, 50.0)
+    t0, t1 = _level_deviation_rms(c0, od0, "t_2"), _level_deviation_rms(c1, od1, "t_2")
+    assert t1 < 0.98 * t0, (t0, t1)
+    q0 = interior(c0, abi.species_id(1), od0.get(abi.species_id(1)))
+    q1 = interior(c1, abi.species_id(1), od1.get(abi.species_id(1)))
+    assert np.std(q1) < np.std(q0), (np.std(q0), np.std(q1))
+    cz, odz = run(0.0, 0.0)
+    for name in ("u_2", "v_2", "w_2", "t_2", "ph_2"):
+        a = od0.get(abi.FIELD_ID[name]); b = odz.get(abi.FIELD_ID[name])
+        assert np.array_equal(np.asarray(a), np.asarray(b)), name
+
+
+def test_explicit_diffusion_of_uniform_fields_is_zero():
+    """horizontal_diffusion 'm' / vertical_diffusion 'm' of a species that is
+    uniform in x, y and k add exactly zero (every difference is 0)."""
+    c = cases.small_case(nx=12, ny=10, kde=12, n_scalar=1, seed=5)
+    c.desc.config.diff_opt = 1
+    c.desc.config.km_opt = 1
+    c.desc.config.khdif = 500.0
+    c.desc.config.kvdif = 20.0
+    od = OracleDomain(c, "f32")
+    od.set(abi.FIELD_ID["muts"], np.asarray(od.get(abi.FIELD_ID["mub"])))  # a column mass, as after a stage
+    q = np.asarray(od.get(abi.species_id(1)))
+    od.set(abi.species_id(1), np.full_like(q, 1e-3))
+    fid = abi.FIELD_ID["h_diabatic"]
+    z = np.zeros_like(np.asarray(od.get(fid)))
+    od.set(fid, z)
+    od.run("sixth_diff_species", 1, 0, 1)
+    got = interior(c, fid, od.get(fid))[:, :-1, :]  # mass levels 1..kde-1
+    assert np.all(got == 0.0), np.abs(got).max()

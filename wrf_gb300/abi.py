@@ -42,7 +42,10 @@ class WrfDynConfig(C.Structure):
         "time_step_sound")] + [("w_crit_cfl", C.c_float), ("dampcoef", C.c_float), ("zdamp", C.c_float),
                                ("diff_6th_opt", C.c_int32), ("diff_6th_slopeopt", C.c_int32),
                                ("diff_6th_factor", C.c_float), ("diff_6th_thresh", C.c_float),
-                               ("moist_mix6_off", C.c_int32), ("scalar_mix6_off", C.c_int32)]
+                               ("moist_mix6_off", C.c_int32), ("scalar_mix6_off", C.c_int32),
+                               ("km_opt", C.c_int32), ("moist_mix2_off", C.c_int32),
+                               ("scalar_mix2_off", C.c_int32), ("pad_cfg", C.c_int32),
+                               ("khdif", C.c_float), ("kvdif", C.c_float)]
 
 
 class WrfGpuScalars(C.Structure):
@@ -63,12 +66,12 @@ F3D = ["u_1", "u_2", "v_1", "v_2", "w_1", "w_2", "t_1", "t_2", "ph_1", "ph_2",
        "ru_tend", "rv_tend", "rw_tend", "t_tend", "ph_tend",
        "u_save", "v_save", "w_save", "t_save", "ph_save",
        "c2a", "pm1", "a", "alpha", "gamma", "t_2save",
-       "ru_m", "rv_m", "ww_m", "advect_tend", "h_diabatic"]
+       "ru_m", "rv_m", "ww_m", "advect_tend", "h_diabatic", "t_init"]
 F2D = ["mu_1", "mu_2", "mub", "mut", "muu", "muv", "muts", "muus", "muvs", "mudf",
        "mu_save", "muave", "mu_tend", "msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy",
        "msftx", "msfty", "ht", "f", "e", "sina", "cosa"]
 F1D = ["znw", "znu", "dnw", "rdnw", "dn", "rdn", "fnm", "fnp", "c1h", "c2h", "c1f", "c2f",
-       "c3h", "c4h", "c3f", "c4f", "u_base", "v_base", "t_base", "z_base"]
+       "c3h", "c4h", "c3f", "c4f", "u_base", "v_base", "t_base", "z_base", "qv_base"]
 F2D_BASE = 100
 F1D_BASE = 200
 SPECIES_BASE = 300
@@ -148,4 +151,9 @@ def default_config(periodic_x=True, periodic_y=True, symmetric_y=False):
     c.diff_6th_thresh = 0.10
     c.moist_mix6_off = 0
     c.scalar_mix6_off = 0
+    c.km_opt = 1
+    c.moist_mix2_off = 0
+    c.scalar_mix2_off = 0
+    c.khdif = 0.0
+    c.kvdif = 0.0
     return c

@@ -398,7 +398,8 @@ def supercell_state(nx, ny, kde, dx, dt, ztop, bubbles, rng, n_scalar=0,
     for nm in ("c1h", "c2h", "c1f", "c2f", "c3h", "c4h", "c3f", "c4f"):
         f[nm] = hc[nm][1:].copy()
 
-    _base_profiles(f, t1, ph1, phb, kde)
+    _base_profiles(f, t1, qv3, ph1, phb, kde)
+    f["t_init"] = mem3(col(t_init, nkm), nkm)
     species = []
     qv_mem = mem3(qv3, nkm)
     species.append((qv_mem, qv_mem.copy()))
@@ -578,7 +579,8 @@ def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10
         fl[nm] = m[nm][1:].copy()
     for nm in ("c1h", "c2h", "c1f", "c2f", "c3h", "c4h", "c3f", "c4f"):
         fl[nm] = hc[nm][1:].copy()
-    _base_profiles(fl, t1, ph1, phb, kde)
+    _base_profiles(fl, t1, qv3, ph1, phb, kde)
+    fl["t_init"] = mem3(col(t_init, nkm), nkm)
     qv_mem = mem3(qv3, nkm)
     species = [(qv_mem, qv_mem.copy())]
     for _ in range(n_scalar):
@@ -590,13 +592,15 @@ def channel_state(nx, ny, kde, dx, dt, ztop, rng, f=1.0e-4, u_max=30.0, z_jet=10
     return Case(name, desc, fl, species, meta)
 
 
-def _base_profiles(f, t1, ph1, phb, kde):
-    """u_base, v_base, t_base, z_base of column (1,1) of the initial state
-    (module_initialize_ideal.F:1578-1586): theta before the moist conversion,
-    the winds, and the mass-level heights from phb + ph_1 (1-D, kms:kme)."""
+def _base_profiles(f, t1, qv3, ph1, phb, kde):
+    """u_base, v_base, t_base, qv_base, z_base of column (1,1) of the initial
+    state (module_initialize_ideal.F:1578-1586): theta before the moist
+    conversion, the winds, qv, and the mass-level heights from phb + ph_1
+    (1-D, kms:kme)."""
     h = abi.HALO
     nkm = kde - 1
-    for nm, col in (("u_base", f["u_1"][h, :nkm, h]), ("v_base", f["v_1"][h, :nkm, h]), ("t_base", t1[0, :, 0])):
+    for nm, col in (("u_base", f["u_1"][h, :nkm, h]), ("v_base", f["v_1"][h, :nkm, h]), ("t_base", t1[0, :, 0]),
+                    ("qv_base", qv3[0, :, 0])):
         a = np.zeros(kde)
         a[:nkm] = col
         f[nm] = a

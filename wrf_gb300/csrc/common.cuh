@@ -87,12 +87,19 @@ struct alignas(16) Mem {
   float* cfl_out;         // [2]: max vertical, max horizontal CFL (atomic max)
 };
 
-// Species s's stored sixth-order diffusion tendency sc_tend, or null where the
-// species is not diffused (diff_6th_opt = 0, or its class's mix6_off).
+// Species s's explicit (diff_opt = 1) and sixth-order diffusion switches
+// (rk_scalar_tend's mix2_off / mix6_off, module_em.F:1378-1435).
+__host__ __device__ inline bool mix2_on(const Mem& m, int s) {
+  return m.cf.diff_opt == 1 && !(s < m.n_moist ? m.cf.moist_mix2_off : m.cf.scalar_mix2_off);
+}
+__host__ __device__ inline bool mix6_on(const Mem& m, int s) {
+  return m.cf.diff_6th_opt != 0 && !(s < m.n_moist ? m.cf.moist_mix6_off : m.cf.scalar_mix6_off);
+}
+// Species s's stored diffusion tendency sc_tend, or null where the species is
+// not diffused.
 __host__ __device__ inline float* sc_tend_of(const Mem& m, int s) {
   if (m.sctend == nullptr) return nullptr;
-  const bool on = s < m.n_moist ? !m.cf.moist_mix6_off : !m.cf.scalar_mix6_off;
-  return on ? m.sctend + (long long)s * m.sct_n : nullptr;
+  return mix2_on(m, s) || mix6_on(m, s) ? m.sctend + (long long)s * m.sct_n : nullptr;
 }
 
 // Tensor map of buffer slot `slot` (field id or species slot), box `box`.

@@ -10,8 +10,8 @@
 //
 // Two calls of the reference that provably leave the state unchanged are not
 // issued: rk_addtend_dry adds physics tendencies that are identically zero
-// with physics off unless the sixth-order diffusion is on (module_em.F:959-1092;
-// k_diff.cu issues it then), and the post-RK calc_p_rho_phi
+// with physics off unless a diffusion or the Rayleigh damping stores
+// tendencies (module_em.F:959-1092; k_diff.cu issues it then), and the post-RK calc_p_rho_phi
 // (solve_em.F:4180-4203) recomputes al and p from the same inputs as the
 // stage-3 call.  initialize_moist_old (solve_em.F:517-527) is also skipped:
 // moist_old is overwritten by rk_update_scalar before any read.
@@ -63,8 +63,10 @@ int check_desc(const WrfGpuDomainDesc& d) {
       c.v_sca_adv_order != 3)
     return WRFGPU_E_ARG;
   if (!c.non_hydrostatic || c.zadvect_implicit != 0 || (c.damp_opt != 0 && c.damp_opt != 2 && c.damp_opt != 3) ||
-      (c.w_damping != 0 && c.w_damping != 1) || c.diff_opt != 0)
+      (c.w_damping != 0 && c.w_damping != 1) || (c.diff_opt != 0 && c.diff_opt != 1))
     return WRFGPU_E_ARG;
+  // explicit diffusion with the constant coefficients of km_opt = 1
+  if (c.diff_opt == 1 && (c.km_opt != 1 || !(c.khdif >= 0.f) || !(c.kvdif >= 0.f))) return WRFGPU_E_ARG;
   if (c.damp_opt == 2 && !(c.zdamp > 0.f)) return WRFGPU_E_ARG;
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) return WRFGPU_E_ARG;
   if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
@@ -123,7 +125,7 @@ struct Ensemble {
   int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0, nlev_max = 0;
   bool damp3 = false;  // some member uses damp_opt = 3
-  bool diff6 = false;  // some member uses diff_6th_opt != 0
+  bool diff6 = false;  // some member stores diffusion tendencies (diff_6th_opt != 0 or diff_opt = 1)
   bool damp2 = false;  // some member uses damp_opt = 2 (Rayleigh damping toward the base state)
   std::vector<size_t> n3, n2, n1;      // element counts per member (padded rows)
   std::vector<size_t> ni_, nk_, nj_, pitch_;  // Fortran extents and the padded row pitch
@@ -251,8 +253,9 @@ struct Ensemble {
       b += al256(n3[m] * 4);  // limiter scratch
       b += 6 * al256(n3[m] * 4);  // face Courant numbers and low-order factors of the PD transport
       if (fp64) b += 3 * al256(n3[m] * 8);
-      if (d.config.diff_6th_opt != 0 || d.config.damp_opt == 2) b += 4 * al256(n3[m] * 4);  // ru_tendf .. t_tendf
-      if (d.config.diff_6th_opt != 0) b += nsp * al256(n3[m] * 4);                            // sc_tend
+      const bool sct = d.config.diff_6th_opt != 0 || d.config.diff_opt == 1;  // stored diffusion tendencies
+      if (sct || d.config.damp_opt == 2) b += 4 * al256(n3[m] * 4);                   // ru_tendf .. t_tendf
+      if (sct) b += nsp * al256(n3[m] * 4);                                           // sc_tend
       off[m] = total;
       total += b;
     }
@@ -289,9 +292,10 @@ struct Ensemble {
       scr[m] = (float*)p; p += al256(n3[m] * 4);
       for (int q = 0; q < 6; ++q) { M.pdc[q] = (float*)p; p += al256(n3[m] * 4); }
       if (fp64) for (int q = 0; q < 3; ++q) { M.wd[q] = (double*)p; p += al256(n3[m] * 8); }
-      if (d.config.diff_6th_opt != 0 || d.config.damp_opt == 2)  // zero outside the loop limits (the pool is cleared)
+      const bool sct = d.config.diff_6th_opt != 0 || d.config.diff_opt == 1;
+      if (sct || d.config.damp_opt == 2)  // zero outside the loop limits (the pool is cleared)
         for (int q = 0; q < 4; ++q) { M.tendf[q] = (float*)p; p += al256(n3[m] * 4); }
-      if (d.config.diff_6th_opt != 0) {
+      if (sct) {
         M.sctend = (float*)p; M.sct_n = (long long)(al256(n3[m] * 4) / 4); p += M.nsp * al256(n3[m] * 4);
       }
       M.ns_total = num_sound_steps(d);
@@ -307,7 +311,7 @@ struct Ensemble {
       ns_max = std::max(ns_max, M.ns_total);
       nlev_max = std::max(nlev_max, M.kme - M.kms + 1);
       damp3 = damp3 || M.cf.damp_opt == 3;
-      diff6 = diff6 || M.cf.diff_6th_opt != 0;
+      diff6 = diff6 || M.cf.diff_6th_opt != 0 || M.cf.diff_opt == 1;
       damp2 = damp2 || M.cf.damp_opt == 2;
       bs2[m + 1] = bs2[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 2);
       bs3[m + 1] = bs3[m] + blocks_for(M.ims, M.ime, M.jms, M.jme, M.kme - M.kms + 1, 3);
@@ -436,9 +440,9 @@ struct Ensemble {
       mark(PH_TEND_W); launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
-      if (diff6 || damp2) {  // module_em.F:879-944 (stage 1), then rk_addtend_dry (solve_em.F:967)
+      if (diff6 || damp2) {  // module_em.F:801-944 (stage 1), then rk_addtend_dry (solve_em.F:967)
         mark(PH_DIFF);
-        if (rk_step == 1 && diff6) launch_sixth_diff(l3, nb3, 0, stream);
+        if (rk_step == 1 && diff6) launch_forward_diff(l3, nb3, 0, stream);
         if (rk_step == 1 && damp2) launch_rayleigh_damp(l2, nb2, stream);
         launch_addtend_dry(l3, nb3, stream);
       }
@@ -480,7 +484,7 @@ struct Ensemble {
       }
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
-      if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_sixth_diff(l3, nb3, 1, stream); }  // module_em.F:1421-1435
+      if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_forward_diff(l3, nb3, 1, stream); }  // module_em.F:1378-1435
       mark(PH_ADVS); launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6);
       if (rk_step == 3) {
         mark(PH_PD);
@@ -627,7 +631,7 @@ struct Ensemble {
       // and of rk_scalar_tend's sixth-order diffusion of one species
       case 130: launch_update_scalar_routine(l3, nb3, rk_step, 0, stream); break;
       case 131: launch_update_scalar_routine(l3, nb3, rk_step, 1, stream); break;
-      case 132: launch_sixth_diff_species_routine(l3, nb3, stream); break;
+      case 132: launch_species_diff_routine(l3, nb3, iteration, stream); break;
       case 24: launch_calc_p_rho_phi(l3, nb3, stream); break;
       case 25: launch_set_w_surface(l2, nb2, stream); break;
       case 26:
@@ -686,8 +690,8 @@ int fortran_call(const FCall& c) {
   if (its != ids || ite != ide || jts != jds || jte != jde || kts != kds || kte != kde) return WRFGPU_E_ARG;
   if (c.nsp < 1 || c.nsp > NSPMAX) return WRFGPU_E_ARG;
   std::lock_guard<std::mutex> lock(g_fmu);
-  // the sixth-order diffusion's stored tendencies are allocated with the domain
-  const int diff6 = c.cfg.diff_6th_opt != 0 ? 1 : 0;
+  // the diffusions' stored tendencies are allocated with the domain
+  const int diff6 = c.cfg.diff_6th_opt != 0 || c.cfg.diff_opt == 1 ? 1 : 0;
   const auto key = std::make_tuple(ide, jde, kde, c.nsp, diff6);
   Ensemble* e = nullptr;
   auto it = g_fcache.find(key);

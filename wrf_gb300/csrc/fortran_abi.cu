@@ -486,12 +486,11 @@ int wrfgpu_rk_scalar_tend(const int* scs, const int* sce, const WrfDynConfig* co
     return WRFGPU_E_ARG;
   // the schemes of this path: 0 (5th/3rd order) and 1 (positive definite)
   if (*adv_opt != 0 && *adv_opt != 1) return WRFGPU_E_ARG;
-  // IEVA off (wwI unused), no cumulus moisture tendency (RQVFTEN, moist_step),
-  // no explicit diffusion (diff_opt = 0: khdif, kvdif, xkmhd, base, alt, rdn,
-  // mix2_off, c1f, c2f), tenddec off (h_tendency, z_tendency)
-  (void)ww; (void)wwI; (void)u_old; (void)v_old; (void)c1f; (void)c2f; (void)alt; (void)h_tendency;
-  (void)z_tendency; (void)RQVFTEN; (void)base; (void)moist_step; (void)rdn; (void)khdif; (void)kvdif;
-  (void)xkmhd; (void)ph; (void)mix2_off;
+  // IEVA off (wwI unused), no cumulus moisture tendency (RQVFTEN), tenddec
+  // off (h_tendency, z_tendency); the explicit diffusion reads khdif, kvdif,
+  // alt, rdn, rdnw and (qv) base
+  (void)ww; (void)wwI; (void)u_old; (void)v_old; (void)c1f; (void)c2f; (void)h_tendency;
+  (void)z_tendency; (void)RQVFTEN; (void)ph;
   const int one = 1;
   const size_t ni = (size_t)(*ime - *ims + 1), nk = (size_t)(*kme - *kms + 1);
   const size_t n3 = ni * nk * (size_t)(*jme - *jms + 1);
@@ -513,18 +512,37 @@ int wrfgpu_rk_scalar_tend(const int* scs, const int* sce, const WrfDynConfig* co
                                 DIMS);
     if (rc) return rc;
     const int d6 = diff_6th_opt ? *diff_6th_opt : 0;
-    const bool off6 = mix6_off && *mix6_off;
-    if (*rk_step == 1 && d6 != 0 && !off6) {  // module_em.F:1421-1435
-      if (!scalar_tends || !phb || !diff_6th_factor) return WRFGPU_E_ARG;
+    const bool on6 = d6 != 0 && !(mix6_off && *mix6_off);
+    const bool on2 = config_flags->diff_opt == 1 && !(mix2_off && *mix2_off);
+    if (*rk_step == 1 && (on2 || on6)) {  // module_em.F:1378-1435
+      if (!scalar_tends || !mut || !c1h || !c2h) return WRFGPU_E_ARG;
+      if (on6 && (!phb || !diff_6th_factor)) return WRFGPU_E_ARG;
+      const bool qv = moist_step && *moist_step && im == WRFGPU_P_QV;
+      if (on2) {
+        if (!khdif || !kvdif || !alt || !rdn || !rdnw || (qv && !base)) return WRFGPU_E_ARG;
+        // km_opt = 1 (isotropic_km): the coefficient array holds khdif / prandtl
+        if (xkmhd && xkmhd[(size_t)(*its - *ims) + ni * ((size_t)(*kts - *kms) + nk * (size_t)(*jts - *jms))] !=
+                         *khdif / (1.f / 3.0f))
+          return WRFGPU_E_ARG;
+      }
       FCall c;
       set_dims(c, DIMS);
-      c.cfg = *config_flags; c.cfg.diff_6th_opt = d6; c.cfg.diff_6th_factor = *diff_6th_factor;
-      c.routine = 132; c.rk_step = 1; c.dtrk = *dt_step; c.rdx = *rdx; c.rdy = *rdy;
+      c.cfg = *config_flags; c.cfg.diff_6th_opt = on6 ? d6 : 0;
+      if (on6) c.cfg.diff_6th_factor = *diff_6th_factor;
+      c.cfg.moist_mix2_off = c.cfg.scalar_mix2_off = on2 ? 0 : 1;
+      c.cfg.moist_mix6_off = c.cfg.scalar_mix6_off = on6 ? 0 : 1;
+      if (on2) { c.cfg.khdif = *khdif; c.cfg.kvdif = *kvdif; }
+      c.routine = 132; c.rk_step = 1; c.iteration = qv ? 1 : 0;
+      c.dtrk = *dt_step; c.rdx = *rdx; c.rdy = *rdy;
       R(WRFGPU_SPECIES_BASE, scalar + off); RW(WRFGPU_H_DIABATIC, scalar_tends + off);
-      R(WRFGPU_MUTS, mut); R(WRFGPU_C1H, c1h); R(WRFGPU_C2H, c2h); R(WRFGPU_PHB, phb);
-      R(WRFGPU_MSFUX, msfux); R(WRFGPU_MSFUY, msfuy); R(WRFGPU_MSFVX, msfvx); R(WRFGPU_MSFVY, msfvy);
-      R(WRFGPU_MSFTX, msftx); R(WRFGPU_MSFTY, msfty);
-      (void)msfvx_inv;
+      R(WRFGPU_MUTS, mut); R(WRFGPU_C1H, c1h); R(WRFGPU_C2H, c2h);
+      R(WRFGPU_MSFUX, msfux); R(WRFGPU_MSFUY, msfuy); R(WRFGPU_MSFVX, msfvx); R(WRFGPU_MSFVX_INV, msfvx_inv);
+      R(WRFGPU_MSFVY, msfvy); R(WRFGPU_MSFTX, msftx); R(WRFGPU_MSFTY, msfty);
+      if (on6) R(WRFGPU_PHB, phb);
+      if (on2) {
+        R(WRFGPU_ALT, alt); R(WRFGPU_RDN, rdn); R(WRFGPU_RDNW, rdnw);
+        if (qv) R(WRFGPU_QV_BASE, base);
+      }
       rc = wrfgpu::fortran_call(c);
       if (rc) return rc;
     }

@@ -1,12 +1,19 @@
-// Sixth-order numerical diffusion of the dry state at the first RK stage
-// and the Rayleigh damping toward the base state (damp_opt = 2)
-// (sixth_order_diffusion, dyn_em/module_big_step_utilities_em.F:6220-6636,
-// called from rk_tendency's forward step, dyn_em/module_em.F:879-932) and
-// the addition of those forward-in-time tendencies to the large-step
-// tendencies at every stage (rk_addtend_dry, dyn_em/module_em.F:959-1092).
+// The forward-in-time tendencies of the first RK stage: explicit diffusion
+// with constant coefficients (diff_opt = 1, km_opt = 1: horizontal_diffusion,
+// horizontal_diffusion_3dmp and the vertical_diffusion family,
+// dyn_em/module_big_step_utilities_em.F:2715-3581, called from rk_tendency's
+// forward step, dyn_em/module_em.F:801-877, and from rk_scalar_tend,
+// :1378-1419), sixth-order numerical diffusion (sixth_order_diffusion,
+// :6220-6636, module_em.F:879-932 and 1421-1435) and the Rayleigh damping
+// toward the base state (damp_opt = 2); and the addition of those
+// tendencies to the large-step tendencies at every stage (rk_addtend_dry,
+// dyn_em/module_em.F:959-1092).
 //
-// Both are point kernels over (i, j) x level blocks.  The diffusion runs once
-// per large step on inputs that L2 holds for its 7-point stencils; the
+// The diffusions are point kernels over (i, j) x level blocks: every point
+// forms its explicit and sixth-order terms in the reference's order and
+// writes its stored tendency once (a vertical flux divergence reads the two
+// fluxes around the level, each formed from its own two levels).  They run
+// once per large step on inputs that L2 holds for their stencils; the
 // addition is one read of the stored tendency per point and stage.
 #include "common.cuh"
 #include "kernels.h"
@@ -135,17 +142,137 @@ __device__ float diff6_point(const Mem& m, const F3& f, const F2& mut, int i, in
   return t;
 }
 
+// ---- explicit diffusion (diff_opt = 1) with constant coefficients (km_opt = 1:
+// isotropic_km, module_diffusion_em.F:1717-1775, sets xkmh = khdif and
+// xkhh = khdif / prandtl everywhere, so each coefficient array access below is
+// that one value xk).
+
+constexpr float PRANDTL = 1.f / 3.0f;  // module_model_constants.F:86
+
+// horizontal_diffusion (module_big_step_utilities_em.F:2715-2950) of variable
+// kind V at (i, k, j) with mass mu, level coefficients c1, c2 and coefficient
+// xk; with `base`, horizontal_diffusion_3dmp (:2953-3060), the field minus
+// its 3-D base state.  Returns the term the reference adds to the tendency.
+template <int V>
+__device__ float hdiff_point(const Mem& m, const F3& f, const F3* base, const F2& mu, float c1, float c2, int i, int k,
+                             int j, float xk) {
+  const F2 msfux = f2(m, WRFGPU_MSFUX), msfuy = f2(m, WRFGPU_MSFUY), msfvx = f2(m, WRFGPU_MSFVX),
+           msfvx_inv = f2(m, WRFGPU_MSFVX_INV), msfvy = f2(m, WRFGPU_MSFVY), msftx = f2(m, WRFGPU_MSFTX),
+           msfty = f2(m, WRFGPU_MSFTY);
+  const float rdx = m.rdx, rdy = m.rdy;
+  auto M = [&](int ii, int jj) { return c1 * mu.ro(ii, jj) + c2; };
+  float mkrdxm, mkrdxp, mrdx, mkrdym, mkrdyp, mrdy;
+  if (V == DV_U) {  // :2801-2814
+    mkrdxm = (msftx.ro(i - 1, j) / msfty.ro(i - 1, j)) * M(i - 1, j) * xk * rdx;
+    mkrdxp = (msftx.ro(i, j) / msfty.ro(i, j)) * M(i, j) * xk * rdx;
+    mrdx = msfux.ro(i, j) * msfuy.ro(i, j) * rdx;
+    mkrdym = ((msfuy.ro(i, j) + msfuy.ro(i, j - 1)) / (msfux.ro(i, j) + msfux.ro(i, j - 1))) * 0.25f *
+             (M(i, j) + M(i, j - 1) + M(i - 1, j - 1) + M(i - 1, j)) * 0.25f * (xk + xk + xk + xk) * rdy;
+    mkrdyp = ((msfuy.ro(i, j) + msfuy.ro(i, j + 1)) / (msfux.ro(i, j) + msfux.ro(i, j + 1))) * 0.25f *
+             (M(i, j) + M(i, j + 1) + M(i - 1, j + 1) + M(i - 1, j)) * 0.25f * (xk + xk + xk + xk) * rdy;
+    mrdy = msfux.ro(i, j) * msfuy.ro(i, j) * rdy;
+  } else if (V == DV_V) {  // :2847-2856 (the y coefficients carry no mass there)
+    mkrdxm = ((msfvx.ro(i, j) + msfvx.ro(i - 1, j)) / (msfvy.ro(i, j) + msfvy.ro(i - 1, j))) * 0.25f *
+             (M(i, j) + M(i, j - 1) + M(i - 1, j - 1) + M(i - 1, j)) * 0.25f * (xk + xk + xk + xk) * rdx;
+    mkrdxp = ((msfvx.ro(i, j) + msfvx.ro(i + 1, j)) / (msfvy.ro(i, j) + msfvy.ro(i + 1, j))) * 0.25f *
+             (M(i, j) + M(i, j - 1) + M(i + 1, j - 1) + M(i + 1, j)) * 0.25f * (xk + xk + xk + xk) * rdx;
+    mrdx = msfvx.ro(i, j) * msfvy.ro(i, j) * rdx;
+    mkrdym = (msfty.ro(i, j - 1) / msftx.ro(i, j - 1)) * xk * rdy;
+    mkrdyp = (msfty.ro(i, j) / msftx.ro(i, j)) * xk * rdy;
+    mrdy = msfvx.ro(i, j) * msfvy.ro(i, j) * rdy;
+  } else if (V == DV_W) {  // :2885-2900
+    mkrdxm = (msfux.ro(i, j) / msfuy.ro(i, j)) * 0.25f * (M(i, j) + M(i - 1, j) + M(i, j) + M(i - 1, j)) * 0.25f *
+             (xk + xk + xk + xk) * rdx;
+    mkrdxp = (msfux.ro(i + 1, j) / msfuy.ro(i + 1, j)) * 0.25f * (M(i + 1, j) + M(i, j) + M(i + 1, j) + M(i, j)) *
+             0.25f * (xk + xk + xk + xk) * rdx;
+    mrdx = msftx.ro(i, j) * msfty.ro(i, j) * rdx;
+    mkrdym = (msfvy.ro(i, j) * msfvx_inv.ro(i, j)) * 0.25f * (M(i, j) + M(i, j - 1) + M(i, j) + M(i, j - 1)) *
+             0.25f * (xk + xk + xk + xk) * rdy;
+    mkrdyp = (msfvy.ro(i, j + 1) * msfvx_inv.ro(i, j + 1)) * 0.25f *
+             (M(i, j + 1) + M(i, j) + M(i, j + 1) + M(i, j)) * 0.25f * (xk + xk + xk + xk) * rdy;
+    mrdy = msftx.ro(i, j) * msfty.ro(i, j) * rdy;
+  } else {  // mass points: :2930-2937, :3030-3037
+    mkrdxm = (msfux.ro(i, j) / msfuy.ro(i, j)) * 0.5f * (xk + xk) * 0.5f * (M(i, j) + M(i - 1, j)) * rdx;
+    mkrdxp = (msfux.ro(i + 1, j) / msfuy.ro(i + 1, j)) * 0.5f * (xk + xk) * 0.5f * (M(i + 1, j) + M(i, j)) * rdx;
+    mrdx = msftx.ro(i, j) * msfty.ro(i, j) * rdx;
+    mkrdym = (msfvy.ro(i, j) * msfvx_inv.ro(i, j)) * 0.5f * (xk + xk) * 0.5f * (M(i, j) + M(i, j - 1)) * rdy;
+    mkrdyp = (msfvy.ro(i, j + 1) * msfvx_inv.ro(i, j + 1)) * 0.5f * (xk + xk) * 0.5f * (M(i, j + 1) + M(i, j)) * rdy;
+    mrdy = msftx.ro(i, j) * msfty.ro(i, j) * rdy;
+  }
+  const float q0 = f.ro(i, k, j);
+  float dxp = f.ro(i + 1, k, j) - q0, dxm = q0 - f.ro(i - 1, k, j);
+  float dyp = f.ro(i, k, j + 1) - q0, dym = q0 - f.ro(i, k, j - 1);
+  if (base) {  // field(+1) - field(0) - base(+1) + base(0), and so on
+    const F3& b = *base;
+    const float b0 = b.ro(i, k, j);
+    dxp = dxp - b.ro(i + 1, k, j) + b0;
+    dxm = dxm - b0 + b.ro(i - 1, k, j);
+    dyp = dyp - b.ro(i, k, j + 1) + b0;
+    dym = dym - b0 + b.ro(i, k, j - 1);
+  }
+  return mrdx * (mkrdxp * dxp - mkrdxm * dxm) + mrdy * (mkrdyp * dyp - mkrdym * dym);
+}
+
+// Vertical diffusion kinds: vertical_diffusion_u / _v (the wind minus its 1-D
+// base profile; module_big_step_utilities_em.F:3382-3581), vertical_diffusion
+// 'w' and 'm' (:3064-3187), vertical_diffusion_mp (a 1-D base profile, qv;
+// :3192-3281) and vertical_diffusion_3dmp (a 3-D base state, theta;
+// :3286-3376).
+enum { VD_U = 0, VD_V = 1, VD_W = 2, VD_M = 3, VD_MP = 4, VD_3DMP = 5 };
+
+// The vertical flux vflux(i, kk) (levels kts..ktf-1) of kind V.
+template <int V>
+__device__ __forceinline__ float vflux_at(const Mem& m, const F3& f, const F1& b1, const F3* b3, const F3& alt, int i,
+                                          int kk, int j, float kvdif) {
+  const F1 rdn = f1(m, WRFGPU_RDN);
+  const float df = f.ro(i, kk + 1, j) - f.ro(i, kk, j);
+  if (V == VD_W) return (kvdif / alt.ro(i, kk, j)) * f1(m, WRFGPU_RDNW)(kk) * df;
+  if (V == VD_U)
+    return kvdif * rdn(kk + 1) /
+           (0.25f * (alt.ro(i, kk, j) + alt.ro(i - 1, kk, j) + alt.ro(i, kk + 1, j) + alt.ro(i - 1, kk + 1, j))) *
+           (df - b1(kk + 1) + b1(kk));
+  if (V == VD_V)
+    return kvdif * rdn(kk + 1) /
+           (0.25f * (alt.ro(i, kk, j) + alt.ro(i, kk, j - 1) + alt.ro(i, kk + 1, j) + alt.ro(i, kk + 1, j - 1))) *
+           (df - b1(kk + 1) + b1(kk));
+  const float a = kvdif * rdn(kk + 1) / (0.5f * (alt.ro(i, kk, j) + alt.ro(i, kk + 1, j)));
+  if (V == VD_M) return a * df;
+  if (V == VD_MP) return a * (df - b1(kk + 1) + b1(kk));
+  return a * (df - b3->ro(i, kk + 1, j) + b3->ro(i, kk, j));
+}
+
+// The term vertical diffusion of kind V adds to the tendency at level k,
+// with the column mass c1 mass + c2 of that level: the divergence of the
+// fluxes vflux(k) - vflux(k-1), vflux(kts-1) = vflux(kts), vflux(ktf) = 0.
+template <int V>
+__device__ float vdiff_point(const Mem& m, const F3& f, const F1& b1, const F3* b3, float mass, float c1, float c2,
+                             int i, int k, int j, float kvdif) {
+  const F3 alt = f3(m, WRFGPU_ALT);
+  const int kts = m.kts, ktf = min(m.kte, m.kde - 1);
+  auto vf = [&](int kk) { return kk >= ktf ? 0.f : vflux_at<V>(m, f, b1, b3, alt, i, max(kk, kts), j, kvdif); };
+  const float dv = vf(k) - vf(k - 1);
+  const float g2 = G * G;
+  if (V == VD_U) return g2 * f1(m, WRFGPU_RDNW)(k) / (c1 * mass + c2) / (0.5f * (alt.ro(i - 1, k, j) + alt.ro(i, k, j))) * dv;
+  if (V == VD_V) return g2 * f1(m, WRFGPU_RDNW)(k) / (c1 * mass + c2) / (0.5f * (alt.ro(i, k, j - 1) + alt.ro(i, k, j))) * dv;
+  if (V == VD_W)
+    return f1(m, WRFGPU_RDN)(k) * G * G / (c1 * mass + c2) / (0.5f * (alt.ro(i, k, j) + alt.ro(i, k - 1, j))) * dv;
+  return g2 / (c1 * mass + c2) / alt.ro(i, k, j) * f1(m, WRFGPU_RDNW)(k) * dv;
+}
+
 // Stage 1, mode 0 (rk_tendency): the forward-in-time tendencies ru_tendf,
-// rv_tendf, rw_tendf and t_tendf of the sixth-order diffusion of u_2, v_2,
-// w_2 and t_2 with mut and the large step dt.  Mode 1 (rk_scalar_tend,
-// module_em.F:1421-1435, after the acoustic steps): each diffused species'
-// sc_tend, with muts and the stage's dt (dt / 3).  Loop limits of periodic /
-// symmetric boundaries (:6330-6443); points outside them keep the zero the
-// buffers were created with.
-__global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L, int mode) {
+// rv_tendf, rw_tendf and t_tendf of u_2, v_2, w_2 and t_2: the explicit
+// diffusion (diff_opt = 1; mut, khdif, kvdif), then the sixth-order diffusion
+// (mut, the large step dt).  Mode 1 (rk_scalar_tend, after the acoustic
+// steps): each diffused species' sc_tend, with muts, khdif / prandtl,
+// kvdif / prandtl and the stage's dt (dt / 3); qv (species 0) diffuses
+// vertically against its base profile qv_base.  Loop limits of periodic /
+// symmetric boundaries (:2760-2790, :3100-3130, :6330-6443); points outside
+// them keep the zero the buffers were created with.
+__global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
-  if (!bp.valid || m.tendf[0] == nullptr || m.cf.diff_6th_opt == 0) return;
+  const bool d1 = m.cf.diff_opt == 1, d6 = m.cf.diff_6th_opt != 0;
+  if (!bp.valid || m.tendf[0] == nullptr || !(d1 || d6)) return;
   const int i = bp.i, j = bp.j, k = bp.k;
   const int ktf = min(m.kte, m.kde - 1);
   if (i < m.its || j < m.jts || k < m.kts || k > ktf) return;
@@ -155,33 +282,83 @@ __global__ void __launch_bounds__(BX* BY) k_sixth_diff(Launch L, int mode) {
   if (mode == 1) {
     if (i > i_end || j > j_end) return;
     const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * stage_of(m, 1).dt_rk);
+    const float khdq = m.cf.khdif / PRANDTL, kvdq = m.cf.kvdif / PRANDTL;
     const F2 muts = f2(m, WRFGPU_MUTS);
+    const F1 qvb = f1(m, WRFGPU_QV_BASE);
     for (int s = 0; s < m.nsp; ++s) {
       float* sc = sc_tend_of(m, s);
-      if (sc) f3p(m, sc)(i, k, j) = diff6_point<DV_M>(m, f3p(m, m.q[s]), muts, i, k, j, c1, c2, coef);
+      if (!sc) continue;
+      const F3 q = f3p(m, m.q[s]);
+      float t = 0.f;
+      if (mix2_on(m, s)) {
+        t = t + hdiff_point<DV_M>(m, q, nullptr, muts, c1, c2, i, k, j, khdq);
+        const float mu = muts.ro(i, j);
+        t = t + (s == 0 ? vdiff_point<VD_MP>(m, q, qvb, nullptr, mu, c1, c2, i, k, j, kvdq)
+                        : vdiff_point<VD_M>(m, q, qvb, nullptr, mu, c1, c2, i, k, j, kvdq));
+      }
+      if (mix6_on(m, s)) t = diff6_point<DV_M>(m, q, muts, i, k, j, c1, c2, coef, t);
+      f3p(m, sc)(i, k, j) = t;
     }
     return;
   }
   const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * m.dt);
+  const float xkmh = m.cf.khdif, xkhh = m.cf.khdif / PRANDTL, kvdif = m.cf.kvdif;
   const F2 mut = f2(m, WRFGPU_MUT);
-  if (i <= m.ite && j <= j_end)
-    f3p(m, m.tendf[0])(i, k, j) = diff6_point<DV_U>(m, f3(m, WRFGPU_U_2), mut, i, k, j, c1, c2, coef);
-  if (i <= i_end && j <= m.jte)
-    f3p(m, m.tendf[1])(i, k, j) = diff6_point<DV_V>(m, f3(m, WRFGPU_V_2), mut, i, k, j, c1, c2, coef);
-  if (i <= i_end && j <= j_end) {
-    if (k >= m.kts + 1) {
-      const F1 c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
-      f3p(m, m.tendf[2])(i, k, j) = diff6_point<DV_W>(m, f3(m, WRFGPU_W_2), mut, i, k, j, c1f(k), c2f(k), coef);
+  if (i <= m.ite && j <= j_end) {
+    const F3 u = f3(m, WRFGPU_U_2);
+    float t = 0.f;
+    if (d1) {
+      t = t + hdiff_point<DV_U>(m, u, nullptr, mut, c1, c2, i, k, j, xkmh);
+      if (k <= ktf - 1)
+        t = t + vdiff_point<VD_U>(m, u, f1(m, WRFGPU_U_BASE), nullptr, f2(m, WRFGPU_MUU).ro(i, j), c1, c2, i, k, j,
+                                  kvdif);
     }
-    f3p(m, m.tendf[3])(i, k, j) = diff6_point<DV_M>(m, f3(m, WRFGPU_T_2), mut, i, k, j, c1, c2, coef);
+    if (d6) t = diff6_point<DV_U>(m, u, mut, i, k, j, c1, c2, coef, t);
+    f3p(m, m.tendf[0])(i, k, j) = t;
+  }
+  if (i <= i_end && j <= m.jte) {
+    const F3 v = f3(m, WRFGPU_V_2);
+    float t = 0.f;
+    if (d1) {
+      t = t + hdiff_point<DV_V>(m, v, nullptr, mut, c1, c2, i, k, j, xkmh);
+      if (k <= ktf - 1 && j <= j_end)
+        t = t + vdiff_point<VD_V>(m, v, f1(m, WRFGPU_V_BASE), nullptr, f2(m, WRFGPU_MUV).ro(i, j), c1, c2, i, k, j,
+                                  kvdif);
+    }
+    if (d6) t = diff6_point<DV_V>(m, v, mut, i, k, j, c1, c2, coef, t);
+    f3p(m, m.tendf[1])(i, k, j) = t;
+  }
+  if (i <= i_end && j <= j_end) {
+    const float mt = mut.ro(i, j);
+    if (k >= m.kts + 1) {
+      const F3 w = f3(m, WRFGPU_W_2);
+      const float c1w = f1(m, WRFGPU_C1F)(k), c2w = f1(m, WRFGPU_C2F)(k);
+      float t = 0.f;
+      if (d1) {
+        t = t + hdiff_point<DV_W>(m, w, nullptr, mut, c1w, c2w, i, k, j, xkmh);
+        t = t + vdiff_point<VD_W>(m, w, c1h, nullptr, mt, c1w, c2w, i, k, j, kvdif);
+      }
+      if (d6) t = diff6_point<DV_W>(m, w, mut, i, k, j, c1w, c2w, coef, t);
+      f3p(m, m.tendf[2])(i, k, j) = t;
+    }
+    const F3 th = f3(m, WRFGPU_T_2), tb = f3(m, WRFGPU_T_INIT);
+    float t = 0.f;
+    if (d1) {
+      t = t + hdiff_point<DV_M>(m, th, &tb, mut, c1, c2, i, k, j, xkhh);
+      t = t + vdiff_point<VD_3DMP>(m, th, c1h, &tb, mt, c1, c2, i, k, j, 3.f * kvdif);
+    }
+    if (d6) t = diff6_point<DV_M>(m, th, mut, i, k, j, c1, c2, coef, t);
+    f3p(m, m.tendf[3])(i, k, j) = t;
   }
 }
 
-// The routine-level form of rk_scalar_tend's sixth-order diffusion
-// (module_em.F:1421-1435): species 0 of a scratch domain accumulated into
-// the caller's scalar_tends, carried in the H_DIABATIC buffer, with mut
-// (MUTS) and the caller's dt_step.
-__global__ void __launch_bounds__(BX* BY) k_sixth_diff_species_routine(Launch L) {
+// The routine-level form of rk_scalar_tend's stage-1 diffusion of one species
+// (module_em.F:1378-1435): species 0 of a scratch domain, its explicit
+// diffusion (diff_opt = 1 and mix2 on; qv: vertical_diffusion_mp against
+// qv_base) and then its sixth-order diffusion (diff_6th_opt != 0 and mix6 on)
+// accumulated into the caller's scalar_tends, carried in the H_DIABATIC
+// buffer, with mut (MUTS) and the caller's dt_step.
+__global__ void __launch_bounds__(BX* BY) k_species_diff_routine(Launch L, int qv) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
@@ -189,10 +366,23 @@ __global__ void __launch_bounds__(BX* BY) k_sixth_diff_species_routine(Launch L)
   const int ktf = min(m.kte, m.kde - 1);
   if (i < m.its || j < m.jts || k < m.kts || k > ktf) return;
   if (i > min(m.ide - 1, m.ite) || j > min(m.jde - 1, m.jte)) return;
-  const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H);
-  const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * stage_of(m, 1).dt_rk);
+  const float c1 = f1(m, WRFGPU_C1H)(k), c2 = f1(m, WRFGPU_C2H)(k);
+  const F2 muts = f2(m, WRFGPU_MUTS);
+  const F3 q = f3p(m, m.q[0]);
   F3 out = f3(m, WRFGPU_H_DIABATIC);
-  out(i, k, j) = diff6_point<DV_M>(m, f3p(m, m.q[0]), f2(m, WRFGPU_MUTS), i, k, j, c1h(k), c2h(k), coef, out(i, k, j));
+  float t = out(i, k, j);
+  if (mix2_on(m, 0)) {
+    const float kvdq = m.cf.kvdif / PRANDTL;
+    t = t + hdiff_point<DV_M>(m, q, nullptr, muts, c1, c2, i, k, j, m.cf.khdif / PRANDTL);
+    const F1 qvb = f1(m, WRFGPU_QV_BASE);
+    t = t + (qv ? vdiff_point<VD_MP>(m, q, qvb, nullptr, muts.ro(i, j), c1, c2, i, k, j, kvdq)
+                : vdiff_point<VD_M>(m, q, qvb, nullptr, muts.ro(i, j), c1, c2, i, k, j, kvdq));
+  }
+  if (mix6_on(m, 0)) {
+    const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * stage_of(m, 1).dt_rk);
+    t = diff6_point<DV_M>(m, q, muts, i, k, j, c1, c2, coef, t);
+  }
+  out(i, k, j) = t;
 }
 
 // Stage 1, damp_opt = 2: rk_rayleigh_damp (module_big_step_utilities_em.F:
@@ -201,8 +391,8 @@ __global__ void __launch_bounds__(BX* BY) k_sixth_diff_species_routine(Launch L)
 // column (i, j) of the memory extent, handling u, v, w and theta of that
 // column; the top layer's level heights are formed again where they are
 // used (the same expressions, so the same bits) instead of being stored.
-// A member that also stores the sixth-order diffusion accumulates onto it
-// (written earlier in the same stage); otherwise every level of the loop
+// A member that also stores the explicit or sixth-order diffusion
+// accumulates onto it (written earlier in the same stage); otherwise every level of the loop
 // range is written, the damped ones as 0 - term and the others as 0, which is
 // the reference's zeroed tendency plus its additions.  The level searches
 // stop at kts.
@@ -234,7 +424,7 @@ __global__ void __launch_bounds__(BX* BY) k_rayleigh_damp(Launch L) {
   const int i = bp.i, j = bp.j;
   if (i < m.its || j < m.jts) return;
   const int kts = m.kts, ktf = min(m.kte, m.kde - 1), kde = m.kde;
-  const bool acc = m.cf.diff_6th_opt != 0;
+  const bool acc = m.cf.diff_6th_opt != 0 || m.cf.diff_opt == 1;
   const float dampcoef = m.cf.dampcoef, zdamp = m.cf.zdamp;
   const F3 ph = f3(m, WRFGPU_PH_2), phb = f3(m, WRFGPU_PHB);
   const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
@@ -345,12 +535,12 @@ __global__ void __launch_bounds__(BX* BY) k_addtend_dry(Launch L) {
 
 }  // namespace
 
-void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s) {
-  k_sixth_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L, mode);
+void launch_forward_diff(const Launch& L, int nblocks, int mode, cudaStream_t s) {
+  k_forward_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L, mode);
 }
 
-void launch_sixth_diff_species_routine(const Launch& L, int nblocks, cudaStream_t s) {
-  k_sixth_diff_species_routine<<<nblocks, dim3(BX, BY), 0, s>>>(L);
+void launch_species_diff_routine(const Launch& L, int nblocks, int qv, cudaStream_t s) {
+  k_species_diff_routine<<<nblocks, dim3(BX, BY), 0, s>>>(L, qv);
 }
 
 void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s) {

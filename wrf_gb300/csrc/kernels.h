@@ -70,8 +70,8 @@ void launch_tend_t_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t
 void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_t s);
 // sixth-order diffusion of the dry state at stage 1, and rk_addtend_dry (k_diff.cu)
 // mode 0: u, v, w, theta into ru_tendf .. t_tendf; 1: the species into sc_tend
-void launch_sixth_diff(const Launch& L, int nblocks, int mode, cudaStream_t s);
-void launch_sixth_diff_species_routine(const Launch& L, int nblocks, cudaStream_t s);
+void launch_forward_diff(const Launch& L, int nblocks, int mode, cudaStream_t s);
+void launch_species_diff_routine(const Launch& L, int nblocks, int qv, cudaStream_t s);
 void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s);
 

@@ -160,6 +160,27 @@ int wrfgpu_get_field(WrfGpuEnsemble* h, int member, int id, double* dst, long lo
  * Asynchronous: returns once the work is enqueued. */
 int wrfgpu_step(WrfGpuEnsemble* h, int nsteps);
 int wrfgpu_sync(WrfGpuEnsemble* h);
+/* Host state bound to the step (the coarse upload / step / download of a host
+ * time loop): for field ids[f] of `member`, in[f] (n[f] values, Fortran memory
+ * layout) is copied in before every step of wrfgpu_step_host and the field is
+ * copied out to out[f] after it; in or out (or one entry of either) may be
+ * null, and in[f] may equal out[f].  Buffers must be page-locked
+ * (cudaHostAlloc / cudaHostRegister) and stay valid while bound; binding a
+ * field again replaces its buffers.  WRFGPU_E_ARG for an unknown field, a
+ * wrong count or pageable memory. */
+int wrfgpu_bind_host_state(WrfGpuEnsemble* h, int member, int nfield, const int* ids, const float* const* in,
+                           float* const* out, const long long* n);
+int wrfgpu_unbind_host_state(WrfGpuEnsemble* h);
+/* nsteps times: the bound inputs copied in, one large step, the bound outputs
+ * copied out, each step's inputs read after the previous step's outputs are
+ * written (so in[f] == out[f] runs a host time loop); returns when the last
+ * copy is complete.  The copies overlap the kernels: the passive scalars'
+ * uploads run during stage 1's dynamics, the dry state's downloads during
+ * the last stage's scalar transport, and the passive scalars' downloads
+ * during the next step of the same call.  The results equal those of
+ * wrfgpu_set_field_f32 of every input, wrfgpu_step and wrfgpu_get_field_f32
+ * of every output, step by step, bit for bit. */
+int wrfgpu_step_host(WrfGpuEnsemble* h, int nsteps);
 /* Advance nsteps and return the device time in milliseconds (CUDA events on
  * the ensemble's stream). */
 int wrfgpu_time_steps(WrfGpuEnsemble* h, int nsteps, float* ms);

@@ -199,7 +199,235 @@ struct Ensemble {
     return WRFGPU_OK;
   }
 
+  // ---------------------------------------------------------------- host I/O step
+  // Host buffers bound to the step (wrfgpu_bind_host_state).  Every
+  // step_host() step copies each `in` buffer into its field before the
+  // solver's kernels and each field into its `out` buffer after them, all in
+  // one captured graph: the passive scalars, first read by stage 1's scalar
+  // transport, cross the host link on a second stream while stage 1's
+  // dynamics run; everything else (the dry state and the moist species, read
+  // from the first kernel on) before the step, and the downloads after it.
+  struct HostIO {
+    int member = 0, id = 0;
+    int species = -1;        // >= 0: the current value of that species (buffers looked up on the device)
+    bool late = false;       // a passive scalar: may arrive while stage 1's dynamics run
+    const float* in = nullptr;
+    float* out = nullptr;
+    float* dev = nullptr;    // a fixed field buffer (species < 0)
+    size_t count = 0, cols = 0, rows = 0, pitch = 0;
+    float* stage = nullptr;  // contiguous device copy
+  };
+  std::vector<HostIO> hio;
+  cudaStream_t cstream = nullptr;  // copy-in branch of the host I/O step
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaGraph_t graph_io[2] = {nullptr, nullptr};
+  cudaGraphExec_t gexec_io[2] = {nullptr, nullptr};
+  int io_swaps = 0;  // species-buffer swaps in one captured I/O step
+  bool io_pending = false;  // enqueue_step: the copy-in branch is still to be joined
+  bool io_step = false;     // enqueue_step runs inside a host I/O step
+  bool io_out_pending = false;
+  cudaEvent_t ev_ofork = nullptr, ev_ojoin = nullptr, ev_dryin = nullptr;
+
+  void io_join() {
+    if (!io_pending) return;
+    cudaStreamWaitEvent(stream, ev_join, 0);
+    io_pending = false;
+  }
+  // the _2 dry state is final once the last stage's fills and set_w_surface
+  // are done (enqueue_step): its bound outputs cross the link on the copy
+  // stream while the scalars advance
+  static bool early_out(const HostIO& b) {
+    return b.species < 0 && (b.id == WRFGPU_U_2 || b.id == WRFGPU_V_2 || b.id == WRFGPU_W_2 ||
+                             b.id == WRFGPU_T_2 || b.id == WRFGPU_PH_2 || b.id == WRFGPU_MU_2);
+  }
+  void copy_out(const HostIO& b, cudaStream_t st) {
+    if (b.species >= 0)
+      launch_pack_species(d_mems, b.member, b.species, b.stage, (int)b.cols, (int)b.rows, (int)b.pitch, st);
+    else
+      launch_pack_rows(b.dev, b.stage, (int)b.cols, (int)b.rows, (int)b.pitch, st);
+    cudaMemcpyAsync(b.out, b.stage, b.count * 4, cudaMemcpyDeviceToHost, st);
+  }
+  void io_dry_out() {
+    if (!io_step) return;
+    bool any = false;
+    for (const HostIO& b : hio) any = any || (b.out && early_out(b));
+    if (!any) return;
+    cudaEventRecord(ev_ofork, stream);
+    cudaStreamWaitEvent(cstream, ev_ofork, 0);
+    for (const HostIO& b : hio)
+      if (b.out && early_out(b)) copy_out(b, cstream);
+    cudaEventRecord(ev_ojoin, cstream);
+    io_out_pending = true;
+  }
+  void drop_io_graph() {
+    for (int v = 0; v < 2; ++v) {
+      if (gexec_io[v]) { cudaGraphExecDestroy(gexec_io[v]); gexec_io[v] = nullptr; }
+      if (graph_io[v]) { cudaGraphDestroy(graph_io[v]); graph_io[v] = nullptr; }
+    }
+  }
+  void unbind_host() {
+    drop_io_graph();
+    for (HostIO& b : hio) if (b.stage) cudaFree(b.stage);
+    hio.clear();
+  }
+  int bind_host(int member, int nfield, const int* ids, const float* const* in, float* const* out,
+                const long long* n) {
+    if (member < 0 || member >= nmem || nfield <= 0 || !ids || !n || (!in && !out)) return WRFGPU_E_ARG;
+    std::vector<HostIO> add;
+    for (int f = 0; f < nfield; ++f) {
+      HostIO b;
+      b.member = member; b.id = ids[f];
+      b.in = in ? in[f] : nullptr;
+      b.out = out ? out[f] : nullptr;
+      b.dev = field_ptr(member, b.id, &b.count, &b.cols, &b.rows, &b.pitch);
+      if (!b.dev || (long long)b.count != n[f] || (!b.in && !b.out)) return WRFGPU_E_ARG;
+      // the copies are graph nodes: the host buffers must be page-locked
+      for (const void* hp : {(const void*)b.in, (const void*)b.out}) {
+        if (!hp) continue;
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, hp) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+          cudaGetLastError();
+          return WRFGPU_E_ARG;
+        }
+      }
+      const int sid = b.id - WRFGPU_SPECIES_BASE;
+      if (sid >= 0 && sid % 2 == 0) {
+        b.species = sid / 2;
+        b.late = b.species >= hm[member].n_moist;
+        b.dev = nullptr;
+      }
+      add.push_back(b);
+    }
+    for (HostIO& b : add) {
+      if (cudaMalloc(&b.stage, b.count * 4) != cudaSuccess) {
+        for (HostIO& c : add) if (c.stage) cudaFree(c.stage);
+        return WRFGPU_E_NOMEM;
+      }
+    }
+    drop_io_graph();
+    for (HostIO& b : add) {  // a later binding of the same field replaces the earlier one
+      for (size_t q = 0; q < hio.size(); ++q)
+        if (hio[q].member == b.member && hio[q].id == b.id) {
+          cudaFree(hio[q].stage);
+          hio.erase(hio.begin() + q);
+          break;
+        }
+      hio.push_back(b);
+    }
+    return WRFGPU_OK;
+  }
+  // one step with its copies, enqueued on `stream` (and `cstream`)
+  int io_streams() {
+    if (cstream) return WRFGPU_OK;
+    CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin})
+      CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    return WRFGPU_OK;
+  }
+  // A passive scalar's download may wait for the head of the next step of the
+  // same call: it then crosses the link while that step uploads the dry state
+  // and runs stage 1's dynamics (the device buffers are not touched before
+  // stage 1's scalar transport, and the same copy stream uploads the scalar's
+  // next input only after it).
+  static bool deferrable(const HostIO& b) { return b.species >= 0 && b.late; }
+  // One step with its copies, enqueued on `stream` and `cstream`.  head: the
+  // previous step's deferred downloads first; defer: this step's passive
+  // scalars left for the next step's head (or flush_deferred).
+  int enqueue_io_step(bool head, bool defer) {
+    if (int rc = io_streams()) return rc;
+    auto unpack = [&](const HostIO& b, cudaStream_t st) {
+      if (b.species >= 0)
+        launch_unpack_species(d_mems, b.member, b.species, b.stage, (int)b.cols, (int)b.rows, (int)b.pitch, st);
+      else
+        launch_unpack_rows(b.stage, b.dev, nullptr, (int)b.cols, (int)b.rows, (int)b.pitch, st);
+    };
+    bool late = false;
+    for (const HostIO& b : hio) late = late || (b.in && b.late);
+    CK(cudaEventRecord(ev_fork, stream));
+    CK(cudaStreamWaitEvent(cstream, ev_fork, 0));
+    if (head)
+      for (const HostIO& b : hio)
+        if (b.out && deferrable(b)) copy_out(b, cstream);
+    // the dry state and the moist species first, at the link's full rate
+    for (const HostIO& b : hio)
+      if (b.in && !b.late) CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaEventRecord(ev_dryin, stream));
+    for (const HostIO& b : hio)
+      if (b.in && !b.late) unpack(b, stream);
+    CK(cudaStreamWaitEvent(cstream, ev_dryin, 0));
+    for (const HostIO& b : hio)
+      if (b.in && b.late) {
+        CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, cstream));
+        unpack(b, cstream);
+      }
+    CK(cudaEventRecord(ev_join, cstream));
+    io_pending = true;
+    io_step = true;
+    io_out_pending = false;
+    enqueue_step();
+    io_step = false;
+    io_join();
+    (void)late;
+    for (const HostIO& b : hio)
+      if (b.out && !early_out(b) && !(defer && deferrable(b))) copy_out(b, stream);
+    if (io_out_pending) {
+      CK(cudaStreamWaitEvent(stream, ev_ojoin, 0));
+      io_out_pending = false;
+    }
+    CK(cudaGetLastError());
+    return WRFGPU_OK;
+  }
+  int flush_deferred() {
+    for (const HostIO& b : hio)
+      if (b.out && deferrable(b)) copy_out(b, stream);
+    CK(cudaGetLastError());
+    return WRFGPU_OK;
+  }
+  // gexec_io[0]: the first step of a call (nothing deferred before it);
+  // gexec_io[1]: every later step
+  int build_io_graph(int v) {
+    if (gexec_io[v]) return WRFGPU_OK;
+    if (int rc = io_streams()) return rc;  // created outside the capture
+    capturing = true;
+    capture_swaps = 0;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_io_step(v == 1, true);
+    capturing = false;
+    io_swaps = capture_swaps;
+    for (int q = 0; q < capture_swaps; ++q) host_flip();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(stream, &g);
+    if (rc || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return rc ? rc : WRFGPU_E_CUDA;
+    }
+    graph_io[v] = g;
+    CK(cudaGraphInstantiate(&gexec_io[v], graph_io[v], 0));
+    return WRFGPU_OK;
+  }
+  int step_host(int nsteps) {
+    if (hio.empty() || nsteps < 0) return WRFGPU_E_ARG;
+    if (nsteps == 0) return WRFGPU_OK;
+    if (flags & WRFGPU_FLAG_NO_GRAPH) {
+      for (int s = 0; s < nsteps; ++s) { int rc = enqueue_io_step(s > 0, true); if (rc) return rc; }
+    } else {
+      for (int v = 0; v < 2; ++v) { int rc = build_io_graph(v); if (rc) return rc; }
+      for (int s = 0; s < nsteps; ++s) {
+        CK(cudaGraphLaunch(gexec_io[s > 0 ? 1 : 0], stream));
+        for (int q = 0; q < io_swaps; ++q) host_flip();
+      }
+    }
+    if (int rc = flush_deferred()) return rc;
+    CK(cudaStreamSynchronize(stream));
+    return WRFGPU_OK;
+  }
+
   ~Ensemble() {
+    unbind_host();
+    if (cstream) cudaStreamDestroy(cstream);
+    for (cudaEvent_t e : {ev_fork, ev_join, ev_ofork, ev_ojoin, ev_dryin})
+      if (e) cudaEventDestroy(e);
     if (d_stage) cudaFree(d_stage);
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
@@ -473,10 +701,21 @@ struct Ensemble {
       }
       mark(PH_SSF); launch_small_step_finish(l2, nb2, a, stream, tune[TU_SSF]);
       if (rk_step == 3) {
-        JobList j;  // solve_em.F:1754-1800
+        // solve_em.F:1754-1800, and the end-of-step fills of the _2 dry state
+        // (set_phys_bc_dry_2, :4439-4535) followed by set_w_surface (:4700-4750),
+        // both issued here: the dry state is final after small_step_finish,
+        // and nothing until the end of the step reads these fields' halos or
+        // w (the scalar transport reads mass fluxes and column masses,
+        // calc_p_rho_phi mass columns), so the result is the same and a host
+        // I/O step can copy the dry state out while the scalars advance
+        JobList j;
         j.f3(WRFGPU_RU_M, 'u'); j.f3(WRFGPU_RV_M, 'v'); j.f3(WRFGPU_WW_M, 'w');
         j.f2(WRFGPU_MUT, 't'); j.f2(WRFGPU_MUTS, 't');
+        j.f3(WRFGPU_U_2, 'u'); j.f3(WRFGPU_V_2, 'v'); j.f3(WRFGPU_W_2, 'w'); j.f3(WRFGPU_T_2, 'p');
+        j.f3(WRFGPU_PH_2, 'w'); j.f2(WRFGPU_MU_2, 't');
         fill(j);
+        mark(PH_WSURF); launch_set_w_surface(l2, nb2, stream);
+        io_dry_out();
         mark(PH_USPD); launch_update_scalar_pd_col(LTM(), nb_tm, a, stream, diff6);
         JobList jo;
         for (int s = 0; s < nsp_max; ++s) jo.sp(s, 1, 'p');
@@ -484,6 +723,7 @@ struct Ensemble {
       }
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
+      io_join();  // passive scalars copied in by a host I/O step are read from here on
       if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_forward_diff(l3, nb3, 1, stream); }  // module_em.F:1378-1435
       mark(PH_ADVS); launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6);
       if (rk_step == 3) {
@@ -501,15 +741,14 @@ struct Ensemble {
         fill(j);
       }
     }
-    {  // set_phys_bc_dry_2 + species (solve_em.F:4439-4535)
+    {  // set_phys_bc_dry_2 of the _1 state + species (solve_em.F:4439-4535); the
+       // _2 state's fills and set_w_surface ran after the last small_step_finish
       JobList j;
-      j.f3(WRFGPU_U_1, 'u'); j.f3(WRFGPU_U_2, 'u'); j.f3(WRFGPU_V_1, 'v'); j.f3(WRFGPU_V_2, 'v');
-      j.f3(WRFGPU_W_1, 'w'); j.f3(WRFGPU_W_2, 'w'); j.f3(WRFGPU_T_1, 'p'); j.f3(WRFGPU_T_2, 'p');
-      j.f3(WRFGPU_PH_1, 'w'); j.f3(WRFGPU_PH_2, 'w'); j.f2(WRFGPU_MU_1, 't'); j.f2(WRFGPU_MU_2, 't');
+      j.f3(WRFGPU_U_1, 'u'); j.f3(WRFGPU_V_1, 'v'); j.f3(WRFGPU_W_1, 'w'); j.f3(WRFGPU_T_1, 'p');
+      j.f3(WRFGPU_PH_1, 'w'); j.f2(WRFGPU_MU_1, 't');
       for (int s = 0; s < nsp_max; ++s) j.sp(s, 0, 'p');
       fill(j);
     }
-    mark(PH_WSURF); launch_set_w_surface(l2, nb2, stream);
     mark(PH_END);
   }
 
@@ -583,6 +822,7 @@ struct Ensemble {
     }
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    drop_io_graph();
     CK(cudaGetLastError());
     return WRFGPU_OK;
   }
@@ -881,6 +1121,23 @@ int wrfgpu_get_field(WrfGpuEnsemble* h, int member, int id, double* dst, long lo
 int wrfgpu_step(WrfGpuEnsemble* h, int nsteps) {
   if (!h || nsteps < 0) return WRFGPU_E_ARG;
   return h->e.step(nsteps);
+}
+
+int wrfgpu_bind_host_state(WrfGpuEnsemble* h, int member, int nfield, const int* ids, const float* const* in,
+                           float* const* out, const long long* n) {
+  if (!h) return WRFGPU_E_ARG;
+  return h->e.bind_host(member, nfield, ids, in, out, n);
+}
+
+int wrfgpu_unbind_host_state(WrfGpuEnsemble* h) {
+  if (!h) return WRFGPU_E_ARG;
+  h->e.unbind_host();
+  return WRFGPU_OK;
+}
+
+int wrfgpu_step_host(WrfGpuEnsemble* h, int nsteps) {
+  if (!h) return WRFGPU_E_ARG;
+  return h->e.step_host(nsteps);
 }
 
 int wrfgpu_sync(WrfGpuEnsemble* h) {

@@ -151,7 +151,37 @@ __global__ void k_pack_rows(const float* __restrict__ src, float* __restrict__ d
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
       dst[(size_t)r * cols + c] = src[(size_t)r * pitch + c];
 }
+// The same for species s of member `member`, whose current and spare buffers
+// are read from the device member table when the copy runs (the buffers
+// exchange roles at every scalar update, so a captured copy must not hold
+// their addresses).  Unpacking writes both buffers.
+__global__ void k_unpack_species(const Mem* __restrict__ mems, int member, int s, const float* __restrict__ src,
+                                 int cols, int rows, int pitch) {
+  float* dst = mems[member].q[s];
+  float* dst2 = mems[member].qa[s];
+  for (int r = blockIdx.y; r < rows; r += gridDim.y)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+      const float v = src[(size_t)r * cols + c];
+      dst[(size_t)r * pitch + c] = v;
+      dst2[(size_t)r * pitch + c] = v;
+    }
+}
+__global__ void k_pack_species(const Mem* __restrict__ mems, int member, int s, float* __restrict__ dst, int cols,
+                               int rows, int pitch) {
+  const float* src = mems[member].q[s];
+  for (int r = blockIdx.y; r < rows; r += gridDim.y)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
+      dst[(size_t)r * cols + c] = src[(size_t)r * pitch + c];
+}
 static dim3 rows_grid(int cols, int rows) { return dim3((cols + 255) / 256, rows < 65535 ? rows : 65535); }
+void launch_unpack_species(const Mem* mems, int member, int s, const float* src, int cols, int rows, int pitch,
+                           cudaStream_t st) {
+  if (cols > 0 && rows > 0) k_unpack_species<<<rows_grid(cols, rows), 256, 0, st>>>(mems, member, s, src, cols, rows, pitch);
+}
+void launch_pack_species(const Mem* mems, int member, int s, float* dst, int cols, int rows, int pitch,
+                         cudaStream_t st) {
+  if (cols > 0 && rows > 0) k_pack_species<<<rows_grid(cols, rows), 256, 0, st>>>(mems, member, s, dst, cols, rows, pitch);
+}
 void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s) {
   if (cols > 0 && rows > 0) k_unpack_rows<<<rows_grid(cols, rows), 256, 0, s>>>(src, dst, dst2, cols, rows, pitch);
 }

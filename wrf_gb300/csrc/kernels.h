@@ -99,6 +99,10 @@ void launch_calc_p_rho_phi(const Launch& L3, int nblocks, cudaStream_t s);
 // host <-> device field copies through a contiguous staging buffer
 void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s);
 void launch_pack_rows(const float* src, float* dst, int cols, int rows, int pitch, cudaStream_t s);
+void launch_unpack_species(const Mem* mems, int member, int s, const float* src, int cols, int rows, int pitch,
+                           cudaStream_t st);
+void launch_pack_species(const Mem* mems, int member, int s, float* dst, int cols, int rows, int pitch,
+                         cudaStream_t st);
 void launch_calc_p_rho_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s);        // mass tiles
 // sct: some member stores the species' sixth-order diffusion tendency sc_tend
 void launch_update_scalar_pd_col(const TileLaunch& L, int nblocks, StepArgs a, cudaStream_t s, bool sct = false);  // mass tiles

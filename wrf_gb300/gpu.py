@@ -41,6 +41,9 @@ def load():
     for nm in ("wrfgpu_set_field_f32", "wrfgpu_get_field_f32", "wrfgpu_set_field", "wrfgpu_get_field"):
         getattr(L, nm).argtypes = [vp, C.c_int, C.c_int, vp, C.c_longlong]
     L.wrfgpu_step.argtypes = [vp, C.c_int]
+    L.wrfgpu_bind_host_state.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(vp), P(vp), P(C.c_longlong)]
+    L.wrfgpu_unbind_host_state.argtypes = [vp]
+    L.wrfgpu_step_host.argtypes = [vp, C.c_int]
     L.wrfgpu_sync.argtypes = [vp]
     L.wrfgpu_time_steps.argtypes = [vp, C.c_int, P(C.c_float)]
     L.wrfgpu_run_routine.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
@@ -122,6 +125,25 @@ class Ensemble:
 
     def step(self, n=1):
         _check(self.L.wrfgpu_step(self.h, n), "wrfgpu_step")
+
+    def bind_host_state(self, member, fids, inputs, outputs=None):
+        """Bind page-locked float32 numpy arrays (one per field id; outputs
+        default to the inputs) to wrfgpu_step_host."""
+        outputs = inputs if outputs is None else outputs
+        n = len(fids)
+        ids = (C.c_int * n)(*fids)
+        vin = (C.c_void_p * n)(*[None if a is None else a.ctypes.data for a in inputs])
+        vout = (C.c_void_p * n)(*[None if a is None else a.ctypes.data for a in outputs])
+        cnt = (C.c_longlong * n)(*[(a if a is not None else b).size for a, b in zip(inputs, outputs)])
+        self._host_bufs = (list(inputs), list(outputs))
+        _check(self.L.wrfgpu_bind_host_state(self.h, member, n, ids, vin, vout, cnt), "bind_host_state")
+
+    def step_host(self, n=1):
+        _check(self.L.wrfgpu_step_host(self.h, n), "step_host")
+
+    def unbind_host_state(self):
+        _check(self.L.wrfgpu_unbind_host_state(self.h), "unbind_host_state")
+        self._host_bufs = None
 
     def sync(self):
         _check(self.L.wrfgpu_sync(self.h), "wrfgpu_sync")

@@ -41,10 +41,12 @@ constexpr float W_BETA = 1.0f;   // w_damp activation Courant number, :89
 
 // Tensor maps (TMA descriptors) of every 3-D field buffer of a member: slot
 // f < WRFGPU_N3D for the fields, WRFGPU_N3D + 3 s + {0, 1, 2} for species s's
-// buffers (first current, old, first spare).  Two boxes per slot: the
-// tile plus a 4-point halo, (TX + 8) x 1 x (TY + 8) from (i0 - 4, j0 - 4),
-// and the tile alone, TX x 1 x TY from (i0, j0).
-constexpr int NMAPSLOT = WRFGPU_N3D + 3 * NSPMAX;
+// buffers (first current, old, first spare), PDC_SLOT + q for the PD
+// transport's face array pdc[q].  Two boxes per slot: the tile plus a
+// 4-point halo, (TX + 8) x 1 x (TY + 8) from (i0 - 4, j0 - 4), and the tile
+// alone, TX x 1 x TY from (i0, j0).
+constexpr int PDC_SLOT = WRFGPU_N3D + 3 * NSPMAX;
+constexpr int NMAPSLOT = PDC_SLOT + 6;
 constexpr int BOX_HALO = 0, BOX_TILE = 1, NBOX = 2;
 
 // Error word bits (Mem::err): set by kernels, read by the host between steps.

@@ -568,6 +568,8 @@ struct Ensemble {
           if ((rc = enc(WRFGPU_N3D + 3 * sp + 1, M.qo[sp]))) return rc;
           if ((rc = enc(WRFGPU_N3D + 3 * sp + 2, M.qa[sp]))) return rc;
         }
+        for (int q = 0; q < 6; ++q)
+          if ((rc = enc(PDC_SLOT + q, M.pdc[q]))) return rc;
       }
       CK(cudaMalloc(&d_tmaps, maps.size() * sizeof(CUtensorMap)));
       CK(cudaMemcpy(d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));

@@ -279,8 +279,10 @@ struct PDPlanes {
   static constexpr int YW = TX + 2, YH = TY + 3;  // y faces j0-1 .. j0+TY+1, columns i0-1 .. i0+TX
   static constexpr int XN = XW * XH, YN = YW * YH, SN = SW * SH;
 };
-constexpr int PD_RING = 3;   // levels L .. L+2 in flight
-constexpr int PD_NPL = 6;    // q and q_old of both species of the pair, ru_m, rv_m
+constexpr int PD_RING = 2;   // levels L, L+1 in flight
+// q and q_old of both species of the pair, ru_m, rv_m, and the x and y faces'
+// Courant numbers and low-order flux factors (k_pd_courant)
+constexpr int PD_NPL = 10;
 constexpr int PD_FSLOT = 3;  // face planes kept for three levels
 // face planes (float2: both species), limiter factors (float2), mbarriers
 constexpr size_t PD_SMEM = (size_t)PD_RING * PD_NPL * HPLANE_BYTES +
@@ -363,7 +365,9 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   const CUtensorMap* maps[PD_NPL] = {tmap_of(m, m.qmap[s0], BOX_HALO), tmap_of(m, m.qmap[s1], BOX_HALO),
                                      tmap_of(m, WRFGPU_N3D + 3 * s0 + 1, BOX_HALO),
                                      tmap_of(m, WRFGPU_N3D + 3 * s1 + 1, BOX_HALO),
-                                     tmap_of(m, WRFGPU_RU_M, BOX_HALO), tmap_of(m, WRFGPU_RV_M, BOX_HALO)};
+                                     tmap_of(m, WRFGPU_RU_M, BOX_HALO), tmap_of(m, WRFGPU_RV_M, BOX_HALO),
+                                     tmap_of(m, PDC_SLOT + 0, BOX_HALO), tmap_of(m, PDC_SLOT + 3, BOX_HALO),
+                                     tmap_of(m, PDC_SLOT + 1, BOX_HALO), tmap_of(m, PDC_SLOT + 4, BOX_HALO)};
   const int x0 = i0 - TMA_HALO - m.ims, z0 = j0 - TMA_HALO - m.jms;
   if (tid == 0) {
     for (int q = 0; q < PD_RING; ++q) mbar_init(&ring.bar[q], 1);
@@ -375,8 +379,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
 
   const F3 fa = f3p(m, m.q[s0]), fb = f3p(m, m.q[s1]), foa = f3p(m, m.qo[s0]), fob = f3p(m, m.qo[s1]);
   const F3 outa = f3p(m, m.qa[s0]), outb = f3p(m, m.qa[s1]), rom = f3(m, WRFGPU_WW_M);
-  const F3 crxa = f3p(m, m.pdc[0]), crya = f3p(m, m.pdc[1]), crza = f3p(m, m.pdc[2]);
-  const F3 lfxa = f3p(m, m.pdc[3]), lfya = f3p(m, m.pdc[4]), lfza = f3p(m, m.pdc[5]);
+  const F3 crza = f3p(m, m.pdc[2]), lfza = f3p(m, m.pdc[5]);
   F2 mut2 = f2(m, WRFGPU_MUTS), msx2 = f2(m, WRFGPU_MSFTX), msy2 = f2(m, WRFGPU_MSFTY);
   F2 mub2 = f2(m, WRFGPU_MUB), mu1 = f2(m, WRFGPU_MU_1), mu2 = f2(m, WRFGPU_MU_2);
   {
@@ -406,19 +409,17 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   // level-independent data of the faces: the face's point and its offset in
   // the halo plane
   bool xok = false, yok = false;
-  int xo = 0, yo = 0, xii = 0, xjj = 0, yii = 0, yjj = 0;
+  int xo = 0, yo = 0;
   if (xq >= 0) {
     const int r = xq / P::XW, c = xq - r * P::XW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     xok = ii >= m.its - 1 && ii <= itf + 2 && jj >= m.jts - 1 && jj <= jtf + 1;
-    xii = ii; xjj = jj;
     xo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);  // (i0-1+c, j0-1+r) in the halo plane
   }
   if (yq >= 0) {
     const int r = yq / P::YW, c = yq - r * P::YW;
     const int ii = i0 - 1 + c, jj = j0 - 1 + r;
     yok = ii >= m.its - 1 && ii <= itf + 1 && jj >= m.jts - 1 && jj <= jtf + 2;
-    yii = ii; yjj = jj;
     yo = (r + TMA_HALO - 1) * HW + (c + TMA_HALO - 1);
   }
 
@@ -455,6 +456,15 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   const int so = sy * P::SW + sx;                // own cell in the factor planes
   const int xoc = sy * P::XW + sx, yoc = sy * P::YW + sx;  // own cell's left / bottom faces
   bool ok = true;
+  // the own cell's z face Courant number and low-order factor of the next
+  // level, loaded one iteration ahead
+  auto zcourant = [&](int lv, float* cr, float* lf) {
+    const bool zin = c.valid && lv <= ktf && lv + 1 > 1 && lv + 1 < m.kde;
+    *cr = zin ? crza.ro(c.i, lv + 1, c.j) : 0.f;
+    *lf = zin ? lfza.ro(c.i, lv + 1, c.j) : 0.f;
+  };
+  float crz_n, lfz_n;
+  zcourant(kts, &crz_n, &lfz_n);
 
   // One barrier per level.  Iteration Lv: faces of level Lv (face slot Lv % 3)
   // and the z face Lv+1 of the own cell; barrier; limiter factor of level Lv
@@ -470,12 +480,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     const int slot = Lv & 1;
     float c1k = 0.f, c2k = 0.f, rdzwk = 0.f;
     if (Lv <= ktf) {
-      // this thread's faces' Courant numbers (k_pd_courant), loaded before
-      // the ring wait so that their latency overlaps it
-      const float crx = xok ? crxa.ro(xii, Lv, xjj) : 0.f, lfx = xok ? lfxa.ro(xii, Lv, xjj) : 0.f;
-      const float cry = yok ? crya.ro(yii, Lv, yjj) : 0.f, lfy = yok ? lfya.ro(yii, Lv, yjj) : 0.f;
-      const bool zin = c.valid && Lv + 1 > 1 && Lv + 1 < m.kde;
-      const float crz = zin ? crza.ro(c.i, Lv + 1, c.j) : 0.f, lfz = zin ? lfza.ro(c.i, Lv + 1, c.j) : 0.f;
+      const float crz = crz_n, lfz = lfz_n;
       if (tid == 0 && Lv + PD_RING - 1 <= ktf) ring.issue(Lv + PD_RING - 1, maps, x0, z0, m.kms);
       const float4 tl = sLV[Lv - m.kms].a;
       c1k = tl.x; c2k = tl.y; rdzwk = tl.z;
@@ -487,6 +492,10 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
       const float* FOB = ring.plane(rs, 3);
       const float* RU = ring.plane(rs, 4);
       const float* RV = ring.plane(rs, 5);
+      const float* CRX = ring.plane(rs, 6);
+      const float* LFX = ring.plane(rs, 7);
+      const float* CRY = ring.plane(rs, 8);
+      const float* LFY = ring.plane(rs, 9);
       auto q2 = [&](int o) { return make_float2(FA[o], FB[o]); };
       auto qo2 = [&](int o) { return make_float2(FOA[o], FOB[o]); };
       const int fs = Lv % PD_FSLOT;
@@ -498,7 +507,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         if (xok) {
           const int o = xo;
           const float vel = RU[o];
-          lo = muls(lfx, flux_upwind_2(qo2(o - 1), qo2(o), upwind_weights(crx)));
+          lo = muls(LFX[o], flux_upwind_2(qo2(o - 1), qo2(o), upwind_weights(CRX[o])));
           const float2 h = muls(vel, pflux5_2(q2(o - 3), q2(o - 2), q2(o - 1), q2(o), q2(o + 1), q2(o + 2), vel));
           hi = sub2(h, lo);
         }
@@ -509,7 +518,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
         if (yok) {
           const int o = yo;
           const float vel = RV[o];
-          lo = muls(lfy, flux_upwind_2(qo2(o - HW), qo2(o), upwind_weights(cry)));
+          lo = muls(LFY[o], flux_upwind_2(qo2(o - HW), qo2(o), upwind_weights(CRY[o])));
           const float2 h =
               muls(vel, pflux5_2(q2(o - 3 * HW), q2(o - 2 * HW), q2(o - HW), q2(o), q2(o + HW), q2(o + 2 * HW), vel));
           hi = sub2(h, lo);
@@ -595,6 +604,7 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
     }
     // ---- slide the windows to level Lv+1 (loads for the next level issued now)
     sc_m1 = sc_0; sc_0 = sc_p1;
+    zcourant(Lv + 1, &crz_n, &lfz_n);
     if (c.valid) {
       c.hzm = c.hz0; c.lzm = c.lz0;
       c.hz0 = c.hz1; c.lz0 = c.lz1;

@@ -395,8 +395,15 @@ __global__ void __launch_bounds__(PD_THREADS, MINB) k_scalar_pd_update(TileLaunc
   auto ld2 = [](const F3& a, const F3& b, int i, int k, int j) { return make_float2(a(i, k, j), b(i, k, j)); };
 
   // this thread's limiter cell (sx, sy) of the region, and its faces
+  // cells 0..31 of each row on one warp (contiguous shared-memory rows, no
+  // bank conflicts), the rows' last two cells on the next 20 threads
+  static_assert(P::SW == 34 && 32 * P::SH < P::SN, "thread map assumes 32-wide tiles");
   const bool has_cell = tid < P::SN;
-  const int sx = has_cell ? tid % P::SW : 0, sy = has_cell ? tid / P::SW : 0;
+  int sx = 0, sy = 0;
+  if (has_cell) {
+    if (tid < 32 * P::SH) { sy = tid >> 5; sx = tid & 31; }
+    else { const int q = tid - 32 * P::SH; sy = q >> 1; sx = 32 + (q & 1); }
+  }
   int xq = -1, yq = -1;  // x / y face this thread computes (index in the face planes)
   if (has_cell) {
     xq = sy * P::XW + sx;  // left face of the cell

@@ -832,6 +832,28 @@ def explicit_case(variant):
     return case
 
 
+def test_full_step_bitwise_explicit_diffusion_symmetric_y(gpulib):
+    """diff_opt = 1 with mirrored y boundaries: the diffusion stencils read
+    the symmetric halo rows (v changes sign across the boundary); every
+    state field and species after two steps bit for bit the oracle's."""
+    case = cases.small_case(nx=16, ny=12, kde=16, n_scalar=2, seed=17)
+    c = case.desc.config
+    c.periodic_y = 0
+    c.symmetric_ys = 1
+    c.symmetric_ye = 1
+    c.diff_opt = 1
+    c.km_opt = 1
+    c.khdif = 1500.0
+    c.kvdif = 40.0
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(2)
+    ge.step(2)
+    ge.sync()
+    bad = _bitwise_diffs(case, ge, od, old_too=False)
+    assert not bad, "\n".join(bad)
+
+
 @pytest.mark.parametrize("variant", ["alone", "with_diff6", "mix2_off"])
 def test_full_step_bitwise_explicit_diffusion(gpulib, variant):
     """diff_opt = 1 (module_em.F:801-877 in rk_tendency's forward step and

@@ -109,3 +109,28 @@ def test_step_host_separate_in_out_and_refusals(gpulib):
         dom.bind_host_state(0, [fids[0]], [_pinned(10)])
     with pytest.raises(G.WrfGpuError):
         dom.bind_host_state(0, [9999], [_pinned(10)])
+
+
+def test_step_host_two_members_of_an_ensemble(gpulib):
+    """Both members of an uneven two-member ensemble bound (their fields
+    interleaved in the binding order): each member's outputs after two
+    steps of one call equal its own plain loop's."""
+    members = [cases.small_case(nx=24, ny=12, kde=14, n_scalar=2, seed=12),
+               cases.small_case(nx=16, ny=20, kde=18, n_scalar=1, seed=13)]
+    ens = G.Ensemble.from_cases(members)
+    bufs = {}
+    for m, cs in enumerate(members):
+        for f in _fids(cs):
+            b = _pinned(ens.field_size(m, f))
+            b[:] = np.asarray(ens.get(m, f), dtype=np.float32)
+            bufs[(m, f)] = b
+    for m, cs in enumerate(members):
+        fids = _fids(cs)
+        ens.bind_host_state(m, fids, [bufs[(m, f)] for f in fids])
+    ens.step_host(2)
+    for m, cs in enumerate(members):
+        ref = G.Domain(cs)
+        ref.step(2)
+        ref.sync()
+        for f in _fids(cs):
+            assert np.array_equal(bufs[(m, f)], np.asarray(ref.get(0, f), dtype=np.float32)), (m, f)

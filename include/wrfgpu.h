@@ -108,6 +108,11 @@ enum WrfGpuFieldId {
   WRFGPU_RU_M, WRFGPU_RV_M, WRFGPU_WW_M, WRFGPU_ADVECT_TEND, WRFGPU_H_DIABATIC,
   WRFGPU_T_INIT,  /* base-state theta perturbation (module_initialize_ideal.F:973): explicit diffusion of theta */
   WRFGPU_N3D,
+  /* rk_tendency's stored forward tendencies ru_tendf, rv_tendf, rw_tendf,
+   * t_tendf (3-D): present only in members that use diff_opt = 1,
+   * diff_6th_opt != 0 or damp_opt = 2 */
+  WRFGPU_TENDF_BASE = 90,
+  WRFGPU_RU_TENDF = WRFGPU_TENDF_BASE, WRFGPU_RV_TENDF, WRFGPU_RW_TENDF, WRFGPU_T_TENDF,
   /* 2-D (ims:ime, jms:jme) */
   WRFGPU_F2D_BASE = 100,
   WRFGPU_MU_1 = WRFGPU_F2D_BASE, WRFGPU_MU_2, WRFGPU_MUB, WRFGPU_MUT, WRFGPU_MUU, WRFGPU_MUV,

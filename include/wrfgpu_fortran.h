@@ -60,8 +60,8 @@ int wrfgpu_rk_step_prep(const WrfDynConfig *config_flags, const int *rk_step, co
  * h_diabatic, base-state, diffusion and damping arguments are read as zero /
  * unused; wwE, wwI are ww (IEVA off)). */
 int wrfgpu_rk_tendency(const WrfDynConfig *config_flags, const int *rk_step, float *ru_tend, float *rv_tend,
-                       float *rw_tend, float *ph_tend, float *t_tend, const float *ru_tendf, const float *rv_tendf,
-                       const float *rw_tendf, const float *ph_tendf, const float *t_tendf, float *mu_tend,
+                       float *rw_tend, float *ph_tend, float *t_tend, float *ru_tendf, float *rv_tendf,
+                       float *rw_tendf, const float *ph_tendf, float *t_tendf, float *mu_tend,
                        float *u_save, float *v_save, float *w_save, float *ph_save, float *t_save, float *mu_save,
                        const float *RTHFTEN, const float *ru, const float *rv, const float *rw, const float *ww,
                        const float *wwE, const float *wwI, const float *u, const float *v, const float *w,

@@ -172,6 +172,10 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
                        p1(WRFGPU_C2H), p2(WRFGPU_MU_1), p2(WRFGPU_MU_2), p2(WRFGPU_MUB), rk_step, dt_rk,
                        p3(WRFGPU_H_DIABATIC), td);
       return 0;
+    case ORACLE_R_FORWARD_TERMS:
+      if (D.tendf.empty()) return -1;
+      D.forward_terms(D.tendf[0].data(), D.tendf[1].data(), D.tendf[2].data(), D.tendf[3].data(), R(D.sc.dt), td);
+      return 0;
     case ORACLE_R_SIXTH_DIFF_SPECIES:
       // rk_scalar_tend's stage-1 diffusion of species `species` into the
       // H_DIABATIC buffer (module_em.F:1378-1435): explicit (diff_opt = 1,

@@ -34,6 +34,9 @@ enum {
    * scalar_tends) carried in the H_DIABATIC field, mu_new in MU_2 */
   ORACLE_R_UPDATE_SCALAR_PD_ARGS = 30,
   ORACLE_R_UPDATE_SCALAR_ARGS = 31,
-  ORACLE_R_SIXTH_DIFF_SPECIES = 32
+  ORACLE_R_SIXTH_DIFF_SPECIES = 32,
+  /* rk_tendency's stage-1 forward terms added to the *_tendf fields
+   * (WRFGPU_RU_TENDF ..), with the large step dt */
+  ORACLE_R_FORWARD_TERMS = 33
 };
 #endif

@@ -144,6 +144,9 @@ struct Domain {
     if (id >= WRFGPU_SPECIES_BASE && id < WRFGPU_SPECIES_BASE + 2 * (n_moist + n_scalar)) {
       *n = n3; return qs[id - WRFGPU_SPECIES_BASE].data();
     }
+    if (id >= WRFGPU_RU_TENDF && id <= WRFGPU_T_TENDF && !tendf.empty()) {
+      *n = n3; return tendf[id - WRFGPU_RU_TENDF].data();
+    }
     *n = 0; return nullptr;
   }
 
@@ -168,6 +171,62 @@ struct Domain {
     if (cf.time_step_sound != 0) return cf.time_step_sound;
     R spacing = std::min(R(sc.dx), R(sc.dy));
     return std::max(2 * ((int)(R(300.) * R(sc.dt) / spacing - R(0.01)) + 1), 4);
+  }
+
+  // rk_tendency's forward step at stage 1 (module_em.F:801-944): the explicit
+  // diffusion (diff_opt = 1, km_opt = 1), the sixth-order diffusion and the
+  // Rayleigh damping (damp_opt = 2) of the stage-1 state added to ru_tendf,
+  // rv_tendf, rw_tendf and t_tendf (t0 .. t3) over tile td, dt the large step.
+  void forward_terms(R* t0, R* t1, R* t2, R* t3, R dt, const Dims& td) {
+    const bool diff1 = cf.diff_opt == 1, diff6 = cf.diff_6th_opt != 0, damp2 = cf.damp_opt == 2;
+    const R rdx = R(sc.rdx), rdy = R(sc.rdy);
+    if (diff1) {
+      // module_em.F:801-877: explicit diffusion with the constant coefficients
+      // of km_opt = 1 (xkmh = khdif, xkhh = khdif / prandtl; theta's vertical
+      // coefficient 3 kvdif)
+      const R khdif = (R)cf.khdif, kvdif = (R)cf.kvdif, prandtl = R(1.) / R(3.0);
+      const R xkmh = khdif, xkhh = khdif / prandtl;
+      horizontal_diffusion('u', p3(WRFGPU_U_2), t0, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                           p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
+                           p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
+      horizontal_diffusion('v', p3(WRFGPU_V_2), t1, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                           p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
+                           p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
+      horizontal_diffusion('w', p3(WRFGPU_W_2), t2, p2(WRFGPU_MUT), p1(WRFGPU_C1F), p1(WRFGPU_C2F),
+                           p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
+                           p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
+      horizontal_diffusion_3dmp(p3(WRFGPU_T_2), t3, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                                p3(WRFGPU_T_INIT), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX_INV),
+                                p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkhh, rdx, rdy, td);
+      vertical_diffusion('u', p3(WRFGPU_U_2), t0, p1(WRFGPU_U_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+                         p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUU), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
+      vertical_diffusion('v', p3(WRFGPU_V_2), t1, p1(WRFGPU_V_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+                         p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUV), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
+      vertical_diffusion('w', p3(WRFGPU_W_2), t2, (R*)nullptr, (R*)nullptr, p1(WRFGPU_C1F),
+                         p1(WRFGPU_C2F), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
+      vertical_diffusion('t', p3(WRFGPU_T_2), t3, (R*)nullptr, p3(WRFGPU_T_INIT), p1(WRFGPU_C1H),
+                         p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW),
+                         R(3.) * kvdif, td);
+    }
+    if (diff6) {
+      // module_em.F:879-932, with the state of stage 1
+      const int fld[4] = {WRFGPU_U_2, WRFGPU_V_2, WRFGPU_W_2, WRFGPU_T_2};
+      const char nm[4] = {'u', 'v', 'w', 'm'};
+      for (int q = 0; q < 4; ++q) {
+        const bool wl = q == 2;  // w sits on full levels
+        R* tt[4] = {t0, t1, t2, t3};
+        sixth_order_diffusion(nm[q], p3(fld[q]), tt[q], p2(WRFGPU_MUT), dt, cf,
+                              p1(wl ? WRFGPU_C1F : WRFGPU_C1H), p1(wl ? WRFGPU_C2F : WRFGPU_C2H), p3(WRFGPU_PHB),
+                              rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY),
+                              p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
+      }
+    }
+    if (damp2)  // module_em.F:933-944
+      rk_rayleigh_damp(t0, t1, t2, t3, p3(WRFGPU_U_2),
+                       p3(WRFGPU_V_2), p3(WRFGPU_W_2), p3(WRFGPU_T_2), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+                       p1(WRFGPU_C1F), p1(WRFGPU_C2F), p2(WRFGPU_MUT), p2(WRFGPU_MUU), p2(WRFGPU_MUV),
+                       p3(WRFGPU_PH_2), p3(WRFGPU_PHB), p1(WRFGPU_U_BASE), p1(WRFGPU_V_BASE), p1(WRFGPU_T_BASE),
+                       p1(WRFGPU_Z_BASE), (R)cf.dampcoef, (R)cf.zdamp, td);
   }
 
   // One large step (solve_em.F:444-4750, physics off).
@@ -273,52 +332,8 @@ struct Domain {
                   p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), cf, p2(WRFGPU_MSFUX),
                   p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
                   (R*)nullptr, p1(WRFGPU_FNM), p1(WRFGPU_FNP), rdx, rdy, td);
-        if (diff1 && rk_step == 1) {
-          // module_em.F:801-877: explicit diffusion with the constant coefficients
-          // of km_opt = 1 (xkmh = khdif, xkhh = khdif / prandtl; theta's vertical
-          // coefficient 3 kvdif)
-          const R khdif = (R)cf.khdif, kvdif = (R)cf.kvdif, prandtl = R(1.) / R(3.0);
-          const R xkmh = khdif, xkhh = khdif / prandtl;
-          horizontal_diffusion('u', p3(WRFGPU_U_2), tendf[0].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
-                               p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
-                               p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
-          horizontal_diffusion('v', p3(WRFGPU_V_2), tendf[1].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
-                               p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
-                               p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
-          horizontal_diffusion('w', p3(WRFGPU_W_2), tendf[2].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1F), p1(WRFGPU_C2F),
-                               p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
-                               p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
-          horizontal_diffusion_3dmp(p3(WRFGPU_T_2), tendf[3].data(), p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
-                                    p3(WRFGPU_T_INIT), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX_INV),
-                                    p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkhh, rdx, rdy, td);
-          vertical_diffusion('u', p3(WRFGPU_U_2), tendf[0].data(), p1(WRFGPU_U_BASE), (R*)nullptr, p1(WRFGPU_C1H),
-                             p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUU), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
-          vertical_diffusion('v', p3(WRFGPU_V_2), tendf[1].data(), p1(WRFGPU_V_BASE), (R*)nullptr, p1(WRFGPU_C1H),
-                             p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUV), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
-          vertical_diffusion('w', p3(WRFGPU_W_2), tendf[2].data(), (R*)nullptr, (R*)nullptr, p1(WRFGPU_C1F),
-                             p1(WRFGPU_C2F), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
-          vertical_diffusion('t', p3(WRFGPU_T_2), tendf[3].data(), (R*)nullptr, p3(WRFGPU_T_INIT), p1(WRFGPU_C1H),
-                             p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW),
-                             R(3.) * kvdif, td);
-        }
-        if (diff6 && rk_step == 1) {
-          // module_em.F:879-932, with the state of stage 1
-          const int fld[4] = {WRFGPU_U_2, WRFGPU_V_2, WRFGPU_W_2, WRFGPU_T_2};
-          const char nm[4] = {'u', 'v', 'w', 'm'};
-          for (int q = 0; q < 4; ++q) {
-            const bool wl = q == 2;  // w sits on full levels
-            sixth_order_diffusion(nm[q], p3(fld[q]), tendf[q].data(), p2(WRFGPU_MUT), dt, cf,
-                                  p1(wl ? WRFGPU_C1F : WRFGPU_C1H), p1(wl ? WRFGPU_C2F : WRFGPU_C2H), p3(WRFGPU_PHB),
-                                  rdx, rdy, p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY),
-                                  p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVY), td);
-          }
-        }
-        if (damp2 && rk_step == 1)  // module_em.F:933-944
-          rk_rayleigh_damp(tendf[0].data(), tendf[1].data(), tendf[2].data(), tendf[3].data(), p3(WRFGPU_U_2),
-                           p3(WRFGPU_V_2), p3(WRFGPU_W_2), p3(WRFGPU_T_2), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
-                           p1(WRFGPU_C1F), p1(WRFGPU_C2F), p2(WRFGPU_MUT), p2(WRFGPU_MUU), p2(WRFGPU_MUV),
-                           p3(WRFGPU_PH_2), p3(WRFGPU_PHB), p1(WRFGPU_U_BASE), p1(WRFGPU_V_BASE), p1(WRFGPU_T_BASE),
-                           p1(WRFGPU_Z_BASE), (R)cf.dampcoef, (R)cf.zdamp, td);
+        if (rk_step == 1 && (diff1 || diff6 || damp2))
+          forward_terms(tendf[0].data(), tendf[1].data(), tendf[2].data(), tendf[3].data(), dt, td);
       });
       for (int t = 0; t < 64; ++t) { mvc = std::max(mvc, tmv[t]); mhc = std::max(mhc, tmh[t]); }
       if (diff1 || diff6 || damp2)

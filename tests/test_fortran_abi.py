@@ -521,3 +521,110 @@ def test_rk_scalar_tend_abi_explicit_diffusion_bitwise(gpulib, case3x):
     assert not bad, bad
     rc, _ = call(xk * np.float32(2.0))
     assert rc == abi.WRFGPU_E_ARG
+
+
+@pytest.fixture(scope="module")
+def case_fwd():
+    """Explicit and sixth-order diffusion and the Rayleigh damping all on:
+    rk_tendency's stage-1 forward step adds three terms to each *_tendf."""
+    c = cases.small_case(nx=16, ny=12, kde=14, n_scalar=1, seed=31)
+    cf = c.desc.config
+    cf.diff_opt = 1
+    cf.km_opt = 1
+    cf.khdif = 900.0
+    cf.kvdif = 35.0
+    cf.diff_6th_opt = 2
+    cf.diff_6th_factor = 0.12
+    cf.damp_opt = 2
+    cf.dampcoef = 0.01
+    cf.zdamp = 5000.0
+    return c
+
+
+def test_rk_tendency_abi_forward_step_bitwise(gpulib, case_fwd):
+    """wrfgpu_rk_tendency (module_em.F:190) at stage 1 with diff_opt = 1,
+    diff_6th_opt = 2 and damp_opt = 2: the large-step tendencies bit for bit
+    the oracle's rk_tendency, and ru_tendf, rv_tendf, rw_tendf, t_tendf,
+    which arrive holding (physics) tendencies, gain the forward step's
+    explicit diffusion, sixth-order diffusion and Rayleigh damping
+    (:801-944) bit for bit as the oracle adds them; a coefficient array
+    that is not khdif is refused."""
+    case = case_fwd
+    od = _state(case)
+    cf = case.desc.config
+    s = case.desc.scalars
+    n3 = od.get(abi.FIELD_ID["u_2"]).size
+    rng = np.random.Generator(np.random.PCG64(43))
+    tf_names = ["ru_tendf", "rv_tendf", "rw_tendf", "t_tendf"]
+    tf0 = {nm: (1e-3 * rng.standard_normal(n3)).astype(np.float32) for nm in tf_names}
+    xk = np.full(n3, np.float32(cf.khdif), dtype=np.float32)
+
+    def call(xkmhd):
+        a = _Argv()
+        a.cfg(cf); a.i32(1)
+        outs = {}
+        for nm in ("ru_tend", "rv_tend", "rw_tend", "ph_tend", "t_tend"):
+            outs[nm] = a.arr(np.zeros(n3, np.float32))
+        for nm in ("ru_tendf", "rv_tendf", "rw_tendf"):
+            outs[nm] = a.arr(tf0[nm].copy())
+        a.arr(np.zeros(n3, np.float32))                    # ph_tendf
+        outs["t_tendf"] = a.arr(tf0["t_tendf"].copy())
+        outs["mu_tend"] = a.arr(np.zeros(od.get(abi.FIELD_ID["mu_2"]).size, np.float32))
+        for nm in ("u_save", "v_save", "w_save", "ph_save", "t_save"):
+            outs[nm] = a.arr(np.zeros(n3, np.float32))
+        outs["mu_save"] = a.arr(np.zeros(od.get(abi.FIELD_ID["mu_2"]).size, np.float32))
+        a.null()                                            # RTHFTEN
+        for nm in ("ru", "rv", "rw", "ww", "ww"):
+            a.arr(_f(od, nm))
+        a.arr(_f(od, "ww"))                                 # wwI
+        for nm in ("u_2", "v_2", "w_2", "t_2", "ph_2"):
+            a.arr(_f(od, nm))
+        for _ in range(5):
+            a.null()                                        # u_old .. ph_old
+        a.null()                                            # h_diabatic
+        for nm in ("phb", "t_init"):
+            a.arr(_f(od, nm))
+        a.null()                                            # mu_old
+        for nm in ("mu_2", "mut", "muu", "muv", "mub", "c1h", "c2h", "c1f", "c2f", "al", "ht", "alt", "p", "pb",
+                   "php", "cqu", "cqv"):
+            a.arr(_f(od, nm))
+        outs["cqw"] = a.arr(_f(od, "cqw"))
+        for nm in ("u_base", "v_base", "t_base", "qv_base", "z_base", "msfux", "msfuy", "msfvx", "msfvx_inv",
+                   "msfvy", "msftx", "msfty"):
+            a.arr(_f(od, nm))
+        a.null()                                            # clat
+        for nm in ("f", "e", "sina", "cosa", "fnm", "fnp", "rdn", "rdnw"):
+            a.arr(_f(od, nm))
+        a.f32(s.dt); a.f32(np.float32(s.rdx)); a.f32(np.float32(s.rdy))
+        a.f32(cf.khdif); a.f32(cf.kvdif); a.arr(xkmhd); a.null()   # khdif, kvdif, xkmhd, xkhh
+        a.i32(cf.diff_6th_opt); a.f32(cf.diff_6th_factor); a.i32(1)
+        a.f32(cf.dampcoef); a.f32(cf.zdamp); a.i32(cf.damp_opt); a.i32(0)
+        for v in (s.cf1, s.cf2, s.cf3, s.cfn, s.cfn1):
+            a.f32(np.float32(v))
+        a.i32(1); a.i32(1); a.i32(0); a.f32(0.0); a.f32(0.0)
+        a.dims(case)
+        a.null(); a.null()                                  # max_vert_cfl, max_horiz_cfl
+        return a.call(gpulib, "wrfgpu_rk_tendency"), outs
+
+    rc, outs = call(xk)
+    assert rc == 0
+    bad = []
+    for nm, v in tf0.items():
+        od.set(abi.FIELD_ID[nm], v)
+    od.run("forward_terms", 1)
+    for nm in tf_names:
+        fid = abi.FIELD_ID[nm]
+        d = max_abs(interior(case, fid, outs[nm], halo=0), interior(case, fid, od.get(fid), halo=0))
+        if d != 0.0:
+            bad.append("%s: max|diff| %.3e" % (nm, d))
+        if np.array_equal(outs[nm], tf0[nm]):
+            bad.append("%s unchanged" % nm)
+    od.run("rk_tendency", 1)
+    for nm in ("ru_tend", "rv_tend", "rw_tend", "ph_tend", "t_tend"):
+        fid = abi.FIELD_ID[nm]
+        d = max_abs(interior(case, fid, outs[nm], halo=0), interior(case, fid, od.get(fid), halo=0))
+        if d != 0.0:
+            bad.append("%s: max|diff| %.3e" % (nm, d))
+    assert not bad, bad
+    rc, _ = call(xk * np.float32(2.0))
+    assert rc == abi.WRFGPU_E_ARG

@@ -72,6 +72,8 @@ F2D = ["mu_1", "mu_2", "mub", "mut", "muu", "muv", "muts", "muus", "muvs", "mudf
        "msftx", "msfty", "ht", "f", "e", "sina", "cosa"]
 F1D = ["znw", "znu", "dnw", "rdnw", "dn", "rdn", "fnm", "fnp", "c1h", "c2h", "c1f", "c2f",
        "c3h", "c4h", "c3f", "c4f", "u_base", "v_base", "t_base", "z_base", "qv_base"]
+TENDF = ["ru_tendf", "rv_tendf", "rw_tendf", "t_tendf"]
+TENDF_BASE = 90
 F2D_BASE = 100
 F1D_BASE = 200
 SPECIES_BASE = 300
@@ -83,6 +85,8 @@ for _i, _n in enumerate(F2D):
     FIELD_ID[_n] = F2D_BASE + _i
 for _i, _n in enumerate(F1D):
     FIELD_ID[_n] = F1D_BASE + _i
+for _i, _n in enumerate(TENDF):
+    FIELD_ID[_n] = TENDF_BASE + _i
 
 
 def species_id(s, old=False):
@@ -91,7 +95,7 @@ def species_id(s, old=False):
 
 
 def field_kind(fid):
-    if 0 <= fid < len(F3D) or fid >= SPECIES_BASE:
+    if 0 <= fid < len(F3D) or fid >= SPECIES_BASE or TENDF_BASE <= fid < TENDF_BASE + len(TENDF):
         return 3
     if F2D_BASE <= fid < F2D_BASE + len(F2D):
         return 2
@@ -111,6 +115,8 @@ ROUTINES = {
     "calc_p_rho_phi": 24, "set_w_surface": 25, "rk_tendency": 26,
     # oracle-only forms checked against the routine-level C entry points
     "rk_update_scalar_pd_args": 30, "rk_update_scalar_args": 31, "sixth_diff_species": 32,
+    # rk_tendency's stage-1 forward terms (diffusion, damping) added to the *_tendf fields
+    "forward_terms": 33,
 }
 
 

@@ -613,6 +613,9 @@ struct Ensemble {
     if (id >= 0 && id < WRFGPU_N3D) { p = M.f3[id]; c = ni_[m]; r = nk_[m] * nj_[m]; pt = pitch_[m]; }
     else if (id >= WRFGPU_F2D_BASE && id < WRFGPU_F2D_END) { p = M.f2[id - WRFGPU_F2D_BASE]; c = ni_[m]; r = nj_[m]; pt = pitch_[m]; }
     else if (id >= WRFGPU_F1D_BASE && id < WRFGPU_F1D_END) { p = M.f1[id - WRFGPU_F1D_BASE]; c = nk_[m]; r = 1; pt = c; }
+    else if (id >= WRFGPU_RU_TENDF && id <= WRFGPU_T_TENDF && M.tendf[id - WRFGPU_RU_TENDF]) {  // when allocated
+      p = M.tendf[id - WRFGPU_RU_TENDF]; c = ni_[m]; r = nk_[m] * nj_[m]; pt = pitch_[m];
+    }
     else if (id >= WRFGPU_SPECIES_BASE && id < WRFGPU_SPECIES_BASE + 2 * M.nsp) {
       int s = (id - WRFGPU_SPECIES_BASE) / 2, old = (id - WRFGPU_SPECIES_BASE) % 2;
       p = old ? M.qo[s] : M.q[s]; c = ni_[m]; r = nk_[m] * nj_[m]; pt = pitch_[m];
@@ -874,6 +877,8 @@ struct Ensemble {
       case 130: launch_update_scalar_routine(l3, nb3, rk_step, 0, stream); break;
       case 131: launch_update_scalar_routine(l3, nb3, rk_step, 1, stream); break;
       case 132: launch_species_diff_routine(l3, nb3, iteration, stream); break;
+      // rk_tendency's forward terms at stage 1 added to the caller's *_tendf
+      case 133: launch_forward_diff(l3, nb3, 2, stream); launch_rayleigh_damp(l2, nb2, stream, true); break;
       case 24: launch_calc_p_rho_phi(l3, nb3, stream); break;
       case 25: launch_set_w_surface(l2, nb2, stream); break;
       case 26:
@@ -933,8 +938,9 @@ int fortran_call(const FCall& c) {
   if (c.nsp < 1 || c.nsp > NSPMAX) return WRFGPU_E_ARG;
   std::lock_guard<std::mutex> lock(g_fmu);
   // the diffusions' stored tendencies are allocated with the domain
-  const int diff6 = c.cfg.diff_6th_opt != 0 || c.cfg.diff_opt == 1 ? 1 : 0;
-  const auto key = std::make_tuple(ide, jde, kde, c.nsp, diff6);
+  const bool sct = c.cfg.diff_6th_opt != 0 || c.cfg.diff_opt == 1;
+  const int bufs = (sct || c.cfg.damp_opt == 2 ? 1 : 0) | (sct ? 2 : 0);  // tendf, sc_tend
+  const auto key = std::make_tuple(ide, jde, kde, c.nsp, bufs);
   Ensemble* e = nullptr;
   auto it = g_fcache.find(key);
   if (it != g_fcache.end()) e = it->second;

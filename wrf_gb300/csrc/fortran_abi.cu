@@ -63,8 +63,8 @@ int wrfgpu_rk_step_prep(const WrfDynConfig* config_flags, const int* rk_step, co
 }
 
 int wrfgpu_rk_tendency(const WrfDynConfig* config_flags, const int* rk_step, float* ru_tend, float* rv_tend,
-                       float* rw_tend, float* ph_tend, float* t_tend, const float* ru_tendf, const float* rv_tendf,
-                       const float* rw_tendf, const float* ph_tendf, const float* t_tendf, float* mu_tend,
+                       float* rw_tend, float* ph_tend, float* t_tend, float* ru_tendf, float* rv_tendf,
+                       float* rw_tendf, const float* ph_tendf, float* t_tendf, float* mu_tend,
                        float* u_save, float* v_save, float* w_save, float* ph_save, float* t_save, float* mu_save,
                        const float* RTHFTEN, const float* ru, const float* rv, const float* rw, const float* ww,
                        const float* wwE, const float* wwI, const float* u, const float* v, const float* w,
@@ -88,14 +88,33 @@ int wrfgpu_rk_tendency(const WrfDynConfig* config_flags, const int* rk_step, flo
                        WRFGPU_DIMS_ARGS, float* max_vert_cfl, float* max_horiz_cfl) {
   if (cfg_ok(config_flags) || !rk_step || !dt || !rdx || !rdy || !cf1 || !cf2 || !cf3 || !cfn || !cfn1)
     return WRFGPU_E_ARG;
-  // physics, diffusion, damping and IEVA inputs of the reference's signature
-  // are zero / off on this path
-  (void)ru_tendf; (void)rv_tendf; (void)rw_tendf; (void)ph_tendf; (void)t_tendf; (void)RTHFTEN; (void)wwE;
-  (void)wwI; (void)u_old; (void)v_old; (void)w_old; (void)t_old; (void)ph_old; (void)h_diabatic; (void)t_init;
-  (void)mu_old; (void)ht; (void)u_base; (void)v_base; (void)t_base; (void)qv_base; (void)z_base; (void)clat;
-  (void)khdif; (void)kvdif; (void)xkmhd; (void)xkhh; (void)diff_6th_opt; (void)diff_6th_factor; (void)adv_opt;
-  (void)dampcoef; (void)zdamp; (void)damp_opt; (void)rad_nudge; (void)n_moist; (void)non_hydrostatic;
-  (void)top_lid; (void)u_frame; (void)v_frame;
+  // physics and IEVA inputs of the reference's signature are zero / off on
+  // this path; the diffusion and damping inputs feed the forward step below
+  (void)ph_tendf; (void)RTHFTEN; (void)wwE; (void)wwI; (void)u_old; (void)v_old; (void)w_old; (void)t_old;
+  (void)ph_old; (void)h_diabatic; (void)mu_old; (void)ht; (void)qv_base; (void)clat; (void)adv_opt;
+  (void)rad_nudge; (void)n_moist; (void)non_hydrostatic; (void)top_lid; (void)u_frame; (void)v_frame;
+  // the forward step's options (module_em.F:801-944): the arguments of the
+  // reference's call where given, else the configuration's
+  WrfDynConfig fcf = *config_flags;
+  if (diff_6th_opt) fcf.diff_6th_opt = *diff_6th_opt;
+  if (diff_6th_factor) fcf.diff_6th_factor = *diff_6th_factor;
+  if (damp_opt) fcf.damp_opt = *damp_opt;
+  if (dampcoef) fcf.dampcoef = *dampcoef;
+  if (zdamp) fcf.zdamp = *zdamp;
+  if (khdif) fcf.khdif = *khdif;
+  if (kvdif) fcf.kvdif = *kvdif;
+  const bool fwd = *rk_step == 1 && (fcf.diff_opt == 1 || fcf.diff_6th_opt != 0 || fcf.damp_opt == 2);
+  if (fwd) {
+    if (!ru_tendf || !rv_tendf || !rw_tendf || !t_tendf || !phb || !ph || !mut || !muu || !muv) return WRFGPU_E_ARG;
+    if (fcf.diff_opt == 1) {
+      if (!t_init || !alt || !rdn || !rdnw || !u_base || !v_base) return WRFGPU_E_ARG;
+      // km_opt = 1 (isotropic_km): the coefficient arrays hold khdif and khdif / prandtl
+      const size_t o0 = (size_t)(*its - *ims) +
+                        (size_t)(*ime - *ims + 1) * ((size_t)(*kts - *kms) + (size_t)(*kme - *kms + 1) * (size_t)(*jts - *jms));
+      if ((xkmhd && xkmhd[o0] != fcf.khdif) || (xkhh && xkhh[o0] != fcf.khdif / (1.f / 3.0f))) return WRFGPU_E_ARG;
+    }
+    if (fcf.damp_opt == 2 && (!u_base || !v_base || !t_base || !z_base)) return WRFGPU_E_ARG;
+  }
   FCall c;
   set_dims(c, DIMS);
   c.cfg = *config_flags; c.routine = WRFGPU_R_RK_TENDENCY; c.rk_step = *rk_step;
@@ -118,7 +137,28 @@ int wrfgpu_rk_tendency(const WrfDynConfig* config_flags, const int* rk_step, flo
   R(WRFGPU_MSFVY, msfvy); R(WRFGPU_MSFTX, msftx); R(WRFGPU_MSFTY, msfty);
   R(WRFGPU_F, f); R(WRFGPU_E, e); R(WRFGPU_SINA, sina); R(WRFGPU_COSA, cosa);
   R(WRFGPU_FNM, fnm); R(WRFGPU_FNP, fnp); R(WRFGPU_RDN, rdn); R(WRFGPU_RDNW, rdnw);
-  return wrfgpu::fortran_call(c);
+  int rc = wrfgpu::fortran_call(c);
+  if (rc || !fwd) return rc;
+  // stage 1's forward terms added to ru_tendf .. t_tendf (rk_addtend_dry,
+  // a separate call of solve_em, adds those to the large-step tendencies)
+  FCall d;
+  set_dims(d, DIMS);
+  d.cfg = fcf; d.routine = 133; d.rk_step = 1;
+  d.dt = *dt; d.rdx = *rdx; d.rdy = *rdy;
+  {
+    FCall& c = d;  // the binding macros name the call `c`
+    RW(WRFGPU_RU_TENDF, ru_tendf); RW(WRFGPU_RV_TENDF, rv_tendf); RW(WRFGPU_RW_TENDF, rw_tendf);
+    RW(WRFGPU_T_TENDF, t_tendf);
+    R(WRFGPU_U_2, u); R(WRFGPU_V_2, v); R(WRFGPU_W_2, w); R(WRFGPU_T_2, t); R(WRFGPU_PH_2, ph);
+    R(WRFGPU_PHB, phb); R(WRFGPU_T_INIT, t_init); R(WRFGPU_ALT, alt);
+    R(WRFGPU_MUT, mut); R(WRFGPU_MUU, muu); R(WRFGPU_MUV, muv);
+    bind_coefs(c, c1h, c2h, c1f, c2f);
+    R(WRFGPU_MSFUX, msfux); R(WRFGPU_MSFUY, msfuy); R(WRFGPU_MSFVX, msfvx); R(WRFGPU_MSFVX_INV, msfvx_inv);
+    R(WRFGPU_MSFVY, msfvy); R(WRFGPU_MSFTX, msftx); R(WRFGPU_MSFTY, msfty);
+    R(WRFGPU_RDN, rdn); R(WRFGPU_RDNW, rdnw);
+    R(WRFGPU_U_BASE, u_base); R(WRFGPU_V_BASE, v_base); R(WRFGPU_T_BASE, t_base); R(WRFGPU_Z_BASE, z_base);
+  }
+  return wrfgpu::fortran_call(d);
 }
 
 // advect_u / advect_v / advect_w / advect_scalar: tendency += -div(flux)

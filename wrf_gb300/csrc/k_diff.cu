@@ -267,7 +267,9 @@ __device__ float vdiff_point(const Mem& m, const F3& f, const F1& b1, const F3* 
 // kvdif / prandtl and the stage's dt (dt / 3); qv (species 0) diffuses
 // vertically against its base profile qv_base.  Loop limits of periodic /
 // symmetric boundaries (:2760-2790, :3100-3130, :6330-6443); points outside
-// them keep the zero the buffers were created with.
+// them keep the zero the buffers were created with.  Mode 2 is mode 0 added
+// onto the stored tendencies' values (the routine-level rk_tendency, whose
+// *_tendf arrays arrive holding the physics tendencies).
 __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
@@ -304,9 +306,10 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
   const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * m.dt);
   const float xkmh = m.cf.khdif, xkhh = m.cf.khdif / PRANDTL, kvdif = m.cf.kvdif;
   const F2 mut = f2(m, WRFGPU_MUT);
+  const bool acc = mode == 2;  // onto the stored values (the routine-level form: physics tendencies)
   if (i <= m.ite && j <= j_end) {
     const F3 u = f3(m, WRFGPU_U_2);
-    float t = 0.f;
+    float t = acc ? f3p(m, m.tendf[0])(i, k, j) : 0.f;
     if (d1) {
       t = t + hdiff_point<DV_U>(m, u, nullptr, mut, c1, c2, i, k, j, xkmh);
       if (k <= ktf - 1)
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
   }
   if (i <= i_end && j <= m.jte) {
     const F3 v = f3(m, WRFGPU_V_2);
-    float t = 0.f;
+    float t = acc ? f3p(m, m.tendf[1])(i, k, j) : 0.f;
     if (d1) {
       t = t + hdiff_point<DV_V>(m, v, nullptr, mut, c1, c2, i, k, j, xkmh);
       if (k <= ktf - 1 && j <= j_end)
@@ -333,7 +336,7 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
     if (k >= m.kts + 1) {
       const F3 w = f3(m, WRFGPU_W_2);
       const float c1w = f1(m, WRFGPU_C1F)(k), c2w = f1(m, WRFGPU_C2F)(k);
-      float t = 0.f;
+      float t = acc ? f3p(m, m.tendf[2])(i, k, j) : 0.f;
       if (d1) {
         t = t + hdiff_point<DV_W>(m, w, nullptr, mut, c1w, c2w, i, k, j, xkmh);
         t = t + vdiff_point<VD_W>(m, w, c1h, nullptr, mt, c1w, c2w, i, k, j, kvdif);
@@ -342,7 +345,7 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
       f3p(m, m.tendf[2])(i, k, j) = t;
     }
     const F3 th = f3(m, WRFGPU_T_2), tb = f3(m, WRFGPU_T_INIT);
-    float t = 0.f;
+    float t = acc ? f3p(m, m.tendf[3])(i, k, j) : 0.f;
     if (d1) {
       t = t + hdiff_point<DV_M>(m, th, &tb, mut, c1, c2, i, k, j, xkhh);
       t = t + vdiff_point<VD_3DMP>(m, th, c1h, &tb, mt, c1, c2, i, k, j, 3.f * kvdif);
@@ -392,7 +395,8 @@ __global__ void __launch_bounds__(BX* BY) k_species_diff_routine(Launch L, int q
 // column; the top layer's level heights are formed again where they are
 // used (the same expressions, so the same bits) instead of being stored.
 // A member that also stores the explicit or sixth-order diffusion
-// accumulates onto it (written earlier in the same stage); otherwise every level of the loop
+// accumulates onto it (written earlier in the same stage), as does the
+// routine-level form (acc_all: onto the caller's tendencies); otherwise every level of the loop
 // range is written, the damped ones as 0 - term and the others as 0, which is
 // the reference's zeroed tendency plus its additions.  The level searches
 // stop at kts.
@@ -417,14 +421,14 @@ __device__ __forceinline__ float rayleigh_profile(const F1& prof, const F1& zb, 
   if (k2 + 1 > ktf) return prof(k2) + (prof(k2) - prof(k2 - 1)) * (z - zb(k2)) / (zb(k2) - zb(k2 - 1));
   return prof(k2) + (prof(k2 + 1) - prof(k2)) * (z - zb(k2)) / (zb(k2 + 1) - zb(k2));
 }
-__global__ void __launch_bounds__(BX* BY) k_rayleigh_damp(Launch L) {
+__global__ void __launch_bounds__(BX* BY) k_rayleigh_damp(Launch L, bool acc_all) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid || m.cf.damp_opt != 2 || m.tendf[0] == nullptr) return;
   const int i = bp.i, j = bp.j;
   if (i < m.its || j < m.jts) return;
   const int kts = m.kts, ktf = min(m.kte, m.kde - 1), kde = m.kde;
-  const bool acc = m.cf.diff_6th_opt != 0 || m.cf.diff_opt == 1;
+  const bool acc = acc_all || m.cf.diff_6th_opt != 0 || m.cf.diff_opt == 1;
   const float dampcoef = m.cf.dampcoef, zdamp = m.cf.zdamp;
   const F3 ph = f3(m, WRFGPU_PH_2), phb = f3(m, WRFGPU_PHB);
   const F1 c1h = f1(m, WRFGPU_C1H), c2h = f1(m, WRFGPU_C2H), c1f = f1(m, WRFGPU_C1F), c2f = f1(m, WRFGPU_C2F);
@@ -543,8 +547,8 @@ void launch_species_diff_routine(const Launch& L, int nblocks, int qv, cudaStrea
   k_species_diff_routine<<<nblocks, dim3(BX, BY), 0, s>>>(L, qv);
 }
 
-void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s) {
-  k_rayleigh_damp<<<nblocks, dim3(BX, BY), 0, s>>>(L2);
+void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s, bool acc_all) {
+  k_rayleigh_damp<<<nblocks, dim3(BX, BY), 0, s>>>(L2, acc_all);
 }
 
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s) {

@@ -366,6 +366,8 @@ def _restart_fields(desc):
     """(file name, field id, stagger, kind) of every array of a restart."""
     out = []
     for nm, fid in abi.FIELD_ID.items():
+        if nm in abi.TENDF:  # stage 1's forward tendencies: rebuilt at every step's first stage
+            continue
         k = abi.field_kind(fid)
         out.append((nm.upper(), fid, _stag_of(fid) if k == 3 else "", k))
     nsp = desc.n_moist + desc.n_scalar

@@ -93,7 +93,7 @@ def contract_bytes_per_cell_step(n_moist, n_species, mixed=False):
 # the capture of k_scalar_pd_update, of k_scalar_adv_update (stage 1) and of
 # the acoustic column kernels.
 NCU_DRAM_BYTES_PER_CELL = {
-    "scalar_pd_update": 1022.0e6 / 5177344,
+    "scalar_pd_update": 1032.8e6 / 5177344,
     "scalar_adv_update": 780.6e6 / 5177344,
     "advance_w": 451.3e6 / 5177344,
 }

@@ -56,9 +56,17 @@ int wrfgpu_rk_step_prep(const WrfDynConfig *config_flags, const int *rk_step, co
                         const float *msftx, const float *msfty, const float *fnm, const float *fnp, const float *dnw,
                         const float *rdx, const float *rdy, const int *n_moist, WRFGPU_DIMS_ARGS);
 
-/* dyn_em/module_em.F:190 rk_tendency (physics off: the *_tendf, RTHFTEN,
- * h_diabatic, base-state, diffusion and damping arguments are read as zero /
- * unused; wwE, wwI are ww (IEVA off)). */
+/* dyn_em/module_em.F:190 rk_tendency.  The large-step tendencies of the
+ * physics-off path (RTHFTEN, h_diabatic, ph_tendf and the *_old arrays are
+ * unused; wwE, wwI are ww, IEVA off).  At rk_step 1, when config_flags (or
+ * the diff_6th_opt, damp_opt, khdif, kvdif, dampcoef, zdamp arguments, which
+ * take precedence as in the reference's call) ask for the explicit diffusion
+ * (diff_opt = 1 with km_opt = 1; xkmhd / xkhh, when given, must hold khdif /
+ * khdif / prandtl), the sixth-order diffusion or the Rayleigh damping
+ * (damp_opt = 2), the forward step (:801-944) adds their tendencies to
+ * ru_tendf, rv_tendf, rw_tendf and t_tendf, which arrive holding the physics
+ * tendencies (zeros with physics off); rk_addtend_dry is the caller's next
+ * call, as in solve_em. */
 int wrfgpu_rk_tendency(const WrfDynConfig *config_flags, const int *rk_step, float *ru_tend, float *rv_tend,
                        float *rw_tend, float *ph_tend, float *t_tend, float *ru_tendf, float *rv_tendf,
                        float *rw_tendf, const float *ph_tendf, float *t_tendf, float *mu_tend,

@@ -247,6 +247,27 @@ int wrfgpu_rk_update_scalar_pd(const int *scs, const int *sce, float *scalar, fl
  * moist step vertically against its base profile. */
 #define WRFGPU_P_QV 2
 
+/* dyn_em/module_em.F:959 rk_addtend_dry: at rk_step 1 the saved tendencies
+ * join the forward ones (ru_tendf += u_save msfuy, rv_tendf += v_save msfvx,
+ * rw_tendf += w_save msfty, ph_tendf += ph_save, t_tendf += t_save), then the
+ * forward tendencies are added to the large-step ones (divided by the map
+ * factors; theta with (c1 mut + c2) h_diabatic / msfty) and mu_tendf to
+ * mu_tend.  The patch dims ips..kpe must be those of the single patch the
+ * domain is (ips = ids, ..., kpe = kde); msftx, msfux, msfvy are unused as
+ * in the reference. */
+int wrfgpu_rk_addtend_dry(float *ru_tend, float *rv_tend, float *rw_tend, float *ph_tend, float *t_tend,
+                          float *ru_tendf, float *rv_tendf, float *rw_tendf, float *ph_tendf, float *t_tendf,
+                          const float *u_save, const float *v_save, const float *w_save, const float *ph_save,
+                          const float *t_save, float *mu_tend, float *mu_tendf, const int *rk_step,
+                          const float *c1, const float *c2, const float *h_diabatic, const float *mut,
+                          const float *msftx, const float *msfty, const float *msfux, const float *msfuy,
+                          const float *msfvx, const float *msfvx_inv, const float *msfvy, const int *ids,
+                          const int *ide, const int *jds, const int *jde, const int *kds, const int *kde,
+                          const int *ims, const int *ime, const int *jms, const int *jme, const int *kms,
+                          const int *kme, const int *ips, const int *ipe, const int *jps, const int *jpe,
+                          const int *kps, const int *kpe, const int *its, const int *ite, const int *jts,
+                          const int *jte, const int *kts, const int *kte);
+
 /* dyn_em/module_em.F:1096 rk_scalar_tend: for each species scs..sce
  * (scalar, scalar_old, scalar_tends: (ims:ime,kms:kme,jms:jme,scs:sce)),
  * advect_tend is zeroed over the tile and receives advect_scalar_pd at the

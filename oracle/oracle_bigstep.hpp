@@ -1040,4 +1040,53 @@ void rk_addtend_dry(R* ru_tend_p, R* rv_tend_p, R* rw_tend_p, R* t_tend_p, R* ru
                           (c1(k) * mut(i, j) + c2(k)) * R(0.) / msfty(i, j);
 }
 
+// module_em.F:959-1092 rk_addtend_dry, every term (the routine-level form):
+// at stage 1 the saved tendencies join the forward ones, and every stage adds
+// the forward ones to the large-step tendencies, theta's with its h_diabatic
+// term; mu_tend += mu_tendf.
+template <typename R>
+void rk_addtend_dry_full(R* ru_tend_p, R* rv_tend_p, R* rw_tend_p, R* ph_tend_p, R* t_tend_p, R* ru_tendf_p,
+                         R* rv_tendf_p, R* rw_tendf_p, R* ph_tendf_p, R* t_tendf_p, R* u_save_p, R* v_save_p,
+                         R* w_save_p, R* ph_save_p, R* t_save_p, R* mu_tend_p, R* mu_tendf_p, int rk_step, R* c1_p,
+                         R* c2_p, R* h_diabatic_p, R* mut_p, R* msfty_p, R* msfuy_p, R* msfvx_p, R* msfvx_inv_p,
+                         const Dims& d) {
+  A3<R> ru_tend(ru_tend_p, d), rv_tend(rv_tend_p, d), rw_tend(rw_tend_p, d), ph_tend(ph_tend_p, d),
+      t_tend(t_tend_p, d), ru_tendf(ru_tendf_p, d), rv_tendf(rv_tendf_p, d), rw_tendf(rw_tendf_p, d),
+      ph_tendf(ph_tendf_p, d), t_tendf(t_tendf_p, d), u_save(u_save_p, d), v_save(v_save_p, d),
+      w_save(w_save_p, d), ph_save(ph_save_p, d), t_save(t_save_p, d), h_diabatic(h_diabatic_p, d);
+  A2<R> mu_tend(mu_tend_p, d), mu_tendf(mu_tendf_p, d), mut(mut_p, d), msfty(msfty_p, d), msfuy(msfuy_p, d),
+      msfvx(msfvx_p, d), msfvx_inv(msfvx_inv_p, d);
+  A1<R> c1(c1_p, d), c2(c2_p, d);
+  const int i_end = std::min(d.ite, d.ide - 1), j_end = std::min(d.jte, d.jde - 1);
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = d.kts; k <= d.kte - 1; ++k)
+      for (int i = d.its; i <= d.ite; ++i) {
+        if (rk_step == 1) ru_tendf(i, k, j) = ru_tendf(i, k, j) + u_save(i, k, j) * msfuy(i, j);
+        ru_tend(i, k, j) = ru_tend(i, k, j) + ru_tendf(i, k, j) / msfuy(i, j);
+      }
+  for (int j = d.jts; j <= d.jte; ++j)
+    for (int k = d.kts; k <= d.kte - 1; ++k)
+      for (int i = d.its; i <= i_end; ++i) {
+        if (rk_step == 1) rv_tendf(i, k, j) = rv_tendf(i, k, j) + v_save(i, k, j) * msfvx(i, j);
+        rv_tend(i, k, j) = rv_tend(i, k, j) + rv_tendf(i, k, j) * msfvx_inv(i, j);
+      }
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = d.kts; k <= d.kte; ++k)
+      for (int i = d.its; i <= i_end; ++i) {
+        if (rk_step == 1) rw_tendf(i, k, j) = rw_tendf(i, k, j) + w_save(i, k, j) * msfty(i, j);
+        rw_tend(i, k, j) = rw_tend(i, k, j) + rw_tendf(i, k, j) / msfty(i, j);
+        if (rk_step == 1) ph_tendf(i, k, j) = ph_tendf(i, k, j) + ph_save(i, k, j);
+        ph_tend(i, k, j) = ph_tend(i, k, j) + ph_tendf(i, k, j) / msfty(i, j);
+      }
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int k = d.kts; k <= d.kte - 1; ++k)
+      for (int i = d.its; i <= i_end; ++i) {
+        if (rk_step == 1) t_tendf(i, k, j) = t_tendf(i, k, j) + t_save(i, k, j);
+        t_tend(i, k, j) = t_tend(i, k, j) + t_tendf(i, k, j) / msfty(i, j) +
+                          (c1(k) * mut(i, j) + c2(k)) * h_diabatic(i, k, j) / msfty(i, j);
+      }
+  for (int j = d.jts; j <= j_end; ++j)
+    for (int i = d.its; i <= i_end; ++i) mu_tend(i, j) = mu_tend(i, j) + mu_tendf(i, j);
+}
+
 }  // namespace wrforacle

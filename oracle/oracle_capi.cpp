@@ -176,6 +176,16 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
       if (D.tendf.empty()) return -1;
       D.forward_terms(D.tendf[0].data(), D.tendf[1].data(), D.tendf[2].data(), D.tendf[3].data(), R(D.sc.dt), td);
       return 0;
+    case ORACLE_R_ADDTEND_DRY_ARGS:
+      if (D.tendf.empty()) return -1;
+      rk_addtend_dry_full(p3(WRFGPU_RU_TEND), p3(WRFGPU_RV_TEND), p3(WRFGPU_RW_TEND), p3(WRFGPU_PH_TEND),
+                          p3(WRFGPU_T_TEND), D.tendf[0].data(), D.tendf[1].data(), D.tendf[2].data(),
+                          p3(WRFGPU_ADVECT_TEND), D.tendf[3].data(), p3(WRFGPU_U_SAVE), p3(WRFGPU_V_SAVE),
+                          p3(WRFGPU_W_SAVE), p3(WRFGPU_PH_SAVE), p3(WRFGPU_T_SAVE), p2(WRFGPU_MU_TEND),
+                          p2(WRFGPU_MUDF), rk_step, p1(WRFGPU_C1H), p1(WRFGPU_C2H), p3(WRFGPU_H_DIABATIC),
+                          p2(WRFGPU_MUT), p2(WRFGPU_MSFTY), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX),
+                          p2(WRFGPU_MSFVX_INV), td);
+      return 0;
     case ORACLE_R_SIXTH_DIFF_SPECIES:
       // rk_scalar_tend's stage-1 diffusion of species `species` into the
       // H_DIABATIC buffer (module_em.F:1378-1435): explicit (diff_opt = 1,

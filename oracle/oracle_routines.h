@@ -37,6 +37,8 @@ enum {
   ORACLE_R_SIXTH_DIFF_SPECIES = 32,
   /* rk_tendency's stage-1 forward terms added to the *_tendf fields
    * (WRFGPU_RU_TENDF ..), with the large step dt */
-  ORACLE_R_FORWARD_TERMS = 33
+  ORACLE_R_FORWARD_TERMS = 33,
+  /* rk_addtend_dry, every term: ph_tendf carried in ADVECT_TEND, mu_tendf in MUDF */
+  ORACLE_R_ADDTEND_DRY_ARGS = 34
 };
 #endif

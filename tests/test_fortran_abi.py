@@ -628,3 +628,58 @@ def test_rk_tendency_abi_forward_step_bitwise(gpulib, case_fwd):
     assert not bad, bad
     rc, _ = call(xk * np.float32(2.0))
     assert rc == abi.WRFGPU_E_ARG
+
+
+@pytest.mark.parametrize("rk", [1, 2])
+def test_rk_addtend_dry_abi_bitwise(gpulib, case_fwd, rk):
+    """wrfgpu_rk_addtend_dry (module_em.F:959-1092) with random tendencies,
+    forward tendencies, saves, h_diabatic and mu tendencies: at stage 1 the
+    saves join the forward tendencies, and every stage adds those to the
+    large-step ones; every output bit for bit the oracle's restatement, and a
+    patch smaller than the domain is refused."""
+    case = case_fwd
+    od = _state(case)
+    n3 = od.get(abi.FIELD_ID["u_2"]).size
+    n2 = od.get(abi.FIELD_ID["mu_2"]).size
+    rng = np.random.Generator(np.random.PCG64(50 + rk))
+    r3 = lambda sc=1e-3: (sc * rng.standard_normal(n3)).astype(np.float32)
+    r2 = lambda sc=1e-3: (sc * rng.standard_normal(n2)).astype(np.float32)
+    ins = {nm: r3() for nm in ("ru_tend", "rv_tend", "rw_tend", "ph_tend", "t_tend", "ru_tendf", "rv_tendf",
+                               "rw_tendf", "ph_tendf", "t_tendf", "u_save", "v_save", "w_save", "ph_save",
+                               "t_save", "h_diabatic")}
+    ins["mu_tend"] = r2(); ins["mu_tendf"] = r2()
+
+    def call(patch_off=0):
+        a = _Argv()
+        outs = {}
+        for nm in ("ru_tend", "rv_tend", "rw_tend", "ph_tend", "t_tend", "ru_tendf", "rv_tendf", "rw_tendf",
+                   "ph_tendf", "t_tendf"):
+            outs[nm] = a.arr(ins[nm].copy())
+        for nm in ("u_save", "v_save", "w_save", "ph_save", "t_save"):
+            a.arr(ins[nm])
+        outs["mu_tend"] = a.arr(ins["mu_tend"].copy()); outs["mu_tendf"] = a.arr(ins["mu_tendf"].copy())
+        a.i32(rk); a.arr(_f(od, "c1h")); a.arr(_f(od, "c2h")); a.arr(ins["h_diabatic"])
+        for nm in ("mut", "msftx", "msfty", "msfux", "msfuy", "msfvx", "msfvx_inv", "msfvy"):
+            a.arr(_f(od, nm))
+        h = abi.HALO
+        for d in [1, case.ide, 1, case.jde, 1, case.kde, 1 - h, case.ide + h, 1 - h, case.jde + h, 1, case.kde,
+                  1, case.ide - patch_off, 1, case.jde, 1, case.kde, 1, case.ide, 1, case.jde, 1, case.kde]:
+            a.i32(d)
+        return a.call(gpulib, "wrfgpu_rk_addtend_dry"), outs
+
+    rc, outs = call()
+    assert rc == 0
+    carriers = {"ph_tendf": "advect_tend", "mu_tendf": "mudf"}
+    for nm, v in ins.items():
+        od.set(abi.FIELD_ID[carriers.get(nm, nm)], v)
+    od.run("addtend_dry_args", rk)
+    bad = []
+    for nm, got in outs.items():
+        fid = abi.FIELD_ID[carriers.get(nm, nm)]
+        d = max_abs(interior(case, fid, got, halo=0), interior(case, fid, od.get(fid), halo=0))
+        if d != 0.0:
+            bad.append("%s: max|diff| %.3e" % (nm, d))
+    assert not bad, bad
+    assert not np.array_equal(outs["ru_tend"], ins["ru_tend"])
+    rc, _ = call(patch_off=4)
+    assert rc == abi.WRFGPU_E_ARG

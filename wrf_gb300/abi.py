@@ -116,7 +116,7 @@ ROUTINES = {
     # oracle-only forms checked against the routine-level C entry points
     "rk_update_scalar_pd_args": 30, "rk_update_scalar_args": 31, "sixth_diff_species": 32,
     # rk_tendency's stage-1 forward terms (diffusion, damping) added to the *_tendf fields
-    "forward_terms": 33,
+    "forward_terms": 33, "addtend_dry_args": 34,
 }
 
 

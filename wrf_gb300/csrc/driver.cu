@@ -879,6 +879,7 @@ struct Ensemble {
       case 132: launch_species_diff_routine(l3, nb3, iteration, stream); break;
       // rk_tendency's forward terms at stage 1 added to the caller's *_tendf
       case 133: launch_forward_diff(l3, nb3, 2, stream); launch_rayleigh_damp(l2, nb2, stream, true); break;
+      case 134: launch_addtend_dry_routine(l3, nb3, rk_step, stream); break;  // rk_addtend_dry
       case 24: launch_calc_p_rho_phi(l3, nb3, stream); break;
       case 25: launch_set_w_surface(l2, nb2, stream); break;
       case 26:

@@ -507,6 +507,43 @@ int wrfgpu_rk_update_scalar_pd(const int* scs, const int* sce, float* scalar, fl
   return WRFGPU_OK;
 }
 
+int wrfgpu_rk_addtend_dry(float* ru_tend, float* rv_tend, float* rw_tend, float* ph_tend, float* t_tend,
+                          float* ru_tendf, float* rv_tendf, float* rw_tendf, float* ph_tendf, float* t_tendf,
+                          const float* u_save, const float* v_save, const float* w_save, const float* ph_save,
+                          const float* t_save, float* mu_tend, float* mu_tendf, const int* rk_step,
+                          const float* c1, const float* c2, const float* h_diabatic, const float* mut,
+                          const float* msftx, const float* msfty, const float* msfux, const float* msfuy,
+                          const float* msfvx, const float* msfvx_inv, const float* msfvy, const int* ids,
+                          const int* ide, const int* jds, const int* jde, const int* kds, const int* kde,
+                          const int* ims, const int* ime, const int* jms, const int* jme, const int* kms,
+                          const int* kme, const int* ips, const int* ipe, const int* jps, const int* jpe,
+                          const int* kps, const int* kpe, const int* its, const int* ite, const int* jts,
+                          const int* jte, const int* kts, const int* kte) {
+  if (!rk_step || !ips || !ipe || !jps || !jpe || !kps || !kpe || !ids || !ide || !jds || !jde || !kds || !kde)
+    return WRFGPU_E_ARG;
+  // one patch covering the domain
+  if (*ips != *ids || *ipe != *ide || *jps != *jds || *jpe != *jde || *kps != *kds || *kpe != *kde)
+    return WRFGPU_E_ARG;
+  (void)msftx; (void)msfux; (void)msfvy;
+  FCall c;
+  set_dims(c, DIMS);
+  c.cfg = default_cfg(0); c.cfg.damp_opt = 2; c.cfg.zdamp = 1.f;  // a configuration that stores ru_tendf ..
+  c.routine = 134; c.rk_step = *rk_step;
+  RW(WRFGPU_RU_TEND, ru_tend); RW(WRFGPU_RV_TEND, rv_tend); RW(WRFGPU_RW_TEND, rw_tend);
+  RW(WRFGPU_PH_TEND, ph_tend); RW(WRFGPU_T_TEND, t_tend);
+  RW(WRFGPU_RU_TENDF, ru_tendf); RW(WRFGPU_RV_TENDF, rv_tendf); RW(WRFGPU_RW_TENDF, rw_tendf);
+  RW(WRFGPU_ADVECT_TEND, ph_tendf); RW(WRFGPU_T_TENDF, t_tendf);
+  R(WRFGPU_U_SAVE, u_save); R(WRFGPU_V_SAVE, v_save); R(WRFGPU_W_SAVE, w_save); R(WRFGPU_PH_SAVE, ph_save);
+  R(WRFGPU_T_SAVE, t_save); RW(WRFGPU_MU_TEND, mu_tend); RW(WRFGPU_MUDF, mu_tendf);
+  R(WRFGPU_C1H, c1); R(WRFGPU_C2H, c2); R(WRFGPU_H_DIABATIC, h_diabatic); R(WRFGPU_MUT, mut);
+  R(WRFGPU_MSFTY, msfty); R(WRFGPU_MSFUY, msfuy); R(WRFGPU_MSFVX, msfvx); R(WRFGPU_MSFVX_INV, msfvx_inv);
+  if (!ru_tend || !rv_tend || !rw_tend || !ph_tend || !t_tend || !ru_tendf || !rv_tendf || !rw_tendf || !ph_tendf ||
+      !t_tendf || !u_save || !v_save || !w_save || !ph_save || !t_save || !mu_tend || !mu_tendf || !c1 || !c2 ||
+      !h_diabatic || !mut || !msfty || !msfuy || !msfvx || !msfvx_inv)
+    return WRFGPU_E_ARG;
+  return wrfgpu::fortran_call(c);
+}
+
 int wrfgpu_rk_scalar_tend(const int* scs, const int* sce, const WrfDynConfig* config_flags, const int* tenddec,
                           const int* rk_step, const float* dt_step, const float* ru, const float* rv,
                           const float* ww, const float* wwE, const float* wwI, const float* u_old,

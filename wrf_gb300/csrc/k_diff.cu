@@ -537,7 +537,57 @@ __global__ void __launch_bounds__(BX* BY) k_addtend_dry(Launch L) {
   }
 }
 
+// The routine-level form of rk_addtend_dry (module_em.F:959-1092), every
+// term of the reference: at stage 1 the saved tendencies join the forward
+// ones (ru_tendf += u_save msfuy, ..., ph_tendf += ph_save, t_tendf +=
+// t_save), and every stage adds them to the large-step tendencies with
+// theta's h_diabatic term; mu_tend += mu_tendf.  ph_tendf is carried in the
+// ADVECT_TEND buffer and mu_tendf in MUDF.
+__global__ void __launch_bounds__(BX* BY) k_addtend_dry_routine(Launch L, int rk_step) {
+  BlockPos bp = block_pos(L);
+  const Mem& m = block_member(L.mem, bp.m);
+  if (!bp.valid || m.tendf[0] == nullptr) return;
+  const int i = bp.i, j = bp.j, k = bp.k;
+  if (i < m.its || j < m.jts || k < m.kts || k > m.kte) return;
+  const int i_end = min(m.ite, m.ide - 1), j_end = min(m.jte, m.jde - 1);
+  const bool s1 = rk_step == 1;
+  const F2 msfuy = f2(m, WRFGPU_MSFUY), msfvx = f2(m, WRFGPU_MSFVX), msfvx_inv = f2(m, WRFGPU_MSFVX_INV),
+           msfty = f2(m, WRFGPU_MSFTY);
+  if (k <= m.kte - 1 && i <= m.ite && j <= j_end) {
+    F3 f = f3p(m, m.tendf[0]), t = f3(m, WRFGPU_RU_TEND);
+    if (s1) f(i, k, j) = f(i, k, j) + f3(m, WRFGPU_U_SAVE)(i, k, j) * msfuy(i, j);
+    t(i, k, j) = t(i, k, j) + f(i, k, j) / msfuy(i, j);
+  }
+  if (k <= m.kte - 1 && i <= i_end && j <= m.jte) {
+    F3 f = f3p(m, m.tendf[1]), t = f3(m, WRFGPU_RV_TEND);
+    if (s1) f(i, k, j) = f(i, k, j) + f3(m, WRFGPU_V_SAVE)(i, k, j) * msfvx(i, j);
+    t(i, k, j) = t(i, k, j) + f(i, k, j) * msfvx_inv(i, j);
+  }
+  if (i <= i_end && j <= j_end) {
+    F3 f = f3p(m, m.tendf[2]), t = f3(m, WRFGPU_RW_TEND);
+    if (s1) f(i, k, j) = f(i, k, j) + f3(m, WRFGPU_W_SAVE)(i, k, j) * msfty(i, j);
+    t(i, k, j) = t(i, k, j) + f(i, k, j) / msfty(i, j);
+    F3 pf = f3(m, WRFGPU_ADVECT_TEND), pt = f3(m, WRFGPU_PH_TEND);
+    if (s1) pf(i, k, j) = pf(i, k, j) + f3(m, WRFGPU_PH_SAVE)(i, k, j);
+    pt(i, k, j) = pt(i, k, j) + pf(i, k, j) / msfty(i, j);
+    if (k <= m.kte - 1) {
+      F3 tf = f3p(m, m.tendf[3]), tt = f3(m, WRFGPU_T_TEND);
+      if (s1) tf(i, k, j) = tf(i, k, j) + f3(m, WRFGPU_T_SAVE)(i, k, j);
+      const float mass = f1(m, WRFGPU_C1H)(k) * f2(m, WRFGPU_MUT)(i, j) + f1(m, WRFGPU_C2H)(k);
+      tt(i, k, j) = tt(i, k, j) + tf(i, k, j) / msfty(i, j) + mass * f3(m, WRFGPU_H_DIABATIC)(i, k, j) / msfty(i, j);
+    }
+    if (k == m.kts) {
+      F2 mt = f2(m, WRFGPU_MU_TEND);
+      mt(i, j) = mt(i, j) + f2(m, WRFGPU_MUDF)(i, j);
+    }
+  }
+}
+
 }  // namespace
+
+void launch_addtend_dry_routine(const Launch& L, int nblocks, int rk_step, cudaStream_t s) {
+  k_addtend_dry_routine<<<nblocks, dim3(BX, BY), 0, s>>>(L, rk_step);
+}
 
 void launch_forward_diff(const Launch& L, int nblocks, int mode, cudaStream_t s) {
   k_forward_diff<<<nblocks, dim3(BX, BY), 0, s>>>(L, mode);

@@ -72,6 +72,7 @@ void launch_tend_ph_col(const TileLaunch& L, int nblocks, int flags, cudaStream_
 // mode 0: u, v, w, theta into ru_tendf .. t_tendf; 1: the species into sc_tend
 void launch_forward_diff(const Launch& L, int nblocks, int mode, cudaStream_t s);
 void launch_species_diff_routine(const Launch& L, int nblocks, int qv, cudaStream_t s);
+void launch_addtend_dry_routine(const Launch& L, int nblocks, int rk_step, cudaStream_t s);
 void launch_rayleigh_damp(const Launch& L2, int nblocks, cudaStream_t s, bool acc_all = false);
 void launch_addtend_dry(const Launch& L, int nblocks, cudaStream_t s);
 

@@ -405,6 +405,35 @@ struct LevelRing {
 };
 template <int NF, int NSLOT> using TileRing = LevelRing<NF, NSLOT, TX, TY>;
 
+// st(i, j) for the interior mass point (i, j) and for every halo point whose
+// periodic image (or, with symmetric y boundaries, mirror image) it is: the
+// points, and the values, that the halo fill of a mass-point field ('p',
+// 'w' or 't', share/module_bc.F:651-1000) gives them (the x halo of the
+// interior rows, then whole halo rows ims..ide+3).  A producer that stores
+// through it leaves out the fill that would follow it.
+template <class ST>
+__device__ __forceinline__ void store_mass_imaged(const Mem& m, int i, int j, ST st) {
+  int xs[3], ys[3];
+  int nx = 0, ny = 0;
+  xs[nx++] = i;
+  if (m.cf.periodic_x) {
+    const int np = m.ide - 1;
+    if (i - np >= m.ims) xs[nx++] = i - np;
+    if (i + np <= m.ide + WRFGPU_HALO - 1) xs[nx++] = i + np;
+  }
+  ys[ny++] = j;
+  const int npy = m.jde - 1;
+  if (m.cf.periodic_y) {
+    if (j - npy >= m.jms) ys[ny++] = j - npy;
+    if (j + npy <= m.jde + WRFGPU_HALO - 1) ys[ny++] = j + npy;
+  } else if (m.cf.symmetric_ys && m.cf.symmetric_ye) {
+    if (1 - j >= m.jms) ys[ny++] = 1 - j;
+    if (2 * npy + 1 - j <= m.jde + WRFGPU_HALO - 1) ys[ny++] = 2 * npy + 1 - j;
+  }
+  for (int a = 0; a < nx; ++a)
+    for (int b = 0; b < ny; ++b) st(xs[a], ys[b]);
+}
+
 struct TileLaunch {
   const Mem* mem;
   const int* block_start;  // [nmem+1] prefix over tiles x per_tile

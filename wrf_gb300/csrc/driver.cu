@@ -699,10 +699,11 @@ struct Ensemble {
         mark(PH_AMUT); launch_advance_mu_t_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AMUT]);
         mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AW], damp3);
         mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream, tune[TU_SUMF]);
-        JobList j;  // solve_em.F:1659-1716
-        j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_P, 'p');
-        j.f2(WRFGPU_MUTS, 't'); j.f2(WRFGPU_MU_2, 't'); j.f2(WRFGPU_MUDF, 't');
-        fill(j);
+        // the fills of solve_em.F:1659-1716 (ph_2, al, p, muts, mu_2, mudf) are
+        // the producers' own halo stores (store_mass_imaged): advance_mu_t,
+        // advance_w and calc_p_rho write each halo image with its interior
+        // point, and nothing in the acoustic step reads these halos before
+        // the next step's advance_uv
       }
       mark(PH_SSF); launch_small_step_finish(l2, nb2, a, stream, tune[TU_SSF]);
       if (rk_step == 3) {

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
     if (mcol && k <= mink) {
       const float a = cur.alt, t1 = cur.t1;
       float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (a * (c1h(k) * muij) + rdnw(k) * (cur.ph1 - ph_k));
-      al(i, k, j) = alv;
+      store_mass_imaged(m, i, j, [&](int ii, int jj) { al(ii, k, jj) = alv; });
       float pv = cur.c2a * (a * (cur.t2 - (c1h(k) * muij) * t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + t1)) - alv);
       if (iteration == 0) {
         pm1(i, k, j) = pv;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
         pv = pv + smdiv * (pv - cur.pm1);
         pm1(i, k, j) = ptmp;
       }
-      p(i, k, j) = pv;
+      store_mass_imaged(m, i, j, [&](int ii, int jj) { p(ii, k, jj) = pv; });
       ph_k = cur.ph1;
     }
     cur = nxt;
@@ -364,9 +364,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L,
   const float mu_tend = MU_TEND.ro(i, j);
   const float muave = MU(i, j);
   const float mu = (float)((RC)muave + (RC)dts * (dmdt + (RC)mu_tend));
-  MU(i, j) = mu;
-  MUDF(i, j) = (float)(dmdt + (RC)mu_tend);
-  MUTS(i, j) = MUT.ro(i, j) + mu;
+  const float mudf = (float)(dmdt + (RC)mu_tend), muts = MUT.ro(i, j) + mu;
+  store_mass_imaged(m, i, j, [&](int ii, int jj) { MU(ii, jj) = mu; MUDF(ii, jj) = mudf; MUTS(ii, jj) = muts; });
   MUAVE(i, j) = .5f * ((1.f + epssm) * mu + (1.f - epssm) * muave);
   const float my = msfty.ro(i, j), mx = msftx.ro(i, j);
   const RC rmy = rcp_rc<RC>((RC)my);  // mixed form only
@@ -635,7 +634,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
       float wst = (float)wup;
       if (damp3) wst = damped(kt, wst, ph_1.ro(i, kt, j), phb.ro(i, kt, j), w_save.ro(i, kt, j));
       w(i, kt, j) = wst;
-      ph(i, kt, j) = rhs[kt] + my * .5f * dts * G * eps1 * wst / (c1f(kt) * mts + c2f(kt));
+      const float phv = rhs[kt] + my * .5f * dts * G * eps1 * wst / (c1f(kt) * mts + c2f(kt));
+      store_mass_imaged(m, i, j, [&](int ii, int jj) { ph(ii, kt, jj) = phv; });
     }
     // four levels at a time: their gamma, eliminated w and rhs (global and
     // local-memory loads, independent of the recursion) go out first
@@ -660,7 +660,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
           float wst = (float)wk;
           if (damp3) wst = damped(k, wst, p1v[q], pbv[q], wsv[q]);
           w(i, k, j) = wst;
-          ph(i, k, j) = rv[q] + my * .5f * dts * G * eps1 * wst / (c1f(k) * mts + c2f(k));
+          const float phv = rv[q] + my * .5f * dts * G * eps1 * wst / (c1f(k) * mts + c2f(k));
+          store_mass_imaged(m, i, j, [&](int ii, int jj) { ph(ii, k, jj) = phv; });
           wup = wk;
         }
       }

@@ -405,34 +405,49 @@ struct LevelRing {
 };
 template <int NF, int NSLOT> using TileRing = LevelRing<NF, NSLOT, TX, TY>;
 
-// st(i, j) for the interior mass point (i, j) and for every halo point whose
-// periodic image (or, with symmetric y boundaries, mirror image) it is: the
-// points, and the values, that the halo fill of a mass-point field ('p',
-// 'w' or 't', share/module_bc.F:651-1000) gives them (the x halo of the
-// interior rows, then whole halo rows ims..ide+3).  A producer that stores
-// through it leaves out the fill that would follow it.
-template <class ST>
-__device__ __forceinline__ void store_mass_imaged(const Mem& m, int i, int j, ST st) {
-  int xs[3], ys[3];
-  int nx = 0, ny = 0;
-  xs[nx++] = i;
-  if (m.cf.periodic_x) {
-    const int np = m.ide - 1;
-    if (i - np >= m.ims) xs[nx++] = i - np;
-    if (i + np <= m.ide + WRFGPU_HALO - 1) xs[nx++] = i + np;
+// The interior mass point (i, j) and every halo point whose periodic image
+// (or, with symmetric y boundaries, mirror image) it is: the points that
+// the halo fill of a mass-point field ('p', 'w' or 't', share/module_bc.F:
+// 651-1000) gives its value (the x halo of the interior rows, then whole
+// halo rows ims..ide+3).  A producer that stores through store() leaves out
+// the fill that would follow it.  Formed once per column; a point away from
+// the edges has no image and store() is one store.
+struct MassImages {
+  static constexpr int NONE = -1000000;
+  int i, j, xa, xb, ya, yb;  // the point, and its x and y images (NONE: absent)
+  bool any;
+  __device__ __forceinline__ void init(const Mem& m, int i_, int j_) {
+    i = i_; j = j_;
+    xa = xb = ya = yb = NONE;
+    if (m.cf.periodic_x) {
+      const int np = m.ide - 1;
+      if (i - np >= m.ims) xa = i - np;
+      if (i + np <= m.ide + WRFGPU_HALO - 1) xb = i + np;
+    }
+    const int npy = m.jde - 1;
+    if (m.cf.periodic_y) {
+      if (j - npy >= m.jms) ya = j - npy;
+      if (j + npy <= m.jde + WRFGPU_HALO - 1) yb = j + npy;
+    } else if (m.cf.symmetric_ys && m.cf.symmetric_ye) {
+      if (1 - j >= m.jms) ya = 1 - j;
+      if (2 * npy + 1 - j <= m.jde + WRFGPU_HALO - 1) yb = 2 * npy + 1 - j;
+    }
+    any = xa != NONE || xb != NONE || ya != NONE || yb != NONE;
   }
-  ys[ny++] = j;
-  const int npy = m.jde - 1;
-  if (m.cf.periodic_y) {
-    if (j - npy >= m.jms) ys[ny++] = j - npy;
-    if (j + npy <= m.jde + WRFGPU_HALO - 1) ys[ny++] = j + npy;
-  } else if (m.cf.symmetric_ys && m.cf.symmetric_ye) {
-    if (1 - j >= m.jms) ys[ny++] = 1 - j;
-    if (2 * npy + 1 - j <= m.jde + WRFGPU_HALO - 1) ys[ny++] = 2 * npy + 1 - j;
+  template <class ST>
+  __device__ __forceinline__ void row(int jj, ST& st) const {
+    st(i, jj);
+    if (xa != NONE) st(xa, jj);
+    if (xb != NONE) st(xb, jj);
   }
-  for (int a = 0; a < nx; ++a)
-    for (int b = 0; b < ny; ++b) st(xs[a], ys[b]);
-}
+  template <class ST>
+  __device__ __forceinline__ void store(ST st) const {
+    if (!any) { st(i, j); return; }
+    row(j, st);
+    if (ya != NONE) row(ya, st);
+    if (yb != NONE) row(yb, st);
+  }
+};
 
 struct TileLaunch {
   const Mem* mem;

@@ -700,7 +700,7 @@ struct Ensemble {
         mark(PH_AW); launch_advance_w_col(LTM(), nb_tm, rk_step, it, fp64, stream, tune[TU_AW], damp3);
         mark(PH_SUMF); launch_sumflux_p_rho_col(LST(), nb_st, rk_step, it, stream, tune[TU_SUMF]);
         // the fills of solve_em.F:1659-1716 (ph_2, al, p, muts, mu_2, mudf) are
-        // the producers' own halo stores (store_mass_imaged): advance_mu_t,
+        // the producers' own halo stores (MassImages): advance_mu_t,
         // advance_w and calc_p_rho write each halo image with its interior
         // point, and nothing in the acoustic step reads these halos before
         // the next step's advance_uv

@@ -44,6 +44,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
   const int mini = min(m.ide - 1, m.ite), minj = min(m.jde - 1, m.jte), mink = min(m.kde - 1, m.kte);
   const int kts = m.kts, kte = m.kte;
   const bool ucol = j <= minj, vcol = i <= mini, mcol = ucol && vcol;
+  MassImages img;  // the halo images of al and p (mass columns)
+  img.init(m, i, j);
   F3 ru_m = f3(m, WRFGPU_RU_M), rv_m = f3(m, WRFGPU_RV_M), ww_m = f3(m, WRFGPU_WW_M);
   F3 u2 = f3(m, WRFGPU_U_2), v2 = f3(m, WRFGPU_V_2), ww = f3(m, WRFGPU_WW), us = f3(m, WRFGPU_U_SAVE),
      vs = f3(m, WRFGPU_V_SAVE), ww1 = f3(m, WRFGPU_WW1);
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
     if (mcol && k <= mink) {
       const float a = cur.alt, t1 = cur.t1;
       float alv = -1.f / (c1h(k) * mutij + c2h(k)) * (a * (c1h(k) * muij) + rdnw(k) * (cur.ph1 - ph_k));
-      store_mass_imaged(m, i, j, [&](int ii, int jj) { al(ii, k, jj) = alv; });
+      img.store([&](int ii, int jj) { al(ii, k, jj) = alv; });
       float pv = cur.c2a * (a * (cur.t2 - (c1h(k) * muij) * t1) / ((c1h(k) * mutij + c2h(k)) * (T0 + t1)) - alv);
       if (iteration == 0) {
         pm1(i, k, j) = pv;
@@ -114,7 +116,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_sumflux_p_rho_col(TileLaunch L
         pv = pv + smdiv * (pv - cur.pm1);
         pm1(i, k, j) = ptmp;
       }
-      store_mass_imaged(m, i, j, [&](int ii, int jj) { p(ii, k, jj) = pv; });
+      img.store([&](int ii, int jj) { p(ii, k, jj) = pv; });
       ph_k = cur.ph1;
     }
     cur = nxt;
@@ -365,7 +367,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_mu_t_col(TileLaunch L,
   const float muave = MU(i, j);
   const float mu = (float)((RC)muave + (RC)dts * (dmdt + (RC)mu_tend));
   const float mudf = (float)(dmdt + (RC)mu_tend), muts = MUT.ro(i, j) + mu;
-  store_mass_imaged(m, i, j, [&](int ii, int jj) { MU(ii, jj) = mu; MUDF(ii, jj) = mudf; MUTS(ii, jj) = muts; });
+  MassImages img;
+  img.init(m, i, j);
+  img.store([&](int ii, int jj) { MU(ii, jj) = mu; MUDF(ii, jj) = mudf; MUTS(ii, jj) = muts; });
   MUAVE(i, j) = .5f * ((1.f + epssm) * mu + (1.f - epssm) * muave);
   const float my = msfty.ro(i, j), mx = msftx.ro(i, j);
   const RC rmy = rcp_rc<RC>((RC)my);  // mixed form only
@@ -608,6 +612,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
     }
     if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
     if (!act) return;
+    MassImages img;  // the halo images of ph
+    img.init(m, i, j);
     w(i, 1, j) = w1;
     // ---- damp_opt = 3 (module_small_step_em.F:1445-1458): after the back
     // substitution, w relaxes toward w_save in the top zdamp metres with
@@ -635,7 +641,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
       if (damp3) wst = damped(kt, wst, ph_1.ro(i, kt, j), phb.ro(i, kt, j), w_save.ro(i, kt, j));
       w(i, kt, j) = wst;
       const float phv = rhs[kt] + my * .5f * dts * G * eps1 * wst / (c1f(kt) * mts + c2f(kt));
-      store_mass_imaged(m, i, j, [&](int ii, int jj) { ph(ii, kt, jj) = phv; });
+      img.store([&](int ii, int jj) { ph(ii, kt, jj) = phv; });
     }
     // four levels at a time: their gamma, eliminated w and rhs (global and
     // local-memory loads, independent of the recursion) go out first
@@ -661,7 +667,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_advance_w_col(TileLaunch L, in
           if (damp3) wst = damped(k, wst, p1v[q], pbv[q], wsv[q]);
           w(i, k, j) = wst;
           const float phv = rv[q] + my * .5f * dts * G * eps1 * wst / (c1f(k) * mts + c2f(k));
-          store_mass_imaged(m, i, j, [&](int ii, int jj) { ph(ii, k, jj) = phv; });
+          img.store([&](int ii, int jj) { ph(ii, k, jj) = phv; });
           wup = wk;
         }
       }

@@ -655,7 +655,7 @@ def run_single(args, world, rank, local, pg):
         h2d = sum(b.nbytes for b in bufs.values())
         d2h = h2d
         dom.bind_host_state(0, list(bufs), list(bufs.values()))
-        dom.step_host(1)  # builds the step's graph with its copies
+        dom.step_host(3)  # captures the step's graphs with their copies (first, middle, last step of a call)
         dom.sync()
         barrier(pg)
         t0 = time.perf_counter()

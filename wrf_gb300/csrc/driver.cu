@@ -216,12 +216,16 @@ struct Ensemble {
     float* dev = nullptr;    // a fixed field buffer (species < 0)
     size_t count = 0, cols = 0, rows = 0, pitch = 0;
     float* stage = nullptr;  // contiguous device copy
+    bool prefetch = false;   // the next step's input may cross during this step's last stage
   };
   std::vector<HostIO> hio;
   cudaStream_t cstream = nullptr;  // copy-in branch of the host I/O step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  cudaGraph_t graph_io[2] = {nullptr, nullptr};
-  cudaGraphExec_t gexec_io[2] = {nullptr, nullptr};
+  // [head][prefetch]: head = the previous step's deferred downloads come
+  // first; prefetch = the next step's early inputs cross during this one
+  cudaGraph_t graph_io[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaGraphExec_t gexec_io[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  bool io_prefetch = false;  // enqueue_step: the dry downloads are followed by the next step's uploads
   int io_swaps = 0;  // species-buffer swaps in one captured I/O step
   bool io_pending = false;  // enqueue_step: the copy-in branch is still to be joined
   bool io_step = false;     // enqueue_step runs inside a host I/O step
@@ -250,20 +254,44 @@ struct Ensemble {
   void io_dry_out() {
     if (!io_step) return;
     bool any = false;
-    for (const HostIO& b : hio) any = any || (b.out && early_out(b));
+    for (const HostIO& b : hio) any = any || (b.out && early_out(b)) || (io_prefetch && b.prefetch);
     if (!any) return;
     cudaEventRecord(ev_ofork, stream);
     cudaStreamWaitEvent(cstream, ev_ofork, 0);
     for (const HostIO& b : hio)
       if (b.out && early_out(b)) copy_out(b, cstream);
+    // the next step's inputs that no later download of this step can change,
+    // into staging buffers that nothing in this step uses again
+    if (io_prefetch)
+      for (const HostIO& b : hio)
+        if (b.prefetch) cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, cstream);
     cudaEventRecord(ev_ojoin, cstream);
     io_out_pending = true;
   }
-  void drop_io_graph() {
-    for (int v = 0; v < 2; ++v) {
-      if (gexec_io[v]) { cudaGraphExecDestroy(gexec_io[v]); gexec_io[v] = nullptr; }
-      if (graph_io[v]) { cudaGraphDestroy(graph_io[v]); graph_io[v] = nullptr; }
+  // An early input (the dry state, moist species) may be uploaded during the
+  // previous step's last stage when its staging buffer is free then (no
+  // output, or an output downloaded at that same point) and its host array
+  // overlaps no output downloaded later in the step.
+  void set_prefetch() {
+    for (HostIO& b : hio) {
+      b.prefetch = b.in && !b.late && (!b.out || early_out(b));
+      if (!b.prefetch) continue;
+      const char* lo = (const char*)b.in;
+      const char* hi = lo + b.count * 4;
+      for (const HostIO& g : hio) {
+        if (!g.out || early_out(g)) continue;
+        const char* glo = (const char*)g.out;
+        const char* ghi = glo + g.count * 4;
+        if (lo < ghi && glo < hi) { b.prefetch = false; break; }
+      }
     }
+  }
+  void drop_io_graph() {
+    for (int h = 0; h < 2; ++h)
+      for (int v = 0; v < 2; ++v) {
+        if (gexec_io[h][v]) { cudaGraphExecDestroy(gexec_io[h][v]); gexec_io[h][v] = nullptr; }
+        if (graph_io[h][v]) { cudaGraphDestroy(graph_io[h][v]); graph_io[h][v] = nullptr; }
+      }
   }
   void unbind_host() {
     drop_io_graph();
@@ -314,6 +342,7 @@ struct Ensemble {
         }
       hio.push_back(b);
     }
+    set_prefetch();
     return WRFGPU_OK;
   }
   // one step with its copies, enqueued on `stream` (and `cstream`)
@@ -333,7 +362,7 @@ struct Ensemble {
   // One step with its copies, enqueued on `stream` and `cstream`.  head: the
   // previous step's deferred downloads first; defer: this step's passive
   // scalars left for the next step's head (or flush_deferred).
-  int enqueue_io_step(bool head, bool defer) {
+  int enqueue_io_step(bool head, bool defer, bool pre) {
     if (int rc = io_streams()) return rc;
     auto unpack = [&](const HostIO& b, cudaStream_t st) {
       if (b.species >= 0)
@@ -349,8 +378,9 @@ struct Ensemble {
       for (const HostIO& b : hio)
         if (b.out && deferrable(b)) copy_out(b, cstream);
     // the dry state and the moist species first, at the link's full rate
-    for (const HostIO& b : hio)
-      if (b.in && !b.late) CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, stream));
+    for (const HostIO& b : hio)  // (already uploaded during the previous step when prefetched)
+      if (b.in && !b.late && !(head && b.prefetch))
+        CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, stream));
     CK(cudaEventRecord(ev_dryin, stream));
     for (const HostIO& b : hio)
       if (b.in && !b.late) unpack(b, stream);
@@ -363,9 +393,11 @@ struct Ensemble {
     CK(cudaEventRecord(ev_join, cstream));
     io_pending = true;
     io_step = true;
+    io_prefetch = pre;
     io_out_pending = false;
     enqueue_step();
     io_step = false;
+    io_prefetch = false;
     io_join();
     (void)late;
     for (const HostIO& b : hio)
@@ -383,15 +415,16 @@ struct Ensemble {
     CK(cudaGetLastError());
     return WRFGPU_OK;
   }
-  // gexec_io[0]: the first step of a call (nothing deferred before it);
-  // gexec_io[1]: every later step
-  int build_io_graph(int v) {
-    if (gexec_io[v]) return WRFGPU_OK;
+  // gexec_io[h][p]: h = a later step of a call (the previous step's deferred
+  // downloads at its head, its prefetched inputs already across), p = not
+  // the call's last step (the next step's inputs prefetched)
+  int build_io_graph(int h, int v) {
+    if (gexec_io[h][v]) return WRFGPU_OK;
     if (int rc = io_streams()) return rc;  // created outside the capture
     capturing = true;
     capture_swaps = 0;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = enqueue_io_step(v == 1, true);
+    const int rc = enqueue_io_step(h == 1, true, v == 1);
     capturing = false;
     io_swaps = capture_swaps;
     for (int q = 0; q < capture_swaps; ++q) host_flip();
@@ -402,19 +435,30 @@ struct Ensemble {
       cudaGetLastError();
       return rc ? rc : WRFGPU_E_CUDA;
     }
-    graph_io[v] = g;
-    CK(cudaGraphInstantiate(&gexec_io[v], graph_io[v], 0));
+    graph_io[h][v] = g;
+    CK(cudaGraphInstantiate(&gexec_io[h][v], graph_io[h][v], 0));
     return WRFGPU_OK;
   }
   int step_host(int nsteps) {
     if (hio.empty() || nsteps < 0) return WRFGPU_E_ARG;
     if (nsteps == 0) return WRFGPU_OK;
     if (flags & WRFGPU_FLAG_NO_GRAPH) {
-      for (int s = 0; s < nsteps; ++s) { int rc = enqueue_io_step(s > 0, true); if (rc) return rc; }
-    } else {
-      for (int v = 0; v < 2; ++v) { int rc = build_io_graph(v); if (rc) return rc; }
       for (int s = 0; s < nsteps; ++s) {
-        CK(cudaGraphLaunch(gexec_io[s > 0 ? 1 : 0], stream));
+        int rc = enqueue_io_step(s > 0, true, s + 1 < nsteps);
+        if (rc) return rc;
+      }
+    } else {
+      // the variants this call needs, captured before the first launch
+      const int need[3][2] = {{0, nsteps > 1 ? 1 : 0}, {1, 1}, {1, 0}};
+      for (int q = 0; q < 3; ++q) {
+        if (q == 1 && nsteps < 3) continue;
+        if (q == 2 && nsteps < 2) continue;
+        int rc = build_io_graph(need[q][0], need[q][1]);
+        if (rc) return rc;
+      }
+      for (int s = 0; s < nsteps; ++s) {
+        const int h = s > 0 ? 1 : 0, v = s + 1 < nsteps ? 1 : 0;
+        CK(cudaGraphLaunch(gexec_io[h][v], stream));
         for (int q = 0; q < io_swaps; ++q) host_flip();
       }
     }

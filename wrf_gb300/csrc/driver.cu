@@ -219,7 +219,10 @@ struct Ensemble {
     bool prefetch = false;   // the next step's input may cross during this step's last stage
   };
   std::vector<HostIO> hio;
-  cudaStream_t cstream = nullptr;  // copy-in branch of the host I/O step
+  cudaStream_t cstream = nullptr;  // downloads of the host I/O step that overlap its kernels
+  cudaStream_t ustream = nullptr;  // uploads of the host I/O step that overlap its kernels
+  std::vector<cudaEvent_t> ev_dn;  // per bound field: its overlapped download is complete
+  cudaEvent_t ev_head = nullptr, ev_ojoin2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // [head][prefetch]: head = the previous step's deferred downloads come
   // first; prefetch = the next step's early inputs cross during this one
@@ -235,7 +238,23 @@ struct Ensemble {
   void io_join() {
     if (!io_pending) return;
     cudaStreamWaitEvent(stream, ev_join, 0);
+    cudaStreamWaitEvent(stream, ev_head, 0);
     io_pending = false;
+  }
+  // Upload of field q on ustream after the downloads of this phase that use
+  // its staging buffer or write its host input (dn[g]: g's download is in
+  // this phase).
+  void upload_after(size_t q, const std::vector<char>& dn) {
+    const HostIO& b = hio[q];
+    const char* lo = (const char*)b.in;
+    const char* hi = lo + b.count * 4;
+    for (size_t g = 0; g < hio.size(); ++g) {
+      if (!dn[g]) continue;
+      const char* glo = (const char*)hio[g].out;
+      const char* ghi = glo + hio[g].count * 4;
+      if (g == q || (lo < ghi && glo < hi)) cudaStreamWaitEvent(ustream, ev_dn[g], 0);
+    }
+    cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, ustream);
   }
   // the _2 dry state is final once the last stage's fills and set_w_surface
   // are done (enqueue_step): its bound outputs cross the link on the copy
@@ -258,14 +277,21 @@ struct Ensemble {
     if (!any) return;
     cudaEventRecord(ev_ofork, stream);
     cudaStreamWaitEvent(cstream, ev_ofork, 0);
-    for (const HostIO& b : hio)
-      if (b.out && early_out(b)) copy_out(b, cstream);
+    cudaStreamWaitEvent(ustream, ev_ofork, 0);
+    std::vector<char> dn(hio.size(), 0);
+    for (size_t q = 0; q < hio.size(); ++q)
+      if (hio[q].out && early_out(hio[q])) {
+        copy_out(hio[q], cstream);
+        cudaEventRecord(ev_dn[q], cstream);
+        dn[q] = 1;
+      }
     // the next step's inputs that no later download of this step can change,
-    // into staging buffers that nothing in this step uses again
+    // on the other copy engine direction, each after the downloads it waits for
     if (io_prefetch)
-      for (const HostIO& b : hio)
-        if (b.prefetch) cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, cstream);
+      for (size_t q = 0; q < hio.size(); ++q)
+        if (hio[q].prefetch) upload_after(q, dn);
     cudaEventRecord(ev_ojoin, cstream);
+    cudaEventRecord(ev_ojoin2, ustream);
     io_out_pending = true;
   }
   // An early input (the dry state, moist species) may be uploaded during the
@@ -347,9 +373,15 @@ struct Ensemble {
   }
   // one step with its copies, enqueued on `stream` (and `cstream`)
   int io_streams() {
+    while (ev_dn.size() < hio.size()) {
+      cudaEvent_t e;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ev_dn.push_back(e);
+    }
     if (cstream) return WRFGPU_OK;
     CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin})
+    CK(cudaStreamCreateWithFlags(&ustream, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin, &ev_head, &ev_ojoin2})
       CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     return WRFGPU_OK;
   }
@@ -374,23 +406,33 @@ struct Ensemble {
     for (const HostIO& b : hio) late = late || (b.in && b.late);
     CK(cudaEventRecord(ev_fork, stream));
     CK(cudaStreamWaitEvent(cstream, ev_fork, 0));
+    CK(cudaStreamWaitEvent(ustream, ev_fork, 0));
+    // the previous step's deferred downloads on one copy direction ...
+    std::vector<char> dn(hio.size(), 0);
     if (head)
-      for (const HostIO& b : hio)
-        if (b.out && deferrable(b)) copy_out(b, cstream);
-    // the dry state and the moist species first, at the link's full rate
-    for (const HostIO& b : hio)  // (already uploaded during the previous step when prefetched)
+      for (size_t q = 0; q < hio.size(); ++q)
+        if (hio[q].out && deferrable(hio[q])) {
+          copy_out(hio[q], cstream);
+          CK(cudaEventRecord(ev_dn[q], cstream));
+          dn[q] = 1;
+        }
+    CK(cudaEventRecord(ev_head, cstream));
+    // ... the dry state and the moist species first on the other, at the
+    // link's full rate (those prefetched during the previous step are across)
+    for (const HostIO& b : hio)
       if (b.in && !b.late && !(head && b.prefetch))
         CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, stream));
     CK(cudaEventRecord(ev_dryin, stream));
     for (const HostIO& b : hio)
       if (b.in && !b.late) unpack(b, stream);
-    CK(cudaStreamWaitEvent(cstream, ev_dryin, 0));
-    for (const HostIO& b : hio)
-      if (b.in && b.late) {
-        CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, cstream));
-        unpack(b, cstream);
+    // then the passive scalars, each after its own deferred download
+    CK(cudaStreamWaitEvent(ustream, ev_dryin, 0));
+    for (size_t q = 0; q < hio.size(); ++q)
+      if (hio[q].in && hio[q].late) {
+        upload_after(q, dn);
+        unpack(hio[q], ustream);
       }
-    CK(cudaEventRecord(ev_join, cstream));
+    CK(cudaEventRecord(ev_join, ustream));
     io_pending = true;
     io_step = true;
     io_prefetch = pre;
@@ -404,6 +446,7 @@ struct Ensemble {
       if (b.out && !early_out(b) && !(defer && deferrable(b))) copy_out(b, stream);
     if (io_out_pending) {
       CK(cudaStreamWaitEvent(stream, ev_ojoin, 0));
+      CK(cudaStreamWaitEvent(stream, ev_ojoin2, 0));
       io_out_pending = false;
     }
     CK(cudaGetLastError());
@@ -470,6 +513,10 @@ struct Ensemble {
   ~Ensemble() {
     unbind_host();
     if (cstream) cudaStreamDestroy(cstream);
+    if (ustream) cudaStreamDestroy(ustream);
+    for (cudaEvent_t e : ev_dn) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ev_head, ev_ojoin2})
+      if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : {ev_fork, ev_join, ev_ofork, ev_ojoin, ev_dryin})
       if (e) cudaEventDestroy(e);
     if (d_stage) cudaFree(d_stage);

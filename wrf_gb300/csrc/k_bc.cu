@@ -136,20 +136,31 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
 
 // Row copies between a contiguous buffer (rows of `cols` values, the
 // caller's Fortran layout) and a field's padded device rows (`pitch` apart);
-// `dst2`, when given, receives the same rows (a species' spare buffer).
+// `dst2`, when given, receives the same rows (a species' spare buffer).  One
+// warp per row, the rows grid-strided over a grid of a few blocks per SM:
+// coalesced loads and stores, and no launch of one tiny block per row
+// fragment.
+__device__ __forceinline__ void copy_rows(const float* __restrict__ src, size_t src_pitch, float* __restrict__ dst,
+                                          float* __restrict__ dst2, size_t dst_pitch, int cols, int rows) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (int r = warp; r < rows; r += nwarp) {
+    const float* sr = src + (size_t)r * src_pitch;
+    float* dr = dst + (size_t)r * dst_pitch;
+    float* dr2 = dst2 ? dst2 + (size_t)r * dst_pitch : nullptr;
+    for (int c = lane; c < cols; c += 32) {
+      const float v = sr[c];
+      dr[c] = v;
+      if (dr2) dr2[c] = v;
+    }
+  }
+}
 __global__ void k_unpack_rows(const float* __restrict__ src, float* __restrict__ dst, float* __restrict__ dst2,
                               int cols, int rows, int pitch) {
-  for (int r = blockIdx.y; r < rows; r += gridDim.y)
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
-      const float v = src[(size_t)r * cols + c];
-      dst[(size_t)r * pitch + c] = v;
-      if (dst2) dst2[(size_t)r * pitch + c] = v;
-    }
+  copy_rows(src, cols, dst, dst2, pitch, cols, rows);
 }
 __global__ void k_pack_rows(const float* __restrict__ src, float* __restrict__ dst, int cols, int rows, int pitch) {
-  for (int r = blockIdx.y; r < rows; r += gridDim.y)
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
-      dst[(size_t)r * cols + c] = src[(size_t)r * pitch + c];
+  copy_rows(src, pitch, dst, nullptr, cols, cols, rows);
 }
 // The same for species s of member `member`, whose current and spare buffers
 // are read from the device member table when the copy runs (the buffers
@@ -157,41 +168,28 @@ __global__ void k_pack_rows(const float* __restrict__ src, float* __restrict__ d
 // their addresses).  Unpacking writes both buffers.
 __global__ void k_unpack_species(const Mem* __restrict__ mems, int member, int s, const float* __restrict__ src,
                                  int cols, int rows, int pitch) {
-  float* dst = mems[member].q[s];
-  float* dst2 = mems[member].qa[s];
-  for (int r = blockIdx.y; r < rows; r += gridDim.y)
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
-      const float v = src[(size_t)r * cols + c];
-      dst[(size_t)r * pitch + c] = v;
-      dst2[(size_t)r * pitch + c] = v;
-    }
+  copy_rows(src, cols, mems[member].q[s], mems[member].qa[s], pitch, cols, rows);
 }
 __global__ void k_pack_species(const Mem* __restrict__ mems, int member, int s, float* __restrict__ dst, int cols,
                                int rows, int pitch) {
-  const float* src = mems[member].q[s];
-  for (int r = blockIdx.y; r < rows; r += gridDim.y)
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
-      dst[(size_t)r * cols + c] = src[(size_t)r * pitch + c];
+  copy_rows(mems[member].q[s], pitch, dst, nullptr, cols, cols, rows);
 }
-static dim3 rows_grid(int cols, int rows) { return dim3((cols + 255) / 256, rows < 65535 ? rows : 65535); }
+static int rows_grid(int rows) {  // 256-thread blocks of 8 row-warps, at most 8 blocks per SM of 152
+  return rows / 8 + 1 < 8 * 152 ? rows / 8 + 1 : 8 * 152;
+}
+void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s) {
+  if (cols > 0 && rows > 0) k_unpack_rows<<<rows_grid(rows), 256, 0, s>>>(src, dst, dst2, cols, rows, pitch);
+}
+void launch_pack_rows(const float* src, float* dst, int cols, int rows, int pitch, cudaStream_t s) {
+  if (cols > 0 && rows > 0) k_pack_rows<<<rows_grid(rows), 256, 0, s>>>(src, dst, cols, rows, pitch);
+}
 void launch_unpack_species(const Mem* mems, int member, int s, const float* src, int cols, int rows, int pitch,
                            cudaStream_t st) {
-  if (cols > 0 && rows > 0) k_unpack_species<<<rows_grid(cols, rows), 256, 0, st>>>(mems, member, s, src, cols, rows, pitch);
+  if (cols > 0 && rows > 0) k_unpack_species<<<rows_grid(rows), 256, 0, st>>>(mems, member, s, src, cols, rows, pitch);
 }
 void launch_pack_species(const Mem* mems, int member, int s, float* dst, int cols, int rows, int pitch,
                          cudaStream_t st) {
-  if (cols > 0 && rows > 0) k_pack_species<<<rows_grid(cols, rows), 256, 0, st>>>(mems, member, s, dst, cols, rows, pitch);
-}
-void launch_unpack_rows(const float* src, float* dst, float* dst2, int cols, int rows, int pitch, cudaStream_t s) {
-  if (cols > 0 && rows > 0) k_unpack_rows<<<rows_grid(cols, rows), 256, 0, s>>>(src, dst, dst2, cols, rows, pitch);
-}
-void launch_pack_rows(const float* src, float* dst, int cols, int rows, int pitch, cudaStream_t s) {
-  if (cols > 0 && rows > 0) k_pack_rows<<<rows_grid(cols, rows), 256, 0, s>>>(src, dst, cols, rows, pitch);
-}
-
-void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s) {
-  if (jobs.n <= 0 || nmem <= 0) return;
-  k_fill_halo<<<dim3(blocks_per_job, jobs.n, nmem), 256, 0, s>>>(d_mems, jobs);
+  if (cols > 0 && rows > 0) k_pack_species<<<rows_grid(rows), 256, 0, st>>>(mems, member, s, dst, cols, rows, pitch);
 }
 
 }  // namespace wrfgpu

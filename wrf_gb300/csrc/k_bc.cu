@@ -192,4 +192,9 @@ void launch_pack_species(const Mem* mems, int member, int s, float* dst, int col
   if (cols > 0 && rows > 0) k_pack_species<<<rows_grid(rows), 256, 0, st>>>(mems, member, s, dst, cols, rows, pitch);
 }
 
+void launch_fill_halo(const Mem* d_mems, int nmem, const HaloJobs& jobs, int blocks_per_job, cudaStream_t s) {
+  if (jobs.n <= 0 || nmem <= 0) return;
+  k_fill_halo<<<dim3(blocks_per_job, jobs.n, nmem), 256, 0, s>>>(d_mems, jobs);
+}
+
 }  // namespace wrfgpu

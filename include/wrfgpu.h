@@ -181,8 +181,10 @@ int wrfgpu_unbind_host_state(WrfGpuEnsemble* h);
  * written (so in[f] == out[f] runs a host time loop); returns when the last
  * copy is complete.  The copies overlap the kernels: the passive scalars'
  * uploads run during stage 1's dynamics, the dry state's downloads during
- * the last stage's scalar transport, and the passive scalars' downloads
- * during the next step of the same call.  The results equal those of
+ * the last stage's scalar transport (followed there, within one call, by
+ * the next step's dry uploads when no later download can change their host
+ * arrays), and the passive scalars' downloads during the next step of the
+ * same call.  The results equal those of
  * wrfgpu_set_field_f32 of every input, wrfgpu_step and wrfgpu_get_field_f32
  * of every output, step by step, bit for bit. */
 int wrfgpu_step_host(WrfGpuEnsemble* h, int nsteps);

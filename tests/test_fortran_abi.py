@@ -145,25 +145,46 @@ def _fid(name):
     return abi.FIELD_ID[name]
 
 
-def _call(lib, routine, spec, od, case, scal):
+def _widen(case, fid, arr, extra, fill=7777.0):
+    """A memory-layout array with `extra` more halo points on each side in i
+    and j (filled with `fill`), and the index slices of the standard window."""
+    h = abi.HALO
+    k = abi.field_kind(fid)
+    if k == 1 or extra == 0:
+        return np.ascontiguousarray(arr, dtype=np.float32), None
+    ni, nj = case.ide + 2 * h, case.jde + 2 * h
+    if k == 3:
+        a = np.asarray(arr, dtype=np.float32).reshape(nj, case.kde, ni)
+        w = np.full((nj + 2 * extra, case.kde, ni + 2 * extra), fill, np.float32)
+        win = (slice(extra, extra + nj), slice(None), slice(extra, extra + ni))
+    else:
+        a = np.asarray(arr, dtype=np.float32).reshape(nj, ni)
+        w = np.full((nj + 2 * extra, ni + 2 * extra), fill, np.float32)
+        win = (slice(extra, extra + nj), slice(extra, extra + ni))
+    w[win] = a
+    return np.ascontiguousarray(w.ravel()), (w.shape, win)
+
+
+def _call(lib, routine, spec, od, case, scal, extra=0, tile=None, arrays=None):
+    """Call wrfgpu_<routine> as Fortran would; `extra`: memory halo beyond 4,
+    `tile`: (its, ite, jts, jte); `arrays`: the (widened) arrays of a
+    previous call to pass again (a tile loop over shared arrays)."""
     keep = []
     args = []
-    arrays = {}
-    h = abi.HALO
+    arrays = {} if arrays is None else arrays
+    h = abi.HALO + extra
+    its, ite, jts, jte = tile if tile else (1, case.ide, 1, case.jde)
     dims = [1, case.ide, 1, case.jde, 1, case.kde, 1 - h, case.ide + h, 1 - h, case.jde + h, 1, case.kde,
-            1, case.ide, 1, case.jde, 1, case.kde]
+            its, ite, jts, jte, 1, case.kde]
     cfg = C.pointer(case.desc.config)
     keep.append(cfg)
     for a in spec:
-        if a[0] == "a":
-            arr = np.ascontiguousarray(od.get(_fid(a[1])), dtype=np.float32)
+        if a[0] in ("a", "z"):
+            if a[1] not in arrays:
+                src = od.get(_fid(a[1])) if a[0] == "a" else np.zeros_like(np.asarray(od.get(_fid(a[1]))))
+                arrays[a[1]] = _widen(case, _fid(a[1]), src, extra)
+            arr = arrays[a[1]][0]
             keep.append(arr)
-            arrays[a[1]] = arr
-            args.append(arr.ctypes.data_as(C.c_void_p))
-        elif a[0] == "z":
-            arr = np.zeros_like(np.asarray(od.get(_fid(a[1])), dtype=np.float32))
-            keep.append(arr)
-            arrays[a[1]] = arr
             args.append(arr.ctypes.data_as(C.c_void_p))
         elif a[0] == "null":
             z = np.zeros(1, np.float32)
@@ -189,6 +210,15 @@ def _call(lib, routine, spec, od, case, scal):
     fn.argtypes = [C.c_void_p] * len(args)
     rc = fn(*args)
     return rc, arrays
+
+
+def _window(arrays, nm):
+    """The standard (halo 4) view of a possibly widened array."""
+    arr, shp = arrays[nm]
+    if shp is None:
+        return arr
+    shape, win = shp
+    return np.ascontiguousarray(arr.reshape(shape)[win]).ravel()
 
 
 def _scalars(case, rk, it):
@@ -224,7 +254,7 @@ def test_routine_abi_bitwise(gpulib, case, routine):
     bad = []
     for nm in outs:
         fid = _fid(nm)
-        a = interior(case, fid, arrays[nm], halo=0)
+        a = interior(case, fid, _window(arrays, nm), halo=0)
         b = interior(case, fid, od.get(fid), halo=0)
         d = max_abs(a, b)
         if d != 0.0:
@@ -232,32 +262,44 @@ def test_routine_abi_bitwise(gpulib, case, routine):
     assert not bad, "%s: %s" % (routine, "; ".join(bad))
 
 
-def test_routine_abi_rejects_tiles(gpulib, case):
-    """A tile smaller than the patch (num_tiles > 1) is refused, not run."""
-    spec, _ = ROUTINES["calc_coef_w"]
-    od = _state(case)
-    scal = _scalars(case, 2, 1)
-    h = abi.HALO
-    fn = gpulib.wrfgpu_calc_coef_w
-    fn.restype = C.c_int
-    # same call with ite = ide - 4
-    keep = []
-    args = []
-    for a in spec:
-        if a[0] == "a":
-            arr = np.ascontiguousarray(od.get(_fid(a[1])), dtype=np.float32)
-            keep.append(arr)
-            args.append(arr.ctypes.data_as(C.c_void_p))
-        elif a[0] == "s":
-            v = C.c_float(scal[a[1]]); keep.append(v); args.append(C.cast(C.pointer(v), C.c_void_p))
-        elif a[0] == "i":
-            v = C.c_int(a[1]); keep.append(v); args.append(C.cast(C.pointer(v), C.c_void_p))
-        elif a[0] == "dims":
-            for d in [1, case.ide, 1, case.jde, 1, case.kde, 1 - h, case.ide + h, 1 - h, case.jde + h, 1, case.kde,
-                      1, case.ide - 4, 1, case.jde, 1, case.kde]:
-                v = C.c_int(d); keep.append(v); args.append(C.cast(C.pointer(v), C.c_void_p))
-    fn.argtypes = [C.c_void_p] * len(args)
-    assert fn(*args) == abi.WRFGPU_E_ARG
+@pytest.mark.parametrize("routine", ["advance_uv", "calc_p_rho", "rk_step_prep", "advance_w", "small_step_finish"])
+def test_routine_abi_tiles_and_wide_halo(gpulib, case, routine):
+    """The routine-level entry points take the memory dims of a wider halo
+    (ims = ids-6: the window ids-4 .. ide+4 is used and the extra halo is
+    left alone) and any tile of the patch (num_tiles > 1: only the tile's
+    points of the outputs come back).  A loop over 2 x 3 tiles on shared
+    arrays, with the wider halo, gives the whole-patch call's outputs bit for
+    bit; a tile outside the patch is refused."""
+    spec, outs = ROUTINES[routine]
+    rk, it = STAGE.get(routine, 2), 1
+    if routine == "small_step_finish":
+        it = 0
+    od = _state(case, full=routine in FULL_STATE)
+    scal = _scalars(case, rk, it)
+    rc, ref = _call(gpulib, routine, spec, od, case, scal)
+    assert rc == 0
+    ib = [1, case.ide // 2, case.ide]
+    jb = [1, case.jde // 3, 2 * case.jde // 3, case.jde]
+    arrays = None
+    for a in range(2):
+        for b in range(3):
+            tile = (ib[a] + (a > 0), ib[a + 1], jb[b] + (b > 0), jb[b + 1])
+            rc, arrays = _call(gpulib, routine, spec, od, case, scal, extra=2, tile=tile, arrays=arrays)
+            assert rc == 0, tile
+    bad = []
+    for nm in outs:
+        if not np.array_equal(_window(arrays, nm), _window(ref, nm)):
+            bad.append(nm)
+        arr, shp = arrays[nm]
+        if shp is not None:
+            shape, win = shp
+            outer = np.ones(shape, bool)
+            outer[win] = False
+            if not np.all(arr.reshape(shape)[outer] == 7777.0):
+                bad.append(nm + " (extra halo)")
+    assert not bad, bad
+    rc, _ = _call(gpulib, routine, spec, od, case, scal, tile=(1, case.ide + 1, 1, case.jde))
+    assert rc == abi.WRFGPU_E_ARG
 
 
 # --------------------------------------------------------------------------

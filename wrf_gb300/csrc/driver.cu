@@ -1024,10 +1024,26 @@ int fortran_call(const FCall& c) {
   const int its = *c.dims[12], ite = *c.dims[13], jts = *c.dims[14], jte = *c.dims[15], kts = *c.dims[16],
             kte = *c.dims[17];
   if (ids != 1 || jds != 1 || kds != 1) return WRFGPU_E_ARG;
-  if (ims != ids - WRFGPU_HALO || ime != ide + WRFGPU_HALO || jms != jds - WRFGPU_HALO || jme != jde + WRFGPU_HALO ||
+  // memory dims: a halo of at least WRFGPU_HALO in i and j (the window
+  // ids-4 .. ide+4 of a wider one is used), the full column in k
+  if (ims > ids - WRFGPU_HALO || ime < ide + WRFGPU_HALO || jms > jds - WRFGPU_HALO || jme < jde + WRFGPU_HALO ||
       kms != kds || kme != kde)
     return WRFGPU_E_ARG;
-  if (its != ids || ite != ide || jts != jds || jte != jde || kts != kds || kte != kde) return WRFGPU_E_ARG;
+  // tile dims: any tile of the patch (the routine runs over the whole patch
+  // and only the tile's points of the outputs are copied back), full columns
+  if (its < ids || ite > ide || its > ite || jts < jds || jte > jde || jts > jte || kts != kds || kte != kde)
+    return WRFGPU_E_ARG;
+  const bool whole = its == ids && ite == ide && jts == jds && jte == jde;
+  const size_t cni = (size_t)(ime - ims + 1), cnk = (size_t)(kme - kms + 1);
+  // the caller's element of (ids - 4, kms, jds - 4) and row length of field id
+  auto host_window = [&](int id, size_t* hcols) -> size_t {
+    const int kind = (id >= WRFGPU_F1D_BASE && id < WRFGPU_F1D_END) ? 1
+                     : (id >= WRFGPU_F2D_BASE && id < WRFGPU_F2D_END) ? 2 : 3;
+    if (kind == 1) { *hcols = 0; return 0; }
+    *hcols = cni;
+    const size_t di = (size_t)(ids - WRFGPU_HALO - ims), dj = (size_t)(jds - WRFGPU_HALO - jms);
+    return di + cni * (kind == 3 ? cnk * dj : dj);
+  };
   if (c.nsp < 1 || c.nsp > NSPMAX) return WRFGPU_E_ARG;
   std::lock_guard<std::mutex> lock(g_fmu);
   // the diffusions' stored tendencies are allocated with the domain
@@ -1075,7 +1091,10 @@ int fortran_call(const FCall& c) {
     size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
     float* p = e->field_ptr(0, b.id, &cnt, &cols, &rows, &pitch);
     if (!p) return WRFGPU_E_ARG;
-    CK(cudaMemcpy2DAsync(p, pitch * 4, b.host, cols * 4, cols * 4, rows, cudaMemcpyHostToDevice, e->stream));
+    size_t hcols = 0;
+    const size_t off = host_window(b.id, &hcols);
+    if (!hcols) hcols = cols;
+    CK(cudaMemcpy2DAsync(p, pitch * 4, b.host + off, hcols * 4, cols * 4, rows, cudaMemcpyHostToDevice, e->stream));
   }
   if (c.zero_saves) {
     for (int f : {WRFGPU_U_SAVE, WRFGPU_V_SAVE, WRFGPU_W_SAVE, WRFGPU_PH_SAVE, WRFGPU_T_SAVE})
@@ -1105,7 +1124,22 @@ int fortran_call(const FCall& c) {
     size_t cnt = 0, cols = 0, rows = 0, pitch = 0;
     float* p = e->field_ptr(0, b.id, &cnt, &cols, &rows, &pitch);
     if (!p) return WRFGPU_E_ARG;
-    CK(cudaMemcpy2DAsync(b.host, cols * 4, p, pitch * 4, cols * 4, rows, cudaMemcpyDeviceToHost, e->stream));
+    size_t hcols = 0;
+    const size_t off = host_window(b.id, &hcols);
+    if (!hcols || whole) {  // the whole window (what the routine leaves alone comes back as it went in)
+      if (!hcols) hcols = cols;
+      CK(cudaMemcpy2DAsync(b.host + off, hcols * 4, p, pitch * 4, cols * 4, rows, cudaMemcpyDeviceToHost,
+                           e->stream));
+      continue;
+    }
+    // only the tile's box its..ite x jts..jte (every level): the points this
+    // tile's call of the reference routine may write
+    const bool f3d = !(b.id >= WRFGPU_F2D_BASE && b.id < WRFGPU_F2D_END);
+    const size_t per_j = f3d ? cnk : 1;  // rows per j, the same on both sides
+    const size_t i0 = (size_t)(its - (ids - WRFGPU_HALO)), j0 = (size_t)(jts - (jds - WRFGPU_HALO));
+    const size_t w = (size_t)(ite - its + 1), h = per_j * (size_t)(jte - jts + 1);
+    CK(cudaMemcpy2DAsync(b.host + off + i0 + hcols * per_j * j0, hcols * 4, p + i0 + pitch * per_j * j0, pitch * 4,
+                         w * 4, h, cudaMemcpyDeviceToHost, e->stream));
   }
   CK(cudaStreamSynchronize(e->stream));
   return WRFGPU_OK;

@@ -24,13 +24,18 @@
  * It is meant for routine-by-routine verification inside an unmodified
  * solve_em; the fast path is the device-resident domain API of wrfgpu.h.
  *
- * Index conventions accepted: ids = jds = kds = 1; the memory dimensions of
- * the serial build, ims = ids-4, ime = ide+4 (same in j), kms = kds,
- * kme = kde; one tile covering the patch (its = ids, ite = ide, jts = jds,
- * jte = jde, kts = kds, kte = kde: solve_em with num_tiles = 1).  Anything
- * else returns WRFGPU_E_ARG.  The options accepted are those of
- * wrfgpu_ensemble_create.  Return: 0 or a negative WRFGPU_E_* code (the
- * reference aborts through wrf_error_fatal instead).
+ * Index conventions accepted: ids = jds = kds = 1 and one patch covering
+ * the domain; memory dimensions with a halo of at least 4 in i and j
+ * (ims <= ids-4, ime >= ide+4, same in j: the window ids-4 .. ide+4 is used
+ * and a wider halo is left as it is) and kms = kds, kme = kde; any tile of
+ * the patch (ids <= its <= ite <= ide, same in j, kts = kds, kte = kde: the
+ * OpenMP tiles of solve_em's tile loops), for which the routine runs over the
+ * patch and only the tile's points of the output arrays are written back
+ * (a whole-patch tile writes back the whole window).  Anything else returns
+ * WRFGPU_E_ARG; max_vert_cfl / max_horiz_cfl are the patch's maxima.  The
+ * options accepted are those of wrfgpu_ensemble_create.  Return: 0 or a
+ * negative WRFGPU_E_* code (the reference aborts through wrf_error_fatal
+ * instead).
  */
 #ifndef WRFGPU_FORTRAN_H
 #define WRFGPU_FORTRAN_H

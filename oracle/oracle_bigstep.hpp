@@ -245,16 +245,19 @@ void zero_tend2d(R* t_p, const Dims& d) {
 }
 
 // module_big_step_utilities_em.F:1365-2178 rhs_ph, phi_adv_z 1/2 vertical
-// term, "gw" term and the advective_order <= 6 horizontal branch
-// (:1768-1930 y, :1930-2075 x) for periodic / symmetric boundaries.
+// term, "gw" term, the advective_order <= 6 horizontal branch (:1768-1930 y,
+// :1930-2075 x; next to an open boundary 4th- and 2nd-order stencils) and the
+// open-boundary terms (:2077-2176).
 template <typename R>
 void rhs_ph(R* ph_tend_p, R* u_p, R* v_p, R* ww_p, R* ph_p, R* ph_old_p, R* phb_p, R* w_p, R* mut_p,
             R* muuf_p, R* muvf_p, R* c1f_p, R* c2f_p, R* fnm_p, R* fnp_p, R* rdnw_p, R cfn, R cfn1, R rdx,
             R rdy, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p,
             int non_hydrostatic, const WrfDynConfig& cf, const Dims& d) {
-  (void)ph_old_p; (void)msfuy_p; (void)msfvx_p; (void)msfvx_inv_p; (void)msftx_p;
-  A3<R> ph_tend(ph_tend_p, d), u(u_p, d), v(v_p, d), ww(ww_p, d), ph(ph_p, d), phb(phb_p, d), w(w_p, d);
-  A2<R> mut(mut_p, d), muuf(muuf_p, d), muvf(muvf_p, d), msfux(msfux_p, d), msfvy(msfvy_p, d), msfty(msfty_p, d);
+  (void)msfuy_p; (void)msfvx_p; (void)msfvx_inv_p;
+  A3<R> ph_tend(ph_tend_p, d), u(u_p, d), v(v_p, d), ww(ww_p, d), ph(ph_p, d), ph_old(ph_old_p, d), phb(phb_p, d),
+      w(w_p, d);
+  A2<R> mut(mut_p, d), muuf(muuf_p, d), muvf(muvf_p, d), msfux(msfux_p, d), msfvy(msfvy_p, d), msftx(msftx_p, d),
+      msfty(msfty_p, d);
   A1<R> c1f(c1f_p, d), c2f(c2f_p, d), fnm(fnm_p, d), fnp(fnp_p, d), rdnw(rdnw_p, d);
   const R g = K<R>::g;
   int itf = std::min(d.ite, d.ide - 1), jtf = std::min(d.jte, d.jde - 1);
@@ -288,56 +291,135 @@ void rhs_ph(R* ph_tend_p, R* u_p, R* v_p, R* ww_p, R* ph_p, R* ph_old_p, R* phb_
           ph_tend(i, k, j) = ph_tend(i, k, j) + (c1f(k) * mut(i, j) + c2f(k)) * g * w(i, k, j) / msfty(i, j);
     }
   }
-  // y (v) advection, 6th-order centred stencil on ph+phb.
-  itf = std::min(d.ite, d.ide - 1); jtf = std::min(d.jte, d.jde - 1);
-  for (int j = d.jts; j <= jtf; ++j) {
-    for (int k = 2; k <= kte - 1; ++k)
-      for (int i = d.its; i <= itf; ++i) {
-        ph_tend(i, k, j) = ph_tend(i, k, j) -
-            (R(0.25) * rdy / msfty(i, j)) *
-                (((c1f(k) * muvf(i, j + 1) + c2f(k)) * (v(i, k, j + 1) + v(i, k - 1, j + 1)) * msfvy(i, j + 1) +
-                  (c1f(k) * muvf(i, j) + c2f(k)) * (v(i, k, j) + v(i, k - 1, j)) * msfvy(i, j)) *
-                 (R(1.) / R(60.)) *
-                 (R(45.) * (ph(i, k, j + 1) - ph(i, k, j - 1)) - R(9.) * (ph(i, k, j + 2) - ph(i, k, j - 2)) +
-                  (ph(i, k, j + 3) - ph(i, k, j - 3)) + R(45.) * (phb(i, k, j + 1) - phb(i, k, j - 1)) -
-                  R(9.) * (phb(i, k, j + 2) - phb(i, k, j - 2)) + (phb(i, k, j + 3) - phb(i, k, j - 3))));
-      }
-    int k = kte;
-    for (int i = d.its; i <= itf; ++i) {
+  const int ids = d.ids, ide = d.ide, jds = d.jds, jde = d.jde;
+  // y (v) advection: the 6th-order centred stencil on ph+phb, 4th order two
+  // rows and 2nd order one row in from an open boundary.
+  auto yterm = [&](int i, int k, int j, int order) {
+    const bool top = k == kte;
+    auto vv = [&](int jj) -> R {
+      return top ? (cfn * v(i, k - 1, jj) + cfn1 * v(i, k - 2, jj)) : (v(i, k, jj) + v(i, k - 1, jj));
+    };
+    const R cy = (top ? R(0.5) : R(0.25)) * rdy / msfty(i, j);
+    const R fp = (c1f(k) * muvf(i, j + 1) + c2f(k)) * vv(j + 1) * msfvy(i, j + 1);
+    const R fm = (c1f(k) * muvf(i, j) + c2f(k)) * vv(j) * msfvy(i, j);
+    if (order == 6)
       ph_tend(i, k, j) = ph_tend(i, k, j) -
-          (R(0.5) * rdy / msfty(i, j)) *
-              (((c1f(k) * muvf(i, j + 1) + c2f(k)) * (cfn * v(i, k - 1, j + 1) + cfn1 * v(i, k - 2, j + 1)) * msfvy(i, j + 1) +
-                (c1f(k) * muvf(i, j) + c2f(k)) * (cfn * v(i, k - 1, j) + cfn1 * v(i, k - 2, j)) * msfvy(i, j)) *
-               (R(1.) / R(60.)) *
-               (R(45.) * (ph(i, k, j + 1) - ph(i, k, j - 1)) - R(9.) * (ph(i, k, j + 2) - ph(i, k, j - 2)) +
-                (ph(i, k, j + 3) - ph(i, k, j - 3)) + R(45.) * (phb(i, k, j + 1) - phb(i, k, j - 1)) -
-                R(9.) * (phb(i, k, j + 2) - phb(i, k, j - 2)) + (phb(i, k, j + 3) - phb(i, k, j - 3))));
-    }
+          cy * ((fp + fm) * (R(1.) / R(60.)) *
+                (R(45.) * (ph(i, k, j + 1) - ph(i, k, j - 1)) - R(9.) * (ph(i, k, j + 2) - ph(i, k, j - 2)) +
+                 (ph(i, k, j + 3) - ph(i, k, j - 3)) + R(45.) * (phb(i, k, j + 1) - phb(i, k, j - 1)) -
+                 R(9.) * (phb(i, k, j + 2) - phb(i, k, j - 2)) + (phb(i, k, j + 3) - phb(i, k, j - 3))));
+    else if (order == 4)
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          cy * ((fp + fm) * (R(1.) / R(12.)) *
+                (R(8.) * (ph(i, k, j + 1) - ph(i, k, j - 1)) - (ph(i, k, j + 2) - ph(i, k, j - 2)) +
+                 R(8.) * (phb(i, k, j + 1) - phb(i, k, j - 1)) - (phb(i, k, j + 2) - phb(i, k, j - 2))));
+    else
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          cy * (fp * (phb(i, k, j + 1) - phb(i, k, j) + ph(i, k, j + 1) - ph(i, k, j)) +
+                fm * (phb(i, k, j) - phb(i, k, j - 1) + ph(i, k, j) - ph(i, k, j - 1)));
+  };
+  auto xterm = [&](int i, int k, int j, int order) {
+    const bool top = k == kte;
+    auto uu = [&](int ii) -> R {
+      return top ? (cfn * u(ii, k - 1, j) + cfn1 * u(ii, k - 2, j)) : (u(ii, k, j) + u(ii, k - 1, j));
+    };
+    const R cx = (top ? R(0.5) : R(0.25)) * rdx / msfty(i, j);
+    const R fp = (c1f(k) * muuf(i + 1, j) + c2f(k)) * uu(i + 1) * msfux(i + 1, j);
+    const R fm = (c1f(k) * muuf(i, j) + c2f(k)) * uu(i) * msfux(i, j);
+    if (order == 6)
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          cx * ((fp + fm) * (R(1.) / R(60.)) *
+                (R(45.) * (ph(i + 1, k, j) - ph(i - 1, k, j)) - R(9.) * (ph(i + 2, k, j) - ph(i - 2, k, j)) +
+                 (ph(i + 3, k, j) - ph(i - 3, k, j)) + R(45.) * (phb(i + 1, k, j) - phb(i - 1, k, j)) -
+                 R(9.) * (phb(i + 2, k, j) - phb(i - 2, k, j)) + (phb(i + 3, k, j) - phb(i - 3, k, j))));
+    else if (order == 4)
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          cx * ((fp + fm) * (R(1.) / R(12.)) *
+                (R(8.) * (ph(i + 1, k, j) - ph(i - 1, k, j)) - (ph(i + 2, k, j) - ph(i - 2, k, j)) +
+                 R(8.) * (phb(i + 1, k, j) - phb(i - 1, k, j)) - (phb(i + 2, k, j) - phb(i - 2, k, j))));
+    else
+      ph_tend(i, k, j) = ph_tend(i, k, j) -
+          cx * (fp * (phb(i + 1, k, j) - phb(i, k, j) + ph(i + 1, k, j) - ph(i, k, j)) +
+                fm * (phb(i, k, j) - phb(i - 1, k, j) + ph(i, k, j) - ph(i - 1, k, j)));
+  };
+  itf = std::min(d.ite, ide - 1); jtf = std::min(d.jte, jde - 1);
+  {
+    int j_start = d.jts, jtf_y = jtf;
+    if (cf.open_ys) j_start = std::max(d.jts, jds + 3);
+    if (cf.open_ye) jtf_y = std::min(jtf_y, jde - 4);
+    for (int j = j_start; j <= jtf_y; ++j)
+      for (int k = 2; k <= kte; ++k)
+        for (int i = d.its; i <= itf; ++i) yterm(i, k, j, 6);
+    auto row = [&](int j, int order) {
+      for (int k = 2; k <= kte; ++k)
+        for (int i = d.its; i <= itf; ++i) yterm(i, k, j, order);
+    };
+    if (cf.open_ys && d.jts <= jds + 2 && jds + 2 <= d.jte) row(jds + 2, 4);
+    if (cf.open_ye && d.jts <= jde - 3 && jde - 3 <= d.jte) row(jde - 3, 4);
+    if (cf.open_ys && d.jts <= jds + 1 && jds + 1 <= d.jte) row(jds + 1, 2);
+    if (cf.open_ye && d.jts <= jde - 2 && jde - 2 <= d.jte) row(jde - 2, 2);
   }
   // x (u) advection.
-  for (int j = d.jts; j <= jtf; ++j) {
-    for (int k = 2; k <= kte - 1; ++k)
+  {
+    int i_start = d.its, itf_x = itf;
+    if (cf.open_xs) i_start = std::max(d.its, ids + 3);
+    if (cf.open_xe) itf_x = std::min(itf_x, ide - 4);
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = 2; k <= kte; ++k)
+        for (int i = i_start; i <= itf_x; ++i) xterm(i, k, j, 6);
+    auto col = [&](int i, int order) {
+      for (int j = d.jts; j <= jtf; ++j)
+        for (int k = 2; k <= kte; ++k) xterm(i, k, j, order);
+    };
+    if (cf.open_xs && d.its <= ids + 2 && ids + 2 <= d.ite) col(ids + 2, 4);
+    if (cf.open_xe && d.its <= ide - 3 && ide - 3 <= d.ite) col(ide - 3, 4);
+    if (cf.open_xs && d.its <= ids + 1 && ids + 1 <= d.ite) col(ids + 1, 2);
+    if (cf.open_xe && d.its <= ide - 2 && ide - 2 <= d.ite) col(ide - 2, 2);
+  }
+  // lateral open boundary conditions: north and south, then east and west
+  if (cf.open_ys && d.jts == jds) {
+    const int j = d.jts;
+    for (int k = 2; k <= kde; ++k) {
+      const int kz = std::min(k, kde - 1);
       for (int i = d.its; i <= itf; ++i) {
-        ph_tend(i, k, j) = ph_tend(i, k, j) -
-            (R(0.25) * rdx / msfty(i, j)) *
-                (((c1f(k) * muuf(i + 1, j) + c2f(k)) * (u(i + 1, k, j) + u(i + 1, k - 1, j)) * msfux(i + 1, j) +
-                  (c1f(k) * muuf(i, j) + c2f(k)) * (u(i, k, j) + u(i, k - 1, j)) * msfux(i, j)) *
-                 (R(1.) / R(60.)) *
-                 (R(45.) * (ph(i + 1, k, j) - ph(i - 1, k, j)) - R(9.) * (ph(i + 2, k, j) - ph(i - 2, k, j)) +
-                  (ph(i + 3, k, j) - ph(i - 3, k, j)) + R(45.) * (phb(i + 1, k, j) - phb(i - 1, k, j)) -
-                  R(9.) * (phb(i + 2, k, j) - phb(i - 2, k, j)) + (phb(i + 3, k, j) - phb(i - 3, k, j))));
+        R vb = R(.5) * (fnm(kz) * (v(i, kz, j + 1) + v(i, kz, j)) + fnp(kz) * (v(i, kz - 1, j + 1) + v(i, kz - 1, j)));
+        R vl = fminr(vb, R(0.));
+        ph_tend(i, k, j) = ph_tend(i, k, j) - rdy * (c1f(k) * mut(i, j) + c2f(k)) * (vl * (ph_old(i, k, j + 1) - ph_old(i, k, j)));
       }
-    int k = kte;
-    for (int i = d.its; i <= itf; ++i) {
-      ph_tend(i, k, j) = ph_tend(i, k, j) -
-          (R(0.5) * rdx / msfty(i, j)) *
-              (((c1f(k) * muuf(i + 1, j) + c2f(k)) * (cfn * u(i + 1, k - 1, j) + cfn1 * u(i + 1, k - 2, j)) * msfux(i + 1, j) +
-                (c1f(k) * muuf(i, j) + c2f(k)) * (cfn * u(i, k - 1, j) + cfn1 * u(i, k - 2, j)) * msfux(i, j)) *
-               (R(1.) / R(60.)) *
-               (R(45.) * (ph(i + 1, k, j) - ph(i - 1, k, j)) - R(9.) * (ph(i + 2, k, j) - ph(i - 2, k, j)) +
-                (ph(i + 3, k, j) - ph(i - 3, k, j)) + R(45.) * (phb(i + 1, k, j) - phb(i - 1, k, j)) -
-                R(9.) * (phb(i + 2, k, j) - phb(i - 2, k, j)) + (phb(i + 3, k, j) - phb(i - 3, k, j))));
     }
+  }
+  if (cf.open_ye && d.jte == jde) {
+    const int j = d.jte - 1;
+    for (int k = 2; k <= kde; ++k) {
+      const int kz = std::min(k, kde - 1);
+      for (int i = d.its; i <= itf; ++i) {
+        R vb = R(.5) * (fnm(kz) * (v(i, kz, j + 1) + v(i, kz, j)) + fnp(kz) * (v(i, kz - 1, j + 1) + v(i, kz - 1, j)));
+        R vr = fmaxr(vb, R(0.));
+        ph_tend(i, k, j) = ph_tend(i, k, j) - rdy * (c1f(k) * mut(i, j) + c2f(k)) * (vr * (ph_old(i, k, j) - ph_old(i, k, j - 1)));
+      }
+    }
+  }
+  if (cf.open_xs && d.its == ids) {
+    const int i = d.its;
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = 2; k <= kde; ++k) {
+        const int kz = k;  // the top level too (module_big_step_utilities_em.F:2137-2139)
+        R ub = R(.5) * (fnm(kz) * (u(i + 1, kz, j) + u(i, kz, j)) + fnp(kz) * (u(i + 1, kz - 1, j) + u(i, kz - 1, j)));
+        R ul = fminr(ub, R(0.));
+        ph_tend(i, k, j) = ph_tend(i, k, j) - (msftx(i, j) / msfty(i, j)) * rdx * (c1f(k) * mut(i, j) + c2f(k)) *
+                                                  (ul * (ph_old(i + 1, k, j) - ph_old(i, k, j)));
+      }
+  }
+  if (cf.open_xe && d.ite == ide) {
+    const int i = d.ite - 1;
+    for (int j = d.jts; j <= jtf; ++j)
+      for (int k = 2; k <= kde; ++k) {
+        const int kz = k < kde ? k : kde - 1;  // :2163-2164
+        R ub = R(.5) * (fnm(kz) * (u(i + 1, kz, j) + u(i, kz, j)) + fnp(kz) * (u(i + 1, kz - 1, j) + u(i, kz - 1, j)));
+        R ur = fmaxr(ub, R(0.));
+        ph_tend(i, k, j) = ph_tend(i, k, j) - (msftx(i, j) / msfty(i, j)) * rdx * (c1f(k) * mut(i, j) + c2f(k)) *
+                                                  (ur * (ph_old(i, k, j) - ph_old(i - 1, k, j)));
+      }
   }
 }
 
@@ -362,7 +444,9 @@ void horizontal_pressure_gradient(R* ru_tend_p, R* rv_tend_p, R* ph_p, R* alt_p,
   const int kde = d.kde;
   int itf = std::min(d.ite, d.ide - 1), jtf = d.jte, ktf = std::min(d.kte, d.kde - 1);
   int i_start = d.its, j_start = d.jts;
-  (void)cf;
+  // module_big_step_utilities_em.F:2273-2276
+  if (cf.open_ys && d.jts == d.jds) j_start = d.jts + 1;
+  if (cf.open_ye && d.jte == d.jde) jtf = jtf - 1;
   for (int j = j_start; j <= jtf; ++j) {
     int k = 1;
     for (int i = i_start; i <= itf; ++i) {
@@ -388,6 +472,11 @@ void horizontal_pressure_gradient(R* ru_tend_p, R* rv_tend_p, R* ph_p, R* alt_p,
       }
   }
   itf = d.ite; jtf = std::min(d.jte, d.jde - 1);
+  i_start = d.its; j_start = d.jts;
+  // :2346-2351
+  if (cf.open_xs && d.its == d.ids) i_start = d.its + 1;
+  if (cf.open_xe && d.ite == d.ide) itf = itf - 1;
+  if (cf.periodic_x) { i_start = d.its; itf = d.ite; }
   for (int j = j_start; j <= jtf; ++j) {
     int k = 1;
     for (int i = i_start; i <= itf; ++i) {
@@ -479,13 +568,16 @@ template <typename R>
 void coriolis(R* ru_p, R* rv_p, R* rw_p, R* ru_tend_p, R* rv_tend_p, R* rw_tend_p, const WrfDynConfig& cf,
               R* msftx_p, R* msfty_p, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvy_p, R* f_p, R* e_p, R* sina_p,
               R* cosa_p, R* fzm_p, R* fzp_p, const Dims& d) {
-  (void)cf;
   A3<R> ru(ru_p, d), rv(rv_p, d), rw(rw_p, d), ru_tend(ru_tend_p, d), rv_tend(rv_tend_p, d), rw_tend(rw_tend_p, d);
   A2<R> msftx(msftx_p, d), msfty(msfty_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx(msfvx_p, d),
       msfvy(msfvy_p, d), f(f_p, d), e(e_p, d), sina(sina_p, d), cosa(cosa_p, d);
   A1<R> fzm(fzm_p, d), fzp(fzp_p, d);
   int ktf = std::min(d.kte, d.kde - 1);
   int i_start = d.its, i_end = d.ite;
+  // module_big_step_utilities_em.F:3710-3717
+  if (cf.open_xs) i_start = std::max(d.ids + 1, d.its);
+  if (cf.open_xe) i_end = std::min(d.ide - 1, d.ite);
+  if (cf.periodic_x) { i_start = d.its; i_end = d.ite; }
   for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
     for (int k = d.kts; k <= ktf; ++k)
       for (int i = i_start; i <= i_end; ++i)
@@ -495,6 +587,9 @@ void coriolis(R* ru_p, R* rv_p, R* rw_p, R* ru_tend_p, R* rv_tend_p, R* rw_tend_
                            R(0.5) * (e(i, j) + e(i - 1, j)) * R(0.5) * (cosa(i, j) + cosa(i - 1, j)) * R(0.25) *
                                (rw(i - 1, k + 1, j) + rw(i - 1, k, j) + rw(i, k + 1, j) + rw(i, k, j));
   int j_start = d.jts, j_end = d.jte;
+  // :3765-3768
+  if (cf.open_ys) j_start = std::max(d.jds + 1, d.jts);
+  if (cf.open_ye) j_end = std::min(d.jde - 1, d.jte);
   for (int j = j_start; j <= j_end; ++j)
     for (int k = d.kts; k <= ktf; ++k)
       for (int i = d.its; i <= std::min(d.ide - 1, d.ite); ++i)
@@ -519,7 +614,7 @@ template <typename R>
 void curvature(R* ru_p, R* rv_p, R* rw_p, R* u_p, R* v_p, R* w_p, R* ru_tend_p, R* rv_tend_p, R* rw_tend_p,
                const WrfDynConfig& cf, R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvy_p, R* msftx_p, R* msfty_p,
                R* xlat_p, R* fzm_p, R* fzp_p, R rdx, R rdy, const Dims& d) {
-  (void)cf; (void)w_p; (void)xlat_p; (void)msfux_p;
+  (void)w_p; (void)xlat_p; (void)msfux_p;
   A3<R> ru(ru_p, d), rv(rv_p, d), rw(rw_p, d), u(u_p, d), v(v_p, d), ru_tend(ru_tend_p, d),
       rv_tend(rv_tend_p, d), rw_tend(rw_tend_p, d);
   A2<R> msfuy(msfuy_p, d), msfvx(msfvx_p, d), msfvy(msfvy_p, d), msftx(msftx_p, d), msfty(msfty_p, d);
@@ -531,12 +626,22 @@ void curvature(R* ru_p, R* rv_p, R* rw_p, R* u_p, R* v_p, R* w_p, R* ru_tend_p, 
   std::vector<R> vx_s((size_t)nx * (d.kme - d.kms + 1) * (d.jme - d.jms + 1));
   A3<R> vxgm(vx_s.data(), d);
   int i_start = d.its - 1, i_end = d.ite, j_start = d.jts - 1, j_end = d.jte;
+  // module_big_step_utilities_em.F:4262-4271
+  if (cf.open_xs && d.its == d.ids) i_start = d.its;
+  if (cf.open_xe && d.ite == d.ide) i_end = d.ite - 1;
+  if (cf.open_ys && d.jts == d.jds) j_start = d.jts;
+  if (cf.open_ye && d.jte == d.jde) j_end = d.jte - 1;
+  if (cf.periodic_x) { i_start = d.its - 1; i_end = d.ite; }
   for (int j = j_start; j <= j_end; ++j)
     for (int k = d.kts; k <= ktf; ++k)
       for (int i = i_start; i <= i_end; ++i)
         vxgm(i, k, j) = R(0.5) * (u(i, k, j) + u(i + 1, k, j)) * (msfvx(i, j + 1) - msfvx(i, j)) * rdy -
                         R(0.5) * (v(i, k, j) + v(i, k, j + 1)) * (msfuy(i + 1, j) - msfuy(i, j)) * rdx;
-  i_start = d.its; i_end = d.ite;
+  // :4292-4298 (i_end keeps the vxgm bound unless open_xe narrows it)
+  i_start = d.its;
+  if (cf.open_xs) i_start = std::max(d.ids + 1, d.its);
+  if (cf.open_xe) i_end = std::min(d.ide - 1, d.ite);
+  if (cf.periodic_x) { i_start = d.its; i_end = d.ite; }
   for (int j = d.jts; j <= std::min(d.jde - 1, d.jte); ++j)
     for (int k = d.kts; k <= ktf; ++k)
       for (int i = i_start; i <= i_end; ++i)
@@ -545,7 +650,10 @@ void curvature(R* ru_p, R* rv_p, R* rw_p, R* u_p, R* v_p, R* w_p, R* ru_tend_p, 
                                (rv(i - 1, k, j + 1) + rv(i, k, j + 1) + rv(i - 1, k, j) + rv(i, k, j)) -
                            u(i, k, j) * reradius * R(0.25) *
                                (rw(i - 1, k + 1, j) + rw(i - 1, k, j) + rw(i, k + 1, j) + rw(i, k, j));
+  // :4352-4356 (j_end keeps the vxgm bound unless open_ye narrows it)
   j_start = d.jts;
+  if (cf.open_ys) j_start = std::max(d.jds + 1, d.jts);
+  if (cf.open_ye) j_end = std::min(d.jde - 1, d.jte);
   for (int j = j_start; j <= j_end; ++j)
     for (int k = d.kts; k <= ktf; ++k)
       for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i)

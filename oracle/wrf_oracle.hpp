@@ -24,7 +24,8 @@
 //
 // Supported option subset (anything else is rejected, like wrf_error_fatal):
 //   rk_ord=3, h_*_adv_order=5, v_*_adv_order=3, non_hydrostatic=.true.,
-//   periodic_x/periodic_y or symmetric_xs/xe/ys/ye lateral boundaries,
+//   periodic_x/periodic_y, symmetric_xs/xe/ys/ye or open_xs/xe/ys/ye lateral
+//   boundaries (open ones without diffusion),
 //   moist_adv_opt/scalar_adv_opt in {0 (ORIGINAL), 1 (POSITIVEDEF)},
 //   hypsometric_opt in {1,2}, phi_adv_z in {1,2}, IEVA off, physics off.
 #pragma once
@@ -132,18 +133,31 @@ inline void check_config(const WrfDynConfig& c) {
   if (c.h_mom_adv_order != 5 || c.h_sca_adv_order != 5) throw std::runtime_error("horizontal advection order must be 5");
   if (c.v_mom_adv_order != 3 || c.v_sca_adv_order != 3) throw std::runtime_error("vertical advection order must be 3");
   if (!c.non_hydrostatic) throw std::runtime_error("hydrostatic option not supported");
-  if (c.open_xs || c.open_xe || c.open_ys || c.open_ye || c.specified || c.nested || c.polar)
-    throw std::runtime_error("open/specified/nested/polar boundaries not supported");
+  if (c.specified || c.nested || c.polar) throw std::runtime_error("specified/nested/polar boundaries not supported");
+  // share/module_bc.F:60-133 boundary_condition_check: one condition per side.
+  auto one = [](int a, int b, int e) { return (a != 0) + (b != 0) + (e != 0) == 1; };
+  if (!one(c.periodic_x, c.symmetric_xs, c.open_xs) || !one(c.periodic_x, c.symmetric_xe, c.open_xe) ||
+      !one(c.periodic_y, c.symmetric_ys, c.open_ys) || !one(c.periodic_y, c.symmetric_ye, c.open_ye))
+    throw std::runtime_error("each lateral boundary needs exactly one condition");
+  if ((c.open_xs || c.open_xe || c.open_ys || c.open_ye) && (c.diff_opt != 0 || c.diff_6th_opt != 0))
+    throw std::runtime_error("open boundaries with explicit or sixth-order diffusion not supported");
   if (c.zadvect_implicit != 0) throw std::runtime_error("IEVA not supported");
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) throw std::runtime_error("diff_6th_opt must be 0, 1 or 2");
 }
 
 // ===========================================================================
 // share/module_bc.F — set_physical_bc2d (:202-649) and set_physical_bc3d
-// (:651-1000), restricted to periodic and symmetric boundaries
+// (:651-1000), restricted to periodic, symmetric and open boundaries
 // (bdyzone = 4, :33).  The serial build has one patch (ips=ids, ipe=ide).
 // ===========================================================================
 static const int BDYZONE = 4;
+
+// open_bc_copy: the variables whose halo takes the open-boundary copy,
+// set_physical_bc2d (module_bc.F:242-251) and set_physical_bc3d (:692-704).
+inline bool open_bc_copy2(char v) {
+  return v == 'u' || v == 'v' || v == 'w' || v == 't' || v == 'x' || v == 'y' || v == 'r' || v == 'p';
+}
+inline bool open_bc_copy3(char v) { return open_bc_copy2(v) || v == 'd' || v == 'e' || v == 'f'; }
 
 template <typename R>
 void set_physical_bc3d(R* dat_p, char variable_in, const WrfDynConfig& cf, const Dims& d) {
@@ -189,6 +203,33 @@ void set_physical_bc3d(R* dat_p, char variable_in, const WrfDynConfig& cf, const
             else dat(ide + i, k, j) = dat(ide - i, k, j);
           }
     }
+    // module_bc.F:864-925: open boundaries copy the edge value into three
+    // halo points, for the variables of open_bc_copy (:692-704).
+    if (cf.open_xs && d.its == ids && open_bc_copy3(variable)) {
+      for (int j = d.jts - BDYZONE; j <= std::min(d.jte, jde + jstag) + BDYZONE; ++j)
+        for (int k = d.kts; k <= k_end; ++k) {
+          dat(ids - 1, k, j) = dat(ids, k, j);
+          dat(ids - 2, k, j) = dat(ids, k, j);
+          dat(ids - 3, k, j) = dat(ids, k, j);
+        }
+    }
+    if (cf.open_xe && d.ite == ide && open_bc_copy3(variable)) {
+      if (variable != 'u' && variable != 'x') {
+        for (int j = d.jts - BDYZONE; j <= std::min(d.jte, jde + jstag) + BDYZONE; ++j)
+          for (int k = d.kts; k <= k_end; ++k) {
+            dat(ide, k, j) = dat(ide - 1, k, j);
+            dat(ide + 1, k, j) = dat(ide - 1, k, j);
+            dat(ide + 2, k, j) = dat(ide - 1, k, j);
+          }
+      } else {
+        for (int j = std::max(jds, d.jts - 1) - BDYZONE; j <= std::min(d.jte + 1, jde + jstag) + BDYZONE; ++j)
+          for (int k = d.kts; k <= k_end; ++k) {
+            dat(ide + 1, k, j) = dat(ide, k, j);
+            dat(ide + 2, k, j) = dat(ide, k, j);
+            dat(ide + 3, k, j) = dat(ide, k, j);
+          }
+      }
+    }
   }
   int i_start = std::max(ids, d.its - 1), i_end = std::min(d.ite + 1, ide + istag);
   if (d.its == ids) i_start = d.ims;
@@ -222,6 +263,32 @@ void set_physical_bc3d(R* dat_p, char variable_in, const WrfDynConfig& cf, const
             else if (variable == 'v') dat(i, k, jde + j) = -dat(i, k, jde - j);
             else dat(i, k, jde + j) = dat(i, k, jde - j);
           }
+    }
+    // module_bc.F:1059-1107
+    if (cf.open_ys && d.jts == jds && open_bc_copy3(variable)) {
+      for (int k = d.kts; k <= k_end; ++k)
+        for (int i = i_start; i <= i_end; ++i) {
+          dat(i, k, jds - 1) = dat(i, k, jds);
+          dat(i, k, jds - 2) = dat(i, k, jds);
+          dat(i, k, jds - 3) = dat(i, k, jds);
+        }
+    }
+    if (cf.open_ye && d.jte == jde && open_bc_copy3(variable)) {
+      if (variable != 'v' && variable != 'y') {
+        for (int k = d.kts; k <= k_end; ++k)
+          for (int i = i_start; i <= i_end; ++i) {
+            dat(i, k, jde) = dat(i, k, jde - 1);
+            dat(i, k, jde + 1) = dat(i, k, jde - 1);
+            dat(i, k, jde + 2) = dat(i, k, jde - 1);
+          }
+      } else {
+        for (int k = d.kts; k <= k_end; ++k)
+          for (int i = i_start; i <= i_end; ++i) {
+            dat(i, k, jde + 1) = dat(i, k, jde);
+            dat(i, k, jde + 2) = dat(i, k, jde);
+            dat(i, k, jde + 3) = dat(i, k, jde);
+          }
+      }
     }
   }
   // (The 3-D fill has no separate corner pass: the y pass above copies whole
@@ -271,6 +338,26 @@ void set_physical_bc2d(R* dat_p, char variable_in, const WrfDynConfig& cf, const
         }
       }
     }
+    // module_bc.F:386-427
+    if (cf.open_xs && d.its == ids && open_bc_copy2(variable))
+      for (int j = std::max(jds, d.jts - 1); j <= std::min(d.jte + 1, jde + jstag); ++j) {
+        dat(ids - 1, j) = dat(ids, j);
+        dat(ids - 2, j) = dat(ids, j);
+        dat(ids - 3, j) = dat(ids, j);
+      }
+    if (cf.open_xe && d.ite == ide && open_bc_copy2(variable)) {
+      for (int j = std::max(jds, d.jts - 1); j <= std::min(d.jte + 1, jde + jstag); ++j) {
+        if (variable != 'u' && variable != 'x') {
+          dat(ide, j) = dat(ide - 1, j);
+          dat(ide + 1, j) = dat(ide - 1, j);
+          dat(ide + 2, j) = dat(ide - 1, j);
+        } else {
+          dat(ide + 1, j) = dat(ide, j);
+          dat(ide + 2, j) = dat(ide, j);
+          dat(ide + 3, j) = dat(ide, j);
+        }
+      }
+    }
   }
   int istart = std::max(ids, d.its - 1), iend = std::min(d.ite + 1, ide + istag);
   if (d.its == ids) istart = d.ims;
@@ -297,6 +384,25 @@ void set_physical_bc2d(R* dat_p, char variable_in, const WrfDynConfig& cf, const
           else if (variable == 'v') dat(i, jde + j) = -dat(i, jde - j);
           else dat(i, jde + j) = dat(i, jde - j);
         }
+    // module_bc.F:558-601
+    if (cf.open_ys && d.jts == jds && open_bc_copy2(variable))
+      for (int i = istart; i <= iend; ++i) {
+        dat(i, jds - 1) = dat(i, jds);
+        dat(i, jds - 2) = dat(i, jds);
+        dat(i, jds - 3) = dat(i, jds);
+      }
+    if (cf.open_ye && d.jte == jde && open_bc_copy2(variable))
+      for (int i = istart; i <= iend; ++i) {
+        if (variable != 'v' && variable != 'y') {
+          dat(i, jde) = dat(i, jde - 1);
+          dat(i, jde + 1) = dat(i, jde - 1);
+          dat(i, jde + 2) = dat(i, jde - 1);
+        } else {
+          dat(i, jde + 1) = dat(i, jde);
+          dat(i, jde + 2) = dat(i, jde);
+          dat(i, jde + 3) = dat(i, jde);
+        }
+      }
   }
   if (cf.periodic_x && cf.periodic_y) {
     if (d.its == ids && d.jts == jds)

@@ -424,3 +424,115 @@ def test_explicit_diffusion_of_uniform_fields_is_zero():
     od.run("sixth_diff_species", 1, 0, 1)
     got = interior(c, fid, od.get(fid))[:, :-1, :]  # mass levels 1..kde-1
     assert np.all(got == 0.0), np.abs(got).max()
+
+
+# ---------------------------------------------------------------------------
+# open lateral boundaries (em_quarter_ss: open_xs/xe/ys/ye)
+# ---------------------------------------------------------------------------
+OPEN_SIDES = [(True, True), (True, False), (False, True)]
+
+
+@pytest.mark.parametrize("x,y", OPEN_SIDES)
+def test_open_boundaries_tiling_does_not_change_bits(x, y):
+    """The degrade flags and the radiation rows depend on the tile's own
+    bounds (module_advect_em.F:500-516, its/jts against ids/jds); j-slab tiles
+    must reproduce the one-tile result bit for bit."""
+    case = cases.open_boundaries(cases.small_case(nx=20, ny=18, kde=12, n_scalar=2, seed=12), x=x, y=y)
+    a = OracleDomain(case, "f32", nthreads=1)
+    b = OracleDomain(case, "f32", nthreads=4)
+    a.step(3)
+    b.step(3)
+    for nm in ("u_2", "v_2", "w_2", "t_2", "ph_2", "mu_2", "p", "al"):
+        fid = abi.FIELD_ID[nm]
+        va = a.get(fid)
+        assert np.all(np.isfinite(va)), nm
+        assert np.array_equal(va, b.get(fid)), nm
+    for s in range(3):
+        assert np.array_equal(a.get(abi.species_id(s)), b.get(abi.species_id(s)))
+
+
+def test_open_boundaries_rest_state_stays_at_rest():
+    """At rest every radiation term multiplies a zero difference and every
+    degraded flux is zero: the open domain stays at rest like the periodic
+    one."""
+    case = cases.open_boundaries(rest_case())
+    od = OracleDomain(case, "f64")
+    for n in range(2):
+        od.step(5)
+        for nm in ("u_2", "v_2"):
+            assert np.max(np.abs(mass_interior(case, od.get(abi.FIELD_ID[nm])))) == 0.0
+        t = mass_interior(case, od.get(abi.FIELD_ID["t_2"]))
+        assert np.max(np.abs(t - mass_interior(case, case.fields["t_2"]))) < 1e-9
+        mu = mass_interior(case, od.get(abi.FIELD_ID["mu_2"]), 2)
+        assert np.max(np.abs(mu - mass_interior(case, case.fields["mu_2"], 2))) < 1e-9
+
+
+@pytest.mark.parametrize("x,y", OPEN_SIDES)
+def test_open_boundaries_keep_a_uniform_flow_uniform(x, y):
+    """A balanced state (hypsometric_opt 1) moving with a uniform wind
+    (u = 10, v = -5 m/s at every level): the degraded stencils next to the
+    open edges and the radiation terms see no horizontal gradient, so every
+    column stays equal to the others up to rounding (the 3rd- and 5th-order
+    faces of a uniform field differ in the last bit, and the acoustic steps
+    carry that difference into the domain: about 1e-10 of each field after
+    four steps).  (A sheared flow with
+    vertical motion would not: next to open_ys / open_ye the reference leaves
+    u's vertical advection out at i = ids, ide, module_advect_em.F:1350-1351,
+    and curvature leaves the boundary u out, :4292-4295.)"""
+    base = rest_case(kde=14)
+    base.fields["u_1"][:] = 10.0
+    base.fields["u_2"][:] = 10.0
+    base.fields["v_1"][:] = -5.0
+    base.fields["v_2"][:] = -5.0
+    case = cases.open_boundaries(base, x=x, y=y)
+    od = OracleDomain(case, "f64")
+    od.step(4)
+    for nm, tol in (("u_2", 1e-8), ("v_2", 1e-8), ("t_2", 1e-8), ("ph_2", 1e-6), ("p", 1e-6)):
+        a = mass_interior(case, od.get(abi.FIELD_ID[nm]))
+        ref = a[:1, :, :1]
+        scale = max(np.max(np.abs(a)), 1.0)
+        assert np.max(np.abs(a - ref)) <= tol * scale, (nm, np.max(np.abs(a - ref)) / scale)
+    q = mass_interior(case, od.get(abi.species_id(0)))
+    assert np.max(np.abs(q - q[:1, :, :1])) <= 1e-8 * np.max(np.abs(q))
+
+
+def _advect_open(case, q, scheme, ru=0.0, rv=0.0):
+    od = OracleDomain(case, "f64")
+    shp = (case.jde + 2 * H, case.kde, case.ide + 2 * H)
+    od.set(abi.FIELD_ID["ru_m"], np.full(shp, ru))
+    od.set(abi.FIELD_ID["rv_m"], np.full(shp, rv))
+    od.set(abi.FIELD_ID["ww_m"], np.zeros(shp))
+    od.set(abi.FIELD_ID["muts"], case.fields["mub"] + case.fields["mu_1"])
+    od.set(abi.species_id(0), q)
+    od.set(abi.species_id(0, True), q)
+    od.run(scheme, 3, 0, 0)
+    return od.get(abi.FIELD_ID["advect_tend"]).reshape(shp)
+
+
+@pytest.mark.parametrize("scheme", ["advect_scalar", "advect_scalar_pd"])
+@pytest.mark.parametrize("axis", ["x", "y"])
+@pytest.mark.parametrize("vel", [7.5, -7.5])
+def test_open_boundary_fluxes_exact_on_linear_fields(scheme, axis, vel):
+    """Next to an open boundary the reference degrades the face fluxes to
+    3rd and 2nd order (module_advect_em.F:3554-3632, PD :6560-6779) and the
+    boundary cell takes the radiation term instead (:4104-4175, PD
+    :7254-7328).  Every one of those fluxes is exact for a linear field, and
+    the radiation term gives the upwind difference at an outflow boundary and
+    nothing at an inflow one: so with a uniform wind every cell has the
+    tendency -U rdx dq, except the inflow boundary cell, which has 0."""
+    case = cases.open_boundaries(cases.small_case(nx=14, ny=12, kde=10, n_scalar=0, seed=3),
+                                 x=axis == "x", y=axis == "y")
+    i, j, _ = _coords(case)
+    c = i if axis == "x" else j
+    b = 0.02
+    q = 1.0 + b * c
+    tend = _advect_open(case, q, scheme, ru=vel if axis == "x" else 0.0, rv=vel if axis == "y" else 0.0)
+    rd = case.desc.scalars.rdx if axis == "x" else case.desc.scalars.rdy
+    got = mass_interior(case, tend)
+    want = np.full(got.shape, -vel * rd * b)
+    inflow = 0 if vel > 0 else -1
+    if axis == "x":
+        want[:, :, inflow] = 0.0
+    else:
+        want[inflow, :, :] = 0.0
+    assert np.max(np.abs(got - want)) <= 1e-12 * abs(vel * rd * b), np.max(np.abs(got - want))

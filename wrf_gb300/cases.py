@@ -753,6 +753,48 @@ def c5_member_desc(spec):
     return supercell_desc(nx, ny, kde, 2000.0, 12.0, 20000.0, n_scalar=spec[8])
 
 
+def open_boundaries(case, x=True, y=True):
+    """The same initial state with open lateral boundaries in x and/or y (the
+    em_quarter_ss namelist: open_xs/xe, open_ys/ye = .true.): the options
+    changed, and the memory halo of every field holding its nearest edge
+    value, as the open-boundary copy of share/module_bc.F:864-1107 leaves
+    it (mass points and w levels copy column ids / ide-1, u copies ids /
+    ide; likewise in y)."""
+    import copy
+    desc = copy.deepcopy(case.desc)
+    c = desc.config
+    if x:
+        c.periodic_x = c.symmetric_xs = c.symmetric_xe = 0
+        c.open_xs = c.open_xe = 1
+    if y:
+        c.periodic_y = c.symmetric_ys = c.symmetric_ye = 0
+        c.open_ys = c.open_ye = 1
+    h = abi.HALO
+    ide, jde = case.ide, case.jde
+
+    def clamp(a, kind, stag):
+        if a.ndim != kind:
+            return a
+        out = a
+        if x:
+            hi = ide if stag == "u" else ide - 1
+            ix = np.clip(np.arange(1 - h, 1 - h + a.shape[-1]), 1, hi) + h - 1
+            out = out[..., ix]
+        if y:
+            hi = jde if stag == "v" else jde - 1
+            jy = np.clip(np.arange(1 - h, 1 - h + a.shape[0]), 1, hi) + h - 1
+            out = out[jy]
+        return np.ascontiguousarray(out)
+
+    fields = {}
+    for nm, a in case.fields.items():
+        stag = "u" if nm in ("u_1", "u_2") else ("v" if nm in ("v_1", "v_2") else None)
+        fields[nm] = clamp(a, a.ndim, stag) if a.ndim in (2, 3) else a.copy()
+    species = [(clamp(q, 3, None), clamp(qo, 3, None)) for q, qo in case.species]
+    name = case.name + ("_openx" if x else "") + ("_openy" if y else "")
+    return Case(name, desc, fields, species, dict(case.meta))
+
+
 def small_case(nx=12, ny=10, kde=12, n_scalar=1, seed=7, dx=2000.0, dt=12.0):
     """A tiny domain for fast parity tests (one bubble, noise, scalars)."""
     rng = np.random.Generator(np.random.PCG64(seed))

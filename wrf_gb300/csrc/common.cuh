@@ -35,6 +35,7 @@ constexpr float CPOVCV = CP / (CP - R_D);
 constexpr float T0 = 300.f;
 constexpr float P0 = 100000.f;
 constexpr float RERADIUS = 1.f / 6370.0e03f;
+constexpr float CB = 25.f;  // radiation-condition wave speed of open boundaries, module_model_constants.F:47
 constexpr float PI_F = 3.14159274f;  // 4 atan(1) in FP32 (module_small_step_em.F:1283)
 constexpr float W_ALPHA = 0.3f;  // w_damp strength (m/s/s), module_model_constants.F:88
 constexpr float W_BETA = 1.0f;   // w_damp activation Courant number, :89
@@ -447,6 +448,16 @@ struct MassImages {
     if (ya != NONE) row(ya, st);
     if (yb != NONE) row(yb, st);
   }
+};
+
+// Edge-strip launches of members with open boundaries (open_adv.cuh):
+// blocks of STRIP_THREADS over each member's strip points.
+constexpr int STRIP_THREADS = 256;
+struct StripLaunch {
+  const Mem* mem;
+  const int* block_start;  // [nmem+1] prefix over strip blocks
+  int nmem;
+  int per_col;  // 1: one thread per strip column; 0: per strip column and level
 };
 
 struct TileLaunch {

@@ -25,6 +25,7 @@
 #include <cudaTypedefs.h>
 #include "common.cuh"
 #include "kernels.h"
+#include "open_adv.cuh"
 #include "fcall.h"
 #include <map>
 #include <mutex>
@@ -69,9 +70,19 @@ int check_desc(const WrfGpuDomainDesc& d) {
   if (c.diff_opt == 1 && (c.km_opt != 1 || !(c.khdif >= 0.f) || !(c.kvdif >= 0.f))) return WRFGPU_E_ARG;
   if (c.damp_opt == 2 && !(c.zdamp > 0.f)) return WRFGPU_E_ARG;
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) return WRFGPU_E_ARG;
-  if (!c.periodic_x) return WRFGPU_E_ARG;  // x: periodic only
-  if (!(c.periodic_y || (c.symmetric_ys && c.symmetric_ye))) return WRFGPU_E_ARG;
-  if (c.open_xs || c.open_xe || c.open_ys || c.open_ye || c.specified || c.nested || c.polar) return WRFGPU_E_ARG;
+  // lateral boundaries, one condition per side (share/module_bc.F:60-133):
+  // x periodic or open on both sides, y periodic, symmetric or open on both
+  if (c.specified || c.nested || c.polar || c.symmetric_xs || c.symmetric_xe) return WRFGPU_E_ARG;
+  const bool ox = c.open_xs && c.open_xe, oy = c.open_ys && c.open_ye;
+  const bool sy = c.symmetric_ys && c.symmetric_ye;
+  if (c.open_xs != c.open_xe || c.open_ys != c.open_ye || c.symmetric_ys != c.symmetric_ye) return WRFGPU_E_ARG;
+  if ((c.periodic_x != 0) == ox) return WRFGPU_E_ARG;
+  if ((c.periodic_y != 0) + sy + oy != 1) return WRFGPU_E_ARG;
+  // open boundaries without the diffusion options (their open-boundary
+  // branches are not built)
+  if ((ox || oy) && (c.diff_opt != 0 || c.diff_6th_opt != 0)) return WRFGPU_E_ARG;
+  // the edge strips of the two open sides of a direction do not overlap
+  if ((ox && d.ide < 12) || (oy && d.jde < 12)) return WRFGPU_E_ARG;
   if (c.hypsometric_opt != 1 && c.hypsometric_opt != 2) return WRFGPU_E_ARG;
   if (d.scalars.dt <= 0 || d.scalars.dx <= 0 || d.scalars.dy <= 0) return WRFGPU_E_ARG;
   // the kernels index a field with 32-bit offsets
@@ -121,6 +132,11 @@ struct Ensemble {
   int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_st = nullptr, *d_bs_tm = nullptr;
   int* d_bs_pr = nullptr;  // mass tiles x pairs of species (the scalar transport)
   int nb2 = 0, nb3 = 0, nb_st = 0, nb_tm = 0, nb_pr = 0;
+  // edge strips of members with open lateral boundaries: per point (strip
+  // columns x levels) and per column
+  int *d_bs_sp = nullptr, *d_bs_sc = nullptr;
+  int nb_sp = 0, nb_sc = 0;
+  bool any_open = false;
   bool capturing = false;
   int capture_swaps = 0;               // species-buffer swaps in one captured step
   int nsp_max = 0, ns_max = 0, nlev_max = 0;
@@ -166,6 +182,8 @@ struct Ensemble {
   TileLaunch LP() const { return TileLaunch{d_mems, d_bs_pr, nmem}; }  // tiles x species pairs
   TileLaunch LST() const { return TileLaunch{d_mems, d_bs_st, nmem}; }  // staggered-extent tiles
   TileLaunch LTM() const { return TileLaunch{d_mems, d_bs_tm, nmem}; }  // mass-extent tiles
+  StripLaunch LSP() const { return StripLaunch{d_mems, d_bs_sp, nmem, 0}; }  // open-boundary strip points
+  StripLaunch LSC() const { return StripLaunch{d_mems, d_bs_sc, nmem, 1}; }  // open-boundary strip columns
 
   // The fused scalar update writes the new value into the spare buffer; the
   // swap kernel exchanges (q, qa) in the device member table and the host
@@ -529,6 +547,8 @@ struct Ensemble {
     if (d_bs_pr) cudaFree(d_bs_pr);
     if (d_bs_st) cudaFree(d_bs_st);
     if (d_bs_tm) cudaFree(d_bs_tm);
+    if (d_bs_sp) cudaFree(d_bs_sp);
+    if (d_bs_sc) cudaFree(d_bs_sc);
     if (d_tmaps) cudaFree(d_tmaps);
     if (d_pd_scratch) cudaFree(d_pd_scratch);
     if (d_err) cudaFree(d_err);
@@ -586,7 +606,8 @@ struct Ensemble {
     CK(cudaMalloc(&d_cfl, sizeof(float) * 2 * n));
     CK(cudaMemsetAsync(d_cfl, 0, sizeof(float) * 2 * n, stream));
     std::vector<float*> scr(n);
-    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0), bpr(n + 1, 0);
+    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0), bpr(n + 1, 0), bsp(n + 1, 0),
+        bsc(n + 1, 0);
     for (int m = 0; m < n; ++m) {
       const WrfGpuDomainDesc& d = ds[m];
       Mem& M = hm[m];
@@ -637,8 +658,13 @@ struct Ensemble {
       bpr[m + 1] = bpr[m] + tiles_x(M) * tiles_y(M) * blocks_per_tile(M.nsp, TILE_PER_PAIR);
       bst[m + 1] = bst[m] + tiles_x(M, true) * tiles_y(M, true);
       btm[m + 1] = btm[m] + tiles_x(M) * tiles_y(M);
+      const int nsc = strip_cols(M.ide, M.jde, M.cf.open_xs, M.cf.open_ys);
+      any_open = any_open || nsc > 0;
+      bsp[m + 1] = bsp[m] + (nsc * (M.kme - M.kms + 1) + STRIP_THREADS - 1) / STRIP_THREADS;
+      bsc[m + 1] = bsc[m] + (nsc + STRIP_THREADS - 1) / STRIP_THREADS;
     }
     nb2 = bs2[n]; nb3 = bs3[n]; nb_st = bst[n]; nb_tm = btm[n]; nb_pr = bpr[n];
+    nb_sp = bsp[n]; nb_sc = bsc[n];
     {  // tensor maps of every 3-D buffer: halo and tile boxes
       int rc = get_tensor_map_encoder();
       if (rc) return rc;
@@ -678,6 +704,10 @@ struct Ensemble {
     CK(cudaMemcpyAsync(d_bs_st, bst.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_bs_tm, sizeof(int) * (n + 1)));
     CK(cudaMemcpyAsync(d_bs_tm, btm.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_bs_sp, sizeof(int) * (n + 1)));
+    CK(cudaMemcpyAsync(d_bs_sp, bsp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&d_bs_sc, sizeof(int) * (n + 1)));
+    CK(cudaMemcpyAsync(d_bs_sc, bsc.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_pd_scratch, sizeof(float*) * n));
     CK(cudaMemcpyAsync(d_pd_scratch, scr.data(), sizeof(float*) * n, cudaMemcpyHostToDevice, stream));
     // map factors default to 1, cosa to 1 (ideal cases); callers overwrite via set_field
@@ -761,9 +791,14 @@ struct Ensemble {
       // rk_tendency (module_em.F:370-781)
       mark(PH_TEND_U); launch_tend_u_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDU]);
       mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDV]);
-      mark(PH_TEND_W); launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
+      mark(PH_TEND_W);
+      // open boundaries: rw_tend next to them from the cqw the tile kernel overwrites
+      if (any_open) launch_strip_tend_w(LSC(), nb_sc, stream);
+      launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
+      // open boundaries: the lower-order fluxes and radiation terms next to them
+      if (any_open) launch_strip_tend(LSP(), nb_sp, stream);
       if (diff6 || damp2) {  // module_em.F:801-944 (stage 1), then rk_addtend_dry (solve_em.F:967)
         mark(PH_DIFF);
         if (rk_step == 1 && diff6) launch_forward_diff(l3, nb3, 0, stream);
@@ -794,7 +829,13 @@ struct Ensemble {
         // the producers' own halo stores (MassImages): advance_mu_t,
         // advance_w and calc_p_rho write each halo image with its interior
         // point, and nothing in the acoustic step reads these halos before
-        // the next step's advance_uv
+        // the next step's advance_uv; open boundaries' copies are the fill's
+        if (any_open) {
+          JobList j;
+          j.f3(WRFGPU_PH_2, 'w'); j.f3(WRFGPU_AL, 'p'); j.f3(WRFGPU_P, 'p');
+          j.f2(WRFGPU_MUTS, 't'); j.f2(WRFGPU_MU_2, 't'); j.f2(WRFGPU_MUDF, 't');
+          fill(j);
+        }
       }
       mark(PH_SSF); launch_small_step_finish(l2, nb2, a, stream, tune[TU_SSF]);
       if (rk_step == 3) {
@@ -828,6 +869,7 @@ struct Ensemble {
         launch_pd_courant(l2, nb2, rk_step, stream);
         launch_scalar_pd_update(LP(), nb_pr, nlev_max, rk_step, stream, tune[TU_PD]);
       }
+      if (any_open) launch_strip_scalar(LSP(), nb_sp, rk_step, stream);
       swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi_col(LTM(), nb_tm, stream, tune[TU_CPRP]);
       if (rk_step < 3) {

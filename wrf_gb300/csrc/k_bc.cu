@@ -1,17 +1,19 @@
 // On-device halo fill: the single-GPU replacement of the reference's
-// set_physical_bc3d / set_physical_bc2d (share/module_bc.F:202-1000) at each
-// sync site of solve_em, for periodic lateral boundaries in x and periodic
-// or symmetric boundaries in y.
+// set_physical_bc3d / set_physical_bc2d (share/module_bc.F:202-1107) at each
+// sync site of solve_em, for periodic or open lateral boundaries in x and
+// periodic, symmetric or open boundaries in y.
 //
-// The reference fills the x halo of rows jds..jde(+stag) first and then
-// copies whole rows into the y halo, so every halo point ends up holding the
-// value of one interior point: its periodic image, or its mirror image (with
-// a sign change for the normal velocity v).  This kernel computes that source
-// point directly, so all points of a field are written in one pass with no
-// ordering between them.  The points written and the values they receive
-// are the reference's, except the never-read column ime of fields that are
-// not x-staggered, which the reference fills with whatever its x pass left
-// there and this kernel leaves untouched.
+// The reference fills the x halo first and then copies whole rows into the
+// y halo, so every halo point ends up holding the value of one other point:
+// its periodic image, its mirror image (with a sign change for the normal
+// velocity v), or, next to an open boundary, the edge value copied into
+// three halo points (module_bc.F:864-1107, for the variables of
+// open_bc_copy).  This kernel computes that source point directly, so all
+// points of a field are written in one pass with no ordering between them.
+// The points written and the values they receive are the reference's,
+// except the never-read column ime of fields that are not x-staggered,
+// which the reference fills with whatever its x pass left there and this
+// kernel leaves untouched.
 // Roofline: pure copy, 2 x 4 B per halo point; a few percent of a step.
 #include "common.cuh"
 #include "kernels.h"
@@ -32,6 +34,21 @@ __device__ __forceinline__ int bc_src(int t, int n, bool stag, bool periodic, bo
   if (t < 1) { if (normal_flip) *neg = !*neg; return 2 - t; }      // dat(ids-i) = -dat(ids+i)
   if (t > n) { if (normal_flip) *neg = !*neg; return 2 * n - t; }  // dat(ide+i) = -dat(ide-i)
   return t;
+}
+
+// Open boundaries (module_bc.F:864-925 in x, :1059-1107 in y): the source of
+// halo index t, or t itself where the open copy writes nothing (the fourth
+// halo point, and t = ide+3 / ide+4 beyond the three copies).
+__device__ __forceinline__ int open_src(int t, int n, bool stag) {
+  if (t >= -2 && t <= 0) return 1;
+  if (stag) return (t >= n + 1 && t <= n + 3) ? n : t;
+  return (t >= n && t <= n + 2) ? n - 1 : t;
+}
+// open_bc_copy of set_physical_bc3d (module_bc.F:699-704) and
+// set_physical_bc2d (:248-251)
+__device__ __forceinline__ bool open_copy(char v, bool f3d) {
+  if (v == 'u' || v == 'v' || v == 'w' || v == 't' || v == 'x' || v == 'y' || v == 'r' || v == 'p') return true;
+  return f3d && (v == 'd' || v == 'e' || v == 'f');
 }
 
 // grid: (blocks per job, jobs, members).  Work units: for the x halo
@@ -58,28 +75,47 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
     if (var == 'w') k_end = min(m.kde, m.kte);
   }
   const int nk = (J.kind == 3) ? (k_end - m.kts + 1) : 1;
+  const bool f3d = J.kind == 3;
   const bool px = m.cf.periodic_x, py = m.cf.periodic_y;
   const bool sy = m.cf.symmetric_ys && m.cf.symmetric_ye;
+  const bool copy = open_copy(var, f3d);
+  const bool ox = m.cf.open_xs && copy, oy = m.cf.open_ys && copy;  // open on both sides
   constexpr int NXW_MAX = 2 * WRFGPU_HALO + 1;
-  const int nxl = WRFGPU_HALO;
-  const int xr0 = m.ide, xr1 = m.ide + 4 + istag;  // periodic x only
-  const int nxw = nxl + (xr1 - xr0 + 1);           // <= NXW_MAX
-  const int yr0 = py ? m.jde : (vs ? m.jde + 1 : m.jde);
-  const int yr1 = py ? m.jde + 4 + jstag : (vs ? m.jde + 4 : m.jde + 3);
-  const int nyrows = WRFGPU_HALO + (yr1 - yr0 + 1);
+  // x halo columns written: periodic, ids-4..ids-1 and ide..ide+4+istag;
+  // open, ids-3..ids-1 and three past the edge point
+  const int nxl = ox ? 3 : WRFGPU_HALO;
+  const int xr0 = ox ? (us ? m.ide + 1 : m.ide) : m.ide;
+  const int xr1 = ox ? xr0 + 2 : m.ide + 4 + istag;
+  const int nxw = nxl + (xr1 - xr0 + 1);  // <= NXW_MAX
+  // y halo rows written
+  const int ynl = oy ? 3 : WRFGPU_HALO;
+  const int yr0 = oy ? (vs ? m.jde + 1 : m.jde) : (py ? m.jde : (vs ? m.jde + 1 : m.jde));
+  const int yr1 = oy ? yr0 + 2 : (py ? m.jde + 4 + jstag : (vs ? m.jde + 4 : m.jde + 3));
+  const int nyrows = ynl + (yr1 - yr0 + 1);
+  // rows of the x units: the domain rows, and with open x and open y the two
+  // 3-D rows of the x pass (jts-bdyzone .. jde+jstag+bdyzone, module_bc.F:870)
+  // that the y pass does not overwrite
+  const bool xextra = ox && oy && f3d;
   const int xj0 = m.jds, xj1 = m.jde + jstag;
+  const int nxj = xj1 - xj0 + 1 + (xextra ? 2 : 0);
   const int yi0 = m.ims, yi1 = us ? m.ime : m.ide + 3;
-  const int nxj = xj1 - xj0 + 1, nyi = yi1 - yi0 + 1;
+  const int nyi = yi1 - yi0 + 1;
+  // source column of x index ti as the x pass leaves it
+  auto xsrc = [&](int ti, bool* neg) -> int {
+    if (px) return bc_src(ti, m.ide, us, true, false, neg);
+    if (ox) return open_src(ti, m.ide, us);
+    return ti;
+  };
   // 32-bit offsets of (i, k, j) / (i, j) in the field
-  const bool f3d = J.kind == 3;
   const int sk = (int)m.sk, sj = f3d ? (int)m.sj : (int)m.s2;
   auto off = [&](int i, int k, int j) { return (i - m.ims) + (f3d ? (k - m.kms) * sk : 0) + (j - m.jms) * sj; };
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
-  if (px) {
+  if (px || ox) {
     const int nunits = nk * nxj;
     for (int u = tid; u < nunits; u += nthr) {
       const int kk = u / nxj;
-      const int tj = xj0 + (u - kk * nxj), k = kk + m.kts;
+      const int r = u - kk * nxj, k = kk + m.kts;
+      const int tj = r <= xj1 - xj0 ? xj0 + r : (r == xj1 - xj0 + 1 ? m.jds - WRFGPU_HALO : m.jde + jstag + WRFGPU_HALO);
       bool negj = false;
       const int sjj = (py || sy) ? bc_src(tj, m.jde, vs, py, var == 'v', &negj) : tj;
       float val[NXW_MAX];
@@ -88,7 +124,7 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
         if (c < nxw) {
           const int ti = c < nxl ? m.ids - nxl + c : xr0 + (c - nxl);
           bool neg = false;
-          const int si = bc_src(ti, m.ide, us, true, false, &neg);
+          const int si = xsrc(ti, &neg);
           val[c] = base[off(si, k, sjj)];
         }
       }
@@ -101,7 +137,7 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
       }
     }
   }
-  if (py || sy) {
+  if (py || sy || oy) {
     constexpr int PER = 4;  // points per lane
     const int lane = threadIdx.x & 31, warp = tid >> 5, nwarps = nthr >> 5;
     const int npiece = (nyi + 32 * PER - 1) / (32 * PER);
@@ -110,9 +146,9 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
       const int row = w / npiece, pc = w - row * npiece;
       const int kk = row / nyrows, r = row - kk * nyrows;
       const int k = kk + m.kts;
-      const int tj = r < WRFGPU_HALO ? m.jds - WRFGPU_HALO + r : yr0 + (r - WRFGPU_HALO);
+      const int tj = r < ynl ? m.jds - ynl + r : yr0 + (r - ynl);
       bool negj = false;
-      const int sjj = bc_src(tj, m.jde, vs, py, var == 'v', &negj);
+      const int sjj = oy ? open_src(tj, m.jde, vs) : bc_src(tj, m.jde, vs, py, var == 'v', &negj);
       float val[PER];
       bool neg[PER];
 #pragma unroll
@@ -121,7 +157,7 @@ __global__ void k_fill_halo(const Mem* __restrict__ mems, HaloJobs jobs) {
         neg[q] = negj;
         if (ii < nyi) {
           const int ti = yi0 + ii;
-          const int si = px ? bc_src(ti, m.ide, us, true, false, &neg[q]) : ti;
+          const int si = xsrc(ti, &neg[q]);
           val[q] = base[off(si, k, sjj)];
         }
       }

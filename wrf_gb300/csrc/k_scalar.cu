@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "ffmath.h"
+#include "open_adv.cuh"
 
 namespace wrfgpu {
 
@@ -106,77 +107,13 @@ __global__ void __launch_bounds__(BX* BY) k_advect_scalar(Launch L, int species,
     if (in_zero && !accum) tend(i, k, j) = 0.f;
     return;
   }
-  F3 fld = f3p(m, m.q[species]), ru = f3(m, WRFGPU_RU_M), rv = f3(m, WRFGPU_RV_M), rom = f3(m, WRFGPU_WW_M);
-  F2 msftx = f2(m, WRFGPU_MSFTX);
-  F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzw = f1(m, WRFGPU_RDNW);
-  float t = accum ? tend(i, k, j) : 0.f;
-  auto fy = [&](int jj) {
-    float vel = rv(i, k, jj);
-    return vel * flux5(fld(i, k, jj - 3), fld(i, k, jj - 2), fld(i, k, jj - 1), fld(i, k, jj), fld(i, k, jj + 1), fld(i, k, jj + 2), vel);
-  };
-  t = t - msftx(i, j) * m.rdy * (fy(j + 1) - fy(j));
-  auto fx = [&](int ii) {
-    float vel = ru(ii, k, j);
-    return vel * flux5(fld(ii - 3, k, j), fld(ii - 2, k, j), fld(ii - 1, k, j), fld(ii, k, j), fld(ii + 1, k, j), fld(ii + 2, k, j), vel);
-  };
-  t = t - msftx(i, j) * m.rdx * (fx(i + 1) - fx(i));
-  auto vf = [&](int kk) -> float {
-    if (kk == m.kts || kk == m.kte) return 0.f;
-    if (kk == m.kts + 1 || kk == ktf) return rom(i, kk, j) * (fzm(kk) * fld(i, kk, j) + fzp(kk) * fld(i, kk - 1, j));
-    float vel = rom(i, kk, j);
-    return vel * flux3(fld(i, kk - 2, j), fld(i, kk - 1, j), fld(i, kk, j), fld(i, kk + 1, j), -vel);
-  };
-  t = t - rdzw(k) * (vf(k + 1) - vf(k));
-  tend(i, k, j) = t;
+  const F3 fld = f3p(m, m.q[species]);
+  const ScalarAdv a{fld, fld, f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M), f2(m, WRFGPU_MSFTX),
+                    f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW)};
+  tend(i, k, j) = adv_scalar_point(m, a, accum ? tend(i, k, j) : 0.f, i, j, k);
 }
 
-// ------------------------------------------------------------ advect_scalar_pd
-struct PDCtx {
-  F3 f, fo, ru, rv, rom;
-  F2 mut, mub, mu_old, msftx, msfty;
-  F1 c1, c2, fzm, fzp, rdzw;
-  float rdx, rdy, dt;
-  int kts, ktf, kde;
-};
-__device__ __forceinline__ PDCtx pd_ctx(const Mem& m, int species, float dt) {
-  PDCtx c{f3p(m, m.q[species]), f3p(m, m.qo[species]), f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M),
-          f2(m, WRFGPU_MUTS), f2(m, WRFGPU_MUB), f2(m, WRFGPU_MU_1), f2(m, WRFGPU_MSFTX), f2(m, WRFGPU_MSFTY),
-          f1(m, WRFGPU_C1H), f1(m, WRFGPU_C2H), f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW),
-          m.rdx, m.rdy, dt, m.kts, min(m.kte, m.kde - 1), m.kde};
-  return c;
-}
-// face fluxes: *hi = high-order minus upwind, *lo = upwind
-__device__ __forceinline__ void pd_fx(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
-  float dx = 2.f / (c.msfty(i, j) + c.msfty(i - 1, j)) / c.rdx;
-  float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i - 1, j) + c.c2(k)));
-  float vel = c.ru(i, k, j);
-  float cr = vel * c.dt / dx / mu;
-  float l = mu * (dx / c.dt) * flux_upwind(c.fo(i - 1, k, j), c.fo(i, k, j), cr);
-  float h = vel * pflux5(c.f(i - 3, k, j), c.f(i - 2, k, j), c.f(i - 1, k, j), c.f(i, k, j), c.f(i + 1, k, j), c.f(i + 2, k, j), vel);
-  *lo = l; *hi = h - l;
-}
-__device__ __forceinline__ void pd_fy(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
-  float dy = 2.f / (c.msftx(i, j) + c.msftx(i, j - 1)) / c.rdy;
-  float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j - 1) + c.c2(k)));
-  float vel = c.rv(i, k, j);
-  float cr = vel * c.dt / dy / mu;
-  float l = mu * (dy / c.dt) * flux_upwind(c.fo(i, k, j - 1), c.fo(i, k, j), cr);
-  float h = vel * pflux5(c.f(i, k, j - 3), c.f(i, k, j - 2), c.f(i, k, j - 1), c.f(i, k, j), c.f(i, k, j + 1), c.f(i, k, j + 2), vel);
-  *lo = l; *hi = h - l;
-}
-__device__ __forceinline__ void pd_fz(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
-  if (k == 1 || k == c.kde) { *hi = 0.f; *lo = 0.f; return; }
-  float dz = 2.f / (c.rdzw(k) + c.rdzw(k - 1));
-  float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j) + c.c2(k)));
-  float vel = c.rom(i, k, j);
-  float cr = vel * c.dt / dz / mu;
-  float l = mu * (dz / c.dt) * flux_upwind(c.fo(i, k - 1, j), c.fo(i, k, j), cr);
-  float h;
-  if (k == c.kts + 1 || k == c.ktf) h = c.rom(i, k, j) * (c.fzm(k) * c.f(i, k, j) + c.fzp(k) * c.f(i, k - 1, j));
-  else h = vel * pflux3(c.f(i, k - 2, j), c.f(i, k - 1, j), c.f(i, k, j), c.f(i, k + 1, j), -vel);
-  *lo = l; *hi = h - l;
-}
-
+// ------------------------------------------------------------ advect_scalar_pd (open_adv.cuh)
 // Pass 1: limiter scale of each cell of the tile + 1-cell halo (-1: not limited).
 // mode 0: only members whose species uses the positive-definite scheme; mode 2: always.
 __global__ void __launch_bounds__(BX* BY) k_pd_scale(Launch L, int species, int rk_step, int mode, float* const* scratch) {
@@ -190,19 +127,7 @@ __global__ void __launch_bounds__(BX* BY) k_pd_scale(Launch L, int species, int 
   if (i < m.its - 1 || i > itf + 1 || j < m.jts - 1 || j > jtf + 1 || k < m.kts || k > ktf) return;
   const Stage st = stage_of(m, rk_step);
   const PDCtx c = pd_ctx(m, species, st.dt_rk);
-  float hx0, lx0, hx1, lx1, hy0, ly0, hy1, ly1, hz0, lz0, hz1, lz1;
-  pd_fx(c, i, k, j, &hx0, &lx0); pd_fx(c, i + 1, k, j, &hx1, &lx1);
-  pd_fy(c, i, k, j, &hy0, &ly0); pd_fy(c, i, k, j + 1, &hy1, &ly1);
-  pd_fz(c, i, k, j, &hz0, &lz0); pd_fz(c, i, k + 1, j, &hz1, &lz1);
-  const float mx = c.msftx(i, j), my = c.msfty(i, j), dt = c.dt;
-  float ph_low = ((c.c1(k) * c.mub(i, j) + c.c2(k)) + (c.c1(k) * c.mu_old(i, j))) * c.fo(i, k, j) -
-                 dt * (mx * my * (c.rdx * (lx1 - lx0) + c.rdy * (ly1 - ly0)) + my * c.rdzw(k) * (lz1 - lz0));
-  float flux_out = dt * ((mx * my) * (c.rdx * (fmaxf_f(0.f, hx1) - fminf_f(0.f, hx0)) +
-                                      c.rdy * (fmaxf_f(0.f, hy1) - fminf_f(0.f, hy0))) +
-                         my * c.rdzw(k) * (fminf_f(0.f, hz1) - fmaxf_f(0.f, hz0)));
-  float s = -1.f;
-  if (flux_out > ph_low) s = fmaxf_f(0.f, ph_low / (flux_out + 1.e-20f));
-  f3p(m, scratch[bp.m])(i, k, j) = s;
+  f3p(m, scratch[bp.m])(i, k, j) = pd_scale_cell(m, c, i, k, j);
 }
 
 // Pass 2: divergence of the limited fluxes (z, then x, then y) into advect_tend.
@@ -223,29 +148,50 @@ __global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int r
   }
   const Stage st = stage_of(m, rk_step);
   const PDCtx c = pd_ctx(m, species, st.dt_rk);
-  F3 sc = f3p(m, scratch[bp.m]);
-  auto lim = [&](float v, int ci, int ck, int cj) {
-    float s = sc(ci, ck, cj);
-    return s >= 0.f ? s * v : v;
-  };
-  float hx0, lx0, hx1, lx1, hy0, ly0, hy1, ly1, hz0, lz0, hz1, lz1;
-  pd_fx(c, i, k, j, &hx0, &lx0); pd_fx(c, i + 1, k, j, &hx1, &lx1);
-  pd_fy(c, i, k, j, &hy0, &ly0); pd_fy(c, i, k, j + 1, &hy1, &ly1);
-  pd_fz(c, i, k, j, &hz0, &lz0); pd_fz(c, i, k + 1, j, &hz1, &lz1);
-  // face (i): left cell i-1 owns positive flux, cell i owns negative flux
-  if (hx0 > 0.f) hx0 = lim(hx0, i - 1, k, j); else if (hx0 < 0.f) hx0 = lim(hx0, i, k, j);
-  if (hx1 > 0.f) hx1 = lim(hx1, i, k, j); else if (hx1 < 0.f) hx1 = lim(hx1, i + 1, k, j);
-  if (hy0 > 0.f) hy0 = lim(hy0, i, k, j - 1); else if (hy0 < 0.f) hy0 = lim(hy0, i, k, j);
-  if (hy1 > 0.f) hy1 = lim(hy1, i, k, j); else if (hy1 < 0.f) hy1 = lim(hy1, i, k, j + 1);
-  // vertical face k: the cell below (k-1) owns negative flux, the cell above (k) positive flux
-  if (k > 1) { if (hz0 < 0.f) hz0 = lim(hz0, i, k - 1, j); else if (hz0 > 0.f) hz0 = lim(hz0, i, k, j); }
-  if (k + 1 < c.kde) { if (hz1 < 0.f) hz1 = lim(hz1, i, k, j); else if (hz1 > 0.f) hz1 = lim(hz1, i, k + 1, j); }
-  const float mx = c.msftx(i, j);
-  float t = accum ? tend(i, k, j) : 0.f;
-  t = t - c.rdzw(k) * (hz1 - hz0 + lz1 - lz0);
-  t = t - mx * (c.rdx * (hx1 - hx0 + lx1 - lx0));
-  t = t - mx * (c.rdy * (hy1 - hy0 + ly1 - ly0));
-  tend(i, k, j) = t;
+  const F3 sc = f3p(m, scratch[bp.m]);
+  tend(i, k, j) = pd_tend_cell(m, c, i, k, j, accum ? tend(i, k, j) : 0.f,
+                               [&](int ci, int ck, int cj) { return sc(ci, ck, cj); });
+}
+
+// ------------------------------------------------------------ edge strips
+// The large step's scalar transport at the points next to an open boundary
+// (open_adv.cuh): advect_scalar, or advect_scalar_pd with the limiter
+// factors of the neighbouring cells formed in place, then rk_update_scalar
+// into the spare buffer, after the tile kernels and from the same inputs
+// (the arithmetic of k_scalar_adv_update / k_scalar_pd_update, so the
+// points the open branches leave alone get the same bits twice).
+__global__ void __launch_bounds__(STRIP_THREADS) k_strip_scalar(StripLaunch L, int rk_step) {
+  const StripPos sp = strip_pos(L);
+  const Mem& m = block_member(L.mem, sp.m);
+  if (!sp.valid) return;
+  const int i = sp.i, j = sp.j, k = sp.k;
+  if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  const F2 msfty = f2(m, WRFGPU_MSFTY), mu_old = f2(m, WRFGPU_MU_1), mu_new = f2(m, WRFGPU_MU_2),
+           mub = f2(m, WRFGPU_MUB);
+  const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  const float muold = mu_old(i, j) + mub(i, j), munew = mu_new(i, j) + mub(i, j);
+  for (int s = 0; s < m.nsp; ++s) {
+    float t;
+    if (pd_applies(m, s, rk_step)) {
+      const PDCtx c = pd_ctx(m, s, st.dt_rk);
+      t = pd_tend_cell(m, c, i, k, j, 0.f, [&](int ci, int ck, int cj) { return pd_scale_cell(m, c, ci, ck, cj); });
+    } else {
+      const F3 fld = f3p(m, m.q[s]);
+      const ScalarAdv a{fld, fld, f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M), f2(m, WRFGPU_MSFTX),
+                        f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW)};
+      t = adv_scalar_point(m, a, 0.f, i, j, k);
+    }
+    const float tendency = msfty(i, j) * t;
+    const F3 q = f3p(m, m.q[s]), qo = f3p(m, m.qo[s]), qa = f3p(m, m.qa[s]);
+    float q1;
+    if (rk_step == 1) { q1 = q(i, k, j); qo(i, k, j) = q1; }
+    else q1 = qo(i, k, j);
+    qa(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+  }
+}
+void launch_strip_scalar(const StripLaunch& L, int nb, int rk_step, cudaStream_t s) {
+  if (nb > 0) k_strip_scalar<<<nb, STRIP_THREADS, 0, s>>>(L, rk_step);
 }
 
 // ------------------------------------------------------------ rk_update_scalar

@@ -20,6 +20,7 @@
 // inputs are prefetched into L2 two levels ahead.
 #include "common.cuh"
 #include "kernels.h"
+#include "open_adv.cuh"
 
 namespace wrfgpu {
 
@@ -443,6 +444,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
   if ((FL & TF_ZERO) && inside && !acc)
     for (int k = kts; k <= kte; ++k) tend(i, k, j) = 0.f;
   if (!(tp.i0 <= itf && tp.j0 <= jtf)) return;  // block-uniform
+  // next to an open boundary rw_tend has been formed by the edge-strip
+  // kernel (k_tend.cu) from the cqw this kernel overwrites: keep it
+  const bool keep = !((m.cf.open_xs || m.cf.open_ys) && in_open_strip(m, i, j));
   const F3 w = f3(m, WRFGPU_W_2), rom = f3(m, WRFGPU_WW), p = f3(m, WRFGPU_P), cqw = f3(m, WRFGPU_CQW);
   const F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
   const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzu = f1(m, WRFGPU_RDN), rdnw = f1(m, WRFGPU_RDNW),
@@ -571,7 +575,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
                                 0.5f * (fzm(k) * (v0 + v1) + fzp(k) * (v0m + v1m)));
       }
     }
-    tend(i, k, j) = t;
+    if (keep) tend(i, k, j) = t;
     ru0m = ru0; ru1m = ru1; rv0m = rv0; rv1m = rv1;
     u0m = u0; u1m = u1; v0m = v0; v1m = v1;
     pkm = pk;

@@ -134,4 +134,12 @@ void launch_advance_mu_t_col(const TileLaunch& L, int nblocks, int rk_step, int 
 void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int iteration, bool fp64, cudaStream_t s,
                           int var = TUNE_DEFAULT[TU_AW], bool damp = false);
 
+// edge strips of members with open lateral boundaries (open_adv.cuh): the
+// tendencies of u, v, theta and ph after their tile kernels (k_tend.cu), rw_tend
+// before its tile kernel (per column), and the scalar transport after its
+// tile kernels (k_scalar.cu)
+void launch_strip_tend(const StripLaunch& L, int nblocks, cudaStream_t s);
+void launch_strip_tend_w(const StripLaunch& L, int nblocks, cudaStream_t s);
+void launch_strip_scalar(const StripLaunch& L, int nblocks, int rk_step, cudaStream_t s);
+
 }  // namespace wrfgpu

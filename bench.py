@@ -553,6 +553,8 @@ def main():
     ap.add_argument("--ref-budget-s", type=float, default=150.0,
                     help="reference arm: time budget of the timed steps (seconds)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-open", action="store_true",
+                    help="skip the same workload with open lateral boundaries added to the default line")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tune-rounds", type=int, default=2,
                     help="autotuning rounds before the warm-up (0: default launch variants; profiling runs)")
@@ -670,6 +672,33 @@ def run_single(args, world, rank, local, pg):
                        "step's input), through the C ABI (wrfgpu_step_host: the copies are nodes of the step's "
                        "graph; the passive scalars' upload overlaps stage 1's dynamics)" % nsp}
 
+    # the same workload with open lateral boundaries on all four sides (the
+    # em_quarter_ss namelist): the tile kernels plus the edge-strip
+    # recomputation next to the open edges and the acoustic-step halo fills
+    open_bc = None
+    if args.workload == "c2" and not args.nx and not args.no_open and world == 1:
+        from wrf_gb300 import cases as C
+        try:
+            ocase = C.open_boundaries(case)
+            odom = G.Domain(ocase, flags=flags)
+            if args.tune_rounds > 0:
+                odom.autotune(args.tune_rounds)
+            odom.step(args.warmup)
+            odom.sync()
+            orc = odom.status(0)[0]
+            osteps = max(3, min(args.steps, 10))
+            oms = odom.time_steps(osteps)
+            ophases = odom.profile_phases(1)
+            open_bc = {"workload": ocase.name, "sides": "open_xs/xe/ys/ye", "status": orc,
+                       "ms_per_step": oms / osteps, "value": cells * osteps / (oms / 1e3), "unit": "cell-steps/s",
+                       "steps": osteps, "overhead_vs_periodic": (oms / osteps) / (ms / args.steps) - 1.0,
+                       "launches_per_step": odom.launches_per_step(),
+                       "phase_ms_delta_vs_periodic": {k: round(ophases[k][0] - phases[k][0], 4)
+                                                      for k in ophases if k in phases}}
+            odom.close()
+        except Exception as ex:  # reported, never required
+            open_bc = {"error": repr(ex)}
+
     ensemble = None
     if args.workload == "c2" and not args.nx and not args.no_ensemble and world == 1:
         dom.close()
@@ -718,6 +747,7 @@ def run_single(args, world, rank, local, pg):
             "phases_ms_per_step": {k: round(v[0], 4) for k, v in phases.items()},
             "ensemble": ensemble,
             "c3_accuracy": c3acc,
+            "open_boundaries": open_bc,
         }
         print(json.dumps(line), flush=True)
 

@@ -457,7 +457,8 @@ struct StripLaunch {
   const Mem* mem;
   const int* block_start;  // [nmem+1] prefix over strip blocks
   int nmem;
-  int per_col;  // 1: one thread per strip column; 0: per strip column and level
+  int w;  // strip width: the columns within w - 1 of an open edge
+  int h;  // 1: the x strips also cover the halo row jds-1 and the y strips the halo column ids-1
 };
 
 struct TileLaunch {

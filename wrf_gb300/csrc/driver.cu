@@ -132,10 +132,11 @@ struct Ensemble {
   int *d_bs2 = nullptr, *d_bs3 = nullptr, *d_bs_st = nullptr, *d_bs_tm = nullptr;
   int* d_bs_pr = nullptr;  // mass tiles x pairs of species (the scalar transport)
   int nb2 = 0, nb3 = 0, nb_st = 0, nb_tm = 0, nb_pr = 0;
-  // edge strips of members with open lateral boundaries: per point (strip
-  // columns x levels) and per column
-  int *d_bs_sp = nullptr, *d_bs_sc = nullptr;
-  int nb_sp = 0, nb_sc = 0;
+  // edge strips of members with open lateral boundaries (strip columns x
+  // levels): the tendencies and the 5th/3rd-order transport, the PD
+  // transport, and its limiter factors (one wider, halo included)
+  int *d_bs_s3 = nullptr, *d_bs_s4 = nullptr, *d_bs_s5 = nullptr;
+  int nb_s3 = 0, nb_s4 = 0, nb_s5 = 0;
   bool any_open = false;
   bool capturing = false;
   int capture_swaps = 0;               // species-buffer swaps in one captured step
@@ -182,8 +183,9 @@ struct Ensemble {
   TileLaunch LP() const { return TileLaunch{d_mems, d_bs_pr, nmem}; }  // tiles x species pairs
   TileLaunch LST() const { return TileLaunch{d_mems, d_bs_st, nmem}; }  // staggered-extent tiles
   TileLaunch LTM() const { return TileLaunch{d_mems, d_bs_tm, nmem}; }  // mass-extent tiles
-  StripLaunch LSP() const { return StripLaunch{d_mems, d_bs_sp, nmem, 0}; }  // open-boundary strip points
-  StripLaunch LSC() const { return StripLaunch{d_mems, d_bs_sc, nmem, 1}; }  // open-boundary strip columns
+  StripLaunch LS3() const { return StripLaunch{d_mems, d_bs_s3, nmem, STRIP_W_TEND, 0}; }
+  StripLaunch LS4() const { return StripLaunch{d_mems, d_bs_s4, nmem, STRIP_W_PD, 0}; }
+  StripLaunch LS5() const { return StripLaunch{d_mems, d_bs_s5, nmem, STRIP_W_PD + 1, 1}; }
 
   // The fused scalar update writes the new value into the spare buffer; the
   // swap kernel exchanges (q, qa) in the device member table and the host
@@ -547,8 +549,9 @@ struct Ensemble {
     if (d_bs_pr) cudaFree(d_bs_pr);
     if (d_bs_st) cudaFree(d_bs_st);
     if (d_bs_tm) cudaFree(d_bs_tm);
-    if (d_bs_sp) cudaFree(d_bs_sp);
-    if (d_bs_sc) cudaFree(d_bs_sc);
+    if (d_bs_s3) cudaFree(d_bs_s3);
+    if (d_bs_s4) cudaFree(d_bs_s4);
+    if (d_bs_s5) cudaFree(d_bs_s5);
     if (d_tmaps) cudaFree(d_tmaps);
     if (d_pd_scratch) cudaFree(d_pd_scratch);
     if (d_err) cudaFree(d_err);
@@ -606,8 +609,8 @@ struct Ensemble {
     CK(cudaMalloc(&d_cfl, sizeof(float) * 2 * n));
     CK(cudaMemsetAsync(d_cfl, 0, sizeof(float) * 2 * n, stream));
     std::vector<float*> scr(n);
-    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0), bpr(n + 1, 0), bsp(n + 1, 0),
-        bsc(n + 1, 0);
+    std::vector<int> bs2(n + 1, 0), bs3(n + 1, 0), bst(n + 1, 0), btm(n + 1, 0), bpr(n + 1, 0), bs_s3(n + 1, 0),
+        bs_s4(n + 1, 0), bs_s5(n + 1, 0);
     for (int m = 0; m < n; ++m) {
       const WrfGpuDomainDesc& d = ds[m];
       Mem& M = hm[m];
@@ -658,13 +661,17 @@ struct Ensemble {
       bpr[m + 1] = bpr[m] + tiles_x(M) * tiles_y(M) * blocks_per_tile(M.nsp, TILE_PER_PAIR);
       bst[m + 1] = bst[m] + tiles_x(M, true) * tiles_y(M, true);
       btm[m + 1] = btm[m] + tiles_x(M) * tiles_y(M);
-      const int nsc = strip_cols(M.ide, M.jde, M.cf.open_xs, M.cf.open_ys);
-      any_open = any_open || nsc > 0;
-      bsp[m + 1] = bsp[m] + (nsc * (M.kme - M.kms + 1) + STRIP_THREADS - 1) / STRIP_THREADS;
-      bsc[m + 1] = bsc[m] + (nsc + STRIP_THREADS - 1) / STRIP_THREADS;
+      auto strip_blocks = [&](int w, int h) {
+        const int nc = strip_cols(M.ide, M.jde, M.cf.open_xs, M.cf.open_ys, w, h);
+        return (nc * (M.kme - M.kms + 1) + STRIP_THREADS - 1) / STRIP_THREADS;
+      };
+      any_open = any_open || M.cf.open_xs || M.cf.open_ys;
+      bs_s3[m + 1] = bs_s3[m] + strip_blocks(STRIP_W_TEND, 0);
+      bs_s4[m + 1] = bs_s4[m] + strip_blocks(STRIP_W_PD, 0);
+      bs_s5[m + 1] = bs_s5[m] + strip_blocks(STRIP_W_PD + 1, 1);
     }
     nb2 = bs2[n]; nb3 = bs3[n]; nb_st = bst[n]; nb_tm = btm[n]; nb_pr = bpr[n];
-    nb_sp = bsp[n]; nb_sc = bsc[n];
+    nb_s3 = bs_s3[n]; nb_s4 = bs_s4[n]; nb_s5 = bs_s5[n];
     {  // tensor maps of every 3-D buffer: halo and tile boxes
       int rc = get_tensor_map_encoder();
       if (rc) return rc;
@@ -704,10 +711,11 @@ struct Ensemble {
     CK(cudaMemcpyAsync(d_bs_st, bst.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
     CK(cudaMalloc(&d_bs_tm, sizeof(int) * (n + 1)));
     CK(cudaMemcpyAsync(d_bs_tm, btm.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
-    CK(cudaMalloc(&d_bs_sp, sizeof(int) * (n + 1)));
-    CK(cudaMemcpyAsync(d_bs_sp, bsp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
-    CK(cudaMalloc(&d_bs_sc, sizeof(int) * (n + 1)));
-    CK(cudaMemcpyAsync(d_bs_sc, bsc.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    for (auto& pr : {std::make_pair(&d_bs_s3, &bs_s3), std::make_pair(&d_bs_s4, &bs_s4),
+                     std::make_pair(&d_bs_s5, &bs_s5)}) {
+      CK(cudaMalloc(pr.first, sizeof(int) * (n + 1)));
+      CK(cudaMemcpyAsync(*pr.first, pr.second->data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream));
+    }
     CK(cudaMalloc(&d_pd_scratch, sizeof(float*) * n));
     CK(cudaMemcpyAsync(d_pd_scratch, scr.data(), sizeof(float*) * n, cudaMemcpyHostToDevice, stream));
     // map factors default to 1, cosa to 1 (ideal cases); callers overwrite via set_field
@@ -793,12 +801,12 @@ struct Ensemble {
       mark(PH_TEND_V); launch_tend_v_col(LST(), nb_st, TF_ALL, stream, tune[TU_TENDV]);
       mark(PH_TEND_W);
       // open boundaries: rw_tend next to them from the cqw the tile kernel overwrites
-      if (any_open) launch_strip_tend_w(LSC(), nb_sc, stream);
+      if (any_open) launch_strip_tend_w(LS3(), nb_s3, stream);
       launch_tend_w_col(LST(), nb_st, tune[TU_TENDW], stream);
       mark(PH_TEND_T); launch_tend_t_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       mark(PH_TEND_PH); launch_tend_ph_col(LST(), nb_st, TF_ZERO | TF_ADV, stream);
       // open boundaries: the lower-order fluxes and radiation terms next to them
-      if (any_open) launch_strip_tend(LSP(), nb_sp, stream);
+      if (any_open) launch_strip_tend(LS3(), nb_s3, stream);
       if (diff6 || damp2) {  // module_em.F:801-944 (stage 1), then rk_addtend_dry (solve_em.F:967)
         mark(PH_DIFF);
         if (rk_step == 1 && diff6) launch_forward_diff(l3, nb3, 0, stream);
@@ -869,7 +877,10 @@ struct Ensemble {
         launch_pd_courant(l2, nb2, rk_step, stream);
         launch_scalar_pd_update(LP(), nb_pr, nlev_max, rk_step, stream, tune[TU_PD]);
       }
-      if (any_open) launch_strip_scalar(LSP(), nb_sp, rk_step, stream);
+      if (any_open) {
+        launch_strip_scalar(LS3(), nb_s3, rk_step, stream);
+        if (rk_step == 3) launch_strip_pd(LS5(), nb_s5, LS4(), nb_s4, rk_step, nsp_max, d_pd_scratch, stream);
+      }
       swap_species();
       mark(PH_CPRP); launch_calc_p_rho_phi_col(LTM(), nb_tm, stream, tune[TU_CPRP]);
       if (rk_step < 3) {

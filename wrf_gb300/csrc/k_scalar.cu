@@ -155,43 +155,79 @@ __global__ void __launch_bounds__(BX* BY) k_pd_tend(Launch L, int species, int r
 
 // ------------------------------------------------------------ edge strips
 // The large step's scalar transport at the points next to an open boundary
-// (open_adv.cuh): advect_scalar, or advect_scalar_pd with the limiter
-// factors of the neighbouring cells formed in place, then rk_update_scalar
-// into the spare buffer, after the tile kernels and from the same inputs
+// (open_adv.cuh), recomputed after the tile kernels from the same inputs
 // (the arithmetic of k_scalar_adv_update / k_scalar_pd_update, so the
-// points the open branches leave alone get the same bits twice).
+// points the open branches leave alone get the same bits twice), then
+// rk_update_scalar into the spare buffer.
+__device__ __forceinline__ void strip_update(const Mem& m, int s, int rk_step, int i, int j, int k, float tendency) {
+  const Stage st = stage_of(m, rk_step);
+  const F2 mu_old = f2(m, WRFGPU_MU_1), mu_new = f2(m, WRFGPU_MU_2), mub = f2(m, WRFGPU_MUB);
+  const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
+  const float muold = mu_old(i, j) + mub(i, j), munew = mu_new(i, j) + mub(i, j);
+  const F3 q = f3p(m, m.q[s]), qo = f3p(m, m.qo[s]), qa = f3p(m, m.qa[s]);
+  float q1;
+  if (rk_step == 1) { q1 = q(i, k, j); qo(i, k, j) = q1; }
+  else q1 = qo(i, k, j);
+  qa(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+}
+// advect_scalar species (every species at stages 1 and 2, the others at the
+// last): the tendency plus the stored sc_tend of the species' diffusion
 __global__ void __launch_bounds__(STRIP_THREADS) k_strip_scalar(StripLaunch L, int rk_step) {
   const StripPos sp = strip_pos(L);
   const Mem& m = block_member(L.mem, sp.m);
   if (!sp.valid) return;
   const int i = sp.i, j = sp.j, k = sp.k;
   if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
-  const Stage st = stage_of(m, rk_step);
-  const F2 msfty = f2(m, WRFGPU_MSFTY), mu_old = f2(m, WRFGPU_MU_1), mu_new = f2(m, WRFGPU_MU_2),
-           mub = f2(m, WRFGPU_MUB);
-  const F1 c1 = f1(m, WRFGPU_C1H), c2 = f1(m, WRFGPU_C2H);
-  const float muold = mu_old(i, j) + mub(i, j), munew = mu_new(i, j) + mub(i, j);
+  const F2 msfty = f2(m, WRFGPU_MSFTY);
   for (int s = 0; s < m.nsp; ++s) {
-    float t;
-    if (pd_applies(m, s, rk_step)) {
-      const PDCtx c = pd_ctx(m, s, st.dt_rk);
-      t = pd_tend_cell(m, c, i, k, j, 0.f, [&](int ci, int ck, int cj) { return pd_scale_cell(m, c, ci, ck, cj); });
-    } else {
-      const F3 fld = f3p(m, m.q[s]);
-      const ScalarAdv a{fld, fld, f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M), f2(m, WRFGPU_MSFTX),
-                        f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW)};
-      t = adv_scalar_point(m, a, 0.f, i, j, k);
-    }
-    const float tendency = msfty(i, j) * t;
-    const F3 q = f3p(m, m.q[s]), qo = f3p(m, m.qo[s]), qa = f3p(m, m.qa[s]);
-    float q1;
-    if (rk_step == 1) { q1 = q(i, k, j); qo(i, k, j) = q1; }
-    else q1 = qo(i, k, j);
-    qa(i, k, j) = ((c1(k) * muold + c2(k)) * q1 + st.dt_rk * tendency) / (c1(k) * munew + c2(k));
+    if (pd_applies(m, s, rk_step)) continue;
+    const F3 fld = f3p(m, m.q[s]);
+    const ScalarAdv a{fld, fld, f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M), f2(m, WRFGPU_MSFTX),
+                      f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW)};
+    float tendency = msfty(i, j) * adv_scalar_point(m, a, 0.f, i, j, k);
+    const F3 sct = f3p(m, sc_tend_of(m, s));
+    if (sct.p) tendency = tendency + sct(i, k, j);
+    strip_update(m, s, rk_step, i, j, k, tendency);
   }
+}
+// advect_scalar_pd species s at the last stage, in two passes: the limiter
+// factors of the strip cells and their neighbours (the strip one wider, halo
+// row / column included) into the member's PD scratch, then the limited
+// divergence and the update at the strip cells
+__global__ void __launch_bounds__(STRIP_THREADS) k_strip_pd_scale(StripLaunch L, int rk_step, int s,
+                                                                 float* const* scratch) {
+  const StripPos sp = strip_pos(L);
+  const Mem& m = block_member(L.mem, sp.m);
+  if (!sp.valid || s >= m.nsp || !pd_applies(m, s, rk_step)) return;
+  const int i = sp.i, j = sp.j, k = sp.k;
+  if (k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  const PDCtx c = pd_ctx(m, s, st.dt_rk);
+  f3p(m, scratch[sp.m])(i, k, j) = pd_scale_cell(m, c, i, k, j);
+}
+__global__ void __launch_bounds__(STRIP_THREADS) k_strip_pd_tend(StripLaunch L, int rk_step, int s,
+                                                                float* const* scratch) {
+  const StripPos sp = strip_pos(L);
+  const Mem& m = block_member(L.mem, sp.m);
+  if (!sp.valid || s >= m.nsp || !pd_applies(m, s, rk_step)) return;
+  const int i = sp.i, j = sp.j, k = sp.k;
+  if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
+  const Stage st = stage_of(m, rk_step);
+  const PDCtx c = pd_ctx(m, s, st.dt_rk);
+  const F3 sc = f3p(m, scratch[sp.m]);
+  const float t = pd_tend_cell(m, c, i, k, j, 0.f, [&](int ci, int ck, int cj) { return sc(ci, ck, cj); });
+  strip_update(m, s, rk_step, i, j, k, f2(m, WRFGPU_MSFTY)(i, j) * t);
 }
 void launch_strip_scalar(const StripLaunch& L, int nb, int rk_step, cudaStream_t s) {
   if (nb > 0) k_strip_scalar<<<nb, STRIP_THREADS, 0, s>>>(L, rk_step);
+}
+void launch_strip_pd(const StripLaunch& wide, int nb_wide, const StripLaunch& L, int nb, int rk_step, int nsp_max,
+                     float* const* d_scratch, cudaStream_t s) {
+  if (nb <= 0) return;
+  for (int sp = 0; sp < nsp_max; ++sp) {
+    k_strip_pd_scale<<<nb_wide, STRIP_THREADS, 0, s>>>(wide, rk_step, sp, d_scratch);
+    k_strip_pd_tend<<<nb, STRIP_THREADS, 0, s>>>(L, rk_step, sp, d_scratch);
+  }
 }
 
 // ------------------------------------------------------------ rk_update_scalar

@@ -321,16 +321,20 @@ __global__ void __launch_bounds__(BX* BY) k_tend_v(Launch L) {
 // Column form: pg_buoy_w overwrites cqw(k) with 1/(1+cqw(k)) after the
 // k = kde point has read the original cqw(kde-1), so each column is walked
 // in order by one thread.  WCQ = false leaves cqw as it is (the edge-strip
-// recomputation, which runs before the step's column kernel).
+// recomputation, which runs before the step's column kernel); it may then
+// form any level range k0..k1 on its own (one level per thread), the values
+// the column walk carries from the levels below loaded at the start.
 template <int FL, bool WCQ = true>
-__device__ __forceinline__ void tend_w_column(const Mem& m, const int i, const int j) {
+__device__ __forceinline__ void tend_w_column(const Mem& m, const int i, const int j, int k0 = -1, int k1 = -1) {
+  static_assert(WCQ || FL == TF_ALL, "level ranges are for the whole rk_tendency");
+  if (k0 < 0) { k0 = m.kts; k1 = m.kte; }
   F3 tend = f3(m, WRFGPU_RW_TEND);
   const bool in_zero = i >= m.its && i <= m.ite && j >= m.jts && j <= m.jte;
   const int itf = min(m.ite, m.ide - 1), jtf = min(m.jte, m.jde - 1), ktf = min(m.kte, m.kde - 1);
   const bool in_acc = i >= m.its && i <= itf && j >= m.jts && j <= jtf;
   if (!in_acc) {
     if ((FL & TF_ZERO) && in_zero)
-      for (int k = m.kts; k <= m.kte; ++k) tend(i, k, j) = 0.f;
+      for (int k = k0; k <= k1; ++k) tend(i, k, j) = 0.f;
     return;
   }
   F3 w = f3(m, WRFGPU_W_2), ru = f3(m, WRFGPU_RU), rv = f3(m, WRFGPU_RV), rom = f3(m, WRFGPU_WW);
@@ -364,7 +368,7 @@ __device__ __forceinline__ void tend_w_column(const Mem& m, const int i, const i
   float muf_c = 0.f, mub_c = 0.f;
   if (FL & TF_PG) { muf_c = f2(m, WRFGPU_MU_2)(i, j); mub_c = f2(m, WRFGPU_MUB)(i, j); }
   // the vertical flux of face k+1 is the lower face of level k+1
-  float vf_lo = (FL & TF_ADV) && m.kts + 1 <= ktf + 1 ? vf(m.kts + 1) : 0.f;
+  float vf_lo = (FL & TF_ADV) && max(k0, m.kts + 1) <= ktf + 1 ? vf(max(k0, m.kts + 1)) : 0.f;
   // values of levels k, k-1, k-2 of the mass fluxes (and of u, v, p) at the
   // points the w-point stencils read, carried down the column instead of
   // re-read (the same values, so the same bits)
@@ -373,7 +377,15 @@ __device__ __forceinline__ void tend_w_column(const Mem& m, const int i, const i
   float rv0 = 0.f, rv1 = 0.f, rv0m = 0.f, rv1m = 0.f, rv0mm = 0.f, rv1mm = 0.f;  // rv(i, k.., j | j+1)
   float u0 = 0.f, u1 = 0.f, u0m = 0.f, u1m = 0.f, v0 = 0.f, v1 = 0.f, v0m = 0.f, v1m = 0.f;
   float pk = 0.f, pkm = 0.f;
-  for (int k = m.kts; k <= m.kte; ++k) {
+  if (k0 - 1 >= m.kts) {  // a range starting above kts: the carried values of the levels below
+    ru0m = ru(i, k0 - 1, j); ru1m = ru(i + 1, k0 - 1, j); rv0m = rv(i, k0 - 1, j); rv1m = rv(i, k0 - 1, j + 1);
+    if (FL & TF_CURV) { u0m = u(i, k0 - 1, j); u1m = u(i + 1, k0 - 1, j); v0m = v(i, k0 - 1, j); v1m = v(i, k0 - 1, j + 1); }
+    if (FL & TF_PG) pkm = p(i, k0 - 1, j);
+    if (k0 - 2 >= m.kts) {
+      ru0mm = ru(i, k0 - 2, j); ru1mm = ru(i + 1, k0 - 2, j); rv0mm = rv(i, k0 - 2, j); rv1mm = rv(i, k0 - 2, j + 1);
+    }
+  }
+  for (int k = k0; k <= k1; ++k) {
     ru0 = ru(i, k, j); ru1 = ru(i + 1, k, j); rv0 = rv(i, k, j); rv1 = rv(i, k, j + 1);
     if (FL & TF_CURV) { u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1); }
     if (FL & TF_PG) pk = p(i, k, j);
@@ -656,8 +668,8 @@ __global__ void __launch_bounds__(STRIP_THREADS) k_strip_tend(StripLaunch L) {
 __global__ void __launch_bounds__(STRIP_THREADS) k_strip_tend_w(StripLaunch L) {
   const StripPos sp = strip_pos(L);
   const Mem& m = block_member(L.mem, sp.m);
-  if (!sp.valid) return;
-  tend_w_column<TF_ALL, false>(m, sp.i, sp.j);
+  if (!sp.valid || sp.k < m.kts || sp.k > m.kte) return;
+  tend_w_column<TF_ALL, false>(m, sp.i, sp.j, sp.k, sp.k);
 }
 void launch_strip_tend(const StripLaunch& L, int nb, cudaStream_t s) {
   if (nb > 0) k_strip_tend<<<nb, STRIP_THREADS, 0, s>>>(L);

@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
   if (!(tp.i0 <= itf && tp.j0 <= jtf)) return;  // block-uniform
   // next to an open boundary rw_tend has been formed by the edge-strip
   // kernel (k_tend.cu) from the cqw this kernel overwrites: keep it
-  const bool keep = !((m.cf.open_xs || m.cf.open_ys) && in_open_strip(m, i, j));
+  const bool keep = !((m.cf.open_xs || m.cf.open_ys) && in_open_strip(m, i, j, STRIP_W_TEND));
   const F3 w = f3(m, WRFGPU_W_2), rom = f3(m, WRFGPU_WW), p = f3(m, WRFGPU_P), cqw = f3(m, WRFGPU_CQW);
   const F3 u = f3(m, WRFGPU_U_2), v = f3(m, WRFGPU_V_2);
   const F1 fzm = f1(m, WRFGPU_FNM), fzp = f1(m, WRFGPU_FNP), rdzu = f1(m, WRFGPU_RDN), rdnw = f1(m, WRFGPU_RDNW),

@@ -141,5 +141,10 @@ void launch_advance_w_col(const TileLaunch& L, int nblocks, int rk_step, int ite
 void launch_strip_tend(const StripLaunch& L, int nblocks, cudaStream_t s);
 void launch_strip_tend_w(const StripLaunch& L, int nblocks, cudaStream_t s);
 void launch_strip_scalar(const StripLaunch& L, int nblocks, int rk_step, cudaStream_t s);
+// the positive-definite species at the last stage, one species at a time
+// through the member's PD scratch: limiter factors over `wide`, then the
+// limited divergence and update over L
+void launch_strip_pd(const StripLaunch& wide, int nb_wide, const StripLaunch& L, int nb, int rk_step, int nsp_max,
+                     float* const* d_scratch, cudaStream_t s);
 
 }  // namespace wrfgpu

@@ -114,42 +114,46 @@ __device__ __forceinline__ float adv_scalar_point(const Mem& m, const ScalarAdv&
 
 // ------------------------------------------------------------ edge strips
 // The points of a member with open boundaries whose large-step results the
-// open branches change: within OPEN_W - 1 = 3 points of an open edge (the
-// positive-definite limiter reaches three cells in; every other change
-// stays within two).  Columns: the x strips i in ids..ids+3 and ide-4..ide
-// for rows jds..jde, then the y strips j in jds..jds+3 and jde-4..jde for
-// the columns outside the x strips (ids = jds = 1).
-constexpr int OPEN_W = 4;
-__host__ __device__ inline int strip_cols(int ide, int jde, bool ox, bool oy) {
-  const int nw = 2 * OPEN_W + 1;
-  int n = ox ? nw * jde : 0;
-  if (oy) n += nw * (ox ? ide - nw : ide);
+// open branches change: within two points of an open edge for the
+// tendencies and the 5th/3rd-order transport (STRIP_W_TEND), within three
+// for the positive-definite transport, whose limiter factors couple
+// neighbouring cells (STRIP_W_PD), and the limiter factors themselves one
+// further, halo row / column included where the other direction is
+// periodic (STRIP_W_PD + 1, h = 1).  A strip of width w: the x strips
+// i in ids..ids+w-1 and ide-w..ide over rows jds-h..jde, then the y strips
+// j in jds..jds+w-1 and jde-w..jde over the columns outside the x strips
+// (ids-h..ide without open x); ids = jds = 1.
+constexpr int STRIP_W_TEND = 3, STRIP_W_PD = 4;
+__host__ __device__ inline int strip_cols(int ide, int jde, bool ox, bool oy, int w, int h) {
+  const int nw = 2 * w + 1;
+  int n = ox ? nw * (jde + h) : 0;
+  if (oy) n += nw * (ox ? ide - nw : ide + h);
   return n;
 }
-__device__ __forceinline__ void strip_col(const Mem& m, int c, int* i, int* j) {
-  const int nw = 2 * OPEN_W + 1;
+__device__ __forceinline__ void strip_col(const Mem& m, int c, int w, int h, int* i, int* j) {
+  const int nw = 2 * w + 1;
   const bool ox = m.cf.open_xs;
   if (ox) {
-    const int nx = nw * m.jde;
+    const int nx = nw * (m.jde + h);
     if (c < nx) {
       const int a = c % nw;
-      *j = 1 + c / nw;
-      *i = a < OPEN_W ? 1 + a : m.ide - OPEN_W + (a - OPEN_W);
+      *j = 1 - h + c / nw;
+      *i = a < w ? 1 + a : m.ide - w + (a - w);
       return;
     }
     c -= nx;
   }
-  const int i0 = ox ? 1 + OPEN_W : 1, ni = ox ? m.ide - nw : m.ide;
+  const int i0 = ox ? 1 + w : 1 - h, ni = ox ? m.ide - nw : m.ide + h;
   const int r = c / ni;
   *i = i0 + c % ni;
-  *j = r < OPEN_W ? 1 + r : m.jde - OPEN_W + (r - OPEN_W);
+  *j = r < w ? 1 + r : m.jde - w + (r - w);
 }
-__device__ __forceinline__ bool in_open_strip(const Mem& m, int i, int j) {
-  return (m.cf.open_xs && (i <= m.ids + OPEN_W - 1 || i >= m.ide - OPEN_W)) ||
-         (m.cf.open_ys && (j <= m.jds + OPEN_W - 1 || j >= m.jde - OPEN_W));
+__device__ __forceinline__ bool in_open_strip(const Mem& m, int i, int j, int w) {
+  return (m.cf.open_xs && (i <= m.ids + w - 1 || i >= m.ide - w)) ||
+         (m.cf.open_ys && (j <= m.jds + w - 1 || j >= m.jde - w));
 }
 // Position of a thread of a strip launch: blocks of STRIP_THREADS over each
-// member's strip columns (per_col) or strip columns x levels kms..kme.
+// member's strip columns x levels kms..kme.
 struct StripPos {
   int m, i, j, k;
   bool valid;
@@ -160,15 +164,14 @@ __device__ __forceinline__ StripPos strip_pos(const StripLaunch& L) {
   sp.m = find_member(L.block_start, L.nmem, b);
   const Mem& m = L.mem[sp.m];
   const int p = (b - __ldg(L.block_start + sp.m)) * STRIP_THREADS + (int)threadIdx.x;
-  const int nc = strip_cols(m.ide, m.jde, m.cf.open_xs, m.cf.open_ys);
+  const int nc = strip_cols(m.ide, m.jde, m.cf.open_xs, m.cf.open_ys, L.w, L.h);
   const int nk = m.kme - m.kms + 1;
-  sp.valid = nc > 0 && p < (L.per_col ? nc : nc * nk);
+  sp.valid = nc > 0 && p < nc * nk;
   sp.i = sp.j = 0;
   sp.k = 0;
   if (sp.valid) {
-    const int c = L.per_col ? p : p % nc;
-    sp.k = L.per_col ? 0 : m.kms + p / nc;
-    strip_col(m, c, &sp.i, &sp.j);
+    sp.k = m.kms + p / nc;
+    strip_col(m, p % nc, L.w, L.h, &sp.i, &sp.j);
   }
   return sp;
 }

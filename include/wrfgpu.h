@@ -153,8 +153,8 @@ typedef struct WrfGpuEnsemble WrfGpuEnsemble;
  * alloc_and_configure_domain) on the device side.  Lateral boundaries, one
  * condition per side (share/module_bc.F:60-133): x periodic or open on both
  * sides, y periodic, symmetric or open on both sides; open sides at least 12
- * points apart and without the diffusion options.  Anything else (specified,
- * nested, polar, symmetric x) returns WRFGPU_E_ARG. */
+ * points apart.  Anything else (specified, nested, polar, symmetric x)
+ * returns WRFGPU_E_ARG. */
 int wrfgpu_ensemble_create(const WrfGpuDomainDesc* descs, int n, int flags, WrfGpuEnsemble** out);
 int wrfgpu_ensemble_destroy(WrfGpuEnsemble* h);
 /* Element count of a field of one member (memory dims, halo included). */

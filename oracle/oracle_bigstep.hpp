@@ -745,8 +745,7 @@ void calc_p_rho_phi(R* qv_p, int n_moist_species, int hypsometric_opt, R* al_p, 
 // sixth-order flux, dropped where it runs up-gradient (diff_6th_opt = 2),
 // tapered over steep terrain (diff_6th_slopeopt >= 1), weighted by the column
 // mass, added to `tendency`.  name: 'u', 'v', 'w' or 'm' (mass-point
-// scalars).  The loop limits are those of periodic / symmetric boundaries
-// (:6330-6443 without the open / specified branches).
+// scalars).  The loop limits of :6330-6443 (without the specified branch).
 template <typename R>
 void sixth_order_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R dt, const WrfDynConfig& cf, R* c1_p,
                            R* c2_p, R* phb_p, R rdx, R rdy, R* msftx_p, R* msfty_p, R* msfux_p, R* msfuy_p,
@@ -757,18 +756,37 @@ void sixth_order_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R dt,
   A1<R> c1(c1_p, d), c2(c2_p, d);
   const R coef = R(cf.diff_6th_factor) * R(0.015625) / (R(2.0) * dt);
   const int ktf = std::min(d.kte, d.kde - 1);
+  int i_start = d.its, j_start = d.jts;
   int i_end = std::min(d.ide - 1, d.ite), j_end = std::min(d.jde - 1, d.jte), k_start = d.kts;
   if (name == 'u') i_end = d.ite;
   if (name == 'v') j_end = d.jte;
   if (name == 'w') k_start = d.kts + 1;
+  // next to open boundaries (:6336-6443)
+  const int ids = d.ids, ide = d.ide, jds = d.jds, jde = d.jde;
+  if (cf.open_xs) i_start = std::max(d.its, ids + 3);
+  if (cf.open_ys) j_start = std::max(d.jts, jds + 3);
+  if (name == 'u') {
+    if (cf.open_xe) i_end = std::min(d.ite, ide - 3);
+    if (cf.open_ye) j_end = std::min(d.jte, jde - 4);
+  } else if (name == 'v') {
+    if (cf.open_xe) i_end = std::min(d.ite, ide - 4);
+    if (cf.open_ye) j_end = std::min(d.jte, jde - 3);
+    if (cf.open_xs) {  // :6383-6388: all four limits on open_xs
+      i_start = std::max(d.its, ids + 3); i_end = std::min(d.ite, ide - 4);
+      j_start = std::max(d.jts, jds + 3); j_end = std::min(d.jte, jde - 3);
+    }
+  } else {
+    if (cf.open_xe) i_end = std::min(d.ite, ide - 4);
+    if (cf.open_ye) j_end = std::min(d.jte, jde - 4);
+  }
   auto mass = [&](int k, int i, int j) { return c1(k) * mut(i, j) + c2(k); };
   // the sixth-order flux through the face between f(-1) and f(0) of a row
   auto flux6 = [](R fm3, R fm2, R fm1, R f0, R fp1, R fp2) {
     return R(10.0) * (f0 - fm1) - R(5.0) * (fp1 - fm2) + (fp2 - fm3);
   };
-  for (int j = d.jts; j <= j_end; ++j)
+  for (int j = j_start; j <= j_end; ++j)
     for (int k = k_start; k <= ktf; ++k)
-      for (int i = d.its; i <= i_end; ++i) {
+      for (int i = i_start; i <= i_end; ++i) {
         // x
         R fx0 = flux6(field(i - 3, k, j), field(i - 2, k, j), field(i - 1, k, j), field(i, k, j), field(i + 1, k, j),
                       field(i + 2, k, j));
@@ -864,14 +882,30 @@ void sixth_order_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R dt,
 // Explicit diffusion (diff_opt = 1) with constant coefficients (km_opt = 1:
 // isotropic_km, module_diffusion_em.F, fills xkmh with khdif and xkhh with
 // khdif / prandtl everywhere, so each coefficient access below reads that
-// one value `xk`; every expression keeps the reference's order).  The loop
-// limits are those of periodic / symmetric boundaries.
+// one value `xk`; every expression keeps the reference's order).
 // ---------------------------------------------------------------------------
+// The loop limits of horizontal_diffusion / horizontal_diffusion_3dmp next to
+// open boundaries (:2786-2790 u, :2834-2839 v, :2874-2879 w, :2919-2924 and
+// :3026-3031 mass points; a periodic x keeps its limits).
+inline void hdiff_open_limits(const WrfDynConfig& cf, char name, const Dims& d, int* i_start, int* i_end,
+                              int* j_start, int* j_end) {
+  const int ids = d.ids, ide = d.ide, jds = d.jds, jde = d.jde;
+  const int xe = name == 'u' ? ide - 1 : ide - 2, ye = name == 'v' ? jde - 1 : jde - 2;
+  if (cf.open_xs) *i_start = std::max(ids + 1, d.its);
+  if (cf.open_xe) *i_end = std::min(xe, d.ite);
+  if (cf.open_ys) *j_start = std::max(jds + 1, d.jts);
+  if (cf.open_ye) *j_end = std::min(ye, d.jte);
+  if (cf.periodic_x) {
+    *i_start = d.its;
+    *i_end = name == 'u' ? d.ite : std::min(d.ite, d.ide - 1);
+  }
+}
+
 // module_big_step_utilities_em.F:2715-2950 horizontal_diffusion
 template <typename R>
-void horizontal_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* c2_p, R* msfux_p,
-                          R* msfuy_p, R* msfvx_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p, R xk, R rdx,
-                          R rdy, const Dims& d) {
+void horizontal_diffusion(const WrfDynConfig& cf, char name, R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* c2_p,
+                          R* msfux_p, R* msfuy_p, R* msfvx_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p, R xk,
+                          R rdx, R rdy, const Dims& d) {
   A3<R> field(field_p, d), tendency(tendency_p, d);
   A2<R> MUT(mut_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx(msfvx_p, d), msfvx_inv(msfvx_inv_p, d),
       msfvy(msfvy_p, d), msftx(msftx_p, d), msfty(msfty_p, d);
@@ -881,10 +915,12 @@ void horizontal_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R* c1_
   if (name == 'u') i_end = d.ite;
   if (name == 'v') j_end = d.jte;
   if (name == 'w') k_start = d.kts + 1;
+  int i_start = d.its, j_start = d.jts;
+  hdiff_open_limits(cf, name, d, &i_start, &i_end, &j_start, &j_end);
   auto M = [&](int k, int i, int j) { return c1(k) * MUT(i, j) + c2(k); };
-  for (int j = d.jts; j <= j_end; ++j)
+  for (int j = j_start; j <= j_end; ++j)
     for (int k = k_start; k <= ktf; ++k)
-      for (int i = d.its; i <= i_end; ++i) {
+      for (int i = i_start; i <= i_end; ++i) {
         R mkrdxm, mkrdxp, mrdx, mkrdym, mkrdyp, mrdy;
         if (name == 'u') {
           mkrdxm = (msftx(i - 1, j) / msfty(i - 1, j)) * M(k, i - 1, j) * xk * rdx;
@@ -937,18 +973,20 @@ void horizontal_diffusion(char name, R* field_p, R* tendency_p, R* mut_p, R* c1_
 
 // :2953-3060 horizontal_diffusion_3dmp: mass-point field minus its base state
 template <typename R>
-void horizontal_diffusion_3dmp(R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* c2_p, R* base_p, R* msfux_p,
-                               R* msfuy_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p, R xk, R rdx, R rdy,
-                               const Dims& d) {
+void horizontal_diffusion_3dmp(const WrfDynConfig& cf, R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* c2_p,
+                               R* base_p, R* msfux_p, R* msfuy_p, R* msfvx_inv_p, R* msfvy_p, R* msftx_p, R* msfty_p,
+                               R xk, R rdx, R rdy, const Dims& d) {
   A3<R> field(field_p, d), tendency(tendency_p, d), base(base_p, d);
   A2<R> MUT(mut_p, d), msfux(msfux_p, d), msfuy(msfuy_p, d), msfvx_inv(msfvx_inv_p, d), msfvy(msfvy_p, d),
       msftx(msftx_p, d), msfty(msfty_p, d);
   A1<R> c1(c1_p, d), c2(c2_p, d);
   const int ktf = std::min(d.kte, d.kde - 1);
   auto M = [&](int k, int i, int j) { return c1(k) * MUT(i, j) + c2(k); };
-  for (int j = d.jts; j <= std::min(d.jte, d.jde - 1); ++j)
+  int i_start = d.its, i_end = std::min(d.ite, d.ide - 1), j_start = d.jts, j_end = std::min(d.jte, d.jde - 1);
+  hdiff_open_limits(cf, 'm', d, &i_start, &i_end, &j_start, &j_end);
+  for (int j = j_start; j <= j_end; ++j)
     for (int k = d.kts; k <= ktf; ++k)
-      for (int i = d.its; i <= std::min(d.ite, d.ide - 1); ++i) {
+      for (int i = i_start; i <= i_end; ++i) {
         const R mkrdxm = (msfux(i, j) / msfuy(i, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i, j) + M(k, i - 1, j)) * rdx;
         const R mkrdxp =
             (msfux(i + 1, j) / msfuy(i + 1, j)) * R(0.5) * (xk + xk) * R(0.5) * (M(k, i + 1, j) + M(k, i, j)) * rdx;
@@ -973,19 +1011,30 @@ void horizontal_diffusion_3dmp(R* field_p, R* tendency_p, R* mut_p, R* c1_p, R* 
 // vertical_diffusion_mp (a 1-D base profile, qv); 't': vertical_diffusion_3dmp
 // (a 3-D base state, theta).  mass: mut (u: muu, v: muv).
 template <typename R>
-void vertical_diffusion(char kind, R* field_p, R* tendency_p, R* base1_p, R* base3_p, R* c1_p, R* c2_p, R* alt_p,
-                        R* mass_p, R* rdn_p, R* rdnw_p, R kvdif, const Dims& d) {
+void vertical_diffusion(const WrfDynConfig& cf, char kind, R* field_p, R* tendency_p, R* base1_p, R* base3_p, R* c1_p,
+                        R* c2_p, R* alt_p, R* mass_p, R* rdn_p, R* rdnw_p, R kvdif, const Dims& d) {
   A3<R> field(field_p, d), tendency(tendency_p, d), alt(alt_p, d), base3(base3_p, d);
   A2<R> MASS(mass_p, d);
   A1<R> c1(c1_p, d), c2(c2_p, d), rdn(rdn_p, d), rdnw(rdnw_p, d), base1(base1_p, d);
   const R g = K<R>::g;
   const int ktf = std::min(d.kte, d.kde - 1);
-  const int i_end = kind == 'u' ? d.ite : std::min(d.ite, d.ide - 1);
-  const int j_end = std::min(d.jte, d.jde - 1);
+  int i_start = d.its, i_end = kind == 'u' ? d.ite : std::min(d.ite, d.ide - 1);
+  int j_start = d.jts, j_end = std::min(d.jte, d.jde - 1);
+  // next to open boundaries: vertical_diffusion_u leaves the boundary u out
+  // (:3443-3446), vertical_diffusion_v the boundary v (:3545-3546)
+  if (kind == 'u') {
+    if (cf.open_xs) i_start = std::max(d.ids + 1, d.its);
+    if (cf.open_xe) i_end = std::min(d.ide - 1, d.ite);
+    if (cf.periodic_x) { i_start = d.its; i_end = d.ite; }
+  }
+  if (kind == 'v') {
+    if (cf.open_ys) j_start = std::max(d.jds + 1, d.jts);
+    if (cf.open_ye) j_end = std::min(d.jde - 1, d.jte);
+  }
   std::vector<R> vf(d.kme - d.kms + 3);
   auto V = [&](int k) -> R& { return vf[k - d.kms + 1]; };  // vflux(0:kte+1)
-  for (int j = d.jts; j <= j_end; ++j)
-    for (int i = d.its; i <= i_end; ++i) {
+  for (int j = j_start; j <= j_end; ++j)
+    for (int i = i_start; i <= i_end; ++i) {
       if (kind == 'w') {
         for (int k = d.kts; k <= ktf - 1; ++k) V(k) = (kvdif / alt(i, k, j)) * rdnw(k) * (field(i, k + 1, j) - field(i, k, j));
         V(ktf) = R(0.);

@@ -193,11 +193,11 @@ int run_routine(Domain<R>& D, int routine, int rk_step, int iteration, int speci
       // sixth-order (diff_6th_opt != 0, its class's mix6_off off)
       if (cf.diff_opt == 1 && !(species < D.n_moist ? cf.moist_mix2_off : cf.scalar_mix2_off)) {
         const R prandtl = R(1.) / R(3.0);
-        horizontal_diffusion('m', D.q(species), p3(WRFGPU_H_DIABATIC), p2(WRFGPU_MUTS), p1(WRFGPU_C1H),
+        horizontal_diffusion(D.cf, 'm', D.q(species), p3(WRFGPU_H_DIABATIC), p2(WRFGPU_MUTS), p1(WRFGPU_C1H),
                              p1(WRFGPU_C2H), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX),
                              p2(WRFGPU_MSFVX_INV), p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY),
                              (R)cf.khdif / prandtl, rdx, rdy, td);
-        vertical_diffusion(iteration == 1 ? 'p' : 'm', D.q(species), p3(WRFGPU_H_DIABATIC), p1(WRFGPU_QV_BASE),
+        vertical_diffusion(D.cf, iteration == 1 ? 'p' : 'm', D.q(species), p3(WRFGPU_H_DIABATIC), p1(WRFGPU_QV_BASE),
                            (R*)nullptr, p1(WRFGPU_C1H), p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUTS),
                            p1(WRFGPU_RDN), p1(WRFGPU_RDNW), (R)cf.kvdif / prandtl, td);
       }

@@ -186,25 +186,25 @@ struct Domain {
       // coefficient 3 kvdif)
       const R khdif = (R)cf.khdif, kvdif = (R)cf.kvdif, prandtl = R(1.) / R(3.0);
       const R xkmh = khdif, xkhh = khdif / prandtl;
-      horizontal_diffusion('u', p3(WRFGPU_U_2), t0, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+      horizontal_diffusion(cf, 'u', p3(WRFGPU_U_2), t0, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
                            p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
                            p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
-      horizontal_diffusion('v', p3(WRFGPU_V_2), t1, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+      horizontal_diffusion(cf, 'v', p3(WRFGPU_V_2), t1, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
                            p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
                            p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
-      horizontal_diffusion('w', p3(WRFGPU_W_2), t2, p2(WRFGPU_MUT), p1(WRFGPU_C1F), p1(WRFGPU_C2F),
+      horizontal_diffusion(cf, 'w', p3(WRFGPU_W_2), t2, p2(WRFGPU_MUT), p1(WRFGPU_C1F), p1(WRFGPU_C2F),
                            p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV),
                            p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkmh, rdx, rdy, td);
-      horizontal_diffusion_3dmp(p3(WRFGPU_T_2), t3, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
+      horizontal_diffusion_3dmp(cf, p3(WRFGPU_T_2), t3, p2(WRFGPU_MUT), p1(WRFGPU_C1H), p1(WRFGPU_C2H),
                                 p3(WRFGPU_T_INIT), p2(WRFGPU_MSFUX), p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX_INV),
                                 p2(WRFGPU_MSFVY), p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), xkhh, rdx, rdy, td);
-      vertical_diffusion('u', p3(WRFGPU_U_2), t0, p1(WRFGPU_U_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+      vertical_diffusion(cf, 'u', p3(WRFGPU_U_2), t0, p1(WRFGPU_U_BASE), (R*)nullptr, p1(WRFGPU_C1H),
                          p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUU), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
-      vertical_diffusion('v', p3(WRFGPU_V_2), t1, p1(WRFGPU_V_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+      vertical_diffusion(cf, 'v', p3(WRFGPU_V_2), t1, p1(WRFGPU_V_BASE), (R*)nullptr, p1(WRFGPU_C1H),
                          p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUV), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
-      vertical_diffusion('w', p3(WRFGPU_W_2), t2, (R*)nullptr, (R*)nullptr, p1(WRFGPU_C1F),
+      vertical_diffusion(cf, 'w', p3(WRFGPU_W_2), t2, (R*)nullptr, (R*)nullptr, p1(WRFGPU_C1F),
                          p1(WRFGPU_C2F), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdif, td);
-      vertical_diffusion('t', p3(WRFGPU_T_2), t3, (R*)nullptr, p3(WRFGPU_T_INIT), p1(WRFGPU_C1H),
+      vertical_diffusion(cf, 't', p3(WRFGPU_T_2), t3, (R*)nullptr, p3(WRFGPU_T_INIT), p1(WRFGPU_C1H),
                          p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUT), p1(WRFGPU_RDN), p1(WRFGPU_RDNW),
                          R(3.) * kvdif, td);
     }
@@ -445,10 +445,10 @@ struct Domain {
           if (rk_step == 1 && mix2(s)) {
             const R prandtl = R(1.) / R(3.0);
             const R khdq = (R)cf.khdif / prandtl, kvdq = (R)cf.kvdif / prandtl;
-            horizontal_diffusion('m', q(s), sct, p2(WRFGPU_MUTS), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MSFUX),
+            horizontal_diffusion(cf, 'm', q(s), sct, p2(WRFGPU_MUTS), p1(WRFGPU_C1H), p1(WRFGPU_C2H), p2(WRFGPU_MSFUX),
                                  p2(WRFGPU_MSFUY), p2(WRFGPU_MSFVX), p2(WRFGPU_MSFVX_INV), p2(WRFGPU_MSFVY),
                                  p2(WRFGPU_MSFTX), p2(WRFGPU_MSFTY), khdq, rdx, rdy, td);
-            vertical_diffusion(s == 0 ? 'p' : 'm', q(s), sct, p1(WRFGPU_QV_BASE), (R*)nullptr, p1(WRFGPU_C1H),
+            vertical_diffusion(cf, s == 0 ? 'p' : 'm', q(s), sct, p1(WRFGPU_QV_BASE), (R*)nullptr, p1(WRFGPU_C1H),
                                p1(WRFGPU_C2H), p3(WRFGPU_ALT), p2(WRFGPU_MUTS), p1(WRFGPU_RDN), p1(WRFGPU_RDNW), kvdq,
                                td);
           }

@@ -25,7 +25,7 @@
 // Supported option subset (anything else is rejected, like wrf_error_fatal):
 //   rk_ord=3, h_*_adv_order=5, v_*_adv_order=3, non_hydrostatic=.true.,
 //   periodic_x/periodic_y, symmetric_xs/xe/ys/ye or open_xs/xe/ys/ye lateral
-//   boundaries (open ones without diffusion),
+//   boundaries,
 //   moist_adv_opt/scalar_adv_opt in {0 (ORIGINAL), 1 (POSITIVEDEF)},
 //   hypsometric_opt in {1,2}, phi_adv_z in {1,2}, IEVA off, physics off.
 #pragma once
@@ -139,8 +139,6 @@ inline void check_config(const WrfDynConfig& c) {
   if (!one(c.periodic_x, c.symmetric_xs, c.open_xs) || !one(c.periodic_x, c.symmetric_xe, c.open_xe) ||
       !one(c.periodic_y, c.symmetric_ys, c.open_ys) || !one(c.periodic_y, c.symmetric_ye, c.open_ye))
     throw std::runtime_error("each lateral boundary needs exactly one condition");
-  if ((c.open_xs || c.open_xe || c.open_ys || c.open_ye) && (c.diff_opt != 0 || c.diff_6th_opt != 0))
-    throw std::runtime_error("open boundaries with explicit or sixth-order diffusion not supported");
   if (c.zadvect_implicit != 0) throw std::runtime_error("IEVA not supported");
   if (c.diff_6th_opt < 0 || c.diff_6th_opt > 2) throw std::runtime_error("diff_6th_opt must be 0, 1 or 2");
 }

@@ -170,12 +170,38 @@ def test_batched_open_and_periodic_members_equal_plain(gpulib):
 
 
 def test_open_domain_needs_room_for_the_strips(gpulib):
-    """Open sides closer than the two edge strips are refused (E_ARG), as are
-    open boundaries combined with the diffusion options."""
+    """Open sides closer than the two edge strips are refused (E_ARG)."""
     small = open_case("x", nx=10, ny=16)
     with pytest.raises(G.WrfGpuError):
         G.Domain(small)
-    diff = open_case("xy")
-    diff.desc.config.diff_6th_opt = 2
-    with pytest.raises(G.WrfGpuError):
-        G.Domain(diff)
+
+
+def _with_diffusion(case, explicit, sixth):
+    c = case.desc.config
+    if sixth:
+        c.diff_6th_opt = 2
+        c.diff_6th_factor = 0.12
+    if explicit:
+        c.diff_opt = 1
+        c.km_opt = 1
+        c.khdif = 300.0
+        c.kvdif = 10.0
+    return case
+
+
+@pytest.mark.parametrize("explicit,sixth", [(True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("sides", ["xy", "x", "y"])
+def test_open_full_step_bitwise_with_diffusion(gpulib, sides, explicit, sixth):
+    """Explicit (diff_opt = 1, km_opt = 1) and sixth-order diffusion with open
+    boundaries: each term keeps its own loop limits next to the open edges
+    (horizontal_diffusion, vertical_diffusion_u / _v, sixth_order_diffusion,
+    including the latter's v limits on open_xs), the species' stored
+    tendencies reach the edge strips' scalar update; 2 steps bit for bit."""
+    case = _with_diffusion(open_case(sides, seed=61), explicit, sixth)
+    od = OracleDomain(case, "f32")
+    ge = G.Domain(case)
+    od.step(2)
+    ge.step(2)
+    ge.sync()
+    bad = _bitwise_diffs(case, ge, od)
+    assert not bad, "\n".join(bad)

@@ -78,9 +78,6 @@ int check_desc(const WrfGpuDomainDesc& d) {
   if (c.open_xs != c.open_xe || c.open_ys != c.open_ye || c.symmetric_ys != c.symmetric_ye) return WRFGPU_E_ARG;
   if ((c.periodic_x != 0) == ox) return WRFGPU_E_ARG;
   if ((c.periodic_y != 0) + sy + oy != 1) return WRFGPU_E_ARG;
-  // open boundaries without the diffusion options (their open-boundary
-  // branches are not built)
-  if ((ox || oy) && (c.diff_opt != 0 || c.diff_6th_opt != 0)) return WRFGPU_E_ARG;
   // the edge strips of the two open sides of a direction do not overlap
   if ((ox && d.ide < 12) || (oy && d.jde < 12)) return WRFGPU_E_ARG;
   if (c.hypsometric_opt != 1 && c.hypsometric_opt != 2) return WRFGPU_E_ARG;

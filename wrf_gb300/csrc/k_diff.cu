@@ -259,15 +259,39 @@ __device__ float vdiff_point(const Mem& m, const F3& f, const F1& b1, const F3* 
   return g2 / (c1 * mass + c2) / alt.ro(i, k, j) * f1(m, WRFGPU_RDNW)(k) * dv;
 }
 
+// Point ranges of the diffusion terms next to open boundaries (a periodic x
+// keeps its ranges): horizontal_diffusion (module_big_step_utilities_em.F:
+// 2786-2790 u, :2834-2839 v, :2874-2879 w, :2919-2924 and :3026-3031 mass
+// points), vertical_diffusion_u / _v (:3443-3446, :3545-3546; the other
+// kinds have none) and sixth_order_diffusion (:6336-6443).
+__device__ __forceinline__ bool hdiff_open_in(const Mem& m, int V, int i, int j) {
+  const bool oxs = m.cf.open_xs, oxe = m.cf.open_xe, oys = m.cf.open_ys, oye = m.cf.open_ye;
+  const bool x = m.cf.periodic_x || ((!oxs || i >= m.ids + 1) && (!oxe || i <= (V == DV_U ? m.ide - 1 : m.ide - 2)));
+  return x && (!oys || j >= m.jds + 1) && (!oye || j <= (V == DV_V ? m.jde - 1 : m.jde - 2));
+}
+__device__ __forceinline__ bool vdiff_open_in(const Mem& m, int V, int i, int j) {
+  if (V == VD_U) return m.cf.periodic_x || ((!m.cf.open_xs || i >= m.ids + 1) && (!m.cf.open_xe || i <= m.ide - 1));
+  if (V == VD_V) return (!m.cf.open_ys || j >= m.jds + 1) && (!m.cf.open_ye || j <= m.jde - 1);
+  return true;
+}
+__device__ __forceinline__ bool diff6_open_in(const Mem& m, int V, int i, int j) {
+  const bool oxs = m.cf.open_xs, oxe = m.cf.open_xe, oys = m.cf.open_ys, oye = m.cf.open_ye;
+  const int ids = m.ids, ide = m.ide, jds = m.jds, jde = m.jde;
+  if (V == DV_V && oxs)  // :6383-6388: all four limits on open_xs
+    return i >= ids + 3 && i <= ide - 4 && j >= jds + 3 && j <= jde - 3;
+  const int xe = V == DV_U ? ide - 3 : ide - 4, ye = V == DV_V ? jde - 3 : jde - 4;
+  return (!oxs || i >= ids + 3) && (!oxe || i <= xe) && (!oys || j >= jds + 3) && (!oye || j <= ye);
+}
+
 // Stage 1, mode 0 (rk_tendency): the forward-in-time tendencies ru_tendf,
 // rv_tendf, rw_tendf and t_tendf of u_2, v_2, w_2 and t_2: the explicit
 // diffusion (diff_opt = 1; mut, khdif, kvdif), then the sixth-order diffusion
 // (mut, the large step dt).  Mode 1 (rk_scalar_tend, after the acoustic
 // steps): each diffused species' sc_tend, with muts, khdif / prandtl,
 // kvdif / prandtl and the stage's dt (dt / 3); qv (species 0) diffuses
-// vertically against its base profile qv_base.  Loop limits of periodic /
-// symmetric boundaries (:2760-2790, :3100-3130, :6330-6443); points outside
-// them keep the zero the buffers were created with.  Mode 2 is mode 0 added
+// vertically against its base profile qv_base.  Loop limits of :2760-2790,
+// :3100-3130, :6330-6443 (open boundaries: each term its own, above);
+// points outside them get no term.  Mode 2 is mode 0 added
 // onto the stored tendencies' values (the routine-level rk_tendency, whose
 // *_tendf arrays arrive holding the physics tendencies).
 __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
@@ -293,12 +317,12 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
       const F3 q = f3p(m, m.q[s]);
       float t = 0.f;
       if (mix2_on(m, s)) {
-        t = t + hdiff_point<DV_M>(m, q, nullptr, muts, c1, c2, i, k, j, khdq);
+        if (hdiff_open_in(m, DV_M, i, j)) t = t + hdiff_point<DV_M>(m, q, nullptr, muts, c1, c2, i, k, j, khdq);
         const float mu = muts.ro(i, j);
         t = t + (s == 0 ? vdiff_point<VD_MP>(m, q, qvb, nullptr, mu, c1, c2, i, k, j, kvdq)
                         : vdiff_point<VD_M>(m, q, qvb, nullptr, mu, c1, c2, i, k, j, kvdq));
       }
-      if (mix6_on(m, s)) t = diff6_point<DV_M>(m, q, muts, i, k, j, c1, c2, coef, t);
+      if (mix6_on(m, s) && diff6_open_in(m, DV_M, i, j)) t = diff6_point<DV_M>(m, q, muts, i, k, j, c1, c2, coef, t);
       f3p(m, sc)(i, k, j) = t;
     }
     return;
@@ -311,24 +335,24 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
     const F3 u = f3(m, WRFGPU_U_2);
     float t = acc ? f3p(m, m.tendf[0])(i, k, j) : 0.f;
     if (d1) {
-      t = t + hdiff_point<DV_U>(m, u, nullptr, mut, c1, c2, i, k, j, xkmh);
-      if (k <= ktf - 1)
+      if (hdiff_open_in(m, DV_U, i, j)) t = t + hdiff_point<DV_U>(m, u, nullptr, mut, c1, c2, i, k, j, xkmh);
+      if (k <= ktf - 1 && vdiff_open_in(m, VD_U, i, j))
         t = t + vdiff_point<VD_U>(m, u, f1(m, WRFGPU_U_BASE), nullptr, f2(m, WRFGPU_MUU).ro(i, j), c1, c2, i, k, j,
                                   kvdif);
     }
-    if (d6) t = diff6_point<DV_U>(m, u, mut, i, k, j, c1, c2, coef, t);
+    if (d6 && diff6_open_in(m, DV_U, i, j)) t = diff6_point<DV_U>(m, u, mut, i, k, j, c1, c2, coef, t);
     f3p(m, m.tendf[0])(i, k, j) = t;
   }
   if (i <= i_end && j <= m.jte) {
     const F3 v = f3(m, WRFGPU_V_2);
     float t = acc ? f3p(m, m.tendf[1])(i, k, j) : 0.f;
     if (d1) {
-      t = t + hdiff_point<DV_V>(m, v, nullptr, mut, c1, c2, i, k, j, xkmh);
-      if (k <= ktf - 1 && j <= j_end)
+      if (hdiff_open_in(m, DV_V, i, j)) t = t + hdiff_point<DV_V>(m, v, nullptr, mut, c1, c2, i, k, j, xkmh);
+      if (k <= ktf - 1 && j <= j_end && vdiff_open_in(m, VD_V, i, j))
         t = t + vdiff_point<VD_V>(m, v, f1(m, WRFGPU_V_BASE), nullptr, f2(m, WRFGPU_MUV).ro(i, j), c1, c2, i, k, j,
                                   kvdif);
     }
-    if (d6) t = diff6_point<DV_V>(m, v, mut, i, k, j, c1, c2, coef, t);
+    if (d6 && diff6_open_in(m, DV_V, i, j)) t = diff6_point<DV_V>(m, v, mut, i, k, j, c1, c2, coef, t);
     f3p(m, m.tendf[1])(i, k, j) = t;
   }
   if (i <= i_end && j <= j_end) {
@@ -338,19 +362,19 @@ __global__ void __launch_bounds__(BX* BY) k_forward_diff(Launch L, int mode) {
       const float c1w = f1(m, WRFGPU_C1F)(k), c2w = f1(m, WRFGPU_C2F)(k);
       float t = acc ? f3p(m, m.tendf[2])(i, k, j) : 0.f;
       if (d1) {
-        t = t + hdiff_point<DV_W>(m, w, nullptr, mut, c1w, c2w, i, k, j, xkmh);
+        if (hdiff_open_in(m, DV_W, i, j)) t = t + hdiff_point<DV_W>(m, w, nullptr, mut, c1w, c2w, i, k, j, xkmh);
         t = t + vdiff_point<VD_W>(m, w, c1h, nullptr, mt, c1w, c2w, i, k, j, kvdif);
       }
-      if (d6) t = diff6_point<DV_W>(m, w, mut, i, k, j, c1w, c2w, coef, t);
+      if (d6 && diff6_open_in(m, DV_W, i, j)) t = diff6_point<DV_W>(m, w, mut, i, k, j, c1w, c2w, coef, t);
       f3p(m, m.tendf[2])(i, k, j) = t;
     }
     const F3 th = f3(m, WRFGPU_T_2), tb = f3(m, WRFGPU_T_INIT);
     float t = acc ? f3p(m, m.tendf[3])(i, k, j) : 0.f;
     if (d1) {
-      t = t + hdiff_point<DV_M>(m, th, &tb, mut, c1, c2, i, k, j, xkhh);
+      if (hdiff_open_in(m, DV_M, i, j)) t = t + hdiff_point<DV_M>(m, th, &tb, mut, c1, c2, i, k, j, xkhh);
       t = t + vdiff_point<VD_3DMP>(m, th, c1h, &tb, mt, c1, c2, i, k, j, 3.f * kvdif);
     }
-    if (d6) t = diff6_point<DV_M>(m, th, mut, i, k, j, c1, c2, coef, t);
+    if (d6 && diff6_open_in(m, DV_M, i, j)) t = diff6_point<DV_M>(m, th, mut, i, k, j, c1, c2, coef, t);
     f3p(m, m.tendf[3])(i, k, j) = t;
   }
 }
@@ -376,12 +400,12 @@ __global__ void __launch_bounds__(BX* BY) k_species_diff_routine(Launch L, int q
   float t = out(i, k, j);
   if (mix2_on(m, 0)) {
     const float kvdq = m.cf.kvdif / PRANDTL;
-    t = t + hdiff_point<DV_M>(m, q, nullptr, muts, c1, c2, i, k, j, m.cf.khdif / PRANDTL);
+    if (hdiff_open_in(m, DV_M, i, j)) t = t + hdiff_point<DV_M>(m, q, nullptr, muts, c1, c2, i, k, j, m.cf.khdif / PRANDTL);
     const F1 qvb = f1(m, WRFGPU_QV_BASE);
     t = t + (qv ? vdiff_point<VD_MP>(m, q, qvb, nullptr, muts.ro(i, j), c1, c2, i, k, j, kvdq)
                 : vdiff_point<VD_M>(m, q, qvb, nullptr, muts.ro(i, j), c1, c2, i, k, j, kvdq));
   }
-  if (mix6_on(m, 0)) {
+  if (mix6_on(m, 0) && diff6_open_in(m, DV_M, i, j)) {
     const float coef = m.cf.diff_6th_factor * 0.015625f / (2.0f * stage_of(m, 1).dt_rk);
     t = diff6_point<DV_M>(m, q, muts, i, k, j, c1, c2, coef, t);
   }

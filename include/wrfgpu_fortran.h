@@ -98,7 +98,10 @@ int wrfgpu_rk_tendency(const WrfDynConfig *config_flags, const int *rk_step, flo
                        WRFGPU_DIMS_ARGS, float *max_vert_cfl, float *max_horiz_cfl);
 
 /* dyn_em/module_advect_em.F:126, :1530, :4364 advect_u / advect_v / advect_w
- * (tendency += -div(flux)); time_step is only used for its sign (forward). */
+ * (tendency += -div(flux)); time_step is only used for its sign (forward).
+ * fld_old enters only the radiation terms of open boundaries, where the
+ * reference's callers (rk_tendency, rk_scalar_tend) pass fld itself: with
+ * open boundaries a different fld_old returns WRFGPU_E_ARG. */
 #define WRFGPU_ADVECT_MOM_ARGS                                                                             \
   const float *fld, const float *fld_old, float *tendency, const float *ru, const float *rv, const float *rom, \
       const float *c1, const float *c2, const float *mut, const int *time_step, const WrfDynConfig *config_flags, \
@@ -214,7 +217,9 @@ int wrfgpu_sumflux(const float *ru, const float *rv, const float *ww, const floa
                    const float *msfuy, const float *msfvx, const float *msfvx_inv, const float *msfvy,
                    const int *iteration, const int *number_of_small_timesteps, WRFGPU_DIMS_ARGS);
 
-/* dyn_em/module_small_step_em.F:295 small_step_finish (h_diabatic unused) */
+/* dyn_em/module_small_step_em.F:295 small_step_finish (h_diabatic unused);
+ * muus and muvs are read as given (solve_em forms them with calc_mu_uv_1
+ * just before, solve_em.F:1732). */
 int wrfgpu_small_step_finish(float *u_2, const float *u_1, float *v_2, const float *v_1, float *w_2,
                              const float *w_1, float *t_2, const float *t_1, float *ph_2, const float *ph_1,
                              float *ww, const float *ww1, float *mu_2, const float *mu_1, const float *mut,

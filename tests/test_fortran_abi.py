@@ -137,6 +137,38 @@ def _state(case, full=False):
     return od
 
 
+def _calc_mu_uv_1(case, od):
+    """muus, muvs from muts as solve_em's calc_mu_uv_1 forms them before
+    small_step_finish (module_big_step_utilities_em.F:184-326: the
+    boundary point one-sided where the direction is not periodic), set into
+    the oracle state so that the entry point receives them."""
+    h = abi.HALO
+    cf = case.desc.config
+    ni, nj = case.ide + 2 * h, case.jde + 2 * h
+    mu = np.asarray(od.get(abi.FIELD_ID["muts"]), dtype=np.float32).reshape(nj, ni)
+    half = np.float32(0.5)
+    muus = np.asarray(od.get(abi.FIELD_ID["muus"]), dtype=np.float32).reshape(nj, ni).copy()
+    muvs = np.asarray(od.get(abi.FIELD_ID["muvs"]), dtype=np.float32).reshape(nj, ni).copy()
+    for jj in range(1, case.jde):
+        for ii in range(1, case.ide + 1):
+            a, b = ii, ii - 1
+            if ii == 1 and not cf.periodic_x:
+                b = ii
+            if ii == case.ide and not cf.periodic_x:
+                a = ii - 1
+            muus[jj + h - 1, ii + h - 1] = half * (mu[jj + h - 1, a + h - 1] + mu[jj + h - 1, b + h - 1])
+    for jj in range(1, case.jde + 1):
+        for ii in range(1, case.ide):
+            a, b = jj, jj - 1
+            if jj == 1 and not cf.periodic_y:
+                b = jj
+            if jj == case.jde and not cf.periodic_y:
+                a = jj - 1
+            muvs[jj + h - 1, ii + h - 1] = half * (mu[a + h - 1, ii + h - 1] + mu[b + h - 1, ii + h - 1])
+    od.set(abi.FIELD_ID["muus"], muus.astype(np.float64))
+    od.set(abi.FIELD_ID["muvs"], muvs.astype(np.float64))
+
+
 def _fid(name):
     if name == "qv":
         return abi.species_id(0)
@@ -247,6 +279,8 @@ def test_routine_abi_bitwise(gpulib, case, routine):
     if routine == "small_step_finish":
         it = 0
     od = _state(case, full=routine in FULL_STATE)
+    if routine == "small_step_finish":
+        _calc_mu_uv_1(case, od)
     scal = _scalars(case, rk, it)
     rc, arrays = _call(gpulib, routine, spec, od, case, scal)
     assert rc == 0, "%s returned %d" % (routine, rc)
@@ -260,6 +294,19 @@ def test_routine_abi_bitwise(gpulib, case, routine):
         if d != 0.0:
             bad.append("%s: max|diff| %.3e" % (nm, d))
     assert not bad, "%s: %s" % (routine, "; ".join(bad))
+
+
+@pytest.fixture(scope="module")
+def case_open():
+    return cases.open_boundaries(cases.small_case(nx=24, ny=20, kde=14, n_scalar=1, seed=22))
+
+
+@pytest.mark.parametrize("routine", sorted(ROUTINES))
+def test_routine_abi_open_boundaries_bitwise(gpulib, case_open, routine):
+    """Every routine-level entry point with open lateral boundaries on all
+    four sides (the em_quarter_ss namelist): the degraded fluxes, radiation
+    terms and boundary limits of the reference routines, bit for bit."""
+    test_routine_abi_bitwise(gpulib, case_open, routine)
 
 
 @pytest.mark.parametrize("routine", ["advance_uv", "calc_p_rho", "rk_step_prep", "advance_w", "small_step_finish"])
@@ -276,6 +323,8 @@ def test_routine_abi_tiles_and_wide_halo(gpulib, case, routine):
     if routine == "small_step_finish":
         it = 0
     od = _state(case, full=routine in FULL_STATE)
+    if routine == "small_step_finish":
+        _calc_mu_uv_1(case, od)
     scal = _scalars(case, rk, it)
     rc, ref = _call(gpulib, routine, spec, od, case, scal)
     assert rc == 0

@@ -1007,6 +1007,7 @@ struct Ensemble {
       case 17: launch_advance_w(l2, nb2, a, fp64, stream); break;
       case 18: launch_sumflux(l3, nb3, a, stream); break;
       case 19: launch_small_step_finish(l2, nb2, a, stream); break;
+      case 119: launch_small_step_finish(l2, nb2, a, stream, TUNE_DEFAULT[TU_SSF], false); break;  // muus, muvs given
       case 20: launch_update_scalar_pd(l3, nb3, a, stream); break;
       case 21: launch_advect_scalar(l3, nb3, StepArgs{rk_step, 0, species, 0}, stream); break;
       case 22: launch_advect_scalar_pd2(l3, nb3, StepArgs{rk_step, 0, species, 2}, d_pd_scratch, stream); break;

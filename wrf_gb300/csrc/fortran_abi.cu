@@ -188,7 +188,9 @@ int wrfgpu_advect_u(const float* u, const float* u_old, float* tendency, const f
                     const WrfDynConfig* config_flags, const float* msfux, const float* msfuy, const float* msfvx,
                     const float* msfvy, const float* msftx, const float* msfty, const float* fzm, const float* fzp,
                     const float* rdx, const float* rdy, const float* rdzw, WRFGPU_DIMS_ARGS) {
-  (void)u_old;
+  // the old field enters only the radiation terms of open boundaries, and
+  // the reference's calls (rk_tendency, rk_scalar_tend) pass the field itself
+  if (u_old != u && config_flags && (config_flags->open_xs || config_flags->open_ys)) return WRFGPU_E_ARG;
   return advect_common(WRFGPU_R_ADVECT_U, WRFGPU_U_2, WRFGPU_RU_TEND, WRFGPU_RDNW, u, tendency, ru, rv, rom, c1, c2,
                        mut, time_step, config_flags, msfux, msfuy, msfvx, msfvy, msftx, msfty, fzm, fzp, rdx, rdy,
                        rdzw, DIMS);
@@ -198,7 +200,9 @@ int wrfgpu_advect_v(const float* v, const float* v_old, float* tendency, const f
                     const WrfDynConfig* config_flags, const float* msfux, const float* msfuy, const float* msfvx,
                     const float* msfvy, const float* msftx, const float* msfty, const float* fzm, const float* fzp,
                     const float* rdx, const float* rdy, const float* rdzw, WRFGPU_DIMS_ARGS) {
-  (void)v_old;
+  // the old field enters only the radiation terms of open boundaries, and
+  // the reference's calls (rk_tendency, rk_scalar_tend) pass the field itself
+  if (v_old != v && config_flags && (config_flags->open_xs || config_flags->open_ys)) return WRFGPU_E_ARG;
   return advect_common(WRFGPU_R_ADVECT_V, WRFGPU_V_2, WRFGPU_RV_TEND, WRFGPU_RDNW, v, tendency, ru, rv, rom, c1, c2,
                        mut, time_step, config_flags, msfux, msfuy, msfvx, msfvy, msftx, msfty, fzm, fzp, rdx, rdy,
                        rdzw, DIMS);
@@ -208,7 +212,9 @@ int wrfgpu_advect_w(const float* w, const float* w_old, float* tendency, const f
                     const WrfDynConfig* config_flags, const float* msfux, const float* msfuy, const float* msfvx,
                     const float* msfvy, const float* msftx, const float* msfty, const float* fzm, const float* fzp,
                     const float* rdx, const float* rdy, const float* rdzu, WRFGPU_DIMS_ARGS) {
-  (void)w_old;
+  // the old field enters only the radiation terms of open boundaries, and
+  // the reference's calls (rk_tendency, rk_scalar_tend) pass the field itself
+  if (w_old != w && config_flags && (config_flags->open_xs || config_flags->open_ys)) return WRFGPU_E_ARG;
   return advect_common(WRFGPU_R_ADVECT_W, WRFGPU_W_2, WRFGPU_RW_TEND, WRFGPU_RDN, w, tendency, ru, rv, rom, c1, c2,
                        mut, time_step, config_flags, msfux, msfuy, msfvx, msfvy, msftx, msfty, fzm, fzp, rdx, rdy,
                        rdzu, DIMS);
@@ -219,7 +225,9 @@ int wrfgpu_advect_scalar(const float* field, const float* field_old, float* tend
                          const float* msfuy, const float* msfvx, const float* msfvy, const float* msftx,
                          const float* msfty, const float* fzm, const float* fzp, const float* rdx, const float* rdy,
                          const float* rdzw, WRFGPU_DIMS_ARGS) {
-  (void)field_old;
+  // the old field enters only the radiation terms of open boundaries, and
+  // the reference's calls (rk_tendency, rk_scalar_tend) pass the field itself
+  if (field_old != field && config_flags && (config_flags->open_xs || config_flags->open_ys)) return WRFGPU_E_ARG;
   return advect_common(121, WRFGPU_SPECIES_BASE, WRFGPU_ADVECT_TEND, WRFGPU_RDNW, field, tendency, ru, rv, rom, c1,
                        c2, mut, time_step, config_flags, msfux, msfuy, msfvx, msfvy, msftx, msfty, fzm, fzp, rdx,
                        rdy, rdzw, DIMS);
@@ -442,7 +450,8 @@ int wrfgpu_small_step_finish(float* u_2, const float* u_1, float* v_2, const flo
   (void)h_diabatic;
   FCall c;
   set_dims(c, DIMS);
-  c.cfg = default_cfg(0); c.routine = WRFGPU_R_SMALL_STEP_FINISH; c.rk_step = *rk_step;
+  // small_step_finish reads the muus, muvs its caller formed with calc_mu_uv_1
+  c.cfg = default_cfg(0); c.routine = 119; c.rk_step = *rk_step;
   c.nsmall = *number_of_small_timesteps; c.dts = *dts;
   RW(WRFGPU_U_2, u_2); R(WRFGPU_U_1, u_1); RW(WRFGPU_V_2, v_2); R(WRFGPU_V_1, v_1); RW(WRFGPU_W_2, w_2);
   R(WRFGPU_W_1, w_1); RW(WRFGPU_T_2, t_2); R(WRFGPU_T_1, t_1); RW(WRFGPU_PH_2, ph_2); R(WRFGPU_PH_1, ph_1);

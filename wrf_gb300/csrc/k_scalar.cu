@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(STRIP_THREADS) k_strip_pd_scale(StripLaunch L,
   const int i = sp.i, j = sp.j, k = sp.k;
   if (k < m.kts || k > min(m.kte, m.kde - 1)) return;
   const Stage st = stage_of(m, rk_step);
-  const PDCtx c = pd_ctx(m, s, st.dt_rk);
+  const PDCtx c = pd_ctx(m, s, st.dt_rk, true);
   f3p(m, scratch[sp.m])(i, k, j) = pd_scale_cell(m, c, i, k, j);
 }
 __global__ void __launch_bounds__(STRIP_THREADS) k_strip_pd_tend(StripLaunch L, int rk_step, int s,
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(STRIP_THREADS) k_strip_pd_tend(StripLaunch L, 
   const int i = sp.i, j = sp.j, k = sp.k;
   if (!mass_pt(m, i, j) || k < m.kts || k > min(m.kte, m.kde - 1)) return;
   const Stage st = stage_of(m, rk_step);
-  const PDCtx c = pd_ctx(m, s, st.dt_rk);
+  const PDCtx c = pd_ctx(m, s, st.dt_rk, true);
   const F3 sc = f3p(m, scratch[sp.m]);
   const float t = pd_tend_cell(m, c, i, k, j, 0.f, [&](int ci, int ck, int cj) { return sc(ci, ck, cj); });
   strip_update(m, s, rk_step, i, j, k, f2(m, WRFGPU_MSFTY)(i, j) * t);

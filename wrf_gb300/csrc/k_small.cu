@@ -643,8 +643,11 @@ __global__ void __launch_bounds__(BX* BY) k_sumflux_p_rho(Launch L, int rk_step,
 }
 
 // ------------------------------------------------------------ small_step_finish
+// calc_mus: form muus, muvs from muts here (calc_mu_uv_1, which solve_em
+// calls right before small_step_finish, solve_em.F:1732); otherwise take the
+// caller's (the routine's own interface: it reads them).
 template <int MINB>
-__global__ void __launch_bounds__(BX* BY, MINB) k_small_step_finish(Launch L, int rk_step) {
+__global__ void __launch_bounds__(BX* BY, MINB) k_small_step_finish(Launch L, int rk_step, bool calc_mus) {
   BlockPos bp = block_pos(L);
   const Mem& m = block_member(L.mem, bp.m);
   if (!bp.valid) return;
@@ -658,13 +661,15 @@ __global__ void __launch_bounds__(BX* BY, MINB) k_small_step_finish(Launch L, in
   // calc_mu_uv_1 on (muts -> muus, muvs)
   float muus = 0.f, muvs = 0.f;
   const bool upt = j <= j_end, vpt = i <= i_end;
-  if (upt) {
+  if (upt && !calc_mus) muus = MUU(i, j);
+  if (vpt && !calc_mus) muvs = MUV(i, j);
+  if (upt && calc_mus) {
     if (i == m.ids && m.its == m.ids) { int im = px ? i - 1 : i; muus = 0.5f * (MU(i, j) + MU(im, j)); }
     else if (i == m.ide && m.ite == m.ide) { int im = px ? i : i - 1; muus = 0.5f * (MU(i - 1, j) + MU(im, j)); }
     else muus = 0.5f * (MU(i, j) + MU(i - 1, j));
     MUU(i, j) = muus;
   }
-  if (vpt) {
+  if (vpt && calc_mus) {
     if (j == m.jds && m.jts == m.jds) { int jm = py ? j - 1 : j; muvs = 0.5f * (MU(i, j) + MU(i, jm)); }
     else if (j == m.jde && m.jte == m.jde) { int jm = py ? j : j - 1; muvs = 0.5f * (MU(i, j - 1) + MU(i, jm)); }
     else muvs = 0.5f * (MU(i, j) + MU(i, j - 1));
@@ -755,10 +760,10 @@ void launch_sumflux_p_rho(const Launch& L, int nb, StepArgs a, bool do_p_rho, cu
   k_sumflux_p_rho<<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, a.iteration, do_p_rho ? 1 : 0);
 }
 void launch_sumflux(const Launch& L, int nb, StepArgs a, cudaStream_t s) { launch_sumflux_p_rho(L, nb, a, false, s); }
-void launch_small_step_finish(const Launch& L, int nb, StepArgs a, cudaStream_t s, int var) {
+void launch_small_step_finish(const Launch& L, int nb, StepArgs a, cudaStream_t s, int var, bool calc_mus) {
   // 4 blocks of 128 threads per SM leave the registers free (~80); 8 hold them to 64
-  if (var == 0) k_small_step_finish<4><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
-  else k_small_step_finish<8><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step);
+  if (var == 0) k_small_step_finish<4><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, calc_mus);
+  else k_small_step_finish<8><<<nb, dim3(BX, BY), 0, s>>>(L, a.rk_step, calc_mus);
 }
 
 }  // namespace wrfgpu

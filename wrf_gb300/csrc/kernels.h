@@ -88,7 +88,9 @@ void launch_advance_mu_t(const Launch& L2, int nblocks, StepArgs a, bool fp64, c
 void launch_advance_w(const Launch& L2, int nblocks, StepArgs a, bool fp64, cudaStream_t s);
 void launch_sumflux_p_rho(const Launch& L3, int nblocks, StepArgs a, bool do_p_rho, cudaStream_t s);
 void launch_sumflux(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);
-void launch_small_step_finish(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s, int var = TUNE_DEFAULT[TU_SSF]);
+// calc_mus: calc_mu_uv_1 fused in (the step); false: the caller's muus, muvs
+void launch_small_step_finish(const Launch& L2, int nblocks, StepArgs a, cudaStream_t s, int var = TUNE_DEFAULT[TU_SSF],
+                              bool calc_mus = true);
 
 // scalars and diagnosis
 void launch_update_scalar_pd(const Launch& L3, int nblocks, StepArgs a, cudaStream_t s);

@@ -183,12 +183,21 @@ struct PDCtx {
   F1 c1, c2, fzm, fzp, rdzw;
   float rdx, rdy, dt;
   int kts, ktf, kde;
+  // the faces' Courant numbers and low-order flux factors formed once per
+  // step by k_pd_courant (the same expressions, so the same bits), when set
+  bool pre;
+  F3 crx, cry, crz, lfx, lfy, lfz;
 };
-__device__ __forceinline__ PDCtx pd_ctx(const Mem& m, int species, float dt) {
+__device__ __forceinline__ PDCtx pd_ctx(const Mem& m, int species, float dt, bool pre = false) {
   PDCtx c{f3p(m, m.q[species]), f3p(m, m.qo[species]), f3(m, WRFGPU_RU_M), f3(m, WRFGPU_RV_M), f3(m, WRFGPU_WW_M),
           f2(m, WRFGPU_MUTS), f2(m, WRFGPU_MUB), f2(m, WRFGPU_MU_1), f2(m, WRFGPU_MSFTX), f2(m, WRFGPU_MSFTY),
           f1(m, WRFGPU_C1H), f1(m, WRFGPU_C2H), f1(m, WRFGPU_FNM), f1(m, WRFGPU_FNP), f1(m, WRFGPU_RDNW),
-          m.rdx, m.rdy, dt, m.kts, min(m.kte, m.kde - 1), m.kde};
+          m.rdx, m.rdy, dt, m.kts, min(m.kte, m.kde - 1), m.kde, false};
+  if (pre && m.pdc[0]) {
+    c.pre = true;
+    c.crx = f3p(m, m.pdc[0]); c.cry = f3p(m, m.pdc[1]); c.crz = f3p(m, m.pdc[2]);
+    c.lfx = f3p(m, m.pdc[3]); c.lfy = f3p(m, m.pdc[4]); c.lfz = f3p(m, m.pdc[5]);
+  }
   return c;
 }
 // Face fluxes (module_advect_em.F:6505-6779): *hi = high-order minus upwind,
@@ -197,17 +206,25 @@ __device__ __forceinline__ PDCtx pd_ctx(const Mem& m, int species, float dt) {
 // faces as ru dt / dx / mu.
 __device__ __forceinline__ void pd_fx(const Mem& m, const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
   const int o = open_order_mass(i, m.cf.open_xs, m.cf.open_xe, m.ids, m.ide);
-  const float dx = 2.f / (c.msfty(i, j) + c.msfty(i - 1, j)) / c.rdx;
-  const float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i - 1, j) + c.c2(k)));
-  float vel, cr;
-  if (o == 2 && m.cf.open_xs && i == m.ids + 1) {
-    vel = c.ru(i, k, j) / mu;
-    cr = vel * c.dt / dx;
-  } else {
+  const bool quirk = o == 2 && m.cf.open_xs && i == m.ids + 1;
+  float vel, cr, lf;
+  if (c.pre && !quirk) {
     vel = c.ru(i, k, j);
-    cr = vel * c.dt / dx / mu;
+    cr = c.crx(i, k, j);
+    lf = c.lfx(i, k, j);
+  } else {
+    const float dx = 2.f / (c.msfty(i, j) + c.msfty(i - 1, j)) / c.rdx;
+    const float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i - 1, j) + c.c2(k)));
+    if (quirk) {
+      vel = c.ru(i, k, j) / mu;
+      cr = vel * c.dt / dx;
+    } else {
+      vel = c.ru(i, k, j);
+      cr = vel * c.dt / dx / mu;
+    }
+    lf = mu * (dx / c.dt);
   }
-  const float l = mu * (dx / c.dt) * flux_upwind(c.fo(i - 1, k, j), c.fo(i, k, j), cr);
+  const float l = lf * flux_upwind(c.fo(i - 1, k, j), c.fo(i, k, j), cr);
   float h;
   if (o == 5)
     h = vel * pflux5(c.f(i - 3, k, j), c.f(i - 2, k, j), c.f(i - 1, k, j), c.f(i, k, j), c.f(i + 1, k, j), c.f(i + 2, k, j), vel);
@@ -219,11 +236,18 @@ __device__ __forceinline__ void pd_fx(const Mem& m, const PDCtx& c, int i, int k
 }
 __device__ __forceinline__ void pd_fy(const Mem& m, const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
   const int o = open_order_mass(j, m.cf.open_ys, m.cf.open_ye, m.jds, m.jde);
-  const float dy = 2.f / (c.msftx(i, j) + c.msftx(i, j - 1)) / c.rdy;
-  const float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j - 1) + c.c2(k)));
   const float vel = c.rv(i, k, j);
-  const float cr = vel * c.dt / dy / mu;
-  const float l = mu * (dy / c.dt) * flux_upwind(c.fo(i, k, j - 1), c.fo(i, k, j), cr);
+  float cr, lf;
+  if (c.pre) {
+    cr = c.cry(i, k, j);
+    lf = c.lfy(i, k, j);
+  } else {
+    const float dy = 2.f / (c.msftx(i, j) + c.msftx(i, j - 1)) / c.rdy;
+    const float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j - 1) + c.c2(k)));
+    cr = vel * c.dt / dy / mu;
+    lf = mu * (dy / c.dt);
+  }
+  const float l = lf * flux_upwind(c.fo(i, k, j - 1), c.fo(i, k, j), cr);
   float h;
   if (o == 5)
     h = vel * pflux5(c.f(i, k, j - 3), c.f(i, k, j - 2), c.f(i, k, j - 1), c.f(i, k, j), c.f(i, k, j + 1), c.f(i, k, j + 2), vel);
@@ -235,11 +259,18 @@ __device__ __forceinline__ void pd_fy(const Mem& m, const PDCtx& c, int i, int k
 }
 __device__ __forceinline__ void pd_fz(const PDCtx& c, int i, int k, int j, float* hi, float* lo) {
   if (k == 1 || k == c.kde) { *hi = 0.f; *lo = 0.f; return; }
-  const float dz = 2.f / (c.rdzw(k) + c.rdzw(k - 1));
-  const float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j) + c.c2(k)));
   const float vel = c.rom(i, k, j);
-  const float cr = vel * c.dt / dz / mu;
-  const float l = mu * (dz / c.dt) * flux_upwind(c.fo(i, k - 1, j), c.fo(i, k, j), cr);
+  float cr, lf;
+  if (c.pre) {
+    cr = c.crz(i, k, j);
+    lf = c.lfz(i, k, j);
+  } else {
+    const float dz = 2.f / (c.rdzw(k) + c.rdzw(k - 1));
+    const float mu = 0.5f * ((c.c1(k) * c.mut(i, j) + c.c2(k)) + (c.c1(k) * c.mut(i, j) + c.c2(k)));
+    cr = vel * c.dt / dz / mu;
+    lf = mu * (dz / c.dt);
+  }
+  const float l = lf * flux_upwind(c.fo(i, k - 1, j), c.fo(i, k, j), cr);
   float h;
   if (k == c.kts + 1 || k == c.ktf) h = c.rom(i, k, j) * (c.fzm(k) * c.f(i, k, j) + c.fzp(k) * c.f(i, k - 1, j));
   else h = vel * pflux3(c.f(i, k - 2, j), c.f(i, k - 1, j), c.f(i, k, j), c.f(i, k + 1, j), -vel);

@@ -773,18 +773,20 @@ def open_boundaries(case, x=True, y=True):
     ide, jde = case.ide, case.jde
 
     def clamp(a, kind, stag):
+        # memory index p holds point p + 1 - h; points beyond 1 .. hi take
+        # the value of the nearest of the two (x first, then y)
         if a.ndim != kind:
             return a
-        out = a
+        out = np.array(a, copy=True, order="C")
         if x:
             hi = ide if stag == "u" else ide - 1
-            ix = np.clip(np.arange(1 - h, 1 - h + a.shape[-1]), 1, hi) + h - 1
-            out = out[..., ix]
+            out[..., :h] = out[..., h:h + 1]
+            out[..., hi + h:] = out[..., hi + h - 1:hi + h]
         if y:
             hi = jde if stag == "v" else jde - 1
-            jy = np.clip(np.arange(1 - h, 1 - h + a.shape[0]), 1, hi) + h - 1
-            out = out[jy]
-        return np.ascontiguousarray(out)
+            out[:h] = out[h:h + 1]
+            out[hi + h:] = out[hi + h - 1:hi + h]
+        return out
 
     fields = {}
     for nm, a in case.fields.items():

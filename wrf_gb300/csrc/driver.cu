@@ -234,6 +234,7 @@ struct Ensemble {
     size_t count = 0, cols = 0, rows = 0, pitch = 0;
     float* stage = nullptr;  // contiguous device copy
     bool prefetch = false;   // the next step's input may cross during this step's last stage
+    bool tail = false;       // the next step's input may cross right behind this step's final downloads
   };
   std::vector<HostIO> hio;
   cudaStream_t cstream = nullptr;  // downloads of the host I/O step that overlap its kernels
@@ -251,6 +252,7 @@ struct Ensemble {
   bool io_step = false;     // enqueue_step runs inside a host I/O step
   bool io_out_pending = false;
   cudaEvent_t ev_ofork = nullptr, ev_ojoin = nullptr, ev_dryin = nullptr;
+  cudaEvent_t ev_tfork = nullptr, ev_tjoin = nullptr, ev_tjoin2 = nullptr;
 
   void io_join() {
     if (!io_pending) return;
@@ -315,9 +317,14 @@ struct Ensemble {
   // previous step's last stage when its staging buffer is free then (no
   // output, or an output downloaded at that same point) and its host array
   // overlaps no output downloaded later in the step.
+  // Every other early input may cross at the end of the previous step, each
+  // behind the final downloads that free its staging buffer or write its host
+  // input, unless a passive scalar's download (left for the next step's
+  // head) writes part of its host input.
   void set_prefetch() {
     for (HostIO& b : hio) {
       b.prefetch = b.in && !b.late && (!b.out || early_out(b));
+      b.tail = false;
       if (!b.prefetch) continue;
       const char* lo = (const char*)b.in;
       const char* hi = lo + b.count * 4;
@@ -326,6 +333,18 @@ struct Ensemble {
         const char* glo = (const char*)g.out;
         const char* ghi = glo + g.count * 4;
         if (lo < ghi && glo < hi) { b.prefetch = false; break; }
+      }
+    }
+    for (HostIO& b : hio) {
+      if (!b.in || b.late || b.prefetch) continue;
+      b.tail = true;
+      const char* lo = (const char*)b.in;
+      const char* hi = lo + b.count * 4;
+      for (const HostIO& g : hio) {
+        if (!g.out || !deferrable(g)) continue;
+        const char* glo = (const char*)g.out;
+        const char* ghi = glo + g.count * 4;
+        if (lo < ghi && glo < hi) { b.tail = false; break; }
       }
     }
   }
@@ -396,9 +415,14 @@ struct Ensemble {
       ev_dn.push_back(e);
     }
     if (cstream) return WRFGPU_OK;
-    CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&ustream, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin, &ev_head, &ev_ojoin2})
+    // the copy streams' pack / unpack kernels take SM slots ahead of the
+    // step's waiting blocks, so a copy does not wait for a long kernel to drain
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&cstream, cudaStreamNonBlocking, greatest));
+    CK(cudaStreamCreateWithPriority(&ustream, cudaStreamNonBlocking, greatest));
+    for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin, &ev_head, &ev_ojoin2, &ev_tfork,
+                           &ev_tjoin, &ev_tjoin2})
       CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     return WRFGPU_OK;
   }
@@ -437,7 +461,7 @@ struct Ensemble {
     // ... the dry state and the moist species first on the other, at the
     // link's full rate (those prefetched during the previous step are across)
     for (const HostIO& b : hio)
-      if (b.in && !b.late && !(head && b.prefetch))
+      if (b.in && !b.late && !(head && (b.prefetch || b.tail)))
         CK(cudaMemcpyAsync(b.stage, b.in, b.count * 4, cudaMemcpyHostToDevice, stream));
     CK(cudaEventRecord(ev_dryin, stream));
     for (const HostIO& b : hio)
@@ -459,12 +483,34 @@ struct Ensemble {
     io_prefetch = false;
     io_join();
     (void)late;
-    for (const HostIO& b : hio)
-      if (b.out && !early_out(b) && !(defer && deferrable(b))) copy_out(b, stream);
     if (io_out_pending) {
       CK(cudaStreamWaitEvent(stream, ev_ojoin, 0));
       CK(cudaStreamWaitEvent(stream, ev_ojoin2, 0));
       io_out_pending = false;
+    }
+    if (!pre) {
+      for (const HostIO& b : hio)
+        if (b.out && !early_out(b) && !(defer && deferrable(b))) copy_out(b, stream);
+    } else {
+      // the final downloads on one link direction and, behind each, the next
+      // step's inputs that wait for it on the other
+      CK(cudaEventRecord(ev_tfork, stream));
+      CK(cudaStreamWaitEvent(cstream, ev_tfork, 0));
+      CK(cudaStreamWaitEvent(ustream, ev_tfork, 0));
+      std::vector<char> tdn(hio.size(), 0);
+      for (size_t q = 0; q < hio.size(); ++q) {
+        const HostIO& b = hio[q];
+        if (!b.out || early_out(b) || (defer && deferrable(b))) continue;
+        copy_out(b, cstream);
+        CK(cudaEventRecord(ev_dn[q], cstream));
+        tdn[q] = 1;
+      }
+      for (size_t q = 0; q < hio.size(); ++q)
+        if (hio[q].tail) upload_after(q, tdn);
+      CK(cudaEventRecord(ev_tjoin, cstream));
+      CK(cudaEventRecord(ev_tjoin2, ustream));
+      CK(cudaStreamWaitEvent(stream, ev_tjoin, 0));
+      CK(cudaStreamWaitEvent(stream, ev_tjoin2, 0));
     }
     CK(cudaGetLastError());
     return WRFGPU_OK;
@@ -496,7 +542,7 @@ struct Ensemble {
       return rc ? rc : WRFGPU_E_CUDA;
     }
     graph_io[h][v] = g;
-    CK(cudaGraphInstantiate(&gexec_io[h][v], graph_io[h][v], 0));
+    CK(cudaGraphInstantiateWithFlags(&gexec_io[h][v], graph_io[h][v], cudaGraphInstantiateFlagUseNodePriority));
     return WRFGPU_OK;
   }
   int step_host(int nsteps) {

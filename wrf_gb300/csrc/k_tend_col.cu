@@ -67,6 +67,18 @@ __device__ __forceinline__ Chunk level_chunk_of(int kts, int ktf) {
 }
 
 // ---------------------------------------------------------------- ru_tend
+// A level's point inputs of the u (v) tendency beyond the staged planes, with
+// the sums and differences of the two columns formed as the reference's
+// expressions form them (so every rounding is unchanged): the tendency so
+// far, the advected field three levels up, the omega sum of the face above,
+// rw, p and ph one level up, alt, al, pb, php and cqu (cqv) of the two
+// columns, and the two sums of the cross velocity for the curvature term.
+struct LevelIn {
+  float t, f3, romsum, rw_l1, rw_r1, p_l1, p_r1, ph_l1, ph_r1, altsum, alsum, pbd, phpd, cq, cs_r, cs_l;
+};
+// They are loaded together, right before the level's arithmetic, so their
+// latencies overlap one another (interleaved with the arithmetic that uses
+// them, the kernel took 1.63 instead of 1.31 ms per 512x512x80 step).
 template <int FL, int MINB>
 __global__ void __launch_bounds__(TX* TY, MINB) k_tend_u_col(TileLaunch L) {
   static_assert(FL & TF_ADV, "the staged form includes advection");
@@ -161,6 +173,29 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_u_col(TileLaunch L) {
       if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i - 1, k0, j); rw_r = rw(i, k0, j); }
     }
     const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;  // own point in the halo planes
+    auto load_in = [&](int k) {
+      LevelIn q;
+      q.t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+      q.f3 = (k + 3 <= kme) ? u(i, k + 3, j) : 0.f;
+      const int kk = k + 1;
+      // rom(i) + rom(i-1) = rom(i-1) + rom(i) exactly: IEEE addition commutes
+      q.romsum = (kk == kts || kk == kte) ? 0.f : rom(i, kk, j) + rom(i - 1, kk, j);
+      q.rw_l1 = q.rw_r1 = 0.f;
+      if (FL & (TF_COR | TF_CURV)) { q.rw_l1 = rw(i - 1, k + 1, j); q.rw_r1 = rw(i, k + 1, j); }
+      q.p_l1 = q.p_r1 = q.ph_l1 = q.ph_r1 = q.altsum = q.alsum = q.pbd = q.phpd = q.cq = 0.f;
+      if (FL & TF_PG) {
+        if (kk != kde) { q.p_l1 = p(i - 1, kk, j); q.p_r1 = p(i, kk, j); }
+        q.ph_l1 = ph(i - 1, k + 1, j); q.ph_r1 = ph(i, k + 1, j);
+        q.altsum = alt(i, k, j) + alt(i - 1, k, j);
+        q.alsum = al(i, k, j) + al(i - 1, k, j);
+        q.pbd = pb(i, k, j) - pb(i - 1, k, j);
+        q.phpd = php(i, k, j) - php(i - 1, k, j);
+        q.cq = cqu(i, k, j);
+      }
+      q.cs_r = q.cs_l = 0.f;
+      if (FL & TF_CURV) { q.cs_r = v(i, k, j) + v(i, k, j + 1); q.cs_l = v(i - 1, k, j) + v(i - 1, k, j + 1); }
+      return q;
+    };
     bool ok = true;
     for (int k = k0; k <= k1; ++k) {
       ok = ring.wait(k) && ok;
@@ -181,8 +216,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_u_col(TileLaunch L) {
         prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqu(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
         prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
       }
-      float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
-      const float up3 = (k + 3 <= kme) ? u(i, k + 3, j) : 0.f;
+      const LevelIn q = load_in(k);
+      float t = q.t;
       t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
       t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
       {  // vertical flux of face k+1
@@ -190,52 +225,45 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_u_col(TileLaunch L) {
         float vf_hi;
         if (kk == kts || kk == kte) vf_hi = 0.f;
         else if (kk == kts + 1 || kk == ktf)
-          vf_hi = 0.5f * (rom(i, kk, j) + rom(i - 1, kk, j)) * (fzm(kk) * up1 + fzp(kk) * u0);
+          vf_hi = 0.5f * q.romsum * (fzm(kk) * up1 + fzp(kk) * u0);
         else {
-          const float vel = 0.5f * (rom(i - 1, kk, j) + rom(i, kk, j));
+          const float vel = 0.5f * q.romsum;
           vf_hi = vel * flux3(um1, u0, up1, up2, -vel);
         }
         t = t - rdzw(k) * (vf_hi - vf_lo);
         vf_lo = vf_hi;
       }
-      float rw_l1 = 0.f, rw_r1 = 0.f;
-      if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i - 1, k + 1, j); rw_r1 = rw(i, k + 1, j); }
       if (FL & TF_PG) {
         const int kk = k + 1;
-        float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
+        float dpn_hi;
         if (kk == kde) {
           if (m.cf.top_lid)
             dpn_hi = .5f * (m.cfn * (p(i - 1, kde - 1, j) + p(i, kde - 1, j)) +
                             m.cfn1 * (p(i - 1, kde - 2, j) + p(i, kde - 2, j)));
           else dpn_hi = 0.f;
         } else {
-          p_l1 = p(i - 1, kk, j); p_r1 = p(i, kk, j);
-          dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+          dpn_hi = .5f * (fzm(kk) * (q.p_l1 + q.p_r1) + fzp(kk) * (p_l + p_r));
         }
-        const float ph_l1 = ph(i - 1, k + 1, j), ph_r1 = ph(i, k + 1, j);
         float dpx = pgA * (c1h(k) * muu_c + c2h(k)) *
-                    ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i - 1, k, j)) * (p_r - p_l) +
-                     (al(i, k, j) + al(i - 1, k, j)) * (pb(i, k, j) - pb(i - 1, k, j)));
-        dpx = dpx + pgB * (php(i, k, j) - php(i - 1, k, j)) *
-                        (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
-        t = t - cqu(i, k, j) * dpx;
+                    ((q.ph_r1 - q.ph_l1 + ph_r - ph_l) + q.altsum * (p_r - p_l) + q.alsum * q.pbd);
+        dpx = dpx + pgB * q.phpd * (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
+        t = t - q.cq * dpx;
         dpn_lo = dpn_hi;
-        p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
+        p_l = q.p_l1; p_r = q.p_r1; ph_l = q.ph_l1; ph_r = q.ph_r1;
       }
       if (FL & (TF_COR | TF_CURV)) {
         const float rvsum = RV[o + HALO_W - 1] + RV[o + HALO_W] + RV[o - 1] + RV[o];
-        const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
+        const float rwsum = q.rw_l1 + rw_l + q.rw_r1 + rw_r;
         if (FL & TF_COR) t = t + corA * rvsum - corB * rwsum;
         if (FL & TF_CURV) {
-          const float vx_r = 0.5f * (u0 + U[o + 1]) * dvx_r * rdy - 0.5f * (v(i, k, j) + v(i, k, j + 1)) * duy_r * rdx;
-          const float vx_l =
-              0.5f * (U[o - 1] + u0) * dvx_l * rdy - 0.5f * (v(i - 1, k, j) + v(i - 1, k, j + 1)) * duy_l * rdx;
+          const float vx_r = 0.5f * (u0 + U[o + 1]) * dvx_r * rdy - 0.5f * q.cs_r * duy_r * rdx;
+          const float vx_l = 0.5f * (U[o - 1] + u0) * dvx_l * rdy - 0.5f * q.cs_l * duy_l * rdx;
           t = t + 0.5f * (vx_r + vx_l) * 0.25f * rvsum - u0 * RERADIUS * 0.25f * rwsum;
         }
       }
-      rw_l = rw_l1; rw_r = rw_r1;
+      rw_l = q.rw_l1; rw_r = q.rw_r1;
       tend(i, k, j) = t;
-      um1 = u0; u0 = up1; up1 = up2; up2 = up3;
+      um1 = u0; u0 = up1; up1 = up2; up2 = q.f3;
     }
     if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
   }
@@ -334,6 +362,28 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_v_col(TileLaunch L) {
       if (FL & (TF_COR | TF_CURV)) { rw_l = rw(i, k0, j - 1); rw_r = rw(i, k0, j); }
     }
     const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
+    auto load_in = [&](int k) {
+      LevelIn q;
+      q.t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+      q.f3 = (k + 3 <= kme) ? v(i, k + 3, j) : 0.f;
+      const int kk = k + 1;
+      q.romsum = (kk == kts || kk == kte) ? 0.f : rom(i, kk, j) + rom(i, kk, j - 1);
+      q.rw_l1 = q.rw_r1 = 0.f;
+      if (FL & (TF_COR | TF_CURV)) { q.rw_l1 = rw(i, k + 1, j - 1); q.rw_r1 = rw(i, k + 1, j); }
+      q.p_l1 = q.p_r1 = q.ph_l1 = q.ph_r1 = q.altsum = q.alsum = q.pbd = q.phpd = q.cq = 0.f;
+      if (FL & TF_PG) {
+        if (kk != kde) { q.p_l1 = p(i, kk, j - 1); q.p_r1 = p(i, kk, j); }
+        q.ph_l1 = ph(i, k + 1, j - 1); q.ph_r1 = ph(i, k + 1, j);
+        q.altsum = alt(i, k, j) + alt(i, k, j - 1);
+        q.alsum = al(i, k, j) + al(i, k, j - 1);
+        q.pbd = pb(i, k, j) - pb(i, k, j - 1);
+        q.phpd = php(i, k, j) - php(i, k, j - 1);
+        q.cq = cqv(i, k, j);
+      }
+      q.cs_r = q.cs_l = 0.f;
+      if (FL & TF_CURV) { q.cs_r = u(i, k, j) + u(i + 1, k, j); q.cs_l = u(i, k, j - 1) + u(i + 1, k, j - 1); }
+      return q;
+    };
     bool ok = true;
     for (int k = k0; k <= k1; ++k) {
       ok = ring.wait(k) && ok;
@@ -353,8 +403,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_v_col(TileLaunch L) {
         prefetch_l2(&php(i, k + 2, j)); prefetch_l2(&cqv(i, k + 2, j)); prefetch_l2(&rw(i, k + 2, j));
         prefetch_l2(&u(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j));
       }
-      float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
-      const float vp3 = (k + 3 <= kme) ? v(i, k + 3, j) : 0.f;
+      const LevelIn q = load_in(k);
+      float t = q.t;
       t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
       t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
       {
@@ -362,53 +412,45 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_v_col(TileLaunch L) {
         float vf_hi;
         if (kk == kts || kk == kte) vf_hi = 0.f;
         else if (kk == kts + 1 || kk == ktf)
-          vf_hi = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1)) * (fzm(kk) * vp1 + fzp(kk) * v0);
+          vf_hi = 0.5f * q.romsum * (fzm(kk) * vp1 + fzp(kk) * v0);
         else {
-          const float vel = 0.5f * (rom(i, kk, j) + rom(i, kk, j - 1));
+          const float vel = 0.5f * q.romsum;
           vf_hi = vel * flux3(vm1, v0, vp1, vp2, -vel);
         }
         t = t - ratio * rdzw(k) * (vf_hi - vf_lo);
         vf_lo = vf_hi;
       }
-      float rw_l1 = 0.f, rw_r1 = 0.f;
-      if (FL & (TF_COR | TF_CURV)) { rw_l1 = rw(i, k + 1, j - 1); rw_r1 = rw(i, k + 1, j); }
       if (FL & TF_PG) {
         const int kk = k + 1;
-        float p_l1 = 0.f, p_r1 = 0.f, dpn_hi;
+        float dpn_hi;
         if (kk == kde) {
           if (m.cf.top_lid)
             dpn_hi = .5f * (m.cfn * (p(i, kde - 1, j - 1) + p(i, kde - 1, j)) +
                             m.cfn1 * (p(i, kde - 2, j - 1) + p(i, kde - 2, j)));
           else dpn_hi = 0.f;
         } else {
-          p_l1 = p(i, kk, j - 1); p_r1 = p(i, kk, j);
-          dpn_hi = .5f * (fzm(kk) * (p_l1 + p_r1) + fzp(kk) * (p_l + p_r));
+          dpn_hi = .5f * (fzm(kk) * (q.p_l1 + q.p_r1) + fzp(kk) * (p_l + p_r));
         }
-        const float ph_l1 = ph(i, k + 1, j - 1), ph_r1 = ph(i, k + 1, j);
         float dpy = pgA * (c1h(k) * muv_c + c2h(k)) *
-                    ((ph_r1 - ph_l1 + ph_r - ph_l) + (alt(i, k, j) + alt(i, k, j - 1)) * (p_r - p_l) +
-                     (al(i, k, j) + al(i, k, j - 1)) * (pb(i, k, j) - pb(i, k, j - 1)));
-        dpy = dpy + pgB * (php(i, k, j) - php(i, k, j - 1)) *
-                        (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
-        t = t - cqv(i, k, j) * dpy;
+                    ((q.ph_r1 - q.ph_l1 + ph_r - ph_l) + q.altsum * (p_r - p_l) + q.alsum * q.pbd);
+        dpy = dpy + pgB * q.phpd * (rdzw(k) * (dpn_hi - dpn_lo) - .5f * ((c1h(k) * mu_l) + (c1h(k) * mu_r)));
+        t = t - q.cq * dpy;
         dpn_lo = dpn_hi;
-        p_l = p_l1; p_r = p_r1; ph_l = ph_l1; ph_r = ph_r1;
+        p_l = q.p_l1; p_r = q.p_r1; ph_l = q.ph_l1; ph_r = q.ph_r1;
       }
       if (FL & (TF_COR | TF_CURV)) {
         const float rusum = RU[o] + RU[o + 1] + RU[o - HALO_W] + RU[o - HALO_W + 1];
-        const float rwsum = rw_l1 + rw_l + rw_r1 + rw_r;
+        const float rwsum = q.rw_l1 + rw_l + q.rw_r1 + rw_r;
         if (FL & TF_COR) t = t - corA * rusum + corB * rwsum;
         if (FL & TF_CURV) {
-          const float vx_r =
-              0.5f * (u(i, k, j) + u(i + 1, k, j)) * dvx_r * rdy - 0.5f * (v0 + V[o + HALO_W]) * duy_r * rdx;
-          const float vx_l =
-              0.5f * (u(i, k, j - 1) + u(i + 1, k, j - 1)) * dvx_l * rdy - 0.5f * (V[o - HALO_W] + v0) * duy_l * rdx;
+          const float vx_r = 0.5f * q.cs_r * dvx_r * rdy - 0.5f * (v0 + V[o + HALO_W]) * duy_r * rdx;
+          const float vx_l = 0.5f * q.cs_l * dvx_l * rdy - 0.5f * (V[o - HALO_W] + v0) * duy_l * rdx;
           t = t - 0.5f * (vx_r + vx_l) * 0.25f * rusum - ratio * v0 * RERADIUS * 0.25f * rwsum;
         }
       }
-      rw_l = rw_l1; rw_r = rw_r1;
+      rw_l = q.rw_l1; rw_r = q.rw_r1;
       tend(i, k, j) = t;
-      vm1 = v0; v0 = vp1; vp1 = vp2; vp2 = vp3;
+      vm1 = v0; v0 = vp1; vp1 = vp2; vp2 = q.f3;
     }
     if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
   }

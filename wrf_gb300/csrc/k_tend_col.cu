@@ -535,9 +535,17 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
     vf_lo = kts + 1 <= ktf + 1 ? vf(kts + 1) : 0.f;
   }
   // levels k-1 (and k-2) of the mass fluxes at the own point and its +i / +j
-  // neighbours, and of u, v, p, carried down the column
+  // neighbours, and of u, v, p, carried down the column; w(k-1 .. k+1) and
+  // omega(k) of the own column for the vertical flux of face k+1
   float ru0m = 0.f, ru1m = 0.f, rv0m = 0.f, rv1m = 0.f;
   float u0m = 0.f, u1m = 0.f, v0m = 0.f, v1m = 0.f, pkm = 0.f;
+  float wkm1 = 0.f, wk0 = 0.f, wkp1 = 0.f, romk = 0.f;
+  const int kme = m.kme;
+  if (acc) {
+    wk0 = w(i, kts, j);
+    wkp1 = kts + 1 <= kme ? w(i, kts + 1, j) : 0.f;
+    romk = rom(i, kts, j);
+  }
   const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
   bool ok = true;
   for (int k = kts; k <= kte; ++k) {
@@ -566,16 +574,28 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
     __syncthreads();
     if (tid == 0 && k - 3 + W_RING <= kte) ring.issue(k - 3 + W_RING, maps, x0, z0, m.kms);
     if (!acc) continue;
+    // the level's global inputs, loaded together before its arithmetic
     const float ru0 = RUk[o], ru1 = RUk[o + 1], rv0 = RVk[o], rv1 = RVk[o + HALO_W];
-    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f, pk = 0.f;
+    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f, pk = 0.f, cqk = 0.f;
     if (FL & TF_CURV) { u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1); }
-    if (FL & TF_PG) pk = p(i, k, j);
+    if (FL & TF_PG) {
+      pk = p(i, k, j);
+      if (k != kde && k >= 2) cqk = cqw(i, k, j);
+    }
+    const float romk1 = k + 1 <= kme ? rom(i, k + 1, j) : 0.f;
+    const float wk2 = k + 2 <= kme ? w(i, k + 2, j) : 0.f;
     float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
     if (adv) {
       t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
       t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
       if (k <= ktf) {
-        const float vf_hi = vf(k + 1);
+        // vf(k + 1) from the carried window (the same operands and order)
+        float vf_hi;
+        if (k + 1 == kts + 1 || k + 1 == ktf + 1) vf_hi = 0.25f * (romk1 + romk) * (wkp1 + wk0);
+        else {
+          const float vel = 0.5f * (romk1 + romk);
+          vf_hi = vel * flux3(wkm1, wk0, wkp1, wk2, -vel);
+        }
         t = t - rdzu(k) * (vf_hi - vf_lo);
         vf_lo = vf_hi;
       } else {
@@ -588,7 +608,6 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
         float cq2 = cqw_top * cq1;
         t = t + rmg * (cq1 * 2.f * rdnw(k - 1) * (-pkm) - (c1f(k) * muf_c) - cq2 * (c1f(k) * mub_c + c2f(k)));
       } else if (k >= 2) {
-        const float cqk = cqw(i, k, j);
         float cq1 = 1.f / (1.f + cqk);
         float cq2 = cqk * cq1;
         cqw(i, k, j) = cq1;
@@ -599,7 +618,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
     // after pg_buoy_w and before coriolis as rk_tendency calls them
     // (module_em.F:729-745); activation at w_beta (zadvect_implicit = 0)
     if (FL == TF_ALL && wdamp && k >= 2 && k <= kde - 1) {
-      const float vert_cfl = fabsf(rom(i, k, j) / (c1f(k) * mut_w + c2f(k)) * rdnw(k) * m.dt);
+      const float vert_cfl = fabsf(romk / (c1f(k) * mut_w + c2f(k)) * rdnw(k) * m.dt);
       if (vert_cfl > W_BETA)
         t = t - sgn1(Wk[o]) * W_ALPHA * (vert_cfl - m.cf.w_crit_cfl) * (c1f(k) * mut_w + c2f(k));
     }
@@ -621,6 +640,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
     ru0m = ru0; ru1m = ru1; rv0m = rv0; rv1m = rv1;
     u0m = u0; u1m = u1; v0m = v0; v1m = v1;
     pkm = pk;
+    wkm1 = wk0; wk0 = wkp1; wkp1 = wk2; romk = romk1;
   }
   if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
 }

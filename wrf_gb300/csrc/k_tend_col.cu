@@ -789,8 +789,10 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
     if (adv2) return rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
     return .5f * (ww(i, kk, j) + ww(i, kk - 1, j)) * rdnw(kk - 1) * (ph(i, kk, j) - ph(i, kk - 1, j) + phb(i, kk, j) - phb(i, kk - 1, j));
   };
-  // carried: wdwn(k) and u, v of levels k-1, k-2 at (i, i+1) / (j, j+1)
+  // carried: wdwn(k), ph, phb and ww of level k, and u, v of levels k-1,
+  // k-2 at (i, i+1) / (j, j+1)
   float u0m = 0.f, u1m = 0.f, v0m = 0.f, v1m = 0.f, u0mm = 0.f, u1mm = 0.f, v0mm = 0.f, v1mm = 0.f, wd_lo = 0.f;
+  float ph_c = 0.f, phb_c = 0.f, ww_c = 0.f;
   if (acc) {
     mut_c = f2(m, WRFGPU_MUT)(i, j); msfty_c = f2(m, WRFGPU_MSFTY)(i, j);
     muv1 = f2(m, WRFGPU_MUV)(i, j + 1); muv0 = f2(m, WRFGPU_MUV)(i, j);
@@ -801,6 +803,7 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
     cy2 = 0.5f * m.rdy / msfty_c; cx2 = 0.5f * m.rdx / msfty_c;
     u0m = u(i, 1, j); u1m = u(i + 1, 1, j); v0m = v(i, 1, j); v1m = v(i, 1, j + 1);  // level k-1 = 1
     wd_lo = (2 <= kte - 1) ? wdwn(2) : 0.f;  // wdwn(k) at k = 2
+    ph_c = ph(i, ks, j); phb_c = phb(i, ks, j); ww_c = ww(i, ks, j);
   }
   const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
   bool ok = true;
@@ -815,27 +818,34 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
       prefetch_l2(&ph(i, k + 2, j)); prefetch_l2(&phb(i, k + 2, j)); prefetch_l2(&u(i, k + 2, j));
       prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ww(i, k + 2, j)); prefetch_l2(&w(i, k + 2, j));
     }
-    float t = 0.f;
-    // vertical advection of ph (:1396-1428)
+    // the level's global inputs, loaded together before its arithmetic
+    float ph_n = 0.f, phb_n = 0.f, ww_n = 0.f, u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f;
     if (k <= kte - 1) {
-      const float wd_hi = wdwn(k + 1);
-      if (adv2) t = t - ww(i, k, j) * (fnm(k) * wd_hi + fnp(k) * wd_lo);
+      ph_n = ph(i, k + 1, j); phb_n = phb(i, k + 1, j); ww_n = ww(i, k + 1, j);
+      u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1);
+    }
+    const float wk = m.cf.non_hydrostatic ? w(i, k, j) : 0.f;
+    float t = 0.f;
+    // vertical advection of ph (:1396-1428): wdwn(k + 1) from the carried
+    // level-k values (the same operands and order)
+    if (k <= kte - 1) {
+      const float wd_hi = adv2 ? rdnw(k) * (ph_n - ph_c + phb_n - phb_c)
+                               : .5f * (ww_n + ww_c) * rdnw(k) * (ph_n - ph_c + phb_n - phb_c);
+      if (adv2) t = t - ww_c * (fnm(k) * wd_hi + fnp(k) * wd_lo);
       else t = t - (fnm(k) * wd_hi + fnp(k) * wd_lo);
       wd_lo = wd_hi;
     }
     // "gw" term (:1432-1446)
     if (m.cf.non_hydrostatic) {
       if (k == kde) t = 0.f;
-      t = t + (c1f(k) * mut_c + c2f(k)) * G * w(i, k, j) / msfty_c;
+      t = t + (c1f(k) * mut_c + c2f(k)) * G * wk / msfty_c;
     }
     auto S = [&](int d) {  // 6th-order centred difference of ph + phb, stride d in the halo plane
       return 45.f * (PH[o + d] - PH[o - d]) - 9.f * (PH[o + 2 * d] - PH[o - 2 * d]) + (PH[o + 3 * d] - PH[o - 3 * d]) +
              45.f * (PHB[o + d] - PHB[o - d]) - 9.f * (PHB[o + 2 * d] - PHB[o - 2 * d]) +
              (PHB[o + 3 * d] - PHB[o - 3 * d]);
     };
-    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f;
     if (k <= kte - 1) {
-      u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1);
       t = t - cy4 * (((c1f(k) * muv1 + c2f(k)) * (v1 + v1m) * mvy1 + (c1f(k) * muv0 + c2f(k)) * (v0 + v0m) * mvy0) *
                      (1.f / 60.f) * S(HALO_W));
       t = t - cx4 * (((c1f(k) * muu1 + c2f(k)) * (u1 + u1m) * mux1 + (c1f(k) * muu0 + c2f(k)) * (u0 + u0m) * mux0) *
@@ -851,6 +861,7 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
     tend(i, k, j) = t;
     u0mm = u0m; u1mm = u1m; v0mm = v0m; v1mm = v1m;
     u0m = u0; u1m = u1; v0m = v0; v1m = v1;
+    ph_c = ph_n; phb_c = phb_n; ww_c = ww_n;
   }
   if (!ok && tid == 0) raise_err(m, ERR_TIMEOUT);
 }

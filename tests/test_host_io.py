@@ -74,6 +74,37 @@ def test_step_host_equals_set_step_get(gpulib, flags):
     dut.unbind_host_state()
 
 
+def test_step_host_many_passive_scalars(gpulib):
+    """qv and six passive scalars: stage 1's transport of a host I/O step
+    runs in two launches (the pairs whose scalars are across first, the
+    last pair after every upload); one call of three steps and then one
+    step per call give the per-field loop's bits."""
+    case = cases.small_case(nx=36, ny=20, kde=14, n_scalar=6, seed=21)
+    ref = G.Domain(case)
+    dut = G.Domain(case)
+    fids = _fids(case)
+    host_ref = {f: np.array(ref.get(0, f), dtype=np.float32).ravel() for f in fids}
+    bufs = []
+    for f in fids:
+        b = _pinned(host_ref[f].size)
+        b[:] = host_ref[f]
+        bufs.append(b)
+    dut.bind_host_state(0, fids, bufs)
+    for calls in ([3], [1, 1]):
+        for n in calls:
+            dut.step_host(n)
+            for _ in range(n):
+                for f in fids:
+                    ref.set(0, f, host_ref[f])
+                ref.step(1)
+                ref.sync()
+                for f in fids:
+                    host_ref[f] = np.array(ref.get(0, f), dtype=np.float32).ravel()
+            bad = [f for f, b in zip(fids, bufs) if not np.array_equal(b, host_ref[f])]
+            assert not bad, (calls, bad)
+    dut.unbind_host_state()
+
+
 def test_step_host_separate_in_out_and_refusals(gpulib):
     """Inputs and outputs in different buffers (the inputs are not written),
     an output-only field, and the refusals: pageable memory, a wrong count,

@@ -253,6 +253,12 @@ struct Ensemble {
   bool io_out_pending = false;
   cudaEvent_t ev_ofork = nullptr, ev_ojoin = nullptr, ev_dryin = nullptr;
   cudaEvent_t ev_tfork = nullptr, ev_tjoin = nullptr, ev_tjoin2 = nullptr;
+  // stage 1's transport of a host I/O step in two launches: the pairs whose
+  // passive scalars cross in the first three quarters of the uploads (after
+  // ev_upA), then the rest (after every upload)
+  bool io_split = false;
+  unsigned io_pairs_early = ~0u;
+  cudaEvent_t ev_upA = nullptr;
 
   void io_join() {
     if (!io_pending) return;
@@ -422,7 +428,7 @@ struct Ensemble {
     CK(cudaStreamCreateWithPriority(&cstream, cudaStreamNonBlocking, greatest));
     CK(cudaStreamCreateWithPriority(&ustream, cudaStreamNonBlocking, greatest));
     for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin, &ev_head, &ev_ojoin2, &ev_tfork,
-                           &ev_tjoin, &ev_tjoin2})
+                           &ev_tjoin, &ev_tjoin2, &ev_upA})
       CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     return WRFGPU_OK;
   }
@@ -468,11 +474,29 @@ struct Ensemble {
       if (b.in && !b.late) unpack(b, stream);
     // then the passive scalars, each after its own deferred download
     CK(cudaStreamWaitEvent(ustream, ev_dryin, 0));
+    std::vector<size_t> lq;  // late inputs in upload order
     for (size_t q = 0; q < hio.size(); ++q)
-      if (hio[q].in && hio[q].late) {
-        upload_after(q, dn);
-        unpack(hio[q], ustream);
-      }
+      if (hio[q].in && hio[q].late) lq.push_back(q);
+    // the pairs none of whose passive scalars is among the last quarter of
+    // the uploads are transported as soon as their own uploads are in
+    // (the stage-1 diffusion of the species reads them all: no split then)
+    io_split = false;
+    io_pairs_early = ~0u;
+    size_t na = 0;
+    if (lq.size() >= 4 && !diff6) {
+      const size_t thr = (3 * lq.size() + 3) / 4;
+      unsigned late_b = 0;
+      for (size_t r = thr; r < lq.size(); ++r) late_b |= 1u << (hio[lq[r]].species / 2);
+      for (size_t r = 0; r < lq.size(); ++r)
+        if (!((late_b >> (hio[lq[r]].species / 2)) & 1u)) na = r + 1;
+      io_pairs_early = ~late_b;
+      io_split = late_b != 0 && na > 0;
+    }
+    for (size_t r = 0; r < lq.size(); ++r) {
+      upload_after(lq[r], dn);
+      unpack(hio[lq[r]], ustream);
+      if (io_split && r + 1 == na) CK(cudaEventRecord(ev_upA, ustream));
+    }
     CK(cudaEventRecord(ev_join, ustream));
     io_pending = true;
     io_step = true;
@@ -912,9 +936,18 @@ struct Ensemble {
       }
       // scalar loop (solve_em.F:1815-2160): rk_scalar_tend + rk_update_scalar of every
       // species, fused; the positive-definite scheme at the last stage
-      io_join();  // passive scalars copied in by a host I/O step are read from here on
-      if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_forward_diff(l3, nb3, 1, stream); }  // module_em.F:1378-1435
-      mark(PH_ADVS); launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6);
+      if (io_pending && io_split) {
+        // a host I/O step's stage 1: the pairs whose passive scalars are
+        // across, then (after every upload) the others
+        cudaStreamWaitEvent(stream, ev_upA, 0);
+        mark(PH_ADVS); launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6, io_pairs_early);
+        io_join();
+        launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6, ~io_pairs_early);
+      } else {
+        io_join();  // passive scalars copied in by a host I/O step are read from here on
+        if (diff6 && rk_step == 1) { mark(PH_DIFF); launch_forward_diff(l3, nb3, 1, stream); }  // module_em.F:1378-1435
+        mark(PH_ADVS); launch_scalar_adv_update(LP(), nb_pr, rk_step, stream, tune[TU_ADV], diff6);
+      }
       if (rk_step == 3) {
         mark(PH_PD);
         launch_pd_courant(l2, nb2, rk_step, stream);

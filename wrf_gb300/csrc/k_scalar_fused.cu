@@ -86,10 +86,12 @@ __device__ __forceinline__ bool adv_pair(const Mem& m, int p, int rk_step, Speci
 
 // SCT: some member stores sc_tend (the species' sixth-order diffusion); the
 // variant without it keeps the common case free of its load and test.
+// pairs: bit p set = pair p of every member is transported by this launch.
 template <int MINB, bool SCT>
-__global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L, int rk_step) {
+__global__ void __launch_bounds__(TX* TY, MINB) k_scalar_adv_update(TileLaunch L, int rk_step, unsigned pairs) {
   extern __shared__ __align__(128) unsigned char smem[];
   const TilePos tp = tile_pos(L, TILE_PER_PAIR);
+  if (!((pairs >> tp.sub) & 1u)) return;  // block-uniform
   const Mem& m = block_member(L.mem, tp.m);
   SpeciesPair sp;
   if (!adv_pair(m, tp.sub, rk_step, &sp)) return;
@@ -647,7 +649,8 @@ template <typename K>
 static void set_smem(K kernel, size_t bytes) {
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
-void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var, bool sct) {
+void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var, bool sct,
+                              unsigned pairs) {
   static bool attr = false;
   if (!attr) {
     set_smem(k_scalar_adv_update<2, false>, ADV_SMEM);
@@ -657,10 +660,10 @@ void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cud
     attr = true;
   }
   const int minb = TUNE_PARAM[TU_ADV][var];
-  if (sct) k_scalar_adv_update<3, true><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
-  else if (minb == 2) k_scalar_adv_update<2, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
-  else if (minb == 3) k_scalar_adv_update<3, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
-  else k_scalar_adv_update<4, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step);
+  if (sct) k_scalar_adv_update<3, true><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step, pairs);
+  else if (minb == 2) k_scalar_adv_update<2, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step, pairs);
+  else if (minb == 3) k_scalar_adv_update<3, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step, pairs);
+  else k_scalar_adv_update<4, false><<<nblocks, dim3(TX, TY), ADV_SMEM, s>>>(L, rk_step, pairs);
 }
 void launch_scalar_pd_update(const TileLaunch& L, int nblocks, int nlev_max, int rk_step, cudaStream_t s, int var) {
   static size_t attr = 0;

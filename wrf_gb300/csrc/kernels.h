@@ -113,9 +113,10 @@ void launch_calc_p_rho_phi_col(const TileLaunch& L, int nblocks, cudaStream_t s,
 void launch_set_w_surface(const Launch& L2, int nblocks, cudaStream_t s);
 void launch_cfl_check_col(const TileLaunch& L, int nblocks, cudaStream_t s, int var = TUNE_DEFAULT[TU_CFL]);  // mass tiles
 
-// fused scalar transport (k_scalar_fused.cu): one block per (tile, species)
+// fused scalar transport (k_scalar_fused.cu): one block per (tile, pair of
+// species); `pairs` selects the pairs this launch transports (bit p: pair p)
 void launch_scalar_adv_update(const TileLaunch& L, int nblocks, int rk_step, cudaStream_t s, int var = TUNE_DEFAULT[TU_ADV],
-                              bool sct = false);
+                              bool sct = false, unsigned pairs = ~0u);
 // the face Courant numbers of the PD transport, once per step before it (column layout)
 void launch_pd_courant(const Launch& L2, int nblocks, int rk_step, cudaStream_t s);
 // nlev_max: the largest kme - kms + 1 of the members (sizes a per-level table in shared memory)

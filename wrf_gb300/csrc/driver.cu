@@ -259,6 +259,25 @@ struct Ensemble {
   bool io_split = false;
   unsigned io_pairs_early = ~0u;
   cudaEvent_t ev_upA = nullptr;
+  // moist species downloaded right after the last stage's transport (their
+  // halo fill issued first), while calc_p_rho_phi runs
+  std::vector<char> io_moist_done;
+  cudaEvent_t ev_mfork = nullptr;
+  bool io_moist_out() {
+    bool any = false;
+    for (const HostIO& b : hio) any = any || (b.out && b.species >= 0 && !b.late);
+    if (!any) return false;
+    cudaEventRecord(ev_mfork, stream);
+    cudaStreamWaitEvent(cstream, ev_mfork, 0);
+    io_moist_done.assign(hio.size(), 0);
+    for (size_t q = 0; q < hio.size(); ++q)
+      if (hio[q].out && hio[q].species >= 0 && !hio[q].late) {
+        copy_out(hio[q], cstream);
+        cudaEventRecord(ev_dn[q], cstream);
+        io_moist_done[q] = 1;
+      }
+    return true;
+  }
 
   void io_join() {
     if (!io_pending) return;
@@ -428,7 +447,7 @@ struct Ensemble {
     CK(cudaStreamCreateWithPriority(&cstream, cudaStreamNonBlocking, greatest));
     CK(cudaStreamCreateWithPriority(&ustream, cudaStreamNonBlocking, greatest));
     for (cudaEvent_t* e : {&ev_fork, &ev_join, &ev_ofork, &ev_ojoin, &ev_dryin, &ev_head, &ev_ojoin2, &ev_tfork,
-                           &ev_tjoin, &ev_tjoin2, &ev_upA})
+                           &ev_tjoin, &ev_tjoin2, &ev_upA, &ev_mfork})
       CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     return WRFGPU_OK;
   }
@@ -502,6 +521,7 @@ struct Ensemble {
     io_step = true;
     io_prefetch = pre;
     io_out_pending = false;
+    io_moist_done.assign(hio.size(), 0);
     enqueue_step();
     io_step = false;
     io_prefetch = false;
@@ -525,6 +545,8 @@ struct Ensemble {
       for (size_t q = 0; q < hio.size(); ++q) {
         const HostIO& b = hio[q];
         if (!b.out || early_out(b) || (defer && deferrable(b))) continue;
+        tdn[q] = 1;
+        if (io_moist_done[q]) continue;  // downloaded after the last transport
         copy_out(b, cstream);
         CK(cudaEventRecord(ev_dn[q], cstream));
         tdn[q] = 1;
@@ -851,6 +873,7 @@ struct Ensemble {
   // ---------------------------------------------------------------- one large step
   void enqueue_step() {
     const Launch l2 = L2(), l3 = L3();
+    bool species_filled = false;  // the end-of-step species fill was issued early
     for (int rk_step = 1; rk_step <= 3; ++rk_step) {
       StepArgs a{rk_step, 0, 0, 0};
       mark(PH_PREP);
@@ -958,6 +981,16 @@ struct Ensemble {
         if (rk_step == 3) launch_strip_pd(LS5(), nb_s5, LS4(), nb_s4, rk_step, nsp_max, d_pd_scratch, stream);
       }
       swap_species();
+      // a host I/O step with a next step: the species' final halo values
+      // (the end-of-step fill, issued here: calc_p_rho_phi reads qv at its
+      // own points only) and the moist species' downloads, beside calc_p_rho_phi
+      if (rk_step == 3 && io_step && io_prefetch) {
+        JobList js;
+        for (int s = 0; s < nsp_max; ++s) js.sp(s, 0, 'p');
+        fill(js);
+        species_filled = true;
+        io_moist_out();
+      }
       mark(PH_CPRP); launch_calc_p_rho_phi_col(LTM(), nb_tm, stream, tune[TU_CPRP]);
       if (rk_step < 3) {
         JobList j;  // rk_phys_bc_dry_2 + species (solve_em.F:3240-3330)
@@ -972,7 +1005,8 @@ struct Ensemble {
       JobList j;
       j.f3(WRFGPU_U_1, 'u'); j.f3(WRFGPU_V_1, 'v'); j.f3(WRFGPU_W_1, 'w'); j.f3(WRFGPU_T_1, 'p');
       j.f3(WRFGPU_PH_1, 'w'); j.f2(WRFGPU_MU_1, 't');
-      for (int s = 0; s < nsp_max; ++s) j.sp(s, 0, 'p');
+      if (!species_filled)
+        for (int s = 0; s < nsp_max; ++s) j.sp(s, 0, 'p');
       fill(j);
     }
     mark(PH_END);

@@ -74,12 +74,17 @@ def test_step_host_equals_set_step_get(gpulib, flags):
     dut.unbind_host_state()
 
 
-def test_step_host_many_passive_scalars(gpulib):
+@pytest.mark.parametrize("lateral", ["periodic", "open"])
+def test_step_host_many_passive_scalars(gpulib, lateral):
     """qv and six passive scalars: stage 1's transport of a host I/O step
     runs in two launches (the pairs whose scalars are across first, the
     last pair after every upload); one call of three steps and then one
-    step per call give the per-field loop's bits."""
+    step per call give the per-field loop's bits, on a periodic domain and
+    on one open on all four sides (the edge strips run before the species'
+    end-of-step fill that a call's earlier steps issue early)."""
     case = cases.small_case(nx=36, ny=20, kde=14, n_scalar=6, seed=21)
+    if lateral == "open":
+        case = cases.open_boundaries(case)
     ref = G.Domain(case)
     dut = G.Domain(case)
     fids = _fids(case)

@@ -704,6 +704,13 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_t_col(TileLaunch L) {
     float vf_lo = 0.f;  // vf(kts) = 0
     bool ok = true;
     for (int k = kts; k <= ktf; ++k) {
+      // the level's own-column loads, issued before the face work and the
+      // barrier so that their latency overlaps them
+      float fp3 = 0.f, romk1 = 0.f;
+      if (acc) {
+        fp3 = (k + 3 <= kme) ? fld(i, k + 3, j) : 0.f;
+        romk1 = (k + 1 == kts || k + 1 == kte) ? 0.f : rom(i, k + 1, j);
+      }
       ok = ring.wait(k) && ok;
       const float* T = ring.plane(k, 0);
       const float* RU = ring.plane(k, 1);
@@ -716,15 +723,14 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_t_col(TileLaunch L) {
       if (!acc) continue;
       if (k + 2 <= kme) { prefetch_l2(&rom(i, k + 2, j)); prefetch_l2(&tend(i, k + 2, j)); }
       float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
-      const float fp3 = (k + 3 <= kme) ? fld(i, k + 3, j) : 0.f;
       t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
       t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
       const int kk = k + 1;
       float vf_hi;
       if (kk == kts || kk == kte) vf_hi = 0.f;
-      else if (kk == kts + 1 || kk == ktf) vf_hi = rom(i, kk, j) * (fzm(kk) * fp1 + fzp(kk) * f0);
+      else if (kk == kts + 1 || kk == ktf) vf_hi = romk1 * (fzm(kk) * fp1 + fzp(kk) * f0);
       else {
-        const float vel = rom(i, kk, j);
+        const float vel = romk1;
         vf_hi = vel * flux3(fm1, f0, fp1, fp2, -vel);
       }
       t = t - rdzw(k) * (vf_hi - vf_lo);
@@ -808,6 +814,16 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
   const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
   bool ok = true;
   for (int k = ks; k <= kte; ++k) {
+    // the level's global inputs, loaded together before the barrier so that
+    // their latency overlaps it
+    float ph_n = 0.f, phb_n = 0.f, ww_n = 0.f, u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f, wk = 0.f;
+    if (acc) {
+      if (k <= kte - 1) {
+        ph_n = ph(i, k + 1, j); phb_n = phb(i, k + 1, j); ww_n = ww(i, k + 1, j);
+        u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1);
+      }
+      if (m.cf.non_hydrostatic) wk = w(i, k, j);
+    }
     __syncthreads();  // every thread is done with level k-1's slot
     if (tid == 0 && k + PH_RING - 1 <= kte) ring.issue(k + PH_RING - 1, maps, x0, z0, m.kms);
     ok = ring.wait(k) && ok;
@@ -818,13 +834,6 @@ __global__ void __launch_bounds__(TX* TY, 4) k_tend_ph_col(TileLaunch L) {
       prefetch_l2(&ph(i, k + 2, j)); prefetch_l2(&phb(i, k + 2, j)); prefetch_l2(&u(i, k + 2, j));
       prefetch_l2(&v(i, k + 2, j)); prefetch_l2(&ww(i, k + 2, j)); prefetch_l2(&w(i, k + 2, j));
     }
-    // the level's global inputs, loaded together before its arithmetic
-    float ph_n = 0.f, phb_n = 0.f, ww_n = 0.f, u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f;
-    if (k <= kte - 1) {
-      ph_n = ph(i, k + 1, j); phb_n = phb(i, k + 1, j); ww_n = ww(i, k + 1, j);
-      u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1);
-    }
-    const float wk = m.cf.non_hydrostatic ? w(i, k, j) : 0.f;
     float t = 0.f;
     // vertical advection of ph (:1396-1428): wdwn(k + 1) from the carried
     // level-k values (the same operands and order)

@@ -549,6 +549,19 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
   const int o = (ty + TMA_HALO) * HALO_W + tx + TMA_HALO;
   bool ok = true;
   for (int k = kts; k <= kte; ++k) {
+    // the level's global inputs, loaded together before the face work and
+    // the level barrier so that their latency overlaps them
+    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f, pk = 0.f, cqk = 0.f, romk1 = 0.f, wk2 = 0.f, t = 0.f;
+    if (acc) {
+      if (FL & TF_CURV) { u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1); }
+      if (FL & TF_PG) {
+        pk = p(i, k, j);
+        if (k != kde && k >= 2) cqk = cqw(i, k, j);
+      }
+      romk1 = k + 1 <= kme ? rom(i, k + 1, j) : 0.f;
+      wk2 = k + 2 <= kme ? w(i, k + 2, j) : 0.f;
+      t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
+    }
     ok = ring.wait(k) && ok;
     const float* Wk = ring.plane(k, 0);
     const float* RUk = ring.plane(k, 1);
@@ -574,17 +587,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) k_tend_w_col(TileLaunch L) {
     __syncthreads();
     if (tid == 0 && k - 3 + W_RING <= kte) ring.issue(k - 3 + W_RING, maps, x0, z0, m.kms);
     if (!acc) continue;
-    // the level's global inputs, loaded together before its arithmetic
     const float ru0 = RUk[o], ru1 = RUk[o + 1], rv0 = RVk[o], rv1 = RVk[o + HALO_W];
-    float u0 = 0.f, u1 = 0.f, v0 = 0.f, v1 = 0.f, pk = 0.f, cqk = 0.f;
-    if (FL & TF_CURV) { u0 = u(i, k, j); u1 = u(i + 1, k, j); v0 = v(i, k, j); v1 = v(i, k, j + 1); }
-    if (FL & TF_PG) {
-      pk = p(i, k, j);
-      if (k != kde && k >= 2) cqk = cqw(i, k, j);
-    }
-    const float romk1 = k + 1 <= kme ? rom(i, k + 1, j) : 0.f;
-    const float wk2 = k + 2 <= kme ? w(i, k + 2, j) : 0.f;
-    float t = (FL & TF_ZERO) ? 0.f : tend(i, k, j);
     if (adv) {
       t = t - mrdy * (FY[(ty + 1) * TX + tx] - FY[ty * TX + tx]);
       t = t - mrdx * (FX[ty * (TX + 1) + tx + 1] - FX[ty * (TX + 1) + tx]);
